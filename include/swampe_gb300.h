@@ -1,0 +1,148 @@
+/*
+ * swampe_gb300.h -- C ABI of the GB300 time-stepping core for SWAMPE-JAX.
+ *
+ * The reference (imalsky/MY_SWAMPE, package my_swampe) is pure Python/JAX and
+ * has no foreign-function interface; its device boundary is the jitted
+ * lax.scan call inside run_model_scan (src/my_swampe/model.py:1715-1758).
+ * Each entry point below replaces one piece of the path behind that call and
+ * cites the reference function it stands for.  The Python package
+ * my_swampe_gb300 binds these symbols with ctypes and keeps the reference's
+ * run_model / run_model_scan / run_model_scan_final signatures on top.
+ *
+ * Conventions
+ *   - Every function returns an int status: SWP_OK (0) or an SWP_ERR_* code.
+ *     Nothing throws or aborts across the ABI; swp_last_error() returns the
+ *     message of the last failure on that plan.
+ *   - All arrays are device pointers owned by the caller; the plan owns only
+ *     static geometry and scratch.  `stream` is a cudaStream_t (NULL = legacy).
+ *   - A plan is not re-entrant: one host thread and one stream per plan.
+ *   - Precision SWP_FP64: every array of "compute type" is double/double2.
+ *     Precision SWP_FAST: compute type is float/float2 (FP32 state, FP32
+ *     pointwise math; Legendre contractions in split precision on the
+ *     tensor cores where available).  Geometry is always built in FP64.
+ *
+ * Memory layout of one truncation group (M, J, I, B members):
+ *   fourier : complex[SWP_NFOURIER][M+1][B][J]   (field, zonal wavenumber m, member, latitude)
+ *   resid   : real[5][B][J][I]   initial condition minus its band-limited part
+ *   params  : double[SWP_NPAR][B]
+ *   member  : double[4][B]       (w_curr, w_mid, dead, updated)
+ *   diag    : double[nsteps+1][5][B]  (rms^2-sum, min |u|, min Phi, max Phi, dead)
+ *   hist    : real[nsteps][5][B][J][I]  (eta, delta, Phi, U, V)
+ */
+#ifndef SWAMPE_GB300_H
+#define SWAMPE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWP_OK 0
+#define SWP_ERR_ARG 1
+#define SWP_ERR_CUDA 2
+#define SWP_ERR_NUMERIC 3
+#define SWP_ERR_STATE 4
+#define SWP_ERR_UNSUPPORTED 5
+
+#define SWP_FP64 0
+#define SWP_FAST 1
+
+#define SWP_NFOURIER 19
+#define SWP_NPAR 10
+#define SWP_MAX_GROUPS 4
+
+typedef struct swp_plan swp_plan;
+
+/* Per-group device buffers (see layout above).  Unused pointers may be NULL. */
+typedef struct {
+  void* fourier;
+  void* resid;
+  const double* params;
+  double* member;
+  double* diag;
+  void* hist;
+} swp_group_state;
+
+/* Adjoint buffers of one group. */
+typedef struct {
+  void* lam;          /* complex[SWP_NFOURIER][M+1][B][J]: adjoint of the Fourier state */
+  void* lam_y;        /* complex[5][M+1][B][J]: scratch for the adjoint of the step outputs */
+  double* grad;       /* double[4][B]: d/d(taurad, taudrag, DPhieq, Phibar), accumulated */
+} swp_group_adjoint;
+
+/* Flags of model.py RunFlags (model.py:156-226) plus the test selector. */
+typedef struct {
+  int scheme;       /* 0 = modified Euler (default), 1 = explicit (expflag)  */
+  int forcflag;
+  int diffflag;
+  int modalflag;
+  int test;         /* 0 = forced (test=None), 1, 2                           */
+  int diagnostics;  /* RMS blow-up gate and per-step diagnostics              */
+  double blowup;    /* RunFlags.blowup_rms                                     */
+} swp_flags;
+
+/* Create a plan for `ngroups` truncations (M[g] in {42, 63, 106}) with B[g]
+ * members each; builds Gauss nodes, Legendre bases and FFT twiddles on the
+ * device in FP64.  Replaces build_static/_cached_geometry (model.py:62-86,
+ * 457-557) and spectral_transform.PmnHmn / gauss_legendre. */
+int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_plan** out);
+int swp_plan_destroy(swp_plan* plan);
+/* Grid sizes of group g (initial_conditions.spectral_params, initial_conditions.py:50-85). */
+int swp_plan_dims(const swp_plan* plan, int g, int* M, int* J, int* I, int* B);
+/* Message of the last failure on this plan (empty string if none). */
+const char* swp_last_error(const swp_plan* plan);
+/* FP64 copies of mus, w (J each) and dense Pmn, Hmn (J, M+1, M+1) for group g
+ * (spectral_transform.py:80-114, 219-287).  Any pointer may be NULL. */
+int swp_geometry(const swp_plan* plan, int g, double* mus, double* w, double* Pmn, double* Hmn, void* stream);
+
+/* Two-level initial state from physical fields phys_ic[g] = real[5][B][J][I]
+ * (eta, delta, Phi, U, V); fills fourier, resid and diag row 0.
+ * Replaces _init_state_from_fields (model.py:694-772). */
+int swp_init_state(swp_plan* plan, const swp_group_state* st, void* const* phys_ic,
+                   const swp_flags* flags, void* stream);
+
+/* Winds diagnosed from eta, delta (model.py:644-666): phys_ed[g] = real[2][B][J][I]
+ * in, phys_uv[g] = real[2][B][J][I] out.  Uses st[g].fourier as scratch. */
+int swp_diagnose_winds(swp_plan* plan, const swp_group_state* st, void* const* phys_ed,
+                       void* const* phys_uv, void* stream);
+
+/* Advance every group by `nsteps` steps starting at absolute time index t0
+ * (the body of lax.scan over t_seq = arange(t0, t0 + nsteps), model.py:795-1194,
+ * 1237-1342).  diag/hist rows are indexed from `row0`.  write_prev_last copies
+ * the Fourier curr carry into the prev carry on the last step (always done for
+ * the explicit scheme, which reads it). */
+int swp_forward(swp_plan* plan, const swp_group_state* st, const swp_flags* flags,
+                int t0, int nsteps, int row0, int write_prev_last, void* stream);
+
+/* Physical curr and RA-filtered prev fields: phys_out[g] = real[8][B][J][I]
+ * (eta, delta, Phi, U, V, eta_prev, delta_prev, Phi_prev) -- the physical
+ * members of the reference State (model.py:380-425). */
+int swp_output_physical(swp_plan* plan, const swp_group_state* st, void* const* phys_out,
+                        const swp_flags* flags, void* stream);
+
+/* Copy of the whole Fourier state of every group into/out of `ckpt[g]`
+ * (same layout as st[g].fourier).  dir = 0: state -> ckpt, 1: ckpt -> state. */
+int swp_state_copy(swp_plan* plan, const swp_group_state* st, void* const* ckpt, int dir, void* stream);
+
+/* Adjoint of one step t (modified Euler, forced or unforced, diagnostics off).
+ * On entry adj[g].lam holds the adjoint of the state after the step; primal
+ * st_in[g] is the state before the step and st_out[g] the state after it.
+ * On exit adj[g].lam holds the adjoint of the state before the step and
+ * adj[g].grad has accumulated the parameter gradients of the step. */
+int swp_adjoint_step(swp_plan* plan, const swp_group_state* st_in, const swp_group_state* st_out,
+                     const swp_group_adjoint* adj, const swp_flags* flags, int t, void* stream);
+
+/* Seed the adjoint from gradients of the physical curr fields
+ * dphys[g] = real[5][B][J][I] (eta, delta, Phi, U, V): adj[g].lam is overwritten. */
+int swp_adjoint_seed(swp_plan* plan, const swp_group_state* st, const swp_group_adjoint* adj,
+                     void* const* dphys, void* stream);
+
+/* Adjoint of swp_init_state: gradients of the physical initial fields
+ * dic[g] = real[5][B][J][I] (eta, delta, Phi, U, V) from adj[g].lam; accumulates
+ * parameter gradients of the initial forcing into adj[g].grad. */
+int swp_adjoint_init(swp_plan* plan, const swp_group_state* st, const swp_group_adjoint* adj,
+                     void* const* phys_ic, void* const* dic, const swp_flags* flags, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,465 @@
+// K1: the per-zonal-wavenumber "Legendre sandwich" of one time step.
+//
+// For a fixed m, everything between the Fourier inputs and the Fourier
+// outputs of a step is independent of the other wavenumbers:
+//   Fourier inputs (J values per field)  --forward Legendre-->  spectral (n = m..N)
+//   --tendency combine, n(n+1), hyperdiffusion, wind inversion-->
+//   --inverse Legendre-->  Fourier outputs (J values per field).
+// One CTA owns one m and a tile of ensemble members and does the whole chain
+// in shared memory.  Reference functions covered:
+//   modEuler_tdiff.py:30-268      phi/delta/eta_timestep (quirks: /4, forced A,B in delta, eta asymmetry)
+//   explicit_tdiff.py:20-233      phi/delta/eta_timestep (delta carry-only, extra drag terms)
+//   spectral_transform.py:370-481 fwd_leg_w / invrs_leg  (negative-m half is conj, never formed)
+//   spectral_transform.py:535-596 invrsUV_with_coeffs
+//   filters.py:11-27,95-151       diffusion, sigma6, sigma6Phi
+//   time_stepping.py:491-534      tstepcoeff, tstepcoeff2, tstepcoeffmn, narray, mJarray, marray
+//   model.py:988-1110             Robert-Asselin filter of the prev carry; spectral prev carry
+// The 19 distinct forward transforms of the reference collapse, by linearity,
+// into 9 combined inputs per member (5 on Pw, 4 on Hw), and both contractions
+// use the equatorial symmetry of the Gauss grid, Pbar(-mu) = (-1)^(n-m) Pbar(mu),
+// so each contraction runs over J/2 latitudes.
+#include "swp_internal.h"
+
+namespace swp {
+
+// combined-input slots of the forward contraction
+enum SlotP { SP_PHI1 = 0, SP_PHI2, SP_D1, SP_D2, SP_E1, NSP };   // on Pw
+enum SlotH { SH_PHI1 = 0, SH_D1, SH_D2, SH_E1, NSH };            // on Hw
+constexpr int NSLOT = NSP + NSH;
+constexpr int NKIN_P = 5;  // inverse inputs on P: eta, delta, Phi, Uprep, Vprep
+constexpr int NKIN_H = 2;  // inverse inputs on H: eta_s (U), -delta_s (V)
+constexpr int NKIN = NKIN_P + NKIN_H;
+constexpr int FWD_TC = 4;  // n-columns per thread in the forward contraction
+constexpr int INV_TJ = 2;  // latitudes per thread in the inverse contraction
+
+template <typename T>
+size_t spec_smem_bytes(int M, int J, int MT) {
+  int Jh = J / 2, R = 2 * MT, cnt = M + 1;
+  size_t x = (size_t)NSLOT * 2 * Jh * R;            // symmetrised inputs (reused for outputs)
+  size_t bf = (size_t)2 * cnt * Jh;                  // two basis blocks
+  size_t kin = (size_t)NKIN * cnt * R;               // inverse inputs
+  size_t coef = (size_t)3 * MT * cnt;                // sigma, sigmaPhi, a/(n(n+1))
+  return (x + bf + kin + coef) * sizeof(T) + 64 * sizeof(int);
+}
+template size_t spec_smem_bytes<double>(int, int, int);
+template size_t spec_smem_bytes<float>(int, int, int);
+
+template <typename T>
+__device__ __forceinline__ const SpecGroup<T>& pick_group(const SpecLaunch<T>& L, int& idx) {
+  int gi = 0;
+  while (gi + 1 < L.ng && (int)blockIdx.x >= L.prefix[gi + 1]) ++gi;
+  idx = blockIdx.x - L.prefix[gi];
+  return L.grp[gi];
+}
+
+// i*m*z
+template <typename T2, typename T>
+__device__ __forceinline__ T2 imul(T m, T2 z) { T2 r; r.x = -m * z.y; r.y = m * z.x; return r; }
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLaunch<T> L) {
+  typedef typename cplx<T>::type T2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int idx;
+  const SpecGroup<T>& G = pick_group(L, idx);
+  const StepCfg& cfg = L.cfg;
+  const int mode = L.mode;
+  const Geom<T>& g = G.g;
+  const int M = g.M, N = M, J = g.J, Jh = J / 2;
+  const int m = idx / G.ntb;
+  const int b0 = (idx % G.ntb) * G.MT;
+  const int MT = G.MT;
+  const int mt = min(MT, G.B - b0);
+  const int R = 2 * MT;
+  const int cnt = N + 1 - m, C0 = (cnt + 1) / 2, C1 = cnt / 2;
+  const int cntmax = N + 1;
+  const size_t FS = (size_t)(M + 1) * G.B * J;  // field stride (complex elements)
+
+  T* X = (T*)smem_raw;                                  // [NSLOT][2][Jh][R]
+  T* Bf = X + (size_t)NSLOT * 2 * Jh * R;                // [2][cnt*Jh]
+  T* Kin = Bf + (size_t)2 * cntmax * Jh;                 // [NKIN][cnt][R]
+  T* sig = Kin + (size_t)NKIN * cntmax * R;              // [MT][cnt]
+  T* sigP = sig + MT * cntmax;
+  T* tcmn = sigP + MT * cntmax;
+  int* sdead = (int*)(tcmn + MT * cntmax);               // [MT]
+
+  // ---- phase 0: per-member spectral coefficients and the blow-up gate
+  for (int t = threadIdx.x; t < MT * cnt; t += blockDim.x) {
+    int bt = t / cnt, k = t % cnt, n = m + k;
+    double s = 1.0, sp = 1.0, tc = 0.0;
+    if (bt < mt) {
+      int b = b0 + bt;
+      double a = G.par[P_A * G.B + b], dt = G.par[P_DT * G.B + b];
+      if (cfg.diffflag && mode == 0) {
+        double K6 = G.par[P_K6 * G.B + b], K6P = G.par[P_K6PHI * G.B + b];
+        double nd = (double)n;
+        double ncoeff = ((nd * nd * nd) / (a * a * a)) * (((nd + 1) * (nd + 1) * (nd + 1)) / (a * a * a));
+        double a6 = a * a * a * a * a * a;
+        s = 1.0 / (1.0 + 2.0 * dt * K6 * (ncoeff - 8.0 / a6));
+        sp = 1.0 / (1.0 + 2.0 * dt * K6P * ncoeff);
+      }
+      tc = (n == 0) ? 0.0 : a / ((double)n * (n + 1));
+    }
+    sig[bt * cntmax + k] = (T)s;
+    sigP[bt * cntmax + k] = (T)sp;
+    tcmn[bt * cntmax + k] = (T)tc;
+  }
+  if (threadIdx.x < MT) {
+    int bt = threadIdx.x, dead = 0;
+    if (bt < mt && cfg.diagnostics && mode == 0) {
+      int b = b0 + bt;
+      double rms = sqrt(G.diag[((size_t)cfg.step * NDIAG + D_RMS2) * G.B + b]);
+      dead = (G.member[MS_DEAD * G.B + b] != 0.0) || (rms > cfg.blowup);
+      if (m == 0) {
+        G.member[MS_DEAD * G.B + b] = dead ? 1.0 : 0.0;
+        G.diag[((size_t)cfg.step * NDIAG + D_DEAD) * G.B + b] = dead ? 1.0 : 0.0;
+      }
+    }
+    sdead[bt] = dead;
+  }
+
+  // ---- phase 1: combined, symmetrised inputs
+  const T2* F = G.four;
+  for (int t = threadIdx.x; t < MT * Jh; t += blockDim.x) {
+    int bt = t / Jh, jp = t % Jh;
+    T2 xs[NSLOT], xa[NSLOT];
+    if (bt < mt) {
+      int b = b0 + bt;
+      double dt = G.par[P_DT * G.B + b], a = G.par[P_A * G.B + b], Pb = G.par[P_PHIBAR * G.B + b];
+      double td = G.par[P_TAUDRAG * G.B + b];
+      T xm = (T)m;
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {
+        int j = side ? (J - 1 - jp) : jp;
+        size_t o = ((size_t)m * G.B + b) * J + j;
+        double tsc = (2.0 * dt) / (a * g.onemu2[j]);       // tstepcoeff
+        T2 c[NSLOT];
+        T2 z = mk<T2>(0, 0);
+#pragma unroll
+        for (int q = 0; q < NSLOT; ++q) c[q] = z;
+        if (mode == 2) {  // diagnose winds: plain forward transforms of eta, delta
+          c[SP_E1] = F[F_ETA * FS + o];
+          c[SP_D1] = F[F_DELTA * FS + o];
+        } else if (cfg.scheme == 0) {
+          T2 eta = F[F_ETA * FS + o], del = F[F_DELTA * FS + o], phi = F[F_PHI * FS + o];
+          T2 A = F[F_A * FS + o], Bm = F[F_B * FS + o], C = F[F_C * FS + o], D = F[F_D * FS + o];
+          T2 E = F[F_E * FS + o], PF = F[F_PHIF * FS + o], Fm = F[F_F * FS + o], Gm = F[F_G * FS + o];
+          T t1 = (T)(tsc / 4.0), t2 = (T)((2.0 * dt / (a * a)) / 4.0);
+          T ia2 = (T)(1.0 / (a * a));
+          T hPb = (T)(Pb * 0.5);
+          T2 Bf = cadd(Bm, Fm), Af = csub(A, Gm);
+          T2 Beff = cfg.forcflag ? Bf : Bm, Aeff = cfg.forcflag ? Af : A;
+          // Phi (modEuler_tdiff.py:80-110)
+          T2 p1 = csub(phi, cscale(imul(xm, C), t1));
+          p1 = csub(p1, cscale(del, (T)(dt * Pb)));
+          p1 = csub(p1, cscale(imul(xm, Beff), hPb * t1));
+          if (cfg.forcflag) p1 = cadd(p1, cscale(PF, (T)dt));
+          c[SP_PHI1] = p1;
+          c[NSP + SH_PHI1] = csub(cscale(D, t1), cscale(Aeff, hPb * t1));
+          c[SP_PHI2] = cscale(cadd(cscale(E, t2), cscale(phi, ia2)), -hPb);
+          // delta (modEuler_tdiff.py:162-201)
+          c[SP_D1] = cadd(del, cscale(imul(xm, Bf), t1));
+          c[NSP + SH_D1] = cscale(Af, t1);
+          T2 d2 = cadd(cscale(phi, t2), cscale(E, t2));
+          d2 = cadd(d2, cscale(imul(xm, C), t1 * (T)0.5 * ia2));
+          d2 = csub(d2, cscale(del, (T)(Pb / (a * a))));
+          if (cfg.forcflag) d2 = cadd(d2, cscale(PF, (T)((dt / 2.0) / (a * a))));
+          c[SP_D2] = d2;
+          c[NSP + SH_D2] = cscale(D, t1 * (T)0.5 * ia2);
+          // eta (modEuler_tdiff.py:253-261)
+          T te = cfg.forcflag ? (T)tsc : (T)(tsc / 2.0);
+          c[SP_E1] = csub(eta, cscale(imul(xm, Aeff), te));
+          c[NSP + SH_E1] = cscale(Beff, te);
+        } else {
+          T2 eta0 = F[F_ETA_PREV * FS + o], del0 = F[F_DELTA_PREV * FS + o], phi0 = F[F_PHI_PREV * FS + o];
+          T2 del1 = F[F_DELTA * FS + o];
+          T2 A = F[F_A * FS + o], Bm = F[F_B * FS + o], C = F[F_C * FS + o], D = F[F_D * FS + o];
+          T2 PF = F[F_PHIF * FS + o], Fm = F[F_F * FS + o], Gm = F[F_G * FS + o];
+          T2 U = F[F_U * FS + o], V = F[F_V * FS + o];
+          T t = (T)tsc;
+          T itd = (T)(1.0 / td);
+          // Phi (explicit_tdiff.py:62-78)
+          T2 p1 = csub(phi0, cscale(imul(xm, C), t));
+          p1 = csub(p1, cscale(del1, (T)(2.0 * dt * Pb)));
+          if (cfg.forcflag) p1 = cadd(p1, cscale(PF, (T)(2.0 * dt)));
+          c[SP_PHI1] = p1;
+          c[NSP + SH_PHI1] = cscale(D, t);
+          // delta (explicit_tdiff.py:134-155)
+          T2 d1 = del0, dh = mk<T2>(0, 0);
+          if (cfg.forcflag) {
+            d1 = csub(d1, cscale(imul(xm, U), t * itd));
+            d1 = cadd(d1, cscale(imul(xm, Fm), t));
+            dh = csub(cscale(V, t * itd), cscale(Gm, t));
+          }
+          c[SP_D1] = d1;
+          c[NSP + SH_D1] = dh;
+          // eta (explicit_tdiff.py:207-226)
+          T2 e1 = csub(eta0, cscale(imul(xm, A), t));
+          T2 eh = cscale(Bm, t);
+          if (cfg.forcflag) {
+            e1 = csub(e1, cscale(imul(xm, V), t * itd));
+            e1 = cadd(e1, cscale(imul(xm, Gm), t));
+            eh = cadd(eh, cscale(U, t * itd));
+            eh = cadd(eh, cscale(Fm, t));
+          }
+          c[SP_E1] = e1;
+          c[NSP + SH_E1] = eh;
+        }
+        if (side == 0) {
+#pragma unroll
+          for (int q = 0; q < NSLOT; ++q) { xs[q] = c[q]; xa[q] = c[q]; }
+        } else {
+#pragma unroll
+          for (int q = 0; q < NSLOT; ++q) { xs[q] = cadd(xs[q], c[q]); xa[q] = csub(xa[q], c[q]); }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < NSLOT; ++q) { xs[q] = mk<T2>(0, 0); xa[q] = xs[q]; }
+    }
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) {
+      T* base = X + (size_t)q * 2 * Jh * R;
+      base[(0 * Jh + jp) * R + 2 * bt] = xs[q].x;
+      base[(0 * Jh + jp) * R + 2 * bt + 1] = xs[q].y;
+      base[(1 * Jh + jp) * R + 2 * bt] = xa[q].x;
+      base[(1 * Jh + jp) * R + 2 * bt + 1] = xa[q].y;
+    }
+  }
+  // ---- phase 2: forward basis block for m
+  {
+    const T* srcP = g.Pw_f + g.boff[m];
+    const T* srcH = g.Hw_f + g.boff[m];
+    int nb = cnt * Jh;
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) { Bf[t] = srcP[t]; Bf[cntmax * Jh + t] = srcH[t]; }
+  }
+  __syncthreads();
+
+  // ---- phase 3: forward contraction over J/2 latitudes + spectral epilogue
+  {
+    const int nt0 = (C0 + FWD_TC - 1) / FWD_TC, nt1 = (C1 + FWD_TC - 1) / FWD_TC;
+    const int tasks = R * (nt0 + nt1);
+    const T* BP = Bf;
+    const T* BH = Bf + cntmax * Jh;
+    for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+      int r = task % R;
+      int ct = task / R;
+      int par = ct < nt0 ? 0 : 1;
+      if (par) ct -= nt0;
+      int Cp = par ? C1 : C0;
+      int c0 = ct * FWD_TC;
+      const T* bp = BP + (par ? Jh * C0 : 0);
+      const T* bh = BH + (par ? Jh * C0 : 0);
+      // P slots read the symmetric sum for even (n-m), the antisymmetric for odd; H the reverse.
+      const int sP = par, sH = 1 - par;
+      T acc[NSLOT][FWD_TC];
+#pragma unroll
+      for (int q = 0; q < NSLOT; ++q)
+#pragma unroll
+        for (int k = 0; k < FWD_TC; ++k) acc[q][k] = (T)0;
+      for (int jp = 0; jp < Jh; ++jp) {
+        T xp[NSP], xh[NSH];
+#pragma unroll
+        for (int q = 0; q < NSP; ++q) xp[q] = X[((size_t)q * 2 * Jh + sP * Jh + jp) * R + r];
+#pragma unroll
+        for (int q = 0; q < NSH; ++q) xh[q] = X[((size_t)(NSP + q) * 2 * Jh + sH * Jh + jp) * R + r];
+        T vp[FWD_TC], vh[FWD_TC];
+#pragma unroll
+        for (int k = 0; k < FWD_TC; ++k) {
+          int c = c0 + k;
+          vp[k] = c < Cp ? bp[jp * Cp + c] : (T)0;
+          vh[k] = c < Cp ? bh[jp * Cp + c] : (T)0;
+        }
+#pragma unroll
+        for (int k = 0; k < FWD_TC; ++k) {
+#pragma unroll
+          for (int q = 0; q < NSP; ++q) acc[q][k] = fma(xp[q], vp[k], acc[q][k]);
+#pragma unroll
+          for (int q = 0; q < NSH; ++q) acc[NSP + q][k] = fma(xh[q], vh[k], acc[NSP + q][k]);
+        }
+      }
+      const int bt = r >> 1, comp = r & 1;
+      double omega = bt < mt ? G.par[P_OMEGA * G.B + b0 + bt] : 0.0;
+#pragma unroll
+      for (int k = 0; k < FWD_TC; ++k) {
+        int c = c0 + k;
+        if (c >= Cp) break;
+        int kk = par + 2 * c;            // n - m
+        int n = m + kk;
+        T nn1 = (T)((double)n * (n + 1));
+        T s = sig[bt * cntmax + kk], sp = sigP[bt * cntmax + kk], tc = tcmn[bt * cntmax + kk];
+        T cphi, cdel, ceta;
+        if (mode == 2) {
+          ceta = acc[SP_E1][k];
+          cdel = acc[SP_D1][k];
+          cphi = (T)0;
+        } else {
+          cphi = sp * (acc[SP_PHI1][k] + acc[NSP + SH_PHI1][k] + nn1 * acc[SP_PHI2][k]);
+          cdel = s * (acc[SP_D1][k] + acc[NSP + SH_D1][k] + nn1 * (acc[SP_D2][k] + acc[NSP + SH_D2][k]));
+          ceta = s * (acc[SP_E1][k] + acc[NSP + SH_E1][k]);
+        }
+        // wind inversion inputs (spectral_transform.py:577-594)
+        T dp = (n == 0) ? (T)0 : cdel;
+        T ep = (n == 0) ? (T)0 : ceta;
+        if (m == 0 && n == 1 && comp == 0) ep -= (T)(omega / sqrt(0.375));
+        T es = ep * tc, ds = dp * tc;
+        int pc = par ? C0 + c : c;
+        Kin[((size_t)0 * cntmax + pc) * R + r] = ceta;
+        Kin[((size_t)1 * cntmax + pc) * R + r] = cdel;
+        Kin[((size_t)2 * cntmax + pc) * R + r] = cphi;
+        // Uprep = -i m delta_s ; Vprep = -i m eta_s  (write the other component)
+        T xm = (T)m;
+        if (comp == 0) {
+          Kin[((size_t)3 * cntmax + pc) * R + r + 1] = -xm * ds;
+          Kin[((size_t)4 * cntmax + pc) * R + r + 1] = -xm * es;
+        } else {
+          Kin[((size_t)3 * cntmax + pc) * R + r - 1] = xm * ds;
+          Kin[((size_t)4 * cntmax + pc) * R + r - 1] = xm * es;
+        }
+        Kin[((size_t)5 * cntmax + pc) * R + r] = es;
+        Kin[((size_t)6 * cntmax + pc) * R + r] = -ds;
+      }
+    }
+  }
+  __syncthreads();
+  // ---- phase 4: inverse basis block for m
+  {
+    const T* srcP = g.P_i + g.boff[m];
+    const T* srcH = g.H_i + g.boff[m];
+    int nb = cnt * Jh;
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) { Bf[t] = srcP[t]; Bf[cntmax * Jh + t] = srcH[t]; }
+  }
+  __syncthreads();
+
+  // ---- phase 5: inverse contraction (even/odd n-m) -> Fourier outputs in smem
+  T* Out = X;  // [5][MT][J][2]
+  {
+    const int njt = (Jh + INV_TJ - 1) / INV_TJ;
+    const int tasks = R * njt;
+    const T* BP = Bf;
+    const T* BH = Bf + cntmax * Jh;
+    for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+      int r = task % R;
+      int j0 = (task / R) * INV_TJ;
+      T E[NKIN][INV_TJ], O[NKIN][INV_TJ];
+#pragma unroll
+      for (int q = 0; q < NKIN; ++q)
+#pragma unroll
+        for (int k = 0; k < INV_TJ; ++k) { E[q][k] = (T)0; O[q][k] = (T)0; }
+      // even n-m
+      for (int c = 0; c < C0; ++c) {
+        T kin[NKIN];
+#pragma unroll
+        for (int q = 0; q < NKIN; ++q) kin[q] = Kin[((size_t)q * cntmax + c) * R + r];
+#pragma unroll
+        for (int k = 0; k < INV_TJ; ++k) {
+          int jp = j0 + k;
+          T p = jp < Jh ? BP[c * Jh + jp] : (T)0;
+          T h = jp < Jh ? BH[c * Jh + jp] : (T)0;
+#pragma unroll
+          for (int q = 0; q < NKIN_P; ++q) E[q][k] = fma(kin[q], p, E[q][k]);
+#pragma unroll
+          for (int q = NKIN_P; q < NKIN; ++q) E[q][k] = fma(kin[q], h, E[q][k]);
+        }
+      }
+      // odd n-m
+      for (int c = 0; c < C1; ++c) {
+        T kin[NKIN];
+#pragma unroll
+        for (int q = 0; q < NKIN; ++q) kin[q] = Kin[((size_t)q * cntmax + C0 + c) * R + r];
+#pragma unroll
+        for (int k = 0; k < INV_TJ; ++k) {
+          int jp = j0 + k;
+          T p = jp < Jh ? BP[Jh * C0 + c * Jh + jp] : (T)0;
+          T h = jp < Jh ? BH[Jh * C0 + c * Jh + jp] : (T)0;
+#pragma unroll
+          for (int q = 0; q < NKIN_P; ++q) O[q][k] = fma(kin[q], p, O[q][k]);
+#pragma unroll
+          for (int q = NKIN_P; q < NKIN; ++q) O[q][k] = fma(kin[q], h, O[q][k]);
+        }
+      }
+      const int bt = r >> 1, comp = r & 1;
+#pragma unroll
+      for (int k = 0; k < INV_TJ; ++k) {
+        int jp = j0 + k;
+        if (jp >= Jh) break;
+        int jn = jp, js = J - 1 - jp;
+        auto put = [&](int f, int j, T v) { Out[(((size_t)f * MT + bt) * J + j) * 2 + comp] = v; };
+        put(0, jn, E[0][k] + O[0][k]); put(0, js, E[0][k] - O[0][k]);
+        put(1, jn, E[1][k] + O[1][k]); put(1, js, E[1][k] - O[1][k]);
+        put(2, jn, E[2][k] + O[2][k]); put(2, js, E[2][k] - O[2][k]);
+        put(3, jn, (E[3][k] + O[3][k]) + (E[5][k] + O[5][k]));
+        put(3, js, (E[3][k] - O[3][k]) + (O[5][k] - E[5][k]));
+        put(4, jn, (E[4][k] + O[4][k]) + (E[6][k] + O[6][k]));
+        put(4, js, (E[4][k] - O[4][k]) + (O[6][k] - E[6][k]));
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- phase 6: write-out and carries (coalesced along j)
+  T2* Fo = G.four;
+  const int do_uv = (mode == 2) || (cfg.test != 1);
+  for (int t = threadIdx.x; t < MT * J; t += blockDim.x) {
+    int bt = t / J, j = t % J;
+    if (bt >= mt || sdead[bt]) continue;
+    int b = b0 + bt;
+    size_t o = ((size_t)m * G.B + b) * J + j;
+    auto get = [&](int f) { return mk<T2>(Out[(((size_t)f * MT + bt) * J + j) * 2], Out[(((size_t)f * MT + bt) * J + j) * 2 + 1]); };
+    if (mode == 2) {
+      Fo[F_U * FS + o] = get(3);
+      Fo[F_V * FS + o] = get(4);
+      continue;
+    }
+    double al = G.par[P_ALPHA * G.B + b];
+    const int cf[3] = {F_ETA, F_DELTA, F_PHI};
+    const int pf[3] = {F_ETA_PREV, F_DELTA_PREV, F_PHI_PREV};
+    const int rf[3] = {F_ETA_MID, F_DELTA_MID, F_PHI_MID};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      T2 nw = get(q);
+      if (cfg.write_prev || cfg.ra_mode) {
+        T2 old = Fo[cf[q] * FS + o];
+        if (cfg.write_prev) Fo[pf[q] * FS + o] = old;
+        if (cfg.ra_mode == 1) Fo[rf[q] * FS + o] = old;
+        else if (cfg.ra_mode == 2) {
+          T2 mid = Fo[rf[q] * FS + o];
+          T aa = (T)al;
+          T2 d = cadd(csub(mid, cscale(old, (T)2)), nw);
+          Fo[rf[q] * FS + o] = cadd(old, cscale(d, aa));
+        }
+      }
+      Fo[cf[q] * FS + o] = nw;
+    }
+    if (do_uv) {
+      Fo[F_U * FS + o] = get(3);
+      Fo[F_V * FS + o] = get(4);
+    }
+  }
+  // residual weights of the initial condition in the physical curr / prev fields
+  if (mode == 0 && m == 0 && threadIdx.x < mt && !sdead[threadIdx.x]) {
+    int b = b0 + threadIdx.x;
+    double wc = G.member[MS_WCURR * G.B + b], wm = G.member[MS_WMID * G.B + b];
+    double al = G.par[P_ALPHA * G.B + b];
+    if (cfg.ra_mode == 1) wm = wc;
+    else if (cfg.ra_mode == 2) wm = wc + al * (wm - 2.0 * wc);
+    G.member[MS_WMID * G.B + b] = wm;
+    G.member[MS_WCURR * G.B + b] = 0.0;
+    G.member[MS_UPDATED * G.B + b] = 1.0;
+  }
+}
+
+template <typename T>
+cudaError_t launch_spec(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_spectral<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr_set = true;
+  }
+  k_spectral<T><<<nblocks, 256, smem, s>>>(L);
+  return cudaGetLastError();
+}
+template cudaError_t launch_spec<double>(const SpecLaunch<double>&, int, size_t, cudaStream_t);
+template cudaError_t launch_spec<float>(const SpecLaunch<float>&, int, size_t, cudaStream_t);
+
+}  // namespace swp

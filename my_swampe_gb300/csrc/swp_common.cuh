@@ -1,0 +1,206 @@
+// Shared definitions for the SWAMPE GB300 time-stepping kernels.
+//
+// Layout conventions (all device memory is owned by the caller):
+//   * Fourier field  : complex[M+1][B][J]   (m slowest, latitude j fastest), per field
+//   * physical field : real[B][J][I]
+//   * per-member scalar parameters: double[NPAR][B]
+// The complex element type is T2 (double2 or float2), real parts first.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace swp {
+
+// ---------------------------------------------------------------- params ---
+enum ParamIndex {
+  P_DT = 0, P_A, P_OMEGA, P_PHIBAR, P_TAURAD, P_TAUDRAG, P_DPHIEQ, P_K6, P_K6PHI, P_ALPHA,
+  NPAR
+};
+
+// Fourier-space state fields, in the order used by the kernels.
+enum FourierField {
+  F_ETA_PREV = 0, F_ETA, F_DELTA_PREV, F_DELTA, F_PHI_PREV, F_PHI, F_U, F_V,
+  F_A, F_B, F_C, F_D, F_E, F_PHIF, F_F, F_G, F_ETA_MID, F_DELTA_MID, F_PHI_MID,
+  NFOURIER
+};
+
+// Physical residual fields (initial condition minus its band-limited part).
+enum ResidualField { R_ETA = 0, R_DELTA, R_PHI, R_U, R_V, NRESID };
+
+template <typename T> struct cplx;
+template <> struct cplx<double> { typedef double2 type; };
+template <> struct cplx<float> { typedef float2 type; };
+
+template <typename T2> __device__ __forceinline__ T2 mk(double r, double i) {
+  T2 z; z.x = r; z.y = i; return z;
+}
+template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { T2 z; z.x = a.x + b.x; z.y = a.y + b.y; return z; }
+template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { T2 z; z.x = a.x - b.x; z.y = a.y - b.y; return z; }
+template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
+  T2 z; z.x = a.x * b.x - a.y * b.y; z.y = a.x * b.y + a.y * b.x; return z;
+}
+// a * conj(b)
+template <typename T2> __device__ __forceinline__ T2 cmulc(T2 a, T2 b) {
+  T2 z; z.x = a.x * b.x + a.y * b.y; z.y = a.y * b.x - a.x * b.y; return z;
+}
+template <typename T2> __device__ __forceinline__ T2 cconj(T2 a) { a.y = -a.y; return a; }
+template <typename T2, typename S> __device__ __forceinline__ T2 cscale(T2 a, S s) { a.x *= s; a.y *= s; return a; }
+// multiply by +i (SIGN>0) or -i (SIGN<0)
+template <int SIGN, typename T2> __device__ __forceinline__ T2 cmul_i(T2 a) {
+  T2 z; if (SIGN > 0) { z.x = -a.y; z.y = a.x; } else { z.x = a.y; z.y = -a.x; } return z;
+}
+
+// ------------------------------------------------------------ small DFTs ---
+// Forward (SIGN=-1) or inverse (SIGN=+1) DFT of R points held in registers.
+template <int SIGN, typename T2> __device__ __forceinline__ void dft2(T2* v) {
+  T2 a = v[0], b = v[1]; v[0] = cadd(a, b); v[1] = csub(a, b);
+}
+
+template <int SIGN, typename T2> __device__ __forceinline__ void dft3(T2* v) {
+  typedef decltype(v[0].x) T;
+  const T c = (T)-0.5;
+  const T s = (T)(SIGN * 0.86602540378443864676);  // sin(+-2pi/3)
+  T2 a = cadd(v[1], v[2]), b = csub(v[1], v[2]);
+  T2 base = mk<T2>(v[0].x + c * a.x, v[0].y + c * a.y);
+  T2 ib = mk<T2>(-s * b.y, s * b.x);  // i*s*b
+  v[0] = cadd(v[0], a);
+  v[1] = cadd(base, ib);
+  v[2] = csub(base, ib);
+}
+
+template <int SIGN, typename T2> __device__ __forceinline__ void dft4(T2* v) {
+  T2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+  T2 t2 = cadd(v[1], v[3]), t3 = cmul_i<SIGN>(csub(v[1], v[3]));
+  v[0] = cadd(t0, t2); v[2] = csub(t0, t2);
+  v[1] = cadd(t1, t3); v[3] = csub(t1, t3);
+}
+
+template <int SIGN, typename T2> __device__ __forceinline__ void dft5(T2* v) {
+  typedef decltype(v[0].x) T;
+  const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;
+  const T s1 = (T)(SIGN * 0.95105651629515357212), s2 = (T)(SIGN * 0.58778525229247312917);
+  T2 a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
+  T2 a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
+  T2 x0 = v[0];
+  T2 r1 = mk<T2>(x0.x + c1 * a1.x + c2 * a2.x, x0.y + c1 * a1.y + c2 * a2.y);
+  T2 r2 = mk<T2>(x0.x + c2 * a1.x + c1 * a2.x, x0.y + c2 * a1.y + c1 * a2.y);
+  // i*(s1 b1 + s2 b2) and i*(s2 b1 - s1 b2)
+  T2 q1 = mk<T2>(-(s1 * b1.y + s2 * b2.y), s1 * b1.x + s2 * b2.x);
+  T2 q2 = mk<T2>(-(s2 * b1.y - s1 * b2.y), s2 * b1.x - s1 * b2.x);
+  v[0] = mk<T2>(x0.x + a1.x + a2.x, x0.y + a1.y + a2.y);
+  v[1] = cadd(r1, q1); v[4] = csub(r1, q1);
+  v[2] = cadd(r2, q2); v[3] = csub(r2, q2);
+}
+
+template <int SIGN, typename T2> __device__ __forceinline__ void dft8(T2* v) {
+  typedef decltype(v[0].x) T;
+  T2 e[4] = {v[0], v[2], v[4], v[6]};
+  T2 o[4] = {v[1], v[3], v[5], v[7]};
+  dft4<SIGN>(e); dft4<SIGN>(o);
+  const T h = (T)0.70710678118654752440;
+  // w8^k = exp(SIGN * i * 2pi k / 8)
+  T2 w1o = mk<T2>(h * (o[1].x - SIGN * o[1].y), h * (o[1].y + SIGN * o[1].x));
+  T2 w2o = cmul_i<SIGN>(o[2]);
+  T2 w3o = mk<T2>(h * (-o[3].x - SIGN * o[3].y), h * (-o[3].y + SIGN * o[3].x));
+  v[0] = cadd(e[0], o[0]); v[4] = csub(e[0], o[0]);
+  v[1] = cadd(e[1], w1o);  v[5] = csub(e[1], w1o);
+  v[2] = cadd(e[2], w2o);  v[6] = csub(e[2], w2o);
+  v[3] = cadd(e[3], w3o);  v[7] = csub(e[3], w3o);
+}
+
+template <int R, int SIGN, typename T2> __device__ __forceinline__ void dftR(T2* v) {
+  if (R == 2) dft2<SIGN>(v);
+  else if (R == 3) dft3<SIGN>(v);
+  else if (R == 4) dft4<SIGN>(v);
+  else if (R == 5) dft5<SIGN>(v);
+  else dft8<SIGN>(v);
+}
+
+// One Stockham autosort pass (radix R) over `ntr` transforms of length L
+// stored contiguously (transform t at in + t*L).  tw[k] = exp(-2 pi i k / L).
+template <int R, int SIGN, typename T2>
+__device__ __forceinline__ void stockham_pass(const T2* __restrict__ in, T2* __restrict__ out,
+                                              int L, int ns, int ntr, const T2* __restrict__ tw) {
+  const int per = L / R;
+  const int tasks = ntr * per;
+  const int twstride = L / (ns * R);
+  for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+    int t = task / per, j = task - t * per;
+    const T2* src = in + t * L;
+    T2* dst = out + t * L;
+    int jm = j % ns;
+    T2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = src[j + r * per];
+#pragma unroll
+    for (int r = 1; r < R; ++r) {
+      int k = (jm * r * twstride) % L;
+      T2 w = tw[k];
+      v[r] = (SIGN < 0) ? cmul(v[r], w) : cmulc(v[r], w);
+    }
+    dftR<R, SIGN>(v);
+    int idx = (j / ns) * ns * R + jm;
+#pragma unroll
+    for (int r = 0; r < R; ++r) dst[idx + r * ns] = v[r];
+  }
+}
+
+// Complex FFT of `ntr` length-L transforms held in smem buffer a (b is scratch).
+// Returns the buffer holding the result.  L in {64, 96, 160}.
+template <int SIGN, typename T2>
+__device__ T2* cfft_batch(T2* a, T2* b, int L, int ntr, const T2* tw) {
+  if (L == 64) {
+    stockham_pass<8, SIGN>(a, b, L, 1, ntr, tw); __syncthreads();
+    stockham_pass<8, SIGN>(b, a, L, 8, ntr, tw); __syncthreads();
+    return a;
+  } else if (L == 96) {
+    stockham_pass<8, SIGN>(a, b, L, 1, ntr, tw); __syncthreads();
+    stockham_pass<4, SIGN>(b, a, L, 8, ntr, tw); __syncthreads();
+    stockham_pass<3, SIGN>(a, b, L, 32, ntr, tw); __syncthreads();
+    return b;
+  } else {  // 160
+    stockham_pass<8, SIGN>(a, b, L, 1, ntr, tw); __syncthreads();
+    stockham_pass<4, SIGN>(b, a, L, 8, ntr, tw); __syncthreads();
+    stockham_pass<5, SIGN>(a, b, L, 32, ntr, tw); __syncthreads();
+    return b;
+  }
+}
+
+// ------------------------------------------------------------- descriptors ---
+// Geometry for one truncation, built on the device in FP64 (geometry.cu) and
+// rounded to the compute type.  Basis blocks are packed per zonal wavenumber m
+// and split by the parity of (n - m):
+//   fwd layout  [par][j'][c]  (j' = 0..J/2-1 southern nodes, n = m + par + 2c)
+//   inv layout  [par][c][j']
+// boff[m] is the element offset of block m (same for all four bases).
+template <typename T>
+struct Geom {
+  int M, J, I, L;          // truncation, latitudes, longitudes, L = I/2
+  const double* mu;        // [J]
+  const double* w;         // [J]
+  const double* onemu2;    // [J]  1 - mu^2
+  const double* area;      // [J]  RMS-wind area weight / cos^2(phi)
+  const int* boff;         // [M+2]
+  const T* Pw_f; const T* Hw_f;   // weighted basis, fwd layout
+  const T* P_f;  const T* H_f;    // unweighted basis, fwd layout (adjoint of inverse)
+  const T* P_i;  const T* H_i;    // unweighted basis, inv layout
+  const T* Pw_i; const T* Hw_i;   // weighted basis, inv layout (adjoint of forward)
+  const typename cplx<T>::type* twL;  // [L]   exp(-2 pi i k / L)
+  const typename cplx<T>::type* twI;  // [L+1] exp(-2 pi i k / I)
+  const T* dayc;           // [I]  dayside-mask * cos(lambda)
+};
+
+// Step configuration shared by a launch.
+struct StepCfg {
+  int scheme;      // 0 = modified Euler, 1 = explicit
+  int forcflag;
+  int diffflag;
+  int test;        // 0 = forced (test None), 1, 2
+  int ra_mode;     // 0 = leave RA mid, 1 = mid <- curr, 2 = Robert-Asselin update
+  int write_prev;  // copy old curr into the Fourier prev carry
+  int diagnostics; // blow-up gate + reductions
+  double blowup;   // RMS threshold
+  int step;        // scan-step index (row of the diagnostic arrays)
+};
+
+}  // namespace swp

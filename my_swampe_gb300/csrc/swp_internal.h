@@ -1,0 +1,132 @@
+// Internal host/device declarations shared by the translation units of
+// libswampe_gb300.so.  Nothing here crosses the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+#include "swp_common.cuh"
+#include "../../include/swampe_gb300.h"
+
+namespace swp {
+
+enum BasisIndex { B_PW_F = 0, B_HW_F, B_P_F, B_H_F, B_P_I, B_H_I, B_PW_I, B_HW_I };
+
+// Per-member scalars kept on the device: weights of the initial-condition
+// residual in the physical curr / RA-prev fields, the blow-up flag and
+// whether the member has taken a step.
+enum MemberScalar { MS_WCURR = 0, MS_WMID, MS_DEAD, MS_UPDATED, NMEMBER };
+// Per-step diagnostics: sum for the RMS wind (before sqrt), min wind speed,
+// min/max of the RA-filtered Phi, blow-up flag.
+enum DiagIndex { D_RMS2 = 0, D_SPIN, D_PHIMIN, D_PHIMAX, D_DEAD, NDIAG };
+// Parameter gradients accumulated by the adjoint.
+enum GradIndex { G_TAURAD = 0, G_TAUDRAG, G_DPHIEQ, G_PHIBAR, NGRAD };
+
+struct GroupGeom {
+  int M = 0, J = 0, I = 0, L = 0;
+  size_t nbasis = 0, bytes = 0;
+  void* mem = nullptr;
+  double *mu = nullptr, *w = nullptr, *onemu2 = nullptr, *area = nullptr;
+  int* boff = nullptr;
+  double* b64[8] = {};
+  float* b32[8] = {};
+  double2 *twL64 = nullptr, *twI64 = nullptr;
+  float2 *twL32 = nullptr, *twI32 = nullptr;
+  double* dayc64 = nullptr;
+  float* dayc32 = nullptr;
+
+  template <typename T> Geom<T> view() const;
+};
+
+template <> inline Geom<double> GroupGeom::view<double>() const {
+  Geom<double> g;
+  g.M = M; g.J = J; g.I = I; g.L = L;
+  g.mu = mu; g.w = w; g.onemu2 = onemu2; g.area = area; g.boff = boff;
+  g.Pw_f = b64[B_PW_F]; g.Hw_f = b64[B_HW_F]; g.P_f = b64[B_P_F]; g.H_f = b64[B_H_F];
+  g.P_i = b64[B_P_I]; g.H_i = b64[B_H_I]; g.Pw_i = b64[B_PW_I]; g.Hw_i = b64[B_HW_I];
+  g.twL = twL64; g.twI = twI64; g.dayc = dayc64;
+  return g;
+}
+template <> inline Geom<float> GroupGeom::view<float>() const {
+  Geom<float> g;
+  g.M = M; g.J = J; g.I = I; g.L = L;
+  g.mu = mu; g.w = w; g.onemu2 = onemu2; g.area = area; g.boff = boff;
+  g.Pw_f = b32[B_PW_F]; g.Hw_f = b32[B_HW_F]; g.P_f = b32[B_P_F]; g.H_f = b32[B_H_F];
+  g.P_i = b32[B_P_I]; g.H_i = b32[B_H_I]; g.Pw_i = b32[B_PW_I]; g.Hw_i = b32[B_HW_I];
+  g.twL = twL32; g.twI = twI32; g.dayc = dayc32;
+  return g;
+}
+
+int geometry_build(GroupGeom& gg, int M, cudaStream_t stream, std::string& err);
+int geometry_dense(const GroupGeom& gg, double* Pd, double* Hd, cudaStream_t stream);
+
+constexpr int MAXG = 4;
+
+// --------------------------------------------------------------- spectral ---
+template <typename T>
+struct SpecGroup {
+  Geom<T> g;
+  int B, MT, ntb;                       // members, members per tile, tiles along b
+  typename cplx<T>::type* four;         // [NFOURIER][M+1][B][J]
+  const double* par;                    // [NPAR][B]
+  double* member;                       // [NMEMBER][B]
+  double* diag;                         // [steps+1][NDIAG][B] or null
+  typename cplx<T>::type* lam;          // adjoint Fourier fields (adjoint launches)
+  const typename cplx<T>::type* lamY;   // adjoint of the K1 outputs (adjoint launches)
+  double* grad;                         // [NGRAD][B] (adjoint launches)
+};
+
+template <typename T>
+struct SpecLaunch {
+  SpecGroup<T> grp[MAXG];
+  int ng;
+  int prefix[MAXG + 1];
+  StepCfg cfg;
+  int mode;                             // 0 = step, 2 = diagnose winds
+};
+
+// ------------------------------------------------------------------- grid ---
+template <typename T>
+struct GridGroup {
+  Geom<T> g;
+  int B, JB, njb;                       // members, rows per CTA, row-blocks per member
+  typename cplx<T>::type* four;         // [NFOURIER][M+1][B][J]
+  T* resid;                             // [NRESID][B][J][I]
+  const double* par;                    // [NPAR][B]
+  double* member;                       // [NMEMBER][B]
+  double* diag;                         // [steps+1][NDIAG][B] or null
+  T* hist;                              // [5][B][J][I] for this step, or null
+  const T* phys_in;                     // init: [5][B][J][I] physical initial fields
+  T* phys_out;                          // output/adjoint: [5 or 8][B][J][I]
+  // adjoint
+  typename cplx<T>::type* lam;          // adjoint Fourier fields
+  const typename cplx<T>::type* primal; // primal Fourier fields of the step
+  double* grad;                         // [NGRAD][B]
+};
+
+template <typename T>
+struct GridLaunch {
+  GridGroup<T> grp[MAXG];
+  int ng;
+  int prefix[MAXG + 1];
+  StepCfg cfg;
+  int mode;
+};
+
+enum GridMode {
+  GM_STEP = 0,       // Fourier (eta, Phi, U, V) -> nonlinear Fourier terms (+history, diagnostics)
+  GM_INIT = 1,       // physical ICs -> full Fourier state, residuals, diagnostics
+  GM_OUTPUT = 2,     // Fourier state -> physical curr/prev fields
+  GM_WINDS = 3,      // Fourier U, V -> physical U, V (diagnosed winds)
+  GM_ADJ_STEP = 4,   // adjoint of GM_STEP
+  GM_ADJ_INIT = 5,   // adjoint of GM_INIT (gradient w.r.t. physical ICs)
+  GM_ADJ_OUTPUT = 6, // adjoint of the physical curr fields of GM_OUTPUT
+  GM_FWD2 = 7        // physical eta, delta -> truncated Fourier (diagnosed winds)
+};
+
+template <typename T> size_t spec_smem_bytes(int M, int J, int MT);
+template <typename T> size_t grid_smem_bytes(int M, int J, int I, int JB, int mode);
+template <typename T> cudaError_t launch_spec(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s);
+template <typename T> cudaError_t launch_spec_adj(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s);
+template <typename T> cudaError_t launch_grid(const GridLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s);
+
+}  // namespace swp

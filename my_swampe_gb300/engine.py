@@ -1,0 +1,209 @@
+"""Device-state owner for one or more truncation groups.
+
+An :class:`Engine` holds a ``libswampe_gb300`` plan (static geometry built on
+the GPU in FP64) and the torch tensors that carry the model state of every
+group in the layout the kernels use:
+
+* ``fourier[g]`` : complex ``(NFOURIER, M+1, B, J)`` -- Fourier-space carries
+  (prev/curr of eta, delta, Phi; U, V; A..E, PhiF, F, G; RA-filtered prev)
+* ``resid[g]``   : real ``(5, B, J, I)`` -- initial condition minus its
+  band-limited part (so physical outputs are exact even for non-band-limited ICs)
+* ``params[g]``  : float64 ``(NPAR, B)`` -- per-member scalars
+* ``member[g]``  : float64 ``(4, B)``    -- per-member residual weights and flags
+
+PyTorch is used only for device memory and streams; every arithmetic step of
+the model runs in the library's CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import torch
+
+from . import _lib
+
+PRECISIONS = {"fp64": _lib.SWP_FP64, "fast": _lib.SWP_FAST}
+
+PARAM_NAMES = ("dt", "a", "omega", "Phibar", "taurad", "taudrag", "DPhieq", "K6", "K6Phi", "alpha")
+
+
+@dataclass
+class RunFlagsC:
+    """Scheme switches passed to the kernels (model.py RunFlags, :156-226)."""
+
+    scheme: int = 0
+    forcflag: bool = True
+    diffflag: bool = True
+    modalflag: bool = True
+    test: Optional[int] = None
+    diagnostics: bool = False
+    blowup_rms: float = 8000.0
+
+    def c(self) -> _lib.Flags:
+        return _lib.Flags(
+            int(self.scheme), int(bool(self.forcflag)), int(bool(self.diffflag)), int(bool(self.modalflag)),
+            0 if self.test is None else int(self.test), int(bool(self.diagnostics)), float(self.blowup_rms),
+        )
+
+
+def _require_cuda(device) -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("my_swampe_gb300 needs a CUDA GPU: there is no CPU fallback")
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    if dev.type != "cuda":
+        raise RuntimeError(f"device must be a CUDA device, got {dev}")
+    return dev
+
+
+class Engine:
+    """One plan + device state for a list of ``(M, B)`` groups."""
+
+    def __init__(self, groups: Sequence[Tuple[int, int]], precision: str = "fp64", device=None):
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, got {precision!r}")
+        for M, _ in groups:
+            if int(M) not in (42, 63, 106):
+                raise ValueError(f"Unsupported value of M={M}. Only 42, 63, and 106 are supported.")
+        if not 1 <= len(groups) <= 4:
+            raise ValueError("between 1 and 4 truncation groups per engine")
+        self.device = _require_cuda(device)
+        self.lib = _lib.load()
+        self.precision = precision
+        self.rdtype = torch.float64 if precision == "fp64" else torch.float32
+        self.cdtype = torch.complex128 if precision == "fp64" else torch.complex64
+        ng = len(groups)
+        Ms = (ctypes.c_int * ng)(*[int(m) for m, _ in groups])
+        Bs = (ctypes.c_int * ng)(*[int(b) for _, b in groups])
+        self._plan = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            rc = self.lib.swp_plan_create(ng, Ms, Bs, PRECISIONS[precision], ctypes.byref(self._plan))
+        if rc != _lib.SWP_OK:
+            msg = self.lib.swp_last_error(self._plan).decode() if self._plan.value else ""
+            if self._plan.value:
+                self.lib.swp_plan_destroy(self._plan)
+            self._plan = ctypes.c_void_p()
+            if rc == 1 and "Unsupported" in msg:
+                raise ValueError(msg)
+            raise RuntimeError(f"swp_plan_create failed ({_lib.ERRORS.get(rc, rc)}): {msg}")
+        self.groups: List[Dict] = []
+        for g in range(ng):
+            M, J, I, B = (ctypes.c_int() for _ in range(4))
+            _lib.check(self.lib.swp_plan_dims(self._plan, g, ctypes.byref(M), ctypes.byref(J), ctypes.byref(I), ctypes.byref(B)), self._plan, "dims")
+            gd = dict(M=M.value, N=M.value, J=J.value, I=I.value, B=B.value)
+            dev = self.device
+            gd["fourier"] = torch.zeros((_lib.NFOURIER, gd["M"] + 1, gd["B"], gd["J"]), dtype=self.cdtype, device=dev)
+            gd["resid"] = torch.zeros((_lib.NRESID, gd["B"], gd["J"], gd["I"]), dtype=self.rdtype, device=dev)
+            gd["params"] = torch.zeros((_lib.NPAR, gd["B"]), dtype=torch.float64, device=dev)
+            gd["member"] = torch.zeros((_lib.NMEMBER, gd["B"]), dtype=torch.float64, device=dev)
+            self.groups.append(gd)
+        self._geo_cache: Dict[int, Dict[str, torch.Tensor]] = {}
+
+    # ------------------------------------------------------------------ utils
+    def __del__(self):
+        try:
+            if getattr(self, "_plan", None) is not None and self._plan.value:
+                self.lib.swp_plan_destroy(self._plan)
+                self._plan = ctypes.c_void_p()
+        except Exception:  # pragma: no cover
+            pass
+
+    @property
+    def stream(self) -> int:
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def _states(self, fourier=None, hist=None, diag=None) -> ctypes.Array:
+        arr = (_lib.GroupState * len(self.groups))()
+        for g, gd in enumerate(self.groups):
+            f = gd["fourier"] if fourier is None else fourier[g]
+            arr[g].fourier = f.data_ptr()
+            arr[g].resid = gd["resid"].data_ptr()
+            arr[g].params = gd["params"].data_ptr()
+            arr[g].member = gd["member"].data_ptr()
+            arr[g].diag = diag[g].data_ptr() if diag is not None and diag[g] is not None else None
+            arr[g].hist = hist[g].data_ptr() if hist is not None and hist[g] is not None else None
+        return arr
+
+    def _check(self, rc, what):
+        _lib.check(rc, self._plan, what)
+
+    # ------------------------------------------------------------- geometry
+    def geometry(self, g: int = 0) -> Dict[str, torch.Tensor]:
+        """FP64 mus, w and dense Pmn, Hmn (J, M+1, N+1) built on the GPU."""
+        if g in self._geo_cache:
+            return self._geo_cache[g]
+        gd = self.groups[g]
+        J, M = gd["J"], gd["M"]
+        mus = torch.empty(J, dtype=torch.float64, device=self.device)
+        w = torch.empty(J, dtype=torch.float64, device=self.device)
+        P = torch.empty((J, M + 1, M + 1), dtype=torch.float64, device=self.device)
+        H = torch.empty_like(P)
+        self._check(self.lib.swp_geometry(self._plan, g, mus.data_ptr(), w.data_ptr(), P.data_ptr(), H.data_ptr(), self.stream), "geometry")
+        out = dict(mus=mus, w=w, Pmn=P, Hmn=H)
+        self._geo_cache[g] = out
+        return out
+
+    # ------------------------------------------------------------ parameters
+    def set_params(self, g: int, **kw) -> None:
+        """Set per-member scalars (float or length-B tensor) of group g."""
+        gd = self.groups[g]
+        for name, v in kw.items():
+            row = PARAM_NAMES.index(name)
+            t = torch.as_tensor(v, dtype=torch.float64, device=self.device)
+            gd["params"][row].copy_(t.expand(gd["B"]) if t.dim() == 0 else t.reshape(gd["B"]))
+
+    # ------------------------------------------------------------------ state
+    def new_diag(self, nsteps: int) -> List[torch.Tensor]:
+        """Per-step diagnostic rows (nsteps+1, 5, B) initialised for min/max/sum."""
+        out = []
+        for gd in self.groups:
+            d = torch.zeros((nsteps + 1, _lib.NDIAG, gd["B"]), dtype=torch.float64, device=self.device)
+            d[:, _lib.D_SPIN] = 1e300
+            d[:, _lib.D_PHIMIN] = 1e300
+            d[:, _lib.D_PHIMAX] = -1e300
+            out.append(d)
+        return out
+
+    def init_state(self, ics: Sequence[torch.Tensor], flags: RunFlagsC, diag=None) -> None:
+        """ics[g]: physical (5, B, J, I) eta, delta, Phi, U, V in the compute dtype."""
+        ptrs = []
+        keep = []
+        for g, gd in enumerate(self.groups):
+            x = ics[g].to(device=self.device, dtype=self.rdtype).contiguous()
+            if tuple(x.shape) != (5, gd["B"], gd["J"], gd["I"]):
+                raise ValueError(f"initial fields of group {g} must have shape {(5, gd['B'], gd['J'], gd['I'])}")
+            keep.append(x)
+            ptrs.append(x.data_ptr())
+            gd["fourier"].zero_()
+            gd["member"].zero_()
+            gd["member"][_lib.MS_WCURR] = 1.0
+            gd["member"][_lib.MS_WMID] = 1.0
+        self._check(self.lib.swp_init_state(self._plan, self._states(diag=diag), _lib.ptr_array(ptrs), ctypes.byref(flags.c()), self.stream), "init_state")
+        self._ic_keep = keep
+
+    def diagnose_winds(self, eta_delta: Sequence[torch.Tensor]) -> List[torch.Tensor]:
+        """U, V from physical eta, delta (model.py:644-666).  Clobbers the Fourier state."""
+        ins, outs = [], []
+        for g, gd in enumerate(self.groups):
+            x = eta_delta[g].to(device=self.device, dtype=self.rdtype).contiguous()
+            ins.append(x)
+            outs.append(torch.empty((2, gd["B"], gd["J"], gd["I"]), dtype=self.rdtype, device=self.device))
+        self._check(self.lib.swp_diagnose_winds(self._plan, self._states(), _lib.ptr_array([x.data_ptr() for x in ins]),
+                                                _lib.ptr_array([o.data_ptr() for o in outs]), self.stream), "diagnose_winds")
+        return outs
+
+    def forward(self, flags: RunFlagsC, t0: int, nsteps: int, row0: int = 0, diag=None, hist=None,
+                write_prev_last: bool = True, fourier=None) -> None:
+        self._check(self.lib.swp_forward(self._plan, self._states(fourier=fourier, hist=hist, diag=diag), ctypes.byref(flags.c()),
+                                         int(t0), int(nsteps), int(row0), int(bool(write_prev_last)), self.stream), "forward")
+
+    def output_physical(self, flags: RunFlagsC, fourier=None) -> List[torch.Tensor]:
+        outs = [torch.empty((8, gd["B"], gd["J"], gd["I"]), dtype=self.rdtype, device=self.device) for gd in self.groups]
+        self._check(self.lib.swp_output_physical(self._plan, self._states(fourier=fourier), _lib.ptr_array([o.data_ptr() for o in outs]),
+                                                 ctypes.byref(flags.c()), self.stream), "output_physical")
+        return outs
+
+    def state_copy(self, ckpt: Sequence[torch.Tensor], to_ckpt: bool) -> None:
+        self._check(self.lib.swp_state_copy(self._plan, self._states(), _lib.ptr_array([c.data_ptr() for c in ckpt]),
+                                            0 if to_ckpt else 1, self.stream), "state_copy")
