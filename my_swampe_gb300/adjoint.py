@@ -1,0 +1,138 @@
+"""Differentiable integration: a ``torch.autograd.Function`` over a whole run.
+
+Forward: two-level initial state from physical fields, ``nsteps`` modified-
+Euler steps in the CUDA kernels, full Fourier state checkpointed every
+``ckpt_every`` steps, physical (eta, delta, Phi, U, V) of the final state
+returned.  Backward: for each checkpoint window, last first, the window is
+recomputed from its checkpoint (states kept per step) and the hand-written
+adjoint step kernels run backwards through it; the adjoint of the initial-
+state construction then gives gradients of the initial physical fields.
+Gradients with respect to taurad, taudrag, DPhieq and Phibar are reduced per
+member in FP64 on the device.
+
+This replaces reverse-mode ``jax.grad`` through ``run_model_scan_final``
+(reference ``unit_tests/test_autodiff.py:49-129``; ``model.py:1330-1334``
+per-step remat) with O(nsteps / ckpt_every) stored states.
+"""
+from __future__ import annotations
+
+from typing import List, Sequence
+
+import torch
+
+from . import _lib
+from .engine import Engine, RunFlagsC
+
+GRAD_PARAMS = ("taurad", "taudrag", "DPhieq", "Phibar")
+
+
+class Integration:
+    """Forward + checkpointed adjoint for an :class:`Engine` (all groups)."""
+
+    def __init__(self, engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, ckpt_every: int = 50):
+        if flags.scheme != 0:
+            raise NotImplementedError("the adjoint is implemented for the modified-Euler scheme")
+        if flags.test == 1:
+            raise NotImplementedError("the adjoint of test=1 (fixed winds) is not implemented")
+        if nsteps < 1:
+            raise ValueError("nsteps must be >= 1 for a differentiable run")
+        self.eng = engine
+        self.flags = RunFlagsC(scheme=0, forcflag=flags.forcflag, diffflag=flags.diffflag, modalflag=flags.modalflag,
+                               test=flags.test, diagnostics=False)
+        self.t0 = int(t0)
+        self.nsteps = int(nsteps)
+        self.K = max(1, min(int(ckpt_every), self.nsteps))
+        self.nwin = (self.nsteps + self.K - 1) // self.K
+        self.ckpt: List[List[torch.Tensor]] = []
+        self.ics: List[torch.Tensor] = []
+        self._slots = None
+
+    # ------------------------------------------------------------- forward
+    def run_forward(self, ics: Sequence[torch.Tensor]) -> List[torch.Tensor]:
+        eng = self.eng
+        self.ics = [x.to(device=eng.device, dtype=eng.rdtype).contiguous() for x in ics]
+        eng.init_state(self.ics, self.flags)
+        self.ckpt = [[gd["fourier"].clone() for gd in eng.groups]]
+        t = self.t0
+        for w in range(self.nwin):
+            n = min(self.K, self.nsteps - w * self.K)
+            eng.forward(self.flags, t0=t, nsteps=n, write_prev_last=(w == self.nwin - 1))
+            t += n
+            if w < self.nwin - 1:
+                self.ckpt.append([gd["fourier"].clone() for gd in eng.groups])
+        out = eng.output_physical(self.flags)
+        return [o[:5] for o in out]
+
+    # ------------------------------------------------------------ backward
+    def run_backward(self, dphys: Sequence[torch.Tensor]):
+        eng = self.eng
+        lam, lamy, grad = eng.new_adjoint_buffers()
+        eng.adjoint_seed(dphys, lam)
+        if self._slots is None:
+            self._slots = [[torch.empty_like(gd["fourier"]) for gd in eng.groups] for _ in range(self.K + 1)]
+        slots = self._slots
+        for w in reversed(range(self.nwin)):
+            n = min(self.K, self.nsteps - w * self.K)
+            t_w = self.t0 + w * self.K
+            for g in range(len(eng.groups)):
+                slots[0][g].copy_(self.ckpt[w][g])
+            for k in range(n):  # recompute the window, keeping every state
+                for g in range(len(eng.groups)):
+                    slots[k + 1][g].copy_(slots[k][g])
+                eng.forward(self.flags, t0=t_w + k, nsteps=1, write_prev_last=False, fourier=slots[k + 1])
+            for k in reversed(range(n)):
+                eng.adjoint_step(self.flags, slots[k], slots[k + 1], lam, lamy, grad, t=t_w + k)
+        # adjoint of the initial-state construction (uses the initial Fourier state for shapes only)
+        dic = eng.adjoint_init(self.flags, self.ics, lam, grad)
+        return dic, grad
+
+
+class _IntegrateFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, integ: Integration, *flat):
+        # flat = per group: taurad, taudrag, DPhieq, Phibar (B,), ics (5, B, J, I)
+        eng = integ.eng
+        ng = len(eng.groups)
+        ics = []
+        for g in range(ng):
+            tr, td, dp, pb, ic = flat[5 * g: 5 * g + 5]
+            eng.set_params(g, taurad=tr.detach(), taudrag=td.detach(), DPhieq=dp.detach(), Phibar=pb.detach())
+            ics.append(ic.detach())
+        outs = integ.run_forward(ics)
+        ctx.integ = integ
+        ctx.in_dtypes = [x.dtype for x in flat]
+        return tuple(o.to(flat[4].dtype) for o in outs)
+
+    @staticmethod
+    def backward(ctx, *gouts):
+        integ = ctx.integ
+        eng = integ.eng
+        dphys = [(g if g is not None else torch.zeros((5, gd["B"], gd["J"], gd["I"]), device=eng.device))
+                 for g, gd in zip(gouts, eng.groups)]
+        dic, grad = integ.run_backward(dphys)
+        res = [None]
+        for g in range(len(eng.groups)):
+            gr = grad[g]
+            res += [gr[_lib.G_TAURAD].to(ctx.in_dtypes[5 * g]), gr[_lib.G_TAUDRAG].to(ctx.in_dtypes[5 * g + 1]),
+                    gr[_lib.G_DPHIEQ].to(ctx.in_dtypes[5 * g + 2]), gr[_lib.G_PHIBAR].to(ctx.in_dtypes[5 * g + 3]),
+                    dic[g].to(ctx.in_dtypes[5 * g + 4])]
+        return tuple(res)
+
+
+def integrate(engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, params: Sequence[dict], ics: Sequence[torch.Tensor],
+              ckpt_every: int = 50):
+    """Differentiable run of every group of ``engine``.
+
+    params[g]: dict with (B,) tensors 'taurad', 'taudrag', 'DPhieq', 'Phibar'
+    (the other per-member scalars are set beforehand with engine.set_params);
+    ics[g]: (5, B, J, I) physical eta, delta, Phi, U, V.  Returns per group a
+    (5, B, J, I) tensor of the final physical curr fields.
+    """
+    integ = Integration(engine, flags, t0, nsteps, ckpt_every)
+    flat = []
+    for g, gd in enumerate(engine.groups):
+        for k in GRAD_PARAMS:
+            v = torch.as_tensor(params[g][k], device=engine.device, dtype=torch.float64)
+            flat.append(v.expand(gd["B"]) if v.dim() == 0 else v)
+        flat.append(ics[g])
+    return list(_IntegrateFn.apply(integ, *flat))

@@ -13,6 +13,7 @@ struct swp_plan {
   GroupGeom geom[MAXG];
   int M[MAXG] = {}, B[MAXG] = {}, MT[MAXG] = {}, JB[MAXG] = {};
   size_t spec_smem = 0;
+  size_t spec_adj_smem = 0;
   size_t grid_smem[8] = {};
   std::string err;
 };
@@ -158,6 +159,71 @@ int winds_impl(swp_plan* p, const swp_group_state* st, void* const* ed, void* co
   return cuda_check(p, e, "winds inverse transform");
 }
 
+template <typename T>
+int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
+                      const swp_group_adjoint* adj, const swp_flags* f, cudaStream_t s) {
+  int nbg = 0, nbs = 0;
+  GridLaunch<T> LG = make_grid<T>(p, st_out, nbg);
+  LG.mode = GM_ADJ_STEP;
+  LG.cfg = make_cfg(f);
+  for (int g = 0; g < p->ng; ++g) {
+    LG.grp[g].primal = (const typename cplx<T>::type*)st_out[g].fourier;
+    LG.grp[g].lam = (typename cplx<T>::type*)adj[g].lam;
+    LG.grp[g].lamy = (typename cplx<T>::type*)adj[g].lam_y;
+    LG.grp[g].grad = adj[g].grad;
+    LG.grp[g].member = nullptr;
+  }
+  cudaError_t e = launch_grid<T>(LG, nbg, p->grid_smem[GM_ADJ_STEP], s);
+  if (e != cudaSuccess) return cuda_check(p, e, "grid adjoint launch");
+  SpecLaunch<T> LS = make_spec<T>(p, st_in, nbs);
+  LS.mode = 0;
+  LS.cfg = make_cfg(f);
+  for (int g = 0; g < p->ng; ++g) {
+    LS.grp[g].lam = (typename cplx<T>::type*)adj[g].lam;
+    LS.grp[g].lamY = (const typename cplx<T>::type*)adj[g].lam_y;
+    LS.grp[g].grad = adj[g].grad;
+  }
+  e = launch_spec_adj<T>(LS, nbs, p->spec_adj_smem, s);
+  return cuda_check(p, e, "spectral adjoint launch");
+}
+
+template <typename T>
+int adjoint_seed_impl(swp_plan* p, const swp_group_state* st, const swp_group_adjoint* adj, void* const* dphys,
+                      cudaStream_t s) {
+  size_t es = sizeof(typename cplx<T>::type);
+  for (int g = 0; g < p->ng; ++g) {
+    size_t bytes = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
+    int rc = cuda_check(p, cudaMemsetAsync(adj[g].lam, 0, bytes, s), "adjoint seed memset");
+    if (rc) return rc;
+  }
+  int nbg = 0;
+  GridLaunch<T> LG = make_grid<T>(p, st, nbg);
+  LG.mode = GM_ADJ_OUTPUT;
+  for (int g = 0; g < p->ng; ++g) {
+    LG.grp[g].phys_in = (const T*)dphys[g];
+    LG.grp[g].lam = (typename cplx<T>::type*)adj[g].lam;
+    LG.grp[g].member = nullptr;
+  }
+  return cuda_check(p, launch_grid<T>(LG, nbg, p->grid_smem[GM_ADJ_OUTPUT], s), "adjoint seed launch");
+}
+
+template <typename T>
+int adjoint_init_impl(swp_plan* p, const swp_group_state* st, const swp_group_adjoint* adj, void* const* phys_ic,
+                      void* const* dic, const swp_flags* f, cudaStream_t s) {
+  int nbg = 0;
+  GridLaunch<T> LG = make_grid<T>(p, st, nbg);
+  LG.mode = GM_ADJ_INIT;
+  LG.cfg = make_cfg(f);
+  for (int g = 0; g < p->ng; ++g) {
+    LG.grp[g].phys_in = (const T*)phys_ic[g];
+    LG.grp[g].phys_out = (T*)dic[g];
+    LG.grp[g].lam = (typename cplx<T>::type*)adj[g].lam;
+    LG.grp[g].grad = adj[g].grad;
+    LG.grp[g].member = nullptr;
+  }
+  return cuda_check(p, launch_grid<T>(LG, nbg, p->grid_smem[GM_ADJ_INIT], s), "adjoint init launch");
+}
+
 }  // namespace
 
 extern "C" {
@@ -192,6 +258,8 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
     p->JB[g] = jb;
     size_t ss = f64 ? spec_smem_bytes<double>(M[g], J, p->MT[g]) : spec_smem_bytes<float>(M[g], J, p->MT[g]);
     p->spec_smem = std::max(p->spec_smem, ss);
+    size_t sa = f64 ? spec_adj_smem_bytes<double>(M[g], J, p->MT[g]) : spec_adj_smem_bytes<float>(M[g], J, p->MT[g]);
+    p->spec_adj_smem = std::max(p->spec_adj_smem, sa);
     for (int mode = 0; mode < 8; ++mode) {
       size_t gs = f64 ? grid_smem_bytes<double>(M[g], J, I, jb, mode) : grid_smem_bytes<float>(M[g], J, I, jb, mode);
       p->grid_smem[mode] = std::max(p->grid_smem[mode], gs);
@@ -288,16 +356,34 @@ int swp_state_copy(swp_plan* p, const swp_group_state* st, void* const* ckpt, in
   return SWP_OK;
 }
 
-int swp_adjoint_step(swp_plan* p, const swp_group_state*, const swp_group_state*, const swp_group_adjoint*,
-                     const swp_flags*, int, void*) {
-  return fail(p, SWP_ERR_UNSUPPORTED, "adjoint not built yet");
+int swp_adjoint_step(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
+                     const swp_group_adjoint* adj, const swp_flags* f, int t, void* stream) {
+  (void)t;  // the modified-Euler step map does not depend on t
+  if (!p || !st_in || !st_out || !adj || !f) return fail(p, SWP_ERR_ARG, "null argument");
+  if (f->scheme != 0) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint is implemented for the modified-Euler scheme");
+  if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint of test=1 (fixed winds) is not implemented");
+  if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint runs with diagnostics off (no blow-up gate)");
+  for (int g = 0; g < p->ng; ++g)
+    if (!adj[g].lam || !adj[g].lam_y || !st_in[g].fourier || !st_out[g].fourier) return fail(p, SWP_ERR_ARG, "missing adjoint buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWP_FP64 ? adjoint_step_impl<double>(p, st_in, st_out, adj, f, s)
+                                  : adjoint_step_impl<float>(p, st_in, st_out, adj, f, s);
 }
-int swp_adjoint_seed(swp_plan* p, const swp_group_state*, const swp_group_adjoint*, void* const*, void*) {
-  return fail(p, SWP_ERR_UNSUPPORTED, "adjoint not built yet");
+
+int swp_adjoint_seed(swp_plan* p, const swp_group_state* st, const swp_group_adjoint* adj, void* const* dphys, void* stream) {
+  if (!p || !st || !adj || !dphys) return fail(p, SWP_ERR_ARG, "null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWP_FP64 ? adjoint_seed_impl<double>(p, st, adj, dphys, s)
+                                  : adjoint_seed_impl<float>(p, st, adj, dphys, s);
 }
-int swp_adjoint_init(swp_plan* p, const swp_group_state*, const swp_group_adjoint*, void* const*, void* const*,
-                     const swp_flags*, void*) {
-  return fail(p, SWP_ERR_UNSUPPORTED, "adjoint not built yet");
+
+int swp_adjoint_init(swp_plan* p, const swp_group_state* st, const swp_group_adjoint* adj, void* const* phys_ic,
+                     void* const* dic, const swp_flags* f, void* stream) {
+  if (!p || !st || !adj || !phys_ic || !dic || !f) return fail(p, SWP_ERR_ARG, "null argument");
+  if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint of test=1 (fixed winds) is not implemented");
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWP_FP64 ? adjoint_init_impl<double>(p, st, adj, phys_ic, dic, f, s)
+                                  : adjoint_init_impl<float>(p, st, adj, phys_ic, dic, f, s);
 }
 
 }  // extern "C"

@@ -11,6 +11,7 @@
 // odd-m sign flip produce.  It is evaluated with the standard three-term
 // recurrence in n, and H = (1 - mu^2) dP/dmu from the derivative identity
 //   (1-x^2) dPbar_n^m/dx = -n x Pbar_n^m + sqrt((2n+1)/(2n-1) (n^2-m^2)) Pbar_{n-1}^m.
+#include <cmath>
 #include "swp_internal.h"
 
 namespace swp {
@@ -32,17 +33,34 @@ __global__ void k_gauss_nodes(int J, double* mu, double* w, int* err) {
     dp = J * (x * p1 - p0) / (x * x - 1.0);
     double dx = p1 / dp;
     x -= dx;
-    if (fabs(dx) <= 1e-16 * fabs(x) + 1e-300) { converged = true; break; }
+    if (fabs(dx) <= 4e-16 * fabs(x) + 1e-300) { converged = true; break; }
   }
-  if (!converged) atomicExch(err, 1);
-  // recompute derivative at the converged root for the weight
+  if (!converged) {
+    // one more Newton update at the last iterate; fail only if it is not at round-off level
+    double p0 = 1.0, p1 = x;
+    for (int n = 2; n <= J; ++n) {
+      double p2 = ((2.0 * n - 1.0) * x * p1 - (n - 1.0) * p0) / n;
+      p0 = p1; p1 = p2;
+    }
+    double d = J * (x * p1 - p0) / (x * x - 1.0);
+    if (fabs(p1 / d) > 1e-14) atomicExch(err, 1);
+  }
+  // weight at the exact root x* = x - delta (delta = P_J/P_J', below one ulp):
+  //   w = 2 / ((1-x^2) P_J'^2),  d ln w / dx = 2x/(1-x^2) - 2 P_J''/P_J',
+  //   P_J'' = (2x P_J' - J(J+1) P_J) / (1-x^2)   (Legendre's equation)
+  // The first-order correction removes the ~1e3..1e4 amplification of the
+  // last-ulp root error near the poles.
   double p0 = 1.0, p1 = x;
   for (int n = 2; n <= J; ++n) {
     double p2 = ((2.0 * n - 1.0) * x * p1 - (n - 1.0) * p0) / n;
     p0 = p1; p1 = p2;
   }
-  dp = J * (x * p1 - p0) / (x * x - 1.0);
-  double wt = 2.0 / ((1.0 - x * x) * dp * dp);
+  double omx2 = (1.0 - x) * (1.0 + x);
+  dp = J * (p0 - x * p1) / omx2;
+  double wt = 2.0 / (omx2 * dp * dp);
+  double delta = p1 / dp;
+  double d2 = (2.0 * x * dp - (double)J * (J + 1.0) * p1) / omx2;
+  wt *= 1.0 - delta * (2.0 * x / omx2 - 2.0 * d2 / dp);
   mu[j] = x;
   mu[J - 1 - j] = -x;
   w[j] = wt;
@@ -66,7 +84,7 @@ __global__ void k_lat_consts(int J, int I, const double* mu, double* onemu2, dou
 }
 
 // One thread per (m, j'): recurrence in n, written into the packed layouts.
-__global__ void k_basis(int M, int J, const double* mu, const double* w, const int* boff,
+__global__ void k_basis(int M, int J, const double* mu, const double* w, const int* boff, const double* damage,
                         double* Pw_f, double* Hw_f, double* P_f, double* H_f,
                         double* P_i, double* H_i, double* Pw_i, double* Hw_i,
                         float* Pw_f32, float* Hw_f32, float* P_f32, float* H_f32,
@@ -99,6 +117,9 @@ __global__ void k_basis(int M, int J, const double* mu, const double* w, const i
     double H = -n * x * P;
     if (n > m) H += sqrt((2.0 * n + 1.0) / (2.0 * n - 1.0) * ((double)n * n - (double)m * m)) * Pprev;
     if (n > m) { pm2 = pm1; pm1 = P; }
+    double dmg = damage[m * (N + 1) + n];
+    P *= dmg;
+    H *= dmg;
     int k = n - m, par = k & 1, c = k >> 1;
     int poff = par ? jh * C0 : 0;
     int Cp = par ? cnt / 2 : C0;
@@ -168,6 +189,30 @@ __global__ void k_twiddles(int I, double2* twL64, double2* twI64, float2* twL32,
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// Reference quirk (spectral_transform.py:117-146): the normalisation
+// sqrt(((2n+1)(n-m)!) / (2 (n+m)!)) is formed as a correctly rounded float of
+// the exact ratio, which for M=106 and m >~ 77 falls into the subnormal range
+// (reduced precision) or rounds to 0 (the mode is dropped).  This returns
+// sqrt(fl(ratio) / ratio): 1 in the normal range, else the damage factor the
+// reference basis carries.  The ratio is accumulated as mantissa * 2^e with
+// plain IEEE double operations (relative error < 3e-14, the same on every
+// host); the subnormal rounding is then exact up to that error.
+static double ref_scale_damage(int m, int n) {
+  int e = 0;
+  double mant = std::frexp((2.0 * n + 1.0) / 2.0, &e);
+  for (int k = n - m + 1; k <= n + m; ++k) {
+    int ek = 0;
+    mant = std::frexp(mant / (double)k, &ek);
+    e += ek;
+  }
+  // ratio = mant * 2^e, mant in [0.5, 1)
+  if (e - 1 >= -1022) return 1.0;               // normal: no damage
+  double q = std::ldexp(mant, e + 1074);        // ratio in units of the smallest subnormal
+  double k = std::nearbyint(q);
+  if (k <= 0.0) return 0.0;
+  return std::sqrt(k / q);
+}
+
 // Build all static arrays for truncation M into one device allocation.
 int geometry_build(GroupGeom& gg, int M, cudaStream_t stream, std::string& err) {
   int J, I;
@@ -192,6 +237,7 @@ int geometry_build(GroupGeom& gg, int M, cudaStream_t stream, std::string& err) 
   for (int k = 0; k < 8; ++k) o_b32[k] = take(nb * 4);
   size_t o_twL64 = take(L * 16), o_twI64 = take((L + 1) * 16), o_twL32 = take(L * 8), o_twI32 = take((L + 1) * 8);
   size_t o_day64 = take(I * 8), o_day32 = take(I * 4), o_err = take(4);
+  size_t o_dmg = take((size_t)(M + 1) * (N + 1) * 8);
   cudaError_t e = cudaMalloc(&gg.mem, off);
   if (e != cudaSuccess) { err = std::string("cudaMalloc(geometry): ") + cudaGetErrorString(e); return SWP_ERR_CUDA; }
   gg.bytes = off;
@@ -203,12 +249,17 @@ int geometry_build(GroupGeom& gg, int M, cudaStream_t stream, std::string& err) 
   gg.twL32 = (float2*)(b + o_twL32); gg.twI32 = (float2*)(b + o_twI32);
   gg.dayc64 = (double*)(b + o_day64); gg.dayc32 = (float*)(b + o_day32);
   int* derr = (int*)(b + o_err);
+  double* ddmg = (double*)(b + o_dmg);
+  std::vector<double> dmg((size_t)(M + 1) * (N + 1), 1.0);
+  for (int m = 0; m <= M; ++m)
+    for (int n = m; n <= N; ++n) dmg[(size_t)m * (N + 1) + n] = ref_scale_damage(m, n);
   cudaMemsetAsync(gg.mem, 0, off, stream);
   cudaMemcpyAsync(gg.boff, boff.data(), (M + 2) * 4, cudaMemcpyHostToDevice, stream);
+  cudaMemcpyAsync(ddmg, dmg.data(), dmg.size() * 8, cudaMemcpyHostToDevice, stream);
   k_gauss_nodes<<<(jh + 63) / 64, 64, 0, stream>>>(J, gg.mu, gg.w, derr);
   k_lat_consts<<<(J + 63) / 64, 64, 0, stream>>>(J, I, gg.mu, gg.onemu2, gg.area);
   dim3 gb(M + 1, (jh + 63) / 64);
-  k_basis<<<gb, 64, 0, stream>>>(M, J, gg.mu, gg.w, gg.boff,
+  k_basis<<<gb, 64, 0, stream>>>(M, J, gg.mu, gg.w, gg.boff, ddmg,
       gg.b64[B_PW_F], gg.b64[B_HW_F], gg.b64[B_P_F], gg.b64[B_H_F],
       gg.b64[B_P_I], gg.b64[B_H_I], gg.b64[B_PW_I], gg.b64[B_HW_I],
       gg.b32[B_PW_F], gg.b32[B_HW_F], gg.b32[B_P_F], gg.b32[B_H_F],

@@ -27,6 +27,7 @@ __host__ __device__ inline int grid_ntr(int mode) {
     case GM_INIT: return 8;
     case GM_OUTPUT: return 8;
     case GM_WINDS: return 2;
+    case GM_ADJ_STEP: return 12;
     default: return 8;
   }
 }
@@ -117,6 +118,57 @@ struct Physics {
     }
   }
 };
+
+// Adjoint of Physics::eval.  lz = adjoints of (A, B, C, D, E, PhiF, F, G),
+// lx = adjoints of (eta, Phi, U, V); gacc accumulates d/d(taurad, taudrag,
+// DPhieq, Phibar).  The Q<0 clamp passes no gradient where Q<0 (the
+// reference's jnp.where semantics); Phieq's Phibar cancels in Q.
+template <typename T>
+struct PhysicsAdj {
+  T Pb, itr, itd, DPe;
+  bool nodrag, forced;
+  __device__ void eval(T eta, T Phi, T U, T V, T ihalf, T day_s, const T* lz, T* lx, double* gacc) const {
+    T lU = lz[0] * eta + lz[2] * Phi + lz[4] * (T)2 * U * ihalf;
+    T lV = lz[1] * eta + lz[3] * Phi + lz[4] * (T)2 * V * ihalf;
+    T leta = lz[0] * U + lz[1] * V;
+    T lPhi = lz[2] * U + lz[3] * V;
+    if (forced) {
+      T Phieq = Pb + DPe * day_s;
+      T Q = itr * (Phieq - (Phi + Pb));
+      bool pos = !(Q < (T)0);
+      T Qc = pos ? Q : (T)0;
+      T pt = Phi + Pb;
+      T pts = fabs(pt) > (T)0 ? pt : tiny_val<T>();
+      T r = Qc / pts;
+      T lF = lz[6], lG = lz[7];
+      T lr = -U * lF - V * lG;
+      T itdd = nodrag ? (T)0 : itd;
+      lU += lF * (-r - itdd);
+      lV += lG * (-r - itdd);
+      T lQc = lr / pts;
+      T lpts = -lr * r / pts;
+      T lQ = lz[5] + (pos ? lQc : (T)0);
+      lPhi += -itr * lQ + lpts;
+      gacc[G_TAURAD] += (double)lQ * (double)(-Q * itr);
+      if (!nodrag) gacc[G_TAUDRAG] += ((double)lF * U + (double)lG * V) * (double)itd * (double)itd;
+      gacc[G_DPHIEQ] += (double)lQ * (double)itr * (double)day_s;
+      gacc[G_PHIBAR] += (double)lpts;
+    }
+    lx[0] = leta; lx[1] = lPhi; lx[2] = lU; lx[3] = lV;
+  }
+};
+
+template <typename T>
+__device__ void block_add_grads(double* gacc, double* sred, double* grad, int B, int b) {
+  // sred[0..3] must be zero-initialised before the first __syncthreads of the kernel
+  for (int q = 0; q < NGRAD; ++q) {
+    double v = gacc[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&sred[q], v);
+  }
+  __syncthreads();
+  if (threadIdx.x < NGRAD && grad) atomicAdd(&grad[threadIdx.x * B + b], sred[threadIdx.x]);
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch<T> Lc) {
@@ -270,6 +322,126 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
       int r = t % JB, k = (t / JB) % (M + 1), q = t / (JB * (M + 1));
       T2 v = r2c_post<T2, T>(res + ((size_t)q * JB + r) * L, L, k, g.twI, invI);
       G.four[(F_A + q) * FS + ((size_t)k * B + b) * J + j0 + r] = v;
+    }
+    return;
+  }
+
+  if (mode == GM_ADJ_STEP || mode == GM_ADJ_INIT) {
+    // ---------------------------------------------- adjoint of GM_STEP / GM_INIT
+    PhysicsAdj<T> pa;
+    pa.Pb = ph.Pb; pa.itr = ph.itr; pa.itd = ph.itd; pa.DPe = ph.DPe; pa.nodrag = ph.nodrag; pa.forced = ph.forced;
+    const int nz = ph.forced ? 8 : 5;
+    const int npr = (mode == GM_ADJ_STEP) ? 4 : 0;  // primal fields transformed here (eta, Phi, U, V)
+    if (threadIdx.x < 4) sred[threadIdx.x] = 0.0;
+    __syncthreads();
+    // batch 1: lambda of the nonlinear Fourier terms -> grid (adjoint of fft(x/I)[:M+1]) and primal grid fields
+    const int pf[4] = {F_ETA, F_PHI, F_U, F_V};
+    const int nb1 = nz + npr;
+    for (int t = threadIdx.x; t < nb1 * JB * L; t += blockDim.x) {
+      int k = t % L, fr = t / L, r = fr % JB, f = fr / JB;
+      T2 z;
+      if (f < nz) {
+        const T2* y = G.lam + (F_A + f) * FS + (size_t)b * J + (j0 + r);
+        z = c2r_pre<T2, T>(y, B * J, M, L, k, g.twI, invI, invI * (T)0.5);
+      } else {
+        const T2* y = G.primal + pf[f - nz] * FS + (size_t)b * J + (j0 + r);
+        z = c2r_pre<T2, T>(y, B * J, M, L, k, g.twI, (T)1, (T)1);
+      }
+      bufA[(size_t)fr * L + k] = z;
+    }
+    __syncthreads();
+    T2* zin = cfft_batch<+1>(bufA, bufB, L, nb1 * JB, g.twL);
+    T2* zout = (zin == bufA) ? bufB : bufA;
+    double gacc[NGRAD] = {0.0, 0.0, 0.0, 0.0};
+    for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
+      int n = t % L, r = t / L, j = j0 + r;
+      T ihalf = (T)(1.0 / (2.0 * g.onemu2[j]));
+      T s = (T)sqrt(g.onemu2[j]);
+      T lx[2][4];
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        T lz[8];
+        for (int q = 0; q < 8; ++q) {
+          T2 v = q < nz ? zin[((size_t)q * JB + r) * L + n] : mk<T2>(0, 0);
+          lz[q] = e ? v.y : v.x;
+        }
+        T eta, Phi, U, V;
+        if (mode == GM_ADJ_STEP) {
+          T2 a0 = zin[((size_t)(nz + 0) * JB + r) * L + n], a1 = zin[((size_t)(nz + 1) * JB + r) * L + n];
+          T2 a2 = zin[((size_t)(nz + 2) * JB + r) * L + n], a3 = zin[((size_t)(nz + 3) * JB + r) * L + n];
+          eta = e ? a0.y : a0.x; Phi = e ? a1.y : a1.x; U = e ? a2.y : a2.x; V = e ? a3.y : a3.x;
+        } else {
+          size_t po = ((size_t)b * J + j) * I + 2 * n + e;
+          eta = G.phys_in[0 * PS + po]; Phi = G.phys_in[2 * PS + po];
+          U = G.phys_in[3 * PS + po]; V = G.phys_in[4 * PS + po];
+        }
+        pa.eval(eta, Phi, U, V, ihalf, sday[2 * n + e] * s, lz, lx[e], gacc);
+      }
+      if (mode == GM_ADJ_STEP) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) zout[((size_t)q * JB + r) * L + n] = mk<T2>(lx[0][q], lx[1][q]);
+      } else {
+        // adjoint of the initial grid fields from the nonlinear terms (eta, delta, Phi, U, V)
+        size_t po = ((size_t)b * J + j) * I + 2 * n;
+        T* o = G.phys_out;
+        o[0 * PS + po] = lx[0][0]; o[0 * PS + po + 1] = lx[1][0];
+        o[1 * PS + po] = (T)0;     o[1 * PS + po + 1] = (T)0;
+        o[2 * PS + po] = lx[0][1]; o[2 * PS + po + 1] = lx[1][1];
+        o[3 * PS + po] = lx[0][2]; o[3 * PS + po + 1] = lx[1][2];
+        o[4 * PS + po] = lx[0][3]; o[4 * PS + po + 1] = lx[1][3];
+      }
+    }
+    block_add_grads<T>(gacc, sred, G.grad, B, b);
+    if (mode == GM_ADJ_STEP) {
+      // adjoint of x = Re(Y_0) + 2 Re sum_{m>=1} Y_m e^{i theta}:  lambda Y_m = c_m sum_i lambda x_i e^{-i theta}
+      T2* res = cfft_batch<-1>(zout, zin, L, 4 * JB, g.twL);
+      const int yf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
+      const int rmap[5] = {0, -1, 1, 2, 3};
+      for (int t = threadIdx.x; t < 5 * JB * (M + 1); t += blockDim.x) {
+        int r = t % JB, k = (t / JB) % (M + 1), q = t / (JB * (M + 1));
+        size_t o = ((size_t)k * B + b) * J + j0 + r;
+        T2 v = G.lam[yf[q] * FS + o];
+        if (rmap[q] >= 0) v = cadd(v, r2c_post<T2, T>(res + ((size_t)rmap[q] * JB + r) * L, L, k, g.twI, k == 0 ? (T)1 : (T)2));
+        G.lamy[(size_t)q * FS + o] = v;
+      }
+      return;
+    }
+    // GM_ADJ_INIT batch 2: adjoint of the Fourier curr carries (fft(x/I)[:M+1]) of the ICs
+    __syncthreads();
+    const int cf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
+    for (int t = threadIdx.x; t < 5 * JB * L; t += blockDim.x) {
+      int k = t % L, fr = t / L, r = fr % JB, f = fr / JB;
+      const T2* y = G.lam + cf[f] * FS + (size_t)b * J + (j0 + r);
+      bufA[(size_t)fr * L + k] = c2r_pre<T2, T>(y, B * J, M, L, k, g.twI, invI, invI * (T)0.5);
+    }
+    __syncthreads();
+    T2* z2 = cfft_batch<+1>(bufA, bufB, L, 5 * JB, g.twL);
+    for (int t = threadIdx.x; t < 5 * JB * L; t += blockDim.x) {
+      int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
+      size_t po = f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
+      T2 v = z2[(size_t)fr * L + n];
+      G.phys_out[po] += v.x;
+      G.phys_out[po + 1] += v.y;
+    }
+    return;
+  }
+
+  if (mode == GM_ADJ_OUTPUT) {
+    // ---------------------------------------------- seed: lambda of physical curr fields -> Fourier
+    __syncthreads();
+    const int nf = 5;
+    for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
+      int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
+      const T* x = G.phys_in + f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
+      bufA[(size_t)fr * L + n] = mk<T2>(x[0], x[1]);
+    }
+    __syncthreads();
+    T2* res = cfft_batch<-1>(bufA, bufB, L, nf * JB, g.twL);
+    const int sf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
+    for (int t = threadIdx.x; t < nf * JB * (M + 1); t += blockDim.x) {
+      int r = t % JB, k = (t / JB) % (M + 1), f = t / (JB * (M + 1));
+      T2 v = r2c_post<T2, T>(res + ((size_t)f * JB + r) * L, L, k, g.twI, k == 0 ? (T)1 : (T)2);
+      G.lam[sf[f] * FS + ((size_t)k * B + b) * J + j0 + r] = v;
     }
     return;
   }

@@ -449,6 +449,334 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
   }
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint of k_spectral (modified Euler, mode 0).  Same per-m decomposition:
+//   lambda of the Fourier outputs (eta, delta, Phi, U, V at column m)
+//   --transposed inverse Legendre (P^T, H^T)--> lambda of the spectral inputs
+//   --transposed wind inversion, n(n+1), hyperdiffusion-->
+//   --transposed forward Legendre (Pw, Hw)--> lambda of the 9 combined inputs
+//   --transposed combination--> lambda of the 11 Fourier state fields.
+// The Phibar gradient of the combination is accumulated from the primal
+// state before the step.
+constexpr int NYS_P = 5;   // lambda eta, delta, Phi, U, V on P
+constexpr int NYS_H = 2;   // lambda U, V on H
+constexpr int NYS = NYS_P + NYS_H;
+constexpr int NKADJ = 5;   // coefficient vectors of the transposed forward contraction
+
+template <typename T>
+size_t spec_adj_smem_bytes(int M, int J, int MT) {
+  int Jh = J / 2, R = 2 * MT, cnt = M + 1;
+  size_t x = (size_t)18 * J * MT;
+  size_t bf = (size_t)2 * cnt * Jh;
+  size_t sres = (size_t)NYS * cnt * R;
+  size_t kad = (size_t)NKADJ * cnt * R;
+  size_t coef = (size_t)3 * MT * cnt;
+  return (x + bf + sres + kad + coef) * sizeof(T) + 64 * sizeof(double);
+}
+template size_t spec_adj_smem_bytes<double>(int, int, int);
+template size_t spec_adj_smem_bytes<float>(int, int, int);
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ SpecLaunch<T> L) {
+  typedef typename cplx<T>::type T2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int idx;
+  const SpecGroup<T>& G = pick_group(L, idx);
+  const StepCfg& cfg = L.cfg;
+  const Geom<T>& g = G.g;
+  const int M = g.M, N = M, J = g.J, Jh = J / 2;
+  const int m = idx / G.ntb;
+  const int b0 = (idx % G.ntb) * G.MT;
+  const int MT = G.MT;
+  const int mt = min(MT, G.B - b0);
+  const int R = 2 * MT;
+  const int cnt = N + 1 - m, C0 = (cnt + 1) / 2, C1 = cnt / 2;
+  const int cntmax = N + 1;
+  const size_t FS = (size_t)(M + 1) * G.B * J;
+
+  T* X = (T*)smem_raw;                                  // [NYS][2][Jh][R], later [9][MT][J][2]
+  T* Bf = X + (size_t)18 * J * MT;                       // [2][cnt*Jh]
+  T* Sres = Bf + (size_t)2 * cntmax * Jh;                // [NYS][cnt][R]
+  T* Kad = Sres + (size_t)NYS * cntmax * R;              // [NKADJ][cnt][R]
+  T* sig = Kad + (size_t)NKADJ * cntmax * R;
+  T* sigP = sig + MT * cntmax;
+  T* tcmn = sigP + MT * cntmax;
+  double* sgrad = (double*)(tcmn + MT * cntmax);         // [MT] Phibar gradient partials
+
+  for (int t = threadIdx.x; t < MT * cnt; t += blockDim.x) {
+    int bt = t / cnt, k = t % cnt, n = m + k;
+    double s = 1.0, sp = 1.0, tc = 0.0;
+    if (bt < mt) {
+      int b = b0 + bt;
+      double a = G.par[P_A * G.B + b], dt = G.par[P_DT * G.B + b];
+      if (cfg.diffflag) {
+        double K6 = G.par[P_K6 * G.B + b], K6P = G.par[P_K6PHI * G.B + b];
+        double nd = (double)n;
+        double ncoeff = ((nd * nd * nd) / (a * a * a)) * (((nd + 1) * (nd + 1) * (nd + 1)) / (a * a * a));
+        double a6 = a * a * a * a * a * a;
+        s = 1.0 / (1.0 + 2.0 * dt * K6 * (ncoeff - 8.0 / a6));
+        sp = 1.0 / (1.0 + 2.0 * dt * K6P * ncoeff);
+      }
+      tc = (n == 0) ? 0.0 : a / ((double)n * (n + 1));
+    }
+    sig[bt * cntmax + k] = (T)s;
+    sigP[bt * cntmax + k] = (T)sp;
+    tcmn[bt * cntmax + k] = (T)tc;
+  }
+  if (threadIdx.x < MT) sgrad[threadIdx.x] = 0.0;
+
+  // ---- phase 1: symmetrised adjoints of the step outputs at column m
+  const T2* LY = G.lamY;  // [5][M+1][B][J]
+  for (int t = threadIdx.x; t < MT * Jh; t += blockDim.x) {
+    int bt = t / Jh, jp = t % Jh;
+    T2 ys[5], ya[5];
+    if (bt < mt) {
+      int b = b0 + bt;
+      size_t on = ((size_t)m * G.B + b) * J + jp, os = ((size_t)m * G.B + b) * J + (J - 1 - jp);
+#pragma unroll
+      for (int f = 0; f < 5; ++f) {
+        T2 u = LY[f * FS + on], v = LY[f * FS + os];
+        ys[f] = cadd(u, v);
+        ya[f] = csub(u, v);
+      }
+    } else {
+#pragma unroll
+      for (int f = 0; f < 5; ++f) { ys[f] = mk<T2>(0, 0); ya[f] = ys[f]; }
+    }
+    auto put = [&](int q, int sa, T2 v) {
+      T* base = X + (size_t)q * 2 * Jh * R;
+      base[(sa * Jh + jp) * R + 2 * bt] = v.x;
+      base[(sa * Jh + jp) * R + 2 * bt + 1] = v.y;
+    };
+#pragma unroll
+    for (int f = 0; f < 5; ++f) { put(f, 0, ys[f]); put(f, 1, ya[f]); }
+    put(5, 0, ys[3]); put(5, 1, ya[3]);
+    put(6, 0, ys[4]); put(6, 1, ya[4]);
+  }
+  {
+    const T* srcP = g.P_f + g.boff[m];
+    const T* srcH = g.H_f + g.boff[m];
+    int nb = cnt * Jh;
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) { Bf[t] = srcP[t]; Bf[cntmax * Jh + t] = srcH[t]; }
+  }
+  __syncthreads();
+
+  // ---- phase 2: transposed inverse Legendre (contract over J/2 latitudes)
+  {
+    const int nt0 = (C0 + FWD_TC - 1) / FWD_TC, nt1 = (C1 + FWD_TC - 1) / FWD_TC;
+    const int tasks = R * (nt0 + nt1);
+    const T* BP = Bf;
+    const T* BH = Bf + cntmax * Jh;
+    for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+      int r = task % R;
+      int ct = task / R;
+      int par = ct < nt0 ? 0 : 1;
+      if (par) ct -= nt0;
+      int Cp = par ? C1 : C0;
+      int c0 = ct * FWD_TC;
+      const T* bp = BP + (par ? Jh * C0 : 0);
+      const T* bh = BH + (par ? Jh * C0 : 0);
+      const int sP = par, sH = 1 - par;
+      T acc[NYS][FWD_TC];
+#pragma unroll
+      for (int q = 0; q < NYS; ++q)
+#pragma unroll
+        for (int k = 0; k < FWD_TC; ++k) acc[q][k] = (T)0;
+      for (int jp = 0; jp < Jh; ++jp) {
+        T xp[NYS_P], xh[NYS_H];
+#pragma unroll
+        for (int q = 0; q < NYS_P; ++q) xp[q] = X[((size_t)q * 2 * Jh + sP * Jh + jp) * R + r];
+#pragma unroll
+        for (int q = 0; q < NYS_H; ++q) xh[q] = X[((size_t)(NYS_P + q) * 2 * Jh + sH * Jh + jp) * R + r];
+        T vp[FWD_TC], vh[FWD_TC];
+#pragma unroll
+        for (int k = 0; k < FWD_TC; ++k) {
+          int c = c0 + k;
+          vp[k] = c < Cp ? bp[jp * Cp + c] : (T)0;
+          vh[k] = c < Cp ? bh[jp * Cp + c] : (T)0;
+        }
+#pragma unroll
+        for (int k = 0; k < FWD_TC; ++k) {
+#pragma unroll
+          for (int q = 0; q < NYS_P; ++q) acc[q][k] = fma(xp[q], vp[k], acc[q][k]);
+#pragma unroll
+          for (int q = 0; q < NYS_H; ++q) acc[NYS_P + q][k] = fma(xh[q], vh[k], acc[NYS_P + q][k]);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < FWD_TC; ++k) {
+        int c = c0 + k;
+        if (c >= Cp) break;
+        int pc = par ? C0 + c : c;
+#pragma unroll
+        for (int q = 0; q < NYS; ++q) Sres[((size_t)q * cntmax + pc) * R + r] = acc[q][k];
+      }
+    }
+  }
+  __syncthreads();
+  // ---- phase 3: transposed wind inversion, n(n+1) and hyperdiffusion
+  for (int t = threadIdx.x; t < MT * cnt; t += blockDim.x) {
+    int bt = t / cnt, kk = t % cnt, n = m + kk;
+    int par = kk & 1, c = kk >> 1;
+    int pc = par ? C0 + c : c;
+    auto S = [&](int q, int comp) { return Sres[((size_t)q * cntmax + pc) * R + 2 * bt + comp]; };
+    T xm = (T)m;
+    T tc = tcmn[bt * cntmax + kk];
+    T s = sig[bt * cntmax + kk], sp = sigP[bt * cntmax + kk];
+    T nn1 = (T)((double)n * (n + 1));
+    // lambda delta_s = (i m) lambda Uprep - lambda Hin_V ; lambda eta_s = (i m) lambda Vprep + lambda Hin_U
+    T lds_r = -xm * S(3, 1) - S(6, 0), lds_i = xm * S(3, 0) - S(6, 1);
+    T les_r = -xm * S(4, 1) + S(5, 0), les_i = xm * S(4, 0) + S(5, 1);
+    T w = (n == 0) ? (T)0 : tc;
+    T lce_r = S(0, 0) + w * les_r, lce_i = S(0, 1) + w * les_i;
+    T lcd_r = S(1, 0) + w * lds_r, lcd_i = S(1, 1) + w * lds_i;
+    T lcp_r = S(2, 0), lcp_i = S(2, 1);
+    auto K = [&](int q, int comp, T v) { Kad[((size_t)q * cntmax + pc) * R + 2 * bt + comp] = v; };
+    K(0, 0, sp * lcp_r); K(0, 1, sp * lcp_i);
+    K(1, 0, nn1 * sp * lcp_r); K(1, 1, nn1 * sp * lcp_i);
+    K(2, 0, s * lcd_r); K(2, 1, s * lcd_i);
+    K(3, 0, nn1 * s * lcd_r); K(3, 1, nn1 * s * lcd_i);
+    K(4, 0, s * lce_r); K(4, 1, s * lce_i);
+  }
+  __syncthreads();
+  {
+    const T* srcP = g.Pw_i + g.boff[m];
+    const T* srcH = g.Hw_i + g.boff[m];
+    int nb = cnt * Jh;
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) { Bf[t] = srcP[t]; Bf[cntmax * Jh + t] = srcH[t]; }
+  }
+  __syncthreads();
+  // ---- phase 4: transposed forward Legendre -> adjoints of the 9 combined inputs
+  T* Cad = X;  // [9][MT][J][2]
+  {
+    const int njt = (Jh + INV_TJ - 1) / INV_TJ;
+    const int tasks = R * njt;
+    const T* BP = Bf;
+    const T* BH = Bf + cntmax * Jh;
+    // P results: K0..K4 on Pw -> PhiP1, PhiP2, dP1, dP2, eP1 ; H results: K0, K2, K3, K4 on Hw -> PhiH1, dH1, dH2, eH1
+    for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+      int r = task % R;
+      int j0 = (task / R) * INV_TJ;
+      T E[9][INV_TJ], O[9][INV_TJ];
+#pragma unroll
+      for (int q = 0; q < 9; ++q)
+#pragma unroll
+        for (int k = 0; k < INV_TJ; ++k) { E[q][k] = (T)0; O[q][k] = (T)0; }
+      auto accum = [&](T (&acc)[9][INV_TJ], int par, int c) {
+        int pc = par ? C0 + c : c;
+        T kv[NKADJ];
+#pragma unroll
+        for (int q = 0; q < NKADJ; ++q) kv[q] = Kad[((size_t)q * cntmax + pc) * R + r];
+#pragma unroll
+        for (int k = 0; k < INV_TJ; ++k) {
+          int jp = j0 + k;
+          T p = jp < Jh ? BP[(par ? Jh * C0 : 0) + c * Jh + jp] : (T)0;
+          T h = jp < Jh ? BH[(par ? Jh * C0 : 0) + c * Jh + jp] : (T)0;
+#pragma unroll
+          for (int q = 0; q < NKADJ; ++q) acc[q][k] = fma(kv[q], p, acc[q][k]);
+          acc[5][k] = fma(kv[0], h, acc[5][k]);
+          acc[6][k] = fma(kv[2], h, acc[6][k]);
+          acc[7][k] = fma(kv[3], h, acc[7][k]);
+          acc[8][k] = fma(kv[4], h, acc[8][k]);
+        }
+      };
+      for (int c = 0; c < C0; ++c) accum(E, 0, c);
+      for (int c = 0; c < C1; ++c) accum(O, 1, c);
+      const int bt = r >> 1, comp = r & 1;
+#pragma unroll
+      for (int k = 0; k < INV_TJ; ++k) {
+        int jp = j0 + k;
+        if (jp >= Jh) break;
+        int jn = jp, js = J - 1 - jp;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+          Cad[(((size_t)q * MT + bt) * J + jn) * 2 + comp] = E[q][k] + O[q][k];
+          Cad[(((size_t)q * MT + bt) * J + js) * 2 + comp] = E[q][k] - O[q][k];
+        }
+#pragma unroll
+        for (int q = 5; q < 9; ++q) {
+          Cad[(((size_t)q * MT + bt) * J + jn) * 2 + comp] = E[q][k] + O[q][k];
+          Cad[(((size_t)q * MT + bt) * J + js) * 2 + comp] = O[q][k] - E[q][k];
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // ---- phase 5: transposed combination -> adjoints of the state fields; Phibar gradient
+  T2* LAM = G.lam;
+  const T2* PX = G.four;  // primal state before the step
+  for (int t = threadIdx.x; t < MT * J; t += blockDim.x) {
+    int bt = t / J, j = t % J;
+    if (bt >= mt) continue;
+    int b = b0 + bt;
+    size_t o = ((size_t)m * G.B + b) * J + j;
+    auto ld = [&](int q) { return mk<T2>(Cad[(((size_t)q * MT + bt) * J + j) * 2], Cad[(((size_t)q * MT + bt) * J + j) * 2 + 1]); };
+    // slot order: 0 PhiP1, 1 PhiP2, 2 dP1, 3 dP2, 4 eP1, 5 PhiH1, 6 dH1, 7 dH2, 8 eH1
+    T2 lPhiP1 = ld(0), lPhiP2 = ld(1), ldP1 = ld(2), ldP2 = ld(3), leP1 = ld(4);
+    T2 lPhiH1 = ld(5), ldH1 = ld(6), ldH2 = ld(7), leH1 = ld(8);
+    double dt = G.par[P_DT * G.B + b], a = G.par[P_A * G.B + b], Pb = G.par[P_PHIBAR * G.B + b];
+    double tsc = (2.0 * dt) / (a * g.onemu2[j]);
+    T t1 = (T)(tsc / 4.0), t2 = (T)((2.0 * dt / (a * a)) / 4.0);
+    T ia2 = (T)(1.0 / (a * a));
+    T hPb = (T)(Pb * 0.5);
+    T te = cfg.forcflag ? (T)tsc : (T)(tsc / 2.0);
+    T xm = (T)m;
+    T forc = cfg.forcflag ? (T)1 : (T)0;
+    // conj(i*alpha*m) z = -i alpha m z
+    auto mimul = [&](T alpha, T2 z) { return imul(-alpha * xm, z); };
+    T2 lphi = csub(cadd(lPhiP1, cscale(ldP2, t2)), cscale(lPhiP2, hPb * ia2));
+    T2 ldel = cadd(csub(ldP1, cscale(lPhiP1, (T)(dt * Pb))), cscale(ldP2, (T)(-Pb / (a * a))));
+    T2 leta = leP1;
+    T2 lC = cadd(mimul(-t1, lPhiP1), mimul(t1 * (T)0.5 * ia2, ldP2));
+    T2 lD = cadd(cscale(lPhiH1, t1), cscale(ldH2, t1 * (T)0.5 * ia2));
+    T2 lE = cadd(cscale(lPhiP2, -hPb * t2), cscale(ldP2, t2));
+    T2 lPF = cscale(cadd(cscale(lPhiP1, (T)dt), cscale(ldP2, (T)((dt / 2.0) / (a * a)))), forc);
+    T2 lBeff = cadd(mimul(-hPb * t1, lPhiP1), cscale(leH1, te));
+    T2 lAeff = cadd(cscale(lPhiH1, -hPb * t1), mimul(-te, leP1));
+    T2 lBf = mimul(t1, ldP1);
+    T2 lAf = cscale(ldH1, t1);
+    T2 lA = cadd(lAeff, lAf), lB = cadd(lBeff, lBf);
+    T2 lF = cadd(cscale(lBeff, forc), lBf);
+    T2 lG = csub(mk<T2>(0, 0), cadd(cscale(lAeff, forc), lAf));
+    T2 z = mk<T2>(0, 0);
+    LAM[F_ETA * FS + o] = leta; LAM[F_DELTA * FS + o] = ldel; LAM[F_PHI * FS + o] = lphi;
+    LAM[F_A * FS + o] = lA; LAM[F_B * FS + o] = lB; LAM[F_C * FS + o] = lC; LAM[F_D * FS + o] = lD;
+    LAM[F_E * FS + o] = lE; LAM[F_PHIF * FS + o] = lPF; LAM[F_F * FS + o] = lF; LAM[F_G * FS + o] = lG;
+    LAM[F_U * FS + o] = z; LAM[F_V * FS + o] = z;
+    LAM[F_ETA_PREV * FS + o] = z; LAM[F_DELTA_PREV * FS + o] = z; LAM[F_PHI_PREV * FS + o] = z;
+    LAM[F_ETA_MID * FS + o] = z; LAM[F_DELTA_MID * FS + o] = z; LAM[F_PHI_MID * FS + o] = z;
+    if (G.grad) {
+      // d(combined inputs)/dPhibar (modEuler_tdiff.py:80-103, 185-193)
+      T2 del = PX[F_DELTA * FS + o], phi = PX[F_PHI * FS + o], E = PX[F_E * FS + o];
+      T2 A = PX[F_A * FS + o], Bm = PX[F_B * FS + o], Fm = PX[F_F * FS + o], Gm = PX[F_G * FS + o];
+      T2 Beff = cfg.forcflag ? cadd(Bm, Fm) : Bm, Aeff = cfg.forcflag ? csub(A, Gm) : A;
+      T2 dP1 = csub(cscale(del, (T)-dt), cscale(imul(xm, Beff), (T)0.5 * t1));
+      T2 dH1 = cscale(Aeff, (T)-0.5 * t1);
+      T2 dP2 = cscale(cadd(cscale(E, t2), cscale(phi, ia2)), (T)-0.5);
+      T2 dd2 = cscale(del, -ia2);
+      double gp = (double)lPhiP1.x * dP1.x + (double)lPhiP1.y * dP1.y + (double)lPhiH1.x * dH1.x +
+                  (double)lPhiH1.y * dH1.y + (double)lPhiP2.x * dP2.x + (double)lPhiP2.y * dP2.y +
+                  (double)ldP2.x * dd2.x + (double)ldP2.y * dd2.y;
+      atomicAdd(&sgrad[bt], gp);
+    }
+  }
+  __syncthreads();
+  if (G.grad && threadIdx.x < mt) atomicAdd(&G.grad[G_PHIBAR * G.B + b0 + threadIdx.x], sgrad[threadIdx.x]);
+}
+
+template <typename T>
+cudaError_t launch_spec_adj(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_spectral_adj<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr_set = true;
+  }
+  k_spectral_adj<T><<<nblocks, 256, smem, s>>>(L);
+  return cudaGetLastError();
+}
+template cudaError_t launch_spec_adj<double>(const SpecLaunch<double>&, int, size_t, cudaStream_t);
+template cudaError_t launch_spec_adj<float>(const SpecLaunch<float>&, int, size_t, cudaStream_t);
+
 template <typename T>
 cudaError_t launch_spec(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
   static bool attr_set = false;

@@ -99,7 +99,8 @@ struct GridGroup {
   T* phys_out;                          // output/adjoint: [5 or 8][B][J][I]
   // adjoint
   typename cplx<T>::type* lam;          // adjoint Fourier fields
-  const typename cplx<T>::type* primal; // primal Fourier fields of the step
+  typename cplx<T>::type* lamy;         // adjoint of the K1 outputs [5][M+1][B][J]
+  const typename cplx<T>::type* primal; // primal Fourier fields after the step
   double* grad;                         // [NGRAD][B]
 };
 
@@ -124,6 +125,7 @@ enum GridMode {
 };
 
 template <typename T> size_t spec_smem_bytes(int M, int J, int MT);
+template <typename T> size_t spec_adj_smem_bytes(int M, int J, int MT);
 template <typename T> size_t grid_smem_bytes(int M, int J, int I, int JB, int mode);
 template <typename T> cudaError_t launch_spec(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s);
 template <typename T> cudaError_t launch_spec_adj(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s);

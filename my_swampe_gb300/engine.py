@@ -207,3 +207,38 @@ class Engine:
     def state_copy(self, ckpt: Sequence[torch.Tensor], to_ckpt: bool) -> None:
         self._check(self.lib.swp_state_copy(self._plan, self._states(), _lib.ptr_array([c.data_ptr() for c in ckpt]),
                                             0 if to_ckpt else 1, self.stream), "state_copy")
+
+    # ---------------------------------------------------------------- adjoint
+    def _adjs(self, lam, lamy, grad) -> ctypes.Array:
+        arr = (_lib.GroupAdjoint * len(self.groups))()
+        for g in range(len(self.groups)):
+            arr[g].lam = lam[g].data_ptr()
+            arr[g].lam_y = lamy[g].data_ptr() if lamy is not None else None
+            arr[g].grad = grad[g].data_ptr() if grad is not None else None
+        return arr
+
+    def new_adjoint_buffers(self):
+        lam = [torch.zeros_like(gd["fourier"]) for gd in self.groups]
+        lamy = [torch.zeros((5,) + tuple(gd["fourier"].shape[1:]), dtype=self.cdtype, device=self.device) for gd in self.groups]
+        grad = [torch.zeros((_lib.NGRAD, gd["B"]), dtype=torch.float64, device=self.device) for gd in self.groups]
+        return lam, lamy, grad
+
+    def adjoint_seed(self, dphys: Sequence[torch.Tensor], lam) -> None:
+        """lam <- adjoint of the Fourier state from gradients of the physical curr fields (5, B, J, I)."""
+        xs = [d.to(device=self.device, dtype=self.rdtype).contiguous() for d in dphys]
+        self._check(self.lib.swp_adjoint_seed(self._plan, self._states(), self._adjs(lam, None, None),
+                                              _lib.ptr_array([x.data_ptr() for x in xs]), self.stream), "adjoint_seed")
+
+    def adjoint_step(self, flags: RunFlagsC, four_in, four_out, lam, lamy, grad, t: int = 3) -> None:
+        self._check(self.lib.swp_adjoint_step(self._plan, self._states(fourier=four_in), self._states(fourier=four_out),
+                                              self._adjs(lam, lamy, grad), ctypes.byref(flags.c()), int(t), self.stream),
+                    "adjoint_step")
+
+    def adjoint_init(self, flags: RunFlagsC, ics: Sequence[torch.Tensor], lam, grad) -> List[torch.Tensor]:
+        xs = [x.to(device=self.device, dtype=self.rdtype).contiguous() for x in ics]
+        outs = [torch.empty_like(x) for x in xs]
+        self._check(self.lib.swp_adjoint_init(self._plan, self._states(), self._adjs(lam, None, grad),
+                                              _lib.ptr_array([x.data_ptr() for x in xs]),
+                                              _lib.ptr_array([o.data_ptr() for o in outs]), ctypes.byref(flags.c()),
+                                              self.stream), "adjoint_init")
+        return outs

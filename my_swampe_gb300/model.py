@@ -149,9 +149,12 @@ def build_static(*, M, dt, a, omega, g, Phibar, taurad, taudrag, DPhieq, K6, K6P
     J, I, _ = _SUPPORTED_M[M]
     mus, w, Pmn, Hmn = geo["mus"], geo["w"], geo["Pmn"], geo["Hmn"]
     lambdas = torch.linspace(-math.pi, math.pi, I + 1, dtype=torch.float64, device=dev)[:-1]
-    dt_, a_, om_, g_, Pb_, tr_, td_ = (_scalar_tensor(v, dev) for v in (dt, a, omega, g, Phibar, taurad, taudrag))
-    K6_ = _scalar_tensor(K6, dev)
-    K6P = K6_ if K6Phi is None else _scalar_tensor(K6Phi, dev)
+    vals = [_scalar_tensor(v, dev) for v in (dt, a, omega, g, Phibar, taurad, taudrag, DPhieq, K6,
+                                             K6 if K6Phi is None else K6Phi)]
+    if any(v.dim() for v in vals):  # ensemble: broadcast every scalar to the member axis
+        Bn = max(v.shape[0] for v in vals if v.dim())
+        vals = [v.expand(Bn) if v.dim() == 0 else v for v in vals]
+    dt_, a_, om_, g_, Pb_, tr_, td_, DP, K6_, K6P = vals
     n = torch.arange(N + 1, dtype=torch.float64, device=dev)
     mm = torch.arange(M + 1, dtype=torch.float64, device=dev)
     nn1 = n * (n + 1)
@@ -187,7 +190,6 @@ def build_static(*, M, dt, a, omega, g, Phibar, taurad, taudrag, DPhieq, K6, K6P
         lam = lambdas[None, :]
         day = ((lambdas > -math.pi / 2) & (lambdas < math.pi / 2))[None, :]
         term_shape = torch.cos(lam) * torch.sqrt(1 - mus[:, None] ** 2)
-        DP = _scalar_tensor(DPhieq, dev)
         if DP.dim():
             Phieq = Pb_[:, None, None] + torch.where(day, DP[:, None, None] * term_shape, 0.0)
         else:
