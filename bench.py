@@ -1,0 +1,421 @@
+"""Benchmark: ensemble member-steps/s for forward + adjoint at M=42, B=256.
+
+One bench "step" is one complete differentiable integration of the workload:
+B = 256 forced members at M = 42 (64 x 128 grid), 1440 modified-Euler time
+steps forward with the full state checkpointed every 50 steps, then the
+adjoint sweep (each 50-step window recomputed from its checkpoint, then the
+hand-written adjoint steps) back to gradients of the loss
+mean((Phi_T - Phi_target)^2) with respect to the initial (eta, delta, Phi,
+U, V) and to taurad, taudrag, DPhieq and Phibar of every member.
+
+value : fast path (FP32 state and pointwise math) on device-resident inputs,
+        B * 1440 / seconds per step.  The plain FP64 GPU path is timed on the
+        same workload and reported beside it with the error of the fast path
+        against it (relative L2 and max of eta, delta, Phi after 1440 steps).
+e2e   : the same metric through the public API (torch.autograd over
+        my_swampe_gb300.adjoint.integrate) with pinned HOST inputs copied in
+        and the gradients copied out inside the timed region.
+--impl reference : the reference's CPU algorithm (the oracle restatement, run
+        with torch autograd on the host cores) on a bounded sample of the
+        same workload.
+
+The data are synthetic (my_swampe_gb300.workloads.forced_ensemble); the
+working set per model step is larger than L2 and L2 is additionally flushed
+with a 512 MB write between timed steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+METRIC = "ensemble steps/s fwd+adjoint at M=42, fast vs plain FP64 GPU, at stated error"
+UNIT = "member-steps/s"
+M_BENCH, B_BENCH, T_BENCH, CKPT = 42, 256, 1440, 50
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200",
+                                          "-i", str(_local_rank())], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "", 1).isdigit())
+        mx = max(float(r[2]) for r in rows if r[2].replace(".", "", 1).isdigit())
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def _local_rank():
+    return int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def _flush_l2(buf):
+    buf.add_(1.0)
+
+
+def _setup(precision, B, seed=1234):
+    import torch
+    from my_swampe_gb300.engine import Engine, RunFlagsC
+    from my_swampe_gb300.adjoint import Integration
+    from my_swampe_gb300 import workloads
+
+    eng = Engine([(M_BENCH, B)], precision)
+    wl = workloads.forced_ensemble(eng, seed=seed)
+    workloads.apply_params(eng, 0, wl["params"])
+    flags = RunFlagsC()
+    integ = Integration(eng, flags, t0=2, nsteps=T_BENCH, ckpt_every=CKPT)
+    ics = wl["ics"].to(eng.rdtype)
+    return eng, wl, flags, integ, ics
+
+
+def _target(eng, wl, flags, ics):
+    """Phi_target: a run at perturbed taurad (x1.1) and DPhieq (x0.9)."""
+    from my_swampe_gb300 import workloads
+
+    p = dict(wl["params"])
+    p["taurad"] = p["taurad"] * 1.1
+    p["DPhieq"] = p["DPhieq"] * 0.9
+    workloads.apply_params(eng, 0, p)
+    eng.init_state([ics], flags)
+    eng.forward(flags, t0=2, nsteps=T_BENCH)
+    tgt = eng.output_physical(flags)[0][2].clone()
+    workloads.apply_params(eng, 0, wl["params"])
+    return tgt
+
+
+def _one_step(integ, ics, target):
+    """forward + adjoint of the loss mean((Phi_T - target)^2); device-resident."""
+    import torch
+
+    out = integ.run_forward([ics])[0]
+    d = torch.zeros_like(out)
+    d[2] = (2.0 / target.numel()) * (out[2] - target)
+    dic, grad = integ.run_backward([d])
+    return out, dic[0], grad[0]
+
+
+def _time_steps(fn, steps, warmup, flush):
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        flush()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    return times
+
+
+def _algorithmic_bytes(kernel, B, J=64, M=42, elem=8):
+    """Algorithmic DRAM bytes of one launch: Fourier columns (J x (M+1) complex
+    per member) each kernel must read and write.
+      spectral : reads 11 step inputs + 3 RA-filtered carries, writes 3 curr + U, V + 3 carries
+      grid     : reads eta, Phi, U, V; writes A..E, PhiF, F, G
+      grid_adj : reads 4 primal + 8 lambda(A..G) + 5 lambda(outputs); writes 5
+      spectral_adj : reads 5 lambda(outputs) + 7 primal inputs; writes 19 lambda fields"""
+    cols = {"spectral": 22, "grid": 12, "grid_adj": 22, "spectral_adj": 31}[kernel]
+    return cols * J * (M + 1) * elem * B
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(_local_rank())
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from __graft_entry__ import build
+
+    build()
+    B = args.B
+    peak, peak_kind = _peaks()
+    flush_buf = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    flush = lambda: _flush_l2(flush_buf)  # noqa: E731
+
+    # ---------------- fast path (headline)
+    eng, wl, flags, integ, ics = _setup("fast", B, seed=1234 + 100000 * rank)
+    target = _target(eng, wl, flags, ics)
+    state = {}
+
+    def step_fast():
+        state["out"], state["dic"], state["grad"] = _one_step(integ, ics, target)
+
+    if world > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler()
+    sampler.start()
+    times = _time_steps(step_fast, args.steps, args.warmup, flush)
+    clocks = sampler.stop()
+    t_mean = float(np.mean(times))
+    t_max = t_mean
+    if world > 1:
+        tt = torch.tensor([t_mean], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * B * T_BENCH / t_max
+    out_fast = state["out"].double()
+    grad_fast = state["grad"].clone()
+
+    # kernel roofline (CUDA events inside the library on the launching stream)
+    kt = eng.time_kernels(flags, nrep=20, adjoint=True)
+    per_step = {k: v for k, v in kt.items()}
+    # per model step of fwd+adjoint: spectral, grid run twice (forward + recompute), adjoints once
+    share = {"spectral": 2 * per_step["spectral"], "grid": 2 * per_step["grid"],
+             "grid_adj": per_step["grid_adj"], "spectral_adj": per_step["spectral_adj"]}
+    dom = max(share, key=share.get)
+    alg = _algorithmic_bytes(dom, B, elem=8)
+    achieved = alg / (per_step[dom] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": None,
+                "ms_per_launch": {k: round(v, 5) for k, v in per_step.items()},
+                "algorithmic_bytes_per_launch": alg}
+
+    # ---------------- e2e through the public API with host buffers
+    from my_swampe_gb300.adjoint import integrate, GRAD_PARAMS
+
+    host_ics = ics.detach().cpu().pin_memory()
+    host_par = {k: wl["params"][k].detach().cpu().pin_memory() for k in GRAD_PARAMS if k != "Phibar"}
+    host_par["Phibar"] = torch.full((B,), wl["params"]["Phibar"], dtype=torch.float64).pin_memory()
+    host_tgt = target.detach().cpu().pin_memory()
+    out_ic = torch.empty(host_ics.shape, dtype=host_ics.dtype).pin_memory()
+    out_par = torch.empty((4, B), dtype=torch.float64).pin_memory()
+
+    def step_e2e():
+        d_ics = host_ics.to("cuda", non_blocking=True).requires_grad_(True)
+        d_par = {k: v.to("cuda", non_blocking=True).requires_grad_(True) for k, v in host_par.items()}
+        d_tgt = host_tgt.to("cuda", non_blocking=True)
+        out = integrate(eng, flags, 2, T_BENCH, [d_par], [d_ics], ckpt_every=CKPT, integration=integ)[0]
+        loss = torch.mean((out[2].double() - d_tgt.double()) ** 2)
+        loss.backward()
+        out_ic.copy_(d_ics.grad, non_blocking=True)
+        for k, name in enumerate(GRAD_PARAMS):
+            out_par[k].copy_(d_par[name].grad, non_blocking=True)
+
+    e2e_times = _time_steps(step_e2e, max(2, args.steps), 1, flush)
+    e2e_t = float(np.mean(e2e_times))
+    if world > 1:
+        tt = torch.tensor([e2e_t], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+    h2d = host_ics.numel() * host_ics.element_size() + sum(v.numel() * 8 for v in host_par.values()) + \
+        host_tgt.numel() * host_tgt.element_size()
+    d2h = out_ic.numel() * out_ic.element_size() + out_par.numel() * 8
+
+    # ---------------- plain FP64 GPU path on the same workload
+    fp64 = None
+    if not args.skip_fp64:
+        del integ
+        eng64, wl64, flags64, integ64, ics64 = _setup("fp64", B, seed=1234 + 100000 * rank)
+        target64 = target.double()
+        st64 = {}
+
+        def step64():
+            st64["out"], st64["dic"], st64["grad"] = _one_step(integ64, ics64, target64)
+
+        t64 = _time_steps(step64, args.fp64_steps, 1, flush)
+        v64 = B * T_BENCH / float(np.mean(t64))
+        o64 = st64["out"]
+        err = {}
+        for k, name in enumerate(("eta", "delta", "Phi")):
+            ref = o64[k]
+            dif = out_fast[k] - ref
+            err[name] = {"rel_l2": float(torch.linalg.vector_norm(dif) / torch.linalg.vector_norm(ref)),
+                         "max_abs": float(dif.abs().max()), "max_rel_to_fieldmax": float(dif.abs().max() / ref.abs().max())}
+        g64 = st64["grad"]
+        gerr = {name: float(torch.linalg.vector_norm(grad_fast[k] - g64[k]) / torch.linalg.vector_norm(g64[k]))
+                for k, name in enumerate(GRAD_PARAMS)}
+        kt64 = eng64.time_kernels(flags64, nrep=5, adjoint=True)
+        fp64 = {"value": round(v64, 1), "ms_per_step": round(1e3 * float(np.mean(t64)), 3), "steps": args.fp64_steps,
+                "speedup_fast_over_fp64": round(value / (world * v64), 2), "error_fast_vs_fp64_after_1440": err,
+                "grad_rel_l2_fast_vs_fp64": gerr,
+                "ms_per_launch": {k: round(v, 5) for k, v in kt64.items()}}
+
+    # ---------------- CPU baseline (oracle restatement, torch autograd, host cores)
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        cpu = _cpu_baseline(args.cpu_members, args.cpu_nsteps)
+
+    launches = 1 + 2 * T_BENCH + 1 + 1 + 4 * T_BENCH + 1  # init, forward, output, seed, windows, init-adjoint
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * t_max, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 state/pointwise, f32 Legendre (fast path); f64 plain path",
+        "data": "synthetic (seeded forced ensemble: taurad, taudrag log-uniform [1e4,1e6] s, DPhieq U[1e5,4e6], Phi noise 1e-3*Phibar at n<=10)",
+        "config": {"workload": "forced ensemble fwd+adjoint, M=42 (64x128), B=256 members per GPU, 1440 steps, checkpoint every 50",
+                   "members_per_gpu": B, "steps_per_member": T_BENCH, "ckpt_every": CKPT,
+                   "l2": "working set > L2 (126 MB); 512 MB L2 flush write between timed steps"},
+        "e2e": {"value": round(world * B * T_BENCH / e2e_t, 1), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1e3 * e2e_t, 3)},
+        "roofline": roofline,
+        "fp64_plain_gpu": fp64,
+        "cpu_baseline": cpu,
+        "gpu_launches": launches * args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _cpu_baseline(members, nsteps):
+    """The oracle (reference algorithm restated) with torch autograd on the host
+    cores: forward + reverse mode over `nsteps` steps for `members` members."""
+    import numpy as np
+    import torch
+
+    from oracle import swampe_oracle as o
+
+    cores = torch.get_num_threads()
+    xp = o.torch_backend()
+    geo = o.cached_geometry(M_BENCH)
+    J, I = geo["J"], geo["I"]
+    rng = np.random.default_rng(7)
+    mu = geo["mus"][:, None]
+    t_total = 0.0
+    for b in range(members):
+        tr = torch.tensor(10.0 ** rng.uniform(4, 6), dtype=torch.float64, requires_grad=True)
+        td = torch.tensor(10.0 ** rng.uniform(4, 6), dtype=torch.float64, requires_grad=True)
+        dp = torch.tensor(rng.uniform(1e5, 4e6), dtype=torch.float64, requires_grad=True)
+        pb = torch.tensor(4.0e6, dtype=torch.float64, requires_grad=True)
+        Phi0 = torch.tensor(4e3 * rng.standard_normal((J, I)) * 0.1, requires_grad=True)
+        eta0 = torch.tensor(2 * 3.2e-5 * mu * np.ones((1, I)), requires_grad=True)
+        z = torch.zeros((J, I), dtype=torch.float64)
+        t0 = time.perf_counter()
+        r = o.run_model_scan_final(xp, M=M_BENCH, dt=30.0, tmax=2 + nsteps, Phibar=pb, omega=3.2e-5, a=8.2e7,
+                                   taurad=tr, taudrag=td, DPhieq=dp, eta0_init=eta0, delta0_init=z,
+                                   Phi0_init=Phi0, U0_init=z, V0_init=z)
+        loss = torch.mean(r["last_state"]["Phi_curr"] ** 2)
+        loss.backward()
+        t_total += time.perf_counter() - t0
+    v = members * nsteps / t_total
+    return {"value": round(v, 2), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{members} member(s) x {nsteps} steps fwd+adjoint (torch autograd through the oracle, FP64), M=42"}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+
+    vals = []
+    for _ in range(args.warmup):
+        _cpu_baseline(1, args.ref_nsteps)
+    for _ in range(args.steps):
+        vals.append(_cpu_baseline(1, args.ref_nsteps)["value"])
+    import torch
+
+    v = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * args.ref_nsteps / v, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded forced member, Phi noise), same regime as our arm",
+        "config": {"workload": "forced ensemble fwd+adjoint, M=42 (64x128), 1 member x "
+                               f"{args.ref_nsteps} steps per timed step (bounded sample of the B=256 x 1440 workload)"},
+        "cpu_baseline": {"value": round(v, 2), "unit": UNIT, "cores": torch.get_num_threads(), "kind": "port",
+                         "sample": f"1 member x {args.ref_nsteps} steps fwd+adjoint per step; JAX (the reference's "
+                                   "runtime) is not installable here, so its algorithm runs as the oracle restatement "
+                                   "with torch autograd"},
+        "e2e": {"value": round(v, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--B", type=int, default=B_BENCH)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--cpu-members", type=int, default=1)
+    ap.add_argument("--cpu-nsteps", type=int, default=40)
+    ap.add_argument("--ref-nsteps", type=int, default=20)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -113,6 +113,14 @@ int swp_diagnose_winds(swp_plan* plan, const swp_group_state* st, void* const* p
 int swp_forward(swp_plan* plan, const swp_group_state* st, const swp_flags* flags,
                 int t0, int nsteps, int row0, int write_prev_last, void* stream);
 
+/* swp_forward over [t0, t0+nsteps) that first copies the state at
+ * t0 + w*ckpt_every into slot w of ckpt[g] (ceil(nsteps/ckpt_every)
+ * contiguous Fourier states) -- the forward sweep of a checkpointed
+ * differentiable run (diagnostics off).  Captured once into a CUDA graph per
+ * argument set and replayed. */
+int swp_forward_checkpointed(swp_plan* plan, const swp_group_state* st, const swp_flags* flags,
+                             int t0, int nsteps, int ckpt_every, void* const* ckpt, void* stream);
+
 /* Physical curr and RA-filtered prev fields: phys_out[g] = real[8][B][J][I]
  * (eta, delta, Phi, U, V, eta_prev, delta_prev, Phi_prev) -- the physical
  * members of the reference State (model.py:380-425). */
@@ -141,6 +149,24 @@ int swp_adjoint_seed(swp_plan* plan, const swp_group_state* st, const swp_group_
  * parameter gradients of the initial forcing into adj[g].grad. */
 int swp_adjoint_init(swp_plan* plan, const swp_group_state* st, const swp_group_adjoint* adj,
                      void* const* phys_ic, void* const* dic, const swp_flags* flags, void* stream);
+
+/* Adjoint of one checkpoint window [t0, t0+nsteps): restores st[g].fourier
+ * (the window's checkpoint) into slot 0 of slots[g] (nsteps+1 contiguous
+ * Fourier states), recomputes the window out of place keeping every state,
+ * then runs the adjoint steps backwards.  adj[g].lam: adjoint of the state at
+ * t0+nsteps on entry, at t0 on exit; adj[g].grad accumulates.  The sequence
+ * is captured once into a CUDA graph per (window length, buffers) and replayed.
+ * Replaces reverse-mode jax.grad through lax.scan with jax.checkpoint per step
+ * (model.py:1330-1334). */
+int swp_adjoint_window(swp_plan* plan, const swp_group_state* st, void* const* slots,
+                       const swp_group_adjoint* adj, const swp_flags* flags, int t0, int nsteps, void* stream);
+
+/* Average device time (ms, CUDA events on `stream`) over nrep launches of the
+ * step kernels on st (modified in place): ms_out[0] spectral (Legendre) kernel,
+ * [1] grid kernel, and with adj != NULL [2] grid adjoint, [3] spectral adjoint.
+ * Measurement hook for the roofline; no reference counterpart. */
+int swp_time_kernels(swp_plan* plan, const swp_group_state* st, const swp_group_adjoint* adj,
+                     const swp_flags* flags, int nrep, float* ms_out, void* stream);
 
 #ifdef __cplusplus
 }

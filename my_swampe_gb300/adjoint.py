@@ -43,7 +43,7 @@ class Integration:
         self.nsteps = int(nsteps)
         self.K = max(1, min(int(ckpt_every), self.nsteps))
         self.nwin = (self.nsteps + self.K - 1) // self.K
-        self.ckpt: List[List[torch.Tensor]] = []
+        self.ckpt: List[torch.Tensor] = []
         self.ics: List[torch.Tensor] = []
         self._slots = None
 
@@ -52,14 +52,10 @@ class Integration:
         eng = self.eng
         self.ics = [x.to(device=eng.device, dtype=eng.rdtype).contiguous() for x in ics]
         eng.init_state(self.ics, self.flags)
-        self.ckpt = [[gd["fourier"].clone() for gd in eng.groups]]
-        t = self.t0
-        for w in range(self.nwin):
-            n = min(self.K, self.nsteps - w * self.K)
-            eng.forward(self.flags, t0=t, nsteps=n, write_prev_last=(w == self.nwin - 1))
-            t += n
-            if w < self.nwin - 1:
-                self.ckpt.append([gd["fourier"].clone() for gd in eng.groups])
+        if not self.ckpt:
+            self.ckpt = [torch.empty((self.nwin,) + tuple(gd["fourier"].shape), dtype=eng.cdtype, device=eng.device)
+                         for gd in eng.groups]
+        eng.forward_checkpointed(self.flags, self.t0, self.nsteps, self.K, self.ckpt)
         out = eng.output_physical(self.flags)
         return [o[:5] for o in out]
 
@@ -69,20 +65,12 @@ class Integration:
         lam, lamy, grad = eng.new_adjoint_buffers()
         eng.adjoint_seed(dphys, lam)
         if self._slots is None:
-            self._slots = [[torch.empty_like(gd["fourier"]) for gd in eng.groups] for _ in range(self.K + 1)]
-        slots = self._slots
+            self._slots = [torch.empty((self.K + 1,) + tuple(gd["fourier"].shape), dtype=eng.cdtype, device=eng.device)
+                           for gd in eng.groups]
         for w in reversed(range(self.nwin)):
             n = min(self.K, self.nsteps - w * self.K)
-            t_w = self.t0 + w * self.K
-            for g in range(len(eng.groups)):
-                slots[0][g].copy_(self.ckpt[w][g])
-            for k in range(n):  # recompute the window, keeping every state
-                for g in range(len(eng.groups)):
-                    slots[k + 1][g].copy_(slots[k][g])
-                eng.forward(self.flags, t0=t_w + k, nsteps=1, write_prev_last=False, fourier=slots[k + 1])
-            for k in reversed(range(n)):
-                eng.adjoint_step(self.flags, slots[k], slots[k + 1], lam, lamy, grad, t=t_w + k)
-        # adjoint of the initial-state construction (uses the initial Fourier state for shapes only)
+            eng.adjoint_window(self.flags, [c[w] for c in self.ckpt], self._slots, lam, lamy, grad,
+                               t0=self.t0 + w * self.K, nsteps=n)
         dic = eng.adjoint_init(self.flags, self.ics, lam, grad)
         return dic, grad
 
@@ -120,15 +108,17 @@ class _IntegrateFn(torch.autograd.Function):
 
 
 def integrate(engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, params: Sequence[dict], ics: Sequence[torch.Tensor],
-              ckpt_every: int = 50):
+              ckpt_every: int = 50, integration: Integration = None):
     """Differentiable run of every group of ``engine``.
 
     params[g]: dict with (B,) tensors 'taurad', 'taudrag', 'DPhieq', 'Phibar'
     (the other per-member scalars are set beforehand with engine.set_params);
     ics[g]: (5, B, J, I) physical eta, delta, Phi, U, V.  Returns per group a
-    (5, B, J, I) tensor of the final physical curr fields.
+    (5, B, J, I) tensor of the final physical curr fields.  Passing the same
+    ``integration`` object across calls reuses its checkpoint buffers and the
+    library's captured CUDA graphs.
     """
-    integ = Integration(engine, flags, t0, nsteps, ckpt_every)
+    integ = integration if integration is not None else Integration(engine, flags, t0, nsteps, ckpt_every)
     flat = []
     for g, gd in enumerate(engine.groups):
         for k in GRAD_PARAMS:

@@ -1,15 +1,26 @@
 // C ABI of libswampe_gb300: plan lifetime, launch decomposition and the
 // step loop.  See include/swampe_gb300.h for the contract of each symbol.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include "swp_internal.h"
 
 using namespace swp;
 
+struct GraphEntry {
+  std::vector<uint64_t> key;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t last_use = 0;
+};
+
 struct swp_plan {
   int precision = SWP_FP64;
   int ng = 0;
+  cudaStream_t cap_stream = nullptr;     // private stream used only for graph capture
+  std::vector<GraphEntry> graphs;        // small LRU cache of instantiated step graphs
+  uint64_t use_clock = 0;
+  bool graphs_enabled = true;
   GroupGeom geom[MAXG];
   int M[MAXG] = {}, B[MAXG] = {}, MT[MAXG] = {}, JB[MAXG] = {};
   size_t spec_smem = 0;
@@ -43,6 +54,7 @@ SpecLaunch<T> make_spec(const swp_plan* p, const swp_group_state* st, int& nbloc
     G.MT = p->MT[g];
     G.ntb = (G.B + G.MT - 1) / G.MT;
     G.four = (typename cplx<T>::type*)st[g].fourier;
+    G.four_out = G.four;
     G.par = st[g].params;
     G.member = st[g].member;
     G.diag = st[g].diag;
@@ -91,9 +103,13 @@ StepCfg make_cfg(const swp_flags* f) {
   return c;
 }
 
+// Launch nsteps steps.  In place on st[g].fourier, or -- when `slots` is given --
+// out of place: step k reads slot k and writes slot k+1 (slot stride `sstride`
+// complex elements), which keeps every intermediate state of a window.
 template <typename T>
-int forward_impl(swp_plan* p, const swp_group_state* st, const swp_flags* f, int t0, int nsteps,
-                 int row0, int write_prev_last, cudaStream_t s) {
+int forward_steps(swp_plan* p, const swp_group_state* st, const swp_flags* f, int t0, int nsteps, int row0,
+                  int write_prev_last, void* const* slots, cudaStream_t s) {
+  typedef typename cplx<T>::type T2;
   int nbs = 0, nbg = 0;
   SpecLaunch<T> LS = make_spec<T>(p, st, nbs);
   GridLaunch<T> LG = make_grid<T>(p, st, nbg);
@@ -110,6 +126,12 @@ int forward_impl(swp_plan* p, const swp_group_state* st, const swp_flags* f, int
     for (int g = 0; g < p->ng; ++g) {
       size_t PS = (size_t)p->B[g] * p->geom[g].J * p->geom[g].I;
       LG.grp[g].hist = st[g].hist ? (T*)st[g].hist + (size_t)(row0 + k) * 5 * PS : nullptr;
+      if (slots) {
+        size_t ss = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J;
+        LS.grp[g].four = (T2*)slots[g] + (size_t)k * ss;
+        LS.grp[g].four_out = (T2*)slots[g] + (size_t)(k + 1) * ss;
+        LG.grp[g].four = LS.grp[g].four_out;
+      }
     }
     cudaError_t e = launch_spec<T>(LS, nbs, p->spec_smem, s);
     if (e != cudaSuccess) return cuda_check(p, e, "spectral kernel launch");
@@ -117,6 +139,74 @@ int forward_impl(swp_plan* p, const swp_group_state* st, const swp_flags* f, int
     if (e != cudaSuccess) return cuda_check(p, e, "grid kernel launch");
   }
   return SWP_OK;
+}
+
+// Run `body(stream)` through a cached CUDA graph keyed by `key` (captured on the
+// plan's private stream, launched on the caller's stream).
+template <typename F>
+int run_graph(swp_plan* p, const std::vector<uint64_t>& key, F body, cudaStream_t s) {
+  if (!p->graphs_enabled) return body(s);
+  GraphEntry* hit = nullptr;
+  for (auto& ge : p->graphs)
+    if (ge.key == key) { hit = &ge; break; }
+  if (!hit) {
+    if (!p->cap_stream) {
+      cudaError_t e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking);
+      if (e != cudaSuccess) return cuda_check(p, e, "capture stream");
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_check(p, e, "graph capture begin");
+    int rc = body(p->cap_stream);
+    e = cudaStreamEndCapture(p->cap_stream, &graph);
+    if (rc != SWP_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
+    if (e != cudaSuccess) return cuda_check(p, e, "graph capture end");
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_check(p, e, "graph instantiate");
+    if (p->graphs.size() >= 16) {  // evict the least recently used graph
+      size_t lru = 0;
+      for (size_t i = 1; i < p->graphs.size(); ++i)
+        if (p->graphs[i].last_use < p->graphs[lru].last_use) lru = i;
+      cudaGraphExecDestroy(p->graphs[lru].exec);
+      p->graphs.erase(p->graphs.begin() + lru);
+    }
+    GraphEntry ge;
+    ge.key = key;
+    ge.exec = exec;
+    p->graphs.push_back(ge);
+    hit = &p->graphs.back();
+  }
+  hit->last_use = ++p->use_clock;
+  return cuda_check(p, cudaGraphLaunch(hit->exec, s), "graph launch");
+}
+
+void key_flags(std::vector<uint64_t>& k, const swp_flags* f) {
+  k.push_back((uint64_t)f->scheme | ((uint64_t)f->forcflag << 4) | ((uint64_t)f->diffflag << 8) |
+              ((uint64_t)f->modalflag << 12) | ((uint64_t)f->test << 16) | ((uint64_t)f->diagnostics << 20));
+  uint64_t bu;
+  memcpy(&bu, &f->blowup, 8);
+  k.push_back(bu);
+}
+
+void key_state(std::vector<uint64_t>& k, const swp_plan* p, const swp_group_state* st) {
+  for (int g = 0; g < p->ng; ++g) {
+    k.push_back((uint64_t)st[g].fourier); k.push_back((uint64_t)st[g].resid); k.push_back((uint64_t)st[g].params);
+    k.push_back((uint64_t)st[g].member); k.push_back((uint64_t)st[g].diag); k.push_back((uint64_t)st[g].hist);
+  }
+}
+
+template <typename T>
+int forward_impl(swp_plan* p, const swp_group_state* st, const swp_flags* f, int t0, int nsteps,
+                 int row0, int write_prev_last, cudaStream_t s) {
+  if (nsteps < 4) return forward_steps<T>(p, st, f, t0, nsteps, row0, write_prev_last, nullptr, s);
+  std::vector<uint64_t> key = {1, (uint64_t)t0, (uint64_t)nsteps, (uint64_t)row0, (uint64_t)write_prev_last};
+  key_flags(key, f);
+  key_state(key, p, st);
+  return run_graph(p, key, [&](cudaStream_t cs) {
+    return forward_steps<T>(p, st, f, t0, nsteps, row0, write_prev_last, nullptr, cs);
+  }, s);
 }
 
 template <typename T>
@@ -224,6 +314,128 @@ int adjoint_init_impl(swp_plan* p, const swp_group_state* st, const swp_group_ad
   return cuda_check(p, launch_grid<T>(LG, nbg, p->grid_smem[GM_ADJ_INIT], s), "adjoint init launch");
 }
 
+template <typename T>
+int adjoint_window_impl(swp_plan* p, const swp_group_state* st, void* const* slots, const swp_group_adjoint* adj,
+                        const swp_flags* f, int t0, int nsteps, cudaStream_t s) {
+  // slot 0 <- checkpoint (outside the graph: its source changes per window)
+  size_t es = sizeof(typename cplx<T>::type);
+  for (int g = 0; g < p->ng; ++g) {
+    size_t bytes = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
+    int rc = cuda_check(p, cudaMemcpyAsync(slots[g], st[g].fourier, bytes, cudaMemcpyDeviceToDevice, s), "window restore");
+    if (rc) return rc;
+  }
+  auto body = [&](cudaStream_t cs) -> int {
+    int rc = forward_steps<T>(p, st, f, t0, nsteps, 0, 0, slots, cs);
+    if (rc) return rc;
+    std::vector<swp_group_state> a(p->ng), b(p->ng);
+    for (int k = nsteps - 1; k >= 0; --k) {
+      for (int g = 0; g < p->ng; ++g) {
+        size_t ss = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
+        a[g] = st[g]; b[g] = st[g];
+        a[g].fourier = (char*)slots[g] + (size_t)k * ss;
+        b[g].fourier = (char*)slots[g] + (size_t)(k + 1) * ss;
+      }
+      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, cs);
+      if (rc) return rc;
+    }
+    return SWP_OK;
+  };
+  // the window map does not depend on t0 except through the RA-filtered carry,
+  // which the adjoint never reads, so one graph serves every window of a length
+  std::vector<uint64_t> key = {2, (uint64_t)nsteps};
+  key_flags(key, f);
+  for (int g = 0; g < p->ng; ++g) {
+    key.push_back((uint64_t)slots[g]); key.push_back((uint64_t)adj[g].lam); key.push_back((uint64_t)adj[g].lam_y);
+    key.push_back((uint64_t)adj[g].grad); key.push_back((uint64_t)st[g].params); key.push_back((uint64_t)st[g].resid);
+    key.push_back((uint64_t)st[g].member);
+  }
+  return run_graph(p, key, body, s);
+}
+
+template <typename T>
+int time_kernels_impl(swp_plan* p, const swp_group_state* st, const swp_group_adjoint* adj, const swp_flags* f,
+                      int nrep, float* ms, cudaStream_t s) {
+  int nbs = 0, nbg = 0;
+  SpecLaunch<T> LS = make_spec<T>(p, st, nbs);
+  GridLaunch<T> LG = make_grid<T>(p, st, nbg);
+  LS.mode = 0;
+  LG.mode = GM_STEP;
+  StepCfg cfg = make_cfg(f);
+  cfg.ra_mode = f->modalflag ? 2 : 1;
+  cfg.diagnostics = 0;
+  LS.cfg = cfg;
+  LG.cfg = cfg;
+  GridLaunch<T> LGa = LG;
+  SpecLaunch<T> LSa = LS;
+  LGa.mode = GM_ADJ_STEP;
+  if (adj) {
+    for (int g = 0; g < p->ng; ++g) {
+      LGa.grp[g].primal = LG.grp[g].four;
+      LGa.grp[g].lam = (typename cplx<T>::type*)adj[g].lam;
+      LGa.grp[g].lamy = (typename cplx<T>::type*)adj[g].lam_y;
+      LGa.grp[g].grad = adj[g].grad;
+      LGa.grp[g].member = nullptr;
+      LSa.grp[g].lam = (typename cplx<T>::type*)adj[g].lam;
+      LSa.grp[g].lamY = (const typename cplx<T>::type*)adj[g].lam_y;
+      LSa.grp[g].grad = adj[g].grad;
+    }
+  }
+  cudaEvent_t ev[5];
+  for (int i = 0; i < 5; ++i) cudaEventCreate(&ev[i]);
+  double acc[4] = {0, 0, 0, 0};
+  for (int r = 0; r < nrep; ++r) {
+    cudaEventRecord(ev[0], s);
+    launch_spec<T>(LS, nbs, p->spec_smem, s);
+    cudaEventRecord(ev[1], s);
+    launch_grid<T>(LG, nbg, p->grid_smem[GM_STEP], s);
+    cudaEventRecord(ev[2], s);
+    if (adj) {
+      launch_grid<T>(LGa, nbg, p->grid_smem[GM_ADJ_STEP], s);
+      cudaEventRecord(ev[3], s);
+      launch_spec_adj<T>(LSa, nbs, p->spec_adj_smem, s);
+      cudaEventRecord(ev[4], s);
+    }
+    cudaError_t e = cudaEventSynchronize(adj ? ev[4] : ev[2]);
+    if (e != cudaSuccess) { for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]); return cuda_check(p, e, "timed kernels"); }
+    float t;
+    cudaEventElapsedTime(&t, ev[0], ev[1]); acc[0] += t;
+    cudaEventElapsedTime(&t, ev[1], ev[2]); acc[1] += t;
+    if (adj) {
+      cudaEventElapsedTime(&t, ev[2], ev[3]); acc[2] += t;
+      cudaEventElapsedTime(&t, ev[3], ev[4]); acc[3] += t;
+    }
+  }
+  for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
+  for (int k = 0; k < 4; ++k) ms[k] = nrep > 0 ? (float)(acc[k] / nrep) : 0.f;
+  return cuda_check(p, cudaGetLastError(), "timed kernels");
+}
+
+template <typename T>
+int forward_ckpt_impl(swp_plan* p, const swp_group_state* st, const swp_flags* f, int t0, int nsteps, int K,
+                      void* const* ckpt, cudaStream_t s) {
+  size_t es = sizeof(typename cplx<T>::type);
+  auto body = [&](cudaStream_t cs) -> int {
+    int nwin = (nsteps + K - 1) / K;
+    for (int w = 0; w < nwin; ++w) {
+      for (int g = 0; g < p->ng; ++g) {
+        size_t bytes = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
+        int rc = cuda_check(p, cudaMemcpyAsync((char*)ckpt[g] + (size_t)w * bytes, st[g].fourier, bytes,
+                                               cudaMemcpyDeviceToDevice, cs), "checkpoint copy");
+        if (rc) return rc;
+      }
+      int n = std::min(K, nsteps - w * K);
+      int rc = forward_steps<T>(p, st, f, t0 + w * K, n, 0, w == nwin - 1, nullptr, cs);
+      if (rc) return rc;
+    }
+    return SWP_OK;
+  };
+  std::vector<uint64_t> key = {3, (uint64_t)t0, (uint64_t)nsteps, (uint64_t)K};
+  key_flags(key, f);
+  key_state(key, p, st);
+  for (int g = 0; g < p->ng; ++g) key.push_back((uint64_t)ckpt[g]);
+  return run_graph(p, key, body, s);
+}
+
 }  // namespace
 
 extern "C" {
@@ -237,6 +449,10 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
   if (!p) return SWP_ERR_ARG;
   p->precision = precision;
   p->ng = ngroups;
+  const char* ng_env = getenv("SWP_NO_GRAPH");
+  p->graphs_enabled = !(ng_env && ng_env[0] == '1');
+  spec_set_attributes();
+  grid_set_attributes();
   cudaStream_t s = 0;
   for (int g = 0; g < ngroups; ++g) {
     if (B[g] < 1) { p->err = "B must be >= 1"; *out = p; return SWP_ERR_ARG; }
@@ -271,6 +487,10 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
 
 int swp_plan_destroy(swp_plan* p) {
   if (!p) return SWP_OK;
+  for (auto& ge : p->graphs)
+    if (ge.exec) cudaGraphExecDestroy(ge.exec);
+  p->graphs.clear();
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   for (int g = 0; g < p->ng; ++g)
     if (p->geom[g].mem) cudaFree(p->geom[g].mem);
   delete p;
@@ -384,6 +604,40 @@ int swp_adjoint_init(swp_plan* p, const swp_group_state* st, const swp_group_adj
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? adjoint_init_impl<double>(p, st, adj, phys_ic, dic, f, s)
                                   : adjoint_init_impl<float>(p, st, adj, phys_ic, dic, f, s);
+}
+
+int swp_adjoint_window(swp_plan* p, const swp_group_state* st, void* const* slots, const swp_group_adjoint* adj,
+                       const swp_flags* f, int t0, int nsteps, void* stream) {
+  if (!p || !st || !slots || !adj || !f) return fail(p, SWP_ERR_ARG, "null argument");
+  if (nsteps < 1) return fail(p, SWP_ERR_ARG, "nsteps must be >= 1");
+  if (f->scheme != 0) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint is implemented for the modified-Euler scheme");
+  if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint of test=1 (fixed winds) is not implemented");
+  if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint runs with diagnostics off (no blow-up gate)");
+  for (int g = 0; g < p->ng; ++g)
+    if (!slots[g] || !adj[g].lam || !adj[g].lam_y || !st[g].fourier) return fail(p, SWP_ERR_ARG, "missing buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWP_FP64 ? adjoint_window_impl<double>(p, st, slots, adj, f, t0, nsteps, s)
+                                  : adjoint_window_impl<float>(p, st, slots, adj, f, t0, nsteps, s);
+}
+
+int swp_time_kernels(swp_plan* p, const swp_group_state* st, const swp_group_adjoint* adj, const swp_flags* f,
+                     int nrep, float* ms_out, void* stream) {
+  if (!p || !st || !f || !ms_out || nrep < 1) return fail(p, SWP_ERR_ARG, "bad argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWP_FP64 ? time_kernels_impl<double>(p, st, adj, f, nrep, ms_out, s)
+                                  : time_kernels_impl<float>(p, st, adj, f, nrep, ms_out, s);
+}
+
+int swp_forward_checkpointed(swp_plan* p, const swp_group_state* st, const swp_flags* f, int t0, int nsteps,
+                             int ckpt_every, void* const* ckpt, void* stream) {
+  if (!p || !st || !f || !ckpt) return fail(p, SWP_ERR_ARG, "null argument");
+  if (nsteps < 1 || ckpt_every < 1) return fail(p, SWP_ERR_ARG, "nsteps and ckpt_every must be >= 1");
+  if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "checkpointed forward runs with diagnostics off");
+  for (int g = 0; g < p->ng; ++g)
+    if (!ckpt[g] || !st[g].fourier || !st[g].params || !st[g].member) return fail(p, SWP_ERR_ARG, "missing buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWP_FP64 ? forward_ckpt_impl<double>(p, st, f, t0, nsteps, ckpt_every, ckpt, s)
+                                  : forward_ckpt_impl<float>(p, st, f, t0, nsteps, ckpt_every, ckpt, s);
 }
 
 }  // extern "C"

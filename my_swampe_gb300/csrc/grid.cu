@@ -553,13 +553,13 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
   }
 }
 
+void grid_set_attributes() {
+  cudaFuncSetAttribute(k_grid<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_grid<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
+
 template <typename T>
 cudaError_t launch_grid(const GridLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_grid<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr_set = true;
-  }
   k_grid<T><<<nblocks, 256, smem, s>>>(L);
   return cudaGetLastError();
 }

@@ -398,7 +398,8 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
   __syncthreads();
 
   // ---- phase 6: write-out and carries (coalesced along j)
-  T2* Fo = G.four;
+  T2* Fo = G.four_out;
+  const T2* Fi = G.four;
   const int do_uv = (mode == 2) || (cfg.test != 1);
   for (int t = threadIdx.x; t < MT * J; t += blockDim.x) {
     int bt = t / J, j = t % J;
@@ -419,11 +420,11 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
     for (int q = 0; q < 3; ++q) {
       T2 nw = get(q);
       if (cfg.write_prev || cfg.ra_mode) {
-        T2 old = Fo[cf[q] * FS + o];
+        T2 old = Fi[cf[q] * FS + o];
         if (cfg.write_prev) Fo[pf[q] * FS + o] = old;
         if (cfg.ra_mode == 1) Fo[rf[q] * FS + o] = old;
         else if (cfg.ra_mode == 2) {
-          T2 mid = Fo[rf[q] * FS + o];
+          T2 mid = Fi[rf[q] * FS + o];
           T aa = (T)al;
           T2 d = cadd(csub(mid, cscale(old, (T)2)), nw);
           Fo[rf[q] * FS + o] = cadd(old, cscale(d, aa));
@@ -766,24 +767,21 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
 
 template <typename T>
 cudaError_t launch_spec_adj(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_spectral_adj<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr_set = true;
-  }
   k_spectral_adj<T><<<nblocks, 256, smem, s>>>(L);
   return cudaGetLastError();
 }
 template cudaError_t launch_spec_adj<double>(const SpecLaunch<double>&, int, size_t, cudaStream_t);
 template cudaError_t launch_spec_adj<float>(const SpecLaunch<float>&, int, size_t, cudaStream_t);
 
+void spec_set_attributes() {
+  cudaFuncSetAttribute(k_spectral<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_spectral<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_spectral_adj<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_spectral_adj<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
+
 template <typename T>
 cudaError_t launch_spec(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_spectral<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr_set = true;
-  }
   k_spectral<T><<<nblocks, 256, smem, s>>>(L);
   return cudaGetLastError();
 }

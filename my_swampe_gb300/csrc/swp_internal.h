@@ -66,7 +66,8 @@ template <typename T>
 struct SpecGroup {
   Geom<T> g;
   int B, MT, ntb;                       // members, members per tile, tiles along b
-  typename cplx<T>::type* four;         // [NFOURIER][M+1][B][J]
+  typename cplx<T>::type* four;         // [NFOURIER][M+1][B][J] state read by the step
+  typename cplx<T>::type* four_out;     // state written by the step (== four for in place)
   const double* par;                    // [NPAR][B]
   double* member;                       // [NMEMBER][B]
   double* diag;                         // [steps+1][NDIAG][B] or null
@@ -130,5 +131,7 @@ template <typename T> size_t grid_smem_bytes(int M, int J, int I, int JB, int mo
 template <typename T> cudaError_t launch_spec(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s);
 template <typename T> cudaError_t launch_spec_adj(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s);
 template <typename T> cudaError_t launch_grid(const GridLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s);
+void spec_set_attributes();
+void grid_set_attributes();
 
 }  // namespace swp

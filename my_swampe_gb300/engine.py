@@ -242,3 +242,28 @@ class Engine:
                                               _lib.ptr_array([o.data_ptr() for o in outs]), ctypes.byref(flags.c()),
                                               self.stream), "adjoint_init")
         return outs
+
+    def forward_checkpointed(self, flags: RunFlagsC, t0: int, nsteps: int, ckpt_every: int, ckpt) -> None:
+        """ckpt[g]: (nwin, NFOURIER, M+1, B, J) buffer receiving the window-start states."""
+        self._check(self.lib.swp_forward_checkpointed(self._plan, self._states(), ctypes.byref(flags.c()), int(t0),
+                                                      int(nsteps), int(ckpt_every),
+                                                      _lib.ptr_array([c.data_ptr() for c in ckpt]), self.stream),
+                    "forward_checkpointed")
+
+    def adjoint_window(self, flags: RunFlagsC, ckpt_state, slots, lam, lamy, grad, t0: int, nsteps: int) -> None:
+        """ckpt_state[g]: Fourier state at t0; slots[g]: (nsteps+1, NFOURIER, M+1, B, J) scratch."""
+        self._check(self.lib.swp_adjoint_window(self._plan, self._states(fourier=ckpt_state),
+                                                _lib.ptr_array([x.data_ptr() for x in slots]),
+                                                self._adjs(lam, lamy, grad), ctypes.byref(flags.c()), int(t0),
+                                                int(nsteps), self.stream), "adjoint_window")
+
+    def time_kernels(self, flags: RunFlagsC, nrep: int = 20, adjoint: bool = True, fourier=None):
+        """Average ms per launch (CUDA events, library stream) of the spectral, grid,
+        grid-adjoint and spectral-adjoint kernels on a scratch copy of the state."""
+        scratch = [gd["fourier"].clone() for gd in self.groups] if fourier is None else fourier
+        lam, lamy, grad = self.new_adjoint_buffers() if adjoint else (None, None, None)
+        ms = (ctypes.c_float * 4)()
+        adjs = self._adjs(lam, lamy, grad) if adjoint else None
+        self._check(self.lib.swp_time_kernels(self._plan, self._states(fourier=scratch), adjs,
+                                              ctypes.byref(flags.c()), int(nrep), ms, self.stream), "time_kernels")
+        return dict(spectral=ms[0], grid=ms[1], grid_adj=ms[2], spectral_adj=ms[3])
