@@ -395,6 +395,28 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile(args):
+    """One checkpoint window of the bench workload, sized for ncu: init, K forward
+    steps (checkpointed), then the window adjoint (K recompute steps + K adjoint
+    steps) -- the same kernel mix per model step as the timed bench."""
+    import torch
+
+    torch.cuda.set_device(0)
+    from __graft_entry__ import build
+
+    build()
+    from my_swampe_gb300.adjoint import Integration
+
+    eng, wl, flags, _, ics = _setup(args.profile, args.B)
+    integ = Integration(eng, flags, t0=2, nsteps=CKPT, ckpt_every=CKPT)
+    out = integ.run_forward([ics])[0]
+    d = torch.zeros_like(out)
+    d[2] = out[2] / out[2].numel()
+    integ.run_backward([d])
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.profile, "B": args.B, "steps": CKPT, "ok": True}))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -408,7 +430,12 @@ def main():
     ap.add_argument("--cpu-members", type=int, default=1)
     ap.add_argument("--cpu-nsteps", type=int, default=40)
     ap.add_argument("--ref-nsteps", type=int, default=20)
+    ap.add_argument("--profile", choices=("fast", "fp64"), default=None,
+                    help="run one checkpoint window of the workload (for ncu) instead of timing")
     args = ap.parse_args()
+    if args.profile:
+        run_profile(args)
+        return
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
