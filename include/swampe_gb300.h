@@ -49,6 +49,8 @@ extern "C" {
 #define SWP_NFOURIER 19
 #define SWP_NPAR 10
 #define SWP_MAX_GROUPS 4
+/* Size of the fixed device scratch used by swp_adjoint_step_noalloc (16 MiB). */
+#define SWP_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
 
 typedef struct swp_plan swp_plan;
 
@@ -167,6 +169,23 @@ int swp_adjoint_window(swp_plan* plan, const swp_group_state* st, void* const* s
  * Measurement hook for the roofline; no reference counterpart. */
 int swp_time_kernels(swp_plan* plan, const swp_group_state* st, const swp_group_adjoint* adj,
                      const swp_flags* flags, int nrep, float* ms_out, void* stream);
+
+/* Allocation-free swp_adjoint_step (no counterpart in the reference, which has
+ * no C interface): identical arguments and results, except that adj[g].lam_y
+ * is ignored and the step's scratch lives in a fixed device array of
+ * SWP_NOALLOC_SCRATCH_BYTES (16 MiB) that every device loading the library
+ * holds until exit.  For callers that cannot call cudaMalloc where they run
+ * the adjoint (inside another framework's custom call or callback that owns
+ * the allocator, hard-latency loops, embedded users of the C ABI).  Calls no
+ * cudaMalloc/cudaFree.  The plan must need at most that much scratch
+ * (5*(M+1)*B*J complex values per group, 256-byte aligned), else SWP_ERR_ARG.
+ * The first call on a device resolves the array's device address
+ * (cudaGetSymbolAddress) -- make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other streams,
+ * other plans, other threads) race on it.  Nothing in it needs to start at
+ * zero: each call overwrites the part it reads. */
+int swp_adjoint_step_noalloc(swp_plan* plan, const swp_group_state* st_in, const swp_group_state* st_out,
+                             const swp_group_adjoint* adj, const swp_flags* flags, void* stream);
 
 #ifdef __cplusplus
 }

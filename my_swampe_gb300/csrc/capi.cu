@@ -438,6 +438,21 @@ int forward_ckpt_impl(swp_plan* p, const swp_group_state* st, const swp_flags* f
 
 }  // namespace
 
+namespace swp {
+// Entry points for other translation units (static_scratch.cu).
+int adjoint_step_dispatch(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
+                          const swp_group_adjoint* adj, const swp_flags* f, cudaStream_t s) {
+  return p->precision == SWP_FP64 ? adjoint_step_impl<double>(p, st_in, st_out, adj, f, s)
+                                  : adjoint_step_impl<float>(p, st_in, st_out, adj, f, s);
+}
+int plan_groups(const swp_plan* p) { return p->ng; }
+size_t plan_lamy_bytes(const swp_plan* p, int g) {
+  size_t es = p->precision == SWP_FP64 ? 16 : 8;
+  return (size_t)5 * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
+}
+int plan_fail(swp_plan* p, int code, const char* msg) { return fail(p, code, msg); }
+}  // namespace swp
+
 extern "C" {
 
 int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_plan** out) {
