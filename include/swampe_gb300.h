@@ -80,6 +80,9 @@ typedef struct {
   int test;         /* 0 = forced (test=None), 1, 2                           */
   int diagnostics;  /* RMS blow-up gate and per-step diagnostics              */
   double blowup;    /* RunFlags.blowup_rms                                     */
+  int t_start;      /* time index of the initial state (the run's starttime); in the
+                       SWP_FAST precision the steps after the first one advance the
+                       band-limited state by increments (see swp_forward)       */
 } swp_flags;
 
 /* Create a plan for `ngroups` truncations (M[g] in {42, 63, 106}) with B[g]
@@ -111,7 +114,11 @@ int swp_diagnose_winds(swp_plan* plan, const swp_group_state* st, void* const* p
  * (the body of lax.scan over t_seq = arange(t0, t0 + nsteps), model.py:795-1194,
  * 1237-1342).  diag/hist rows are indexed from `row0`.  write_prev_last copies
  * the Fourier curr carry into the prev carry on the last step (always done for
- * the explicit scheme, which reads it). */
+ * the explicit scheme, which reads it).  SWP_FAST, modified Euler, t > t_start:
+ * the state is band-limited, so the step is evaluated as curr + Inv(dc) with
+ * dc = (sigma-1) Fwd(curr) + sigma (tendency) -- algebraically the reference's
+ * Inv(sigma Fwd(curr + ...)), but the FP32 transform error then scales with
+ * the increment instead of the field. */
 int swp_forward(swp_plan* plan, const swp_group_state* st, const swp_flags* flags,
                 int t0, int nsteps, int row0, int write_prev_last, void* stream);
 
@@ -185,7 +192,7 @@ int swp_time_kernels(swp_plan* plan, const swp_group_state* st, const swp_group_
  * other plans, other threads) race on it.  Nothing in it needs to start at
  * zero: each call overwrites the part it reads. */
 int swp_adjoint_step_noalloc(swp_plan* plan, const swp_group_state* st_in, const swp_group_state* st_out,
-                             const swp_group_adjoint* adj, const swp_flags* flags, void* stream);
+                             const swp_group_adjoint* adj, const swp_flags* flags, int t, void* stream);
 
 #ifdef __cplusplus
 }

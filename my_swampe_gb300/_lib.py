@@ -63,6 +63,7 @@ class Flags(ctypes.Structure):
         ("test", ctypes.c_int),
         ("diagnostics", ctypes.c_int),
         ("blowup", ctypes.c_double),
+        ("t_start", ctypes.c_int),
     ]
 
 
@@ -110,7 +111,7 @@ def load(path: os.PathLike | str | None = None) -> ctypes.CDLL:
         "swp_adjoint_window": (i, [vp, gsp, vpp, gap, fp, i, i, vp]),
         "swp_time_kernels": (i, [vp, gsp, gap, fp, i, ctypes.POINTER(ctypes.c_float), vp]),
         "swp_forward_checkpointed": (i, [vp, gsp, fp, i, i, i, vpp, vp]),
-        "swp_adjoint_step_noalloc": (i, [vp, gsp, gsp, gap, fp, vp]),
+        "swp_adjoint_step_noalloc": (i, [vp, gsp, gsp, gap, fp, i, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -38,7 +38,7 @@ class Integration:
             raise ValueError("nsteps must be >= 1 for a differentiable run")
         self.eng = engine
         self.flags = RunFlagsC(scheme=0, forcflag=flags.forcflag, diffflag=flags.diffflag, modalflag=flags.modalflag,
-                               test=flags.test, diagnostics=False)
+                               test=flags.test, diagnostics=False, t_start=int(t0))
         self.t0 = int(t0)
         self.nsteps = int(nsteps)
         self.K = max(1, min(int(ckpt_every), self.nsteps))

@@ -103,6 +103,10 @@ StepCfg make_cfg(const swp_flags* f) {
   return c;
 }
 
+bool step_incremental(const swp_plan* p, const swp_flags* f, int t) {
+  return p->precision == SWP_FAST && f->scheme == 0 && t > f->t_start;
+}
+
 // Launch nsteps steps.  In place on st[g].fourier, or -- when `slots` is given --
 // out of place: step k reads slot k and writes slot k+1 (slot stride `sstride`
 // complex elements), which keeps every intermediate state of a window.
@@ -121,6 +125,7 @@ int forward_steps(swp_plan* p, const swp_group_state* st, const swp_flags* f, in
     cfg.step = row0 + k;
     cfg.ra_mode = (f->modalflag && t > 2) ? 2 : 1;
     cfg.write_prev = (f->scheme == 1) || (write_prev_last && k == nsteps - 1);
+    cfg.incremental = step_incremental(p, f, t) ? 1 : 0;
     LS.cfg = cfg;
     LG.cfg = cfg;
     for (int g = 0; g < p->ng; ++g) {
@@ -188,6 +193,7 @@ void key_flags(std::vector<uint64_t>& k, const swp_flags* f) {
   uint64_t bu;
   memcpy(&bu, &f->blowup, 8);
   k.push_back(bu);
+  k.push_back((uint64_t)(int64_t)f->t_start);
 }
 
 void key_state(std::vector<uint64_t>& k, const swp_plan* p, const swp_group_state* st) {
@@ -251,7 +257,7 @@ int winds_impl(swp_plan* p, const swp_group_state* st, void* const* ed, void* co
 
 template <typename T>
 int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
-                      const swp_group_adjoint* adj, const swp_flags* f, cudaStream_t s) {
+                      const swp_group_adjoint* adj, const swp_flags* f, int t, cudaStream_t s) {
   int nbg = 0, nbs = 0;
   GridLaunch<T> LG = make_grid<T>(p, st_out, nbg);
   LG.mode = GM_ADJ_STEP;
@@ -268,6 +274,7 @@ int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group
   SpecLaunch<T> LS = make_spec<T>(p, st_in, nbs);
   LS.mode = 0;
   LS.cfg = make_cfg(f);
+  LS.cfg.incremental = step_incremental(p, f, t) ? 1 : 0;
   for (int g = 0; g < p->ng; ++g) {
     LS.grp[g].lam = (typename cplx<T>::type*)adj[g].lam;
     LS.grp[g].lamY = (const typename cplx<T>::type*)adj[g].lam_y;
@@ -335,14 +342,15 @@ int adjoint_window_impl(swp_plan* p, const swp_group_state* st, void* const* slo
         a[g].fourier = (char*)slots[g] + (size_t)k * ss;
         b[g].fourier = (char*)slots[g] + (size_t)(k + 1) * ss;
       }
-      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, cs);
+      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, t0 + k, cs);
       if (rc) return rc;
     }
     return SWP_OK;
   };
   // the window map does not depend on t0 except through the RA-filtered carry,
   // which the adjoint never reads, so one graph serves every window of a length
-  std::vector<uint64_t> key = {2, (uint64_t)nsteps};
+  // (whether the window starts at t_start decides the projected first step)
+  std::vector<uint64_t> key = {2, (uint64_t)nsteps, (uint64_t)(t0 == f->t_start)};
   key_flags(key, f);
   for (int g = 0; g < p->ng; ++g) {
     key.push_back((uint64_t)slots[g]); key.push_back((uint64_t)adj[g].lam); key.push_back((uint64_t)adj[g].lam_y);
@@ -441,9 +449,9 @@ int forward_ckpt_impl(swp_plan* p, const swp_group_state* st, const swp_flags* f
 namespace swp {
 // Entry points for other translation units (static_scratch.cu).
 int adjoint_step_dispatch(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
-                          const swp_group_adjoint* adj, const swp_flags* f, cudaStream_t s) {
-  return p->precision == SWP_FP64 ? adjoint_step_impl<double>(p, st_in, st_out, adj, f, s)
-                                  : adjoint_step_impl<float>(p, st_in, st_out, adj, f, s);
+                          const swp_group_adjoint* adj, const swp_flags* f, int t, cudaStream_t s) {
+  return p->precision == SWP_FP64 ? adjoint_step_impl<double>(p, st_in, st_out, adj, f, t, s)
+                                  : adjoint_step_impl<float>(p, st_in, st_out, adj, f, t, s);
 }
 int plan_groups(const swp_plan* p) { return p->ng; }
 size_t plan_lamy_bytes(const swp_plan* p, int g) {
@@ -593,7 +601,6 @@ int swp_state_copy(swp_plan* p, const swp_group_state* st, void* const* ckpt, in
 
 int swp_adjoint_step(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
                      const swp_group_adjoint* adj, const swp_flags* f, int t, void* stream) {
-  (void)t;  // the modified-Euler step map does not depend on t
   if (!p || !st_in || !st_out || !adj || !f) return fail(p, SWP_ERR_ARG, "null argument");
   if (f->scheme != 0) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint is implemented for the modified-Euler scheme");
   if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint of test=1 (fixed winds) is not implemented");
@@ -601,8 +608,8 @@ int swp_adjoint_step(swp_plan* p, const swp_group_state* st_in, const swp_group_
   for (int g = 0; g < p->ng; ++g)
     if (!adj[g].lam || !adj[g].lam_y || !st_in[g].fourier || !st_out[g].fourier) return fail(p, SWP_ERR_ARG, "missing adjoint buffer");
   cudaStream_t s = (cudaStream_t)stream;
-  return p->precision == SWP_FP64 ? adjoint_step_impl<double>(p, st_in, st_out, adj, f, s)
-                                  : adjoint_step_impl<float>(p, st_in, st_out, adj, f, s);
+  return p->precision == SWP_FP64 ? adjoint_step_impl<double>(p, st_in, st_out, adj, f, t, s)
+                                  : adjoint_step_impl<float>(p, st_in, st_out, adj, f, t, s);
 }
 
 int swp_adjoint_seed(swp_plan* p, const swp_group_state* st, const swp_group_adjoint* adj, void* const* dphys, void* stream) {

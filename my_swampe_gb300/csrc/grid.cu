@@ -188,7 +188,8 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
   T2* bufA = (T2*)smem_raw;
   T2* bufB = bufA + (size_t)ntrmax * L;
   T* sday = (T*)(bufB + (size_t)ntrmax * L);
-  double* sred = (double*)(sday + I);  // block reductions: [0]=rms2 [1]=spin [2]=phimin [3]=phimax
+  // block reductions [0]=rms2 [1]=spin [2]=phimin [3]=phimax (doubles: 16-byte aligned address)
+  double* sred = (double*)(((uintptr_t)(sday + I) + 15) & ~(uintptr_t)15);
   for (int i = threadIdx.x; i < I; i += blockDim.x) sday[i] = g.dayc[i];
   if (threadIdx.x == 0) { sred[0] = 0.0; sred[1] = 1e300; sred[2] = 1e300; sred[3] = -1e300; }
 

@@ -22,10 +22,14 @@
 
 namespace swp {
 
-// combined-input slots of the forward contraction
-enum SlotP { SP_PHI1 = 0, SP_PHI2, SP_D1, SP_D2, SP_E1, NSP };   // on Pw
-enum SlotH { SH_PHI1 = 0, SH_D1, SH_D2, SH_E1, NSH };            // on Hw
-constexpr int NSLOT = NSP + NSH;
+// combined-input slots of the forward contraction.  The FP32 path carries three
+// more P slots (the current eta, delta, Phi on their own) for the incremental
+// form of the step; the FP64 path keeps the reference's projection form.
+enum SlotP { SP_PHI1 = 0, SP_PHI2, SP_D1, SP_D2, SP_E1, SP_IPHI, SP_ID, SP_IE };  // on Pw
+enum SlotH { SH_PHI1 = 0, SH_D1, SH_D2, SH_E1, NSH };                            // on Hw
+template <typename T> struct SlotCount { static constexpr int NP = 5; static constexpr bool INCR = false; };
+template <> struct SlotCount<float> { static constexpr int NP = 8; static constexpr bool INCR = true; };
+constexpr int NSP = 5;
 constexpr int NKIN_P = 5;  // inverse inputs on P: eta, delta, Phi, Uprep, Vprep
 constexpr int NKIN_H = 2;  // inverse inputs on H: eta_s (U), -delta_s (V)
 constexpr int NKIN = NKIN_P + NKIN_H;
@@ -35,10 +39,10 @@ constexpr int INV_TJ = 2;  // latitudes per thread in the inverse contraction
 template <typename T>
 size_t spec_smem_bytes(int M, int J, int MT) {
   int Jh = J / 2, R = 2 * MT, cnt = M + 1;
-  size_t x = (size_t)NSLOT * 2 * Jh * R;            // symmetrised inputs (reused for outputs)
+  size_t x = (size_t)(SlotCount<T>::NP + NSH) * 2 * Jh * R;  // symmetrised inputs (reused for outputs)
   size_t bf = (size_t)2 * cnt * Jh;                  // two basis blocks
   size_t kin = (size_t)NKIN * cnt * R;               // inverse inputs
-  size_t coef = (size_t)3 * MT * cnt;                // sigma, sigmaPhi, a/(n(n+1))
+  size_t coef = (size_t)5 * MT * cnt;                // sigma, sigmaPhi, their -1's, a/(n(n+1))
   return (x + bf + kin + coef) * sizeof(T) + 64 * sizeof(int);
 }
 template size_t spec_smem_bytes<double>(int, int, int);
@@ -59,6 +63,8 @@ __device__ __forceinline__ T2 imul(T m, T2 z) { T2 r; r.x = -m * z.y; r.y = m * 
 template <typename T>
 __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLaunch<T> L) {
   typedef typename cplx<T>::type T2;
+  constexpr int NSPX = SlotCount<T>::NP;
+  constexpr int NSLOT = NSPX + NSH;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int idx;
   const SpecGroup<T>& G = pick_group(L, idx);
@@ -80,13 +86,16 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
   T* Kin = Bf + (size_t)2 * cntmax * Jh;                 // [NKIN][cnt][R]
   T* sig = Kin + (size_t)NKIN * cntmax * R;              // [MT][cnt]
   T* sigP = sig + MT * cntmax;
-  T* tcmn = sigP + MT * cntmax;
-  int* sdead = (int*)(tcmn + MT * cntmax);               // [MT]
+  T* sigm1 = sigP + MT * cntmax;                         // sigma - 1, formed without cancellation
+  T* sigPm1 = sigm1 + MT * cntmax;
+  T* tcmn = sigPm1 + MT * cntmax;
+  int* sdead = (int*)(((uintptr_t)(tcmn + MT * cntmax) + 15) & ~(uintptr_t)15);  // [MT]
+  const bool incr = SlotCount<T>::INCR && cfg.incremental && mode == 0 && cfg.scheme == 0;
 
   // ---- phase 0: per-member spectral coefficients and the blow-up gate
   for (int t = threadIdx.x; t < MT * cnt; t += blockDim.x) {
     int bt = t / cnt, k = t % cnt, n = m + k;
-    double s = 1.0, sp = 1.0, tc = 0.0;
+    double s = 1.0, sp = 1.0, sm1 = 0.0, spm1 = 0.0, tc = 0.0;
     if (bt < mt) {
       int b = b0 + bt;
       double a = G.par[P_A * G.B + b], dt = G.par[P_DT * G.B + b];
@@ -95,13 +104,18 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
         double nd = (double)n;
         double ncoeff = ((nd * nd * nd) / (a * a * a)) * (((nd + 1) * (nd + 1) * (nd + 1)) / (a * a * a));
         double a6 = a * a * a * a * a * a;
-        s = 1.0 / (1.0 + 2.0 * dt * K6 * (ncoeff - 8.0 / a6));
-        sp = 1.0 / (1.0 + 2.0 * dt * K6P * ncoeff);
+        double x = 2.0 * dt * K6 * (ncoeff - 8.0 / a6), xp = 2.0 * dt * K6P * ncoeff;
+        s = 1.0 / (1.0 + x);
+        sp = 1.0 / (1.0 + xp);
+        sm1 = -x / (1.0 + x);
+        spm1 = -xp / (1.0 + xp);
       }
       tc = (n == 0) ? 0.0 : a / ((double)n * (n + 1));
     }
     sig[bt * cntmax + k] = (T)s;
     sigP[bt * cntmax + k] = (T)sp;
+    sigm1[bt * cntmax + k] = (T)sm1;
+    sigPm1[bt * cntmax + k] = (T)spm1;
     tcmn[bt * cntmax + k] = (T)tc;
   }
   if (threadIdx.x < MT) {
@@ -149,27 +163,28 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
           T hPb = (T)(Pb * 0.5);
           T2 Bf = cadd(Bm, Fm), Af = csub(A, Gm);
           T2 Beff = cfg.forcflag ? Bf : Bm, Aeff = cfg.forcflag ? Af : A;
-          // Phi (modEuler_tdiff.py:80-110)
-          T2 p1 = csub(phi, cscale(imul(xm, C), t1));
+          // Phi (modEuler_tdiff.py:80-110); incremental form: curr goes to its own slot
+          T2 p1 = incr ? cscale(imul(xm, C), -t1) : csub(phi, cscale(imul(xm, C), t1));
           p1 = csub(p1, cscale(del, (T)(dt * Pb)));
           p1 = csub(p1, cscale(imul(xm, Beff), hPb * t1));
           if (cfg.forcflag) p1 = cadd(p1, cscale(PF, (T)dt));
           c[SP_PHI1] = p1;
-          c[NSP + SH_PHI1] = csub(cscale(D, t1), cscale(Aeff, hPb * t1));
+          c[NSPX + SH_PHI1] = csub(cscale(D, t1), cscale(Aeff, hPb * t1));
           c[SP_PHI2] = cscale(cadd(cscale(E, t2), cscale(phi, ia2)), -hPb);
           // delta (modEuler_tdiff.py:162-201)
-          c[SP_D1] = cadd(del, cscale(imul(xm, Bf), t1));
-          c[NSP + SH_D1] = cscale(Af, t1);
+          c[SP_D1] = incr ? cscale(imul(xm, Bf), t1) : cadd(del, cscale(imul(xm, Bf), t1));
+          c[NSPX + SH_D1] = cscale(Af, t1);
           T2 d2 = cadd(cscale(phi, t2), cscale(E, t2));
           d2 = cadd(d2, cscale(imul(xm, C), t1 * (T)0.5 * ia2));
           d2 = csub(d2, cscale(del, (T)(Pb / (a * a))));
           if (cfg.forcflag) d2 = cadd(d2, cscale(PF, (T)((dt / 2.0) / (a * a))));
           c[SP_D2] = d2;
-          c[NSP + SH_D2] = cscale(D, t1 * (T)0.5 * ia2);
+          c[NSPX + SH_D2] = cscale(D, t1 * (T)0.5 * ia2);
           // eta (modEuler_tdiff.py:253-261)
           T te = cfg.forcflag ? (T)tsc : (T)(tsc / 2.0);
-          c[SP_E1] = csub(eta, cscale(imul(xm, Aeff), te));
-          c[NSP + SH_E1] = cscale(Beff, te);
+          c[SP_E1] = incr ? cscale(imul(xm, Aeff), -te) : csub(eta, cscale(imul(xm, Aeff), te));
+          c[NSPX + SH_E1] = cscale(Beff, te);
+          if (incr) { c[SP_IPHI] = phi; c[SP_ID] = del; c[SP_IE] = eta; }
         } else {
           T2 eta0 = F[F_ETA_PREV * FS + o], del0 = F[F_DELTA_PREV * FS + o], phi0 = F[F_PHI_PREV * FS + o];
           T2 del1 = F[F_DELTA * FS + o];
@@ -183,7 +198,7 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
           p1 = csub(p1, cscale(del1, (T)(2.0 * dt * Pb)));
           if (cfg.forcflag) p1 = cadd(p1, cscale(PF, (T)(2.0 * dt)));
           c[SP_PHI1] = p1;
-          c[NSP + SH_PHI1] = cscale(D, t);
+          c[NSPX + SH_PHI1] = cscale(D, t);
           // delta (explicit_tdiff.py:134-155)
           T2 d1 = del0, dh = mk<T2>(0, 0);
           if (cfg.forcflag) {
@@ -192,7 +207,7 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
             dh = csub(cscale(V, t * itd), cscale(Gm, t));
           }
           c[SP_D1] = d1;
-          c[NSP + SH_D1] = dh;
+          c[NSPX + SH_D1] = dh;
           // eta (explicit_tdiff.py:207-226)
           T2 e1 = csub(eta0, cscale(imul(xm, A), t));
           T2 eh = cscale(Bm, t);
@@ -203,7 +218,7 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
             eh = cadd(eh, cscale(Fm, t));
           }
           c[SP_E1] = e1;
-          c[NSP + SH_E1] = eh;
+          c[NSPX + SH_E1] = eh;
         }
         if (side == 0) {
 #pragma unroll
@@ -258,11 +273,11 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
 #pragma unroll
         for (int k = 0; k < FWD_TC; ++k) acc[q][k] = (T)0;
       for (int jp = 0; jp < Jh; ++jp) {
-        T xp[NSP], xh[NSH];
+        T xp[NSPX], xh[NSH];
 #pragma unroll
-        for (int q = 0; q < NSP; ++q) xp[q] = X[((size_t)q * 2 * Jh + sP * Jh + jp) * R + r];
+        for (int q = 0; q < NSPX; ++q) xp[q] = X[((size_t)q * 2 * Jh + sP * Jh + jp) * R + r];
 #pragma unroll
-        for (int q = 0; q < NSH; ++q) xh[q] = X[((size_t)(NSP + q) * 2 * Jh + sH * Jh + jp) * R + r];
+        for (int q = 0; q < NSH; ++q) xh[q] = X[((size_t)(NSPX + q) * 2 * Jh + sH * Jh + jp) * R + r];
         T vp[FWD_TC], vh[FWD_TC];
 #pragma unroll
         for (int k = 0; k < FWD_TC; ++k) {
@@ -273,9 +288,9 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
 #pragma unroll
         for (int k = 0; k < FWD_TC; ++k) {
 #pragma unroll
-          for (int q = 0; q < NSP; ++q) acc[q][k] = fma(xp[q], vp[k], acc[q][k]);
+          for (int q = 0; q < NSPX; ++q) acc[q][k] = fma(xp[q], vp[k], acc[q][k]);
 #pragma unroll
-          for (int q = 0; q < NSH; ++q) acc[NSP + q][k] = fma(xh[q], vh[k], acc[NSP + q][k]);
+          for (int q = 0; q < NSH; ++q) acc[NSPX + q][k] = fma(xh[q], vh[k], acc[NSPX + q][k]);
         }
       }
       const int bt = r >> 1, comp = r & 1;
@@ -288,15 +303,34 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
         int n = m + kk;
         T nn1 = (T)((double)n * (n + 1));
         T s = sig[bt * cntmax + kk], sp = sigP[bt * cntmax + kk], tc = tcmn[bt * cntmax + kk];
-        T cphi, cdel, ceta;
+        T cphi, cdel, ceta;      // spectral eta, delta (full, for the winds)
+        T kphi, kdel, keta;      // what the inverse transform turns into the new Fourier carries
         if (mode == 2) {
           ceta = acc[SP_E1][k];
           cdel = acc[SP_D1][k];
           cphi = (T)0;
+          kphi = cphi; kdel = cdel; keta = ceta;
         } else {
-          cphi = sp * (acc[SP_PHI1][k] + acc[NSP + SH_PHI1][k] + nn1 * acc[SP_PHI2][k]);
-          cdel = s * (acc[SP_D1][k] + acc[NSP + SH_D1][k] + nn1 * (acc[SP_D2][k] + acc[NSP + SH_D2][k]));
-          ceta = s * (acc[SP_E1][k] + acc[NSP + SH_E1][k]);
+          T sphi = acc[SP_PHI1][k] + acc[NSPX + SH_PHI1][k] + nn1 * acc[SP_PHI2][k];
+          T sdel = acc[SP_D1][k] + acc[NSPX + SH_D1][k] + nn1 * (acc[SP_D2][k] + acc[NSPX + SH_D2][k]);
+          T seta = acc[SP_E1][k] + acc[NSPX + SH_E1][k];
+          if (incr) {
+            // new = curr + Inv(dc), dc = (sigma - 1) Fwd(curr) + sigma * tendency
+            T iphi = acc[NSPX > SP_IPHI ? SP_IPHI : 0][k], idel = acc[NSPX > SP_ID ? SP_ID : 0][k];
+            T ieta = acc[NSPX > SP_IE ? SP_IE : 0][k];
+            T sm1 = sigm1[bt * cntmax + kk], spm1 = sigPm1[bt * cntmax + kk];
+            cdel = s * (idel + sdel);
+            ceta = s * (ieta + seta);
+            cphi = sp * (iphi + sphi);
+            kphi = spm1 * iphi + sp * sphi;
+            kdel = sm1 * idel + s * sdel;
+            keta = sm1 * ieta + s * seta;
+          } else {
+            cphi = sp * sphi;
+            cdel = s * sdel;
+            ceta = s * seta;
+            kphi = cphi; kdel = cdel; keta = ceta;
+          }
         }
         // wind inversion inputs (spectral_transform.py:577-594)
         T dp = (n == 0) ? (T)0 : cdel;
@@ -304,9 +338,9 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
         if (m == 0 && n == 1 && comp == 0) ep -= (T)(omega / sqrt(0.375));
         T es = ep * tc, ds = dp * tc;
         int pc = par ? C0 + c : c;
-        Kin[((size_t)0 * cntmax + pc) * R + r] = ceta;
-        Kin[((size_t)1 * cntmax + pc) * R + r] = cdel;
-        Kin[((size_t)2 * cntmax + pc) * R + r] = cphi;
+        Kin[((size_t)0 * cntmax + pc) * R + r] = keta;
+        Kin[((size_t)1 * cntmax + pc) * R + r] = kdel;
+        Kin[((size_t)2 * cntmax + pc) * R + r] = kphi;
         // Uprep = -i m delta_s ; Vprep = -i m eta_s  (write the other component)
         T xm = (T)m;
         if (comp == 0) {
@@ -419,8 +453,9 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
       T2 nw = get(q);
-      if (cfg.write_prev || cfg.ra_mode) {
+      if (incr || cfg.write_prev || cfg.ra_mode) {
         T2 old = Fi[cf[q] * FS + o];
+        if (incr) nw = cadd(old, nw);
         if (cfg.write_prev) Fo[pf[q] * FS + o] = old;
         if (cfg.ra_mode == 1) Fo[rf[q] * FS + o] = old;
         else if (cfg.ra_mode == 2) {
@@ -462,16 +497,21 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
 constexpr int NYS_P = 5;   // lambda eta, delta, Phi, U, V on P
 constexpr int NYS_H = 2;   // lambda U, V on H
 constexpr int NYS = NYS_P + NYS_H;
-constexpr int NKADJ = 5;   // coefficient vectors of the transposed forward contraction
+// coefficient vectors of the transposed forward contraction: 5, plus the three
+// identity slots of the incremental form on the FP32 path
+template <typename T> struct AdjCount { static constexpr int NK = SlotCount<T>::NP; };
 
 template <typename T>
 size_t spec_adj_smem_bytes(int M, int J, int MT) {
   int Jh = J / 2, R = 2 * MT, cnt = M + 1;
-  size_t x = (size_t)18 * J * MT;
+  constexpr int NK = AdjCount<T>::NK;
+  size_t x = (size_t)2 * (NK + 4) * J * MT;
+  size_t x2 = (size_t)NYS * 2 * Jh * R;
+  if (x2 > x) x = x2;
   size_t bf = (size_t)2 * cnt * Jh;
   size_t sres = (size_t)NYS * cnt * R;
-  size_t kad = (size_t)NKADJ * cnt * R;
-  size_t coef = (size_t)3 * MT * cnt;
+  size_t kad = (size_t)NK * cnt * R;
+  size_t coef = (size_t)5 * MT * cnt;
   return (x + bf + sres + kad + coef) * sizeof(T) + 64 * sizeof(double);
 }
 template size_t spec_adj_smem_bytes<double>(int, int, int);
@@ -480,10 +520,13 @@ template size_t spec_adj_smem_bytes<float>(int, int, int);
 template <typename T>
 __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ SpecLaunch<T> L) {
   typedef typename cplx<T>::type T2;
+  constexpr int NKADJ = AdjCount<T>::NK;
+  constexpr int NCAD = NKADJ + 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int idx;
   const SpecGroup<T>& G = pick_group(L, idx);
   const StepCfg& cfg = L.cfg;
+  const bool incr = SlotCount<T>::INCR && cfg.incremental;
   const Geom<T>& g = G.g;
   const int M = g.M, N = M, J = g.J, Jh = J / 2;
   const int m = idx / G.ntb;
@@ -495,18 +538,23 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
   const int cntmax = N + 1;
   const size_t FS = (size_t)(M + 1) * G.B * J;
 
-  T* X = (T*)smem_raw;                                  // [NYS][2][Jh][R], later [9][MT][J][2]
-  T* Bf = X + (size_t)18 * J * MT;                       // [2][cnt*Jh]
+  T* X = (T*)smem_raw;                                  // [NYS][2][Jh][R], later [NCAD][MT][J][2]
+  const size_t xsz = ((size_t)2 * NCAD * J * MT > (size_t)NYS * 2 * Jh * R) ? (size_t)2 * NCAD * J * MT
+                                                                            : (size_t)NYS * 2 * Jh * R;
+  T* Bf = X + xsz;                                       // [2][cnt*Jh]
   T* Sres = Bf + (size_t)2 * cntmax * Jh;                // [NYS][cnt][R]
   T* Kad = Sres + (size_t)NYS * cntmax * R;              // [NKADJ][cnt][R]
   T* sig = Kad + (size_t)NKADJ * cntmax * R;
   T* sigP = sig + MT * cntmax;
-  T* tcmn = sigP + MT * cntmax;
-  double* sgrad = (double*)(tcmn + MT * cntmax);         // [MT] Phibar gradient partials
+  T* sigm1 = sigP + MT * cntmax;
+  T* sigPm1 = sigm1 + MT * cntmax;
+  T* tcmn = sigPm1 + MT * cntmax;
+  // [MT] Phibar gradient partials: doubles, so round the address up to 16 bytes
+  double* sgrad = (double*)(((uintptr_t)(tcmn + MT * cntmax) + 15) & ~(uintptr_t)15);
 
   for (int t = threadIdx.x; t < MT * cnt; t += blockDim.x) {
     int bt = t / cnt, k = t % cnt, n = m + k;
-    double s = 1.0, sp = 1.0, tc = 0.0;
+    double s = 1.0, sp = 1.0, sm1 = 0.0, spm1 = 0.0, tc = 0.0;
     if (bt < mt) {
       int b = b0 + bt;
       double a = G.par[P_A * G.B + b], dt = G.par[P_DT * G.B + b];
@@ -515,13 +563,18 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
         double nd = (double)n;
         double ncoeff = ((nd * nd * nd) / (a * a * a)) * (((nd + 1) * (nd + 1) * (nd + 1)) / (a * a * a));
         double a6 = a * a * a * a * a * a;
-        s = 1.0 / (1.0 + 2.0 * dt * K6 * (ncoeff - 8.0 / a6));
-        sp = 1.0 / (1.0 + 2.0 * dt * K6P * ncoeff);
+        double x = 2.0 * dt * K6 * (ncoeff - 8.0 / a6), xp = 2.0 * dt * K6P * ncoeff;
+        s = 1.0 / (1.0 + x);
+        sp = 1.0 / (1.0 + xp);
+        sm1 = -x / (1.0 + x);
+        spm1 = -xp / (1.0 + xp);
       }
       tc = (n == 0) ? 0.0 : a / ((double)n * (n + 1));
     }
     sig[bt * cntmax + k] = (T)s;
     sigP[bt * cntmax + k] = (T)sp;
+    sigm1[bt * cntmax + k] = (T)sm1;
+    sigPm1[bt * cntmax + k] = (T)spm1;
     tcmn[bt * cntmax + k] = (T)tc;
   }
   if (threadIdx.x < MT) sgrad[threadIdx.x] = 0.0;
@@ -638,6 +691,17 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
     K(2, 0, s * lcd_r); K(2, 1, s * lcd_i);
     K(3, 0, nn1 * s * lcd_r); K(3, 1, nn1 * s * lcd_i);
     K(4, 0, s * lce_r); K(4, 1, s * lce_i);
+    if (NKADJ > 5) {
+      // identity slots of the incremental form: d/d Fwd(curr) of
+      //   dc_f = (sigma_f - 1) Fwd(curr_f) + ...  and of the full c_eta, c_delta used for the winds
+      T sm1 = sigm1[bt * cntmax + kk], spm1 = sigPm1[bt * cntmax + kk];
+      T ide_r = incr ? (s * w * les_r + sm1 * S(0, 0)) : (T)0, ide_i = incr ? (s * w * les_i + sm1 * S(0, 1)) : (T)0;
+      T idd_r = incr ? (s * w * lds_r + sm1 * S(1, 0)) : (T)0, idd_i = incr ? (s * w * lds_i + sm1 * S(1, 1)) : (T)0;
+      T idp_r = incr ? spm1 * S(2, 0) : (T)0, idp_i = incr ? spm1 * S(2, 1) : (T)0;
+      K(NKADJ > 5 ? 5 : 0, 0, idp_r); K(NKADJ > 5 ? 5 : 0, 1, idp_i);
+      K(NKADJ > 6 ? 6 : 0, 0, idd_r); K(NKADJ > 6 ? 6 : 0, 1, idd_i);
+      K(NKADJ > 7 ? 7 : 0, 0, ide_r); K(NKADJ > 7 ? 7 : 0, 1, ide_i);
+    }
   }
   __syncthreads();
   {
@@ -648,7 +712,7 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
   }
   __syncthreads();
   // ---- phase 4: transposed forward Legendre -> adjoints of the 9 combined inputs
-  T* Cad = X;  // [9][MT][J][2]
+  T* Cad = X;  // [NCAD][MT][J][2]
   {
     const int njt = (Jh + INV_TJ - 1) / INV_TJ;
     const int tasks = R * njt;
@@ -658,12 +722,12 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
     for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
       int r = task % R;
       int j0 = (task / R) * INV_TJ;
-      T E[9][INV_TJ], O[9][INV_TJ];
+      T E[NCAD][INV_TJ], O[NCAD][INV_TJ];
 #pragma unroll
-      for (int q = 0; q < 9; ++q)
+      for (int q = 0; q < NCAD; ++q)
 #pragma unroll
         for (int k = 0; k < INV_TJ; ++k) { E[q][k] = (T)0; O[q][k] = (T)0; }
-      auto accum = [&](T (&acc)[9][INV_TJ], int par, int c) {
+      auto accum = [&](T (&acc)[NCAD][INV_TJ], int par, int c) {
         int pc = par ? C0 + c : c;
         T kv[NKADJ];
 #pragma unroll
@@ -675,10 +739,10 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
           T h = jp < Jh ? BH[(par ? Jh * C0 : 0) + c * Jh + jp] : (T)0;
 #pragma unroll
           for (int q = 0; q < NKADJ; ++q) acc[q][k] = fma(kv[q], p, acc[q][k]);
-          acc[5][k] = fma(kv[0], h, acc[5][k]);
-          acc[6][k] = fma(kv[2], h, acc[6][k]);
-          acc[7][k] = fma(kv[3], h, acc[7][k]);
-          acc[8][k] = fma(kv[4], h, acc[8][k]);
+          acc[NKADJ + 0][k] = fma(kv[0], h, acc[NKADJ + 0][k]);
+          acc[NKADJ + 1][k] = fma(kv[2], h, acc[NKADJ + 1][k]);
+          acc[NKADJ + 2][k] = fma(kv[3], h, acc[NKADJ + 2][k]);
+          acc[NKADJ + 3][k] = fma(kv[4], h, acc[NKADJ + 3][k]);
         }
       };
       for (int c = 0; c < C0; ++c) accum(E, 0, c);
@@ -690,12 +754,12 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
         if (jp >= Jh) break;
         int jn = jp, js = J - 1 - jp;
 #pragma unroll
-        for (int q = 0; q < 5; ++q) {
+        for (int q = 0; q < NKADJ; ++q) {
           Cad[(((size_t)q * MT + bt) * J + jn) * 2 + comp] = E[q][k] + O[q][k];
           Cad[(((size_t)q * MT + bt) * J + js) * 2 + comp] = E[q][k] - O[q][k];
         }
 #pragma unroll
-        for (int q = 5; q < 9; ++q) {
+        for (int q = NKADJ; q < NCAD; ++q) {
           Cad[(((size_t)q * MT + bt) * J + jn) * 2 + comp] = E[q][k] + O[q][k];
           Cad[(((size_t)q * MT + bt) * J + js) * 2 + comp] = O[q][k] - E[q][k];
         }
@@ -712,9 +776,9 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
     int b = b0 + bt;
     size_t o = ((size_t)m * G.B + b) * J + j;
     auto ld = [&](int q) { return mk<T2>(Cad[(((size_t)q * MT + bt) * J + j) * 2], Cad[(((size_t)q * MT + bt) * J + j) * 2 + 1]); };
-    // slot order: 0 PhiP1, 1 PhiP2, 2 dP1, 3 dP2, 4 eP1, 5 PhiH1, 6 dH1, 7 dH2, 8 eH1
+    // slot order: 0 PhiP1, 1 PhiP2, 2 dP1, 3 dP2, 4 eP1, [identity Phi, delta, eta], PhiH1, dH1, dH2, eH1
     T2 lPhiP1 = ld(0), lPhiP2 = ld(1), ldP1 = ld(2), ldP2 = ld(3), leP1 = ld(4);
-    T2 lPhiH1 = ld(5), ldH1 = ld(6), ldH2 = ld(7), leH1 = ld(8);
+    T2 lPhiH1 = ld(NKADJ), ldH1 = ld(NKADJ + 1), ldH2 = ld(NKADJ + 2), leH1 = ld(NKADJ + 3);
     double dt = G.par[P_DT * G.B + b], a = G.par[P_A * G.B + b], Pb = G.par[P_PHIBAR * G.B + b];
     double tsc = (2.0 * dt) / (a * g.onemu2[j]);
     T t1 = (T)(tsc / 4.0), t2 = (T)((2.0 * dt / (a * a)) / 4.0);
@@ -725,9 +789,18 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
     T forc = cfg.forcflag ? (T)1 : (T)0;
     // conj(i*alpha*m) z = -i alpha m z
     auto mimul = [&](T alpha, T2 z) { return imul(-alpha * xm, z); };
-    T2 lphi = csub(cadd(lPhiP1, cscale(ldP2, t2)), cscale(lPhiP2, hPb * ia2));
-    T2 ldel = cadd(csub(ldP1, cscale(lPhiP1, (T)(dt * Pb))), cscale(ldP2, (T)(-Pb / (a * a))));
-    T2 leta = leP1;
+    // projection form: curr enters PhiP1, dP1, eP1 with coefficient 1; incremental
+    // form: through the identity slots and directly (new = curr + ...)
+    T2 idphi = lPhiP1, iddel = ldP1, ideta = leP1;
+    if (incr) {
+      size_t oy = o;  // lamY has the same (m, b, j) layout
+      idphi = cadd(ld(NKADJ > 5 ? 5 : 0), G.lamY[2 * FS + oy]);
+      iddel = cadd(ld(NKADJ > 6 ? 6 : 0), G.lamY[1 * FS + oy]);
+      ideta = cadd(ld(NKADJ > 7 ? 7 : 0), G.lamY[0 * FS + oy]);
+    }
+    T2 lphi = csub(cadd(idphi, cscale(ldP2, t2)), cscale(lPhiP2, hPb * ia2));
+    T2 ldel = cadd(csub(iddel, cscale(lPhiP1, (T)(dt * Pb))), cscale(ldP2, (T)(-Pb / (a * a))));
+    T2 leta = ideta;
     T2 lC = cadd(mimul(-t1, lPhiP1), mimul(t1 * (T)0.5 * ia2, ldP2));
     T2 lD = cadd(cscale(lPhiH1, t1), cscale(ldH2, t1 * (T)0.5 * ia2));
     T2 lE = cadd(cscale(lPhiP2, -hPb * t2), cscale(ldP2, t2));

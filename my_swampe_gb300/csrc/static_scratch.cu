@@ -16,7 +16,7 @@
 
 namespace swp {
 int adjoint_step_dispatch(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
-                          const swp_group_adjoint* adj, const swp_flags* f, cudaStream_t s);
+                          const swp_group_adjoint* adj, const swp_flags* f, int t, cudaStream_t s);
 int plan_groups(const swp_plan* p);
 size_t plan_lamy_bytes(const swp_plan* p, int g);
 int plan_fail(swp_plan* p, int code, const char* msg);
@@ -53,7 +53,7 @@ int scratch_address(void** out, std::string& err) {
 }  // namespace
 
 extern "C" int swp_adjoint_step_noalloc(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
-                                        const swp_group_adjoint* adj, const swp_flags* f, void* stream) {
+                                        const swp_group_adjoint* adj, const swp_flags* f, int t, void* stream) {
   using namespace swp;
   if (!p || !st_in || !st_out || !adj || !f) return plan_fail(p, SWP_ERR_ARG, "null argument");
   int ng = plan_groups(p);
@@ -78,5 +78,7 @@ extern "C" int swp_adjoint_step_noalloc(swp_plan* p, const swp_group_state* st_i
     a[g] = adj[g];
     a[g].lam_y = (char*)base + off[g];
   }
-  return adjoint_step_dispatch(p, st_in, st_out, a, f, (cudaStream_t)stream);
+  if (f->scheme != 0 || f->test == 1 || f->diagnostics)
+    return plan_fail(p, SWP_ERR_UNSUPPORTED, "adjoint: modified Euler, test != 1, diagnostics off");
+  return adjoint_step_dispatch(p, st_in, st_out, a, f, t, (cudaStream_t)stream);
 }

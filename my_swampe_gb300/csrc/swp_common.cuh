@@ -201,6 +201,7 @@ struct StepCfg {
   int diagnostics; // blow-up gate + reductions
   double blowup;   // RMS threshold
   int step;        // scan-step index (row of the diagnostic arrays)
+  int incremental; // advance a band-limited state by increments (FP32 path)
 };
 
 }  // namespace swp

@@ -40,11 +40,13 @@ class RunFlagsC:
     test: Optional[int] = None
     diagnostics: bool = False
     blowup_rms: float = 8000.0
+    t_start: int = 2
 
     def c(self) -> _lib.Flags:
         return _lib.Flags(
             int(self.scheme), int(bool(self.forcflag)), int(bool(self.diffflag)), int(bool(self.modalflag)),
             0 if self.test is None else int(self.test), int(bool(self.diagnostics)), float(self.blowup_rms),
+            int(self.t_start),
         )
 
 

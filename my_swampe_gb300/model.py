@@ -407,7 +407,7 @@ def run_model_scan(
         U0, V0 = eng.diagnose_winds([torch.stack((eta0, delta0), 0).to(eng.rdtype)])[0].to(torch.float64)
 
     flags = RunFlagsC(scheme=1 if expflag else 0, forcflag=forcflag, diffflag=diffflag, modalflag=modalflag,
-                      test=test, diagnostics=diagnostics, blowup_rms=8000.0)
+                      test=test, diagnostics=diagnostics, blowup_rms=8000.0, t_start=starttime_eff)
     T = tmax - starttime_eff
     diag = eng.new_diag(T) if diagnostics else None
     gd = eng.groups[0]

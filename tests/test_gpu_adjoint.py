@@ -117,3 +117,16 @@ def test_param_gradients_match_central_fd(cuda):
             out = eng.output_physical(flags)[0][:5]
             fd = float(((out[:, 0] - out[:, 1]) * Wt).sum()) / (2 * h)
             assert abs(pg[k] - fd) <= tol * abs(fd), (k, rel_h, pg[k], fd)
+
+
+def test_fast_adjoint_matches_fp64_adjoint(cuda):
+    """The FP32 adjoint (incremental steps after the first) against the FP64 one."""
+    params, ics, W = _case(seed=4)
+    l64, p64, ic64 = _gpu_grads(params, ics, W, 12, ckpt_every=5, precision="fp64")
+    l32, p32, ic32 = _gpu_grads(params, ics, W, 12, ckpt_every=5, precision="fast")
+    for k in p64:
+        assert abs(p32[k] - p64[k]) <= 2e-4 * abs(p64[k]), (k, p32[k], p64[k])
+    for f in range(5):
+        scale = np.max(np.abs(ic64[f]))
+        rel = np.linalg.norm(ic32[f] - ic64[f]) / max(np.linalg.norm(ic64[f]), 1e-300)
+        assert rel <= 2e-4, (f, rel)

@@ -178,3 +178,25 @@ def test_fast_precision_is_close(cuda):
         want = np.asarray(r[f + "_curr"])
         rel = np.linalg.norm(got - want) / np.linalg.norm(want)
         assert rel < 1e-5, (f, rel)
+
+
+def test_fast_precision_long_forced_run_error(cuda):
+    """FP32 path (incremental steps) against the FP64 GPU path over 400 steps of
+    the forced benchmark regime: relative L2 of Phi, eta, delta <= 5e-6."""
+    import torch
+    from my_swampe_gb300 import workloads
+    from my_swampe_gb300.engine import Engine, RunFlagsC
+
+    outs = {}
+    for prec in ("fp64", "fast"):
+        eng = Engine([(42, 4)], prec)
+        wl = workloads.forced_ensemble(eng, seed=77)
+        workloads.apply_params(eng, 0, wl["params"])
+        flags = RunFlagsC()
+        eng.init_state([wl["ics"]], flags)
+        eng.forward(flags, t0=2, nsteps=400)
+        outs[prec] = eng.output_physical(flags)[0].double()
+    for k, name in enumerate(("eta", "delta", "Phi")):
+        ref = outs["fp64"][k]
+        rel = float(torch.linalg.vector_norm(outs["fast"][k] - ref) / torch.linalg.vector_norm(ref))
+        assert rel < 5e-6, (name, rel)

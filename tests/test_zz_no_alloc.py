@@ -48,7 +48,7 @@ def test_noalloc_adjoint_step_matches_caller_scratch(cuda):
         adj_b[0].lam, adj_b[0].lam_y, adj_b[0].grad = lam_b.data_ptr(), None, grad_b.data_ptr()
         rc = lib.swp_adjoint_step(eng._plan, st_in, st_out, adj_a, ctypes.byref(fl), 4, eng.stream)
         assert rc == 0, lib.swp_last_error(eng._plan)
-        rc = lib.swp_adjoint_step_noalloc(eng._plan, st_in, st_out, adj_b, ctypes.byref(fl), eng.stream)
+        rc = lib.swp_adjoint_step_noalloc(eng._plan, st_in, st_out, adj_b, ctypes.byref(fl), 4, eng.stream)
         assert rc == 0, lib.swp_last_error(eng._plan)
         torch.cuda.synchronize()
         a, b = lam_a.cpu().numpy(), lam_b.cpu().numpy()
@@ -70,6 +70,6 @@ def test_noalloc_rejects_plans_beyond_the_scratch_size(cuda):
     adj = (_lib.GroupAdjoint * 1)()
     lam = eng.new_adjoint_buffers()[0][0]
     adj[0].lam = lam.data_ptr()
-    rc = lib.swp_adjoint_step_noalloc(eng._plan, st, st, adj, ctypes.byref(RunFlagsC().c()), eng.stream)
+    rc = lib.swp_adjoint_step_noalloc(eng._plan, st, st, adj, ctypes.byref(RunFlagsC().c()), 3, eng.stream)
     assert rc == _lib.SWP_OK + 1
     assert b"SWP_NOALLOC_SCRATCH_BYTES" in lib.swp_last_error(eng._plan)
