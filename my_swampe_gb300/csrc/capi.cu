@@ -489,10 +489,13 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
     int mt = 8;
     while (mt > 1 && (f64 ? spec_smem_bytes<double>(M[g], J, mt) : spec_smem_bytes<float>(M[g], J, mt)) > cap) mt /= 2;
     p->MT[g] = std::min(mt, B[g]);
-    int jb = 8;
-    size_t gcap = 100 * 1024;
+    // rows per grid CTA: 4 keeps several CTAs per SM resident; smaller when the
+    // largest mode (the adjoint, 12 transforms per row) would not fit
+    int jb = 4;
+    size_t gcap = 200 * 1024;
     while (jb > 1 && ((J % jb) != 0 ||
-                      (f64 ? grid_smem_bytes<double>(M[g], J, I, jb, GM_STEP) : grid_smem_bytes<float>(M[g], J, I, jb, GM_STEP)) > gcap))
+                      (f64 ? grid_smem_bytes<double>(M[g], J, I, jb, GM_ADJ_STEP)
+                           : grid_smem_bytes<float>(M[g], J, I, jb, GM_ADJ_STEP)) > gcap))
       jb /= 2;
     p->JB[g] = jb;
     size_t ss = f64 ? spec_smem_bytes<double>(M[g], J, p->MT[g]) : spec_smem_bytes<float>(M[g], J, p->MT[g]);

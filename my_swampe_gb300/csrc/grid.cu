@@ -1,5 +1,5 @@
-// K2: the per-latitude grid-space half of a time step, and its set-up and
-// output variants.  One CTA owns one ensemble member and a block of JB
+// K2: the per-latitude grid-space half of a time step, its set-up, output and
+// adjoint variants.  One CTA owns one ensemble member and a block of JB
 // latitude rows.  For each row it
 //   * turns truncated Fourier coefficients (m = 0..M) into I real grid values
 //     with a half-length complex FFT (the reference's ifft of a Hermitian-
@@ -10,7 +10,11 @@
 //     the run is forced, model.py:560-603),
 //   * and returns them to truncated Fourier space (fft(x/I)[:M+1],
 //     spectral_transform.py:309-328) with a half-length complex FFT.
-// Mixed-radix Stockham passes (radix 8/4/3/5) run in shared memory.
+// Mixed-radix Stockham passes (radix 8/4/3/5) run in shared memory on
+// transforms padded to L+1 entries (bank-conflict-free across a warp).
+// Fourier rows are staged through shared memory with the latitude index
+// fastest, so every global access is a contiguous JB-element run.
+// The kernel is specialised per mode at compile time.
 #include "swp_internal.h"
 #include <float.h>
 
@@ -20,24 +24,18 @@ template <typename T> __device__ __forceinline__ T tiny_val();
 template <> __device__ __forceinline__ double tiny_val<double>() { return DBL_MIN; }
 template <> __device__ __forceinline__ float tiny_val<float>() { return FLT_MIN; }
 
-// number of simultaneously held transforms per row for each mode
-__host__ __device__ inline int grid_ntr(int mode) {
-  switch (mode) {
-    case GM_STEP: return 8;
-    case GM_INIT: return 8;
-    case GM_OUTPUT: return 8;
-    case GM_WINDS: return 2;
-    case GM_ADJ_STEP: return 12;
-    default: return 8;
-  }
+// transforms per row held simultaneously in each mode
+__host__ __device__ constexpr int grid_ntr(int mode) {
+  return mode == GM_ADJ_STEP ? 12 : (mode == GM_WINDS || mode == GM_FWD2) ? 2 : 8;
 }
 
 template <typename T>
 size_t grid_smem_bytes(int M, int J, int I, int JB, int mode) {
-  int L = I / 2;
+  (void)M; (void)J;
+  int LS = I / 2 + 1;
   size_t ntr = (size_t)grid_ntr(mode) * JB;
-  size_t buf = ntr * L * sizeof(typename cplx<T>::type);
-  return 2 * buf + (size_t)I * sizeof(T) + 64 * sizeof(double);
+  size_t buf = ntr * LS * sizeof(typename cplx<T>::type);
+  return 2 * buf + (size_t)I * sizeof(T) + 16 + 8 * sizeof(double);
 }
 template size_t grid_smem_bytes<double>(int, int, int, int, int);
 template size_t grid_smem_bytes<float>(int, int, int, int, int);
@@ -50,8 +48,9 @@ __device__ __forceinline__ const GridGroup<T>& pick_ggroup(const GridLaunch<T>& 
   return L.grp[gi];
 }
 
-// Build the half-length spectrum Z (length L) of a C2R transform from the
-// truncated Fourier row y[0..M] (stride ys).  scale0/scale multiply Y_0 / Y_m.
+// Half-length spectrum Z_k (k < L) of the C2R transform
+//   x_i = Re(Y_0) + 2 Re sum_{m=1..M} Y_m e^{2 pi i m i / I},   x_{2n} + i x_{2n+1} = sum_k Z_k e^{2 pi i k n / L}
+// from the truncated row y[m * ys], m = 0..M.  scale0 / scale multiply Y_0 / Y_m.
 template <typename T2, typename T>
 __device__ __forceinline__ T2 c2r_pre(const T2* y, int ys, int M, int L, int k, const T2* twI, T scale0, T scale) {
   T2 hk = mk<T2>(0, 0), hl = mk<T2>(0, 0);
@@ -65,7 +64,8 @@ __device__ __forceinline__ T2 c2r_pre(const T2* y, int ys, int M, int L, int k, 
   return z;
 }
 
-// Unpack bin k (0..M) of a R2C transform from the half-length spectrum Z.
+// Bin k (0..M) of the R2C transform from the half-length spectrum Z (after the
+// forward FFT of x_{2n} + i x_{2n+1}), times `scale`.
 template <typename T2, typename T>
 __device__ __forceinline__ T2 r2c_post(const T2* Z, int L, int k, const T2* twI, T scale) {
   T2 zk = Z[k], zl = cconj(Z[(L - k) % L]);
@@ -100,7 +100,7 @@ template <typename T>
 struct Physics {
   T Pb, itr, itd, DPe;
   bool nodrag, forced;
-  __device__ void eval(T eta, T Phi, T U, T V, T ihalf, T day_s, T* out) const {
+  __device__ __forceinline__ void eval(T eta, T Phi, T U, T V, T ihalf, T day_s, T* out) const {
     // ABCDE_init (initial_conditions.py:499-503)
     out[0] = U * eta; out[1] = V * eta; out[2] = U * Phi; out[3] = V * Phi;
     out[4] = (U * U + V * V) * ihalf;
@@ -115,6 +115,8 @@ struct Physics {
       out[5] = Q;
       out[6] = nodrag ? Ru : Ru - U * itd;               // forcing.py:143-153
       out[7] = nodrag ? Rv : Rv - V * itd;
+    } else {
+      out[5] = out[6] = out[7] = (T)0;
     }
   }
 };
@@ -127,7 +129,8 @@ template <typename T>
 struct PhysicsAdj {
   T Pb, itr, itd, DPe;
   bool nodrag, forced;
-  __device__ void eval(T eta, T Phi, T U, T V, T ihalf, T day_s, const T* lz, T* lx, double* gacc) const {
+  __device__ __forceinline__ void eval(T eta, T Phi, T U, T V, T ihalf, T day_s, const T* lz, T* lx,
+                                       double* gacc) const {
     T lU = lz[0] * eta + lz[2] * Phi + lz[4] * (T)2 * U * ihalf;
     T lV = lz[1] * eta + lz[3] * Phi + lz[4] * (T)2 * V * ihalf;
     T leta = lz[0] * U + lz[1] * V;
@@ -158,9 +161,60 @@ struct PhysicsAdj {
   }
 };
 
+// Per-CTA context shared by the mode bodies.
+template <typename T>
+struct GridCtx {
+  typedef typename cplx<T>::type T2;
+  const GridGroup<T>* G;
+  int M, J, I, L, LS, JB, B, b, j0;
+  size_t FS, PS;
+  T2* bufA;
+  T2* bufB;
+  T* sday;
+  double* sred;
+  T invI;
+};
+
+// Stage the rows j0..j0+JB-1 of `nf` Fourier fields of member b into `stage`
+// ([f][m][r], r fastest; global reads are JB-long contiguous runs).
+template <typename T>
+__device__ __forceinline__ void stage_rows(const GridCtx<T>& c, const typename cplx<T>::type* const* src, int nf,
+                                           typename cplx<T>::type* stage) {
+  const int n1 = c.M + 1;
+  for (int t = threadIdx.x; t < nf * n1 * c.JB; t += blockDim.x) {
+    int r = t % c.JB, k = (t / c.JB) % n1, f = t / (c.JB * n1);
+    stage[t] = src[f][((size_t)k * c.B + c.b) * c.J + c.j0 + r];
+  }
+}
+
+// Z spectra of the C2R transforms of the staged rows: out[(f*JB + r)*LS + k].
+template <typename T>
+__device__ __forceinline__ void build_c2r(const GridCtx<T>& c, const typename cplx<T>::type* stage, int nf,
+                                          const T* scale0, const T* scale, typename cplx<T>::type* out) {
+  const int n1 = c.M + 1;
+  for (int t = threadIdx.x; t < nf * c.JB * c.L; t += blockDim.x) {
+    int k = t % c.L, fr = t / c.L, r = fr % c.JB, f = fr / c.JB;
+    out[(size_t)fr * c.LS + k] = c2r_pre<typename cplx<T>::type, T>(stage + (size_t)f * n1 * c.JB + r, c.JB, c.M, c.L, k,
+                                                                    c.G->g.twI, scale0[f], scale[f]);
+  }
+}
+
+// Truncated R2C bins of `nf` transforms in `res` (stride LS) written to global
+// Fourier fields dst[f] (r fastest).  Bin scale: k == 0 ? s0 : s.
+template <typename T>
+__device__ __forceinline__ void write_r2c(const GridCtx<T>& c, const typename cplx<T>::type* res, int nf,
+                                          typename cplx<T>::type* const* dst, T s0, T s) {
+  const int n1 = c.M + 1;
+  for (int t = threadIdx.x; t < nf * n1 * c.JB; t += blockDim.x) {
+    int r = t % c.JB, k = (t / c.JB) % n1, q = t / (c.JB * n1);
+    typename cplx<T>::type v = r2c_post<typename cplx<T>::type, T>(res + ((size_t)q * c.JB + r) * c.LS, c.L, k,
+                                                                     c.G->g.twI, k == 0 ? s0 : s);
+    dst[q][((size_t)k * c.B + c.b) * c.J + c.j0 + r] = v;
+  }
+}
+
 template <typename T>
 __device__ void block_add_grads(double* gacc, double* sred, double* grad, int B, int b) {
-  // sred[0..3] must be zero-initialised before the first __syncthreads of the kernel
   for (int q = 0; q < NGRAD; ++q) {
     double v = gacc[q];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -170,93 +224,131 @@ __device__ void block_add_grads(double* gacc, double* sred, double* grad, int B,
   if (threadIdx.x < NGRAD && grad) atomicAdd(&grad[threadIdx.x * B + b], sred[threadIdx.x]);
 }
 
-template <typename T>
+template <typename T, int MODE>
 __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch<T> Lc) {
   typedef typename cplx<T>::type T2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int idx;
   const GridGroup<T>& G = pick_ggroup(Lc, idx);
   const StepCfg& cfg = Lc.cfg;
-  const int mode = Lc.mode;
-  const Geom<T>& g = G.g;
-  const int M = g.M, J = g.J, I = g.I, L = g.L, JB = G.JB;
-  const int b = idx / G.njb;
-  const int j0 = (idx % G.njb) * JB;
-  const size_t FS = (size_t)(M + 1) * G.B * J;
-  const size_t PS = (size_t)G.B * J * I;  // physical field stride
-  const int ntrmax = grid_ntr(mode) * JB;
-  T2* bufA = (T2*)smem_raw;
-  T2* bufB = bufA + (size_t)ntrmax * L;
-  T* sday = (T*)(bufB + (size_t)ntrmax * L);
-  // block reductions [0]=rms2 [1]=spin [2]=phimin [3]=phimax (doubles: 16-byte aligned address)
-  double* sred = (double*)(((uintptr_t)(sday + I) + 15) & ~(uintptr_t)15);
-  for (int i = threadIdx.x; i < I; i += blockDim.x) sday[i] = g.dayc[i];
-  if (threadIdx.x == 0) { sred[0] = 0.0; sred[1] = 1e300; sred[2] = 1e300; sred[3] = -1e300; }
+  GridCtx<T> c;
+  c.G = &G;
+  c.M = G.g.M; c.J = G.g.J; c.I = G.g.I; c.L = G.g.L; c.LS = c.L + 1; c.JB = G.JB; c.B = G.B;
+  c.b = idx / G.njb;
+  c.j0 = (idx % G.njb) * c.JB;
+  c.FS = (size_t)(c.M + 1) * G.B * c.J;
+  c.PS = (size_t)G.B * c.J * c.I;
+  constexpr int NTR = grid_ntr(MODE);
+  c.bufA = (T2*)smem_raw;
+  c.bufB = c.bufA + (size_t)NTR * c.JB * c.LS;
+  c.sday = (T*)(c.bufB + (size_t)NTR * c.JB * c.LS);
+  c.sred = (double*)(((uintptr_t)(c.sday + c.I) + 15) & ~(uintptr_t)15);
+  c.invI = (T)(1.0 / c.I);
+  for (int i = threadIdx.x; i < c.I; i += blockDim.x) c.sday[i] = G.g.dayc[i];
+  if (threadIdx.x == 0) { c.sred[0] = 0.0; c.sred[1] = 1e300; c.sred[2] = 1e300; c.sred[3] = -1e300; }
 
-  const int B = G.B;
+  const int B = G.B, b = c.b, J = c.J, I = c.I, L = c.L, LS = c.LS, JB = c.JB, M = c.M, j0 = c.j0;
+  const size_t FS = c.FS, PS = c.PS;
+  const Geom<T>& g = G.g;
   double Pb = G.par[P_PHIBAR * B + b], tr = G.par[P_TAURAD * B + b];
   double td = G.par[P_TAUDRAG * B + b], DPe = G.par[P_DPHIEQ * B + b];
   Physics<T> ph;
   ph.Pb = (T)Pb; ph.itr = (T)(1.0 / tr); ph.itd = (T)(1.0 / td); ph.DPe = (T)DPe;
   ph.nodrag = (td == -1.0); ph.forced = (cfg.test == 0);
-  const T invI = (T)(1.0 / I);
-  const double wcur = G.member ? G.member[MS_WCURR * B + b] : 0.0;
-  const double wmid = G.member ? G.member[MS_WMID * B + b] : 0.0;
-  const bool dead = (cfg.diagnostics && G.member) ? (G.member[MS_DEAD * B + b] != 0.0) : false;
+  const T invI = c.invI;
+  T2* bufA = c.bufA;
+  T2* bufB = c.bufB;
 
-  if (mode == GM_STEP || mode == GM_OUTPUT || mode == GM_WINDS) {
+  if (MODE == GM_STEP || MODE == GM_OUTPUT || MODE == GM_WINDS) {
     // ------------------------------------------------ Fourier -> physical
+    const double wcur = G.member ? G.member[MS_WCURR * B + b] : 0.0;
+    const double wmid = G.member ? G.member[MS_WMID * B + b] : 0.0;
+    const bool dead = (cfg.diagnostics && G.member) ? (G.member[MS_DEAD * B + b] != 0.0) : false;
     int fl[8], nf = 0;
-    if (mode == GM_STEP) {
+    if (MODE == GM_STEP) {
       fl[nf++] = F_ETA; fl[nf++] = F_PHI; fl[nf++] = F_U; fl[nf++] = F_V;
       if (G.hist) fl[nf++] = F_DELTA;
       if (cfg.diagnostics) fl[nf++] = dead ? F_PHI : F_PHI_MID;
-    } else if (mode == GM_OUTPUT) {
+    } else if (MODE == GM_OUTPUT) {
       fl[nf++] = F_ETA; fl[nf++] = F_DELTA; fl[nf++] = F_PHI; fl[nf++] = F_U; fl[nf++] = F_V;
       fl[nf++] = F_ETA_MID; fl[nf++] = F_DELTA_MID; fl[nf++] = F_PHI_MID;
     } else {
       fl[nf++] = F_U; fl[nf++] = F_V;
     }
-    __syncthreads();
-    for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
-      int k = t % L, fr = t / L, r = fr % JB, f = fr / JB;
-      const T2* y = G.four + fl[f] * FS + (size_t)b * J + (j0 + r);
-      bufA[(size_t)fr * L + k] = c2r_pre<T2, T>(y, B * J, M, L, k, g.twI, (T)1, (T)1);
+    const T2* src[8];
+    T one[8];
+    double wv[8];
+    int rfv[8];
+#pragma unroll
+    for (int f = 0; f < 8; ++f) {
+      one[f] = (T)1;
+      wv[f] = 0.0;
+      rfv[f] = 0;
+      src[f] = nullptr;
+      if (f < nf) {
+        int fld = fl[f];
+        src[f] = G.four + fld * FS;
+        int rf = -1;
+        if (fld == F_ETA || fld == F_ETA_MID) rf = R_ETA;
+        else if (fld == F_DELTA || fld == F_DELTA_MID) rf = R_DELTA;
+        else if (fld == F_PHI || fld == F_PHI_MID) rf = R_PHI;
+        else if (fld == F_U) rf = R_U;
+        else if (fld == F_V) rf = R_V;
+        double w = (fld == F_ETA_MID || fld == F_DELTA_MID || fld == F_PHI_MID) ? wmid : wcur;
+        if ((fld == F_U || fld == F_V) && cfg.test == 1) w = 1.0;  // fixed initial winds (model.py:979-983)
+        if (rf >= 0 && G.resid && w != 0.0) { wv[f] = w; rfv[f] = rf; }
+      }
     }
     __syncthreads();
-    T2* zin = cfft_batch<+1>(bufA, bufB, L, nf * JB, g.twL);
+    stage_rows<T>(c, src, nf, bufB);
+    __syncthreads();
+    build_c2r<T>(c, bufB, nf, one, one, bufA);
+    __syncthreads();
+    T2* zin = cfft_batch<+1>(bufA, bufB, L, LS, nf * JB, g.twL);
     T2* zout = (zin == bufA) ? bufB : bufA;
-    // residual weights of the initial condition per loaded field
-    auto wres = [&](int f, int& rf) -> double {
-      rf = -1;
-      int fld = fl[f];
-      if (fld == F_ETA) rf = R_ETA; else if (fld == F_DELTA) rf = R_DELTA; else if (fld == F_PHI) rf = R_PHI;
-      else if (fld == F_U) rf = R_U; else if (fld == F_V) rf = R_V;
-      else if (fld == F_ETA_MID) rf = R_ETA; else if (fld == F_DELTA_MID) rf = R_DELTA; else if (fld == F_PHI_MID) rf = R_PHI;
-      if (rf < 0) return 0.0;
-      if ((fld == F_U || fld == F_V) && cfg.test == 1) return 1.0;  // fixed initial winds (model.py:979-983)
-      if (fld == F_ETA_MID || fld == F_DELTA_MID || fld == F_PHI_MID) return wmid;
-      return wcur;
-    };
-    double wv[8]; int rfv[8];
-    for (int f = 0; f < nf; ++f) wv[f] = wres(f, rfv[f]);
+    // initial-condition residual (non-zero only before a member's first step and
+    // for the fixed test-1 winds): added in shared memory, off the hot loop
+    bool need_resid = false;
+#pragma unroll
+    for (int f = 0; f < 8; ++f) need_resid |= (wv[f] != 0.0);
+    if (need_resid) {
+      for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
+        int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
+        double w = 0.0;
+        int rf = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (q == f) { w = wv[q]; rf = rfv[q]; }
+        if (w != 0.0) {
+          const T* rs = G.resid + rf * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
+          T2 z = zin[(size_t)fr * LS + n];
+          z.x += (T)w * rs[0];
+          z.y += (T)w * rs[1];
+          zin[(size_t)fr * LS + n] = z;
+        }
+      }
+      __syncthreads();
+    }
     double lrms = 0.0, lspin = 1e300, lmin = 1e300, lmax = -1e300;
     for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
       int n = t % L, r = t / L, j = j0 + r;
       T vals[8][2];
-      for (int f = 0; f < nf; ++f) {
-        T2 z = zin[((size_t)f * JB + r) * L + n];
-        vals[f][0] = z.x; vals[f][1] = z.y;
-        if (wv[f] != 0.0 && G.resid) {
-          const T* rs = G.resid + rfv[f] * PS + ((size_t)b * J + j) * I + 2 * n;
-          vals[f][0] += (T)wv[f] * rs[0];
-          vals[f][1] += (T)wv[f] * rs[1];
+#pragma unroll
+      for (int f = 0; f < 8; ++f) {
+        if (f < nf) {
+          T2 z = zin[((size_t)f * JB + r) * LS + n];
+          vals[f][0] = z.x; vals[f][1] = z.y;
+        } else {
+          vals[f][0] = vals[f][1] = (T)0;
         }
       }
-      if (mode == GM_OUTPUT || mode == GM_WINDS) {
-        for (int f = 0; f < nf; ++f) {
-          T* o = G.phys_out + f * PS + ((size_t)b * J + j) * I + 2 * n;
-          o[0] = vals[f][0]; o[1] = vals[f][1];
+      if (MODE == GM_OUTPUT || MODE == GM_WINDS) {
+#pragma unroll
+        for (int f = 0; f < 8; ++f) {
+          if (f < nf) {
+            T* o = G.phys_out + f * PS + ((size_t)b * J + j) * I + 2 * n;
+            o[0] = vals[f][0]; o[1] = vals[f][1];
+          }
         }
         continue;
       }
@@ -265,36 +357,37 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
       T s = (T)sqrt(g.onemu2[j]);
       T outs[2][8];
 #pragma unroll
-      for (int e = 0; e < 2; ++e) {
-        ph.eval(vals[0][e], vals[1][e], vals[2][e], vals[3][e], ihalf, sday[2 * n + e] * s, outs[e]);
-      }
-      int nout = ph.forced ? 8 : 5;
-      for (int q = 0; q < nout; ++q) zout[((size_t)q * JB + r) * L + n] = mk<T2>(outs[0][q], outs[1][q]);
+      for (int e = 0; e < 2; ++e)
+        ph.eval(vals[0][e], vals[1][e], vals[2][e], vals[3][e], ihalf, c.sday[2 * n + e] * s, outs[e]);
+      const int nout = ph.forced ? 8 : 5;
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < nout) zout[((size_t)q * JB + r) * LS + n] = mk<T2>(outs[0][q], outs[1][q]);
       if (G.hist) {
         // history layout [5][B][J][I]: eta, delta, Phi, U, V
-        const int hf[5] = {0, 4, 1, 2, 3};  // index into vals
-        for (int q = 0; q < 5; ++q) {
-          T* o = G.hist + q * PS + ((size_t)b * J + j) * I + 2 * n;
-          o[0] = vals[hf[q]][0]; o[1] = vals[hf[q]][1];
-        }
+        T* base = G.hist + ((size_t)b * J + j) * I + 2 * n;
+        base[0] = vals[0][0]; base[1] = vals[0][1];
+        base[PS] = vals[4][0]; base[PS + 1] = vals[4][1];
+        base[2 * PS] = vals[1][0]; base[2 * PS + 1] = vals[1][1];
+        base[3 * PS] = vals[2][0]; base[3 * PS + 1] = vals[2][1];
+        base[4 * PS] = vals[3][0]; base[4 * PS + 1] = vals[3][1];
       }
       if (cfg.diagnostics) {
-        int fp = G.hist ? 5 : 4;
         double aw = g.area[j];
+        int fp = G.hist ? 5 : 4;
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
           double U = vals[2][e], V = vals[3][e];
           lrms += aw * (U * U + V * V);
           lspin = fmin(lspin, sqrt(U * U + V * V));
-          double p = vals[fp][e];
+          double p = fp == 5 ? vals[5][e] : vals[4][e];
           lmin = fmin(lmin, p);
           lmax = fmax(lmax, p);
         }
       }
     }
-    if (mode == GM_OUTPUT || mode == GM_WINDS) return;
+    if (MODE == GM_OUTPUT || MODE == GM_WINDS) return;
     if (cfg.diagnostics) {
-      // warp reduce then one atomic per warp into smem, one per block to global
       for (int o = 16; o > 0; o >>= 1) {
         lrms += __shfl_down_sync(0xffffffffu, lrms, o);
         lspin = fmin(lspin, __shfl_down_sync(0xffffffffu, lspin, o));
@@ -302,56 +395,156 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
         lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));
       }
       if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&sred[0], lrms);
-        atomic_min_d(&sred[1], lspin);
-        atomic_min_d(&sred[2], lmin);
-        atomic_max_d(&sred[3], lmax);
+        atomicAdd(&c.sred[0], lrms);
+        atomic_min_d(&c.sred[1], lspin);
+        atomic_min_d(&c.sred[2], lmin);
+        atomic_max_d(&c.sred[3], lmax);
       }
     }
     __syncthreads();
     if (cfg.diagnostics && threadIdx.x == 0) {
       double* dn = G.diag + (size_t)(cfg.step + 1) * NDIAG * B;
       double* dc = G.diag + (size_t)cfg.step * NDIAG * B;
-      atomicAdd(&dn[D_RMS2 * B + b], sred[0]);
-      atomic_min_d(&dn[D_SPIN * B + b], sred[1]);
-      atomic_min_d(&dc[D_PHIMIN * B + b], sred[2]);
-      atomic_max_d(&dc[D_PHIMAX * B + b], sred[3]);
+      atomicAdd(&dn[D_RMS2 * B + b], c.sred[0]);
+      atomic_min_d(&dn[D_SPIN * B + b], c.sred[1]);
+      atomic_min_d(&dc[D_PHIMIN * B + b], c.sred[2]);
+      atomic_max_d(&dc[D_PHIMAX * B + b], c.sred[3]);
     }
-    int nout = ph.forced ? 8 : 5;
-    T2* res = cfft_batch<-1>(zout, zin, L, nout * JB, g.twL);
-    for (int t = threadIdx.x; t < nout * JB * (M + 1); t += blockDim.x) {
-      int r = t % JB, k = (t / JB) % (M + 1), q = t / (JB * (M + 1));
-      T2 v = r2c_post<T2, T>(res + ((size_t)q * JB + r) * L, L, k, g.twI, invI);
-      G.four[(F_A + q) * FS + ((size_t)k * B + b) * J + j0 + r] = v;
-    }
+    const int nout = ph.forced ? 8 : 5;
+    T2* res = cfft_batch<-1>(zout, zin, L, LS, nout * JB, g.twL);
+    T2* dst[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) dst[q] = G.four + (F_A + q) * FS;
+    write_r2c<T>(c, res, nout, dst, invI, invI);
     return;
   }
 
-  if (mode == GM_ADJ_STEP || mode == GM_ADJ_INIT) {
+  if (MODE == GM_FWD2) {
+    // ------------------------------------------------ physical eta, delta -> Fourier
+    __syncthreads();
+    for (int t = threadIdx.x; t < 2 * JB * L; t += blockDim.x) {
+      int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
+      const T* x = G.phys_in + f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
+      bufA[(size_t)fr * LS + n] = mk<T2>(x[0], x[1]);
+    }
+    __syncthreads();
+    T2* res = cfft_batch<-1>(bufA, bufB, L, LS, 2 * JB, g.twL);
+    T2* dst[2] = {G.four + F_ETA * FS, G.four + F_DELTA * FS};
+    write_r2c<T>(c, res, 2, dst, invI, invI);
+    return;
+  }
+
+  if (MODE == GM_INIT) {
+    // ------------------------------------------------ physical ICs -> state
+    // round 1: eta, delta, Phi, U, V -> Fourier curr (+prev, RA carry) and residuals
+    __syncthreads();
+    const int nf = 5;
+    for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
+      int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
+      const T* x = G.phys_in + f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
+      bufA[(size_t)fr * LS + n] = mk<T2>(x[0], x[1]);
+    }
+    __syncthreads();
+    T2* res = cfft_batch<-1>(bufA, bufB, L, LS, nf * JB, g.twL);
+    T2* other = (res == bufA) ? bufB : bufA;
+    const int n1 = M + 1;
+    // unpack into global and keep the truncated rows in `other` ([f][m][r])
+    for (int t = threadIdx.x; t < nf * n1 * JB; t += blockDim.x) {
+      int r = t % JB, k = (t / JB) % n1, f = t / (JB * n1);
+      T2 v = r2c_post<T2, T>(res + ((size_t)f * JB + r) * LS, L, k, g.twI, invI);
+      size_t o = ((size_t)k * B + b) * J + j0 + r;
+      const int sf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
+      G.four[sf[f] * FS + o] = v;
+      if (f < 3) {
+        G.four[(f == 0 ? F_ETA_PREV : f == 1 ? F_DELTA_PREV : F_PHI_PREV) * FS + o] = v;
+        G.four[(f == 0 ? F_ETA_MID : f == 1 ? F_DELTA_MID : F_PHI_MID) * FS + o] = v;
+      }
+      other[t] = v;
+    }
+    __syncthreads();
+    // band-limited reconstruction -> residual = x - C2R(trunc FFT(x))
+    T one[5] = {(T)1, (T)1, (T)1, (T)1, (T)1};
+    build_c2r<T>(c, other, nf, one, one, res);
+    __syncthreads();
+    T2* zr = cfft_batch<+1>(res, other, L, LS, nf * JB, g.twL);
+    for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
+      int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
+      size_t po = f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
+      const T* x = G.phys_in + po;
+      T2 z = zr[(size_t)fr * LS + n];
+      G.resid[po] = x[0] - z.x;
+      G.resid[po + 1] = x[1] - z.y;
+    }
+    __syncthreads();
+    // round 2: nonlinear terms and forcing from the raw initial grids (model.py:723-732)
+    double lrms = 0.0, lspin = 1e300;
+    const int nout = ph.forced ? 8 : 5;
+    for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
+      int n = t % L, r = t / L, j = j0 + r;
+      size_t po = ((size_t)b * J + j) * I + 2 * n;
+      T ihalf = (T)(1.0 / (2.0 * g.onemu2[j]));
+      T s = (T)sqrt(g.onemu2[j]);
+      T outs[2][8];
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        T eta = G.phys_in[0 * PS + po + e], Phi = G.phys_in[2 * PS + po + e];
+        T U = G.phys_in[3 * PS + po + e], V = G.phys_in[4 * PS + po + e];
+        ph.eval(eta, Phi, U, V, ihalf, c.sday[2 * n + e] * s, outs[e]);
+        if (cfg.diagnostics) {
+          double Ud = U, Vd = V;
+          lrms += g.area[j] * (Ud * Ud + Vd * Vd);
+          lspin = fmin(lspin, sqrt(Ud * Ud + Vd * Vd));
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < nout) bufA[((size_t)q * JB + r) * LS + n] = mk<T2>(outs[0][q], outs[1][q]);
+    }
+    if (cfg.diagnostics) {
+      for (int o = 16; o > 0; o >>= 1) {
+        lrms += __shfl_down_sync(0xffffffffu, lrms, o);
+        lspin = fmin(lspin, __shfl_down_sync(0xffffffffu, lspin, o));
+      }
+      if ((threadIdx.x & 31) == 0) { atomicAdd(&c.sred[0], lrms); atomic_min_d(&c.sred[1], lspin); }
+    }
+    __syncthreads();
+    if (cfg.diagnostics && threadIdx.x == 0) {
+      atomicAdd(&G.diag[D_RMS2 * B + b], c.sred[0]);
+      atomic_min_d(&G.diag[D_SPIN * B + b], c.sred[1]);
+    }
+    T2* res2 = cfft_batch<-1>(bufA, bufB, L, LS, nout * JB, g.twL);
+    T2* dst[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) dst[q] = G.four + (F_A + q) * FS;
+    write_r2c<T>(c, res2, nout, dst, invI, invI);
+    return;
+  }
+
+  if (MODE == GM_ADJ_STEP || MODE == GM_ADJ_INIT) {
     // ---------------------------------------------- adjoint of GM_STEP / GM_INIT
     PhysicsAdj<T> pa;
     pa.Pb = ph.Pb; pa.itr = ph.itr; pa.itd = ph.itd; pa.DPe = ph.DPe; pa.nodrag = ph.nodrag; pa.forced = ph.forced;
     const int nz = ph.forced ? 8 : 5;
-    const int npr = (mode == GM_ADJ_STEP) ? 4 : 0;  // primal fields transformed here (eta, Phi, U, V)
-    if (threadIdx.x < 4) sred[threadIdx.x] = 0.0;
-    __syncthreads();
-    // batch 1: lambda of the nonlinear Fourier terms -> grid (adjoint of fft(x/I)[:M+1]) and primal grid fields
+    const int npr = (MODE == GM_ADJ_STEP) ? 4 : 0;  // primal fields transformed here (eta, Phi, U, V)
+    if (threadIdx.x < 4) c.sred[threadIdx.x] = 0.0;
+    // batch 1: lambda of the nonlinear Fourier terms -> grid (adjoint of fft(x/I)[:M+1]:
+    // lambda x_i = (1/I) Re sum_{m=0..M} lambda_m e^{i theta}) and the primal grid fields
+    const T2* src[12];
+    T s0[12], s1[12];
     const int pf[4] = {F_ETA, F_PHI, F_U, F_V};
     const int nb1 = nz + npr;
-    for (int t = threadIdx.x; t < nb1 * JB * L; t += blockDim.x) {
-      int k = t % L, fr = t / L, r = fr % JB, f = fr / JB;
-      T2 z;
-      if (f < nz) {
-        const T2* y = G.lam + (F_A + f) * FS + (size_t)b * J + (j0 + r);
-        z = c2r_pre<T2, T>(y, B * J, M, L, k, g.twI, invI, invI * (T)0.5);
-      } else {
-        const T2* y = G.primal + pf[f - nz] * FS + (size_t)b * J + (j0 + r);
-        z = c2r_pre<T2, T>(y, B * J, M, L, k, g.twI, (T)1, (T)1);
-      }
-      bufA[(size_t)fr * L + k] = z;
+#pragma unroll
+    for (int f = 0; f < 12; ++f) {
+      if (f < nz) { src[f] = G.lam + (F_A + f) * FS; s0[f] = invI; s1[f] = invI * (T)0.5; }
+      else if (f < nb1) { src[f] = G.primal + pf[f - nz] * FS; s0[f] = (T)1; s1[f] = (T)1; }
+      else { src[f] = nullptr; s0[f] = s1[f] = (T)0; }
     }
     __syncthreads();
-    T2* zin = cfft_batch<+1>(bufA, bufB, L, nb1 * JB, g.twL);
+    stage_rows<T>(c, src, nb1, bufB);
+    __syncthreads();
+    build_c2r<T>(c, bufB, nb1, s0, s1, bufA);
+    __syncthreads();
+    T2* zin = cfft_batch<+1>(bufA, bufB, L, LS, nb1 * JB, g.twL);
     T2* zout = (zin == bufA) ? bufB : bufA;
     double gacc[NGRAD] = {0.0, 0.0, 0.0, 0.0};
     for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
@@ -362,25 +555,26 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
 #pragma unroll
       for (int e = 0; e < 2; ++e) {
         T lz[8];
+#pragma unroll
         for (int q = 0; q < 8; ++q) {
-          T2 v = q < nz ? zin[((size_t)q * JB + r) * L + n] : mk<T2>(0, 0);
+          T2 v = q < nz ? zin[((size_t)q * JB + r) * LS + n] : mk<T2>(0, 0);
           lz[q] = e ? v.y : v.x;
         }
         T eta, Phi, U, V;
-        if (mode == GM_ADJ_STEP) {
-          T2 a0 = zin[((size_t)(nz + 0) * JB + r) * L + n], a1 = zin[((size_t)(nz + 1) * JB + r) * L + n];
-          T2 a2 = zin[((size_t)(nz + 2) * JB + r) * L + n], a3 = zin[((size_t)(nz + 3) * JB + r) * L + n];
+        if (MODE == GM_ADJ_STEP) {
+          T2 a0 = zin[((size_t)(nz + 0) * JB + r) * LS + n], a1 = zin[((size_t)(nz + 1) * JB + r) * LS + n];
+          T2 a2 = zin[((size_t)(nz + 2) * JB + r) * LS + n], a3 = zin[((size_t)(nz + 3) * JB + r) * LS + n];
           eta = e ? a0.y : a0.x; Phi = e ? a1.y : a1.x; U = e ? a2.y : a2.x; V = e ? a3.y : a3.x;
         } else {
           size_t po = ((size_t)b * J + j) * I + 2 * n + e;
           eta = G.phys_in[0 * PS + po]; Phi = G.phys_in[2 * PS + po];
           U = G.phys_in[3 * PS + po]; V = G.phys_in[4 * PS + po];
         }
-        pa.eval(eta, Phi, U, V, ihalf, sday[2 * n + e] * s, lz, lx[e], gacc);
+        pa.eval(eta, Phi, U, V, ihalf, c.sday[2 * n + e] * s, lz, lx[e], gacc);
       }
-      if (mode == GM_ADJ_STEP) {
+      if (MODE == GM_ADJ_STEP) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) zout[((size_t)q * JB + r) * L + n] = mk<T2>(lx[0][q], lx[1][q]);
+        for (int q = 0; q < 4; ++q) zout[((size_t)q * JB + r) * LS + n] = mk<T2>(lx[0][q], lx[1][q]);
       } else {
         // adjoint of the initial grid fields from the nonlinear terms (eta, delta, Phi, U, V)
         size_t po = ((size_t)b * J + j) * I + 2 * n;
@@ -392,17 +586,18 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
         o[4 * PS + po] = lx[0][3]; o[4 * PS + po + 1] = lx[1][3];
       }
     }
-    block_add_grads<T>(gacc, sred, G.grad, B, b);
-    if (mode == GM_ADJ_STEP) {
+    block_add_grads<T>(gacc, c.sred, G.grad, B, b);
+    if (MODE == GM_ADJ_STEP) {
       // adjoint of x = Re(Y_0) + 2 Re sum_{m>=1} Y_m e^{i theta}:  lambda Y_m = c_m sum_i lambda x_i e^{-i theta}
-      T2* res = cfft_batch<-1>(zout, zin, L, 4 * JB, g.twL);
+      T2* res = cfft_batch<-1>(zout, zin, L, LS, 4 * JB, g.twL);
+      const int n1 = M + 1;
       const int yf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
       const int rmap[5] = {0, -1, 1, 2, 3};
-      for (int t = threadIdx.x; t < 5 * JB * (M + 1); t += blockDim.x) {
-        int r = t % JB, k = (t / JB) % (M + 1), q = t / (JB * (M + 1));
+      for (int t = threadIdx.x; t < 5 * n1 * JB; t += blockDim.x) {
+        int r = t % JB, k = (t / JB) % n1, q = t / (JB * n1);
         size_t o = ((size_t)k * B + b) * J + j0 + r;
         T2 v = G.lam[yf[q] * FS + o];
-        if (rmap[q] >= 0) v = cadd(v, r2c_post<T2, T>(res + ((size_t)rmap[q] * JB + r) * L, L, k, g.twI, k == 0 ? (T)1 : (T)2));
+        if (rmap[q] >= 0) v = cadd(v, r2c_post<T2, T>(res + ((size_t)rmap[q] * JB + r) * LS, L, k, g.twI, k == 0 ? (T)1 : (T)2));
         G.lamy[(size_t)q * FS + o] = v;
       }
       return;
@@ -410,158 +605,71 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
     // GM_ADJ_INIT batch 2: adjoint of the Fourier curr carries (fft(x/I)[:M+1]) of the ICs
     __syncthreads();
     const int cf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
-    for (int t = threadIdx.x; t < 5 * JB * L; t += blockDim.x) {
-      int k = t % L, fr = t / L, r = fr % JB, f = fr / JB;
-      const T2* y = G.lam + cf[f] * FS + (size_t)b * J + (j0 + r);
-      bufA[(size_t)fr * L + k] = c2r_pre<T2, T>(y, B * J, M, L, k, g.twI, invI, invI * (T)0.5);
-    }
+    const T2* src2[5];
+    T s20[5], s21[5];
+#pragma unroll
+    for (int f = 0; f < 5; ++f) { src2[f] = G.lam + cf[f] * FS; s20[f] = invI; s21[f] = invI * (T)0.5; }
+    stage_rows<T>(c, src2, 5, bufB);
     __syncthreads();
-    T2* z2 = cfft_batch<+1>(bufA, bufB, L, 5 * JB, g.twL);
+    build_c2r<T>(c, bufB, 5, s20, s21, bufA);
+    __syncthreads();
+    T2* z2 = cfft_batch<+1>(bufA, bufB, L, LS, 5 * JB, g.twL);
     for (int t = threadIdx.x; t < 5 * JB * L; t += blockDim.x) {
       int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
       size_t po = f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
-      T2 v = z2[(size_t)fr * L + n];
+      T2 v = z2[(size_t)fr * LS + n];
       G.phys_out[po] += v.x;
       G.phys_out[po + 1] += v.y;
     }
     return;
   }
 
-  if (mode == GM_ADJ_OUTPUT) {
+  if (MODE == GM_ADJ_OUTPUT) {
     // ---------------------------------------------- seed: lambda of physical curr fields -> Fourier
     __syncthreads();
     const int nf = 5;
     for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
       int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
       const T* x = G.phys_in + f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
-      bufA[(size_t)fr * L + n] = mk<T2>(x[0], x[1]);
+      bufA[(size_t)fr * LS + n] = mk<T2>(x[0], x[1]);
     }
     __syncthreads();
-    T2* res = cfft_batch<-1>(bufA, bufB, L, nf * JB, g.twL);
-    const int sf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
-    for (int t = threadIdx.x; t < nf * JB * (M + 1); t += blockDim.x) {
-      int r = t % JB, k = (t / JB) % (M + 1), f = t / (JB * (M + 1));
-      T2 v = r2c_post<T2, T>(res + ((size_t)f * JB + r) * L, L, k, g.twI, k == 0 ? (T)1 : (T)2);
-      G.lam[sf[f] * FS + ((size_t)k * B + b) * J + j0 + r] = v;
-    }
-    return;
-  }
-
-  if (mode == GM_FWD2) {
-    // ------------------------------------------------ physical eta, delta -> Fourier
-    __syncthreads();
-    const int nf = 2;
-    for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
-      int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
-      const T* x = G.phys_in + f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
-      bufA[(size_t)fr * L + n] = mk<T2>(x[0], x[1]);
-    }
-    __syncthreads();
-    T2* res = cfft_batch<-1>(bufA, bufB, L, nf * JB, g.twL);
-    for (int t = threadIdx.x; t < nf * JB * (M + 1); t += blockDim.x) {
-      int r = t % JB, k = (t / JB) % (M + 1), f = t / (JB * (M + 1));
-      T2 v = r2c_post<T2, T>(res + ((size_t)f * JB + r) * L, L, k, g.twI, invI);
-      G.four[(f == 0 ? F_ETA : F_DELTA) * FS + ((size_t)k * B + b) * J + j0 + r] = v;
-    }
-    return;
-  }
-
-  if (mode == GM_INIT) {
-    // ------------------------------------------------ physical ICs -> state
-    // round 1: eta, delta, Phi, U, V  -> Fourier curr (+prev, mid) and residuals
-    __syncthreads();
-    const int nf = 5;
-    for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
-      int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
-      const T* x = G.phys_in + f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
-      bufA[(size_t)fr * L + n] = mk<T2>(x[0], x[1]);
-    }
-    __syncthreads();
-    T2* res = cfft_batch<-1>(bufA, bufB, L, nf * JB, g.twL);
-    T2* other = (res == bufA) ? bufB : bufA;
-    const int sf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
-    // unpack into global and keep a copy of the truncated row in `other`
-    for (int t = threadIdx.x; t < nf * JB * (M + 1); t += blockDim.x) {
-      int r = t % JB, k = (t / JB) % (M + 1), f = t / (JB * (M + 1));
-      T2 v = r2c_post<T2, T>(res + ((size_t)f * JB + r) * L, L, k, g.twI, invI);
-      size_t o = ((size_t)k * B + b) * J + j0 + r;
-      G.four[sf[f] * FS + o] = v;
-      if (f < 3) {
-        G.four[(f == 0 ? F_ETA_PREV : f == 1 ? F_DELTA_PREV : F_PHI_PREV) * FS + o] = v;
-        G.four[(f == 0 ? F_ETA_MID : f == 1 ? F_DELTA_MID : F_PHI_MID) * FS + o] = v;
-      }
-      other[((size_t)f * JB + r) * (M + 1) + k] = v;
-    }
-    __syncthreads();
-    // band-limited reconstruction -> residual = x - C2R(trunc FFT(x))
-    for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
-      int k = t % L, fr = t / L;
-      res[(size_t)fr * L + k] = c2r_pre<T2, T>(other + (size_t)fr * (M + 1), 1, M, L, k, g.twI, (T)1, (T)1);
-    }
-    __syncthreads();
-    T2* zr = cfft_batch<+1>(res, other, L, nf * JB, g.twL);
-    for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
-      int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
-      size_t po = f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
-      const T* x = G.phys_in + po;
-      T2 z = zr[(size_t)fr * L + n];
-      G.resid[po] = x[0] - z.x;
-      G.resid[po + 1] = x[1] - z.y;
-    }
-    __syncthreads();
-    // round 2: nonlinear terms and forcing from the raw initial grids (model.py:723-732)
-    double lrms = 0.0, lspin = 1e300;
-    int nout = ph.forced ? 8 : 5;
-    for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
-      int n = t % L, r = t / L, j = j0 + r;
-      size_t po = ((size_t)b * J + j) * I + 2 * n;
-      T ihalf = (T)(1.0 / (2.0 * g.onemu2[j]));
-      T s = (T)sqrt(g.onemu2[j]);
-      T outs[2][8];
-#pragma unroll
-      for (int e = 0; e < 2; ++e) {
-        T eta = G.phys_in[0 * PS + po + e], Phi = G.phys_in[2 * PS + po + e];
-        T U = G.phys_in[3 * PS + po + e], V = G.phys_in[4 * PS + po + e];
-        ph.eval(eta, Phi, U, V, ihalf, sday[2 * n + e] * s, outs[e]);
-        if (cfg.diagnostics) {
-          double Ud = U, Vd = V;
-          lrms += g.area[j] * (Ud * Ud + Vd * Vd);
-          lspin = fmin(lspin, sqrt(Ud * Ud + Vd * Vd));
-        }
-      }
-      for (int q = 0; q < nout; ++q) bufA[((size_t)q * JB + r) * L + n] = mk<T2>(outs[0][q], outs[1][q]);
-    }
-    if (cfg.diagnostics) {
-      for (int o = 16; o > 0; o >>= 1) {
-        lrms += __shfl_down_sync(0xffffffffu, lrms, o);
-        lspin = fmin(lspin, __shfl_down_sync(0xffffffffu, lspin, o));
-      }
-      if ((threadIdx.x & 31) == 0) { atomicAdd(&sred[0], lrms); atomic_min_d(&sred[1], lspin); }
-    }
-    __syncthreads();
-    if (cfg.diagnostics && threadIdx.x == 0) {
-      double* d0 = G.diag;
-      atomicAdd(&d0[D_RMS2 * B + b], sred[0]);
-      atomic_min_d(&d0[D_SPIN * B + b], sred[1]);
-    }
-    T2* res2 = cfft_batch<-1>(bufA, bufB, L, nout * JB, g.twL);
-    for (int t = threadIdx.x; t < nout * JB * (M + 1); t += blockDim.x) {
-      int r = t % JB, k = (t / JB) % (M + 1), q = t / (JB * (M + 1));
-      T2 v = r2c_post<T2, T>(res2 + ((size_t)q * JB + r) * L, L, k, g.twI, invI);
-      G.four[(F_A + q) * FS + ((size_t)k * B + b) * J + j0 + r] = v;
-    }
+    T2* res = cfft_batch<-1>(bufA, bufB, L, LS, nf * JB, g.twL);
+    T2* dst[5] = {G.lam + F_ETA * FS, G.lam + F_DELTA * FS, G.lam + F_PHI * FS, G.lam + F_U * FS, G.lam + F_V * FS};
+    write_r2c<T>(c, res, nf, dst, (T)1, (T)2);
     return;
   }
 }
 
+template <typename T, int MODE>
+static void set_attr_one() {
+  cudaFuncSetAttribute(k_grid<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
+
 void grid_set_attributes() {
-  cudaFuncSetAttribute(k_grid<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_grid<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  set_attr_one<double, GM_STEP>(); set_attr_one<float, GM_STEP>();
+  set_attr_one<double, GM_INIT>(); set_attr_one<float, GM_INIT>();
+  set_attr_one<double, GM_OUTPUT>(); set_attr_one<float, GM_OUTPUT>();
+  set_attr_one<double, GM_WINDS>(); set_attr_one<float, GM_WINDS>();
+  set_attr_one<double, GM_ADJ_STEP>(); set_attr_one<float, GM_ADJ_STEP>();
+  set_attr_one<double, GM_ADJ_INIT>(); set_attr_one<float, GM_ADJ_INIT>();
+  set_attr_one<double, GM_ADJ_OUTPUT>(); set_attr_one<float, GM_ADJ_OUTPUT>();
+  set_attr_one<double, GM_FWD2>(); set_attr_one<float, GM_FWD2>();
 }
 
 template <typename T>
 cudaError_t launch_grid(const GridLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
-  k_grid<T><<<nblocks, 256, smem, s>>>(L);
+  switch (L.mode) {
+    case GM_STEP: k_grid<T, GM_STEP><<<nblocks, 256, smem, s>>>(L); break;
+    case GM_INIT: k_grid<T, GM_INIT><<<nblocks, 256, smem, s>>>(L); break;
+    case GM_OUTPUT: k_grid<T, GM_OUTPUT><<<nblocks, 256, smem, s>>>(L); break;
+    case GM_WINDS: k_grid<T, GM_WINDS><<<nblocks, 256, smem, s>>>(L); break;
+    case GM_ADJ_STEP: k_grid<T, GM_ADJ_STEP><<<nblocks, 256, smem, s>>>(L); break;
+    case GM_ADJ_INIT: k_grid<T, GM_ADJ_INIT><<<nblocks, 256, smem, s>>>(L); break;
+    case GM_ADJ_OUTPUT: k_grid<T, GM_ADJ_OUTPUT><<<nblocks, 256, smem, s>>>(L); break;
+    case GM_FWD2: k_grid<T, GM_FWD2><<<nblocks, 256, smem, s>>>(L); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 template cudaError_t launch_grid<double>(const GridLaunch<double>&, int, size_t, cudaStream_t);

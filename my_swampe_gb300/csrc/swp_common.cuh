@@ -116,25 +116,26 @@ template <int R, int SIGN, typename T2> __device__ __forceinline__ void dftR(T2*
   else dft8<SIGN>(v);
 }
 
-// One Stockham autosort pass (radix R) over `ntr` transforms of length L
-// stored contiguously (transform t at in + t*L).  tw[k] = exp(-2 pi i k / L).
+// One Stockham autosort pass (radix R) over `ntr` transforms of length L held
+// in shared memory with stride `ls` (transform t at in + t*ls; ls = L+1 keeps
+// the transforms of a warp on different banks).  tw[k] = exp(-2 pi i k / L).
 template <int R, int SIGN, typename T2>
 __device__ __forceinline__ void stockham_pass(const T2* __restrict__ in, T2* __restrict__ out,
-                                              int L, int ns, int ntr, const T2* __restrict__ tw) {
+                                              int L, int ls, int ns, int ntr, const T2* __restrict__ tw) {
   const int per = L / R;
   const int tasks = ntr * per;
   const int twstride = L / (ns * R);
   for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
     int t = task / per, j = task - t * per;
-    const T2* src = in + t * L;
-    T2* dst = out + t * L;
+    const T2* src = in + t * ls;
+    T2* dst = out + t * ls;
     int jm = j % ns;
     T2 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = src[j + r * per];
 #pragma unroll
     for (int r = 1; r < R; ++r) {
-      int k = (jm * r * twstride) % L;
+      int k = jm * r * twstride;  // < L
       T2 w = tw[k];
       v[r] = (SIGN < 0) ? cmul(v[r], w) : cmulc(v[r], w);
     }
@@ -145,23 +146,23 @@ __device__ __forceinline__ void stockham_pass(const T2* __restrict__ in, T2* __r
   }
 }
 
-// Complex FFT of `ntr` length-L transforms held in smem buffer a (b is scratch).
-// Returns the buffer holding the result.  L in {64, 96, 160}.
+// Complex FFT of `ntr` length-L transforms (stride ls) held in smem buffer a
+// (b is scratch).  Returns the buffer holding the result.  L in {64, 96, 160}.
 template <int SIGN, typename T2>
-__device__ T2* cfft_batch(T2* a, T2* b, int L, int ntr, const T2* tw) {
+__device__ T2* cfft_batch(T2* a, T2* b, int L, int ls, int ntr, const T2* tw) {
   if (L == 64) {
-    stockham_pass<8, SIGN>(a, b, L, 1, ntr, tw); __syncthreads();
-    stockham_pass<8, SIGN>(b, a, L, 8, ntr, tw); __syncthreads();
+    stockham_pass<8, SIGN>(a, b, L, ls, 1, ntr, tw); __syncthreads();
+    stockham_pass<8, SIGN>(b, a, L, ls, 8, ntr, tw); __syncthreads();
     return a;
   } else if (L == 96) {
-    stockham_pass<8, SIGN>(a, b, L, 1, ntr, tw); __syncthreads();
-    stockham_pass<4, SIGN>(b, a, L, 8, ntr, tw); __syncthreads();
-    stockham_pass<3, SIGN>(a, b, L, 32, ntr, tw); __syncthreads();
+    stockham_pass<8, SIGN>(a, b, L, ls, 1, ntr, tw); __syncthreads();
+    stockham_pass<4, SIGN>(b, a, L, ls, 8, ntr, tw); __syncthreads();
+    stockham_pass<3, SIGN>(a, b, L, ls, 32, ntr, tw); __syncthreads();
     return b;
   } else {  // 160
-    stockham_pass<8, SIGN>(a, b, L, 1, ntr, tw); __syncthreads();
-    stockham_pass<4, SIGN>(b, a, L, 8, ntr, tw); __syncthreads();
-    stockham_pass<5, SIGN>(a, b, L, 32, ntr, tw); __syncthreads();
+    stockham_pass<8, SIGN>(a, b, L, ls, 1, ntr, tw); __syncthreads();
+    stockham_pass<4, SIGN>(b, a, L, ls, 8, ntr, tw); __syncthreads();
+    stockham_pass<5, SIGN>(a, b, L, ls, 32, ntr, tw); __syncthreads();
     return b;
   }
 }
