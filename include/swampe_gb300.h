@@ -177,6 +177,14 @@ int swp_adjoint_window(swp_plan* plan, const swp_group_state* st, void* const* s
 int swp_time_kernels(swp_plan* plan, const swp_group_state* st, const swp_group_adjoint* adj,
                      const swp_flags* flags, int nrep, float* ms_out, void* stream);
 
+/* Self-check of the tensor-core building blocks (no reference counterpart):
+ * D[128, N] = A[128, K] . B[N, K]^T with tcgen05 kind::tf32 MMAs, FP32
+ * accumulation in TMEM, read back with tcgen05.ld; split3 = 1 uses the
+ * 3xTF32 split (hi*hi + hi*lo + lo*hi).  Device pointers, row-major FP32;
+ * N in 16..256 (multiple of 16), K in 8..128 (multiple of 8).  Synchronises
+ * the stream; SWP_ERR_NUMERIC if the MMA completion wait timed out. */
+int swp_tc_selftest(const float* A, const float* B, float* D, int N, int K, int split3, void* stream);
+
 /* Allocation-free swp_adjoint_step (no counterpart in the reference, which has
  * no C interface): identical arguments and results, except that adj[g].lam_y
  * is ignored and the step's scratch lives in a fixed device array of

@@ -72,6 +72,7 @@ EXPORTS = (
     "swp_init_state", "swp_diagnose_winds", "swp_forward", "swp_output_physical",
     "swp_state_copy", "swp_adjoint_step", "swp_adjoint_seed", "swp_adjoint_init",
     "swp_adjoint_window", "swp_time_kernels", "swp_forward_checkpointed", "swp_adjoint_step_noalloc",
+    "swp_tc_selftest",
 )
 
 _lib = None
@@ -112,6 +113,7 @@ def load(path: os.PathLike | str | None = None) -> ctypes.CDLL:
         "swp_time_kernels": (i, [vp, gsp, gap, fp, i, ctypes.POINTER(ctypes.c_float), vp]),
         "swp_forward_checkpointed": (i, [vp, gsp, fp, i, i, i, vpp, vp]),
         "swp_adjoint_step_noalloc": (i, [vp, gsp, gsp, gap, fp, i, vp]),
+        "swp_tc_selftest": (i, [vp, vp, vp, i, i, i, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
