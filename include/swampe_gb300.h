@@ -185,6 +185,17 @@ int swp_time_kernels(swp_plan* plan, const swp_group_state* st, const swp_group_
  * the stream; SWP_ERR_NUMERIC if the MMA completion wait timed out. */
 int swp_tc_selftest(const float* A, const float* B, float* D, int N, int K, int split3, void* stream);
 
+/* Device status word of the plan (no reference counterpart): *status = 1 if a
+ * bounded wait inside a tensor-core kernel ran out since the last call (the
+ * affected step results are then invalid), else 0.  Synchronises the stream
+ * and clears the word. */
+int swp_device_status(swp_plan* plan, int* status, void* stream);
+
+/* 1 if the plan's modified-Euler steps run the tcgen05 Legendre kernel (FP32
+ * plans whose groups are all M = 42, unless SWP_NO_TC=1 was set when the plan
+ * was created), else 0.  No reference counterpart. */
+int swp_plan_uses_tensor_cores(const swp_plan* plan);
+
 /* Allocation-free swp_adjoint_step (no counterpart in the reference, which has
  * no C interface): identical arguments and results, except that adj[g].lam_y
  * is ignored and the step's scratch lives in a fixed device array of

@@ -72,7 +72,7 @@ EXPORTS = (
     "swp_init_state", "swp_diagnose_winds", "swp_forward", "swp_output_physical",
     "swp_state_copy", "swp_adjoint_step", "swp_adjoint_seed", "swp_adjoint_init",
     "swp_adjoint_window", "swp_time_kernels", "swp_forward_checkpointed", "swp_adjoint_step_noalloc",
-    "swp_tc_selftest",
+    "swp_tc_selftest", "swp_device_status", "swp_plan_uses_tensor_cores",
 )
 
 _lib = None
@@ -114,6 +114,8 @@ def load(path: os.PathLike | str | None = None) -> ctypes.CDLL:
         "swp_forward_checkpointed": (i, [vp, gsp, fp, i, i, i, vpp, vp]),
         "swp_adjoint_step_noalloc": (i, [vp, gsp, gsp, gap, fp, i, vp]),
         "swp_tc_selftest": (i, [vp, vp, vp, i, i, i, vp]),
+        "swp_device_status": (i, [vp, ip, vp]),
+        "swp_plan_uses_tensor_cores": (i, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

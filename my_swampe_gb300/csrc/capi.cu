@@ -4,6 +4,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <type_traits>
 #include "swp_internal.h"
 
 using namespace swp;
@@ -26,6 +27,11 @@ struct swp_plan {
   size_t spec_smem = 0;
   size_t spec_adj_smem = 0;
   size_t grid_smem[8] = {};
+  // tensor-core Legendre kernel of the FP32 step (every group at M = 42)
+  bool use_tc = false;
+  float* tcbasis[MAXG] = {};
+  void* coefmem[MAXG] = {};              // per-call coefficient tables (CoefTables) of each group
+  int* d_err = nullptr;                  // device error word set by bounded waits that ran out
   std::string err;
 };
 
@@ -39,6 +45,25 @@ int fail(swp_plan* p, int code, const std::string& msg) {
 int cuda_check(swp_plan* p, cudaError_t e, const char* where) {
   if (e == cudaSuccess) return SWP_OK;
   return fail(p, SWP_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+CoefTables<T> plan_coefs(const swp_plan* p, int g) {
+  CoefTables<T> C;
+  C.carve((T*)p->coefmem[g], p->M[g], p->B[g], p->geom[g].J);
+  return C;
+}
+
+// Refresh the coefficient tables from the members' parameters: first launch of
+// every call that runs step kernels.
+template <typename T>
+int update_coefs(swp_plan* p, const swp_group_state* st, cudaStream_t s) {
+  for (int g = 0; g < p->ng; ++g) {
+    cudaError_t e = launch_coefs<T>(st[g].params, p->geom[g].onemu2, p->M[g], p->B[g], p->geom[g].J,
+                                    plan_coefs<T>(p, g), s);
+    if (e != cudaSuccess) return cuda_check(p, e, "coefficient kernel launch");
+  }
+  return SWP_OK;
 }
 
 template <typename T>
@@ -58,6 +83,10 @@ SpecLaunch<T> make_spec(const swp_plan* p, const swp_group_state* st, int& nbloc
     G.par = st[g].params;
     G.member = st[g].member;
     G.diag = st[g].diag;
+    CoefTables<T> C = plan_coefs<T>(p, g);
+    G.nco = C.nco;
+    G.jco = C.jco;
+    G.mco = C.mco;
     L.prefix[g] = acc;
     acc += (p->M[g] + 1) * G.ntb;
   }
@@ -107,6 +136,31 @@ bool step_incremental(const swp_plan* p, const swp_flags* f, int t) {
   return p->precision == SWP_FAST && f->scheme == 0 && t > f->t_start;
 }
 
+// The Legendre kernel of a modified-Euler step: tcgen05 (3xTF32) on the FP32
+// path when the plan packed the tensor-core basis, the SIMT kernel otherwise.
+template <typename T>
+cudaError_t launch_step_spec(const swp_plan* p, const SpecLaunch<T>& LS, int nbs, cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (p->use_tc && LS.mode == 0 && LS.cfg.scheme == 0) {
+      SpecLaunch<float> LT = LS;
+      const int mt = spec_tc_members_per_cta();
+      int acc = 0;
+      TcBasis tb;
+      memset(&tb, 0, sizeof(tb));
+      for (int g = 0; g < p->ng; ++g) {
+        LT.grp[g].MT = mt;
+        LT.grp[g].ntb = (p->B[g] + mt - 1) / mt;
+        LT.prefix[g] = acc;
+        acc += (p->M[g] + 1) * LT.grp[g].ntb;
+        tb.p[g] = p->tcbasis[g];
+      }
+      LT.prefix[p->ng] = acc;
+      return launch_spec_tc(LT, acc, tb, p->d_err, s);
+    }
+  }
+  return launch_spec<T>(LS, nbs, p->spec_smem, s);
+}
+
 // Launch nsteps steps.  In place on st[g].fourier, or -- when `slots` is given --
 // out of place: step k reads slot k and writes slot k+1 (slot stride `sstride`
 // complex elements), which keeps every intermediate state of a window.
@@ -120,6 +174,10 @@ int forward_steps(swp_plan* p, const swp_group_state* st, const swp_flags* f, in
   LS.mode = 0;
   LG.mode = GM_STEP;
   StepCfg cfg = make_cfg(f);
+  if (nsteps > 0) {
+    int rc = update_coefs<T>(p, st, s);
+    if (rc) return rc;
+  }
   for (int k = 0; k < nsteps; ++k) {
     int t = t0 + k;
     cfg.step = row0 + k;
@@ -138,7 +196,7 @@ int forward_steps(swp_plan* p, const swp_group_state* st, const swp_flags* f, in
         LG.grp[g].four = LS.grp[g].four_out;
       }
     }
-    cudaError_t e = launch_spec<T>(LS, nbs, p->spec_smem, s);
+    cudaError_t e = launch_step_spec<T>(p, LS, nbs, s);
     if (e != cudaSuccess) return cuda_check(p, e, "spectral kernel launch");
     e = launch_grid<T>(LG, nbg, p->grid_smem[GM_STEP], s);
     if (e != cudaSuccess) return cuda_check(p, e, "grid kernel launch");
@@ -245,6 +303,8 @@ int winds_impl(swp_plan* p, const swp_group_state* st, void* const* ed, void* co
   for (int g = 0; g < p->ng; ++g) LG.grp[g].phys_in = (const T*)ed[g];
   cudaError_t e = launch_grid<T>(LG, nbg, p->grid_smem[GM_FWD2], s);
   if (e != cudaSuccess) return cuda_check(p, e, "winds forward transform");
+  int rc = update_coefs<T>(p, st, s);
+  if (rc) return rc;
   SpecLaunch<T> LS = make_spec<T>(p, st, nbs);
   LS.mode = 2;
   e = launch_spec<T>(LS, nbs, p->spec_smem, s);
@@ -257,8 +317,13 @@ int winds_impl(swp_plan* p, const swp_group_state* st, void* const* ed, void* co
 
 template <typename T>
 int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
-                      const swp_group_adjoint* adj, const swp_flags* f, int t, cudaStream_t s) {
+                      const swp_group_adjoint* adj, const swp_flags* f, int t, cudaStream_t s,
+                      bool refresh_coefs = true) {
   int nbg = 0, nbs = 0;
+  if (refresh_coefs) {
+    int rc = update_coefs<T>(p, st_in, s);
+    if (rc) return rc;
+  }
   GridLaunch<T> LG = make_grid<T>(p, st_out, nbg);
   LG.mode = GM_ADJ_STEP;
   LG.cfg = make_cfg(f);
@@ -342,7 +407,7 @@ int adjoint_window_impl(swp_plan* p, const swp_group_state* st, void* const* slo
         a[g].fourier = (char*)slots[g] + (size_t)k * ss;
         b[g].fourier = (char*)slots[g] + (size_t)(k + 1) * ss;
       }
-      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, t0 + k, cs);
+      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, t0 + k, cs, false);
       if (rc) return rc;
     }
     return SWP_OK;
@@ -371,6 +436,7 @@ int time_kernels_impl(swp_plan* p, const swp_group_state* st, const swp_group_ad
   StepCfg cfg = make_cfg(f);
   cfg.ra_mode = f->modalflag ? 2 : 1;
   cfg.diagnostics = 0;
+  cfg.incremental = step_incremental(p, f, f->t_start + 1) ? 1 : 0;  // the steady-state step form
   LS.cfg = cfg;
   LG.cfg = cfg;
   GridLaunch<T> LGa = LG;
@@ -388,12 +454,14 @@ int time_kernels_impl(swp_plan* p, const swp_group_state* st, const swp_group_ad
       LSa.grp[g].grad = adj[g].grad;
     }
   }
+  int rc = update_coefs<T>(p, st, s);
+  if (rc) return rc;
   cudaEvent_t ev[5];
   for (int i = 0; i < 5; ++i) cudaEventCreate(&ev[i]);
   double acc[4] = {0, 0, 0, 0};
   for (int r = 0; r < nrep; ++r) {
     cudaEventRecord(ev[0], s);
-    launch_spec<T>(LS, nbs, p->spec_smem, s);
+    launch_step_spec<T>(p, LS, nbs, s);
     cudaEventRecord(ev[1], s);
     launch_grid<T>(LG, nbg, p->grid_smem[GM_STEP], s);
     cudaEventRecord(ev[2], s);
@@ -476,7 +544,13 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
   p->graphs_enabled = !(ng_env && ng_env[0] == '1');
   spec_set_attributes();
   grid_set_attributes();
+  spec_tc_set_attributes();
   cudaStream_t s = 0;
+  if (cudaMalloc(&p->d_err, sizeof(int)) != cudaSuccess || cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess) {
+    p->err = "device error word allocation failed";
+    *out = p;
+    return SWP_ERR_CUDA;
+  }
   for (int g = 0; g < ngroups; ++g) {
     if (B[g] < 1) { p->err = "B must be >= 1"; *out = p; return SWP_ERR_ARG; }
     int rc = geometry_build(p->geom[g], M[g], s, p->err);
@@ -485,6 +559,13 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
     p->B[g] = B[g];
     int J = p->geom[g].J, I = p->geom[g].I;
     bool f64 = precision == SWP_FP64;
+    size_t cbytes = f64 ? CoefTables<double>::count(M[g], B[g], J) * sizeof(double)
+                        : CoefTables<float>::count(M[g], B[g], J) * sizeof(float);
+    if (cudaMalloc(&p->coefmem[g], cbytes) != cudaSuccess) {
+      p->err = "coefficient table allocation failed";
+      *out = p;
+      return SWP_ERR_CUDA;
+    }
     size_t cap = f64 ? 150 * 1024 : 110 * 1024;
     int mt = 8;
     while (mt > 1 && (f64 ? spec_smem_bytes<double>(M[g], J, mt) : spec_smem_bytes<float>(M[g], J, mt)) > cap) mt /= 2;
@@ -507,6 +588,26 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
       p->grid_smem[mode] = std::max(p->grid_smem[mode], gs);
     }
   }
+  // tensor-core step kernel: FP32 plans whose groups are all M = 42, unless SWP_NO_TC=1
+  const char* tc_env = getenv("SWP_NO_TC");
+  bool tc = precision == SWP_FAST && !(tc_env && tc_env[0] == '1');
+  for (int g = 0; g < ngroups; ++g) tc = tc && spec_tc_supported(M[g]);
+  if (tc) {
+    for (int g = 0; g < ngroups; ++g) {
+      if (cudaMalloc(&p->tcbasis[g], spec_tc_basis_floats() * sizeof(float)) != cudaSuccess ||
+          pack_tc_basis(p->geom[g], p->tcbasis[g], s) != SWP_OK) {
+        p->err = "tensor-core basis packing failed";
+        *out = p;
+        return SWP_ERR_CUDA;
+      }
+    }
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+      p->err = "tensor-core basis packing failed";
+      *out = p;
+      return SWP_ERR_CUDA;
+    }
+    p->use_tc = true;
+  }
   *out = p;
   return SWP_OK;
 }
@@ -517,11 +618,29 @@ int swp_plan_destroy(swp_plan* p) {
     if (ge.exec) cudaGraphExecDestroy(ge.exec);
   p->graphs.clear();
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
-  for (int g = 0; g < p->ng; ++g)
+  for (int g = 0; g < p->ng; ++g) {
     if (p->geom[g].mem) cudaFree(p->geom[g].mem);
+    if (p->tcbasis[g]) cudaFree(p->tcbasis[g]);
+    if (p->coefmem[g]) cudaFree(p->coefmem[g]);
+  }
+  if (p->d_err) cudaFree(p->d_err);
   delete p;
   return SWP_OK;
 }
+
+int swp_device_status(swp_plan* p, int* status, void* stream) {
+  if (!p || !status) return SWP_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(p->d_err, 0, sizeof(int), s);
+  if (e != cudaSuccess) return cuda_check(p, e, "device status");
+  *status = h;
+  return SWP_OK;
+}
+
+int swp_plan_uses_tensor_cores(const swp_plan* p) { return p && p->use_tc ? 1 : 0; }
 
 int swp_plan_dims(const swp_plan* p, int g, int* M, int* J, int* I, int* B) {
   if (!p || g < 0 || g >= p->ng) return SWP_ERR_ARG;

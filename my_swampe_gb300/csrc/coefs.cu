@@ -1,0 +1,73 @@
+// Per-call coefficient tables of the step kernels (see CoefTables in
+// swp_internal.h).  One small launch per library call that runs steps: the
+// parameters may change between calls (set_params, gradient sweeps), never
+// within one.  The expressions are the ones the reference evaluates:
+//   filters.py:95-151          sigma, sigmaPhi (hyperdiffusion), with sigma - 1
+//                              and sigmaPhi - 1 formed without cancellation
+//   time_stepping.py:491-534   tstepcoeff, tstepcoeff2, tstepcoeffmn
+//   modEuler_tdiff.py:80-261, explicit_tdiff.py:62-226  scalar factors
+//   spectral_transform.py:577-594  a / (n(n+1)), omega / sqrt(0.375)
+#include <algorithm>
+#include "swp_internal.h"
+
+namespace swp {
+
+template <typename T>
+__global__ void k_coefs(const double* __restrict__ par, const double* __restrict__ onemu2, int M, int B, int J,
+                        CoefTables<T> C) {
+  const int cnt = M + 1;
+  const int n_nco = B * cnt, n_jco = B * J;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_nco + n_jco + B; t += gridDim.x * blockDim.x) {
+    if (t < n_nco) {
+      const int b = t / cnt, n = t % cnt;
+      const double a = par[P_A * B + b], dt = par[P_DT * B + b];
+      const double K6 = par[P_K6 * B + b], K6P = par[P_K6PHI * B + b];
+      const double nd = (double)n;
+      const double ncoeff = ((nd * nd * nd) / (a * a * a)) * (((nd + 1) * (nd + 1) * (nd + 1)) / (a * a * a));
+      const double a6 = a * a * a * a * a * a;
+      const double x = 2.0 * dt * K6 * (ncoeff - 8.0 / a6), xp = 2.0 * dt * K6P * ncoeff;
+      const size_t o = (size_t)b * cnt + n, qs = (size_t)B * cnt;
+      C.nco[NC_SIG * qs + o] = (T)(1.0 / (1.0 + x));
+      C.nco[NC_SIGP * qs + o] = (T)(1.0 / (1.0 + xp));
+      C.nco[NC_SIGM1 * qs + o] = (T)(-x / (1.0 + x));
+      C.nco[NC_SIGPM1 * qs + o] = (T)(-xp / (1.0 + xp));
+      C.nco[NC_TC * qs + o] = (T)((n == 0) ? 0.0 : a / ((double)n * (n + 1)));
+    } else if (t < n_nco + n_jco) {
+      const int u = t - n_nco, b = u / J, j = u % J;
+      const double a = par[P_A * B + b], dt = par[P_DT * B + b];
+      C.jco[u] = (T)((2.0 * dt) / (a * onemu2[j]));
+    } else {
+      const int b = t - n_nco - n_jco;
+      const double a = par[P_A * B + b], dt = par[P_DT * B + b], Pb = par[P_PHIBAR * B + b];
+      const double td = par[P_TAUDRAG * B + b], om = par[P_OMEGA * B + b];
+      T* mc = C.mco;
+      mc[MC_DT * B + b] = (T)dt;
+      mc[MC_T2 * B + b] = (T)((2.0 * dt / (a * a)) / 4.0);
+      mc[MC_IA2 * B + b] = (T)(1.0 / (a * a));
+      mc[MC_HPB * B + b] = (T)(Pb * 0.5);
+      mc[MC_DTPB * B + b] = (T)(dt * Pb);
+      mc[MC_PBA2 * B + b] = (T)(Pb / (a * a));
+      mc[MC_PFD * B + b] = (T)((dt / 2.0) / (a * a));
+      mc[MC_2DTPB * B + b] = (T)(2.0 * dt * Pb);
+      mc[MC_2DT * B + b] = (T)(2.0 * dt);
+      mc[MC_ITD * B + b] = (T)(1.0 / td);
+      mc[MC_OM * B + b] = (T)(om / sqrt(0.375));
+      mc[MC_ALPHA * B + b] = (T)par[P_ALPHA * B + b];
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_coefs(const double* par, const double* onemu2, int M, int B, int J, const CoefTables<T>& C,
+                         cudaStream_t s) {
+  const int total = B * (M + 1) + B * J + B;
+  const int nb = std::min((total + 255) / 256, 1216);
+  k_coefs<T><<<nb, 256, 0, s>>>(par, onemu2, M, B, J, C);
+  return cudaGetLastError();
+}
+template cudaError_t launch_coefs<double>(const double*, const double*, int, int, int, const CoefTables<double>&,
+                                          cudaStream_t);
+template cudaError_t launch_coefs<float>(const double*, const double*, int, int, int, const CoefTables<float>&,
+                                         cudaStream_t);
+
+}  // namespace swp

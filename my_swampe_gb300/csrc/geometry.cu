@@ -68,10 +68,19 @@ __global__ void k_gauss_nodes(int J, double* mu, double* w, int* err) {
 }
 
 // Per-latitude constants that need neighbouring nodes (RMS-wind weights).
-__global__ void k_lat_consts(int J, int I, const double* mu, double* onemu2, double* area) {
+__global__ void k_lat_consts(int J, int I, const double* mu, double* onemu2, double* area, double* ihalf64,
+                             double* coslat64, float* ihalf32, float* coslat32) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= J) return;
   onemu2[j] = 1.0 - mu[j] * mu[j];
+  // 1 / (2 (1 - mu^2)) of the kinetic-energy term E (initial_conditions.py:499-503)
+  // and cos(phi) = sqrt(1 - mu^2) of the dayside forcing (forcing.py:55-60),
+  // per latitude in both compute types
+  const double ih = 1.0 / (2.0 * onemu2[j]), cl = sqrt(onemu2[j]);
+  ihalf64[j] = ih;
+  coslat64[j] = cl;
+  ihalf32[j] = (float)ih;
+  coslat32[j] = (float)cl;
   // time_stepping.py:568-576: area_comp = a^2 sin(phi+pi/2)^2 dphi dlambda,
   // integrand (U/cos phi)^2 + (V/cos phi)^2, normalised by 4 pi a^2.
   double phi = asin(mu[j]);
@@ -231,6 +240,7 @@ int geometry_build(GroupGeom& gg, int M, cudaStream_t stream, std::string& err) 
   size_t off = 0;
   auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
   size_t o_mu = take(J * 8), o_w = take(J * 8), o_om = take(J * 8), o_area = take(J * 8);
+  size_t o_ih64 = take(J * 8), o_cl64 = take(J * 8), o_ih32 = take(J * 4), o_cl32 = take(J * 4);
   size_t o_boff = take((M + 2) * 4);
   size_t o_b64[8], o_b32[8];
   for (int k = 0; k < 8; ++k) o_b64[k] = take(nb * 8);
@@ -244,6 +254,8 @@ int geometry_build(GroupGeom& gg, int M, cudaStream_t stream, std::string& err) 
   char* b = (char*)gg.mem;
   gg.mu = (double*)(b + o_mu); gg.w = (double*)(b + o_w); gg.onemu2 = (double*)(b + o_om);
   gg.area = (double*)(b + o_area); gg.boff = (int*)(b + o_boff);
+  gg.ihalf64 = (double*)(b + o_ih64); gg.coslat64 = (double*)(b + o_cl64);
+  gg.ihalf32 = (float*)(b + o_ih32); gg.coslat32 = (float*)(b + o_cl32);
   for (int k = 0; k < 8; ++k) { gg.b64[k] = (double*)(b + o_b64[k]); gg.b32[k] = (float*)(b + o_b32[k]); }
   gg.twL64 = (double2*)(b + o_twL64); gg.twI64 = (double2*)(b + o_twI64);
   gg.twL32 = (float2*)(b + o_twL32); gg.twI32 = (float2*)(b + o_twI32);
@@ -257,7 +269,8 @@ int geometry_build(GroupGeom& gg, int M, cudaStream_t stream, std::string& err) 
   cudaMemcpyAsync(gg.boff, boff.data(), (M + 2) * 4, cudaMemcpyHostToDevice, stream);
   cudaMemcpyAsync(ddmg, dmg.data(), dmg.size() * 8, cudaMemcpyHostToDevice, stream);
   k_gauss_nodes<<<(jh + 63) / 64, 64, 0, stream>>>(J, gg.mu, gg.w, derr);
-  k_lat_consts<<<(J + 63) / 64, 64, 0, stream>>>(J, I, gg.mu, gg.onemu2, gg.area);
+  k_lat_consts<<<(J + 63) / 64, 64, 0, stream>>>(J, I, gg.mu, gg.onemu2, gg.area, gg.ihalf64, gg.coslat64,
+                                                 gg.ihalf32, gg.coslat32);
   dim3 gb(M + 1, (jh + 63) / 64);
   k_basis<<<gb, 64, 0, stream>>>(M, J, gg.mu, gg.w, gg.boff, ddmg,
       gg.b64[B_PW_F], gg.b64[B_HW_F], gg.b64[B_P_F], gg.b64[B_H_F],

@@ -130,7 +130,7 @@ struct PhysicsAdj {
   T Pb, itr, itd, DPe;
   bool nodrag, forced;
   __device__ __forceinline__ void eval(T eta, T Phi, T U, T V, T ihalf, T day_s, const T* lz, T* lx,
-                                       double* gacc) const {
+                                       T* gacc) const {
     T lU = lz[0] * eta + lz[2] * Phi + lz[4] * (T)2 * U * ihalf;
     T lV = lz[1] * eta + lz[3] * Phi + lz[4] * (T)2 * V * ihalf;
     T leta = lz[0] * U + lz[1] * V;
@@ -152,10 +152,12 @@ struct PhysicsAdj {
       T lpts = -lr * r / pts;
       T lQ = lz[5] + (pos ? lQc : (T)0);
       lPhi += -itr * lQ + lpts;
-      gacc[G_TAURAD] += (double)lQ * (double)(-Q * itr);
-      if (!nodrag) gacc[G_TAUDRAG] += ((double)lF * U + (double)lG * V) * (double)itd * (double)itd;
-      gacc[G_DPHIEQ] += (double)lQ * (double)itr * (double)day_s;
-      gacc[G_PHIBAR] += (double)lpts;
+      // per-thread partial sums in the compute type (two points per thread);
+      // the block and global reductions run in FP64
+      gacc[G_TAURAD] += lQ * (-Q * itr);
+      if (!nodrag) gacc[G_TAUDRAG] += (lF * U + lG * V) * itd * itd;
+      gacc[G_DPHIEQ] += lQ * itr * day_s;
+      gacc[G_PHIBAR] += lpts;
     }
     lx[0] = leta; lx[1] = lPhi; lx[2] = lU; lx[3] = lV;
   }
@@ -214,9 +216,9 @@ __device__ __forceinline__ void write_r2c(const GridCtx<T>& c, const typename cp
 }
 
 template <typename T>
-__device__ void block_add_grads(double* gacc, double* sred, double* grad, int B, int b) {
+__device__ void block_add_grads(const T* gacc, double* sred, double* grad, int B, int b) {
   for (int q = 0; q < NGRAD; ++q) {
-    double v = gacc[q];
+    double v = (double)gacc[q];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(&sred[q], v);
   }
@@ -353,8 +355,8 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
         continue;
       }
       // GM_STEP: physics on the two points (2n, 2n+1)
-      T ihalf = (T)(1.0 / (2.0 * g.onemu2[j]));
-      T s = (T)sqrt(g.onemu2[j]);
+      T ihalf = g.ihalf[j];
+      T s = g.coslat[j];
       T outs[2][8];
 #pragma unroll
       for (int e = 0; e < 2; ++e)
@@ -482,8 +484,8 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
     for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
       int n = t % L, r = t / L, j = j0 + r;
       size_t po = ((size_t)b * J + j) * I + 2 * n;
-      T ihalf = (T)(1.0 / (2.0 * g.onemu2[j]));
-      T s = (T)sqrt(g.onemu2[j]);
+      T ihalf = g.ihalf[j];
+      T s = g.coslat[j];
       T outs[2][8];
 #pragma unroll
       for (int e = 0; e < 2; ++e) {
@@ -546,11 +548,11 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
     __syncthreads();
     T2* zin = cfft_batch<+1>(bufA, bufB, L, LS, nb1 * JB, g.twL);
     T2* zout = (zin == bufA) ? bufB : bufA;
-    double gacc[NGRAD] = {0.0, 0.0, 0.0, 0.0};
+    T gacc[NGRAD] = {(T)0, (T)0, (T)0, (T)0};
     for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
       int n = t % L, r = t / L, j = j0 + r;
-      T ihalf = (T)(1.0 / (2.0 * g.onemu2[j]));
-      T s = (T)sqrt(g.onemu2[j]);
+      T ihalf = g.ihalf[j];
+      T s = g.coslat[j];
       T lx[2][4];
 #pragma unroll
       for (int e = 0; e < 2; ++e) {

@@ -1,0 +1,148 @@
+// Pieces shared by the SIMT and tensor-core Legendre kernels of a step:
+// the combined-input slots and their evaluation at one (m, member, latitude).
+#pragma once
+#include "swp_internal.h"
+
+namespace swp {
+
+// combined-input slots of the forward contraction.  The FP32 path carries three
+// more P slots (the current eta, delta, Phi on their own) for the incremental
+// form of the step; the FP64 path keeps the reference's projection form.
+enum SlotP { SP_PHI1 = 0, SP_PHI2, SP_D1, SP_D2, SP_E1, SP_IPHI, SP_ID, SP_IE };  // on Pw
+enum SlotH { SH_PHI1 = 0, SH_D1, SH_D2, SH_E1, NSH };                            // on Hw
+template <typename T> struct SlotCount { static constexpr int NP = 5; static constexpr bool INCR = false; };
+template <> struct SlotCount<float> { static constexpr int NP = 8; static constexpr bool INCR = true; };
+constexpr int NSP = 5;
+template <typename T>
+__device__ __forceinline__ const SpecGroup<T>& pick_group(const SpecLaunch<T>& L, int& idx) {
+  int gi = 0;
+  while (gi + 1 < L.ng && (int)blockIdx.x >= L.prefix[gi + 1]) ++gi;
+  idx = blockIdx.x - L.prefix[gi];
+  return L.grp[gi];
+}
+
+// i*m*z
+template <typename T2, typename T>
+__device__ __forceinline__ T2 imul(T m, T2 z) { T2 r; r.x = -m * z.y; r.y = m * z.x; return r; }
+
+// Per-(member, n) spectral coefficients of a CTA's tile from the call's tables
+// into shared memory; without hyperdiffusion sigma = 1, sigma - 1 = 0.
+template <typename T>
+__device__ __forceinline__ void load_spec_coefs(const SpecGroup<T>& G, bool diff, int m, int b0, int mt, int MT,
+                                                int cnt, int cntmax, T* sig, T* sigP, T* sigm1, T* sigPm1, T* tcmn) {
+  const size_t qs = (size_t)G.B * cntmax;
+  for (int t = threadIdx.x; t < MT * cnt; t += blockDim.x) {
+    const int bt = t / cnt, k = t % cnt, n = m + k;
+    T s = (T)1, sp = (T)1, sm1 = (T)0, spm1 = (T)0, tc = (T)0;
+    if (bt < mt) {
+      const size_t o = (size_t)(b0 + bt) * cntmax + n;
+      if (diff) {
+        s = G.nco[NC_SIG * qs + o];
+        sp = G.nco[NC_SIGP * qs + o];
+        sm1 = G.nco[NC_SIGM1 * qs + o];
+        spm1 = G.nco[NC_SIGPM1 * qs + o];
+      }
+      tc = G.nco[NC_TC * qs + o];
+    }
+    sig[bt * cntmax + k] = s;
+    sigP[bt * cntmax + k] = sp;
+    sigm1[bt * cntmax + k] = sm1;
+    sigPm1[bt * cntmax + k] = spm1;
+    tcmn[bt * cntmax + k] = tc;
+  }
+}
+
+// The combined inputs of the forward contraction at (m, member b, latitude j):
+// every reference tendency term that is a Legendre transform of a pointwise
+// product of Fourier inputs (modEuler_tdiff.py:72-110, 162-201, 253-261;
+// explicit_tdiff.py:62-78, 134-155, 207-226), grouped by the basis (Pw or Hw)
+// and by the output factor (1 or n(n+1)) they are applied with.  mode 2 is the
+// plain transform of eta, delta used to diagnose winds (model.py:644-666).
+template <typename T>
+__device__ __forceinline__ void step_combos(const SpecGroup<T>& G, const StepCfg& cfg, int mode, bool incr, int m,
+                                            int b, int j, size_t FS, typename cplx<T>::type* c) {
+  typedef typename cplx<T>::type T2;
+  constexpr int NSPX = SlotCount<T>::NP;
+  constexpr int NSLOT = NSPX + NSH;
+  const Geom<T>& g = G.g;
+  const T2* F = G.four;
+  const T* mc = G.mco;
+  const int B = G.B;
+  const T xm = (T)m;
+  const size_t o = ((size_t)m * G.B + b) * g.J + j;
+  const T tsc = G.jco[(size_t)b * g.J + j];           // tstepcoeff
+  T2 z = mk<T2>(0, 0);
+#pragma unroll
+  for (int q = 0; q < NSLOT; ++q) c[q] = z;
+  if (mode == 2) {  // diagnose winds: plain forward transforms of eta, delta
+    c[SP_E1] = F[F_ETA * FS + o];
+    c[SP_D1] = F[F_DELTA * FS + o];
+  } else if (cfg.scheme == 0) {
+    T2 eta = F[F_ETA * FS + o], del = F[F_DELTA * FS + o], phi = F[F_PHI * FS + o];
+    T2 A = F[F_A * FS + o], Bm = F[F_B * FS + o], C = F[F_C * FS + o], D = F[F_D * FS + o];
+    T2 E = F[F_E * FS + o], PF = F[F_PHIF * FS + o], Fm = F[F_F * FS + o], Gm = F[F_G * FS + o];
+    T t1 = tsc * (T)0.25, t2 = mc[MC_T2 * B + b];
+    T ia2 = mc[MC_IA2 * B + b];
+    T hPb = mc[MC_HPB * B + b];
+    T2 Bf = cadd(Bm, Fm), Af = csub(A, Gm);
+    T2 Beff = cfg.forcflag ? Bf : Bm, Aeff = cfg.forcflag ? Af : A;
+    // Phi (modEuler_tdiff.py:80-110); incremental form: curr goes to its own slot
+    T2 p1 = incr ? cscale(imul(xm, C), -t1) : csub(phi, cscale(imul(xm, C), t1));
+    p1 = csub(p1, cscale(del, mc[MC_DTPB * B + b]));
+    p1 = csub(p1, cscale(imul(xm, Beff), hPb * t1));
+    if (cfg.forcflag) p1 = cadd(p1, cscale(PF, mc[MC_DT * B + b]));
+    c[SP_PHI1] = p1;
+    c[NSPX + SH_PHI1] = csub(cscale(D, t1), cscale(Aeff, hPb * t1));
+    c[SP_PHI2] = cscale(cadd(cscale(E, t2), cscale(phi, ia2)), -hPb);
+    // delta (modEuler_tdiff.py:162-201)
+    c[SP_D1] = incr ? cscale(imul(xm, Bf), t1) : cadd(del, cscale(imul(xm, Bf), t1));
+    c[NSPX + SH_D1] = cscale(Af, t1);
+    T2 d2 = cadd(cscale(phi, t2), cscale(E, t2));
+    d2 = cadd(d2, cscale(imul(xm, C), t1 * (T)0.5 * ia2));
+    d2 = csub(d2, cscale(del, mc[MC_PBA2 * B + b]));
+    if (cfg.forcflag) d2 = cadd(d2, cscale(PF, mc[MC_PFD * B + b]));
+    c[SP_D2] = d2;
+    c[NSPX + SH_D2] = cscale(D, t1 * (T)0.5 * ia2);
+    // eta (modEuler_tdiff.py:253-261)
+    T te = cfg.forcflag ? tsc : tsc * (T)0.5;
+    c[SP_E1] = incr ? cscale(imul(xm, Aeff), -te) : csub(eta, cscale(imul(xm, Aeff), te));
+    c[NSPX + SH_E1] = cscale(Beff, te);
+    if (incr) { c[SP_IPHI] = phi; c[SP_ID] = del; c[SP_IE] = eta; }
+  } else {
+    T2 eta0 = F[F_ETA_PREV * FS + o], del0 = F[F_DELTA_PREV * FS + o], phi0 = F[F_PHI_PREV * FS + o];
+    T2 del1 = F[F_DELTA * FS + o];
+    T2 A = F[F_A * FS + o], Bm = F[F_B * FS + o], C = F[F_C * FS + o], D = F[F_D * FS + o];
+    T2 PF = F[F_PHIF * FS + o], Fm = F[F_F * FS + o], Gm = F[F_G * FS + o];
+    T2 U = F[F_U * FS + o], V = F[F_V * FS + o];
+    T t = tsc;
+    T itd = mc[MC_ITD * B + b];
+    // Phi (explicit_tdiff.py:62-78)
+    T2 p1 = csub(phi0, cscale(imul(xm, C), t));
+    p1 = csub(p1, cscale(del1, mc[MC_2DTPB * B + b]));
+    if (cfg.forcflag) p1 = cadd(p1, cscale(PF, mc[MC_2DT * B + b]));
+    c[SP_PHI1] = p1;
+    c[NSPX + SH_PHI1] = cscale(D, t);
+    // delta (explicit_tdiff.py:134-155)
+    T2 d1 = del0, dh = mk<T2>(0, 0);
+    if (cfg.forcflag) {
+      d1 = csub(d1, cscale(imul(xm, U), t * itd));
+      d1 = cadd(d1, cscale(imul(xm, Fm), t));
+      dh = csub(cscale(V, t * itd), cscale(Gm, t));
+    }
+    c[SP_D1] = d1;
+    c[NSPX + SH_D1] = dh;
+    // eta (explicit_tdiff.py:207-226)
+    T2 e1 = csub(eta0, cscale(imul(xm, A), t));
+    T2 eh = cscale(Bm, t);
+    if (cfg.forcflag) {
+      e1 = csub(e1, cscale(imul(xm, V), t * itd));
+      e1 = cadd(e1, cscale(imul(xm, Gm), t));
+      eh = cadd(eh, cscale(U, t * itd));
+      eh = cadd(eh, cscale(Fm, t));
+    }
+    c[SP_E1] = e1;
+    c[NSPX + SH_E1] = eh;
+  }
+}
+
+}  // namespace swp

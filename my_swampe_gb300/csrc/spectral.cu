@@ -19,17 +19,10 @@
 // use the equatorial symmetry of the Gauss grid, Pbar(-mu) = (-1)^(n-m) Pbar(mu),
 // so each contraction runs over J/2 latitudes.
 #include "swp_internal.h"
+#include "spec_common.cuh"
 
 namespace swp {
 
-// combined-input slots of the forward contraction.  The FP32 path carries three
-// more P slots (the current eta, delta, Phi on their own) for the incremental
-// form of the step; the FP64 path keeps the reference's projection form.
-enum SlotP { SP_PHI1 = 0, SP_PHI2, SP_D1, SP_D2, SP_E1, SP_IPHI, SP_ID, SP_IE };  // on Pw
-enum SlotH { SH_PHI1 = 0, SH_D1, SH_D2, SH_E1, NSH };                            // on Hw
-template <typename T> struct SlotCount { static constexpr int NP = 5; static constexpr bool INCR = false; };
-template <> struct SlotCount<float> { static constexpr int NP = 8; static constexpr bool INCR = true; };
-constexpr int NSP = 5;
 constexpr int NKIN_P = 5;  // inverse inputs on P: eta, delta, Phi, Uprep, Vprep
 constexpr int NKIN_H = 2;  // inverse inputs on H: eta_s (U), -delta_s (V)
 constexpr int NKIN = NKIN_P + NKIN_H;
@@ -47,18 +40,6 @@ size_t spec_smem_bytes(int M, int J, int MT) {
 }
 template size_t spec_smem_bytes<double>(int, int, int);
 template size_t spec_smem_bytes<float>(int, int, int);
-
-template <typename T>
-__device__ __forceinline__ const SpecGroup<T>& pick_group(const SpecLaunch<T>& L, int& idx) {
-  int gi = 0;
-  while (gi + 1 < L.ng && (int)blockIdx.x >= L.prefix[gi + 1]) ++gi;
-  idx = blockIdx.x - L.prefix[gi];
-  return L.grp[gi];
-}
-
-// i*m*z
-template <typename T2, typename T>
-__device__ __forceinline__ T2 imul(T m, T2 z) { T2 r; r.x = -m * z.y; r.y = m * z.x; return r; }
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLaunch<T> L) {
@@ -93,31 +74,7 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
   const bool incr = SlotCount<T>::INCR && cfg.incremental && mode == 0 && cfg.scheme == 0;
 
   // ---- phase 0: per-member spectral coefficients and the blow-up gate
-  for (int t = threadIdx.x; t < MT * cnt; t += blockDim.x) {
-    int bt = t / cnt, k = t % cnt, n = m + k;
-    double s = 1.0, sp = 1.0, sm1 = 0.0, spm1 = 0.0, tc = 0.0;
-    if (bt < mt) {
-      int b = b0 + bt;
-      double a = G.par[P_A * G.B + b], dt = G.par[P_DT * G.B + b];
-      if (cfg.diffflag && mode == 0) {
-        double K6 = G.par[P_K6 * G.B + b], K6P = G.par[P_K6PHI * G.B + b];
-        double nd = (double)n;
-        double ncoeff = ((nd * nd * nd) / (a * a * a)) * (((nd + 1) * (nd + 1) * (nd + 1)) / (a * a * a));
-        double a6 = a * a * a * a * a * a;
-        double x = 2.0 * dt * K6 * (ncoeff - 8.0 / a6), xp = 2.0 * dt * K6P * ncoeff;
-        s = 1.0 / (1.0 + x);
-        sp = 1.0 / (1.0 + xp);
-        sm1 = -x / (1.0 + x);
-        spm1 = -xp / (1.0 + xp);
-      }
-      tc = (n == 0) ? 0.0 : a / ((double)n * (n + 1));
-    }
-    sig[bt * cntmax + k] = (T)s;
-    sigP[bt * cntmax + k] = (T)sp;
-    sigm1[bt * cntmax + k] = (T)sm1;
-    sigPm1[bt * cntmax + k] = (T)spm1;
-    tcmn[bt * cntmax + k] = (T)tc;
-  }
+  load_spec_coefs<T>(G, cfg.diffflag && mode == 0, m, b0, mt, MT, cnt, cntmax, sig, sigP, sigm1, sigPm1, tcmn);
   if (threadIdx.x < MT) {
     int bt = threadIdx.x, dead = 0;
     if (bt < mt && cfg.diagnostics && mode == 0) {
@@ -139,87 +96,11 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
     T2 xs[NSLOT], xa[NSLOT];
     if (bt < mt) {
       int b = b0 + bt;
-      double dt = G.par[P_DT * G.B + b], a = G.par[P_A * G.B + b], Pb = G.par[P_PHIBAR * G.B + b];
-      double td = G.par[P_TAUDRAG * G.B + b];
-      T xm = (T)m;
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
         int j = side ? (J - 1 - jp) : jp;
-        size_t o = ((size_t)m * G.B + b) * J + j;
-        double tsc = (2.0 * dt) / (a * g.onemu2[j]);       // tstepcoeff
         T2 c[NSLOT];
-        T2 z = mk<T2>(0, 0);
-#pragma unroll
-        for (int q = 0; q < NSLOT; ++q) c[q] = z;
-        if (mode == 2) {  // diagnose winds: plain forward transforms of eta, delta
-          c[SP_E1] = F[F_ETA * FS + o];
-          c[SP_D1] = F[F_DELTA * FS + o];
-        } else if (cfg.scheme == 0) {
-          T2 eta = F[F_ETA * FS + o], del = F[F_DELTA * FS + o], phi = F[F_PHI * FS + o];
-          T2 A = F[F_A * FS + o], Bm = F[F_B * FS + o], C = F[F_C * FS + o], D = F[F_D * FS + o];
-          T2 E = F[F_E * FS + o], PF = F[F_PHIF * FS + o], Fm = F[F_F * FS + o], Gm = F[F_G * FS + o];
-          T t1 = (T)(tsc / 4.0), t2 = (T)((2.0 * dt / (a * a)) / 4.0);
-          T ia2 = (T)(1.0 / (a * a));
-          T hPb = (T)(Pb * 0.5);
-          T2 Bf = cadd(Bm, Fm), Af = csub(A, Gm);
-          T2 Beff = cfg.forcflag ? Bf : Bm, Aeff = cfg.forcflag ? Af : A;
-          // Phi (modEuler_tdiff.py:80-110); incremental form: curr goes to its own slot
-          T2 p1 = incr ? cscale(imul(xm, C), -t1) : csub(phi, cscale(imul(xm, C), t1));
-          p1 = csub(p1, cscale(del, (T)(dt * Pb)));
-          p1 = csub(p1, cscale(imul(xm, Beff), hPb * t1));
-          if (cfg.forcflag) p1 = cadd(p1, cscale(PF, (T)dt));
-          c[SP_PHI1] = p1;
-          c[NSPX + SH_PHI1] = csub(cscale(D, t1), cscale(Aeff, hPb * t1));
-          c[SP_PHI2] = cscale(cadd(cscale(E, t2), cscale(phi, ia2)), -hPb);
-          // delta (modEuler_tdiff.py:162-201)
-          c[SP_D1] = incr ? cscale(imul(xm, Bf), t1) : cadd(del, cscale(imul(xm, Bf), t1));
-          c[NSPX + SH_D1] = cscale(Af, t1);
-          T2 d2 = cadd(cscale(phi, t2), cscale(E, t2));
-          d2 = cadd(d2, cscale(imul(xm, C), t1 * (T)0.5 * ia2));
-          d2 = csub(d2, cscale(del, (T)(Pb / (a * a))));
-          if (cfg.forcflag) d2 = cadd(d2, cscale(PF, (T)((dt / 2.0) / (a * a))));
-          c[SP_D2] = d2;
-          c[NSPX + SH_D2] = cscale(D, t1 * (T)0.5 * ia2);
-          // eta (modEuler_tdiff.py:253-261)
-          T te = cfg.forcflag ? (T)tsc : (T)(tsc / 2.0);
-          c[SP_E1] = incr ? cscale(imul(xm, Aeff), -te) : csub(eta, cscale(imul(xm, Aeff), te));
-          c[NSPX + SH_E1] = cscale(Beff, te);
-          if (incr) { c[SP_IPHI] = phi; c[SP_ID] = del; c[SP_IE] = eta; }
-        } else {
-          T2 eta0 = F[F_ETA_PREV * FS + o], del0 = F[F_DELTA_PREV * FS + o], phi0 = F[F_PHI_PREV * FS + o];
-          T2 del1 = F[F_DELTA * FS + o];
-          T2 A = F[F_A * FS + o], Bm = F[F_B * FS + o], C = F[F_C * FS + o], D = F[F_D * FS + o];
-          T2 PF = F[F_PHIF * FS + o], Fm = F[F_F * FS + o], Gm = F[F_G * FS + o];
-          T2 U = F[F_U * FS + o], V = F[F_V * FS + o];
-          T t = (T)tsc;
-          T itd = (T)(1.0 / td);
-          // Phi (explicit_tdiff.py:62-78)
-          T2 p1 = csub(phi0, cscale(imul(xm, C), t));
-          p1 = csub(p1, cscale(del1, (T)(2.0 * dt * Pb)));
-          if (cfg.forcflag) p1 = cadd(p1, cscale(PF, (T)(2.0 * dt)));
-          c[SP_PHI1] = p1;
-          c[NSPX + SH_PHI1] = cscale(D, t);
-          // delta (explicit_tdiff.py:134-155)
-          T2 d1 = del0, dh = mk<T2>(0, 0);
-          if (cfg.forcflag) {
-            d1 = csub(d1, cscale(imul(xm, U), t * itd));
-            d1 = cadd(d1, cscale(imul(xm, Fm), t));
-            dh = csub(cscale(V, t * itd), cscale(Gm, t));
-          }
-          c[SP_D1] = d1;
-          c[NSPX + SH_D1] = dh;
-          // eta (explicit_tdiff.py:207-226)
-          T2 e1 = csub(eta0, cscale(imul(xm, A), t));
-          T2 eh = cscale(Bm, t);
-          if (cfg.forcflag) {
-            e1 = csub(e1, cscale(imul(xm, V), t * itd));
-            e1 = cadd(e1, cscale(imul(xm, Gm), t));
-            eh = cadd(eh, cscale(U, t * itd));
-            eh = cadd(eh, cscale(Fm, t));
-          }
-          c[SP_E1] = e1;
-          c[NSPX + SH_E1] = eh;
-        }
+        step_combos<T>(G, cfg, mode, incr, m, b, j, FS, c);
         if (side == 0) {
 #pragma unroll
           for (int q = 0; q < NSLOT; ++q) { xs[q] = c[q]; xa[q] = c[q]; }
@@ -294,14 +175,14 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
         }
       }
       const int bt = r >> 1, comp = r & 1;
-      double omega = bt < mt ? G.par[P_OMEGA * G.B + b0 + bt] : 0.0;
+      const T om = bt < mt ? G.mco[MC_OM * G.B + b0 + bt] : (T)0;
 #pragma unroll
       for (int k = 0; k < FWD_TC; ++k) {
         int c = c0 + k;
         if (c >= Cp) break;
         int kk = par + 2 * c;            // n - m
         int n = m + kk;
-        T nn1 = (T)((double)n * (n + 1));
+        T nn1 = (T)(n * (n + 1));
         T s = sig[bt * cntmax + kk], sp = sigP[bt * cntmax + kk], tc = tcmn[bt * cntmax + kk];
         T cphi, cdel, ceta;      // spectral eta, delta (full, for the winds)
         T kphi, kdel, keta;      // what the inverse transform turns into the new Fourier carries
@@ -335,7 +216,7 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
         // wind inversion inputs (spectral_transform.py:577-594)
         T dp = (n == 0) ? (T)0 : cdel;
         T ep = (n == 0) ? (T)0 : ceta;
-        if (m == 0 && n == 1 && comp == 0) ep -= (T)(omega / sqrt(0.375));
+        if (m == 0 && n == 1 && comp == 0) ep -= om;
         T es = ep * tc, ds = dp * tc;
         int pc = par ? C0 + c : c;
         Kin[((size_t)0 * cntmax + pc) * R + r] = keta;
@@ -446,7 +327,7 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
       Fo[F_V * FS + o] = get(4);
       continue;
     }
-    double al = G.par[P_ALPHA * G.B + b];
+    const T aa = G.mco[MC_ALPHA * G.B + b];
     const int cf[3] = {F_ETA, F_DELTA, F_PHI};
     const int pf[3] = {F_ETA_PREV, F_DELTA_PREV, F_PHI_PREV};
     const int rf[3] = {F_ETA_MID, F_DELTA_MID, F_PHI_MID};
@@ -460,7 +341,6 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
         if (cfg.ra_mode == 1) Fo[rf[q] * FS + o] = old;
         else if (cfg.ra_mode == 2) {
           T2 mid = Fi[rf[q] * FS + o];
-          T aa = (T)al;
           T2 d = cadd(csub(mid, cscale(old, (T)2)), nw);
           Fo[rf[q] * FS + o] = cadd(old, cscale(d, aa));
         }
@@ -552,31 +432,7 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
   // [MT] Phibar gradient partials: doubles, so round the address up to 16 bytes
   double* sgrad = (double*)(((uintptr_t)(tcmn + MT * cntmax) + 15) & ~(uintptr_t)15);
 
-  for (int t = threadIdx.x; t < MT * cnt; t += blockDim.x) {
-    int bt = t / cnt, k = t % cnt, n = m + k;
-    double s = 1.0, sp = 1.0, sm1 = 0.0, spm1 = 0.0, tc = 0.0;
-    if (bt < mt) {
-      int b = b0 + bt;
-      double a = G.par[P_A * G.B + b], dt = G.par[P_DT * G.B + b];
-      if (cfg.diffflag) {
-        double K6 = G.par[P_K6 * G.B + b], K6P = G.par[P_K6PHI * G.B + b];
-        double nd = (double)n;
-        double ncoeff = ((nd * nd * nd) / (a * a * a)) * (((nd + 1) * (nd + 1) * (nd + 1)) / (a * a * a));
-        double a6 = a * a * a * a * a * a;
-        double x = 2.0 * dt * K6 * (ncoeff - 8.0 / a6), xp = 2.0 * dt * K6P * ncoeff;
-        s = 1.0 / (1.0 + x);
-        sp = 1.0 / (1.0 + xp);
-        sm1 = -x / (1.0 + x);
-        spm1 = -xp / (1.0 + xp);
-      }
-      tc = (n == 0) ? 0.0 : a / ((double)n * (n + 1));
-    }
-    sig[bt * cntmax + k] = (T)s;
-    sigP[bt * cntmax + k] = (T)sp;
-    sigm1[bt * cntmax + k] = (T)sm1;
-    sigPm1[bt * cntmax + k] = (T)spm1;
-    tcmn[bt * cntmax + k] = (T)tc;
-  }
+  load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, cntmax, sig, sigP, sigm1, sigPm1, tcmn);
   if (threadIdx.x < MT) sgrad[threadIdx.x] = 0.0;
 
   // ---- phase 1: symmetrised adjoints of the step outputs at column m
@@ -677,7 +533,7 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
     T xm = (T)m;
     T tc = tcmn[bt * cntmax + kk];
     T s = sig[bt * cntmax + kk], sp = sigP[bt * cntmax + kk];
-    T nn1 = (T)((double)n * (n + 1));
+    T nn1 = (T)(n * (n + 1));
     // lambda delta_s = (i m) lambda Uprep - lambda Hin_V ; lambda eta_s = (i m) lambda Vprep + lambda Hin_U
     T lds_r = -xm * S(3, 1) - S(6, 0), lds_i = xm * S(3, 0) - S(6, 1);
     T les_r = -xm * S(4, 1) + S(5, 0), les_i = xm * S(4, 0) + S(5, 1);
@@ -779,12 +635,14 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
     // slot order: 0 PhiP1, 1 PhiP2, 2 dP1, 3 dP2, 4 eP1, [identity Phi, delta, eta], PhiH1, dH1, dH2, eH1
     T2 lPhiP1 = ld(0), lPhiP2 = ld(1), ldP1 = ld(2), ldP2 = ld(3), leP1 = ld(4);
     T2 lPhiH1 = ld(NKADJ), ldH1 = ld(NKADJ + 1), ldH2 = ld(NKADJ + 2), leH1 = ld(NKADJ + 3);
-    double dt = G.par[P_DT * G.B + b], a = G.par[P_A * G.B + b], Pb = G.par[P_PHIBAR * G.B + b];
-    double tsc = (2.0 * dt) / (a * g.onemu2[j]);
-    T t1 = (T)(tsc / 4.0), t2 = (T)((2.0 * dt / (a * a)) / 4.0);
-    T ia2 = (T)(1.0 / (a * a));
-    T hPb = (T)(Pb * 0.5);
-    T te = cfg.forcflag ? (T)tsc : (T)(tsc / 2.0);
+    const T* mc = G.mco;
+    const int B = G.B;
+    const T tsc = G.jco[(size_t)b * J + j];
+    const T dt = mc[MC_DT * B + b];
+    T t1 = tsc * (T)0.25, t2 = mc[MC_T2 * B + b];
+    T ia2 = mc[MC_IA2 * B + b];
+    T hPb = mc[MC_HPB * B + b];
+    T te = cfg.forcflag ? tsc : tsc * (T)0.5;
     T xm = (T)m;
     T forc = cfg.forcflag ? (T)1 : (T)0;
     // conj(i*alpha*m) z = -i alpha m z
@@ -799,12 +657,12 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
       ideta = cadd(ld(NKADJ > 7 ? 7 : 0), G.lamY[0 * FS + oy]);
     }
     T2 lphi = csub(cadd(idphi, cscale(ldP2, t2)), cscale(lPhiP2, hPb * ia2));
-    T2 ldel = cadd(csub(iddel, cscale(lPhiP1, (T)(dt * Pb))), cscale(ldP2, (T)(-Pb / (a * a))));
+    T2 ldel = cadd(csub(iddel, cscale(lPhiP1, mc[MC_DTPB * B + b])), cscale(ldP2, -mc[MC_PBA2 * B + b]));
     T2 leta = ideta;
     T2 lC = cadd(mimul(-t1, lPhiP1), mimul(t1 * (T)0.5 * ia2, ldP2));
     T2 lD = cadd(cscale(lPhiH1, t1), cscale(ldH2, t1 * (T)0.5 * ia2));
     T2 lE = cadd(cscale(lPhiP2, -hPb * t2), cscale(ldP2, t2));
-    T2 lPF = cscale(cadd(cscale(lPhiP1, (T)dt), cscale(ldP2, (T)((dt / 2.0) / (a * a)))), forc);
+    T2 lPF = cscale(cadd(cscale(lPhiP1, dt), cscale(ldP2, mc[MC_PFD * B + b])), forc);
     T2 lBeff = cadd(mimul(-hPb * t1, lPhiP1), cscale(leH1, te));
     T2 lAeff = cadd(cscale(lPhiH1, -hPb * t1), mimul(-te, leP1));
     T2 lBf = mimul(t1, ldP1);
@@ -824,14 +682,17 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
       T2 del = PX[F_DELTA * FS + o], phi = PX[F_PHI * FS + o], E = PX[F_E * FS + o];
       T2 A = PX[F_A * FS + o], Bm = PX[F_B * FS + o], Fm = PX[F_F * FS + o], Gm = PX[F_G * FS + o];
       T2 Beff = cfg.forcflag ? cadd(Bm, Fm) : Bm, Aeff = cfg.forcflag ? csub(A, Gm) : A;
-      T2 dP1 = csub(cscale(del, (T)-dt), cscale(imul(xm, Beff), (T)0.5 * t1));
+      T2 dP1 = csub(cscale(del, -dt), cscale(imul(xm, Beff), (T)0.5 * t1));
       T2 dH1 = cscale(Aeff, (T)-0.5 * t1);
       T2 dP2 = cscale(cadd(cscale(E, t2), cscale(phi, ia2)), (T)-0.5);
       T2 dd2 = cscale(del, -ia2);
-      double gp = (double)lPhiP1.x * dP1.x + (double)lPhiP1.y * dP1.y + (double)lPhiH1.x * dH1.x +
-                  (double)lPhiH1.y * dH1.y + (double)lPhiP2.x * dP2.x + (double)lPhiP2.y * dP2.y +
-                  (double)ldP2.x * dd2.x + (double)ldP2.y * dd2.y;
-      atomicAdd(&sgrad[bt], gp);
+      T gp = lPhiP1.x * dP1.x + lPhiP1.y * dP1.y + lPhiH1.x * dH1.x + lPhiH1.y * dH1.y + lPhiP2.x * dP2.x +
+             lPhiP2.y * dP2.y + ldP2.x * dd2.x + ldP2.y * dd2.y;
+      // J is a multiple of 32, so a warp holds one member: reduce over the warp
+      // in the compute type, accumulate the warp sums in FP64
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) gp += __shfl_xor_sync(0xffffffffu, gp, off);
+      if ((threadIdx.x & 31) == 0) atomicAdd(&sgrad[bt], (double)gp);
     }
   }
   __syncthreads();

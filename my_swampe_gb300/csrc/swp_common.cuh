@@ -189,6 +189,8 @@ struct Geom {
   const typename cplx<T>::type* twL;  // [L]   exp(-2 pi i k / L)
   const typename cplx<T>::type* twI;  // [L+1] exp(-2 pi i k / I)
   const T* dayc;           // [I]  dayside-mask * cos(lambda)
+  const T* ihalf;          // [J]  1 / (2 (1 - mu^2))
+  const T* coslat;         // [J]  sqrt(1 - mu^2)
 };
 
 // Step configuration shared by a launch.

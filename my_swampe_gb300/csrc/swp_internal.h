@@ -26,6 +26,8 @@ struct GroupGeom {
   size_t nbasis = 0, bytes = 0;
   void* mem = nullptr;
   double *mu = nullptr, *w = nullptr, *onemu2 = nullptr, *area = nullptr;
+  double *ihalf64 = nullptr, *coslat64 = nullptr;
+  float *ihalf32 = nullptr, *coslat32 = nullptr;
   int* boff = nullptr;
   double* b64[8] = {};
   float* b32[8] = {};
@@ -44,6 +46,7 @@ template <> inline Geom<double> GroupGeom::view<double>() const {
   g.Pw_f = b64[B_PW_F]; g.Hw_f = b64[B_HW_F]; g.P_f = b64[B_P_F]; g.H_f = b64[B_H_F];
   g.P_i = b64[B_P_I]; g.H_i = b64[B_H_I]; g.Pw_i = b64[B_PW_I]; g.Hw_i = b64[B_HW_I];
   g.twL = twL64; g.twI = twI64; g.dayc = dayc64;
+  g.ihalf = ihalf64; g.coslat = coslat64;
   return g;
 }
 template <> inline Geom<float> GroupGeom::view<float>() const {
@@ -53,6 +56,7 @@ template <> inline Geom<float> GroupGeom::view<float>() const {
   g.Pw_f = b32[B_PW_F]; g.Hw_f = b32[B_HW_F]; g.P_f = b32[B_P_F]; g.H_f = b32[B_H_F];
   g.P_i = b32[B_P_I]; g.H_i = b32[B_H_I]; g.Pw_i = b32[B_PW_I]; g.Hw_i = b32[B_HW_I];
   g.twL = twL32; g.twI = twI32; g.dayc = dayc32;
+  g.ihalf = ihalf32; g.coslat = coslat32;
   return g;
 }
 
@@ -60,6 +64,46 @@ int geometry_build(GroupGeom& gg, int M, cudaStream_t stream, std::string& err);
 int geometry_dense(const GroupGeom& gg, double* Pd, double* Hd, cudaStream_t stream);
 
 constexpr int MAXG = 4;
+
+// Per-call coefficient tables (coefs.cu): every factor of a step that depends
+// only on a member's parameters, and on n or the latitude, computed once per
+// call in FP64 with the reference's expressions and stored in the compute
+// type, so that the step kernels do no FP64 arithmetic of their own.
+//   nco[q][b][n]   q: hyperdiffusion sigma, sigmaPhi, sigma - 1, sigmaPhi - 1
+//                     (filters.py:95-151), a / (n(n+1)) (spectral_transform.py:577)
+//   jco[b][j]      tstepcoeff = 2 dt / (a (1 - mu_j^2)) (time_stepping.py:491-500)
+//   mco[q][b]      scalar factors of the tendencies (modEuler_tdiff.py, explicit_tdiff.py)
+enum NCoef { NC_SIG = 0, NC_SIGP, NC_SIGM1, NC_SIGPM1, NC_TC, NNCO };
+enum MCoef {
+  MC_DT = 0,   // dt
+  MC_T2,       // (2 dt / a^2) / 4
+  MC_IA2,      // 1 / a^2
+  MC_HPB,      // Phibar / 2
+  MC_DTPB,     // dt Phibar
+  MC_PBA2,     // Phibar / a^2
+  MC_PFD,      // (dt / 2) / a^2
+  MC_2DTPB,    // 2 dt Phibar
+  MC_2DT,      // 2 dt
+  MC_ITD,      // 1 / taudrag
+  MC_OM,       // omega / sqrt(0.375)  (the planetary-vorticity part of eta_{0,1})
+  MC_ALPHA,    // Robert-Asselin alpha
+  NMCO
+};
+template <typename T>
+struct CoefTables {
+  T* nco = nullptr;   // [NNCO][B][M+1]
+  T* jco = nullptr;   // [B][J]
+  T* mco = nullptr;   // [NMCO][B]
+  static size_t count(int M, int B, int J) { return (size_t)NNCO * B * (M + 1) + (size_t)B * J + (size_t)NMCO * B; }
+  void carve(T* base, int M, int B, int J) {
+    nco = base;
+    jco = nco + (size_t)NNCO * B * (M + 1);
+    mco = jco + (size_t)B * J;
+  }
+};
+template <typename T>
+cudaError_t launch_coefs(const double* par, const double* onemu2, int M, int B, int J, const CoefTables<T>& C,
+                         cudaStream_t s);
 
 // --------------------------------------------------------------- spectral ---
 template <typename T>
@@ -74,6 +118,9 @@ struct SpecGroup {
   typename cplx<T>::type* lam;          // adjoint Fourier fields (adjoint launches)
   const typename cplx<T>::type* lamY;   // adjoint of the K1 outputs (adjoint launches)
   double* grad;                         // [NGRAD][B] (adjoint launches)
+  const T* nco;                         // coefficient tables of the call (CoefTables)
+  const T* jco;
+  const T* mco;
 };
 
 template <typename T>
@@ -133,5 +180,15 @@ template <typename T> cudaError_t launch_spec_adj(const SpecLaunch<T>& L, int nb
 template <typename T> cudaError_t launch_grid(const GridLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s);
 void spec_set_attributes();
 void grid_set_attributes();
+
+// tensor-core Legendre kernel of the FP32 modified-Euler step (tc_legendre.cu)
+struct TcBasis { const float* p[MAXG]; };  // packed basis of each group
+size_t spec_tc_smem_bytes();
+size_t spec_tc_basis_floats();
+int spec_tc_members_per_cta();
+bool spec_tc_supported(int M);
+int pack_tc_basis(const GroupGeom& gg, float* out, cudaStream_t s);
+void spec_tc_set_attributes();
+cudaError_t launch_spec_tc(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err, cudaStream_t s);
 
 }  // namespace swp

@@ -130,6 +130,19 @@ class Engine:
     def _check(self, rc, what):
         _lib.check(rc, self._plan, what)
 
+    @property
+    def uses_tensor_cores(self) -> bool:
+        """True when the modified-Euler steps run the tcgen05 Legendre kernel."""
+        return bool(self.lib.swp_plan_uses_tensor_cores(self._plan))
+
+    def check_device_status(self) -> None:
+        """Synchronise and raise if a bounded device wait ran out since the last check."""
+        st = ctypes.c_int(0)
+        self._check(self.lib.swp_device_status(self._plan, ctypes.byref(st), self.stream), "device status")
+        if st.value:
+            raise RuntimeError("libswampe_gb300: a tensor-core kernel timed out waiting on the GPU; "
+                               "the step results since the last check are invalid")
+
     # ------------------------------------------------------------- geometry
     def geometry(self, g: int = 0) -> Dict[str, torch.Tensor]:
         """FP64 mus, w and dense Pmn, Hmn (J, M+1, N+1) built on the GPU."""

@@ -423,6 +423,7 @@ def run_model_scan(
     if T > 0:
         eng.forward(flags, t0=starttime_eff, nsteps=T, row0=0, diag=diag, hist=hist, write_prev_last=True)
     phys = eng.output_physical(flags)[0]
+    eng.check_device_status()
     last = _assemble_state(eng, phys, Rum, Rvm, batched)
     res: Dict[str, Any] = dict(static=static, t_seq=torch.arange(starttime_eff, tmax, dtype=torch.int32, device=dev),
                                last_state=last, starttime=starttime_eff)

@@ -7,7 +7,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("N,K", [(32, 64), (16, 8), (64, 64), (48, 32)])
+@pytest.mark.parametrize("N,K", [(32, 64), (16, 8), (64, 64), (48, 32), (64, 24)])
 def test_tc_gemm_selftest(cuda, N, K):
     import torch
     from my_swampe_gb300 import _lib

@@ -1,0 +1,115 @@
+"""The tcgen05 Legendre kernel of the FP32 modified-Euler step (M = 42) against
+the SIMT FP32 kernel and the FP64 path, through the C ABI.
+
+Both FP32 kernels carry the same incremental step form.  The SIMT kernel
+contracts FP32 operands (24 significant bits); the tensor-core one contracts
+in 3xTF32 (hi + lo, 11 bits each: about 22 significant bits per operand, FP32
+accumulation), which makes its error a few times larger: after 200 steps the
+SIMT path stays within 5e-6 (relative L2) of the FP64 path, the tensor-core
+path within 1.5e-5 (observed <= 6.3e-6, in delta, the smallest field)."""
+import os
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine(groups, precision, tc=True):
+    from my_swampe_gb300.engine import Engine
+
+    old = os.environ.get("SWP_NO_TC")
+    if tc:
+        os.environ.pop("SWP_NO_TC", None)
+    else:
+        os.environ["SWP_NO_TC"] = "1"
+    try:
+        return Engine(groups, precision)
+    finally:
+        if old is None:
+            os.environ.pop("SWP_NO_TC", None)
+        else:
+            os.environ["SWP_NO_TC"] = old
+
+
+def test_tensor_core_path_selection(cuda):
+    assert _engine([(42, 4)], "fast").uses_tensor_cores
+    assert _engine([(42, 4), (42, 9)], "fast").uses_tensor_cores
+    assert not _engine([(42, 4)], "fast", tc=False).uses_tensor_cores
+    assert not _engine([(42, 4)], "fp64").uses_tensor_cores
+    assert not _engine([(63, 4)], "fast").uses_tensor_cores
+    assert not _engine([(42, 4), (63, 4)], "fast").uses_tensor_cores
+
+
+def _run(eng, nsteps, seeds, modal=1):
+    from my_swampe_gb300 import workloads
+    from my_swampe_gb300.engine import RunFlagsC
+
+    ics = []
+    for g, seed in enumerate(seeds):
+        wl = workloads.forced_ensemble(eng, g=g, seed=seed)
+        workloads.apply_params(eng, g, wl["params"])
+        ics.append(wl["ics"])
+    flags = RunFlagsC()
+    flags.modalflag = modal
+    eng.init_state(ics, flags)
+    eng.forward(flags, t0=2, nsteps=nsteps)
+    out = [o.double() for o in eng.output_physical(flags)]
+    eng.check_device_status()
+    return out
+
+
+def _rel(a, b):
+    import torch
+
+    return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+
+
+@pytest.mark.parametrize("B", [8, 13])
+def test_tc_step_matches_simt_and_fp64(cuda, B):
+    """B = 13 leaves a ragged member tile (5 of 8)."""
+    nsteps = 200
+    tc = _engine([(42, B)], "fast")
+    assert tc.uses_tensor_cores
+    out_tc = _run(tc, nsteps, [21])
+    out_simt = _run(_engine([(42, B)], "fast", tc=False), nsteps, [21])
+    out_64 = _run(_engine([(42, B)], "fp64"), nsteps, [21])
+    for k, name in enumerate(("eta", "delta", "Phi", "U", "V")):
+        r_tc = _rel(out_tc[0][k], out_64[0][k])
+        r_simt = _rel(out_simt[0][k], out_64[0][k])
+        assert r_simt < 5e-6, (name, r_tc, r_simt)
+        assert r_tc < 1.5e-5, (name, r_tc, r_simt)
+        assert _rel(out_tc[0][k], out_simt[0][k]) < 1.5e-5, name
+
+
+def test_tc_step_two_groups_one_launch(cuda):
+    """Two M = 42 groups with different member counts in one launch match
+    each group run on its own."""
+    import torch
+
+    both = _run(_engine([(42, 5), (42, 11)], "fast"), 40, [3, 4])
+    a = _run(_engine([(42, 5)], "fast"), 40, [3])
+    b = _run(_engine([(42, 11)], "fast"), 40, [4])
+    for k in range(5):
+        assert torch.equal(both[0][k], a[0][k])
+        assert torch.equal(both[1][k], b[0][k])
+
+
+def test_tc_step_with_diagnostics_matches_fp64(cuda):
+    """The reference driver (blow-up gate, RMS winds, history) on the FP32
+    tensor-core path against the FP64 path."""
+    import numpy as np
+
+    from conftest import FIXTURE_CASES
+    from my_swampe_gb300 import run_model_scan
+
+    kw = dict(FIXTURE_CASES["reference_case_forced_default"])
+    kw.update(tmax=30)
+    f64 = run_model_scan(**kw, diagnostics=True, jit_scan=False)
+    f32 = run_model_scan(**kw, diagnostics=True, jit_scan=False, precision="fast")
+    assert f32["outs"]["rms"].shape == f64["outs"]["rms"].shape
+    for name in ("Phi", "U"):
+        got = getattr(f32["last_state"], name + "_curr").double().cpu().numpy()
+        want = getattr(f64["last_state"], name + "_curr").cpu().numpy()
+        assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-5, name
+    np.testing.assert_allclose(f32["outs"]["rms"].cpu().numpy(), f64["outs"]["rms"].cpu().numpy(), rtol=1e-5)
+    np.testing.assert_array_equal(f32["outs"]["dead"].cpu().numpy(), f64["outs"]["dead"].cpu().numpy())
