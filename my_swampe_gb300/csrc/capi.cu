@@ -570,14 +570,9 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
     int mt = 8;
     while (mt > 1 && (f64 ? spec_smem_bytes<double>(M[g], J, mt) : spec_smem_bytes<float>(M[g], J, mt)) > cap) mt /= 2;
     p->MT[g] = std::min(mt, B[g]);
-    // rows per grid CTA: 4 keeps several CTAs per SM resident; smaller when the
-    // largest mode (the adjoint, 12 transforms per row) would not fit
-    int jb = 4;
-    size_t gcap = 200 * 1024;
-    while (jb > 1 && ((J % jb) != 0 ||
-                      (f64 ? grid_smem_bytes<double>(M[g], J, I, jb, GM_ADJ_STEP)
-                           : grid_smem_bytes<float>(M[g], J, I, jb, GM_ADJ_STEP)) > gcap))
-      jb /= 2;
+    // rows per grid CTA, fixed per truncation at compile time: 4 keeps several
+    // CTAs per SM resident; 2 where the adjoint's 12 transforms per row would not fit
+    int jb = grid_rows_per_cta(M[g], f64);
     p->JB[g] = jb;
     size_t ss = f64 ? spec_smem_bytes<double>(M[g], J, p->MT[g]) : spec_smem_bytes<float>(M[g], J, p->MT[g]);
     p->spec_smem = std::max(p->spec_smem, ss);

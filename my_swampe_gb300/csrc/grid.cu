@@ -163,12 +163,15 @@ struct PhysicsAdj {
   }
 };
 
-// Per-CTA context shared by the mode bodies.
-template <typename T>
+// Per-CTA context shared by the mode bodies.  The grid sizes are compile-time
+// (one instantiation per truncation), so every index division in the hot
+// loops is by a constant.
+template <typename T, int M_, int JB_>
 struct GridCtx {
   typedef typename cplx<T>::type T2;
+  static constexpr int M = M_, J = trunc_J(M_), I = trunc_I(M_), L = I / 2, LS = L + 1, JB = JB_;
   const GridGroup<T>* G;
-  int M, J, I, L, LS, JB, B, b, j0;
+  int B, b, j0;
   size_t FS, PS;
   T2* bufA;
   T2* bufB;
@@ -179,39 +182,39 @@ struct GridCtx {
 
 // Stage the rows j0..j0+JB-1 of `nf` Fourier fields of member b into `stage`
 // ([f][m][r], r fastest; global reads are JB-long contiguous runs).
-template <typename T>
-__device__ __forceinline__ void stage_rows(const GridCtx<T>& c, const typename cplx<T>::type* const* src, int nf,
+template <typename T, typename C>
+__device__ __forceinline__ void stage_rows(const C& c, const typename cplx<T>::type* const* src, int nf,
                                            typename cplx<T>::type* stage) {
-  const int n1 = c.M + 1;
-  for (int t = threadIdx.x; t < nf * n1 * c.JB; t += blockDim.x) {
-    int r = t % c.JB, k = (t / c.JB) % n1, f = t / (c.JB * n1);
-    stage[t] = src[f][((size_t)k * c.B + c.b) * c.J + c.j0 + r];
+  const int n1 = C::M + 1;
+  for (int t = threadIdx.x; t < nf * n1 * C::JB; t += blockDim.x) {
+    int r = t % C::JB, k = (t / C::JB) % n1, f = t / (C::JB * n1);
+    stage[t] = src[f][((size_t)k * c.B + c.b) * C::J + c.j0 + r];
   }
 }
 
 // Z spectra of the C2R transforms of the staged rows: out[(f*JB + r)*LS + k].
-template <typename T>
-__device__ __forceinline__ void build_c2r(const GridCtx<T>& c, const typename cplx<T>::type* stage, int nf,
+template <typename T, typename C>
+__device__ __forceinline__ void build_c2r(const C& c, const typename cplx<T>::type* stage, int nf,
                                           const T* scale0, const T* scale, typename cplx<T>::type* out) {
-  const int n1 = c.M + 1;
-  for (int t = threadIdx.x; t < nf * c.JB * c.L; t += blockDim.x) {
-    int k = t % c.L, fr = t / c.L, r = fr % c.JB, f = fr / c.JB;
-    out[(size_t)fr * c.LS + k] = c2r_pre<typename cplx<T>::type, T>(stage + (size_t)f * n1 * c.JB + r, c.JB, c.M, c.L, k,
+  const int n1 = C::M + 1;
+  for (int t = threadIdx.x; t < nf * C::JB * C::L; t += blockDim.x) {
+    int k = t % C::L, fr = t / C::L, r = fr % C::JB, f = fr / C::JB;
+    out[(size_t)fr * C::LS + k] = c2r_pre<typename cplx<T>::type, T>(stage + (size_t)f * n1 * C::JB + r, C::JB, C::M, C::L, k,
                                                                     c.G->g.twI, scale0[f], scale[f]);
   }
 }
 
 // Truncated R2C bins of `nf` transforms in `res` (stride LS) written to global
 // Fourier fields dst[f] (r fastest).  Bin scale: k == 0 ? s0 : s.
-template <typename T>
-__device__ __forceinline__ void write_r2c(const GridCtx<T>& c, const typename cplx<T>::type* res, int nf,
+template <typename T, typename C>
+__device__ __forceinline__ void write_r2c(const C& c, const typename cplx<T>::type* res, int nf,
                                           typename cplx<T>::type* const* dst, T s0, T s) {
-  const int n1 = c.M + 1;
-  for (int t = threadIdx.x; t < nf * n1 * c.JB; t += blockDim.x) {
-    int r = t % c.JB, k = (t / c.JB) % n1, q = t / (c.JB * n1);
-    typename cplx<T>::type v = r2c_post<typename cplx<T>::type, T>(res + ((size_t)q * c.JB + r) * c.LS, c.L, k,
+  const int n1 = C::M + 1;
+  for (int t = threadIdx.x; t < nf * n1 * C::JB; t += blockDim.x) {
+    int r = t % C::JB, k = (t / C::JB) % n1, q = t / (C::JB * n1);
+    typename cplx<T>::type v = r2c_post<typename cplx<T>::type, T>(res + ((size_t)q * C::JB + r) * C::LS, C::L, k,
                                                                      c.G->g.twI, k == 0 ? s0 : s);
-    dst[q][((size_t)k * c.B + c.b) * c.J + c.j0 + r] = v;
+    dst[q][((size_t)k * c.B + c.b) * C::J + c.j0 + r] = v;
   }
 }
 
@@ -226,30 +229,30 @@ __device__ void block_add_grads(const T* gacc, double* sred, double* grad, int B
   if (threadIdx.x < NGRAD && grad) atomicAdd(&grad[threadIdx.x * B + b], sred[threadIdx.x]);
 }
 
-template <typename T, int MODE>
-__global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch<T> Lc) {
+template <typename T, int MODE, int MM, int JBB>
+__device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGroup<T>& G, int idx) {
   typedef typename cplx<T>::type T2;
+  typedef GridCtx<T, MM, JBB> Ctx;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  int idx;
-  const GridGroup<T>& G = pick_ggroup(Lc, idx);
   const StepCfg& cfg = Lc.cfg;
-  GridCtx<T> c;
+  constexpr int J = Ctx::J, I = Ctx::I, L = Ctx::L, LS = Ctx::LS, JB = Ctx::JB, M = Ctx::M;
+  Ctx c;
   c.G = &G;
-  c.M = G.g.M; c.J = G.g.J; c.I = G.g.I; c.L = G.g.L; c.LS = c.L + 1; c.JB = G.JB; c.B = G.B;
-  c.b = idx / G.njb;
-  c.j0 = (idx % G.njb) * c.JB;
-  c.FS = (size_t)(c.M + 1) * G.B * c.J;
-  c.PS = (size_t)G.B * c.J * c.I;
+  c.B = G.B;
+  c.b = idx / (J / JB);
+  c.j0 = (idx % (J / JB)) * JB;
+  c.FS = (size_t)(M + 1) * G.B * J;
+  c.PS = (size_t)G.B * J * I;
   constexpr int NTR = grid_ntr(MODE);
   c.bufA = (T2*)smem_raw;
-  c.bufB = c.bufA + (size_t)NTR * c.JB * c.LS;
-  c.sday = (T*)(c.bufB + (size_t)NTR * c.JB * c.LS);
-  c.sred = (double*)(((uintptr_t)(c.sday + c.I) + 15) & ~(uintptr_t)15);
-  c.invI = (T)(1.0 / c.I);
-  for (int i = threadIdx.x; i < c.I; i += blockDim.x) c.sday[i] = G.g.dayc[i];
+  c.bufB = c.bufA + (size_t)NTR * JB * LS;
+  c.sday = (T*)(c.bufB + (size_t)NTR * JB * LS);
+  c.sred = (double*)(((uintptr_t)(c.sday + I) + 15) & ~(uintptr_t)15);
+  c.invI = (T)1 / (T)I;
+  for (int i = threadIdx.x; i < I; i += blockDim.x) c.sday[i] = G.g.dayc[i];
   if (threadIdx.x == 0) { c.sred[0] = 0.0; c.sred[1] = 1e300; c.sred[2] = 1e300; c.sred[3] = -1e300; }
 
-  const int B = G.B, b = c.b, J = c.J, I = c.I, L = c.L, LS = c.LS, JB = c.JB, M = c.M, j0 = c.j0;
+  const int B = G.B, b = c.b, j0 = c.j0;
   const size_t FS = c.FS, PS = c.PS;
   const Geom<T>& g = G.g;
   double Pb = G.par[P_PHIBAR * B + b], tr = G.par[P_TAURAD * B + b];
@@ -306,7 +309,7 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
     __syncthreads();
     build_c2r<T>(c, bufB, nf, one, one, bufA);
     __syncthreads();
-    T2* zin = cfft_batch<+1>(bufA, bufB, L, LS, nf * JB, g.twL);
+    T2* zin = cfft_batch_c<+1, L>(bufA, bufB, nf * JB, g.twL);
     T2* zout = (zin == bufA) ? bufB : bufA;
     // initial-condition residual (non-zero only before a member's first step and
     // for the fixed test-1 winds): added in shared memory, off the hot loop
@@ -413,7 +416,7 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
       atomic_max_d(&dc[D_PHIMAX * B + b], c.sred[3]);
     }
     const int nout = ph.forced ? 8 : 5;
-    T2* res = cfft_batch<-1>(zout, zin, L, LS, nout * JB, g.twL);
+    T2* res = cfft_batch_c<-1, L>(zout, zin, nout * JB, g.twL);
     T2* dst[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) dst[q] = G.four + (F_A + q) * FS;
@@ -430,7 +433,7 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
       bufA[(size_t)fr * LS + n] = mk<T2>(x[0], x[1]);
     }
     __syncthreads();
-    T2* res = cfft_batch<-1>(bufA, bufB, L, LS, 2 * JB, g.twL);
+    T2* res = cfft_batch_c<-1, L>(bufA, bufB, 2 * JB, g.twL);
     T2* dst[2] = {G.four + F_ETA * FS, G.four + F_DELTA * FS};
     write_r2c<T>(c, res, 2, dst, invI, invI);
     return;
@@ -447,7 +450,7 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
       bufA[(size_t)fr * LS + n] = mk<T2>(x[0], x[1]);
     }
     __syncthreads();
-    T2* res = cfft_batch<-1>(bufA, bufB, L, LS, nf * JB, g.twL);
+    T2* res = cfft_batch_c<-1, L>(bufA, bufB, nf * JB, g.twL);
     T2* other = (res == bufA) ? bufB : bufA;
     const int n1 = M + 1;
     // unpack into global and keep the truncated rows in `other` ([f][m][r])
@@ -468,7 +471,7 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
     T one[5] = {(T)1, (T)1, (T)1, (T)1, (T)1};
     build_c2r<T>(c, other, nf, one, one, res);
     __syncthreads();
-    T2* zr = cfft_batch<+1>(res, other, L, LS, nf * JB, g.twL);
+    T2* zr = cfft_batch_c<+1, L>(res, other, nf * JB, g.twL);
     for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
       int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
       size_t po = f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
@@ -514,7 +517,7 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
       atomicAdd(&G.diag[D_RMS2 * B + b], c.sred[0]);
       atomic_min_d(&G.diag[D_SPIN * B + b], c.sred[1]);
     }
-    T2* res2 = cfft_batch<-1>(bufA, bufB, L, LS, nout * JB, g.twL);
+    T2* res2 = cfft_batch_c<-1, L>(bufA, bufB, nout * JB, g.twL);
     T2* dst[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) dst[q] = G.four + (F_A + q) * FS;
@@ -546,7 +549,7 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
     __syncthreads();
     build_c2r<T>(c, bufB, nb1, s0, s1, bufA);
     __syncthreads();
-    T2* zin = cfft_batch<+1>(bufA, bufB, L, LS, nb1 * JB, g.twL);
+    T2* zin = cfft_batch_c<+1, L>(bufA, bufB, nb1 * JB, g.twL);
     T2* zout = (zin == bufA) ? bufB : bufA;
     T gacc[NGRAD] = {(T)0, (T)0, (T)0, (T)0};
     for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
@@ -591,7 +594,7 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
     block_add_grads<T>(gacc, c.sred, G.grad, B, b);
     if (MODE == GM_ADJ_STEP) {
       // adjoint of x = Re(Y_0) + 2 Re sum_{m>=1} Y_m e^{i theta}:  lambda Y_m = c_m sum_i lambda x_i e^{-i theta}
-      T2* res = cfft_batch<-1>(zout, zin, L, LS, 4 * JB, g.twL);
+      T2* res = cfft_batch_c<-1, L>(zout, zin, 4 * JB, g.twL);
       const int n1 = M + 1;
       const int yf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
       const int rmap[5] = {0, -1, 1, 2, 3};
@@ -615,7 +618,7 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
     __syncthreads();
     build_c2r<T>(c, bufB, 5, s20, s21, bufA);
     __syncthreads();
-    T2* z2 = cfft_batch<+1>(bufA, bufB, L, LS, 5 * JB, g.twL);
+    T2* z2 = cfft_batch_c<+1, L>(bufA, bufB, 5 * JB, g.twL);
     for (int t = threadIdx.x; t < 5 * JB * L; t += blockDim.x) {
       int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
       size_t po = f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
@@ -636,12 +639,32 @@ __global__ void __launch_bounds__(256) k_grid(const __grid_constant__ GridLaunch
       bufA[(size_t)fr * LS + n] = mk<T2>(x[0], x[1]);
     }
     __syncthreads();
-    T2* res = cfft_batch<-1>(bufA, bufB, L, LS, nf * JB, g.twL);
+    T2* res = cfft_batch_c<-1, L>(bufA, bufB, nf * JB, g.twL);
     T2* dst[5] = {G.lam + F_ETA * FS, G.lam + F_DELTA * FS, G.lam + F_PHI * FS, G.lam + F_U * FS, G.lam + F_V * FS};
     write_r2c<T>(c, res, nf, dst, (T)1, (T)2);
     return;
   }
 }
+
+// JB (latitude rows per CTA) of each truncation: 4, or 2 where the adjoint
+// step's 12 transforms per row would not fit in 200 KB of shared memory.
+template <typename T>
+__host__ __device__ constexpr int grid_jb(int M) {
+  return (size_t)2 * grid_ntr(GM_ADJ_STEP) * 4 * (trunc_I(M) / 2 + 1) * 2 * sizeof(T) <= 200 * 1024 ? 4 : 2;
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_grid(const __grid_constant__ GridLaunch<T> Lc) {
+  int idx;
+  const GridGroup<T>& G = pick_ggroup(Lc, idx);
+  switch (G.g.M) {  // groups of different truncations share one launch
+    case 42: grid_body<T, MODE, 42, grid_jb<T>(42)>(Lc, G, idx); break;
+    case 63: grid_body<T, MODE, 63, grid_jb<T>(63)>(Lc, G, idx); break;
+    default: grid_body<T, MODE, 106, grid_jb<T>(106)>(Lc, G, idx); break;
+  }
+}
+
+int grid_rows_per_cta(int M, bool fp64) { return fp64 ? grid_jb<double>(M) : grid_jb<float>(M); }
 
 template <typename T, int MODE>
 static void set_attr_one() {

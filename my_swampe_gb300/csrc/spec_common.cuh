@@ -58,29 +58,28 @@ __device__ __forceinline__ void load_spec_coefs(const SpecGroup<T>& G, bool diff
 // explicit_tdiff.py:62-78, 134-155, 207-226), grouped by the basis (Pw or Hw)
 // and by the output factor (1 or n(n+1)) they are applied with.  mode 2 is the
 // plain transform of eta, delta used to diagnose winds (model.py:644-666).
-template <typename T>
-__device__ __forceinline__ void step_combos(const SpecGroup<T>& G, const StepCfg& cfg, int mode, bool incr, int m,
-                                            int b, int j, size_t FS, typename cplx<T>::type* c) {
+// `ld(f)` returns Fourier field f at the point (from global memory or a staged copy).
+template <typename T, typename LD>
+__device__ __forceinline__ void step_combos_ld(const SpecGroup<T>& G, const StepCfg& cfg, int mode, bool incr, int m,
+                                               int b, int j, LD ld, typename cplx<T>::type* c) {
   typedef typename cplx<T>::type T2;
   constexpr int NSPX = SlotCount<T>::NP;
   constexpr int NSLOT = NSPX + NSH;
   const Geom<T>& g = G.g;
-  const T2* F = G.four;
   const T* mc = G.mco;
   const int B = G.B;
   const T xm = (T)m;
-  const size_t o = ((size_t)m * G.B + b) * g.J + j;
   const T tsc = G.jco[(size_t)b * g.J + j];           // tstepcoeff
   T2 z = mk<T2>(0, 0);
 #pragma unroll
   for (int q = 0; q < NSLOT; ++q) c[q] = z;
   if (mode == 2) {  // diagnose winds: plain forward transforms of eta, delta
-    c[SP_E1] = F[F_ETA * FS + o];
-    c[SP_D1] = F[F_DELTA * FS + o];
+    c[SP_E1] = ld(F_ETA);
+    c[SP_D1] = ld(F_DELTA);
   } else if (cfg.scheme == 0) {
-    T2 eta = F[F_ETA * FS + o], del = F[F_DELTA * FS + o], phi = F[F_PHI * FS + o];
-    T2 A = F[F_A * FS + o], Bm = F[F_B * FS + o], C = F[F_C * FS + o], D = F[F_D * FS + o];
-    T2 E = F[F_E * FS + o], PF = F[F_PHIF * FS + o], Fm = F[F_F * FS + o], Gm = F[F_G * FS + o];
+    T2 eta = ld(F_ETA), del = ld(F_DELTA), phi = ld(F_PHI);
+    T2 A = ld(F_A), Bm = ld(F_B), C = ld(F_C), D = ld(F_D);
+    T2 E = ld(F_E), PF = ld(F_PHIF), Fm = ld(F_F), Gm = ld(F_G);
     T t1 = tsc * (T)0.25, t2 = mc[MC_T2 * B + b];
     T ia2 = mc[MC_IA2 * B + b];
     T hPb = mc[MC_HPB * B + b];
@@ -109,11 +108,11 @@ __device__ __forceinline__ void step_combos(const SpecGroup<T>& G, const StepCfg
     c[NSPX + SH_E1] = cscale(Beff, te);
     if (incr) { c[SP_IPHI] = phi; c[SP_ID] = del; c[SP_IE] = eta; }
   } else {
-    T2 eta0 = F[F_ETA_PREV * FS + o], del0 = F[F_DELTA_PREV * FS + o], phi0 = F[F_PHI_PREV * FS + o];
-    T2 del1 = F[F_DELTA * FS + o];
-    T2 A = F[F_A * FS + o], Bm = F[F_B * FS + o], C = F[F_C * FS + o], D = F[F_D * FS + o];
-    T2 PF = F[F_PHIF * FS + o], Fm = F[F_F * FS + o], Gm = F[F_G * FS + o];
-    T2 U = F[F_U * FS + o], V = F[F_V * FS + o];
+    T2 eta0 = ld(F_ETA_PREV), del0 = ld(F_DELTA_PREV), phi0 = ld(F_PHI_PREV);
+    T2 del1 = ld(F_DELTA);
+    T2 A = ld(F_A), Bm = ld(F_B), C = ld(F_C), D = ld(F_D);
+    T2 PF = ld(F_PHIF), Fm = ld(F_F), Gm = ld(F_G);
+    T2 U = ld(F_U), V = ld(F_V);
     T t = tsc;
     T itd = mc[MC_ITD * B + b];
     // Phi (explicit_tdiff.py:62-78)
@@ -142,6 +141,55 @@ __device__ __forceinline__ void step_combos(const SpecGroup<T>& G, const StepCfg
     }
     c[SP_E1] = e1;
     c[NSPX + SH_E1] = eh;
+  }
+}
+
+// step_combos_ld on the state in global memory
+template <typename T>
+__device__ __forceinline__ void step_combos(const SpecGroup<T>& G, const StepCfg& cfg, int mode, bool incr, int m,
+                                            int b, int j, size_t FS, typename cplx<T>::type* c) {
+  const typename cplx<T>::type* F = G.four;
+  const size_t o = ((size_t)m * G.B + b) * G.g.J + j;
+  step_combos_ld<T>(G, cfg, mode, incr, m, b, j, [&](int f) { return F[f * FS + o]; }, c);
+}
+
+// Write-out of one (member, latitude) point of a step at column m: the new curr
+// eta, delta, Phi (incremental form: old + increment), the prev carry, the
+// Robert-Asselin mid carry (model.py:988-1110) and the winds.  All loads come
+// before the first store: the input and output states may be one buffer, so
+// the compiler could not reorder them itself.
+template <typename T>
+__device__ __forceinline__ void write_step_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
+                                                 size_t o, T al, const typename cplx<T>::type* nw_in, bool uv,
+                                                 typename cplx<T>::type u, typename cplx<T>::type v) {
+  typedef typename cplx<T>::type T2;
+  const T2* Fi = G.four;
+  T2* Fo = G.four_out;
+  const int cf[3] = {F_ETA, F_DELTA, F_PHI};
+  const int pf[3] = {F_ETA_PREV, F_DELTA_PREV, F_PHI_PREV};
+  const int rf[3] = {F_ETA_MID, F_DELTA_MID, F_PHI_MID};
+  const bool need_old = incr || cfg.write_prev || cfg.ra_mode;
+  T2 old[3], mid[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    old[q] = need_old ? Fi[cf[q] * FS + o] : mk<T2>(0, 0);
+    mid[q] = cfg.ra_mode == 2 ? Fi[rf[q] * FS + o] : mk<T2>(0, 0);
+  }
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    T2 nw = nw_in[q];
+    if (incr) nw = cadd(old[q], nw);
+    if (cfg.write_prev) Fo[pf[q] * FS + o] = old[q];
+    if (cfg.ra_mode == 1) Fo[rf[q] * FS + o] = old[q];
+    else if (cfg.ra_mode == 2) {
+      const T2 d = cadd(csub(mid[q], cscale(old[q], (T)2)), nw);
+      Fo[rf[q] * FS + o] = cadd(old[q], cscale(d, al));
+    }
+    Fo[cf[q] * FS + o] = nw;
+  }
+  if (uv) {
+    Fo[F_U * FS + o] = u;
+    Fo[F_V * FS + o] = v;
   }
 }
 

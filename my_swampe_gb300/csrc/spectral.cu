@@ -313,8 +313,6 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
   __syncthreads();
 
   // ---- phase 6: write-out and carries (coalesced along j)
-  T2* Fo = G.four_out;
-  const T2* Fi = G.four;
   const int do_uv = (mode == 2) || (cfg.test != 1);
   for (int t = threadIdx.x; t < MT * J; t += blockDim.x) {
     int bt = t / J, j = t % J;
@@ -323,34 +321,12 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
     size_t o = ((size_t)m * G.B + b) * J + j;
     auto get = [&](int f) { return mk<T2>(Out[(((size_t)f * MT + bt) * J + j) * 2], Out[(((size_t)f * MT + bt) * J + j) * 2 + 1]); };
     if (mode == 2) {
-      Fo[F_U * FS + o] = get(3);
-      Fo[F_V * FS + o] = get(4);
+      G.four_out[F_U * FS + o] = get(3);
+      G.four_out[F_V * FS + o] = get(4);
       continue;
     }
-    const T aa = G.mco[MC_ALPHA * G.B + b];
-    const int cf[3] = {F_ETA, F_DELTA, F_PHI};
-    const int pf[3] = {F_ETA_PREV, F_DELTA_PREV, F_PHI_PREV};
-    const int rf[3] = {F_ETA_MID, F_DELTA_MID, F_PHI_MID};
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      T2 nw = get(q);
-      if (incr || cfg.write_prev || cfg.ra_mode) {
-        T2 old = Fi[cf[q] * FS + o];
-        if (incr) nw = cadd(old, nw);
-        if (cfg.write_prev) Fo[pf[q] * FS + o] = old;
-        if (cfg.ra_mode == 1) Fo[rf[q] * FS + o] = old;
-        else if (cfg.ra_mode == 2) {
-          T2 mid = Fi[rf[q] * FS + o];
-          T2 d = cadd(csub(mid, cscale(old, (T)2)), nw);
-          Fo[rf[q] * FS + o] = cadd(old, cscale(d, aa));
-        }
-      }
-      Fo[cf[q] * FS + o] = nw;
-    }
-    if (do_uv) {
-      Fo[F_U * FS + o] = get(3);
-      Fo[F_V * FS + o] = get(4);
-    }
+    const T2 nw[3] = {get(0), get(1), get(2)};
+    write_step_point<T>(G, cfg, incr, FS, o, G.mco[MC_ALPHA * G.B + b], nw, do_uv != 0, get(3), get(4));
   }
   // residual weights of the initial condition in the physical curr / prev fields
   if (mode == 0 && m == 0 && threadIdx.x < mt && !sdead[threadIdx.x]) {

@@ -167,6 +167,58 @@ __device__ T2* cfft_batch(T2* a, T2* b, int L, int ls, int ntr, const T2* tw) {
   }
 }
 
+// Compile-time-length variant of the above (ls = L + 1): every index division
+// is by a constant.
+template <int R, int SIGN, int L, int NS, typename T2>
+__device__ __forceinline__ void stockham_pass_c(const T2* __restrict__ in, T2* __restrict__ out, int ntr,
+                                                const T2* __restrict__ tw) {
+  constexpr int LS = L + 1, PER = L / R, TWS = L / (NS * R);
+  const int tasks = ntr * PER;
+  for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+    const int t = task / PER, j = task - t * PER;
+    const T2* src = in + t * LS;
+    T2* dst = out + t * LS;
+    const int jm = j % NS;
+    T2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = src[j + r * PER];
+#pragma unroll
+    for (int r = 1; r < R; ++r) {
+      const T2 w = tw[jm * r * TWS];
+      v[r] = (SIGN < 0) ? cmul(v[r], w) : cmulc(v[r], w);
+    }
+    dftR<R, SIGN>(v);
+    const int idx = (j / NS) * NS * R + jm;
+#pragma unroll
+    for (int r = 0; r < R; ++r) dst[idx + r * NS] = v[r];
+  }
+}
+
+template <int SIGN, int L, typename T2>
+__device__ __forceinline__ T2* cfft_batch_c(T2* a, T2* b, int ntr, const T2* tw) {
+  static_assert(L == 64 || L == 96 || L == 160, "transform length");
+  if (L == 64) {
+    stockham_pass_c<8, SIGN, L, 1>(a, b, ntr, tw); __syncthreads();
+    stockham_pass_c<8, SIGN, L, 8>(b, a, ntr, tw); __syncthreads();
+    return a;
+  } else if (L == 96) {
+    stockham_pass_c<8, SIGN, L, 1>(a, b, ntr, tw); __syncthreads();
+    stockham_pass_c<4, SIGN, L, 8>(b, a, ntr, tw); __syncthreads();
+    stockham_pass_c<3, SIGN, L, 32>(a, b, ntr, tw); __syncthreads();
+    return b;
+  } else {
+    stockham_pass_c<8, SIGN, L, 1>(a, b, ntr, tw); __syncthreads();
+    stockham_pass_c<4, SIGN, L, 8>(b, a, ntr, tw); __syncthreads();
+    stockham_pass_c<5, SIGN, L, 32>(a, b, ntr, tw); __syncthreads();
+    return b;
+  }
+}
+
+// Gauss grid of each supported truncation (the reference's M -> (J, I) table,
+// spectral_transform.py / model.py: 42 -> 64 x 128, 63 -> 96 x 192, 106 -> 160 x 320).
+__host__ __device__ constexpr int trunc_J(int M) { return M == 42 ? 64 : M == 63 ? 96 : 160; }
+__host__ __device__ constexpr int trunc_I(int M) { return 2 * trunc_J(M); }
+
 // ------------------------------------------------------------- descriptors ---
 // Geometry for one truncation, built on the device in FP64 (geometry.cu) and
 // rounded to the compute type.  Basis blocks are packed per zonal wavenumber m

@@ -54,6 +54,18 @@ static_assert(TC_NOUT * TC_MT * TC_OST <= TC_A, "output staging must fit in the 
 // the MMA reads all 128 rows of the last A2 operand: they must stay in the A region
 static_assert(3 * TC_A2 + TC_ROWS * TC_K2 <= TC_A, "A2 over-read must stay in the A region");
 static_assert(TC_B2 <= TC_B1, "B2 reuses the B1 buffer");
+// inputs of a modified-Euler step, staged by bulk copies at the start of the A region
+constexpr int TC_NIN = 11;
+static_assert(TC_NIN * TC_MT * TC_J * 2 <= TC_A, "staged inputs must fit in the A region");
+__host__ __device__ constexpr int stage_field(int q) {  // staged slot -> Fourier field
+  return q == 0 ? F_ETA : q == 1 ? F_DELTA : q == 2 ? F_PHI : F_A + (q - 3);
+}
+// Fourier field -> staged slot, for the fields stage_field covers (F_A..F_G are
+// consecutive); any other field is never read by the modified-Euler combination
+__host__ __device__ constexpr int stage_slot(int f) {
+  return f == F_ETA ? 0 : f == F_DELTA ? 1 : f == F_PHI ? 2 : (f >= F_A && f <= F_G) ? f - F_A + 3 : 0;
+}
+static_assert(F_G - F_A + 4 == TC_NIN, "staged fields");
 
 // slots of forward group g (compile-time, so that the slot arrays stay in registers)
 __host__ __device__ constexpr int group_p(int g) {
@@ -144,8 +156,12 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   const int cnt = TC_CNT - m, C0 = (cnt + 1) / 2, C1 = cnt / 2;
   const size_t FS = (size_t)TC_CNT * G.B * J;
   const bool incr = cfg.incremental != 0;
+  if (cfg.scheme != 0 || L.mode != 0) {  // the host launches this kernel for modified-Euler steps only
+    if (threadIdx.x == 0) atomicExch(err, 2);
+    return;
+  }
 
-  float* sA = (float*)smem_raw;            // A1 | A2 + D1 staging | output staging
+  float* sA = (float*)smem_raw;            // staged inputs | A1 | A2 + D1 staging | output staging
   float* sB = sA + TC_A;                   // B1, then B2
   float* sRes = sA + TC_RES0;
   float* sig = sB + TC_B1;                 // [MT][CNT] x 5
@@ -153,26 +169,39 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   float* sigm1 = sigP + TC_MT * TC_CNT;
   float* sigPm1 = sigm1 + TC_MT * TC_CNT;
   float* tcmn = sigPm1 + TC_MT * TC_CNT;
-  uint64_t* mbar = (uint64_t*)(((uintptr_t)(tcmn + TC_MT * TC_CNT) + 15) & ~(uintptr_t)15);  // [3]
-  uint32_t* tslot = (uint32_t*)(mbar + 3);
+  // [4]: 0 basis copies, 1 GEMM1 commits, 2 GEMM2 commit, 3 input copies
+  uint64_t* mbar = (uint64_t*)(((uintptr_t)(tcmn + TC_MT * TC_CNT) + 15) & ~(uintptr_t)15);
+  uint32_t* tslot = (uint32_t*)(mbar + 4);
   int* sflag = (int*)(tslot + 1);
   int* sdead = sflag + 1;                  // [MT]
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // what thread 0 has issued, for the bounded drain on failure
-  int n_tma = 0, n_c1 = 0, n_c2 = 0;
+  int n_tma = 0, n_in = 0, n_c1 = 0, n_c2 = 0;
 
-  // ---- phase 0: TMEM, barriers, first basis copy, per-member coefficients, blow-up gate
+  // ---- phase 0: barriers; bulk copies of the tile's inputs (one contiguous block
+  // of mt x J values per field) and of the forward basis; TMEM; coefficients; blow-up gate
+  if (threadIdx.x == 0) {
+    *sflag = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) tc::mbar_init(&mbar[q], 1);
+    tc::fence_mbar_init();
+    const uint32_t row_bytes = (uint32_t)(mt * J * sizeof(T2));
+    tc::mbar_expect_tx(&mbar[3], row_bytes * TC_NIN);
+#pragma unroll
+    for (int q = 0; q < TC_NIN; ++q) {
+      const int f = stage_field(q);
+      tc::bulk_g2s(sA + (size_t)q * TC_MT * J * 2, G.four + (size_t)f * FS + ((size_t)m * G.B + b0) * J, row_bytes,
+                   &mbar[3]);
+    }
+    n_in = 1;
+    tc::mbar_expect_tx(&mbar[0], (uint32_t)(TC_B1 * sizeof(float)));
+    tc::bulk_g2s(sB, gbasis + (size_t)m * TC_BLOCK, (uint32_t)(TC_B1 * sizeof(float)), &mbar[0]);
+    n_tma = 1;
+  }
   if (warp == 0) {
     tc::tmem_alloc(tslot, TC_TMEM_COLS);
     tc::tmem_relinquish();
-  }
-  if (threadIdx.x == 0) {
-    *sflag = 0;
-    tc::mbar_init(&mbar[0], 1);
-    tc::mbar_init(&mbar[1], 1);
-    tc::mbar_init(&mbar[2], 1);
-    tc::fence_mbar_init();
   }
   load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, TC_MT, cnt, TC_CNT, sig, sigP, sigm1, sigPm1, tcmn);
   if (threadIdx.x < TC_MT) {
@@ -193,34 +222,36 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
-  if (threadIdx.x == 0) {
-    tc::mbar_expect_tx(&mbar[0], (uint32_t)(TC_B1 * sizeof(float)));
-    tc::bulk_g2s(sB, gbasis + (size_t)m * TC_BLOCK, (uint32_t)(TC_B1 * sizeof(float)), &mbar[0]);
-    n_tma = 1;
-  }
 
-  // ---- phase 1: combined, symmetrised inputs of (member, j'); a warp covers 4 members x 8 j'
+  // ---- phase 1: combined, symmetrised inputs of (member, j') from the staged
+  // copy; a warp covers 4 members x 8 j'
   const int jp = (warp & 3) * 8 + (lane & 7);
   const int bt = (warp >> 2) * 4 + (lane >> 3);
   T2 xs[NSLOT], xa[NSLOT];
-  if (bt < mt) {
-    const int b = b0 + bt;
+  bool ok = tc::mbar_wait_bounded(&mbar[3], 0);
+  ok = __syncthreads_and(ok);
+  if (ok) {
+    const T2* stg = (const T2*)sA;
+    if (bt < mt) {
+      const int b = b0 + bt;
 #pragma unroll
-    for (int side = 0; side < 2; ++side) {
-      const int j = side ? (J - 1 - jp) : jp;
-      T2 c[NSLOT];
-      step_combos<T>(G, cfg, 0, incr, m, b, j, FS, c);
-      if (side == 0) {
+      for (int side = 0; side < 2; ++side) {
+        const int j = side ? (J - 1 - jp) : jp;
+        T2 c[NSLOT];
+        step_combos_ld<T>(G, cfg, 0, incr, m, b, j,
+                          [&](int f) { return stg[(stage_slot(f) * TC_MT + bt) * J + j]; }, c);
+        if (side == 0) {
 #pragma unroll
-        for (int q = 0; q < NSLOT; ++q) { xs[q] = c[q]; xa[q] = c[q]; }
-      } else {
+          for (int q = 0; q < NSLOT; ++q) { xs[q] = c[q]; xa[q] = c[q]; }
+        } else {
 #pragma unroll
-        for (int q = 0; q < NSLOT; ++q) { xs[q] = cadd(xs[q], c[q]); xa[q] = csub(xa[q], c[q]); }
+          for (int q = 0; q < NSLOT; ++q) { xs[q] = cadd(xs[q], c[q]); xa[q] = csub(xa[q], c[q]); }
+        }
       }
-    }
-  } else {
+    } else {
 #pragma unroll
-    for (int q = 0; q < NSLOT; ++q) { xs[q] = mk<T2>(0, 0); xa[q] = xs[q]; }
+      for (int q = 0; q < NSLOT; ++q) { xs[q] = mk<T2>(0, 0); xa[q] = xs[q]; }
+    }
   }
   // parity 0: P slots take the symmetric sum and H slots the antisymmetric one; parity 1 the reverse
   auto write_A1 = [&](int par) {
@@ -249,22 +280,24 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   const uint32_t idesc2 = tc::idesc_tf32(TC_ROWS, TC_N2);
   const uint32_t aHs = tc::smem_u32(sA), aLs = aHs + (uint32_t)(TC_ROWS * TC_K1 * 4);
   const uint32_t bbase = tc::smem_u32(sB);
-  bool ok = true;
 
   // ---- phase 2: GEMM1, parity 0 then parity 1 (the A buffer is refilled in between)
-  write_A1(0);
-  tc::fence_proxy_async();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    if (!tc::mbar_wait_bounded(&mbar[0], 0)) *sflag = 1;
-    if (!*sflag) mma_3xtf32(tbase, aHs, aLs, bbase, bbase + TC_N1 * TC_K1 * 4, TC_K1, idesc1);
-    tc::mma_commit(&mbar[1]);
-    n_c1 = 1;
+  if (ok) {
+    __syncthreads();  // every thread has read its staged inputs: A1 overwrites them
+    write_A1(0);
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (!tc::mbar_wait_bounded(&mbar[0], 0)) *sflag = 1;
+      if (!*sflag) mma_3xtf32(tbase, aHs, aLs, bbase, bbase + TC_N1 * TC_K1 * 4, TC_K1, idesc1);
+      tc::mma_commit(&mbar[1]);
+      n_c1 = 1;
+    }
+    ok = tc::mbar_wait_bounded(&mbar[1], 0);
+    tc::fence_after_sync();
+    ok = __syncthreads_and(ok);
+    ok = ok && !*sflag;  // written by thread 0 before the barrier: the same value for every thread
   }
-  ok = tc::mbar_wait_bounded(&mbar[1], 0);
-  tc::fence_after_sync();
-  ok = __syncthreads_and(ok);
-  ok = ok && !*sflag;  // written by thread 0 before the barrier: the same value for every thread
   if (ok) {
     write_A1(1);
     tc::fence_proxy_async();
@@ -419,38 +452,15 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     tc::fence_before_sync();
     __syncthreads();
     // ---- phase 7: write-out and carries (coalesced along j), as in k_spectral
-    T2* Fo = G.four_out;
-    const T2* Fi = G.four;
     for (int t = threadIdx.x; t < TC_MT * J; t += blockDim.x) {
       const int bti = t / J, j = t % J;
       if (bti >= mt || sdead[bti]) continue;
       const int b = b0 + bti;
       const size_t o = ((size_t)m * G.B + b) * J + j;
       auto get = [&](int f) { return *(const float2*)&Out[(size_t)(f * TC_MT + bti) * TC_OST + 2 * j]; };
-      const T al = G.mco[MC_ALPHA * G.B + b];
-      const int cf[3] = {F_ETA, F_DELTA, F_PHI};
-      const int pf[3] = {F_ETA_PREV, F_DELTA_PREV, F_PHI_PREV};
-      const int rf[3] = {F_ETA_MID, F_DELTA_MID, F_PHI_MID};
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        T2 nw = get(q);
-        if (incr || cfg.write_prev || cfg.ra_mode) {
-          const T2 old = Fi[cf[q] * FS + o];
-          if (incr) nw = cadd(old, nw);
-          if (cfg.write_prev) Fo[pf[q] * FS + o] = old;
-          if (cfg.ra_mode == 1) Fo[rf[q] * FS + o] = old;
-          else if (cfg.ra_mode == 2) {
-            const T2 mid = Fi[rf[q] * FS + o];
-            const T2 d = cadd(csub(mid, cscale(old, (T)2)), nw);
-            Fo[rf[q] * FS + o] = cadd(old, cscale(d, al));
-          }
-        }
-        Fo[cf[q] * FS + o] = nw;
-      }
-      if (cfg.test != 1) {
-        Fo[F_U * FS + o] = cadd(get(3), get(5));
-        Fo[F_V * FS + o] = cadd(get(4), get(6));
-      }
+      const T2 nw[3] = {get(0), get(1), get(2)};
+      write_step_point<T>(G, cfg, incr, FS, o, G.mco[MC_ALPHA * G.B + b], nw, cfg.test != 1, cadd(get(3), get(5)),
+                          cadd(get(4), get(6)));
     }
     if (m == 0 && threadIdx.x < mt && !sdead[threadIdx.x]) {
       const int b = b0 + threadIdx.x;
@@ -466,6 +476,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     // a wait ran out: report, then drain (bounded) what this CTA issued before freeing TMEM
     if (threadIdx.x == 0) {
       atomicExch(err, 1);
+      if (n_in > 0) tc::mbar_wait_bounded(&mbar[3], 0, 1u << 20);
       if (n_tma > 0) tc::mbar_wait_bounded(&mbar[0], (uint32_t)(n_tma - 1), 1u << 20);
       if (n_c1 > 0) tc::mbar_wait_bounded(&mbar[1], (uint32_t)(n_c1 - 1), 1u << 20);
       if (n_c2 > 0) tc::mbar_wait_bounded(&mbar[2], 0, 1u << 20);
