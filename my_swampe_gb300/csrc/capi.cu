@@ -460,17 +460,23 @@ int time_kernels_impl(swp_plan* p, const swp_group_state* st, const swp_group_ad
   for (int i = 0; i < 5; ++i) cudaEventCreate(&ev[i]);
   double acc[4] = {0, 0, 0, 0};
   for (int r = 0; r < nrep; ++r) {
+    cudaError_t le[4] = {cudaSuccess, cudaSuccess, cudaSuccess, cudaSuccess};
     cudaEventRecord(ev[0], s);
-    launch_step_spec<T>(p, LS, nbs, s);
+    le[0] = launch_step_spec<T>(p, LS, nbs, s);
     cudaEventRecord(ev[1], s);
-    launch_grid<T>(LG, nbg, p->grid_smem[GM_STEP], s);
+    le[1] = launch_grid<T>(LG, nbg, p->grid_smem[GM_STEP], s);
     cudaEventRecord(ev[2], s);
     if (adj) {
-      launch_grid<T>(LGa, nbg, p->grid_smem[GM_ADJ_STEP], s);
+      le[2] = launch_grid<T>(LGa, nbg, p->grid_smem[GM_ADJ_STEP], s);
       cudaEventRecord(ev[3], s);
-      launch_spec_adj<T>(LSa, nbs, p->spec_adj_smem, s);
+      le[3] = launch_spec_adj<T>(LSa, nbs, p->spec_adj_smem, s);
       cudaEventRecord(ev[4], s);
     }
+    for (int k = 0; k < 4; ++k)
+      if (le[k] != cudaSuccess) {
+        for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
+        return cuda_check(p, le[k], "timed kernel launch");
+      }
     cudaError_t e = cudaEventSynchronize(adj ? ev[4] : ev[2]);
     if (e != cudaSuccess) { for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]); return cuda_check(p, e, "timed kernels"); }
     float t;

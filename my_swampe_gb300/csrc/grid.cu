@@ -35,7 +35,9 @@ size_t grid_smem_bytes(int M, int J, int I, int JB, int mode) {
   int LS = I / 2 + 1;
   size_t ntr = (size_t)grid_ntr(mode) * JB;
   size_t buf = ntr * LS * sizeof(typename cplx<T>::type);
-  return 2 * buf + (size_t)I * sizeof(T) + 16 + 8 * sizeof(double);
+  // two transform buffers, the dayside row, the twiddles (L + (L+1)), reductions
+  return 2 * buf + (size_t)I * sizeof(T) + 16 + (size_t)(I + 1) * sizeof(typename cplx<T>::type) + 16 +
+         8 * sizeof(double);
 }
 template size_t grid_smem_bytes<double>(int, int, int, int, int);
 template size_t grid_smem_bytes<float>(int, int, int, int, int);
@@ -176,19 +178,26 @@ struct GridCtx {
   T2* bufA;
   T2* bufB;
   T* sday;
+  const T2* twL;   // shared-memory copies of the geometry's twiddles
+  const T2* twI;
   double* sred;
   T invI;
 };
 
 // Stage the rows j0..j0+JB-1 of `nf` Fourier fields of member b into `stage`
-// ([f][m][r], r fastest; global reads are JB-long contiguous runs).
+// ([f][r][m], m fastest; the global reads are JB-long contiguous runs).  The
+// field pointers go through a shared-memory table rather than a local array.
 template <typename T, typename C>
 __device__ __forceinline__ void stage_rows(const C& c, const typename cplx<T>::type* const* src, int nf,
                                            typename cplx<T>::type* stage) {
-  const int n1 = C::M + 1;
+  typedef typename cplx<T>::type T2;
+  __shared__ const T2* s_src[16];
+  if (threadIdx.x < 16) s_src[threadIdx.x] = (int)threadIdx.x < nf ? src[threadIdx.x] : nullptr;
+  __syncthreads();
+  constexpr int n1 = C::M + 1;
   for (int t = threadIdx.x; t < nf * n1 * C::JB; t += blockDim.x) {
-    int r = t % C::JB, k = (t / C::JB) % n1, f = t / (C::JB * n1);
-    stage[t] = src[f][((size_t)k * c.B + c.b) * C::J + c.j0 + r];
+    const int r = t % C::JB, k = (t / C::JB) % n1, f = t / (C::JB * n1);
+    stage[(f * C::JB + r) * n1 + k] = s_src[f][((size_t)k * c.B + c.b) * C::J + c.j0 + r];
   }
 }
 
@@ -196,11 +205,11 @@ __device__ __forceinline__ void stage_rows(const C& c, const typename cplx<T>::t
 template <typename T, typename C>
 __device__ __forceinline__ void build_c2r(const C& c, const typename cplx<T>::type* stage, int nf,
                                           const T* scale0, const T* scale, typename cplx<T>::type* out) {
-  const int n1 = C::M + 1;
+  constexpr int n1 = C::M + 1;
   for (int t = threadIdx.x; t < nf * C::JB * C::L; t += blockDim.x) {
-    int k = t % C::L, fr = t / C::L, r = fr % C::JB, f = fr / C::JB;
-    out[(size_t)fr * C::LS + k] = c2r_pre<typename cplx<T>::type, T>(stage + (size_t)f * n1 * C::JB + r, C::JB, C::M, C::L, k,
-                                                                    c.G->g.twI, scale0[f], scale[f]);
+    const int k = t % C::L, fr = t / C::L, f = fr / C::JB;
+    out[(size_t)fr * C::LS + k] = c2r_pre<typename cplx<T>::type, T>(stage + (size_t)fr * n1, 1, C::M, C::L, k,
+                                                                    c.twI, scale0[f], scale[f]);
   }
 }
 
@@ -209,12 +218,15 @@ __device__ __forceinline__ void build_c2r(const C& c, const typename cplx<T>::ty
 template <typename T, typename C>
 __device__ __forceinline__ void write_r2c(const C& c, const typename cplx<T>::type* res, int nf,
                                           typename cplx<T>::type* const* dst, T s0, T s) {
-  const int n1 = C::M + 1;
+  typedef typename cplx<T>::type T2;
+  __shared__ T2* s_dst[16];
+  if (threadIdx.x < 16) s_dst[threadIdx.x] = (int)threadIdx.x < nf ? dst[threadIdx.x] : nullptr;
+  __syncthreads();
+  constexpr int n1 = C::M + 1;
   for (int t = threadIdx.x; t < nf * n1 * C::JB; t += blockDim.x) {
-    int r = t % C::JB, k = (t / C::JB) % n1, q = t / (C::JB * n1);
-    typename cplx<T>::type v = r2c_post<typename cplx<T>::type, T>(res + ((size_t)q * C::JB + r) * C::LS, C::L, k,
-                                                                     c.G->g.twI, k == 0 ? s0 : s);
-    dst[q][((size_t)k * c.B + c.b) * C::J + c.j0 + r] = v;
+    const int r = t % C::JB, k = (t / C::JB) % n1, q = t / (C::JB * n1);
+    const T2 v = r2c_post<T2, T>(res + ((size_t)q * C::JB + r) * C::LS, C::L, k, c.twI, k == 0 ? s0 : s);
+    s_dst[q][((size_t)k * c.B + c.b) * C::J + c.j0 + r] = v;
   }
 }
 
@@ -247,9 +259,13 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
   c.bufA = (T2*)smem_raw;
   c.bufB = c.bufA + (size_t)NTR * JB * LS;
   c.sday = (T*)(c.bufB + (size_t)NTR * JB * LS);
-  c.sred = (double*)(((uintptr_t)(c.sday + I) + 15) & ~(uintptr_t)15);
+  T2* stw = (T2*)(((uintptr_t)(c.sday + I) + 15) & ~(uintptr_t)15);  // twL [L], then twI [L+1]
+  c.twL = stw;
+  c.twI = stw + L;
+  c.sred = (double*)(((uintptr_t)(stw + 2 * L + 1) + 15) & ~(uintptr_t)15);
   c.invI = (T)1 / (T)I;
   for (int i = threadIdx.x; i < I; i += blockDim.x) c.sday[i] = G.g.dayc[i];
+  for (int i = threadIdx.x; i < 2 * L + 1; i += blockDim.x) stw[i] = i < L ? G.g.twL[i] : G.g.twI[i - L];
   if (threadIdx.x == 0) { c.sred[0] = 0.0; c.sred[1] = 1e300; c.sred[2] = 1e300; c.sred[3] = -1e300; }
 
   const int B = G.B, b = c.b, j0 = c.j0;
@@ -309,7 +325,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     __syncthreads();
     build_c2r<T>(c, bufB, nf, one, one, bufA);
     __syncthreads();
-    T2* zin = cfft_batch_c<+1, L>(bufA, bufB, nf * JB, g.twL);
+    T2* zin = cfft_batch_c<+1, L>(bufA, bufB, nf * JB, c.twL);
     T2* zout = (zin == bufA) ? bufB : bufA;
     // initial-condition residual (non-zero only before a member's first step and
     // for the fixed test-1 winds): added in shared memory, off the hot loop
@@ -416,7 +432,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       atomic_max_d(&dc[D_PHIMAX * B + b], c.sred[3]);
     }
     const int nout = ph.forced ? 8 : 5;
-    T2* res = cfft_batch_c<-1, L>(zout, zin, nout * JB, g.twL);
+    T2* res = cfft_batch_c<-1, L>(zout, zin, nout * JB, c.twL);
     T2* dst[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) dst[q] = G.four + (F_A + q) * FS;
@@ -433,7 +449,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       bufA[(size_t)fr * LS + n] = mk<T2>(x[0], x[1]);
     }
     __syncthreads();
-    T2* res = cfft_batch_c<-1, L>(bufA, bufB, 2 * JB, g.twL);
+    T2* res = cfft_batch_c<-1, L>(bufA, bufB, 2 * JB, c.twL);
     T2* dst[2] = {G.four + F_ETA * FS, G.four + F_DELTA * FS};
     write_r2c<T>(c, res, 2, dst, invI, invI);
     return;
@@ -450,13 +466,13 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       bufA[(size_t)fr * LS + n] = mk<T2>(x[0], x[1]);
     }
     __syncthreads();
-    T2* res = cfft_batch_c<-1, L>(bufA, bufB, nf * JB, g.twL);
+    T2* res = cfft_batch_c<-1, L>(bufA, bufB, nf * JB, c.twL);
     T2* other = (res == bufA) ? bufB : bufA;
     const int n1 = M + 1;
     // unpack into global and keep the truncated rows in `other` ([f][m][r])
     for (int t = threadIdx.x; t < nf * n1 * JB; t += blockDim.x) {
-      int r = t % JB, k = (t / JB) % n1, f = t / (JB * n1);
-      T2 v = r2c_post<T2, T>(res + ((size_t)f * JB + r) * LS, L, k, g.twI, invI);
+      const int r = t % JB, k = (t / JB) % n1, f = t / (JB * n1);
+      T2 v = r2c_post<T2, T>(res + ((size_t)f * JB + r) * LS, L, k, c.twI, invI);
       size_t o = ((size_t)k * B + b) * J + j0 + r;
       const int sf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
       G.four[sf[f] * FS + o] = v;
@@ -464,14 +480,14 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
         G.four[(f == 0 ? F_ETA_PREV : f == 1 ? F_DELTA_PREV : F_PHI_PREV) * FS + o] = v;
         G.four[(f == 0 ? F_ETA_MID : f == 1 ? F_DELTA_MID : F_PHI_MID) * FS + o] = v;
       }
-      other[t] = v;
+      other[(f * JB + r) * n1 + k] = v;  // staged layout of build_c2r
     }
     __syncthreads();
     // band-limited reconstruction -> residual = x - C2R(trunc FFT(x))
     T one[5] = {(T)1, (T)1, (T)1, (T)1, (T)1};
     build_c2r<T>(c, other, nf, one, one, res);
     __syncthreads();
-    T2* zr = cfft_batch_c<+1, L>(res, other, nf * JB, g.twL);
+    T2* zr = cfft_batch_c<+1, L>(res, other, nf * JB, c.twL);
     for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
       int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
       size_t po = f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
@@ -517,7 +533,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       atomicAdd(&G.diag[D_RMS2 * B + b], c.sred[0]);
       atomic_min_d(&G.diag[D_SPIN * B + b], c.sred[1]);
     }
-    T2* res2 = cfft_batch_c<-1, L>(bufA, bufB, nout * JB, g.twL);
+    T2* res2 = cfft_batch_c<-1, L>(bufA, bufB, nout * JB, c.twL);
     T2* dst[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) dst[q] = G.four + (F_A + q) * FS;
@@ -549,7 +565,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     __syncthreads();
     build_c2r<T>(c, bufB, nb1, s0, s1, bufA);
     __syncthreads();
-    T2* zin = cfft_batch_c<+1, L>(bufA, bufB, nb1 * JB, g.twL);
+    T2* zin = cfft_batch_c<+1, L>(bufA, bufB, nb1 * JB, c.twL);
     T2* zout = (zin == bufA) ? bufB : bufA;
     T gacc[NGRAD] = {(T)0, (T)0, (T)0, (T)0};
     for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
@@ -594,7 +610,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     block_add_grads<T>(gacc, c.sred, G.grad, B, b);
     if (MODE == GM_ADJ_STEP) {
       // adjoint of x = Re(Y_0) + 2 Re sum_{m>=1} Y_m e^{i theta}:  lambda Y_m = c_m sum_i lambda x_i e^{-i theta}
-      T2* res = cfft_batch_c<-1, L>(zout, zin, 4 * JB, g.twL);
+      T2* res = cfft_batch_c<-1, L>(zout, zin, 4 * JB, c.twL);
       const int n1 = M + 1;
       const int yf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
       const int rmap[5] = {0, -1, 1, 2, 3};
@@ -602,7 +618,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
         int r = t % JB, k = (t / JB) % n1, q = t / (JB * n1);
         size_t o = ((size_t)k * B + b) * J + j0 + r;
         T2 v = G.lam[yf[q] * FS + o];
-        if (rmap[q] >= 0) v = cadd(v, r2c_post<T2, T>(res + ((size_t)rmap[q] * JB + r) * LS, L, k, g.twI, k == 0 ? (T)1 : (T)2));
+        if (rmap[q] >= 0) v = cadd(v, r2c_post<T2, T>(res + ((size_t)rmap[q] * JB + r) * LS, L, k, c.twI, k == 0 ? (T)1 : (T)2));
         G.lamy[(size_t)q * FS + o] = v;
       }
       return;
@@ -618,7 +634,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     __syncthreads();
     build_c2r<T>(c, bufB, 5, s20, s21, bufA);
     __syncthreads();
-    T2* z2 = cfft_batch_c<+1, L>(bufA, bufB, 5 * JB, g.twL);
+    T2* z2 = cfft_batch_c<+1, L>(bufA, bufB, 5 * JB, c.twL);
     for (int t = threadIdx.x; t < 5 * JB * L; t += blockDim.x) {
       int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
       size_t po = f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
@@ -639,7 +655,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       bufA[(size_t)fr * LS + n] = mk<T2>(x[0], x[1]);
     }
     __syncthreads();
-    T2* res = cfft_batch_c<-1, L>(bufA, bufB, nf * JB, g.twL);
+    T2* res = cfft_batch_c<-1, L>(bufA, bufB, nf * JB, c.twL);
     T2* dst[5] = {G.lam + F_ETA * FS, G.lam + F_DELTA * FS, G.lam + F_PHI * FS, G.lam + F_U * FS, G.lam + F_V * FS};
     write_r2c<T>(c, res, nf, dst, (T)1, (T)2);
     return;
@@ -666,9 +682,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_grid(const __gr
 
 int grid_rows_per_cta(int M, bool fp64) { return fp64 ? grid_jb<double>(M) : grid_jb<float>(M); }
 
+// Largest dynamic shared memory the kernel may request: 227 KB per block minus
+// the kernel's static shared memory (the pointer tables of stage_rows / write_r2c).
 template <typename T, int MODE>
 static void set_attr_one() {
-  cudaFuncSetAttribute(k_grid<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncAttributes fa;
+  size_t stat = cudaFuncGetAttributes(&fa, k_grid<T, MODE>) == cudaSuccess ? fa.sharedSizeBytes : 1024;
+  cudaFuncSetAttribute(k_grid<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(227 * 1024 - stat));
 }
 
 void grid_set_attributes() {

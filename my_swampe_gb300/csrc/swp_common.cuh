@@ -31,7 +31,13 @@ template <typename T> struct cplx;
 template <> struct cplx<double> { typedef double2 type; };
 template <> struct cplx<float> { typedef float2 type; };
 
-template <typename T2> __device__ __forceinline__ T2 mk(double r, double i) {
+// Scalar type of a complex vector type.  mk takes its arguments in that type:
+// a double signature would round-trip every float through FP64 conversions.
+template <typename T2> struct scalar_of;
+template <> struct scalar_of<double2> { typedef double type; };
+template <> struct scalar_of<float2> { typedef float type; };
+template <typename T2>
+__device__ __forceinline__ T2 mk(typename scalar_of<T2>::type r, typename scalar_of<T2>::type i) {
   T2 z; z.x = r; z.y = i; return z;
 }
 template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { T2 z; z.x = a.x + b.x; z.y = a.y + b.y; return z; }
@@ -44,7 +50,9 @@ template <typename T2> __device__ __forceinline__ T2 cmulc(T2 a, T2 b) {
   T2 z; z.x = a.x * b.x + a.y * b.y; z.y = a.y * b.x - a.x * b.y; return z;
 }
 template <typename T2> __device__ __forceinline__ T2 cconj(T2 a) { a.y = -a.y; return a; }
-template <typename T2, typename S> __device__ __forceinline__ T2 cscale(T2 a, S s) { a.x *= s; a.y *= s; return a; }
+template <typename T2> __device__ __forceinline__ T2 cscale(T2 a, typename scalar_of<T2>::type s) {
+  a.x *= s; a.y *= s; return a;
+}
 // multiply by +i (SIGN>0) or -i (SIGN<0)
 template <int SIGN, typename T2> __device__ __forceinline__ T2 cmul_i(T2 a) {
   T2 z; if (SIGN > 0) { z.x = -a.y; z.y = a.x; } else { z.x = a.y; z.y = -a.x; } return z;
@@ -167,25 +175,38 @@ __device__ T2* cfft_batch(T2* a, T2* b, int L, int ls, int ntr, const T2* tw) {
   }
 }
 
-// Compile-time-length variant of the above (ls = L + 1): every index division
-// is by a constant.
+// n / d for 0 <= n < 2^16 and 2 <= d <= 256 by one multiply-high (exact in
+// that range: the rounding error of the reciprocal stays below 1/d).
+struct FastDiv {
+  uint32_t m;
+  __device__ __forceinline__ explicit FastDiv(int d) : m(0xFFFFFFFFu / (uint32_t)d + 1u) {}
+  __device__ __forceinline__ int operator()(int n) const { return (int)__umulhi((uint32_t)n, m); }
+};
+
+// Compile-time-length variant of the above (ls = L + 1).  Lanes take the same
+// butterfly of consecutive transforms (transform index fastest): with the odd
+// stride L + 1 every load and store of a pass is free of bank conflicts once a
+// half-warp spans 16 transforms.  ntr >= 2.
 template <int R, int SIGN, int L, int NS, typename T2>
 __device__ __forceinline__ void stockham_pass_c(const T2* __restrict__ in, T2* __restrict__ out, int ntr,
                                                 const T2* __restrict__ tw) {
   constexpr int LS = L + 1, PER = L / R, TWS = L / (NS * R);
   const int tasks = ntr * PER;
+  const FastDiv divt(ntr);
   for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
-    const int t = task / PER, j = task - t * PER;
+    const int j = divt(task), t = task - j * ntr;
     const T2* src = in + t * LS;
     T2* dst = out + t * LS;
     const int jm = j % NS;
     T2 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = src[j + r * PER];
+    if (NS > 1) {  // the first pass has no twiddles
 #pragma unroll
-    for (int r = 1; r < R; ++r) {
-      const T2 w = tw[jm * r * TWS];
-      v[r] = (SIGN < 0) ? cmul(v[r], w) : cmulc(v[r], w);
+      for (int r = 1; r < R; ++r) {
+        const T2 w = tw[jm * r * TWS];
+        v[r] = (SIGN < 0) ? cmul(v[r], w) : cmulc(v[r], w);
+      }
     }
     dftR<R, SIGN>(v);
     const int idx = (j / NS) * NS * R + jm;
