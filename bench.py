@@ -19,9 +19,10 @@ e2e   : the same metric through the public API (torch.autograd over
         with torch autograd on the host cores) on a bounded sample of the
         same workload.
 
-The data are synthetic (my_swampe_gb300.workloads.forced_ensemble); the
-working set per model step is larger than L2 and L2 is additionally flushed
-with a 512 MB write between timed steps.
+The data are synthetic (my_swampe_gb300.workloads.forced_ensemble).  One
+integration touches ~9 GB (29 checkpoints and 51 window slots of the 107 MB
+FP32 state), far more than L2; L2 is also flushed with a 512 MB write
+between timed steps.
 """
 from __future__ import annotations
 
@@ -182,6 +183,27 @@ def _algorithmic_bytes(kernel, B, J=64, M=42, elem=8):
     return cols * J * (M + 1) * elem * B
 
 
+# ncu summary (profiles/) of each kernel at this workload, which records the
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
+_PROFILE_OF = {"spectral": "k_spectral_tc_fast_M42_B256.md", "grid": "k_grid_step_fast_M42_B256.md",
+               "grid_adj": "k_grid_adjoint_fast_M42_B256.md", "spectral_adj": "k_spectral_adj_fast_M42_B256.md"}
+
+
+def _ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from its committed ncu summary (the line
+    'traffic_bytes_per_launch: N'), or None when there is no capture."""
+    p = ROOT / "profiles" / _PROFILE_OF.get(kernel, "")
+    if not p.is_file():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return int(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -237,7 +259,7 @@ def run_ours(args):
     alg = _algorithmic_bytes(dom, B, elem=8)
     achieved = alg / (per_step[dom] * 1e-3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": None,
+                "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": _ncu_traffic(dom),
                 "ms_per_launch": {k: round(v, 5) for k, v in per_step.items()},
                 "algorithmic_bytes_per_launch": alg}
 
@@ -306,7 +328,11 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.skip_cpu:
         cpu = _cpu_baseline(args.cpu_members, args.cpu_nsteps)
 
-    launches = 1 + 2 * T_BENCH + 1 + 1 + 4 * T_BENCH + 1  # init, forward, output, seed, windows, init-adjoint
+    # kernels of ours per integration: init; per forward window a coefficient kernel
+    # + (Legendre, grid) per step; output; seed; per adjoint window a coefficient
+    # kernel + 2 recompute + 2 adjoint kernels per step; adjoint of the init
+    nwin = -(-T_BENCH // CKPT)
+    launches = 1 + (nwin + 2 * T_BENCH) + 1 + 1 + (nwin + 4 * T_BENCH) + 1
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(1e3 * t_max, 3), "higher_is_better": True, "scaling": "weak",
@@ -314,7 +340,7 @@ def run_ours(args):
         "data": "synthetic (seeded forced ensemble: taurad, taudrag log-uniform [1e4,1e6] s, DPhieq U[1e5,4e6], Phi noise 1e-3*Phibar at n<=10)",
         "config": {"workload": "forced ensemble fwd+adjoint, M=42 (64x128), B=256 members per GPU, 1440 steps, checkpoint every 50",
                    "members_per_gpu": B, "steps_per_member": T_BENCH, "ckpt_every": CKPT,
-                   "l2": "working set > L2 (126 MB); 512 MB L2 flush write between timed steps"},
+                   "l2": "integration touches ~9 GB (checkpoints + window slots) > L2 (126 MB); 512 MB L2 flush write between timed steps"},
         "e2e": {"value": round(world * B * T_BENCH / e2e_t, 1), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1e3 * e2e_t, 3)},
         "roofline": roofline,
@@ -396,9 +422,15 @@ def run_reference(args):
 
 
 def run_profile(args):
-    """One checkpoint window of the bench workload, sized for ncu: init, K forward
-    steps (checkpointed), then the window adjoint (K recompute steps + K adjoint
-    steps) -- the same kernel mix per model step as the timed bench."""
+    """Small cases of the bench workload for ncu (no timing).
+
+    --profile-case window: one checkpoint window, i.e. init, K forward steps
+        (checkpointed), then the window adjoint (K recompute steps + K adjoint
+        steps): the kernel mix of the timed bench, for the launch list.
+    --profile-case steps: init, 4 forward steps, 3 adjoint steps, each launched
+        on its own (no graphs): a handful of launches of every step kernel, for
+        full captures (launch order: grid INIT, then per forward step Legendre +
+        grid STEP, then per adjoint step grid ADJ_STEP + Legendre adjoint)."""
     import torch
 
     torch.cuda.set_device(0)
@@ -408,6 +440,20 @@ def run_profile(args):
     from my_swampe_gb300.adjoint import Integration
 
     eng, wl, flags, _, ics = _setup(args.profile, args.B)
+    if args.profile_case == "steps":
+        eng.init_state([ics], flags)
+        eng.forward(flags, t0=2, nsteps=3)
+        four_in = [eng.groups[0]["fourier"].clone()]
+        eng.forward(flags, t0=5, nsteps=1)
+        four_out = [eng.groups[0]["fourier"]]
+        lam, lamy, grad = eng.new_adjoint_buffers()
+        lam[0].copy_(torch.randn_like(lam[0]))
+        for _ in range(3):
+            eng.adjoint_step(flags, four_in, four_out, lam, lamy, grad, t=6)
+        torch.cuda.synchronize()
+        eng.check_device_status()
+        print(json.dumps({"profile": args.profile, "case": "steps", "B": args.B, "ok": True}))
+        return
     integ = Integration(eng, flags, t0=2, nsteps=CKPT, ckpt_every=CKPT)
     out = integ.run_forward([ics])[0]
     d = torch.zeros_like(out)
@@ -431,7 +477,8 @@ def main():
     ap.add_argument("--cpu-nsteps", type=int, default=40)
     ap.add_argument("--ref-nsteps", type=int, default=20)
     ap.add_argument("--profile", choices=("fast", "fp64"), default=None,
-                    help="run one checkpoint window of the workload (for ncu) instead of timing")
+                    help="run a small case of the workload (for ncu) instead of timing")
+    ap.add_argument("--profile-case", choices=("window", "steps"), default="window")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)

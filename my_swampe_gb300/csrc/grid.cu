@@ -230,12 +230,13 @@ __device__ __forceinline__ void write_r2c(const C& c, const typename cplx<T>::ty
   }
 }
 
+// Warp sums in the compute type, block and global sums in FP64.
 template <typename T>
 __device__ void block_add_grads(const T* gacc, double* sred, double* grad, int B, int b) {
   for (int q = 0; q < NGRAD; ++q) {
-    double v = (double)gacc[q];
+    T v = gacc[q];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&sred[q], v);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&sred[q], (double)v);
   }
   __syncthreads();
   if (threadIdx.x < NGRAD && grad) atomicAdd(&grad[threadIdx.x * B + b], sred[threadIdx.x]);
@@ -271,20 +272,33 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
   const int B = G.B, b = c.b, j0 = c.j0;
   const size_t FS = c.FS, PS = c.PS;
   const Geom<T>& g = G.g;
-  double Pb = G.par[P_PHIBAR * B + b], tr = G.par[P_TAURAD * B + b];
-  double td = G.par[P_TAUDRAG * B + b], DPe = G.par[P_DPHIEQ * B + b];
+  // per-member scalars, formed once per CTA by thread 0 (FP64 parameters in,
+  // compute type out) and shared: FP64 arithmetic replicated over all 256
+  // threads of every CTA would load GB300's small FP64 pipe
+  __shared__ T s_par[6];     // Phibar, 1/taurad, 1/taudrag, DPhieq, w_curr, w_mid
+  __shared__ int s_flag[2];  // no drag (taudrag == -1), member blown up
+  if (threadIdx.x == 0) {
+    const double Pb = G.par[P_PHIBAR * B + b], tr = G.par[P_TAURAD * B + b];
+    const double td = G.par[P_TAUDRAG * B + b], DPe = G.par[P_DPHIEQ * B + b];
+    const double wc = G.member ? G.member[MS_WCURR * B + b] : 0.0;
+    const double wm = G.member ? G.member[MS_WMID * B + b] : 0.0;
+    s_par[0] = (T)Pb; s_par[1] = (T)(1.0 / tr); s_par[2] = (T)(1.0 / td); s_par[3] = (T)DPe;
+    s_par[4] = (T)wc; s_par[5] = (T)wm;
+    s_flag[0] = td == -1.0;
+    s_flag[1] = (cfg.diagnostics && G.member) ? (G.member[MS_DEAD * B + b] != 0.0) : 0;
+  }
+  __syncthreads();
   Physics<T> ph;
-  ph.Pb = (T)Pb; ph.itr = (T)(1.0 / tr); ph.itd = (T)(1.0 / td); ph.DPe = (T)DPe;
-  ph.nodrag = (td == -1.0); ph.forced = (cfg.test == 0);
+  ph.Pb = s_par[0]; ph.itr = s_par[1]; ph.itd = s_par[2]; ph.DPe = s_par[3];
+  ph.nodrag = s_flag[0] != 0; ph.forced = (cfg.test == 0);
   const T invI = c.invI;
   T2* bufA = c.bufA;
   T2* bufB = c.bufB;
 
   if (MODE == GM_STEP || MODE == GM_OUTPUT || MODE == GM_WINDS) {
     // ------------------------------------------------ Fourier -> physical
-    const double wcur = G.member ? G.member[MS_WCURR * B + b] : 0.0;
-    const double wmid = G.member ? G.member[MS_WMID * B + b] : 0.0;
-    const bool dead = (cfg.diagnostics && G.member) ? (G.member[MS_DEAD * B + b] != 0.0) : false;
+    const T wcur = s_par[4], wmid = s_par[5];
+    const bool dead = s_flag[1] != 0;
     int fl[8], nf = 0;
     if (MODE == GM_STEP) {
       fl[nf++] = F_ETA; fl[nf++] = F_PHI; fl[nf++] = F_U; fl[nf++] = F_V;
@@ -298,12 +312,12 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     }
     const T2* src[8];
     T one[8];
-    double wv[8];
+    T wv[8];
     int rfv[8];
 #pragma unroll
     for (int f = 0; f < 8; ++f) {
       one[f] = (T)1;
-      wv[f] = 0.0;
+      wv[f] = (T)0;
       rfv[f] = 0;
       src[f] = nullptr;
       if (f < nf) {
@@ -315,9 +329,9 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
         else if (fld == F_PHI || fld == F_PHI_MID) rf = R_PHI;
         else if (fld == F_U) rf = R_U;
         else if (fld == F_V) rf = R_V;
-        double w = (fld == F_ETA_MID || fld == F_DELTA_MID || fld == F_PHI_MID) ? wmid : wcur;
-        if ((fld == F_U || fld == F_V) && cfg.test == 1) w = 1.0;  // fixed initial winds (model.py:979-983)
-        if (rf >= 0 && G.resid && w != 0.0) { wv[f] = w; rfv[f] = rf; }
+        T w = (fld == F_ETA_MID || fld == F_DELTA_MID || fld == F_PHI_MID) ? wmid : wcur;
+        if ((fld == F_U || fld == F_V) && cfg.test == 1) w = (T)1;  // fixed initial winds (model.py:979-983)
+        if (rf >= 0 && G.resid && w != (T)0) { wv[f] = w; rfv[f] = rf; }
       }
     }
     __syncthreads();
@@ -331,20 +345,20 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     // for the fixed test-1 winds): added in shared memory, off the hot loop
     bool need_resid = false;
 #pragma unroll
-    for (int f = 0; f < 8; ++f) need_resid |= (wv[f] != 0.0);
+    for (int f = 0; f < 8; ++f) need_resid |= (wv[f] != (T)0);
     if (need_resid) {
       for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
         int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
-        double w = 0.0;
+        T w = (T)0;
         int rf = 0;
 #pragma unroll
         for (int q = 0; q < 8; ++q)
           if (q == f) { w = wv[q]; rf = rfv[q]; }
-        if (w != 0.0) {
+        if (w != (T)0) {
           const T* rs = G.resid + rf * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
           T2 z = zin[(size_t)fr * LS + n];
-          z.x += (T)w * rs[0];
-          z.y += (T)w * rs[1];
+          z.x += w * rs[0];
+          z.y += w * rs[1];
           zin[(size_t)fr * LS + n] = z;
         }
       }
