@@ -2,11 +2,13 @@
 
 One bench "step" is one complete differentiable integration of the workload:
 B = 256 forced members at M = 42 (64 x 128 grid), 1440 modified-Euler time
-steps forward with the full state checkpointed every 50 steps, then the
-adjoint sweep (each 50-step window recomputed from its checkpoint, then the
-hand-written adjoint steps) back to gradients of the loss
+steps forward, then the hand-written adjoint steps back to gradients of the loss
 mean((Phi_T - Phi_target)^2) with respect to the initial (eta, delta, Phi,
-U, V) and to taurad, taudrag, DPhieq and Phibar of every member.
+U, V) and to taurad, taudrag, DPhieq and Phibar of every member.  The adjoint
+gets its primal states as the library's Integration decides (--store auto):
+the FP32 run keeps all 1441 states (154 GB of HBM) and needs no
+recomputation; the FP64 run (twice the bytes) checkpoints every 50 steps and
+recomputes each window.  --store checkpoint forces the recomputing form.
 
 value : fast path (FP32 state and pointwise math) on device-resident inputs,
         B * 1440 / seconds per step.  The plain FP64 GPU path is timed on the
@@ -20,9 +22,9 @@ e2e   : the same metric through the public API (torch.autograd over
         same workload.
 
 The data are synthetic (my_swampe_gb300.workloads.forced_ensemble).  One
-integration touches ~9 GB (29 checkpoints and 51 window slots of the 107 MB
-FP32 state), far more than L2; L2 is also flushed with a 512 MB write
-between timed steps.
+integration touches far more than L2 (154 GB of stored states, or ~9 GB of
+checkpoints and window slots); L2 is also flushed with a 512 MB write between
+timed steps.
 """
 from __future__ import annotations
 
@@ -111,7 +113,7 @@ def _flush_l2(buf):
     buf.add_(1.0)
 
 
-def _setup(precision, B, seed=1234):
+def _setup(precision, B, seed=1234, store="auto"):
     import torch
     from my_swampe_gb300.engine import Engine, RunFlagsC
     from my_swampe_gb300.adjoint import Integration
@@ -121,7 +123,7 @@ def _setup(precision, B, seed=1234):
     wl = workloads.forced_ensemble(eng, seed=seed)
     workloads.apply_params(eng, 0, wl["params"])
     flags = RunFlagsC()
-    integ = Integration(eng, flags, t0=2, nsteps=T_BENCH, ckpt_every=CKPT)
+    integ = Integration(eng, flags, t0=2, nsteps=T_BENCH, ckpt_every=CKPT, store=store)
     ics = wl["ics"].to(eng.rdtype)
     return eng, wl, flags, integ, ics
 
@@ -226,7 +228,7 @@ def run_ours(args):
     flush = lambda: _flush_l2(flush_buf)  # noqa: E731
 
     # ---------------- fast path (headline)
-    eng, wl, flags, integ, ics = _setup("fast", B, seed=1234 + 100000 * rank)
+    eng, wl, flags, integ, ics = _setup("fast", B, seed=1234 + 100000 * rank, store=args.store)
     target = _target(eng, wl, flags, ics)
     state = {}
 
@@ -264,7 +266,7 @@ def run_ours(args):
                 "algorithmic_bytes_per_launch": alg}
 
     # ---------------- e2e through the public API with host buffers
-    from my_swampe_gb300.adjoint import integrate, GRAD_PARAMS
+    from my_swampe_gb300.adjoint import integrate, GRAD_PARAMS, Integration
 
     host_ics = ics.detach().cpu().pin_memory()
     host_par = {k: wl["params"][k].detach().cpu().pin_memory() for k in GRAD_PARAMS if k != "Phibar"}
@@ -294,11 +296,24 @@ def run_ours(args):
         host_tgt.numel() * host_tgt.element_size()
     d2h = out_ic.numel() * out_ic.element_size() + out_par.numel() * 8
 
+    store_fast = integ.store
+    integ.release()
+    del integ, step_e2e, step_fast
+    torch.cuda.empty_cache()
+    # ---------------- fast path with the FP64 run's state policy (checkpoints + recompute),
+    # so the FP64 speed-up can also be read at equal algorithm
+    fast_ckpt = None
+    if not args.skip_fp64 and store_fast != "checkpoint":
+        integ_c = Integration(eng, flags, t0=2, nsteps=T_BENCH, ckpt_every=CKPT, store="checkpoint")
+        tc_ = _time_steps(lambda: _one_step(integ_c, ics, target), 2, 1, flush)
+        fast_ckpt = world * B * T_BENCH / float(np.mean(tc_))
+        integ_c.release()
+        del integ_c
+        torch.cuda.empty_cache()
     # ---------------- plain FP64 GPU path on the same workload
     fp64 = None
     if not args.skip_fp64:
-        del integ
-        eng64, wl64, flags64, integ64, ics64 = _setup("fp64", B, seed=1234 + 100000 * rank)
+        eng64, wl64, flags64, integ64, ics64 = _setup("fp64", B, seed=1234 + 100000 * rank, store=args.store)
         target64 = target.double()
         st64 = {}
 
@@ -319,7 +334,11 @@ def run_ours(args):
                 for k, name in enumerate(GRAD_PARAMS)}
         kt64 = eng64.time_kernels(flags64, nrep=5, adjoint=True)
         fp64 = {"value": round(v64, 1), "ms_per_step": round(1e3 * float(np.mean(t64)), 3), "steps": args.fp64_steps,
-                "speedup_fast_over_fp64": round(value / (world * v64), 2), "error_fast_vs_fp64_after_1440": err,
+                "adjoint_states": integ64.store,
+                "speedup_fast_over_fp64": round(value / (world * v64), 2),
+                "fast_with_checkpoint_states": None if fast_ckpt is None else round(fast_ckpt, 1),
+                "speedup_at_equal_state_policy": round((fast_ckpt if fast_ckpt else value) / (world * v64), 2),
+                "error_fast_vs_fp64_after_1440": err,
                 "grad_rel_l2_fast_vs_fp64": gerr,
                 "ms_per_launch": {k: round(v, 5) for k, v in kt64.items()}}
 
@@ -328,11 +347,16 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.skip_cpu:
         cpu = _cpu_baseline(args.cpu_members, args.cpu_nsteps)
 
-    # kernels of ours per integration: init; per forward window a coefficient kernel
-    # + (Legendre, grid) per step; output; seed; per adjoint window a coefficient
-    # kernel + 2 recompute + 2 adjoint kernels per step; adjoint of the init
-    nwin = -(-T_BENCH // CKPT)
-    launches = 1 + (nwin + 2 * T_BENCH) + 1 + 1 + (nwin + 4 * T_BENCH) + 1
+    # kernels of ours per integration: init; output; seed; adjoint of the init;
+    # stored states: a coefficient kernel + (Legendre, grid) per step forward, a
+    # coefficient kernel + (grid adjoint, Legendre adjoint) per step backward;
+    # checkpoints: a coefficient kernel per window both ways and, backward, the
+    # 2 recompute kernels per step as well
+    if store_fast == "all":
+        launches = 4 + (1 + 2 * T_BENCH) + (1 + 2 * T_BENCH)
+    else:
+        nwin = -(-T_BENCH // CKPT)
+        launches = 4 + (nwin + 2 * T_BENCH) + (nwin + 4 * T_BENCH)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(1e3 * t_max, 3), "higher_is_better": True, "scaling": "weak",
@@ -340,7 +364,8 @@ def run_ours(args):
         "data": "synthetic (seeded forced ensemble: taurad, taudrag log-uniform [1e4,1e6] s, DPhieq U[1e5,4e6], Phi noise 1e-3*Phibar at n<=10)",
         "config": {"workload": "forced ensemble fwd+adjoint, M=42 (64x128), B=256 members per GPU, 1440 steps, checkpoint every 50",
                    "members_per_gpu": B, "steps_per_member": T_BENCH, "ckpt_every": CKPT,
-                   "l2": "integration touches ~9 GB (checkpoints + window slots) > L2 (126 MB); 512 MB L2 flush write between timed steps"},
+                   "adjoint_states": store_fast,
+                   "l2": "integration touches >= 9 GB (stored states or checkpoints + window slots) > L2 (126 MB); 512 MB L2 flush write between timed steps"},
         "e2e": {"value": round(world * B * T_BENCH / e2e_t, 1), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1e3 * e2e_t, 3)},
         "roofline": roofline,
@@ -479,6 +504,8 @@ def main():
     ap.add_argument("--profile", choices=("fast", "fp64"), default=None,
                     help="run a small case of the workload (for ncu) instead of timing")
     ap.add_argument("--profile-case", choices=("window", "steps"), default="window")
+    ap.add_argument("--store", choices=("auto", "all", "checkpoint"), default="auto",
+                    help="how the adjoint gets its primal states (Integration store policy)")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)

@@ -170,6 +170,23 @@ int swp_adjoint_init(swp_plan* plan, const swp_group_state* st, const swp_group_
 int swp_adjoint_window(swp_plan* plan, const swp_group_state* st, void* const* slots,
                        const swp_group_adjoint* adj, const swp_flags* flags, int t0, int nsteps, void* stream);
 
+/* swp_forward over [t0, t0+nsteps) that keeps every state: states[g] holds
+ * nsteps+1 contiguous Fourier states (slot 0 <- st[g].fourier, slot k <- the
+ * state after k steps); the final state is also copied back into st[g].fourier.
+ * The forward sweep of a differentiable run when the whole trajectory fits in
+ * device memory (at B=256, M=42, FP32 and 1440 steps: 154 GB), so that the
+ * adjoint needs no recomputation -- what jax.grad through lax.scan stores
+ * without remat (model.py:1237-1342).  Diagnostics off.  Captured once into a
+ * CUDA graph per argument set and replayed. */
+int swp_forward_stored(swp_plan* plan, const swp_group_state* st, const swp_flags* flags,
+                       int t0, int nsteps, void* const* states, void* stream);
+
+/* Adjoint of the steps t0+nsteps-1 down to t0 over the states kept by
+ * swp_forward_stored (no recomputation).  adj[g].lam: adjoint of the state at
+ * t0+nsteps on entry, at t0 on exit; adj[g].grad accumulates. */
+int swp_adjoint_stored(swp_plan* plan, const swp_group_state* st, void* const* states,
+                       const swp_group_adjoint* adj, const swp_flags* flags, int t0, int nsteps, void* stream);
+
 /* Average device time (ms, CUDA events on `stream`) over nrep launches of the
  * step kernels on st (modified in place): ms_out[0] spectral (Legendre) kernel,
  * [1] grid kernel, and with adj != NULL [2] grid adjoint, [3] spectral adjoint.

@@ -72,7 +72,8 @@ EXPORTS = (
     "swp_init_state", "swp_diagnose_winds", "swp_forward", "swp_output_physical",
     "swp_state_copy", "swp_adjoint_step", "swp_adjoint_seed", "swp_adjoint_init",
     "swp_adjoint_window", "swp_time_kernels", "swp_forward_checkpointed", "swp_adjoint_step_noalloc",
-    "swp_tc_selftest", "swp_device_status", "swp_plan_uses_tensor_cores",
+    "swp_tc_selftest", "swp_device_status", "swp_plan_uses_tensor_cores", "swp_forward_stored",
+    "swp_adjoint_stored",
 )
 
 _lib = None
@@ -116,6 +117,8 @@ def load(path: os.PathLike | str | None = None) -> ctypes.CDLL:
         "swp_tc_selftest": (i, [vp, vp, vp, i, i, i, vp]),
         "swp_device_status": (i, [vp, ip, vp]),
         "swp_plan_uses_tensor_cores": (i, [vp]),
+        "swp_forward_stored": (i, [vp, gsp, fp, i, i, vpp, vp]),
+        "swp_adjoint_stored": (i, [vp, gsp, vpp, gap, fp, i, i, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -27,9 +27,24 @@ GRAD_PARAMS = ("taurad", "taudrag", "DPhieq", "Phibar")
 
 
 class Integration:
-    """Forward + checkpointed adjoint for an :class:`Engine` (all groups)."""
+    """Forward + adjoint of a whole run for an :class:`Engine` (all groups).
 
-    def __init__(self, engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, ckpt_every: int = 50):
+    Two ways to give the adjoint the primal states it needs:
+
+    * ``store="all"``: the forward sweep keeps every state (nsteps + 1 Fourier
+      states per group) and the adjoint runs straight over them: no
+      recomputation.  At B=256, M=42, FP32, 1440 steps that is 154 GB, which
+      GB300's HBM holds.
+    * ``store="checkpoint"``: the state every ``ckpt_every`` steps is kept; each
+      window is recomputed from its checkpoint before its adjoint steps (one
+      extra forward sweep, memory O(nsteps / ckpt_every + ckpt_every)).
+
+    ``store="auto"`` (default) keeps everything when it fits in
+    ``mem_fraction`` of the free device memory, else checkpoints.
+    """
+
+    def __init__(self, engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, ckpt_every: int = 50,
+                 store: str = "auto", mem_fraction: float = 0.8):
         if flags.scheme != 0:
             raise NotImplementedError("the adjoint is implemented for the modified-Euler scheme")
         if flags.test == 1:
@@ -46,12 +61,33 @@ class Integration:
         self.ckpt: List[torch.Tensor] = []
         self.ics: List[torch.Tensor] = []
         self._slots = None
+        self._states = None
+        if store not in ("auto", "all", "checkpoint"):
+            raise ValueError(f"store must be 'auto', 'all' or 'checkpoint', got {store!r}")
+        if store == "auto":
+            need = (self.nsteps + 1) * engine.state_bytes()
+            free, _ = torch.cuda.mem_get_info(engine.device)
+            store = "all" if need <= mem_fraction * free else "checkpoint"
+        self.store = store
+
+    def release(self) -> None:
+        """Drop the stored states, checkpoints and window slots."""
+        self._states = None
+        self._slots = None
+        self.ckpt = []
 
     # ------------------------------------------------------------- forward
     def run_forward(self, ics: Sequence[torch.Tensor]) -> List[torch.Tensor]:
         eng = self.eng
         self.ics = [x.to(device=eng.device, dtype=eng.rdtype).contiguous() for x in ics]
         eng.init_state(self.ics, self.flags)
+        if self.store == "all":
+            if self._states is None:
+                self._states = [torch.empty((self.nsteps + 1,) + tuple(gd["fourier"].shape), dtype=eng.cdtype,
+                                            device=eng.device) for gd in eng.groups]
+            eng.forward_stored(self.flags, self.t0, self.nsteps, self._states)
+            out = eng.output_physical(self.flags)
+            return [o[:5] for o in out]
         if not self.ckpt:
             self.ckpt = [torch.empty((self.nwin,) + tuple(gd["fourier"].shape), dtype=eng.cdtype, device=eng.device)
                          for gd in eng.groups]
@@ -64,6 +100,10 @@ class Integration:
         eng = self.eng
         lam, lamy, grad = eng.new_adjoint_buffers()
         eng.adjoint_seed(dphys, lam)
+        if self.store == "all":
+            eng.adjoint_stored(self.flags, self._states, lam, lamy, grad, t0=self.t0, nsteps=self.nsteps)
+            dic = eng.adjoint_init(self.flags, self.ics, lam, grad)
+            return dic, grad
         if self._slots is None:
             self._slots = [torch.empty((self.K + 1,) + tuple(gd["fourier"].shape), dtype=eng.cdtype, device=eng.device)
                            for gd in eng.groups]
@@ -108,7 +148,7 @@ class _IntegrateFn(torch.autograd.Function):
 
 
 def integrate(engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, params: Sequence[dict], ics: Sequence[torch.Tensor],
-              ckpt_every: int = 50, integration: Integration = None):
+              ckpt_every: int = 50, integration: Integration = None, store: str = "auto"):
     """Differentiable run of every group of ``engine``.
 
     params[g]: dict with (B,) tensors 'taurad', 'taudrag', 'DPhieq', 'Phibar'
@@ -116,9 +156,10 @@ def integrate(engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, params: Se
     ics[g]: (5, B, J, I) physical eta, delta, Phi, U, V.  Returns per group a
     (5, B, J, I) tensor of the final physical curr fields.  Passing the same
     ``integration`` object across calls reuses its checkpoint buffers and the
-    library's captured CUDA graphs.
+    library's captured CUDA graphs.  ``store`` selects how the adjoint gets
+    its primal states (see :class:`Integration`).
     """
-    integ = integration if integration is not None else Integration(engine, flags, t0, nsteps, ckpt_every)
+    integ = integration if integration is not None else Integration(engine, flags, t0, nsteps, ckpt_every, store)
     flat = []
     for g, gd in enumerate(engine.groups):
         for k in GRAD_PARAMS:

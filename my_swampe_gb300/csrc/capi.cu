@@ -518,6 +518,69 @@ int forward_ckpt_impl(swp_plan* p, const swp_group_state* st, const swp_flags* f
   return run_graph(p, key, body, s);
 }
 
+// Forward over [t0, t0+nsteps) keeping every state: states[g] holds nsteps+1
+// contiguous Fourier states (slot 0 = the state at t0).  The final state is
+// copied back into st[g].fourier.
+template <typename T>
+int forward_stored_impl(swp_plan* p, const swp_group_state* st, const swp_flags* f, int t0, int nsteps,
+                        void* const* states, cudaStream_t s) {
+  size_t es = sizeof(typename cplx<T>::type);
+  auto body = [&](cudaStream_t cs) -> int {
+    for (int g = 0; g < p->ng; ++g) {
+      size_t bytes = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
+      int rc = cuda_check(p, cudaMemcpyAsync(states[g], st[g].fourier, bytes, cudaMemcpyDeviceToDevice, cs),
+                          "stored forward: first state");
+      if (rc) return rc;
+    }
+    int rc = forward_steps<T>(p, st, f, t0, nsteps, 0, 1, states, cs);
+    if (rc) return rc;
+    for (int g = 0; g < p->ng; ++g) {
+      size_t bytes = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
+      rc = cuda_check(p, cudaMemcpyAsync(st[g].fourier, (const char*)states[g] + (size_t)nsteps * bytes, bytes,
+                                         cudaMemcpyDeviceToDevice, cs), "stored forward: last state");
+      if (rc) return rc;
+    }
+    return SWP_OK;
+  };
+  std::vector<uint64_t> key = {4, (uint64_t)t0, (uint64_t)nsteps};
+  key_flags(key, f);
+  key_state(key, p, st);
+  for (int g = 0; g < p->ng; ++g) key.push_back((uint64_t)states[g]);
+  return run_graph(p, key, body, s);
+}
+
+// Adjoint sweep over states stored by forward_stored_impl: steps t0+nsteps-1
+// down to t0, no recomputation.
+template <typename T>
+int adjoint_stored_impl(swp_plan* p, const swp_group_state* st, void* const* states, const swp_group_adjoint* adj,
+                        const swp_flags* f, int t0, int nsteps, cudaStream_t s) {
+  size_t es = sizeof(typename cplx<T>::type);
+  auto body = [&](cudaStream_t cs) -> int {
+    int rc = update_coefs<T>(p, st, cs);
+    if (rc) return rc;
+    std::vector<swp_group_state> a(p->ng), b(p->ng);
+    for (int k = nsteps - 1; k >= 0; --k) {
+      for (int g = 0; g < p->ng; ++g) {
+        size_t ss = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
+        a[g] = st[g]; b[g] = st[g];
+        a[g].fourier = (char*)states[g] + (size_t)k * ss;
+        b[g].fourier = (char*)states[g] + (size_t)(k + 1) * ss;
+      }
+      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, t0 + k, cs, false);
+      if (rc) return rc;
+    }
+    return SWP_OK;
+  };
+  std::vector<uint64_t> key = {5, (uint64_t)t0, (uint64_t)nsteps};
+  key_flags(key, f);
+  for (int g = 0; g < p->ng; ++g) {
+    key.push_back((uint64_t)states[g]); key.push_back((uint64_t)adj[g].lam); key.push_back((uint64_t)adj[g].lam_y);
+    key.push_back((uint64_t)adj[g].grad); key.push_back((uint64_t)st[g].params); key.push_back((uint64_t)st[g].resid);
+    key.push_back((uint64_t)st[g].member);
+  }
+  return run_graph(p, key, body, s);
+}
+
 }  // namespace
 
 namespace swp {
@@ -783,6 +846,32 @@ int swp_forward_checkpointed(swp_plan* p, const swp_group_state* st, const swp_f
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? forward_ckpt_impl<double>(p, st, f, t0, nsteps, ckpt_every, ckpt, s)
                                   : forward_ckpt_impl<float>(p, st, f, t0, nsteps, ckpt_every, ckpt, s);
+}
+
+int swp_forward_stored(swp_plan* p, const swp_group_state* st, const swp_flags* f, int t0, int nsteps,
+                       void* const* states, void* stream) {
+  if (!p || !st || !f || !states) return fail(p, SWP_ERR_ARG, "null argument");
+  if (nsteps < 1) return fail(p, SWP_ERR_ARG, "nsteps must be >= 1");
+  if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "stored forward runs with diagnostics off");
+  for (int g = 0; g < p->ng; ++g)
+    if (!states[g] || !st[g].fourier || !st[g].params || !st[g].member) return fail(p, SWP_ERR_ARG, "missing buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWP_FP64 ? forward_stored_impl<double>(p, st, f, t0, nsteps, states, s)
+                                  : forward_stored_impl<float>(p, st, f, t0, nsteps, states, s);
+}
+
+int swp_adjoint_stored(swp_plan* p, const swp_group_state* st, void* const* states, const swp_group_adjoint* adj,
+                       const swp_flags* f, int t0, int nsteps, void* stream) {
+  if (!p || !st || !states || !adj || !f) return fail(p, SWP_ERR_ARG, "null argument");
+  if (nsteps < 1) return fail(p, SWP_ERR_ARG, "nsteps must be >= 1");
+  if (f->scheme != 0) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint is implemented for the modified-Euler scheme");
+  if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint of test=1 (fixed winds) is not implemented");
+  if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint runs with diagnostics off (no blow-up gate)");
+  for (int g = 0; g < p->ng; ++g)
+    if (!states[g] || !adj[g].lam || !adj[g].lam_y || !st[g].params) return fail(p, SWP_ERR_ARG, "missing buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWP_FP64 ? adjoint_stored_impl<double>(p, st, states, adj, f, t0, nsteps, s)
+                                  : adjoint_stored_impl<float>(p, st, states, adj, f, t0, nsteps, s);
 }
 
 }  // extern "C"

@@ -265,6 +265,22 @@ class Engine:
                                                       _lib.ptr_array([c.data_ptr() for c in ckpt]), self.stream),
                     "forward_checkpointed")
 
+    def forward_stored(self, flags: RunFlagsC, t0: int, nsteps: int, states) -> None:
+        """states[g]: (nsteps+1, NFOURIER, M+1, B, J) buffer receiving every state of the run."""
+        self._check(self.lib.swp_forward_stored(self._plan, self._states(), ctypes.byref(flags.c()), int(t0), int(nsteps),
+                                                _lib.ptr_array([x.data_ptr() for x in states]), self.stream),
+                    "forward_stored")
+
+    def adjoint_stored(self, flags: RunFlagsC, states, lam, lamy, grad, t0: int, nsteps: int) -> None:
+        """Adjoint sweep over the states kept by forward_stored (no recomputation)."""
+        self._check(self.lib.swp_adjoint_stored(self._plan, self._states(), _lib.ptr_array([x.data_ptr() for x in states]),
+                                                self._adjs(lam, lamy, grad), ctypes.byref(flags.c()), int(t0),
+                                                int(nsteps), self.stream), "adjoint_stored")
+
+    def state_bytes(self) -> int:
+        """Bytes of one Fourier state of every group."""
+        return sum(gd["fourier"].numel() * gd["fourier"].element_size() for gd in self.groups)
+
     def adjoint_window(self, flags: RunFlagsC, ckpt_state, slots, lam, lamy, grad, t0: int, nsteps: int) -> None:
         """ckpt_state[g]: Fourier state at t0; slots[g]: (nsteps+1, NFOURIER, M+1, B, J) scratch."""
         self._check(self.lib.swp_adjoint_window(self._plan, self._states(fourier=ckpt_state),

@@ -28,7 +28,7 @@ def _case(M=42, seed=0):
     return params, (eta0, delta0, Phi0, U0, V0), W
 
 
-def _gpu_grads(params, ics, W, nsteps, ckpt_every, M=42, precision="fp64"):
+def _gpu_grads(params, ics, W, nsteps, ckpt_every, M=42, precision="fp64", store="checkpoint"):
     import torch
     from my_swampe_gb300.engine import Engine, RunFlagsC
     from my_swampe_gb300.adjoint import integrate
@@ -40,7 +40,8 @@ def _gpu_grads(params, ics, W, nsteps, ckpt_every, M=42, precision="fp64"):
     p = {k: torch.tensor([params[k]], dtype=torch.float64, device=dev, requires_grad=True)
          for k in ("taurad", "taudrag", "DPhieq", "Phibar")}
     ic = torch.tensor(np.stack(ics)[:, None], dtype=torch.float64, device=dev, requires_grad=True)
-    out = integrate(eng, RunFlagsC(), t0=2, nsteps=nsteps, params=[p], ics=[ic], ckpt_every=ckpt_every)[0]
+    out = integrate(eng, RunFlagsC(), t0=2, nsteps=nsteps, params=[p], ics=[ic], ckpt_every=ckpt_every,
+                    store=store)[0]
     Wt = torch.tensor(W[:, None], dtype=torch.float64, device=dev)
     loss = (out.double() * Wt).sum()
     loss.backward()
@@ -130,3 +131,18 @@ def test_fast_adjoint_matches_fp64_adjoint(cuda):
         scale = np.max(np.abs(ic64[f]))
         rel = np.linalg.norm(ic32[f] - ic64[f]) / max(np.linalg.norm(ic64[f]), 1e-300)
         assert rel <= 2e-4, (f, rel)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fast"])
+def test_stored_states_adjoint_matches_checkpointed(cuda, precision):
+    """The adjoint over stored states (no recomputation) equals the checkpointed
+    adjoint: same loss bit for bit, same initial-field gradients bit for bit
+    (no atomics on that path), parameter gradients to the order of their FP64
+    atomic reductions."""
+    params, ics, W = _case(seed=4)
+    loss_a, g_a, ic_a = _gpu_grads(params, ics, W, nsteps=23, ckpt_every=5, precision=precision, store="all")
+    loss_c, g_c, ic_c = _gpu_grads(params, ics, W, nsteps=23, ckpt_every=5, precision=precision, store="checkpoint")
+    assert loss_a == loss_c
+    np.testing.assert_array_equal(ic_a, ic_c)
+    for k in g_a:
+        assert abs(g_a[k] - g_c[k]) <= 1e-12 * max(abs(g_c[k]), 1e-300), (k, g_a[k], g_c[k])
