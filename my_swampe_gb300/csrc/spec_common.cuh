@@ -158,23 +158,34 @@ __device__ __forceinline__ void step_combos(const SpecGroup<T>& G, const StepCfg
 // Robert-Asselin mid carry (model.py:988-1110) and the winds.  All loads come
 // before the first store: the input and output states may be one buffer, so
 // the compiler could not reorder them itself.
+// The carries the write-out of a point reads: old curr (3) and RA mid (3).
 template <typename T>
-__device__ __forceinline__ void write_step_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
-                                                 size_t o, T al, const typename cplx<T>::type* nw_in, bool uv,
-                                                 typename cplx<T>::type u, typename cplx<T>::type v) {
+__device__ __forceinline__ void load_step_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
+                                                size_t o, typename cplx<T>::type* old, typename cplx<T>::type* mid) {
   typedef typename cplx<T>::type T2;
   const T2* Fi = G.four;
-  T2* Fo = G.four_out;
   const int cf[3] = {F_ETA, F_DELTA, F_PHI};
-  const int pf[3] = {F_ETA_PREV, F_DELTA_PREV, F_PHI_PREV};
   const int rf[3] = {F_ETA_MID, F_DELTA_MID, F_PHI_MID};
   const bool need_old = incr || cfg.write_prev || cfg.ra_mode;
-  T2 old[3], mid[3];
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
     old[q] = need_old ? Fi[cf[q] * FS + o] : mk<T2>(0, 0);
     mid[q] = cfg.ra_mode == 2 ? Fi[rf[q] * FS + o] : mk<T2>(0, 0);
   }
+}
+
+// write_step_point with its carries already loaded (load_step_point)
+template <typename T>
+__device__ __forceinline__ void store_step_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
+                                                 size_t o, T al, const typename cplx<T>::type* nw_in, bool uv,
+                                                 typename cplx<T>::type u, typename cplx<T>::type v,
+                                                 const typename cplx<T>::type* old,
+                                                 const typename cplx<T>::type* mid) {
+  typedef typename cplx<T>::type T2;
+  T2* Fo = G.four_out;
+  const int cf[3] = {F_ETA, F_DELTA, F_PHI};
+  const int pf[3] = {F_ETA_PREV, F_DELTA_PREV, F_PHI_PREV};
+  const int rf[3] = {F_ETA_MID, F_DELTA_MID, F_PHI_MID};
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
     T2 nw = nw_in[q];
@@ -191,6 +202,15 @@ __device__ __forceinline__ void write_step_point(const SpecGroup<T>& G, const St
     Fo[F_U * FS + o] = u;
     Fo[F_V * FS + o] = v;
   }
+}
+
+template <typename T>
+__device__ __forceinline__ void write_step_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
+                                                 size_t o, T al, const typename cplx<T>::type* nw_in, bool uv,
+                                                 typename cplx<T>::type u, typename cplx<T>::type v) {
+  typename cplx<T>::type old[3], mid[3];
+  load_step_point<T>(G, cfg, incr, FS, o, old, mid);
+  store_step_point<T>(G, cfg, incr, FS, o, al, nw_in, uv, u, v, old, mid);
 }
 
 }  // namespace swp

@@ -228,7 +228,10 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   const int jp = (warp & 3) * 8 + (lane & 7);
   const int bt = (warp >> 2) * 4 + (lane >> 3);
   T2 xs[NSLOT], xa[NSLOT];
-  bool ok = tc::mbar_wait_bounded(&mbar[3], 0);
+  T2 pold[2][3], pmid[2][3];  // write-out carries, loaded ahead of GEMM2
+  // one thread waits on each mbarrier and the block barrier releases the rest:
+  // 256 spinning threads would take issue slots from the co-resident CTA
+  bool ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[3], 0) : true;
   ok = __syncthreads_and(ok);
   if (ok) {
     const T2* stg = (const T2*)sA;
@@ -293,9 +296,9 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       tc::mma_commit(&mbar[1]);
       n_c1 = 1;
     }
-    ok = tc::mbar_wait_bounded(&mbar[1], 0);
-    tc::fence_after_sync();
+    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 0) : true;
     ok = __syncthreads_and(ok);
+    tc::fence_after_sync();
     ok = ok && !*sflag;  // written by thread 0 before the barrier: the same value for every thread
   }
   if (ok) {
@@ -308,9 +311,9 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       tc::mma_commit(&mbar[1]);
       n_c1 = 2;
     }
-    ok = tc::mbar_wait_bounded(&mbar[1], 1);
-    tc::fence_after_sync();
+    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 1) : true;
     ok = __syncthreads_and(ok);
+    tc::fence_after_sync();
   }
   if (ok) {
     // B1 is no longer read: fetch B2 into the same buffer, overlapped with the epilogue
@@ -403,6 +406,15 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     __syncthreads();
     tc::fence_after_sync();
     // ---- phase 5: GEMM2, both parities (rows 112..127 read the staging area and are ignored)
+    // Each thread first issues the global loads of its write-out points (the
+    // two (member, j) points t and t + 256 of phase 7), so that their latency
+    // overlaps the GEMM.
+    static_assert(TC_MT * TC_J == 2 * 256, "two write-out points per thread");
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int t = threadIdx.x + u * 256, bti = t / J, j = t % J;
+      if (bti < mt) load_step_point<T>(G, cfg, incr, FS, ((size_t)m * G.B + b0 + bti) * J + j, pold[u], pmid[u]);
+    }
     if (threadIdx.x == 0) {
       if (!tc::mbar_wait_bounded(&mbar[0], 1)) *sflag = 1;
       if (!*sflag) {
@@ -416,9 +428,9 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       tc::mma_commit(&mbar[2]);
       n_c2 = 1;
     }
-    ok = tc::mbar_wait_bounded(&mbar[2], 0);
-    tc::fence_after_sync();
+    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[2], 0) : true;
     ok = __syncthreads_and(ok);
+    tc::fence_after_sync();
     ok = ok && !*sflag;
   }
   if (ok) {
@@ -452,15 +464,16 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     tc::fence_before_sync();
     __syncthreads();
     // ---- phase 7: write-out and carries (coalesced along j), as in k_spectral
-    for (int t = threadIdx.x; t < TC_MT * J; t += blockDim.x) {
-      const int bti = t / J, j = t % J;
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int t = threadIdx.x + u * 256, bti = t / J, j = t % J;
       if (bti >= mt || sdead[bti]) continue;
       const int b = b0 + bti;
       const size_t o = ((size_t)m * G.B + b) * J + j;
       auto get = [&](int f) { return *(const float2*)&Out[(size_t)(f * TC_MT + bti) * TC_OST + 2 * j]; };
       const T2 nw[3] = {get(0), get(1), get(2)};
-      write_step_point<T>(G, cfg, incr, FS, o, G.mco[MC_ALPHA * G.B + b], nw, cfg.test != 1, cadd(get(3), get(5)),
-                          cadd(get(4), get(6)));
+      store_step_point<T>(G, cfg, incr, FS, o, G.mco[MC_ALPHA * G.B + b], nw, cfg.test != 1, cadd(get(3), get(5)),
+                          cadd(get(4), get(6)), pold[u], pmid[u]);
     }
     if (m == 0 && threadIdx.x < mt && !sdead[threadIdx.x]) {
       const int b = b0 + threadIdx.x;
