@@ -639,16 +639,15 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
     int mt = 8;
     while (mt > 1 && (f64 ? spec_smem_bytes<double>(M[g], J, mt) : spec_smem_bytes<float>(M[g], J, mt)) > cap) mt /= 2;
     p->MT[g] = std::min(mt, B[g]);
-    // rows per grid CTA, fixed per truncation at compile time: 4 keeps several
-    // CTAs per SM resident; 2 where the adjoint's 12 transforms per row would not fit
-    int jb = grid_rows_per_cta(M[g], f64);
-    p->JB[g] = jb;
+    // rows per grid CTA: fixed per truncation and mode at compile time (grid.cu grid_jb)
+    p->JB[g] = grid_rows_per_cta(M[g], f64, GM_STEP);
     size_t ss = f64 ? spec_smem_bytes<double>(M[g], J, p->MT[g]) : spec_smem_bytes<float>(M[g], J, p->MT[g]);
     p->spec_smem = std::max(p->spec_smem, ss);
     size_t sa = f64 ? spec_adj_smem_bytes<double>(M[g], J, p->MT[g]) : spec_adj_smem_bytes<float>(M[g], J, p->MT[g]);
     p->spec_adj_smem = std::max(p->spec_adj_smem, sa);
     for (int mode = 0; mode < 8; ++mode) {
-      size_t gs = f64 ? grid_smem_bytes<double>(M[g], J, I, jb, mode) : grid_smem_bytes<float>(M[g], J, I, jb, mode);
+      const int jbm = grid_rows_per_cta(M[g], f64, mode);
+      size_t gs = f64 ? grid_smem_bytes<double>(M[g], J, I, jbm, mode) : grid_smem_bytes<float>(M[g], J, I, jbm, mode);
       p->grid_smem[mode] = std::max(p->grid_smem[mode], gs);
     }
   }

@@ -676,11 +676,16 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
   }
 }
 
-// JB (latitude rows per CTA) of each truncation: 4, or 2 where the adjoint
-// step's 12 transforms per row would not fit in 200 KB of shared memory.
+// JB (latitude rows per CTA) of a truncation and mode: 8 where the mode's two
+// transform buffers stay within 72 KB (three or more CTAs per SM), else 4, or
+// 2 where even 4 rows would exceed 200 KB (the FP64 adjoint at M=106).
 template <typename T>
-__host__ __device__ constexpr int grid_jb(int M) {
-  return (size_t)2 * grid_ntr(GM_ADJ_STEP) * 4 * (trunc_I(M) / 2 + 1) * 2 * sizeof(T) <= 200 * 1024 ? 4 : 2;
+__host__ __device__ constexpr size_t grid_buf_bytes(int M, int mode, int jb) {
+  return (size_t)2 * grid_ntr(mode) * jb * (trunc_I(M) / 2 + 1) * 2 * sizeof(T);
+}
+template <typename T>
+__host__ __device__ constexpr int grid_jb(int M, int mode) {
+  return grid_buf_bytes<T>(M, mode, 8) <= 72 * 1024 ? 8 : grid_buf_bytes<T>(M, mode, 4) <= 200 * 1024 ? 4 : 2;
 }
 
 template <typename T, int MODE>
@@ -688,13 +693,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_grid(const __gr
   int idx;
   const GridGroup<T>& G = pick_ggroup(Lc, idx);
   switch (G.g.M) {  // groups of different truncations share one launch
-    case 42: grid_body<T, MODE, 42, grid_jb<T>(42)>(Lc, G, idx); break;
-    case 63: grid_body<T, MODE, 63, grid_jb<T>(63)>(Lc, G, idx); break;
-    default: grid_body<T, MODE, 106, grid_jb<T>(106)>(Lc, G, idx); break;
+    case 42: grid_body<T, MODE, 42, grid_jb<T>(42, MODE)>(Lc, G, idx); break;
+    case 63: grid_body<T, MODE, 63, grid_jb<T>(63, MODE)>(Lc, G, idx); break;
+    default: grid_body<T, MODE, 106, grid_jb<T>(106, MODE)>(Lc, G, idx); break;
   }
 }
 
-int grid_rows_per_cta(int M, bool fp64) { return fp64 ? grid_jb<double>(M) : grid_jb<float>(M); }
+int grid_rows_per_cta(int M, bool fp64, int mode) { return fp64 ? grid_jb<double>(M, mode) : grid_jb<float>(M, mode); }
 
 // Largest dynamic shared memory the kernel may request: 227 KB per block minus
 // the kernel's static shared memory (the pointer tables of stage_rows / write_r2c).
@@ -717,7 +722,19 @@ void grid_set_attributes() {
 }
 
 template <typename T>
-cudaError_t launch_grid(const GridLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
+cudaError_t launch_grid(const GridLaunch<T>& L0, int nblocks0, size_t smem, cudaStream_t s) {
+  // rows per CTA and the block decomposition follow the mode (grid_jb)
+  (void)nblocks0;
+  GridLaunch<T> L = L0;
+  int nblocks = 0;
+  for (int g = 0; g < L.ng; ++g) {
+    GridGroup<T>& G = L.grp[g];
+    G.JB = grid_jb<T>(G.g.M, L.mode);
+    G.njb = G.g.J / G.JB;
+    L.prefix[g] = nblocks;
+    nblocks += G.B * G.njb;
+  }
+  L.prefix[L.ng] = nblocks;
   switch (L.mode) {
     case GM_STEP: k_grid<T, GM_STEP><<<nblocks, 256, smem, s>>>(L); break;
     case GM_INIT: k_grid<T, GM_INIT><<<nblocks, 256, smem, s>>>(L); break;

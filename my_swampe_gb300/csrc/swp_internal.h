@@ -180,7 +180,7 @@ template <typename T> cudaError_t launch_spec_adj(const SpecLaunch<T>& L, int nb
 template <typename T> cudaError_t launch_grid(const GridLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s);
 void spec_set_attributes();
 void grid_set_attributes();
-int grid_rows_per_cta(int M, bool fp64);  // JB the grid kernel is compiled for
+int grid_rows_per_cta(int M, bool fp64, int mode);  // JB the grid kernel is compiled for
 
 // tensor-core Legendre kernel of the FP32 modified-Euler step (tc_legendre.cu)
 struct TcBasis { const float* p[MAXG]; };  // packed basis of each group
