@@ -195,9 +195,28 @@ __device__ __forceinline__ void stage_rows(const C& c, const typename cplx<T>::t
   if (threadIdx.x < 16) s_src[threadIdx.x] = (int)threadIdx.x < nf ? src[threadIdx.x] : nullptr;
   __syncthreads();
   constexpr int n1 = C::M + 1;
-  for (int t = threadIdx.x; t < nf * n1 * C::JB; t += blockDim.x) {
-    const int r = t % C::JB, k = (t / C::JB) % n1, f = t / (C::JB * n1);
-    stage[(f * C::JB + r) * n1 + k] = s_src[f][((size_t)k * c.B + c.b) * C::J + c.j0 + r];
+  // batches of 8 loads in flight before their shared-memory stores (the compiler
+  // cannot move a global load above a store through a possibly aliasing pointer)
+  constexpr int NB = 8;
+  const int total = nf * n1 * C::JB;
+  for (int t0 = threadIdx.x; t0 < total; t0 += NB * blockDim.x) {
+    T2 v[NB];
+#pragma unroll
+    for (int u = 0; u < NB; ++u) {
+      const int t = t0 + u * blockDim.x;
+      if (t < total) {
+        const int r = t % C::JB, k = (t / C::JB) % n1, f = t / (C::JB * n1);
+        v[u] = s_src[f][((size_t)k * c.B + c.b) * C::J + c.j0 + r];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < NB; ++u) {
+      const int t = t0 + u * blockDim.x;
+      if (t < total) {
+        const int r = t % C::JB, k = (t / C::JB) % n1, f = t / (C::JB * n1);
+        stage[(f * C::JB + r) * n1 + k] = v[u];
+      }
+    }
   }
 }
 
@@ -624,16 +643,33 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     block_add_grads<T>(gacc, c.sred, G.grad, B, b);
     if (MODE == GM_ADJ_STEP) {
       // adjoint of x = Re(Y_0) + 2 Re sum_{m>=1} Y_m e^{i theta}:  lambda Y_m = c_m sum_i lambda x_i e^{-i theta}
-      T2* res = cfft_batch_c<-1, L>(zout, zin, 4 * JB, c.twL);
       const int n1 = M + 1;
       const int yf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
       const int rmap[5] = {0, -1, 1, 2, 3};
-      for (int t = threadIdx.x; t < 5 * n1 * JB; t += blockDim.x) {
-        int r = t % JB, k = (t / JB) % n1, q = t / (JB * n1);
-        size_t o = ((size_t)k * B + b) * J + j0 + r;
-        T2 v = G.lam[yf[q] * FS + o];
-        if (rmap[q] >= 0) v = cadd(v, r2c_post<T2, T>(res + ((size_t)rmap[q] * JB + r) * LS, L, k, c.twI, k == 0 ? (T)1 : (T)2));
-        G.lamy[(size_t)q * FS + o] = v;
+      constexpr int NY = 5 * (M + 1) * JB;
+      constexpr int NU = (NY + 255) / 256;
+      // a thread's lambda loads are issued before the transforms, so that
+      // their latency overlaps them, and before its first store
+      T2 lv[NU];
+#pragma unroll
+      for (int u = 0; u < NU; ++u) {
+        const int t = threadIdx.x + u * 256;
+        if (t < NY) {
+          const int r = t % JB, k = (t / JB) % n1, q = t / (JB * n1);
+          lv[u] = G.lam[yf[q] * FS + ((size_t)k * B + b) * J + j0 + r];
+        }
+      }
+      T2* res = cfft_batch_c<-1, L>(zout, zin, 4 * JB, c.twL);
+#pragma unroll
+      for (int u = 0; u < NU; ++u) {
+        const int t = threadIdx.x + u * 256;
+        if (t < NY) {
+          const int r = t % JB, k = (t / JB) % n1, q = t / (JB * n1);
+          const size_t o = ((size_t)k * B + b) * J + j0 + r;
+          T2 v = lv[u];
+          if (rmap[q] >= 0) v = cadd(v, r2c_post<T2, T>(res + ((size_t)rmap[q] * JB + r) * LS, L, k, c.twI, k == 0 ? (T)1 : (T)2));
+          G.lamy[(size_t)q * FS + o] = v;
+        }
       }
       return;
     }

@@ -647,6 +647,12 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
     T2 lF = cadd(cscale(lBeff, forc), lBf);
     T2 lG = csub(mk<T2>(0, 0), cadd(cscale(lAeff, forc), lAf));
     T2 z = mk<T2>(0, 0);
+    // primal values of the Phibar gradient, loaded before the stores below
+    T2 pdel = z, pphi = z, pE = z, pA = z, pB = z, pF = z, pG = z;
+    if (G.grad) {
+      pdel = PX[F_DELTA * FS + o]; pphi = PX[F_PHI * FS + o]; pE = PX[F_E * FS + o];
+      pA = PX[F_A * FS + o]; pB = PX[F_B * FS + o]; pF = PX[F_F * FS + o]; pG = PX[F_G * FS + o];
+    }
     LAM[F_ETA * FS + o] = leta; LAM[F_DELTA * FS + o] = ldel; LAM[F_PHI * FS + o] = lphi;
     LAM[F_A * FS + o] = lA; LAM[F_B * FS + o] = lB; LAM[F_C * FS + o] = lC; LAM[F_D * FS + o] = lD;
     LAM[F_E * FS + o] = lE; LAM[F_PHIF * FS + o] = lPF; LAM[F_F * FS + o] = lF; LAM[F_G * FS + o] = lG;
@@ -655,8 +661,7 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
     LAM[F_ETA_MID * FS + o] = z; LAM[F_DELTA_MID * FS + o] = z; LAM[F_PHI_MID * FS + o] = z;
     if (G.grad) {
       // d(combined inputs)/dPhibar (modEuler_tdiff.py:80-103, 185-193)
-      T2 del = PX[F_DELTA * FS + o], phi = PX[F_PHI * FS + o], E = PX[F_E * FS + o];
-      T2 A = PX[F_A * FS + o], Bm = PX[F_B * FS + o], Fm = PX[F_F * FS + o], Gm = PX[F_G * FS + o];
+      const T2 del = pdel, phi = pphi, E = pE, A = pA, Bm = pB, Fm = pF, Gm = pG;
       T2 Beff = cfg.forcflag ? cadd(Bm, Fm) : Bm, Aeff = cfg.forcflag ? csub(A, Gm) : A;
       T2 dP1 = csub(cscale(del, -dt), cscale(imul(xm, Beff), (T)0.5 * t1));
       T2 dH1 = cscale(Aeff, (T)-0.5 * t1);
