@@ -187,13 +187,23 @@ struct GridCtx {
 // Stage the rows j0..j0+JB-1 of `nf` Fourier fields of member b into `stage`
 // ([f][r][m], m fastest; the global reads are JB-long contiguous runs).  The
 // field pointers go through a shared-memory table rather than a local array.
+// With scale0 / scale (per field, may be null for 1) the staged value of m = 0
+// is multiplied by scale0[f] and those of m >= 1 by scale[f] (the C2R bin scales).
 template <typename T, typename C>
 __device__ __forceinline__ void stage_rows(const C& c, const typename cplx<T>::type* const* src, int nf,
-                                           typename cplx<T>::type* stage) {
+                                           typename cplx<T>::type* stage, const T* scale0 = nullptr,
+                                           const T* scale = nullptr) {
   typedef typename cplx<T>::type T2;
   __shared__ const T2* s_src[16];
-  if (threadIdx.x < 16) s_src[threadIdx.x] = (int)threadIdx.x < nf ? src[threadIdx.x] : nullptr;
+  __shared__ T s_sc[2][16];
+  if (threadIdx.x < 16) {
+    const bool on = (int)threadIdx.x < nf;
+    s_src[threadIdx.x] = on ? src[threadIdx.x] : nullptr;
+    s_sc[0][threadIdx.x] = (on && scale0) ? scale0[threadIdx.x] : (T)1;
+    s_sc[1][threadIdx.x] = (on && scale) ? scale[threadIdx.x] : (T)1;
+  }
   __syncthreads();
+  const bool scaled = scale0 != nullptr;
   constexpr int n1 = C::M + 1;
   // batches of 8 loads in flight before their shared-memory stores (the compiler
   // cannot move a global load above a store through a possibly aliasing pointer)
@@ -214,22 +224,37 @@ __device__ __forceinline__ void stage_rows(const C& c, const typename cplx<T>::t
       const int t = t0 + u * blockDim.x;
       if (t < total) {
         const int r = t % C::JB, k = (t / C::JB) % n1, f = t / (C::JB * n1);
-        stage[(f * C::JB + r) * n1 + k] = v[u];
+        stage[(f * C::JB + r) * n1 + k] = scaled ? cscale(v[u], s_sc[k == 0 ? 0 : 1][f]) : v[u];
       }
     }
   }
 }
 
-// Z spectra of the C2R transforms of the staged rows: out[(f*JB + r)*LS + k].
+// C2R of the `nf` x JB staged rows (layout of stage_rows, scales already
+// applied): the half-length spectrum Z (c2r_pre) is formed inside the first,
+// twiddle-free radix-8 pass, which writes `other`; the remaining passes run in
+// place of the staged rows.  Returns the buffer holding x_{2n} + i x_{2n+1}
+// ([t][n], stride LS).
 template <typename T, typename C>
-__device__ __forceinline__ void build_c2r(const C& c, const typename cplx<T>::type* stage, int nf,
-                                          const T* scale0, const T* scale, typename cplx<T>::type* out) {
-  constexpr int n1 = C::M + 1;
-  for (int t = threadIdx.x; t < nf * C::JB * C::L; t += blockDim.x) {
-    const int k = t % C::L, fr = t / C::L, f = fr / C::JB;
-    out[(size_t)fr * C::LS + k] = c2r_pre<typename cplx<T>::type, T>(stage + (size_t)fr * n1, 1, C::M, C::L, k,
-                                                                    c.twI, scale0[f], scale[f]);
+__device__ __forceinline__ typename cplx<T>::type* c2r_transform(const C& c, typename cplx<T>::type* stage, int nf,
+                                                                  typename cplx<T>::type* other) {
+  typedef typename cplx<T>::type T2;
+  constexpr int L = C::L, LS = C::LS, PER = L / 8, n1 = C::M + 1;
+  const int ntr = nf * C::JB;
+  const FastDiv divt(ntr);
+  for (int task = threadIdx.x; task < ntr * PER; task += blockDim.x) {
+    const int j = divt(task), t = task - j * ntr;
+    const T2* y = stage + (size_t)t * n1;
+    T2 v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = c2r_pre<T2, T>(y, 1, C::M, L, j + r * PER, c.twI, (T)1, (T)1);
+    dftR<8, +1>(v);
+    T2* dst = other + (size_t)t * LS + j * 8;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) dst[r] = v[r];
   }
+  __syncthreads();
+  return cfft_rest_c<+1, L>(other, stage, ntr, c.twL);
 }
 
 // Truncated R2C bins of `nf` transforms in `res` (stride LS) written to global
@@ -330,12 +355,10 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       fl[nf++] = F_U; fl[nf++] = F_V;
     }
     const T2* src[8];
-    T one[8];
     T wv[8];
     int rfv[8];
 #pragma unroll
     for (int f = 0; f < 8; ++f) {
-      one[f] = (T)1;
       wv[f] = (T)0;
       rfv[f] = 0;
       src[f] = nullptr;
@@ -356,9 +379,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     __syncthreads();
     stage_rows<T>(c, src, nf, bufB);
     __syncthreads();
-    build_c2r<T>(c, bufB, nf, one, one, bufA);
-    __syncthreads();
-    T2* zin = cfft_batch_c<+1, L>(bufA, bufB, nf * JB, c.twL);
+    T2* zin = c2r_transform<T>(c, bufB, nf, bufA);
     T2* zout = (zin == bufA) ? bufB : bufA;
     // initial-condition residual (non-zero only before a member's first step and
     // for the fixed test-1 winds): added in shared memory, off the hot loop
@@ -517,10 +538,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     }
     __syncthreads();
     // band-limited reconstruction -> residual = x - C2R(trunc FFT(x))
-    T one[5] = {(T)1, (T)1, (T)1, (T)1, (T)1};
-    build_c2r<T>(c, other, nf, one, one, res);
-    __syncthreads();
-    T2* zr = cfft_batch_c<+1, L>(res, other, nf * JB, c.twL);
+    T2* zr = c2r_transform<T>(c, other, nf, res);
     for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
       int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
       size_t po = f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
@@ -594,11 +612,9 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       else { src[f] = nullptr; s0[f] = s1[f] = (T)0; }
     }
     __syncthreads();
-    stage_rows<T>(c, src, nb1, bufB);
+    stage_rows<T>(c, src, nb1, bufB, s0, s1);
     __syncthreads();
-    build_c2r<T>(c, bufB, nb1, s0, s1, bufA);
-    __syncthreads();
-    T2* zin = cfft_batch_c<+1, L>(bufA, bufB, nb1 * JB, c.twL);
+    T2* zin = c2r_transform<T>(c, bufB, nb1, bufA);
     T2* zout = (zin == bufA) ? bufB : bufA;
     T gacc[NGRAD] = {(T)0, (T)0, (T)0, (T)0};
     for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
@@ -680,11 +696,9 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     T s20[5], s21[5];
 #pragma unroll
     for (int f = 0; f < 5; ++f) { src2[f] = G.lam + cf[f] * FS; s20[f] = invI; s21[f] = invI * (T)0.5; }
-    stage_rows<T>(c, src2, 5, bufB);
+    stage_rows<T>(c, src2, 5, bufB, s20, s21);
     __syncthreads();
-    build_c2r<T>(c, bufB, 5, s20, s21, bufA);
-    __syncthreads();
-    T2* z2 = cfft_batch_c<+1, L>(bufA, bufB, 5 * JB, c.twL);
+    T2* z2 = c2r_transform<T>(c, bufB, 5, bufA);
     for (int t = threadIdx.x; t < 5 * JB * L; t += blockDim.x) {
       int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
       size_t po = f * PS + ((size_t)b * J + j0 + r) * I + 2 * n;

@@ -235,6 +235,25 @@ __device__ __forceinline__ T2* cfft_batch_c(T2* a, T2* b, int ntr, const T2* tw)
   }
 }
 
+// Passes 2.. of cfft_batch_c after a first radix-8 pass (NS = 1) that left its
+// output in `a`.  Returns the buffer holding the result.
+template <int SIGN, int L, typename T2>
+__device__ __forceinline__ T2* cfft_rest_c(T2* a, T2* b, int ntr, const T2* tw) {
+  static_assert(L == 64 || L == 96 || L == 160, "transform length");
+  if (L == 64) {
+    stockham_pass_c<8, SIGN, L, 8>(a, b, ntr, tw); __syncthreads();
+    return b;
+  } else if (L == 96) {
+    stockham_pass_c<4, SIGN, L, 8>(a, b, ntr, tw); __syncthreads();
+    stockham_pass_c<3, SIGN, L, 32>(b, a, ntr, tw); __syncthreads();
+    return a;
+  } else {
+    stockham_pass_c<4, SIGN, L, 8>(a, b, ntr, tw); __syncthreads();
+    stockham_pass_c<5, SIGN, L, 32>(b, a, ntr, tw); __syncthreads();
+    return a;
+  }
+}
+
 // Gauss grid of each supported truncation (the reference's M -> (J, I) table,
 // spectral_transform.py / model.py: 42 -> 64 x 128, 63 -> 96 x 192, 106 -> 160 x 320).
 __host__ __device__ constexpr int trunc_J(int M) { return M == 42 ? 64 : M == 63 ? 96 : 160; }
