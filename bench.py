@@ -254,8 +254,10 @@ def run_ours(args):
     # kernel roofline (CUDA events inside the library on the launching stream)
     kt = eng.time_kernels(flags, nrep=20, adjoint=True)
     per_step = {k: v for k, v in kt.items()}
-    # per model step of fwd+adjoint: spectral, grid run twice (forward + recompute), adjoints once
-    share = {"spectral": 2 * per_step["spectral"], "grid": 2 * per_step["grid"],
+    # per model step of fwd+adjoint: the adjoint kernels run once; the forward ones
+    # once with stored states, twice (forward + window recompute) with checkpoints
+    nfwd = 1 if integ.store == "all" else 2
+    share = {"spectral": nfwd * per_step["spectral"], "grid": nfwd * per_step["grid"],
              "grid_adj": per_step["grid_adj"], "spectral_adj": per_step["spectral_adj"]}
     dom = max(share, key=share.get)
     alg = _algorithmic_bytes(dom, B, elem=8)

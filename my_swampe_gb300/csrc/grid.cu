@@ -37,7 +37,7 @@ size_t grid_smem_bytes(int M, int J, int I, int JB, int mode) {
   size_t buf = ntr * LS * sizeof(typename cplx<T>::type);
   // two transform buffers, the dayside row, the twiddles (L + (L+1)), reductions
   return 2 * buf + (size_t)I * sizeof(T) + 16 + (size_t)(I + 1) * sizeof(typename cplx<T>::type) + 16 +
-         8 * sizeof(double);
+         8 * NGRAD * sizeof(double);
 }
 template size_t grid_smem_bytes<double>(int, int, int, int, int);
 template size_t grid_smem_bytes<float>(int, int, int, int, int);
@@ -274,16 +274,22 @@ __device__ __forceinline__ void write_r2c(const C& c, const typename cplx<T>::ty
   }
 }
 
-// Warp sums in the compute type, block and global sums in FP64.
+// Warp sums in the compute type into per-warp FP64 slots (no shared-memory
+// atomics), then one thread per gradient sums the 8 slots and adds to global.
 template <typename T>
 __device__ void block_add_grads(const T* gacc, double* sred, double* grad, int B, int b) {
+  const int warp = threadIdx.x >> 5;
   for (int q = 0; q < NGRAD; ++q) {
     T v = gacc[q];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&sred[q], (double)v);
+    if ((threadIdx.x & 31) == 0) sred[warp * NGRAD + q] = (double)v;
   }
   __syncthreads();
-  if (threadIdx.x < NGRAD && grad) atomicAdd(&grad[threadIdx.x * B + b], sred[threadIdx.x]);
+  if (threadIdx.x < NGRAD && grad) {
+    double acc = 0.0;
+    for (int w = 0; w < 8; ++w) acc += sred[w * NGRAD + threadIdx.x];
+    atomicAdd(&grad[threadIdx.x * B + b], acc);
+  }
 }
 
 template <typename T, int MODE, int MM, int JBB>
@@ -598,7 +604,6 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     pa.Pb = ph.Pb; pa.itr = ph.itr; pa.itd = ph.itd; pa.DPe = ph.DPe; pa.nodrag = ph.nodrag; pa.forced = ph.forced;
     const int nz = ph.forced ? 8 : 5;
     const int npr = (MODE == GM_ADJ_STEP) ? 4 : 0;  // primal fields transformed here (eta, Phi, U, V)
-    if (threadIdx.x < 4) c.sred[threadIdx.x] = 0.0;
     // batch 1: lambda of the nonlinear Fourier terms -> grid (adjoint of fft(x/I)[:M+1]:
     // lambda x_i = (1/I) Re sum_{m=0..M} lambda_m e^{i theta}) and the primal grid fields
     const T2* src[12];

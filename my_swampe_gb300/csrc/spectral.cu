@@ -368,7 +368,7 @@ size_t spec_adj_smem_bytes(int M, int J, int MT) {
   size_t sres = (size_t)NYS * cnt * R;
   size_t kad = (size_t)NK * cnt * R;
   size_t coef = (size_t)5 * MT * cnt;
-  return (x + bf + sres + kad + coef) * sizeof(T) + 64 * sizeof(double);
+  return (x + bf + sres + kad + coef) * sizeof(T) + 16 + (size_t)MT * (J / 32) * sizeof(double);
 }
 template size_t spec_adj_smem_bytes<double>(int, int, int);
 template size_t spec_adj_smem_bytes<float>(int, int, int);
@@ -405,11 +405,13 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
   T* sigm1 = sigP + MT * cntmax;
   T* sigPm1 = sigm1 + MT * cntmax;
   T* tcmn = sigPm1 + MT * cntmax;
-  // [MT] Phibar gradient partials: doubles, so round the address up to 16 bytes
+  // [MT][J/32] Phibar gradient partials of each warp-sized run of latitudes
+  // (doubles: round the address up to 16 bytes)
   double* sgrad = (double*)(((uintptr_t)(tcmn + MT * cntmax) + 15) & ~(uintptr_t)15);
+  const int nws = J / 32;
 
   load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, cntmax, sig, sigP, sigm1, sigPm1, tcmn);
-  if (threadIdx.x < MT) sgrad[threadIdx.x] = 0.0;
+  for (int t = threadIdx.x; t < MT * nws; t += blockDim.x) sgrad[t] = 0.0;
 
   // ---- phase 1: symmetrised adjoints of the step outputs at column m
   const T2* LY = G.lamY;  // [5][M+1][B][J]
@@ -673,11 +675,15 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
       // in the compute type, accumulate the warp sums in FP64
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) gp += __shfl_xor_sync(0xffffffffu, gp, off);
-      if ((threadIdx.x & 31) == 0) atomicAdd(&sgrad[bt], (double)gp);
+      if ((threadIdx.x & 31) == 0) sgrad[bt * nws + j / 32] = (double)gp;
     }
   }
   __syncthreads();
-  if (G.grad && threadIdx.x < mt) atomicAdd(&G.grad[G_PHIBAR * G.B + b0 + threadIdx.x], sgrad[threadIdx.x]);
+  if (G.grad && threadIdx.x < mt) {
+    double acc = 0.0;
+    for (int w = 0; w < nws; ++w) acc += sgrad[threadIdx.x * nws + w];
+    atomicAdd(&G.grad[G_PHIBAR * G.B + b0 + threadIdx.x], acc);
+  }
 }
 
 template <typename T>
