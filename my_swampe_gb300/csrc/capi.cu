@@ -30,6 +30,7 @@ struct swp_plan {
   // tensor-core Legendre kernel of the FP32 step (every group at M = 42)
   bool use_tc = false;
   float* tcbasis[MAXG] = {};
+  float* tcbasis_adj[MAXG] = {};
   void* coefmem[MAXG] = {};              // per-call coefficient tables (CoefTables) of each group
   int* d_err = nullptr;                  // device error word set by bounded waits that ran out
   std::string err;
@@ -159,6 +160,31 @@ cudaError_t launch_step_spec(const swp_plan* p, const SpecLaunch<T>& LS, int nbs
     }
   }
   return launch_spec<T>(LS, nbs, p->spec_smem, s);
+}
+
+// The Legendre adjoint of a modified-Euler step: tcgen05 on the FP32 path when
+// the plan packed the tensor-core basis, the SIMT kernel otherwise.
+template <typename T>
+cudaError_t launch_step_spec_adj(const swp_plan* p, const SpecLaunch<T>& LS, int nbs, cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (p->use_tc && LS.cfg.scheme == 0) {
+      SpecLaunch<float> LT = LS;
+      const int mt = spec_tc_members_per_cta();
+      int acc = 0;
+      TcBasis tb;
+      memset(&tb, 0, sizeof(tb));
+      for (int g = 0; g < p->ng; ++g) {
+        LT.grp[g].MT = mt;
+        LT.grp[g].ntb = (p->B[g] + mt - 1) / mt;
+        LT.prefix[g] = acc;
+        acc += (p->M[g] + 1) * LT.grp[g].ntb;
+        tb.p[g] = p->tcbasis_adj[g];
+      }
+      LT.prefix[p->ng] = acc;
+      return launch_spec_adj_tc(LT, acc, tb, p->d_err, s);
+    }
+  }
+  return launch_spec_adj<T>(LS, nbs, p->spec_adj_smem, s);
 }
 
 // Launch nsteps steps.  In place on st[g].fourier, or -- when `slots` is given --
@@ -345,7 +371,7 @@ int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group
     LS.grp[g].lamY = (const typename cplx<T>::type*)adj[g].lam_y;
     LS.grp[g].grad = adj[g].grad;
   }
-  e = launch_spec_adj<T>(LS, nbs, p->spec_adj_smem, s);
+  e = launch_step_spec_adj<T>(p, LS, nbs, s);
   return cuda_check(p, e, "spectral adjoint launch");
 }
 
@@ -469,7 +495,7 @@ int time_kernels_impl(swp_plan* p, const swp_group_state* st, const swp_group_ad
     if (adj) {
       le[2] = launch_grid<T>(LGa, nbg, p->grid_smem[GM_ADJ_STEP], s);
       cudaEventRecord(ev[3], s);
-      le[3] = launch_spec_adj<T>(LSa, nbs, p->spec_adj_smem, s);
+      le[3] = launch_step_spec_adj<T>(p, LSa, nbs, s);
       cudaEventRecord(ev[4], s);
     }
     for (int k = 0; k < 4; ++k)
@@ -658,7 +684,9 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
   if (tc) {
     for (int g = 0; g < ngroups; ++g) {
       if (cudaMalloc(&p->tcbasis[g], spec_tc_basis_floats() * sizeof(float)) != cudaSuccess ||
-          pack_tc_basis(p->geom[g], p->tcbasis[g], s) != SWP_OK) {
+          pack_tc_basis(p->geom[g], p->tcbasis[g], s) != SWP_OK ||
+          cudaMalloc(&p->tcbasis_adj[g], spec_tc_basis_floats() * sizeof(float)) != cudaSuccess ||
+          pack_tc_basis_adj(p->geom[g], p->tcbasis_adj[g], s) != SWP_OK) {
         p->err = "tensor-core basis packing failed";
         *out = p;
         return SWP_ERR_CUDA;
@@ -684,6 +712,7 @@ int swp_plan_destroy(swp_plan* p) {
   for (int g = 0; g < p->ng; ++g) {
     if (p->geom[g].mem) cudaFree(p->geom[g].mem);
     if (p->tcbasis[g]) cudaFree(p->tcbasis[g]);
+    if (p->tcbasis_adj[g]) cudaFree(p->tcbasis_adj[g]);
     if (p->coefmem[g]) cudaFree(p->coefmem[g]);
   }
   if (p->d_err) cudaFree(p->d_err);

@@ -213,4 +213,92 @@ __device__ __forceinline__ void write_step_point(const SpecGroup<T>& G, const St
   store_step_point<T>(G, cfg, incr, FS, o, al, nw_in, uv, u, v, old, mid);
 }
 
+// ----------------------------------------------------------------- adjoint
+// Global values the adjoint write-out of one (m, member, latitude) point
+// reads: the adjoint of the step's curr outputs (incremental form) and the
+// primal inputs of the Phibar gradient.  Loaded ahead of the stores.
+template <typename T>
+struct AdjPointIn {
+  typename cplx<T>::type ly[3];  // lamY eta, delta, Phi
+  typename cplx<T>::type px[7];  // primal delta, Phi, E, A, B, F, G
+};
+
+template <typename T>
+__device__ __forceinline__ void adj_load_point(const SpecGroup<T>& G, bool incr, size_t FS, size_t o,
+                                               AdjPointIn<T>& in) {
+  typedef typename cplx<T>::type T2;
+  const T2 z = mk<T2>(0, 0);
+#pragma unroll
+  for (int q = 0; q < 3; ++q) in.ly[q] = incr ? G.lamY[q * FS + o] : z;
+  const int pf[7] = {F_DELTA, F_PHI, F_E, F_A, F_B, F_F, F_G};
+#pragma unroll
+  for (int q = 0; q < 7; ++q) in.px[q] = G.grad ? G.four[pf[q] * FS + o] : z;
+}
+
+// Transposed combination of the step inputs at one point (adjoint of
+// step_combos, modified Euler): from the adjoints of the combined inputs
+// ld(q) -- slot order PhiP1, PhiP2, dP1, dP2, eP1, [identity Phi, delta, eta
+// when NK = 8], then the H slots PhiH1, dH1, dH2, eH1 -- to the adjoints of the
+// 19 state fields, written to G.lam.  Returns this point's term of dL/dPhibar
+// (modEuler_tdiff.py:80-103, 185-193).
+template <typename T, int NK, typename LD>
+__device__ __forceinline__ T adj_store_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
+                                             size_t o, int m, int b, int j, LD ld, const AdjPointIn<T>& in) {
+  typedef typename cplx<T>::type T2;
+  T2 lPhiP1 = ld(0), lPhiP2 = ld(1), ldP1 = ld(2), ldP2 = ld(3), leP1 = ld(4);
+  T2 lPhiH1 = ld(NK), ldH1 = ld(NK + 1), ldH2 = ld(NK + 2), leH1 = ld(NK + 3);
+  const T* mc = G.mco;
+  const int B = G.B;
+  const T tsc = G.jco[(size_t)b * G.g.J + j];
+  const T dt = mc[MC_DT * B + b];
+  T t1 = tsc * (T)0.25, t2 = mc[MC_T2 * B + b];
+  T ia2 = mc[MC_IA2 * B + b];
+  T hPb = mc[MC_HPB * B + b];
+  T te = cfg.forcflag ? tsc : tsc * (T)0.5;
+  T xm = (T)m;
+  T forc = cfg.forcflag ? (T)1 : (T)0;
+  // conj(i*alpha*m) z = -i alpha m z
+  auto mimul = [&](T alpha, T2 z) { return imul(-alpha * xm, z); };
+  // projection form: curr enters PhiP1, dP1, eP1 with coefficient 1; incremental
+  // form: through the identity slots and directly (new = curr + ...)
+  T2 idphi = lPhiP1, iddel = ldP1, ideta = leP1;
+  if (incr) {
+    idphi = cadd(ld(NK > 5 ? 5 : 0), in.ly[2]);
+    iddel = cadd(ld(NK > 6 ? 6 : 0), in.ly[1]);
+    ideta = cadd(ld(NK > 7 ? 7 : 0), in.ly[0]);
+  }
+  T2 lphi = csub(cadd(idphi, cscale(ldP2, t2)), cscale(lPhiP2, hPb * ia2));
+  T2 ldel = cadd(csub(iddel, cscale(lPhiP1, mc[MC_DTPB * B + b])), cscale(ldP2, -mc[MC_PBA2 * B + b]));
+  T2 leta = ideta;
+  T2 lC = cadd(mimul(-t1, lPhiP1), mimul(t1 * (T)0.5 * ia2, ldP2));
+  T2 lD = cadd(cscale(lPhiH1, t1), cscale(ldH2, t1 * (T)0.5 * ia2));
+  T2 lE = cadd(cscale(lPhiP2, -hPb * t2), cscale(ldP2, t2));
+  T2 lPF = cscale(cadd(cscale(lPhiP1, dt), cscale(ldP2, mc[MC_PFD * B + b])), forc);
+  T2 lBeff = cadd(mimul(-hPb * t1, lPhiP1), cscale(leH1, te));
+  T2 lAeff = cadd(cscale(lPhiH1, -hPb * t1), mimul(-te, leP1));
+  T2 lBf = mimul(t1, ldP1);
+  T2 lAf = cscale(ldH1, t1);
+  T2 lA = cadd(lAeff, lAf), lB = cadd(lBeff, lBf);
+  T2 lF = cadd(cscale(lBeff, forc), lBf);
+  T2 lG = csub(mk<T2>(0, 0), cadd(cscale(lAeff, forc), lAf));
+  const T2 z = mk<T2>(0, 0);
+  T2* LAM = G.lam;
+  LAM[F_ETA * FS + o] = leta; LAM[F_DELTA * FS + o] = ldel; LAM[F_PHI * FS + o] = lphi;
+  LAM[F_A * FS + o] = lA; LAM[F_B * FS + o] = lB; LAM[F_C * FS + o] = lC; LAM[F_D * FS + o] = lD;
+  LAM[F_E * FS + o] = lE; LAM[F_PHIF * FS + o] = lPF; LAM[F_F * FS + o] = lF; LAM[F_G * FS + o] = lG;
+  LAM[F_U * FS + o] = z; LAM[F_V * FS + o] = z;
+  LAM[F_ETA_PREV * FS + o] = z; LAM[F_DELTA_PREV * FS + o] = z; LAM[F_PHI_PREV * FS + o] = z;
+  LAM[F_ETA_MID * FS + o] = z; LAM[F_DELTA_MID * FS + o] = z; LAM[F_PHI_MID * FS + o] = z;
+  if (!G.grad) return (T)0;
+  // d(combined inputs)/dPhibar
+  const T2 del = in.px[0], phi = in.px[1], E = in.px[2], A = in.px[3], Bm = in.px[4], Fm = in.px[5], Gm = in.px[6];
+  T2 Beff = cfg.forcflag ? cadd(Bm, Fm) : Bm, Aeff = cfg.forcflag ? csub(A, Gm) : A;
+  T2 dP1 = csub(cscale(del, -dt), cscale(imul(xm, Beff), (T)0.5 * t1));
+  T2 dH1 = cscale(Aeff, (T)-0.5 * t1);
+  T2 dP2 = cscale(cadd(cscale(E, t2), cscale(phi, ia2)), (T)-0.5);
+  T2 dd2 = cscale(del, -ia2);
+  return lPhiP1.x * dP1.x + lPhiP1.y * dP1.y + lPhiH1.x * dH1.x + lPhiH1.y * dH1.y + lPhiP2.x * dP2.x +
+         lPhiP2.y * dP2.y + ldP2.x * dd2.x + ldP2.y * dd2.y;
+}
+
 }  // namespace swp

@@ -602,75 +602,16 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
   }
   __syncthreads();
   // ---- phase 5: transposed combination -> adjoints of the state fields; Phibar gradient
-  T2* LAM = G.lam;
-  const T2* PX = G.four;  // primal state before the step
   for (int t = threadIdx.x; t < MT * J; t += blockDim.x) {
     int bt = t / J, j = t % J;
     if (bt >= mt) continue;
     int b = b0 + bt;
     size_t o = ((size_t)m * G.B + b) * J + j;
     auto ld = [&](int q) { return mk<T2>(Cad[(((size_t)q * MT + bt) * J + j) * 2], Cad[(((size_t)q * MT + bt) * J + j) * 2 + 1]); };
-    // slot order: 0 PhiP1, 1 PhiP2, 2 dP1, 3 dP2, 4 eP1, [identity Phi, delta, eta], PhiH1, dH1, dH2, eH1
-    T2 lPhiP1 = ld(0), lPhiP2 = ld(1), ldP1 = ld(2), ldP2 = ld(3), leP1 = ld(4);
-    T2 lPhiH1 = ld(NKADJ), ldH1 = ld(NKADJ + 1), ldH2 = ld(NKADJ + 2), leH1 = ld(NKADJ + 3);
-    const T* mc = G.mco;
-    const int B = G.B;
-    const T tsc = G.jco[(size_t)b * J + j];
-    const T dt = mc[MC_DT * B + b];
-    T t1 = tsc * (T)0.25, t2 = mc[MC_T2 * B + b];
-    T ia2 = mc[MC_IA2 * B + b];
-    T hPb = mc[MC_HPB * B + b];
-    T te = cfg.forcflag ? tsc : tsc * (T)0.5;
-    T xm = (T)m;
-    T forc = cfg.forcflag ? (T)1 : (T)0;
-    // conj(i*alpha*m) z = -i alpha m z
-    auto mimul = [&](T alpha, T2 z) { return imul(-alpha * xm, z); };
-    // projection form: curr enters PhiP1, dP1, eP1 with coefficient 1; incremental
-    // form: through the identity slots and directly (new = curr + ...)
-    T2 idphi = lPhiP1, iddel = ldP1, ideta = leP1;
-    if (incr) {
-      size_t oy = o;  // lamY has the same (m, b, j) layout
-      idphi = cadd(ld(NKADJ > 5 ? 5 : 0), G.lamY[2 * FS + oy]);
-      iddel = cadd(ld(NKADJ > 6 ? 6 : 0), G.lamY[1 * FS + oy]);
-      ideta = cadd(ld(NKADJ > 7 ? 7 : 0), G.lamY[0 * FS + oy]);
-    }
-    T2 lphi = csub(cadd(idphi, cscale(ldP2, t2)), cscale(lPhiP2, hPb * ia2));
-    T2 ldel = cadd(csub(iddel, cscale(lPhiP1, mc[MC_DTPB * B + b])), cscale(ldP2, -mc[MC_PBA2 * B + b]));
-    T2 leta = ideta;
-    T2 lC = cadd(mimul(-t1, lPhiP1), mimul(t1 * (T)0.5 * ia2, ldP2));
-    T2 lD = cadd(cscale(lPhiH1, t1), cscale(ldH2, t1 * (T)0.5 * ia2));
-    T2 lE = cadd(cscale(lPhiP2, -hPb * t2), cscale(ldP2, t2));
-    T2 lPF = cscale(cadd(cscale(lPhiP1, dt), cscale(ldP2, mc[MC_PFD * B + b])), forc);
-    T2 lBeff = cadd(mimul(-hPb * t1, lPhiP1), cscale(leH1, te));
-    T2 lAeff = cadd(cscale(lPhiH1, -hPb * t1), mimul(-te, leP1));
-    T2 lBf = mimul(t1, ldP1);
-    T2 lAf = cscale(ldH1, t1);
-    T2 lA = cadd(lAeff, lAf), lB = cadd(lBeff, lBf);
-    T2 lF = cadd(cscale(lBeff, forc), lBf);
-    T2 lG = csub(mk<T2>(0, 0), cadd(cscale(lAeff, forc), lAf));
-    T2 z = mk<T2>(0, 0);
-    // primal values of the Phibar gradient, loaded before the stores below
-    T2 pdel = z, pphi = z, pE = z, pA = z, pB = z, pF = z, pG = z;
+    AdjPointIn<T> in;
+    adj_load_point<T>(G, incr, FS, o, in);
+    T gp = adj_store_point<T, NKADJ>(G, cfg, incr, FS, o, m, b, j, ld, in);
     if (G.grad) {
-      pdel = PX[F_DELTA * FS + o]; pphi = PX[F_PHI * FS + o]; pE = PX[F_E * FS + o];
-      pA = PX[F_A * FS + o]; pB = PX[F_B * FS + o]; pF = PX[F_F * FS + o]; pG = PX[F_G * FS + o];
-    }
-    LAM[F_ETA * FS + o] = leta; LAM[F_DELTA * FS + o] = ldel; LAM[F_PHI * FS + o] = lphi;
-    LAM[F_A * FS + o] = lA; LAM[F_B * FS + o] = lB; LAM[F_C * FS + o] = lC; LAM[F_D * FS + o] = lD;
-    LAM[F_E * FS + o] = lE; LAM[F_PHIF * FS + o] = lPF; LAM[F_F * FS + o] = lF; LAM[F_G * FS + o] = lG;
-    LAM[F_U * FS + o] = z; LAM[F_V * FS + o] = z;
-    LAM[F_ETA_PREV * FS + o] = z; LAM[F_DELTA_PREV * FS + o] = z; LAM[F_PHI_PREV * FS + o] = z;
-    LAM[F_ETA_MID * FS + o] = z; LAM[F_DELTA_MID * FS + o] = z; LAM[F_PHI_MID * FS + o] = z;
-    if (G.grad) {
-      // d(combined inputs)/dPhibar (modEuler_tdiff.py:80-103, 185-193)
-      const T2 del = pdel, phi = pphi, E = pE, A = pA, Bm = pB, Fm = pF, Gm = pG;
-      T2 Beff = cfg.forcflag ? cadd(Bm, Fm) : Bm, Aeff = cfg.forcflag ? csub(A, Gm) : A;
-      T2 dP1 = csub(cscale(del, -dt), cscale(imul(xm, Beff), (T)0.5 * t1));
-      T2 dH1 = cscale(Aeff, (T)-0.5 * t1);
-      T2 dP2 = cscale(cadd(cscale(E, t2), cscale(phi, ia2)), (T)-0.5);
-      T2 dd2 = cscale(del, -ia2);
-      T gp = lPhiP1.x * dP1.x + lPhiP1.y * dP1.y + lPhiH1.x * dH1.x + lPhiH1.y * dH1.y + lPhiP2.x * dP2.x +
-             lPhiP2.y * dP2.y + ldP2.x * dd2.x + ldP2.y * dd2.y;
       // J is a multiple of 32, so a warp holds one member: reduce over the warp
       // in the compute type, accumulate the warp sums in FP64
 #pragma unroll

@@ -191,5 +191,9 @@ bool spec_tc_supported(int M);
 int pack_tc_basis(const GroupGeom& gg, float* out, cudaStream_t s);
 void spec_tc_set_attributes();
 cudaError_t launch_spec_tc(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err, cudaStream_t s);
+int pack_tc_basis_adj(const GroupGeom& gg, float* out, cudaStream_t s);
+size_t spec_tc_adj_smem_bytes();
+cudaError_t launch_spec_adj_tc(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
+                               cudaStream_t s);
 
 }  // namespace swp

@@ -122,6 +122,15 @@ int pack_tc_basis(const GroupGeom& gg, float* out, cudaStream_t s) {
   return cudaGetLastError() == cudaSuccess ? SWP_OK : SWP_ERR_CUDA;
 }
 
+// The adjoint's operand blocks: GEMM1' contracts with the unweighted basis in
+// the forward layout (transposed inverse Legendre), GEMM2' with the weighted
+// basis in the inverse layout (transposed forward Legendre).
+int pack_tc_basis_adj(const GroupGeom& gg, float* out, cudaStream_t s) {
+  if (gg.M != TC_M || gg.J != TC_J) return SWP_ERR_ARG;
+  k_pack_tc_basis<<<TC_CNT, 256, 0, s>>>(gg.b64[B_P_F], gg.b64[B_H_F], gg.b64[B_PW_I], gg.b64[B_HW_I], gg.boff, out);
+  return cudaGetLastError() == cudaSuccess ? SWP_OK : SWP_ERR_CUDA;
+}
+
 namespace {
 // the three products of one 3xTF32 K-sweep into d_tmem (K a multiple of 8)
 __device__ __forceinline__ void mma_3xtf32(uint32_t d_tmem, uint32_t aH, uint32_t aL, uint32_t bH, uint32_t bL, int K,
@@ -500,12 +509,355 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   if (warp == 0) tc::tmem_dealloc(tbase, TC_TMEM_COLS);
 }
 
+
+// ===========================================================================
+// Adjoint of k_spectral_tc (modified Euler), the tensor-core form of
+// k_spectral_adj (spectral.cu):
+//   GEMM1' (transposed inverse Legendre), per parity:
+//     D1'[row, c] = sum_k A1'[row, k] B1'[c, k]
+//     row = group q (7: lambda of eta, delta, Phi, Uprep, Vprep on P; of U, V on
+//     H) x member x re/im = 112 of 128 rows, k = [P at j' | H at j'] (unweighted)
+//   epilogue: transposed wind inversion, n(n+1), hyperdiffusion, incremental form
+//   GEMM2' (transposed forward Legendre), per parity:
+//     D2'[row, col] = sum_c A2'[row, c] B2'[col, c]
+//     row = slot q (8: PhiP1, PhiP2, dP1, dP2, eP1, identity Phi, delta, eta)
+//     x member x re/im = 128 rows, col = [Pw at j' | Hw at j']; the Hw columns
+//     of slots 0, 2, 3, 4 are the H slots PhiH1, dH1, dH2, eH1
+//   write-out: adj_store_point (transposed combination) + Phibar gradient.
+// ===========================================================================
+namespace {
+constexpr int TCA_NIN = 5;                          // staged lambda of eta, delta, Phi, U, V
+constexpr int TCA_A2 = TC_ROWS * TC_K2;             // one A2' operand: 128 rows (3072 floats)
+constexpr int TCA_RES0 = 4 * TCA_A2;                // D1' staging after the A2' operands
+constexpr int TCA_RES = 7 * TC_CNT * 16;            // [q][n-m][member, re/im]
+constexpr int TCA_NOUT = 12;                        // 8 P slots + 4 H slots
+constexpr int TCA_A = TCA_RES0 + TCA_RES > TC_A ? TCA_RES0 + TCA_RES : TC_A;
+static_assert(TCA_NOUT * TC_MT * TC_OST <= TCA_A, "adjoint output staging must fit in the A region");
+static_assert(TCA_NIN * TC_MT * TC_J * 2 <= TCA_A, "staged lambda must fit in the A region");
+__host__ __device__ constexpr int adj_hslot(int q) {  // H result of GEMM2' row group q, or -1
+  return q == 0 ? 0 : q == 2 ? 1 : q == 3 ? 2 : q == 4 ? 3 : -1;
+}
+}  // namespace
+
+size_t spec_tc_adj_smem_bytes() { return (size_t)(TCA_A + TC_B1 + TC_COEF) * sizeof(float) + 256; }
+
+__global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constant__ SpecLaunch<float> L,
+                                                            const __grid_constant__ TcBasis basis, int* err) {
+  typedef float T;
+  typedef float2 T2;
+  constexpr int NKADJ = 8;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  int idx;
+  const SpecGroup<T>& G = pick_group(L, idx);
+  int gi = 0;
+  while (gi + 1 < L.ng && (int)blockIdx.x >= L.prefix[gi + 1]) ++gi;
+  const float* gbasis = basis.p[gi];
+  const StepCfg& cfg = L.cfg;
+  const int J = TC_J;
+  const int m = idx / G.ntb;
+  const int b0 = (idx % G.ntb) * TC_MT;
+  const int mt = min(TC_MT, G.B - b0);
+  const int cnt = TC_CNT - m, C0 = (cnt + 1) / 2, C1 = cnt / 2;
+  const size_t FS = (size_t)TC_CNT * G.B * J;
+  const bool incr = cfg.incremental != 0;
+  if (cfg.scheme != 0) {  // the host launches this kernel for modified-Euler steps only
+    if (threadIdx.x == 0) atomicExch(err, 2);
+    return;
+  }
+
+  float* sA = (float*)smem_raw;            // staged lambda | A1' | A2' + D1' staging | output staging
+  float* sB = sA + TCA_A;                  // B1', then B2'
+  float* sRes = sA + TCA_RES0;
+  float* sig = sB + TC_B1;
+  float* sigP = sig + TC_MT * TC_CNT;
+  float* sigm1 = sigP + TC_MT * TC_CNT;
+  float* sigPm1 = sigm1 + TC_MT * TC_CNT;
+  float* tcmn = sigPm1 + TC_MT * TC_CNT;
+  uint64_t* mbar = (uint64_t*)(((uintptr_t)(tcmn + TC_MT * TC_CNT) + 15) & ~(uintptr_t)15);  // [4]
+  uint32_t* tslot = (uint32_t*)(mbar + 4);
+  int* sflag = (int*)(tslot + 1);
+  double* sgrad = (double*)(((uintptr_t)(sflag + 1) + 15) & ~(uintptr_t)15);  // [MT][2]
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int n_tma = 0, n_in = 0, n_c1 = 0, n_c2 = 0;
+
+  // ---- phase 0: barriers; bulk copies of lambda_Y (5 fields) and of B1'; TMEM; coefficients
+  if (threadIdx.x == 0) {
+    *sflag = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) tc::mbar_init(&mbar[q], 1);
+    tc::fence_mbar_init();
+    const uint32_t row_bytes = (uint32_t)(mt * J * sizeof(T2));
+    tc::mbar_expect_tx(&mbar[3], row_bytes * TCA_NIN);
+#pragma unroll
+    for (int q = 0; q < TCA_NIN; ++q)
+      tc::bulk_g2s(sA + (size_t)q * TC_MT * J * 2, G.lamY + (size_t)q * FS + ((size_t)m * G.B + b0) * J, row_bytes,
+                   &mbar[3]);
+    n_in = 1;
+    tc::mbar_expect_tx(&mbar[0], (uint32_t)(TC_B1 * sizeof(float)));
+    tc::bulk_g2s(sB, gbasis + (size_t)m * TC_BLOCK, (uint32_t)(TC_B1 * sizeof(float)), &mbar[0]);
+    n_tma = 1;
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, TC_TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, TC_MT, cnt, TC_CNT, sig, sigP, sigm1, sigPm1, tcmn);
+  if (threadIdx.x < 2 * TC_MT) sgrad[threadIdx.x] = 0.0;
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = *tslot;
+
+  // ---- phase 1: symmetrised lambda_Y of (member, j')
+  const int jp = (warp & 3) * 8 + (lane & 7);
+  const int bt = (warp >> 2) * 4 + (lane >> 3);
+  T2 ys[TCA_NIN], ya[TCA_NIN];
+  AdjPointIn<T> pin[2];  // write-out inputs, loaded ahead of GEMM2'
+  bool ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[3], 0) : true;
+  ok = __syncthreads_and(ok);
+  if (ok) {
+    const T2* stg = (const T2*)sA;
+#pragma unroll
+    for (int f = 0; f < TCA_NIN; ++f) {
+      if (bt < mt) {
+        const T2 u = stg[(f * TC_MT + bt) * J + jp], v = stg[(f * TC_MT + bt) * J + (J - 1 - jp)];
+        ys[f] = cadd(u, v);
+        ya[f] = csub(u, v);
+      } else {
+        ys[f] = mk<T2>(0, 0);
+        ya[f] = ys[f];
+      }
+    }
+  }
+  // parity 0: the P groups take the symmetric sums, the H groups the antisymmetric ones
+  auto write_A1 = [&](int par) {
+    float* aH = sA;
+    float* aL = sA + TC_ROWS * TC_K1;
+#pragma unroll
+    for (int gq = 0; gq < 7; ++gq) {
+      const bool hg = gq >= 5;
+      const int f = hg ? gq - 2 : gq;  // H groups carry lambda U, V
+      const T2 v = hg ? (par ? ys[f] : ya[f]) : (par ? ya[f] : ys[f]);
+#pragma unroll
+      for (int comp = 0; comp < 2; ++comp) {
+        const int row = gq * 16 + bt * 2 + comp;
+        float hi, lo;
+        tc::split_tf32(comp ? v.y : v.x, hi, lo);
+        aH[tc::cm_index(row, hg ? TC_JH + jp : jp, TC_K1)] = hi;
+        aL[tc::cm_index(row, hg ? TC_JH + jp : jp, TC_K1)] = lo;
+        aH[tc::cm_index(row, hg ? jp : TC_JH + jp, TC_K1)] = 0.f;
+        aL[tc::cm_index(row, hg ? jp : TC_JH + jp, TC_K1)] = 0.f;
+      }
+    }
+  };
+  const uint32_t idesc1 = tc::idesc_tf32(TC_ROWS, TC_N1);
+  const uint32_t idesc2 = tc::idesc_tf32(TC_ROWS, TC_N2);
+  const uint32_t aHs = tc::smem_u32(sA), aLs = aHs + (uint32_t)(TC_ROWS * TC_K1 * 4);
+  const uint32_t bbase = tc::smem_u32(sB);
+
+  // ---- phase 2: GEMM1', parity 0 then parity 1
+  if (ok) {
+    __syncthreads();  // the staged lambda is read: A1' overwrites it
+    write_A1(0);
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (!tc::mbar_wait_bounded(&mbar[0], 0)) *sflag = 1;
+      if (!*sflag) mma_3xtf32(tbase, aHs, aLs, bbase, bbase + TC_N1 * TC_K1 * 4, TC_K1, idesc1);
+      tc::mma_commit(&mbar[1]);
+      n_c1 = 1;
+    }
+    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 0) : true;
+    ok = __syncthreads_and(ok);
+    tc::fence_after_sync();
+    ok = ok && !*sflag;
+  }
+  if (ok) {
+    write_A1(1);
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const uint32_t b1 = bbase + 2u * TC_N1 * TC_K1 * 4u;
+      mma_3xtf32(tbase + TC_N1, aHs, aLs, b1, b1 + TC_N1 * TC_K1 * 4, TC_K1, idesc1);
+      tc::mma_commit(&mbar[1]);
+      n_c1 = 2;
+    }
+    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 1) : true;
+    ok = __syncthreads_and(ok);
+    tc::fence_after_sync();
+  }
+  if (ok) {
+    if (threadIdx.x == 0) {
+      tc::mbar_expect_tx(&mbar[0], (uint32_t)(TC_B2 * sizeof(float)));
+      tc::bulk_g2s(sB, gbasis + (size_t)m * TC_BLOCK + TC_B1, (uint32_t)(TC_B2 * sizeof(float)), &mbar[0]);
+      n_tma = 2;
+    }
+    // ---- phase 3: D1' -> sRes[q][n-m][member, re/im]; zero the A2' operands
+    {
+      const int quarter = warp & 3, par = warp >> 2;
+      const int row = quarter * 32 + lane;
+      const int gq = row >> 4, btc = row & 15;
+      const int Cp = par ? C1 : C0;
+#pragma unroll
+      for (int c0 = 0; c0 < TC_N1; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(par * TC_N1 + c0), v);
+        if (gq < 7) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int c = c0 + i;
+            if (c < Cp) sRes[(gq * TC_CNT + (par + 2 * c)) * 16 + btc] = v[i];
+          }
+        }
+      }
+    }
+    for (int i = threadIdx.x; i < TCA_RES0; i += blockDim.x) sA[i] = 0.f;
+    tc::fence_before_sync();
+    __syncthreads();
+    // ---- phase 4: transposed wind inversion, n(n+1), hyperdiffusion -> A2' [par][hi, lo][128][K2]
+    for (int t = threadIdx.x; t < TC_MT * cnt; t += blockDim.x) {
+      const int bti = t % TC_MT, kk = t / TC_MT, n = m + kk;
+      const int par = kk & 1, c = kk >> 1;
+      auto S = [&](int q, int comp) { return sRes[(q * TC_CNT + kk) * 16 + bti * 2 + comp]; };
+      const T xm = (T)m;
+      const T tcv = tcmn[bti * TC_CNT + kk];
+      const T s = sig[bti * TC_CNT + kk], sp = sigP[bti * TC_CNT + kk];
+      const T sm1 = sigm1[bti * TC_CNT + kk], spm1 = sigPm1[bti * TC_CNT + kk];
+      const T nn1 = (T)(n * (n + 1));
+      // lambda delta_s = (i m) lambda Uprep - lambda Hin_V ; lambda eta_s = (i m) lambda Vprep + lambda Hin_U
+      const T lds_r = -xm * S(3, 1) - S(6, 0), lds_i = xm * S(3, 0) - S(6, 1);
+      const T les_r = -xm * S(4, 1) + S(5, 0), les_i = xm * S(4, 0) + S(5, 1);
+      const T w = (n == 0) ? (T)0 : tcv;
+      const T lce_r = S(0, 0) + w * les_r, lce_i = S(0, 1) + w * les_i;
+      const T lcd_r = S(1, 0) + w * lds_r, lcd_i = S(1, 1) + w * lds_i;
+      const T lcp_r = S(2, 0), lcp_i = S(2, 1);
+      T kv[NKADJ][2];
+      kv[0][0] = sp * lcp_r; kv[0][1] = sp * lcp_i;
+      kv[1][0] = nn1 * sp * lcp_r; kv[1][1] = nn1 * sp * lcp_i;
+      kv[2][0] = s * lcd_r; kv[2][1] = s * lcd_i;
+      kv[3][0] = nn1 * s * lcd_r; kv[3][1] = nn1 * s * lcd_i;
+      kv[4][0] = s * lce_r; kv[4][1] = s * lce_i;
+      kv[5][0] = incr ? spm1 * S(2, 0) : (T)0; kv[5][1] = incr ? spm1 * S(2, 1) : (T)0;
+      kv[6][0] = incr ? (s * w * lds_r + sm1 * S(1, 0)) : (T)0; kv[6][1] = incr ? (s * w * lds_i + sm1 * S(1, 1)) : (T)0;
+      kv[7][0] = incr ? (s * w * les_r + sm1 * S(0, 0)) : (T)0; kv[7][1] = incr ? (s * w * les_i + sm1 * S(0, 1)) : (T)0;
+      float* aH = sA + (size_t)(2 * par) * TCA_A2;
+      float* aL = aH + TCA_A2;
+#pragma unroll
+      for (int q = 0; q < NKADJ; ++q)
+#pragma unroll
+        for (int comp = 0; comp < 2; ++comp) {
+          const int row = q * 16 + bti * 2 + comp;
+          float hi, lo;
+          tc::split_tf32(kv[q][comp], hi, lo);
+          aH[tc::cm_index(row, c, TC_K2)] = hi;
+          aL[tc::cm_index(row, c, TC_K2)] = lo;
+        }
+    }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    // ---- phase 5: GEMM2', both parities; write-out inputs loaded meanwhile
+    static_assert(TC_MT * TC_J == 2 * 256, "two write-out points per thread");
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int t = threadIdx.x + u * 256, bti = t / J, j = t % J;
+      if (bti < mt) adj_load_point<T>(G, incr, FS, ((size_t)m * G.B + b0 + bti) * J + j, pin[u]);
+    }
+    if (threadIdx.x == 0) {
+      if (!tc::mbar_wait_bounded(&mbar[0], 1)) *sflag = 1;
+      if (!*sflag) {
+        for (int par = 0; par < 2; ++par) {
+          const uint32_t a2 = aHs + (uint32_t)(2 * par * TCA_A2) * 4u;
+          const uint32_t bp = bbase + (uint32_t)(2 * par * TC_N2 * TC_K2) * 4u;
+          mma_3xtf32(tbase + 2 * TC_N1 + par * TC_N2, a2, a2 + TCA_A2 * 4, bp, bp + TC_N2 * TC_K2 * 4, TC_K2,
+                     idesc2);
+        }
+      }
+      tc::mma_commit(&mbar[2]);
+      n_c2 = 1;
+    }
+    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[2], 0) : true;
+    ok = __syncthreads_and(ok);
+    tc::fence_after_sync();
+    ok = ok && !*sflag;
+  }
+  if (ok) {
+    // ---- phase 6: D2' -> output staging Out[slot][member][j][re/im]: slots 0..7
+    // from the Pw columns of rows q, slots 8..11 from the Hw columns of rows 0, 2, 3, 4
+    float* Out = sA;
+    {
+      const int quarter = warp & 3, half = warp >> 2;
+      const int row = quarter * 32 + lane;
+      const int q = row >> 4, btc = row & 15, bti = btc >> 1, comp = btc & 1;
+      const bool hcols = half == 1;
+      const int slot = hcols ? (adj_hslot(q) >= 0 ? NKADJ + adj_hslot(q) : -1) : q;
+      const uint32_t lanes = (uint32_t)(quarter * 32) << 16;
+#pragma unroll
+      for (int cc = 0; cc < 2; ++cc) {
+        const int col0 = half * TC_JH + cc * 16;
+        float E[16], O[16];
+        tc::tmem_ld16(tbase + lanes + (uint32_t)(2 * TC_N1 + col0), E);
+        tc::tmem_ld16(tbase + lanes + (uint32_t)(2 * TC_N1 + TC_N2 + col0), O);
+        if (slot >= 0) {
+          float* o = Out + (size_t)(slot * TC_MT + bti) * TC_OST + comp;
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int jj = cc * 16 + i;
+            o[2 * jj] = E[i] + O[i];
+            o[2 * (J - 1 - jj)] = hcols ? (O[i] - E[i]) : (E[i] - O[i]);
+          }
+        }
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    // ---- phase 7: transposed combination -> lambda of the state fields; Phibar gradient
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int t = threadIdx.x + u * 256, bti = t / J, j = t % J;
+      if (bti >= mt) continue;  // uniform over a warp: a warp covers 32 latitudes of one member
+      const int b = b0 + bti;
+      const size_t o = ((size_t)m * G.B + b) * J + j;
+      auto ld = [&](int q) { return *(const float2*)&Out[(size_t)(q * TC_MT + bti) * TC_OST + 2 * j]; };
+      T gp = adj_store_point<T, NKADJ>(G, cfg, incr, FS, o, m, b, j, ld, pin[u]);
+      if (G.grad) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) gp += __shfl_xor_sync(0xffffffffu, gp, off);
+        if (lane == 0) sgrad[bti * 2 + j / 32] = (double)gp;
+      }
+    }
+    __syncthreads();
+    if (G.grad && threadIdx.x < mt)
+      atomicAdd(&G.grad[G_PHIBAR * G.B + b0 + threadIdx.x], sgrad[threadIdx.x * 2] + sgrad[threadIdx.x * 2 + 1]);
+  } else {
+    if (threadIdx.x == 0) {
+      atomicExch(err, 1);
+      if (n_in > 0) tc::mbar_wait_bounded(&mbar[3], 0, 1u << 20);
+      if (n_tma > 0) tc::mbar_wait_bounded(&mbar[0], (uint32_t)(n_tma - 1), 1u << 20);
+      if (n_c1 > 0) tc::mbar_wait_bounded(&mbar[1], (uint32_t)(n_c1 - 1), 1u << 20);
+      if (n_c2 > 0) tc::mbar_wait_bounded(&mbar[2], 0, 1u << 20);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tbase, TC_TMEM_COLS);
+}
+
 void spec_tc_set_attributes() {
   cudaFuncSetAttribute(k_spectral_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spec_tc_smem_bytes());
+  cudaFuncSetAttribute(k_spectral_adj_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spec_tc_adj_smem_bytes());
 }
 
 cudaError_t launch_spec_tc(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err, cudaStream_t s) {
   k_spectral_tc<<<nblocks, 256, spec_tc_smem_bytes(), s>>>(L, basis, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spec_adj_tc(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
+                               cudaStream_t s) {
+  k_spectral_adj_tc<<<nblocks, 256, spec_tc_adj_smem_bytes(), s>>>(L, basis, err);
   return cudaGetLastError();
 }
 

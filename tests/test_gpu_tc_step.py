@@ -118,3 +118,41 @@ def test_tc_step_with_diagnostics_matches_fp64(cuda):
         assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-5, name
     np.testing.assert_allclose(f32["outs"]["rms"].cpu().numpy(), f64["outs"]["rms"].cpu().numpy(), rtol=1e-5)
     np.testing.assert_array_equal(f32["outs"]["dead"].cpu().numpy(), f64["outs"]["dead"].cpu().numpy())
+
+
+def _grads(eng, nsteps=40):
+    import torch
+    from my_swampe_gb300 import workloads
+    from my_swampe_gb300.adjoint import GRAD_PARAMS, integrate
+    from my_swampe_gb300.engine import RunFlagsC
+
+    wl = workloads.forced_ensemble(eng, seed=9)
+    workloads.apply_params(eng, 0, wl["params"])
+    B = eng.groups[0]["B"]
+    p = {k: torch.as_tensor(wl["params"][k], dtype=torch.float64, device=eng.device).expand(B).clone().requires_grad_(True)
+         for k in GRAD_PARAMS if k != "Phibar"}
+    p["Phibar"] = torch.full((B,), wl["params"]["Phibar"], dtype=torch.float64, device=eng.device, requires_grad=True)
+    ics = wl["ics"].to(eng.rdtype).clone().requires_grad_(True)
+    out = integrate(eng, RunFlagsC(), t0=2, nsteps=nsteps, params=[p], ics=[ics], store="all")[0]
+    loss = (out[2].double() ** 2).mean() + (out[0].double() * 1e8).pow(2).mean()
+    loss.backward()
+    eng.check_device_status()
+    return {k: v.grad.clone() for k, v in p.items()}, ics.grad.double().clone()
+
+
+@pytest.mark.parametrize("B", [8, 11])
+def test_tc_adjoint_matches_simt_adjoint(cuda, B):
+    """The tcgen05 Legendre adjoint (3xTF32) against the SIMT FP32 adjoint on the
+    same forward (bounds: 3xTF32 operand rounding, as for the forward kernel)."""
+    import torch
+
+    tc = _engine([(42, B)], "fast")
+    assert tc.uses_tensor_cores
+    g_tc, ic_tc = _grads(tc)
+    g_simt, ic_simt = _grads(_engine([(42, B)], "fast", tc=False))
+    for k in g_tc:
+        rel = float(torch.linalg.vector_norm(g_tc[k] - g_simt[k]) / torch.linalg.vector_norm(g_simt[k]))
+        assert rel < 2e-5, (k, rel)
+    for f in range(5):
+        rel = float(torch.linalg.vector_norm(ic_tc[f] - ic_simt[f]) / torch.linalg.vector_norm(ic_simt[f]))
+        assert rel < 2e-4, (f, rel)
