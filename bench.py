@@ -188,7 +188,7 @@ def _algorithmic_bytes(kernel, B, J=64, M=42, elem=8):
 # ncu summary (profiles/) of each kernel at this workload, which records the
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
 _PROFILE_OF = {"spectral": "k_spectral_tc_fast_M42_B256.md", "grid": "k_grid_step_fast_M42_B256.md",
-               "grid_adj": "k_grid_adjoint_fast_M42_B256.md", "spectral_adj": "k_spectral_adj_fast_M42_B256.md"}
+               "grid_adj": "k_grid_adjoint_fast_M42_B256.md", "spectral_adj": "k_spectral_adj_tc_fast_M42_B256.md"}
 
 
 def _ncu_traffic(kernel):

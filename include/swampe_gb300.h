@@ -213,6 +213,25 @@ int swp_device_status(swp_plan* plan, int* status, void* stream);
  * was created), else 0.  No reference counterpart. */
 int swp_plan_uses_tensor_cores(const swp_plan* plan);
 
+/* Autotuner of the plan's tile shapes (no reference counterpart): for every
+ * group, each member tile MT in {1, 2, 4, 8} (<= B) of the SIMT Legendre
+ * kernels that fits in shared memory is timed -- nrep launches of the step's
+ * Legendre kernel and of its adjoint on the caller's buffers st / adj, which
+ * it overwrites (pass scratch copies) -- and the fastest is kept for the
+ * plan's later calls (captured graphs are dropped).  chosen_mt[g] (may be
+ * NULL) receives the choice.  The tensor-core kernels (FP32, M = 42) keep
+ * their fixed tile of 8 members and are not affected. */
+int swp_plan_autotune(swp_plan* plan, const swp_group_state* st, const swp_group_adjoint* adj,
+                      const swp_flags* flags, int nrep, int* chosen_mt, void* stream);
+
+/* Tile shapes of group g: member tile of the SIMT Legendre kernels and
+ * latitude rows per CTA of the grid step kernel. */
+int swp_plan_tiles(const swp_plan* plan, int g, int* mt, int* jb);
+
+/* Set the member tile of group g (1, 2, 4 or 8) -- e.g. a previously tuned
+ * value; SWP_ERR_ARG if it does not fit in shared memory. */
+int swp_plan_set_tile(swp_plan* plan, int g, int mt);
+
 /* Allocation-free swp_adjoint_step (no counterpart in the reference, which has
  * no C interface): identical arguments and results, except that adj[g].lam_y
  * is ignored and the step's scratch lives in a fixed device array of

@@ -73,7 +73,7 @@ EXPORTS = (
     "swp_state_copy", "swp_adjoint_step", "swp_adjoint_seed", "swp_adjoint_init",
     "swp_adjoint_window", "swp_time_kernels", "swp_forward_checkpointed", "swp_adjoint_step_noalloc",
     "swp_tc_selftest", "swp_device_status", "swp_plan_uses_tensor_cores", "swp_forward_stored",
-    "swp_adjoint_stored",
+    "swp_adjoint_stored", "swp_plan_autotune", "swp_plan_tiles", "swp_plan_set_tile",
 )
 
 _lib = None
@@ -119,6 +119,9 @@ def load(path: os.PathLike | str | None = None) -> ctypes.CDLL:
         "swp_plan_uses_tensor_cores": (i, [vp]),
         "swp_forward_stored": (i, [vp, gsp, fp, i, i, vpp, vp]),
         "swp_adjoint_stored": (i, [vp, gsp, vpp, gap, fp, i, i, vp]),
+        "swp_plan_autotune": (i, [vp, gsp, gap, fp, i, ip, vp]),
+        "swp_plan_tiles": (i, [vp, i, ip, ip]),
+        "swp_plan_set_tile": (i, [vp, i, i]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

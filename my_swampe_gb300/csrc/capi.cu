@@ -607,6 +607,85 @@ int adjoint_stored_impl(swp_plan* p, const swp_group_state* st, void* const* sta
   return run_graph(p, key, body, s);
 }
 
+// Shared memory of the SIMT Legendre kernels for the plan's current member tiles.
+void refresh_spec_smem(swp_plan* p) {
+  p->spec_smem = 0;
+  p->spec_adj_smem = 0;
+  const bool f64 = p->precision == SWP_FP64;
+  for (int g = 0; g < p->ng; ++g) {
+    const int J = p->geom[g].J;
+    size_t ss = f64 ? spec_smem_bytes<double>(p->M[g], J, p->MT[g]) : spec_smem_bytes<float>(p->M[g], J, p->MT[g]);
+    size_t sa = f64 ? spec_adj_smem_bytes<double>(p->M[g], J, p->MT[g]) : spec_adj_smem_bytes<float>(p->M[g], J, p->MT[g]);
+    p->spec_smem = std::max(p->spec_smem, ss);
+    p->spec_adj_smem = std::max(p->spec_adj_smem, sa);
+  }
+}
+
+void clear_graphs(swp_plan* p) {
+  for (auto& ge : p->graphs)
+    if (ge.exec) cudaGraphExecDestroy(ge.exec);
+  p->graphs.clear();
+}
+
+// Member tile (MT) of the SIMT Legendre kernels, per group: every power of two
+// up to 8 (and B) whose kernels fit in shared memory is timed on the caller's
+// buffers (forward Legendre kernel + its adjoint, steady-state step form), and
+// the fastest is kept.  The tensor-core kernels use a fixed tile of 8.
+template <typename T>
+int autotune_impl(swp_plan* p, const swp_group_state* st, const swp_group_adjoint* adj, const swp_flags* f, int nrep,
+                  int* chosen, cudaStream_t s) {
+  const bool f64 = p->precision == SWP_FP64;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return fail(p, SWP_ERR_CUDA, "autotune events");
+  int rc = update_coefs<T>(p, st, s);
+  for (int g = 0; g < p->ng && rc == SWP_OK; ++g) {
+    const int J = p->geom[g].J;
+    const int keep = p->MT[g];
+    int best = keep;
+    float best_ms = 3.4e38f;
+    for (int mt = 1; mt <= 8 && mt <= std::max(1, p->B[g]); mt *= 2) {
+      size_t ss = f64 ? spec_smem_bytes<double>(p->M[g], J, mt) : spec_smem_bytes<float>(p->M[g], J, mt);
+      size_t sa = f64 ? spec_adj_smem_bytes<double>(p->M[g], J, mt) : spec_adj_smem_bytes<float>(p->M[g], J, mt);
+      if (ss > 227 * 1024 || sa > 227 * 1024) continue;
+      p->MT[g] = mt;
+      refresh_spec_smem(p);
+      int nbs = 0;
+      SpecLaunch<T> LS = make_spec<T>(p, st, nbs);
+      LS.mode = 0;
+      LS.cfg = make_cfg(f);
+      LS.cfg.diagnostics = 0;
+      LS.cfg.ra_mode = f->modalflag ? 2 : 1;
+      LS.cfg.incremental = step_incremental(p, f, f->t_start + 1) ? 1 : 0;
+      SpecLaunch<T> LA = LS;
+      for (int q = 0; q < p->ng; ++q) {
+        LA.grp[q].lam = (typename cplx<T>::type*)adj[q].lam;
+        LA.grp[q].lamY = (const typename cplx<T>::type*)adj[q].lam_y;
+        LA.grp[q].grad = adj[q].grad;
+      }
+      cudaError_t e = cudaSuccess;
+      for (int r = 0; r < nrep + 1 && e == cudaSuccess; ++r) {  // the first repetition warms up
+        if (r == 1) cudaEventRecord(e0, s);
+        e = launch_spec<T>(LS, nbs, p->spec_smem, s);
+        if (e == cudaSuccess) e = launch_spec_adj<T>(LA, nbs, p->spec_adj_smem, s);
+      }
+      cudaEventRecord(e1, s);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess) { rc = cuda_check(p, e, "autotune launch"); break; }
+      if (ms < best_ms) { best_ms = ms; best = mt; }
+    }
+    p->MT[g] = rc == SWP_OK ? best : keep;
+    if (chosen) chosen[g] = p->MT[g];
+  }
+  refresh_spec_smem(p);
+  clear_graphs(p);  // captured graphs hold the old launch shapes
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
 }  // namespace
 
 namespace swp {
@@ -900,6 +979,38 @@ int swp_adjoint_stored(swp_plan* p, const swp_group_state* st, void* const* stat
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? adjoint_stored_impl<double>(p, st, states, adj, f, t0, nsteps, s)
                                   : adjoint_stored_impl<float>(p, st, states, adj, f, t0, nsteps, s);
+}
+
+int swp_plan_autotune(swp_plan* p, const swp_group_state* st, const swp_group_adjoint* adj, const swp_flags* f,
+                      int nrep, int* chosen_mt, void* stream) {
+  if (!p || !st || !adj || !f || nrep < 1) return fail(p, SWP_ERR_ARG, "bad argument");
+  for (int g = 0; g < p->ng; ++g)
+    if (!st[g].fourier || !st[g].params || !st[g].member || !adj[g].lam || !adj[g].lam_y)
+      return fail(p, SWP_ERR_ARG, "missing buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWP_FP64 ? autotune_impl<double>(p, st, adj, f, nrep, chosen_mt, s)
+                                  : autotune_impl<float>(p, st, adj, f, nrep, chosen_mt, s);
+}
+
+int swp_plan_tiles(const swp_plan* p, int g, int* mt, int* jb) {
+  if (!p || g < 0 || g >= p->ng) return SWP_ERR_ARG;
+  if (mt) *mt = p->MT[g];
+  if (jb) *jb = p->JB[g];
+  return SWP_OK;
+}
+
+int swp_plan_set_tile(swp_plan* p, int g, int mt) {
+  if (!p || g < 0 || g >= p->ng) return SWP_ERR_ARG;
+  const bool f64 = p->precision == SWP_FP64;
+  const int J = p->geom[g].J;
+  if (mt < 1 || mt > 8 || (mt & (mt - 1)) != 0) return fail(p, SWP_ERR_ARG, "member tile must be 1, 2, 4 or 8");
+  size_t ss = f64 ? spec_smem_bytes<double>(p->M[g], J, mt) : spec_smem_bytes<float>(p->M[g], J, mt);
+  size_t sa = f64 ? spec_adj_smem_bytes<double>(p->M[g], J, mt) : spec_adj_smem_bytes<float>(p->M[g], J, mt);
+  if (ss > 227 * 1024 || sa > 227 * 1024) return fail(p, SWP_ERR_ARG, "member tile does not fit in shared memory");
+  p->MT[g] = mt;
+  refresh_spec_smem(p);
+  clear_graphs(p);
+  return SWP_OK;
 }
 
 }  // extern "C"

@@ -28,6 +28,9 @@ PRECISIONS = {"fp64": _lib.SWP_FP64, "fast": _lib.SWP_FAST}
 
 PARAM_NAMES = ("dt", "a", "omega", "Phibar", "taurad", "taudrag", "DPhieq", "K6", "K6Phi", "alpha")
 
+# member tiles chosen by Engine.autotune, per (precision, ((M, B), ...))
+_TUNED: Dict[Tuple, List[int]] = {}
+
 
 @dataclass
 class RunFlagsC:
@@ -62,7 +65,8 @@ def _require_cuda(device) -> torch.device:
 class Engine:
     """One plan + device state for a list of ``(M, B)`` groups."""
 
-    def __init__(self, groups: Sequence[Tuple[int, int]], precision: str = "fp64", device=None):
+    def __init__(self, groups: Sequence[Tuple[int, int]], precision: str = "fp64", device=None,
+                 autotune: bool = False):
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, got {precision!r}")
         for M, _ in groups:
@@ -101,6 +105,8 @@ class Engine:
             gd["member"] = torch.zeros((_lib.NMEMBER, gd["B"]), dtype=torch.float64, device=dev)
             self.groups.append(gd)
         self._geo_cache: Dict[int, Dict[str, torch.Tensor]] = {}
+        if autotune:
+            self.autotune()
 
     # ------------------------------------------------------------------ utils
     def __del__(self):
@@ -129,6 +135,33 @@ class Engine:
 
     def _check(self, rc, what):
         _lib.check(rc, self._plan, what)
+
+    def tiles(self) -> List[Tuple[int, int]]:
+        """(member tile of the SIMT Legendre kernels, latitude rows per grid CTA) per group."""
+        out = []
+        for g in range(len(self.groups)):
+            mt, jb = ctypes.c_int(), ctypes.c_int()
+            self._check(self.lib.swp_plan_tiles(self._plan, g, ctypes.byref(mt), ctypes.byref(jb)), "tiles")
+            out.append((mt.value, jb.value))
+        return out
+
+    def autotune(self, nrep: int = 5, use_cache: bool = True) -> List[int]:
+        """Pick the member tile of every group by timing (swp_plan_autotune) on
+        scratch copies of this engine's buffers.  Results are cached per
+        (precision, groups) for the process."""
+        key = (self.precision, tuple((gd["M"], gd["B"]) for gd in self.groups))
+        if use_cache and key in _TUNED:
+            for g, mt in enumerate(_TUNED[key]):
+                self._check(self.lib.swp_plan_set_tile(self._plan, g, int(mt)), "set_tile")
+            return list(_TUNED[key])
+        scratch = [gd["fourier"].clone() for gd in self.groups]
+        lam, lamy, grad = self.new_adjoint_buffers()
+        chosen = (ctypes.c_int * len(self.groups))()
+        self._check(self.lib.swp_plan_autotune(self._plan, self._states(fourier=scratch), self._adjs(lam, lamy, grad),
+                                               ctypes.byref(RunFlagsC().c()), int(nrep), chosen, self.stream),
+                    "autotune")
+        _TUNED[key] = [int(x) for x in chosen]
+        return list(_TUNED[key])
 
     @property
     def uses_tensor_cores(self) -> bool:

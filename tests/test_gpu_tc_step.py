@@ -156,3 +156,29 @@ def test_tc_adjoint_matches_simt_adjoint(cuda, B):
     for f in range(5):
         rel = float(torch.linalg.vector_norm(ic_tc[f] - ic_simt[f]) / torch.linalg.vector_norm(ic_simt[f]))
         assert rel < 2e-4, (f, rel)
+
+
+@pytest.mark.parametrize("precision,M", [("fp64", 42), ("fast", 63)])
+def test_autotuned_tiles_give_identical_steps(cuda, precision, M):
+    """The autotuner picks a member tile among those that fit; a step's result
+    does not depend on the tile (each member's arithmetic is the same)."""
+    import torch
+    from my_swampe_gb300 import workloads
+    from my_swampe_gb300.engine import Engine, RunFlagsC
+
+    outs = []
+    for tile in (None, 1):
+        eng = Engine([(M, 6)], precision)
+        if tile is None:
+            chosen = eng.autotune(nrep=2, use_cache=False)
+            assert chosen[0] in (1, 2, 4) and eng.tiles()[0][0] == chosen[0]
+        else:
+            eng.lib.swp_plan_set_tile(eng._plan, 0, tile)
+            assert eng.tiles()[0][0] == 1
+        wl = workloads.forced_ensemble(eng, seed=2)
+        workloads.apply_params(eng, 0, wl["params"])
+        flags = RunFlagsC()
+        eng.init_state([wl["ics"]], flags)
+        eng.forward(flags, t0=2, nsteps=6)
+        outs.append(eng.output_physical(flags)[0])
+    assert torch.equal(outs[0], outs[1])
