@@ -341,10 +341,13 @@ int winds_impl(swp_plan* p, const swp_group_state* st, void* const* ed, void* co
   return cuda_check(p, e, "winds inverse transform");
 }
 
+// `sweep`: the step is one of an adjoint sweep, whose lambda always comes from
+// the Legendre adjoint (or the seed), so the grid adjoint may use its tied
+// F / G components.
 template <typename T>
 int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
                       const swp_group_adjoint* adj, const swp_flags* f, int t, cudaStream_t s,
-                      bool refresh_coefs = true) {
+                      bool refresh_coefs = true, bool sweep = false) {
   int nbg = 0, nbs = 0;
   if (refresh_coefs) {
     int rc = update_coefs<T>(p, st_in, s);
@@ -353,6 +356,7 @@ int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group
   GridLaunch<T> LG = make_grid<T>(p, st_out, nbg);
   LG.mode = GM_ADJ_STEP;
   LG.cfg = make_cfg(f);
+  LG.cfg.lam_fg_tied = (sweep && f->forcflag && f->test == 0) ? 1 : 0;
   for (int g = 0; g < p->ng; ++g) {
     LG.grp[g].primal = (const typename cplx<T>::type*)st_out[g].fourier;
     LG.grp[g].lam = (typename cplx<T>::type*)adj[g].lam;
@@ -433,7 +437,7 @@ int adjoint_window_impl(swp_plan* p, const swp_group_state* st, void* const* slo
         a[g].fourier = (char*)slots[g] + (size_t)k * ss;
         b[g].fourier = (char*)slots[g] + (size_t)(k + 1) * ss;
       }
-      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, t0 + k, cs, false);
+      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, t0 + k, cs, false, true);
       if (rc) return rc;
     }
     return SWP_OK;
@@ -468,6 +472,7 @@ int time_kernels_impl(swp_plan* p, const swp_group_state* st, const swp_group_ad
   GridLaunch<T> LGa = LG;
   SpecLaunch<T> LSa = LS;
   LGa.mode = GM_ADJ_STEP;
+  LGa.cfg.lam_fg_tied = (f->forcflag && f->test == 0) ? 1 : 0;  // as inside an adjoint sweep
   if (adj) {
     for (int g = 0; g < p->ng; ++g) {
       LGa.grp[g].primal = LG.grp[g].four;
@@ -592,7 +597,7 @@ int adjoint_stored_impl(swp_plan* p, const swp_group_state* st, void* const* sta
         a[g].fourier = (char*)states[g] + (size_t)k * ss;
         b[g].fourier = (char*)states[g] + (size_t)(k + 1) * ss;
       }
-      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, t0 + k, cs, false);
+      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, t0 + k, cs, false, true);
       if (rc) return rc;
     }
     return SWP_OK;

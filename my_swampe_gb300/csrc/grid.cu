@@ -602,7 +602,13 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     // ---------------------------------------------- adjoint of GM_STEP / GM_INIT
     PhysicsAdj<T> pa;
     pa.Pb = ph.Pb; pa.itr = ph.itr; pa.itd = ph.itd; pa.DPe = ph.DPe; pa.nodrag = ph.nodrag; pa.forced = ph.forced;
-    const int nz = ph.forced ? 8 : 5;
+    // With forcing on, the Legendre adjoint writes lambda_F = lambda_B and
+    // lambda_G = -lambda_A exactly (adj_store_point, forc = 1); inside an
+    // adjoint sweep (cfg.lam_fg_tied) F and G are then not transformed but
+    // taken from B and A.
+    const bool tied = MODE == GM_ADJ_STEP && ph.forced && cfg.lam_fg_tied != 0;
+    const int nzl = ph.forced ? 8 : 5;               // lambda fields the physics adjoint reads
+    const int nz = tied ? 6 : nzl;                   // of them, transformed here
     const int npr = (MODE == GM_ADJ_STEP) ? 4 : 0;  // primal fields transformed here (eta, Phi, U, V)
     // batch 1: lambda of the nonlinear Fourier terms -> grid (adjoint of fft(x/I)[:M+1]:
     // lambda x_i = (1/I) Re sum_{m=0..M} lambda_m e^{i theta}) and the primal grid fields
@@ -635,6 +641,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
           T2 v = q < nz ? zin[((size_t)q * JB + r) * LS + n] : mk<T2>(0, 0);
           lz[q] = e ? v.y : v.x;
         }
+        if (tied) { lz[6] = lz[1]; lz[7] = -lz[0]; }
         T eta, Phi, U, V;
         if (MODE == GM_ADJ_STEP) {
           T2 a0 = zin[((size_t)(nz + 0) * JB + r) * LS + n], a1 = zin[((size_t)(nz + 1) * JB + r) * LS + n];

@@ -297,6 +297,7 @@ struct StepCfg {
   double blowup;   // RMS threshold
   int step;        // scan-step index (row of the diagnostic arrays)
   int incremental; // advance a band-limited state by increments (FP32 path)
+  int lam_fg_tied; // adjoint sweep: lambda_F = lambda_B, lambda_G = -lambda_A hold (forced)
 };
 
 }  // namespace swp
