@@ -20,6 +20,14 @@
 
 namespace swp {
 
+// x / pts on the FP32 path as x * (correctly rounded 1/pts): one reciprocal
+// per point instead of IEEE divisions (within 1 ulp of the quotient); the FP64
+// path divides exactly.
+__device__ __forceinline__ float div_pts(float x, float inv, float) { return x * inv; }
+__device__ __forceinline__ double div_pts(double x, double, double pts) { return x / pts; }
+__device__ __forceinline__ float recip_pts(float pts) { return __frcp_rn(pts); }
+__device__ __forceinline__ double recip_pts(double) { return 0.0; }
+
 template <typename T> __device__ __forceinline__ T tiny_val();
 template <> __device__ __forceinline__ double tiny_val<double>() { return DBL_MIN; }
 template <> __device__ __forceinline__ float tiny_val<float>() { return FLT_MIN; }
@@ -112,7 +120,7 @@ struct Physics {
       T Qc = Q < (T)0 ? (T)0 : Q;                        // forcing.py:133
       T pt = Phi + Pb;
       T pts = fabs(pt) > (T)0 ? pt : tiny_val<T>();     // forcing.py:139-140
-      T r = Qc / pts;
+      T r = div_pts(Qc, recip_pts(pts), pts);
       T Ru = -U * r, Rv = -V * r;
       out[5] = Q;
       out[6] = nodrag ? Ru : Ru - U * itd;               // forcing.py:143-153
@@ -144,14 +152,15 @@ struct PhysicsAdj {
       T Qc = pos ? Q : (T)0;
       T pt = Phi + Pb;
       T pts = fabs(pt) > (T)0 ? pt : tiny_val<T>();
-      T r = Qc / pts;
+      const T ipts = recip_pts(pts);
+      T r = div_pts(Qc, ipts, pts);
       T lF = lz[6], lG = lz[7];
       T lr = -U * lF - V * lG;
       T itdd = nodrag ? (T)0 : itd;
       lU += lF * (-r - itdd);
       lV += lG * (-r - itdd);
-      T lQc = lr / pts;
-      T lpts = -lr * r / pts;
+      T lQc = div_pts(lr, ipts, pts);
+      T lpts = div_pts(-lr * r, ipts, pts);
       T lQ = lz[5] + (pos ? lQc : (T)0);
       lPhi += -itr * lQ + lpts;
       // per-thread partial sums in the compute type (two points per thread);
@@ -267,6 +276,8 @@ __device__ __forceinline__ void write_r2c(const C& c, const typename cplx<T>::ty
   if (threadIdx.x < 16) s_dst[threadIdx.x] = (int)threadIdx.x < nf ? dst[threadIdx.x] : nullptr;
   __syncthreads();
   constexpr int n1 = C::M + 1;
+  // unrolled so that several independent bins are in flight per thread
+#pragma unroll 4
   for (int t = threadIdx.x; t < nf * n1 * C::JB; t += blockDim.x) {
     const int r = t % C::JB, k = (t / C::JB) % n1, q = t / (C::JB * n1);
     const T2 v = r2c_post<T2, T>(res + ((size_t)q * C::JB + r) * C::LS, C::L, k, c.twI, k == 0 ? s0 : s);
@@ -411,6 +422,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       __syncthreads();
     }
     double lrms = 0.0, lspin = 1e300, lmin = 1e300, lmax = -1e300;
+#pragma unroll 2
     for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
       int n = t % L, r = t / L, j = j0 + r;
       T vals[8][2];
