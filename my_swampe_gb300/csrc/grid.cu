@@ -762,8 +762,12 @@ __host__ __device__ constexpr int grid_jb(int M, int mode) {
   return grid_buf_bytes<T>(M, mode, 8) <= 72 * 1024 ? 8 : grid_buf_bytes<T>(M, mode, 4) <= 200 * 1024 ? 4 : 2;
 }
 
+// Resident CTAs per SM the register budget is sized for: FP32 adjoint 4 (its
+// 52 KB of shared memory allow 4), FP32 forward modes 3 (8 rows per CTA at
+// M=42 take 68 KB), FP64 2.
 template <typename T, int MODE>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_grid(const __grid_constant__ GridLaunch<T> Lc) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? (MODE == GM_ADJ_STEP ? 4 : 3) : 2)
+    k_grid(const __grid_constant__ GridLaunch<T> Lc) {
   int idx;
   const GridGroup<T>& G = pick_ggroup(Lc, idx);
   switch (G.g.M) {  // groups of different truncations share one launch
