@@ -370,6 +370,14 @@ def run_model_scan(
             Bm = b
     batched = Bm is not None
     B = Bm if batched else 1
+    # shapes of the explicit initial fields, checked at entry like the reference
+    # (before any device work)
+    for name, x in (("eta0_init", eta0_init), ("delta0_init", delta0_init), ("Phi0_init", Phi0_init),
+                    ("U0_init", U0_init), ("V0_init", V0_init)):
+        if x is not None:
+            shp = tuple(torch.as_tensor(x).shape)
+            if shp != (J, I) and not (batched and shp == (B, J, I)):
+                raise ValueError(f"{name} must have shape {(J, I)}, got {shp}.")
 
     eng = Engine([(M, B)], precision, device)
     dev = eng.device

@@ -1,0 +1,129 @@
+"""Host-side behaviour that needs no GPU: argument validation at entry (the
+reference's unit_tests/test_invalid_input.py cases), the loud failure of the
+product path without CUDA, continuation helpers and the per-member parameter
+rules.  All checks run before any device work."""
+import numpy as np
+import pytest
+
+from my_swampe_gb300 import continuation
+from my_swampe_gb300.model import run_model_scan, run_model_scan_final
+
+BASE = dict(M=42, dt=600.0, Phibar=3.0e5, omega=3.2e-5, a=8.2e7)
+J, I = 64, 128
+
+
+def test_tmax_too_small():
+    with pytest.raises(ValueError, match="tmax"):
+        run_model_scan(**BASE, tmax=1)
+
+
+@pytest.mark.parametrize("dt", [0.0, -30.0])
+def test_dt_non_positive(dt):
+    kw = dict(BASE, dt=dt)
+    with pytest.raises(ValueError, match="dt"):
+        run_model_scan(**kw, tmax=4)
+
+
+def test_starttime_after_tmax():
+    with pytest.raises(ValueError, match="starttime"):
+        run_model_scan(**BASE, tmax=4, starttime=10)
+
+
+def test_unsupported_test_selector():
+    with pytest.raises(NotImplementedError, match="test=99"):
+        run_model_scan(**BASE, tmax=4, test=99)
+
+
+@pytest.mark.parametrize("M", [21, 85, 0])
+def test_unsupported_M(M):
+    kw = dict(BASE, M=M)
+    with pytest.raises(ValueError, match="M"):
+        run_model_scan(**kw, tmax=4)
+
+
+def test_partial_initial_conditions():
+    with pytest.raises(ValueError, match="eta0_init.*delta0_init.*Phi0_init"):
+        run_model_scan(**BASE, tmax=4, eta0_init=np.zeros((J, I)))
+
+
+def test_partial_velocity_initial_conditions():
+    z = np.zeros((J, I))
+    with pytest.raises(ValueError, match="U0_init.*V0_init"):
+        run_model_scan(**BASE, tmax=4, eta0_init=z, delta0_init=z, Phi0_init=z, U0_init=z)
+
+
+def test_wrong_shape_initial_condition():
+    z = np.zeros((J, I))
+    with pytest.raises(ValueError, match="Phi0_init"):
+        run_model_scan(**BASE, tmax=4, eta0_init=z, delta0_init=z, Phi0_init=np.zeros((J + 1, I)))
+
+
+def test_contflag_without_contTime():
+    with pytest.raises(ValueError, match="contTime"):
+        run_model_scan(**BASE, tmax=4, contflag=True)
+
+
+def test_contTime_non_numeric():
+    with pytest.raises(ValueError, match="numeric"):
+        run_model_scan(**BASE, tmax=4, contflag=True, contTime="ten")
+
+
+def test_semi_implicit_with_expflag_and_unimplemented_schemes():
+    with pytest.raises(ValueError, match="semi_implicit"):
+        run_model_scan(**BASE, tmax=4, semi_implicit=True, expflag=True)
+    with pytest.raises(ValueError, match="raw_filter"):
+        run_model_scan(**BASE, tmax=4, raw_filter=True, expflag=True)
+    with pytest.raises(NotImplementedError):
+        run_model_scan(**BASE, tmax=4, semi_implicit=True)
+
+
+def test_final_rejects_return_history():
+    with pytest.raises(TypeError):
+        run_model_scan_final(**BASE, tmax=4, return_history=True)
+
+
+def test_member_parameter_lengths_must_agree():
+    with pytest.raises(ValueError, match="same length"):
+        run_model_scan(**BASE, tmax=4, taurad=[1e4, 2e4], DPhieq=[1e5, 2e5, 3e5])
+    with pytest.raises(ValueError, match="scalars or 1-D"):
+        run_model_scan(**BASE, tmax=4, taurad=np.ones((2, 2)))
+
+
+def test_member_axis_of_fields_must_match_parameters():
+    z = np.zeros((3, J, I))
+    with pytest.raises(ValueError, match="member axis"):
+        run_model_scan(**BASE, tmax=4, taurad=[1e4, 2e4], eta0_init=z, delta0_init=z, Phi0_init=z)
+
+
+def test_valid_call_without_cuda_fails_loudly():
+    """The product path has no CPU fallback."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(RuntimeError, match="CUDA|GPU|libswampe"):
+        run_model_scan(**BASE, tmax=4)
+
+
+def test_continuation_timestamps_round_trip():
+    """continuation.py:67-132: timestamp = floor(dt * t / unit) and back; exact
+    when dt * t is a whole number of units."""
+    for units, dt, t in (("hours", 600.0, 36), ("minutes", 30.0, 14), ("seconds", 12.0, 5), ("days", 1200.0, 720),
+                         ("steps", 600.0, 17)):
+        ts = continuation.compute_timestamp(units, t, dt)
+        assert continuation.compute_t_from_timestamp(units, float(ts), dt) == t, units
+    assert continuation.compute_timestamp("hours", 12, 600.0) == "2"
+    assert continuation.compute_timestamp("hours", 13, 600.0) == "2"  # floor, as the reference's int()
+    with pytest.raises(ValueError, match="units"):
+        continuation.compute_timestamp("fortnights", 1, 1.0)
+
+
+def test_continuation_pickles_round_trip(tmp_path):
+    rng = np.random.default_rng(3)
+    fields = [rng.standard_normal((J, I)) for _ in range(5)]
+    spin, geo = rng.standard_normal((10, 2)), rng.standard_normal((10, 2))
+    continuation.save_data(7, *fields, spin, geo, custompath=str(tmp_path))
+    back = continuation.load_data(7, custompath=str(tmp_path))
+    for a, b in zip(fields, back):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(continuation.read_pickle("spinup-winds", custompath=str(tmp_path)), spin)
