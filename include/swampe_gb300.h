@@ -23,8 +23,15 @@
  *
  * Memory layout of one truncation group (M, J, I, B members):
  *   fourier : complex[SWP_NFOURIER][M+1][B][J]   (field, zonal wavenumber m, member, latitude)
+ *             fields: eta_prev, eta, delta_prev, delta, Phi_prev, Phi, U, V, A, B, C, D,
+ *             E, PhiF, F, G, eta_mid, delta_mid, Phi_mid.  The *_mid carries are the
+ *             Robert-Asselin-filtered lineage (the physical prev level, and the n-1
+ *             base of the semi-implicit scheme).  The semi-implicit scheme never
+ *             reads the unfiltered prev carries; it keeps its lagged momentum-forcing
+ *             remainders Rum_lag, Rvm_lag in the eta_prev, delta_prev slots.
  *   resid   : real[5][B][J][I]   initial condition minus its band-limited part
- *   params  : double[SWP_NPAR][B]
+ *   params  : double[SWP_NPAR][B]  (dt, a, omega, Phibar, taurad, taudrag, DPhieq,
+ *             K6, K6Phi, RA alpha, semi-implicit si_alpha, RAW williams_alpha)
  *   member  : double[4][B]       (w_curr, w_mid, dead, updated)
  *   diag    : double[nsteps+1][5][B]  (rms^2-sum, min |u|, min Phi, max Phi, dead)
  *   hist    : real[nsteps][5][B][J][I]  (eta, delta, Phi, U, V)
@@ -47,7 +54,7 @@ extern "C" {
 #define SWP_FAST 1
 
 #define SWP_NFOURIER 19
-#define SWP_NPAR 10
+#define SWP_NPAR 12
 #define SWP_MAX_GROUPS 4
 /* Size of the fixed device scratch used by swp_adjoint_step_noalloc (16 MiB). */
 #define SWP_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
@@ -73,7 +80,8 @@ typedef struct {
 
 /* Flags of model.py RunFlags (model.py:156-226) plus the test selector. */
 typedef struct {
-  int scheme;       /* 0 = modified Euler (default), 1 = explicit (expflag)  */
+  int scheme;       /* 0 = modified Euler (default), 1 = explicit (expflag),
+                       2 = semi-implicit leapfrog (semi_implicit=True; forward only) */
   int forcflag;
   int diffflag;
   int modalflag;
@@ -83,6 +91,8 @@ typedef struct {
   int t_start;      /* time index of the initial state (the run's starttime); in the
                        SWP_FAST precision the steps after the first one advance the
                        band-limited state by increments (see swp_forward)       */
+  int raw_filter;   /* Robert-Asselin-Williams filter (RunFlags.raw_filter), weight
+                       williams_alpha = params row 11; forward only               */
 } swp_flags;
 
 /* Create a plan for `ngroups` truncations (M[g] in {42, 63, 106}) with B[g]

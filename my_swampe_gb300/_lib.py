@@ -17,7 +17,7 @@ SWP_OK = 0
 SWP_FP64 = 0
 SWP_FAST = 1
 NFOURIER = 19
-NPAR = 10
+NPAR = 12
 NMEMBER = 4
 NDIAG = 5
 NGRAD = 4
@@ -27,7 +27,9 @@ NRESID = 5
 F_ETA_PREV, F_ETA, F_DELTA_PREV, F_DELTA, F_PHI_PREV, F_PHI, F_U, F_V = range(8)
 F_A, F_B, F_C, F_D, F_E, F_PHIF, F_F, F_G, F_ETA_MID, F_DELTA_MID, F_PHI_MID = range(8, 19)
 # parameter rows
-P_DT, P_A, P_OMEGA, P_PHIBAR, P_TAURAD, P_TAUDRAG, P_DPHIEQ, P_K6, P_K6PHI, P_ALPHA = range(10)
+P_DT, P_A, P_OMEGA, P_PHIBAR, P_TAURAD, P_TAUDRAG, P_DPHIEQ, P_K6, P_K6PHI, P_ALPHA, P_SIALPHA, P_WALPHA = range(12)
+# the semi-implicit scheme keeps its lagged remainders Rum_lag, Rvm_lag in the unfiltered prev slots
+F_RU_LAG, F_RV_LAG = F_ETA_PREV, F_DELTA_PREV
 MS_WCURR, MS_WMID, MS_DEAD, MS_UPDATED = range(4)
 D_RMS2, D_SPIN, D_PHIMIN, D_PHIMAX, D_DEAD = range(5)
 G_TAURAD, G_TAUDRAG, G_DPHIEQ, G_PHIBAR = range(4)
@@ -64,6 +66,7 @@ class Flags(ctypes.Structure):
         ("diagnostics", ctypes.c_int),
         ("blowup", ctypes.c_double),
         ("t_start", ctypes.c_int),
+        ("raw_filter", ctypes.c_int),
     ]
 
 

@@ -47,6 +47,8 @@ class Integration:
                  store: str = "auto", mem_fraction: float = 0.8):
         if flags.scheme != 0:
             raise NotImplementedError("the adjoint is implemented for the modified-Euler scheme")
+        if flags.raw_filter:
+            raise NotImplementedError("the adjoint is implemented for the classic Robert-Asselin filter")
         if flags.test == 1:
             raise NotImplementedError("the adjoint of test=1 (fixed winds) is not implemented")
         if nsteps < 1:

@@ -125,6 +125,10 @@ StepCfg make_cfg(const swp_flags* f) {
   StepCfg c;
   memset(&c, 0, sizeof(c));
   c.scheme = f->scheme;
+  c.raw = f->raw_filter != 0;
+  // relaxation and drag are implicit only where the physical forcing is on
+  // (model.py:912-914: forcflag and test is None)
+  c.si_relax = f->scheme == 2 && f->forcflag && f->test == 0;
   c.forcflag = f->forcflag;
   c.diffflag = f->diffflag;
   c.test = f->test;
@@ -133,8 +137,11 @@ StepCfg make_cfg(const swp_flags* f) {
   return c;
 }
 
+// The incremental form needs a band-limited Fourier curr carry: true after a
+// member's first modified-Euler step, but the RAW filter mixes the initial
+// condition's (not band-limited) Fourier coefficients back into it.
 bool step_incremental(const swp_plan* p, const swp_flags* f, int t) {
-  return p->precision == SWP_FAST && f->scheme == 0 && t > f->t_start;
+  return p->precision == SWP_FAST && f->scheme == 0 && !f->raw_filter && t > f->t_start;
 }
 
 // The Legendre kernel of a modified-Euler step: tcgen05 (3xTF32) on the FP32
@@ -208,7 +215,9 @@ int forward_steps(swp_plan* p, const swp_group_state* st, const swp_flags* f, in
     int t = t0 + k;
     cfg.step = row0 + k;
     cfg.ra_mode = (f->modalflag && t > 2) ? 2 : 1;
-    cfg.write_prev = (f->scheme == 1) || (write_prev_last && k == nsteps - 1);
+    // the semi-implicit scheme keeps its lagged remainders in the prev slots
+    cfg.write_prev = f->scheme != 2 && ((f->scheme == 1) || (write_prev_last && k == nsteps - 1));
+    cfg.si_lag_init = f->scheme == 2 && t == f->t_start;
     cfg.incremental = step_incremental(p, f, t) ? 1 : 0;
     LS.cfg = cfg;
     LG.cfg = cfg;
@@ -273,7 +282,8 @@ int run_graph(swp_plan* p, const std::vector<uint64_t>& key, F body, cudaStream_
 
 void key_flags(std::vector<uint64_t>& k, const swp_flags* f) {
   k.push_back((uint64_t)f->scheme | ((uint64_t)f->forcflag << 4) | ((uint64_t)f->diffflag << 8) |
-              ((uint64_t)f->modalflag << 12) | ((uint64_t)f->test << 16) | ((uint64_t)f->diagnostics << 20));
+              ((uint64_t)f->modalflag << 12) | ((uint64_t)f->test << 16) | ((uint64_t)f->diagnostics << 20) |
+              ((uint64_t)(f->raw_filter != 0) << 24));
   uint64_t bu;
   memcpy(&bu, &f->blowup, 8);
   k.push_back(bu);
@@ -862,12 +872,25 @@ int swp_diagnose_winds(swp_plan* p, const swp_group_state* st, void* const* ed, 
   return p->precision == SWP_FP64 ? winds_impl<double>(p, st, ed, uv, s) : winds_impl<float>(p, st, ed, uv, s);
 }
 
+// Scheme switches every stepping entry checks (model.py:1531-1537).  The
+// adjoint covers the modified-Euler scheme with the classic filter.
+static int check_scheme(swp_plan* p, const swp_flags* f, bool adjoint) {
+  if (f->scheme < 0 || f->scheme > 2) return fail(p, SWP_ERR_ARG, "scheme must be 0, 1 or 2");
+  if (f->test < 0 || f->test > 2) return fail(p, SWP_ERR_ARG, "test must be 0 (None), 1 or 2");
+  if (f->raw_filter && f->scheme == 1)
+    return fail(p, SWP_ERR_ARG, "raw_filter is incompatible with the explicit scheme");
+  if (adjoint && f->scheme != 0)
+    return fail(p, SWP_ERR_UNSUPPORTED, "adjoint is implemented for the modified-Euler scheme");
+  if (adjoint && f->raw_filter)
+    return fail(p, SWP_ERR_UNSUPPORTED, "adjoint is implemented for the classic Robert-Asselin filter");
+  return SWP_OK;
+}
+
 int swp_forward(swp_plan* p, const swp_group_state* st, const swp_flags* f, int t0, int nsteps, int row0,
                 int write_prev_last, void* stream) {
   if (!p || !st || !f) return fail(p, SWP_ERR_ARG, "null argument");
   if (nsteps < 0) return fail(p, SWP_ERR_ARG, "nsteps must be >= 0");
-  if (f->scheme != 0 && f->scheme != 1) return fail(p, SWP_ERR_ARG, "scheme must be 0 or 1");
-  if (f->test < 0 || f->test > 2) return fail(p, SWP_ERR_ARG, "test must be 0 (None), 1 or 2");
+  if (int rc = check_scheme(p, f, false)) return rc;
   for (int g = 0; g < p->ng; ++g) {
     if (!st[g].fourier || !st[g].params || !st[g].member) return fail(p, SWP_ERR_ARG, "missing state buffer");
     if (f->diagnostics && !st[g].diag) return fail(p, SWP_ERR_ARG, "diagnostics requested without a diag buffer");
@@ -900,7 +923,7 @@ int swp_state_copy(swp_plan* p, const swp_group_state* st, void* const* ckpt, in
 int swp_adjoint_step(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
                      const swp_group_adjoint* adj, const swp_flags* f, int t, void* stream) {
   if (!p || !st_in || !st_out || !adj || !f) return fail(p, SWP_ERR_ARG, "null argument");
-  if (f->scheme != 0) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint is implemented for the modified-Euler scheme");
+  if (int rc = check_scheme(p, f, true)) return rc;
   if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint of test=1 (fixed winds) is not implemented");
   if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint runs with diagnostics off (no blow-up gate)");
   for (int g = 0; g < p->ng; ++g)
@@ -930,7 +953,7 @@ int swp_adjoint_window(swp_plan* p, const swp_group_state* st, void* const* slot
                        const swp_flags* f, int t0, int nsteps, void* stream) {
   if (!p || !st || !slots || !adj || !f) return fail(p, SWP_ERR_ARG, "null argument");
   if (nsteps < 1) return fail(p, SWP_ERR_ARG, "nsteps must be >= 1");
-  if (f->scheme != 0) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint is implemented for the modified-Euler scheme");
+  if (int rc = check_scheme(p, f, true)) return rc;
   if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint of test=1 (fixed winds) is not implemented");
   if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint runs with diagnostics off (no blow-up gate)");
   for (int g = 0; g < p->ng; ++g)
@@ -953,6 +976,7 @@ int swp_forward_checkpointed(swp_plan* p, const swp_group_state* st, const swp_f
   if (!p || !st || !f || !ckpt) return fail(p, SWP_ERR_ARG, "null argument");
   if (nsteps < 1 || ckpt_every < 1) return fail(p, SWP_ERR_ARG, "nsteps and ckpt_every must be >= 1");
   if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "checkpointed forward runs with diagnostics off");
+  if (int rc = check_scheme(p, f, false)) return rc;
   for (int g = 0; g < p->ng; ++g)
     if (!ckpt[g] || !st[g].fourier || !st[g].params || !st[g].member) return fail(p, SWP_ERR_ARG, "missing buffer");
   cudaStream_t s = (cudaStream_t)stream;
@@ -965,6 +989,7 @@ int swp_forward_stored(swp_plan* p, const swp_group_state* st, const swp_flags* 
   if (!p || !st || !f || !states) return fail(p, SWP_ERR_ARG, "null argument");
   if (nsteps < 1) return fail(p, SWP_ERR_ARG, "nsteps must be >= 1");
   if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "stored forward runs with diagnostics off");
+  if (int rc = check_scheme(p, f, false)) return rc;
   for (int g = 0; g < p->ng; ++g)
     if (!states[g] || !st[g].fourier || !st[g].params || !st[g].member) return fail(p, SWP_ERR_ARG, "missing buffer");
   cudaStream_t s = (cudaStream_t)stream;
@@ -976,7 +1001,7 @@ int swp_adjoint_stored(swp_plan* p, const swp_group_state* st, void* const* stat
                        const swp_flags* f, int t0, int nsteps, void* stream) {
   if (!p || !st || !states || !adj || !f) return fail(p, SWP_ERR_ARG, "null argument");
   if (nsteps < 1) return fail(p, SWP_ERR_ARG, "nsteps must be >= 1");
-  if (f->scheme != 0) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint is implemented for the modified-Euler scheme");
+  if (int rc = check_scheme(p, f, true)) return rc;
   if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint of test=1 (fixed winds) is not implemented");
   if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint runs with diagnostics off (no blow-up gate)");
   for (int g = 0; g < p->ng; ++g)

@@ -4,6 +4,9 @@
 // within one.  The expressions are the ones the reference evaluates:
 //   filters.py:95-151          sigma, sigmaPhi (hyperdiffusion), with sigma - 1
 //                              and sigmaPhi - 1 formed without cancellation
+//   filters.py:154-213         exponential sigma, sigmaPhi (semi-implicit scheme)
+//   semi_implicit_tdiff.py     implicit / explicit shares 2 dt si_alpha, 2 dt (1 - si_alpha)
+//   model.py:1007-1087         RAW weights alpha w, alpha (1 - w)
 //   time_stepping.py:491-534   tstepcoeff, tstepcoeff2, tstepcoeffmn
 //   modEuler_tdiff.py:80-261, explicit_tdiff.py:62-226  scalar factors
 //   spectral_transform.py:577-594  a / (n(n+1)), omega / sqrt(0.375)
@@ -32,6 +35,8 @@ __global__ void k_coefs(const double* __restrict__ par, const double* __restrict
       C.nco[NC_SIGM1 * qs + o] = (T)(-x / (1.0 + x));
       C.nco[NC_SIGPM1 * qs + o] = (T)(-xp / (1.0 + xp));
       C.nco[NC_TC * qs + o] = (T)((n == 0) ? 0.0 : a / ((double)n * (n + 1)));
+      C.nco[NC_SIGX * qs + o] = (T)exp(-(2.0 * dt * K6) * fmax(ncoeff - 8.0 / a6, 0.0));
+      C.nco[NC_SIGPX * qs + o] = (T)exp(-(2.0 * dt * K6P) * ncoeff);
     } else if (t < n_nco + n_jco) {
       const int u = t - n_nco, b = u / J, j = u % J;
       const double a = par[P_A * B + b], dt = par[P_DT * B + b];
@@ -52,7 +57,15 @@ __global__ void k_coefs(const double* __restrict__ par, const double* __restrict
       mc[MC_2DT * B + b] = (T)(2.0 * dt);
       mc[MC_ITD * B + b] = (T)(1.0 / td);
       mc[MC_OM * B + b] = (T)(om / sqrt(0.375));
-      mc[MC_ALPHA * B + b] = (T)par[P_ALPHA * B + b];
+      const double al = par[P_ALPHA * B + b], sa = par[P_SIALPHA * B + b], wa = par[P_WALPHA * B + b];
+      mc[MC_ALPHA * B + b] = (T)al;
+      mc[MC_SIXI * B + b] = (T)(2.0 * dt * sa);
+      mc[MC_SIEX * B + b] = (T)(2.0 * dt * (1.0 - sa));
+      mc[MC_SIITD * B + b] = (T)(td == -1.0 ? 0.0 : 1.0 / td);
+      mc[MC_SIITR * B + b] = (T)(1.0 / par[P_TAURAD * B + b]);
+      mc[MC_RAWM * B + b] = (T)(al * wa);
+      mc[MC_RAWN * B + b] = (T)(al * (1.0 - wa));
+      mc[MC_PB * B + b] = (T)Pb;
     }
   }
 }

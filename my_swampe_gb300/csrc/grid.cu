@@ -336,7 +336,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
   // per-member scalars, formed once per CTA by thread 0 (FP64 parameters in,
   // compute type out) and shared: FP64 arithmetic replicated over all 256
   // threads of every CTA would load GB300's small FP64 pipe
-  __shared__ T s_par[6];     // Phibar, 1/taurad, 1/taudrag, DPhieq, w_curr, w_mid
+  __shared__ T s_par[7];     // Phibar, 1/taurad, 1/taudrag, DPhieq, w_curr, w_mid, w_winds
   __shared__ int s_flag[2];  // no drag (taudrag == -1), member blown up
   if (threadIdx.x == 0) {
     const double Pb = G.par[P_PHIBAR * B + b], tr = G.par[P_TAURAD * B + b];
@@ -345,6 +345,10 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     const double wm = G.member ? G.member[MS_WMID * B + b] : 0.0;
     s_par[0] = (T)Pb; s_par[1] = (T)(1.0 / tr); s_par[2] = (T)(1.0 / td); s_par[3] = (T)DPe;
     s_par[4] = (T)wc; s_par[5] = (T)wm;
+    // the winds of a stepped member are band-limited (the RAW filter leaves
+    // them alone while it moves eta, delta, Phi of the new level)
+    const bool stepped = G.member && G.member[MS_UPDATED * B + b] != 0.0;
+    s_par[6] = stepped ? (T)0 : (T)wc;
     s_flag[0] = td == -1.0;
     s_flag[1] = (cfg.diagnostics && G.member) ? (G.member[MS_DEAD * B + b] != 0.0) : 0;
   }
@@ -358,7 +362,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
 
   if (MODE == GM_STEP || MODE == GM_OUTPUT || MODE == GM_WINDS) {
     // ------------------------------------------------ Fourier -> physical
-    const T wcur = s_par[4], wmid = s_par[5];
+    const T wcur = s_par[4], wmid = s_par[5], wuv = s_par[6];
     const bool dead = s_flag[1] != 0;
     int fl[8], nf = 0;
     if (MODE == GM_STEP) {
@@ -389,7 +393,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
         else if (fld == F_U) rf = R_U;
         else if (fld == F_V) rf = R_V;
         T w = (fld == F_ETA_MID || fld == F_DELTA_MID || fld == F_PHI_MID) ? wmid : wcur;
-        if ((fld == F_U || fld == F_V) && cfg.test == 1) w = (T)1;  // fixed initial winds (model.py:979-983)
+        if (fld == F_U || fld == F_V) w = cfg.test == 1 ? (T)1 : wuv;  // test 1: fixed initial winds (model.py:979-983)
         if (rf >= 0 && G.resid && w != (T)0) { wv[f] = w; rfv[f] = rf; }
       }
     }

@@ -26,19 +26,22 @@ template <typename T2, typename T>
 __device__ __forceinline__ T2 imul(T m, T2 z) { T2 r; r.x = -m * z.y; r.y = m * z.x; return r; }
 
 // Per-(member, n) spectral coefficients of a CTA's tile from the call's tables
-// into shared memory; without hyperdiffusion sigma = 1, sigma - 1 = 0.
+// into shared memory; without hyperdiffusion sigma = 1, sigma - 1 = 0.  `expo`
+// selects the exponential sigmas of the semi-implicit scheme.
 template <typename T>
 __device__ __forceinline__ void load_spec_coefs(const SpecGroup<T>& G, bool diff, int m, int b0, int mt, int MT,
-                                                int cnt, int cntmax, T* sig, T* sigP, T* sigm1, T* sigPm1, T* tcmn) {
+                                                int cnt, int cntmax, T* sig, T* sigP, T* sigm1, T* sigPm1, T* tcmn,
+                                                bool expo = false) {
   const size_t qs = (size_t)G.B * cntmax;
+  const int rs = expo ? NC_SIGX : NC_SIG, rp = expo ? NC_SIGPX : NC_SIGP;
   for (int t = threadIdx.x; t < MT * cnt; t += blockDim.x) {
     const int bt = t / cnt, k = t % cnt, n = m + k;
     T s = (T)1, sp = (T)1, sm1 = (T)0, spm1 = (T)0, tc = (T)0;
     if (bt < mt) {
       const size_t o = (size_t)(b0 + bt) * cntmax + n;
       if (diff) {
-        s = G.nco[NC_SIG * qs + o];
-        sp = G.nco[NC_SIGP * qs + o];
+        s = G.nco[rs * qs + o];
+        sp = G.nco[rp * qs + o];
         sm1 = G.nco[NC_SIGM1 * qs + o];
         spm1 = G.nco[NC_SIGPM1 * qs + o];
       }
@@ -107,6 +110,51 @@ __device__ __forceinline__ void step_combos_ld(const SpecGroup<T>& G, const Step
     c[SP_E1] = incr ? cscale(imul(xm, Aeff), -te) : csub(eta, cscale(imul(xm, Aeff), te));
     c[NSPX + SH_E1] = cscale(Beff, te);
     if (incr) { c[SP_IPHI] = phi; c[SP_ID] = del; c[SP_IE] = eta; }
+  } else if (cfg.scheme == 2) {
+    // semi-implicit leapfrog (semi_implicit_tdiff.py si_timestep): explicit
+    // parts of eta*, delta*, Phi* on the n-1 base (the filtered lineage);
+    // SP_D2 carries the terms applied with n(n+1)/a^2, the rest factor 1.
+    // The per-degree implicit solve is the spectral kernel's epilogue.
+    T2 eta0 = ld(F_ETA_MID), del0 = ld(F_DELTA_MID), phi0 = ld(F_PHI_MID);
+    T2 A = ld(F_A), Bm = ld(F_B), C = ld(F_C), D = ld(F_D), E = ld(F_E);
+    const T ex = mc[MC_SIEX * B + b];
+    const T itd = cfg.si_relax ? mc[MC_SIITD * B + b] : (T)0;
+    const T itr = cfg.si_relax ? mc[MC_SIITR * B + b] : (T)0;
+    const T gd = ex * itd, gr = ex * itr, tdt = mc[MC_2DT * B + b];
+    T2 Aeff = A, Beff = Bm, PFx = mk<T2>(0, 0);
+    if (cfg.forcflag) {
+      T2 Fx, Gx;
+      if (cfg.si_relax) {
+        // lagged remainder Fm + Um / taudrag of the previous step; on the first
+        // step the state's own (model.py:737-739)
+        if (cfg.si_lag_init) {
+          Fx = cadd(ld(F_F), cscale(ld(F_U), itd));
+          Gx = cadd(ld(F_G), cscale(ld(F_V), itd));
+        } else {
+          Fx = ld(F_RU_LAG);
+          Gx = ld(F_RV_LAG);
+        }
+        PFx = cadd(ld(F_PHIF), cscale(ld(F_PHI), itr));
+      } else {
+        Fx = ld(F_F);
+        Gx = ld(F_G);
+        PFx = ld(F_PHIF);
+      }
+      Aeff = csub(A, Gx);
+      Beff = cadd(Bm, Fx);
+    }
+    T2 e1 = csub(cscale(eta0, (T)1 - gd), cscale(imul(xm, Aeff), tsc));
+    T2 d1 = cadd(cscale(del0, (T)1 - gd), cscale(imul(xm, Beff), tsc));
+    T2 p1 = csub(cscale(phi0, (T)1 - gr), cscale(imul(xm, C), tsc));
+    p1 = csub(p1, cscale(del0, ex * mc[MC_PB * B + b]));
+    if (cfg.forcflag) p1 = cadd(p1, cscale(PFx, tdt));
+    c[SP_E1] = e1;
+    c[SP_D1] = d1;
+    c[SP_PHI1] = p1;
+    c[SP_D2] = cscale(cadd(cscale(E, tdt), cscale(phi0, ex)), mc[MC_IA2 * B + b]);
+    c[NSPX + SH_E1] = cscale(Beff, tsc);
+    c[NSPX + SH_D1] = cscale(Aeff, tsc);
+    c[NSPX + SH_PHI1] = cscale(D, tsc);
   } else {
     T2 eta0 = ld(F_ETA_PREV), del0 = ld(F_DELTA_PREV), phi0 = ld(F_PHI_PREV);
     T2 del1 = ld(F_DELTA);
@@ -155,13 +203,19 @@ __device__ __forceinline__ void step_combos(const SpecGroup<T>& G, const StepCfg
 
 // Write-out of one (member, latitude) point of a step at column m: the new curr
 // eta, delta, Phi (incremental form: old + increment), the prev carry, the
-// Robert-Asselin mid carry (model.py:988-1110) and the winds.  All loads come
-// before the first store: the input and output states may be one buffer, so
-// the compiler could not reorder them itself.
-// The carries the write-out of a point reads: old curr (3) and RA mid (3).
+// Robert-Asselin mid carry (model.py:988-1110) and the winds.  With the RAW
+// filter (model.py:1007-1087) the mid level moves by al * d and the new level
+// by -an * d; classic RA is al = alpha, an = 0.  The semi-implicit scheme also
+// advances its lagged momentum-forcing remainders (model.py:1135-1143).  All
+// loads come before the first store: the input and output states may be one
+// buffer, so the compiler could not reorder them itself.
+// The carries the write-out of a point reads: old curr (3), RA mid (3) and, for
+// the semi-implicit scheme, the next lagged remainders Fm + Um / taudrag,
+// Gm + Vm / taudrag of the incoming state (2).
 template <typename T>
 __device__ __forceinline__ void load_step_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
-                                                size_t o, typename cplx<T>::type* old, typename cplx<T>::type* mid) {
+                                                size_t o, typename cplx<T>::type* old, typename cplx<T>::type* mid,
+                                                typename cplx<T>::type* lag = nullptr, int b = 0) {
   typedef typename cplx<T>::type T2;
   const T2* Fi = G.four;
   const int cf[3] = {F_ETA, F_DELTA, F_PHI};
@@ -172,15 +226,21 @@ __device__ __forceinline__ void load_step_point(const SpecGroup<T>& G, const Ste
     old[q] = need_old ? Fi[cf[q] * FS + o] : mk<T2>(0, 0);
     mid[q] = cfg.ra_mode == 2 ? Fi[rf[q] * FS + o] : mk<T2>(0, 0);
   }
+  if (lag && cfg.scheme == 2) {
+    const T itd = G.mco[MC_SIITD * G.B + b];
+    lag[0] = cadd(Fi[F_F * FS + o], cscale(Fi[F_U * FS + o], itd));
+    lag[1] = cadd(Fi[F_G * FS + o], cscale(Fi[F_V * FS + o], itd));
+  }
 }
 
 // write_step_point with its carries already loaded (load_step_point)
 template <typename T>
 __device__ __forceinline__ void store_step_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
-                                                 size_t o, T al, const typename cplx<T>::type* nw_in, bool uv,
+                                                 size_t o, T al, T an, const typename cplx<T>::type* nw_in, bool uv,
                                                  typename cplx<T>::type u, typename cplx<T>::type v,
                                                  const typename cplx<T>::type* old,
-                                                 const typename cplx<T>::type* mid) {
+                                                 const typename cplx<T>::type* mid,
+                                                 const typename cplx<T>::type* lag = nullptr) {
   typedef typename cplx<T>::type T2;
   T2* Fo = G.four_out;
   const int cf[3] = {F_ETA, F_DELTA, F_PHI};
@@ -195,8 +255,13 @@ __device__ __forceinline__ void store_step_point(const SpecGroup<T>& G, const St
     else if (cfg.ra_mode == 2) {
       const T2 d = cadd(csub(mid[q], cscale(old[q], (T)2)), nw);
       Fo[rf[q] * FS + o] = cadd(old[q], cscale(d, al));
+      if (cfg.raw) nw = csub(nw, cscale(d, an));
     }
     Fo[cf[q] * FS + o] = nw;
+  }
+  if (lag && cfg.scheme == 2) {
+    Fo[F_RU_LAG * FS + o] = lag[0];
+    Fo[F_RV_LAG * FS + o] = lag[1];
   }
   if (uv) {
     Fo[F_U * FS + o] = u;
@@ -206,11 +271,35 @@ __device__ __forceinline__ void store_step_point(const SpecGroup<T>& G, const St
 
 template <typename T>
 __device__ __forceinline__ void write_step_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
-                                                 size_t o, T al, const typename cplx<T>::type* nw_in, bool uv,
+                                                 size_t o, int b, const typename cplx<T>::type* nw_in, bool uv,
                                                  typename cplx<T>::type u, typename cplx<T>::type v) {
-  typename cplx<T>::type old[3], mid[3];
-  load_step_point<T>(G, cfg, incr, FS, o, old, mid);
-  store_step_point<T>(G, cfg, incr, FS, o, al, nw_in, uv, u, v, old, mid);
+  typename cplx<T>::type old[3], mid[3], lag[2];
+  load_step_point<T>(G, cfg, incr, FS, o, old, mid, lag, b);
+  const T al = G.mco[(cfg.raw ? MC_RAWM : MC_ALPHA) * G.B + b];
+  const T an = cfg.raw ? G.mco[MC_RAWN * G.B + b] : (T)0;
+  store_step_point<T>(G, cfg, incr, FS, o, al, an, nw_in, uv, u, v, old, mid, lag);
+}
+
+// Residual weights of the initial condition in the physical curr / mid fields
+// after a step (the new level is band-limited): classic RA mid = curr + al d,
+// RAW also moves the new level by -an d (model.py:988-1087).
+__device__ __forceinline__ void step_residual_weights(const StepCfg& cfg, double al, double wa, double& wc,
+                                                      double& wm) {
+  if (cfg.ra_mode == 1) {
+    wm = wc;
+    wc = 0.0;
+  } else if (cfg.ra_mode == 2) {
+    const double dw = wm - 2.0 * wc;
+    if (cfg.raw) {
+      wm = wc + (al * wa) * dw;
+      wc = -(al * (1.0 - wa)) * dw;
+    } else {
+      wm = wc + al * dw;
+      wc = 0.0;
+    }
+  } else {
+    wc = 0.0;
+  }
 }
 
 // ----------------------------------------------------------------- adjoint

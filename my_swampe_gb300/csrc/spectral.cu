@@ -13,7 +13,8 @@
 //   spectral_transform.py:535-596 invrsUV_with_coeffs
 //   filters.py:11-27,95-151       diffusion, sigma6, sigma6Phi
 //   time_stepping.py:491-534      tstepcoeff, tstepcoeff2, tstepcoeffmn, narray, mJarray, marray
-//   model.py:988-1110             Robert-Asselin filter of the prev carry; spectral prev carry
+//   semi_implicit_tdiff.py        si_timestep (implicit gravity waves, relaxation and drag)
+//   model.py:988-1110             Robert-Asselin / RAW filters of the prev carry; spectral prev carry
 // The 19 distinct forward transforms of the reference collapse, by linearity,
 // into 9 combined inputs per member (5 on Pw, 4 on Hw), and both contractions
 // use the equatorial symmetry of the Gauss grid, Pbar(-mu) = (-1)^(n-m) Pbar(mu),
@@ -74,7 +75,8 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
   const bool incr = SlotCount<T>::INCR && cfg.incremental && mode == 0 && cfg.scheme == 0;
 
   // ---- phase 0: per-member spectral coefficients and the blow-up gate
-  load_spec_coefs<T>(G, cfg.diffflag && mode == 0, m, b0, mt, MT, cnt, cntmax, sig, sigP, sigm1, sigPm1, tcmn);
+  load_spec_coefs<T>(G, cfg.diffflag && mode == 0, m, b0, mt, MT, cnt, cntmax, sig, sigP, sigm1, sigPm1, tcmn,
+                     cfg.scheme == 2);
   if (threadIdx.x < MT) {
     int bt = threadIdx.x, dead = 0;
     if (bt < mt && cfg.diagnostics && mode == 0) {
@@ -176,6 +178,21 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
       }
       const int bt = r >> 1, comp = r & 1;
       const T om = bt < mt ? G.mco[MC_OM * G.B + b0 + bt] : (T)0;
+      // semi-implicit solve constants (semi_implicit_tdiff.py): implicit share
+      // xi, implicit drag / relaxation kd, kr, explicit drag gd, Phibar, 1/a^2
+      T si_xi = (T)0, si_kd = (T)0, si_kr = (T)0, si_gd = (T)0, si_pb = (T)0, si_ia2 = (T)0;
+      if (mode == 0 && cfg.scheme == 2 && bt < mt) {
+        const T* mc = G.mco;
+        const int b = b0 + bt, B = G.B;
+        si_xi = mc[MC_SIXI * B + b];
+        if (cfg.si_relax) {
+          si_kd = si_xi * mc[MC_SIITD * B + b];
+          si_kr = si_xi * mc[MC_SIITR * B + b];
+          si_gd = mc[MC_SIEX * B + b] * mc[MC_SIITD * B + b];
+        }
+        si_pb = mc[MC_PB * B + b];
+        si_ia2 = mc[MC_IA2 * B + b];
+      }
 #pragma unroll
       for (int k = 0; k < FWD_TC; ++k) {
         int c = c0 + k;
@@ -190,6 +207,25 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
           ceta = acc[SP_E1][k];
           cdel = acc[SP_D1][k];
           cphi = (T)0;
+          kphi = cphi; kdel = cdel; keta = ceta;
+        } else if (cfg.scheme == 2) {
+          // eta* , delta*, Phi* -> the implicit (delta, Phi) pair per degree,
+          // eliminated for delta; then the exponential hyperdiffusion
+          T seta = acc[SP_E1][k] + acc[NSPX + SH_E1][k];
+          T sdel = acc[SP_D1][k] + acc[NSPX + SH_D1][k] + nn1 * acc[SP_D2][k];
+          T sphi = acc[SP_PHI1][k] + acc[NSPX + SH_PHI1][k];
+          if (m == 0 && n == 1 && comp == 0) {  // f_{0,1}: explicit then implicit drag toward it
+            seta += si_gd * om;
+            seta += si_kd * om;
+          }
+          T bq = si_xi * (nn1 * si_ia2), cq = si_xi * si_pb;
+          T ikr = (T)1 / ((T)1 + si_kr);
+          T dnew = (sdel + bq * sphi * ikr) / (((T)1 + si_kd) + bq * cq * ikr);
+          T pnew = (sphi - cq * dnew) * ikr;
+          T enew = seta / ((T)1 + si_kd);
+          cphi = sp * pnew;
+          cdel = s * dnew;
+          ceta = s * enew;
           kphi = cphi; kdel = cdel; keta = ceta;
         } else {
           T sphi = acc[SP_PHI1][k] + acc[NSPX + SH_PHI1][k] + nn1 * acc[SP_PHI2][k];
@@ -326,17 +362,15 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
       continue;
     }
     const T2 nw[3] = {get(0), get(1), get(2)};
-    write_step_point<T>(G, cfg, incr, FS, o, G.mco[MC_ALPHA * G.B + b], nw, do_uv != 0, get(3), get(4));
+    write_step_point<T>(G, cfg, incr, FS, o, b, nw, do_uv != 0, get(3), get(4));
   }
   // residual weights of the initial condition in the physical curr / prev fields
   if (mode == 0 && m == 0 && threadIdx.x < mt && !sdead[threadIdx.x]) {
     int b = b0 + threadIdx.x;
     double wc = G.member[MS_WCURR * G.B + b], wm = G.member[MS_WMID * G.B + b];
-    double al = G.par[P_ALPHA * G.B + b];
-    if (cfg.ra_mode == 1) wm = wc;
-    else if (cfg.ra_mode == 2) wm = wc + al * (wm - 2.0 * wc);
+    step_residual_weights(cfg, G.par[P_ALPHA * G.B + b], G.par[P_WALPHA * G.B + b], wc, wm);
     G.member[MS_WMID * G.B + b] = wm;
-    G.member[MS_WCURR * G.B + b] = 0.0;
+    G.member[MS_WCURR * G.B + b] = wc;
     G.member[MS_UPDATED * G.B + b] = 1.0;
   }
 }

@@ -14,6 +14,8 @@ namespace swp {
 // ---------------------------------------------------------------- params ---
 enum ParamIndex {
   P_DT = 0, P_A, P_OMEGA, P_PHIBAR, P_TAURAD, P_TAUDRAG, P_DPHIEQ, P_K6, P_K6PHI, P_ALPHA,
+  P_SIALPHA,  // implicit weight of the semi-implicit scheme (RunFlags.si_alpha)
+  P_WALPHA,   // Williams weight of the RAW filter (RunFlags.williams_alpha)
   NPAR
 };
 
@@ -23,6 +25,11 @@ enum FourierField {
   F_A, F_B, F_C, F_D, F_E, F_PHIF, F_F, F_G, F_ETA_MID, F_DELTA_MID, F_PHI_MID,
   NFOURIER
 };
+// The semi-implicit scheme reads the filtered lineage (*_MID) as its n-1 base
+// and never the unfiltered prev carries; their slots hold its lagged
+// momentum-forcing remainders (model.py:775-792, 1135-1143).
+constexpr int F_RU_LAG = F_ETA_PREV;
+constexpr int F_RV_LAG = F_DELTA_PREV;
 
 // Physical residual fields (initial condition minus its band-limited part).
 enum ResidualField { R_ETA = 0, R_DELTA, R_PHI, R_U, R_V, NRESID };
@@ -287,7 +294,7 @@ struct Geom {
 
 // Step configuration shared by a launch.
 struct StepCfg {
-  int scheme;      // 0 = modified Euler, 1 = explicit
+  int scheme;      // 0 = modified Euler, 1 = explicit, 2 = semi-implicit
   int forcflag;
   int diffflag;
   int test;        // 0 = forced (test None), 1, 2
@@ -298,6 +305,9 @@ struct StepCfg {
   int step;        // scan-step index (row of the diagnostic arrays)
   int incremental; // advance a band-limited state by increments (FP32 path)
   int lam_fg_tied; // adjoint sweep: lambda_F = lambda_B, lambda_G = -lambda_A hold (forced)
+  int raw;         // Robert-Asselin-Williams filter: the new level moves too
+  int si_relax;    // semi-implicit: relaxation and drag implicit (forcflag, test None)
+  int si_lag_init; // semi-implicit first step: lagged remainder from the current state
 };
 
 }  // namespace swp

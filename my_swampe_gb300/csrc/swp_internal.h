@@ -70,10 +70,12 @@ constexpr int MAXG = 4;
 // call in FP64 with the reference's expressions and stored in the compute
 // type, so that the step kernels do no FP64 arithmetic of their own.
 //   nco[q][b][n]   q: hyperdiffusion sigma, sigmaPhi, sigma - 1, sigmaPhi - 1
-//                     (filters.py:95-151), a / (n(n+1)) (spectral_transform.py:577)
+//                     (filters.py:95-151), a / (n(n+1)) (spectral_transform.py:577),
+//                     the exponential sigma, sigmaPhi of the semi-implicit scheme
+//                     (filters.py:154-213)
 //   jco[b][j]      tstepcoeff = 2 dt / (a (1 - mu_j^2)) (time_stepping.py:491-500)
 //   mco[q][b]      scalar factors of the tendencies (modEuler_tdiff.py, explicit_tdiff.py)
-enum NCoef { NC_SIG = 0, NC_SIGP, NC_SIGM1, NC_SIGPM1, NC_TC, NNCO };
+enum NCoef { NC_SIG = 0, NC_SIGP, NC_SIGM1, NC_SIGPM1, NC_TC, NC_SIGX, NC_SIGPX, NNCO };
 enum MCoef {
   MC_DT = 0,   // dt
   MC_T2,       // (2 dt / a^2) / 4
@@ -87,6 +89,13 @@ enum MCoef {
   MC_ITD,      // 1 / taudrag
   MC_OM,       // omega / sqrt(0.375)  (the planetary-vorticity part of eta_{0,1})
   MC_ALPHA,    // Robert-Asselin alpha
+  MC_SIXI,     // 2 dt si_alpha            (implicit share of the semi-implicit step)
+  MC_SIEX,     // 2 dt (1 - si_alpha)      (explicit share)
+  MC_SIITD,    // 1 / taudrag, 0 for the taudrag = -1 sentinel
+  MC_SIITR,    // 1 / taurad
+  MC_RAWM,     // alpha williams_alpha       (RAW: displacement of the mid level)
+  MC_RAWN,     // alpha (1 - williams_alpha) (RAW: displacement of the new level)
+  MC_PB,       // Phibar
   NMCO
 };
 template <typename T>

@@ -481,17 +481,17 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       const size_t o = ((size_t)m * G.B + b) * J + j;
       auto get = [&](int f) { return *(const float2*)&Out[(size_t)(f * TC_MT + bti) * TC_OST + 2 * j]; };
       const T2 nw[3] = {get(0), get(1), get(2)};
-      store_step_point<T>(G, cfg, incr, FS, o, G.mco[MC_ALPHA * G.B + b], nw, cfg.test != 1, cadd(get(3), get(5)),
+      const T al = G.mco[(cfg.raw ? MC_RAWM : MC_ALPHA) * G.B + b];
+      const T an = cfg.raw ? G.mco[MC_RAWN * G.B + b] : (T)0;
+      store_step_point<T>(G, cfg, incr, FS, o, al, an, nw, cfg.test != 1, cadd(get(3), get(5)),
                           cadd(get(4), get(6)), pold[u], pmid[u]);
     }
     if (m == 0 && threadIdx.x < mt && !sdead[threadIdx.x]) {
       const int b = b0 + threadIdx.x;
       double wc = G.member[MS_WCURR * G.B + b], wm = G.member[MS_WMID * G.B + b];
-      const double al = G.par[P_ALPHA * G.B + b];
-      if (cfg.ra_mode == 1) wm = wc;
-      else if (cfg.ra_mode == 2) wm = wc + al * (wm - 2.0 * wc);
+      step_residual_weights(cfg, G.par[P_ALPHA * G.B + b], G.par[P_WALPHA * G.B + b], wc, wm);
       G.member[MS_WMID * G.B + b] = wm;
-      G.member[MS_WCURR * G.B + b] = 0.0;
+      G.member[MS_WCURR * G.B + b] = wc;
       G.member[MS_UPDATED * G.B + b] = 1.0;
     }
   } else {

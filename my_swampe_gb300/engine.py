@@ -26,7 +26,8 @@ from . import _lib
 
 PRECISIONS = {"fp64": _lib.SWP_FP64, "fast": _lib.SWP_FAST}
 
-PARAM_NAMES = ("dt", "a", "omega", "Phibar", "taurad", "taudrag", "DPhieq", "K6", "K6Phi", "alpha")
+PARAM_NAMES = ("dt", "a", "omega", "Phibar", "taurad", "taudrag", "DPhieq", "K6", "K6Phi", "alpha",
+               "si_alpha", "williams_alpha")
 
 # member tiles chosen by Engine.autotune, per (precision, ((M, B), ...))
 _TUNED: Dict[Tuple, List[int]] = {}
@@ -36,7 +37,7 @@ _TUNED: Dict[Tuple, List[int]] = {}
 class RunFlagsC:
     """Scheme switches passed to the kernels (model.py RunFlags, :156-226)."""
 
-    scheme: int = 0
+    scheme: int = 0          # 0 modified Euler, 1 explicit, 2 semi-implicit
     forcflag: bool = True
     diffflag: bool = True
     modalflag: bool = True
@@ -44,12 +45,13 @@ class RunFlagsC:
     diagnostics: bool = False
     blowup_rms: float = 8000.0
     t_start: int = 2
+    raw_filter: bool = False
 
     def c(self) -> _lib.Flags:
         return _lib.Flags(
             int(self.scheme), int(bool(self.forcflag)), int(bool(self.diffflag)), int(bool(self.modalflag)),
             0 if self.test is None else int(self.test), int(bool(self.diagnostics)), float(self.blowup_rms),
-            int(self.t_start),
+            int(self.t_start), int(bool(self.raw_filter)),
         )
 
 
@@ -102,6 +104,8 @@ class Engine:
             gd["fourier"] = torch.zeros((_lib.NFOURIER, gd["M"] + 1, gd["B"], gd["J"]), dtype=self.cdtype, device=dev)
             gd["resid"] = torch.zeros((_lib.NRESID, gd["B"], gd["J"], gd["I"]), dtype=self.rdtype, device=dev)
             gd["params"] = torch.zeros((_lib.NPAR, gd["B"]), dtype=torch.float64, device=dev)
+            gd["params"][_lib.P_SIALPHA] = 0.5   # RunFlags defaults (model.py:186-187)
+            gd["params"][_lib.P_WALPHA] = 0.53
             gd["member"] = torch.zeros((_lib.NMEMBER, gd["B"]), dtype=torch.float64, device=dev)
             self.groups.append(gd)
         self._geo_cache: Dict[int, Dict[str, torch.Tensor]] = {}

@@ -311,8 +311,10 @@ def run_model_scan(
     reference (``model.py:1345-1765``); ``remat_step``, ``jit_scan`` and
     ``donate_state`` are accepted for compatibility and have no effect (the
     scan body is always a compiled kernel pair and the state is updated in
-    place).  The opt-in semi-implicit scheme and RAW filter are not part of
-    this time-stepping core and raise ``NotImplementedError``.
+    place).  ``semi_implicit`` selects the semi-implicit leapfrog
+    (``semi_implicit_tdiff.py``) and ``raw_filter`` the Robert-Asselin-Williams
+    filter (``model.py:1007-1087``); both run forward only (the hand-written
+    adjoint covers the modified-Euler scheme with the classic filter).
     """
     if tmax < 2:
         raise ValueError("tmax must be >= 2 (SWAMPE uses a 2-level initialization).")
@@ -327,8 +329,6 @@ def run_model_scan(
             "raw_filter=True is incompatible with expflag=True (the explicit scheme reads the "
             "unfiltered spectral prev carry, so the RAW lineage change would alter its parity behavior)."
         )
-    if semi_implicit or raw_filter:
-        raise NotImplementedError("semi_implicit and raw_filter are opt-in schemes outside this time-stepping core")
     if test not in (None, 1, 2):
         raise NotImplementedError(f"test={test} is not implemented (use None, 1 or 2)")
     M = int(M)
@@ -361,7 +361,8 @@ def run_model_scan(
     if have_ic and ((U0_init is None) != (V0_init is None)):
         raise ValueError("Provide both U0_init and V0_init, or neither.")
 
-    Bm = _member_count(dt, a, omega, Phibar, taurad, taudrag, DPhieq, K6, K6Phi, alpha)
+    Bm = _member_count(dt, a, omega, Phibar, taurad, taudrag, DPhieq, K6, K6Phi, alpha,
+                       si_alpha if semi_implicit else None, williams_alpha if raw_filter else None)
     for x in (eta0_init, delta0_init, Phi0_init, U0_init, V0_init):
         if x is not None and torch.as_tensor(x).dim() == 3:
             b = torch.as_tensor(x).shape[0]
@@ -383,7 +384,8 @@ def run_model_scan(
     dev = eng.device
     K6Phi_eff = K6 if K6Phi is None else K6Phi
     eng.set_params(0, dt=dt, a=a, omega=omega, Phibar=Phibar, taurad=taurad, taudrag=taudrag,
-                   DPhieq=DPhieq if test is None else 0.0, K6=K6, K6Phi=K6Phi_eff, alpha=alpha)
+                   DPhieq=DPhieq if test is None else 0.0, K6=K6, K6Phi=K6Phi_eff, alpha=alpha,
+                   si_alpha=si_alpha, williams_alpha=williams_alpha)
     static = build_static(M=M, dt=dt, a=a, omega=omega, g=g, Phibar=Phibar, taurad=taurad, taudrag=taudrag,
                           DPhieq=DPhieq, K6=K6, K6Phi=K6Phi, test=test, engine=eng)
 
@@ -414,8 +416,9 @@ def run_model_scan(
         eta0, delta0, Phi0 = fields
         U0, V0 = eng.diagnose_winds([torch.stack((eta0, delta0), 0).to(eng.rdtype)])[0].to(torch.float64)
 
-    flags = RunFlagsC(scheme=1 if expflag else 0, forcflag=forcflag, diffflag=diffflag, modalflag=modalflag,
-                      test=test, diagnostics=diagnostics, blowup_rms=8000.0, t_start=starttime_eff)
+    flags = RunFlagsC(scheme=2 if semi_implicit else (1 if expflag else 0), forcflag=forcflag, diffflag=diffflag,
+                      modalflag=modalflag, test=test, diagnostics=diagnostics, blowup_rms=8000.0,
+                      t_start=starttime_eff, raw_filter=bool(raw_filter))
     T = tmax - starttime_eff
     diag = eng.new_diag(T) if diagnostics else None
     gd = eng.groups[0]
@@ -432,7 +435,11 @@ def run_model_scan(
         eng.forward(flags, t0=starttime_eff, nsteps=T, row0=0, diag=diag, hist=hist, write_prev_last=True)
     phys = eng.output_physical(flags)[0]
     eng.check_device_status()
-    last = _assemble_state(eng, phys, Rum, Rvm, batched)
+    if semi_implicit and T > 0:  # the lagged remainders the steps advanced
+        Rum, Rvm = four[_lib.F_RU_LAG].clone(), four[_lib.F_RV_LAG].clone()
+    # the Fourier prev carry follows the filtered lineage with the semi-implicit
+    # scheme or the RAW filter, the unfiltered curr otherwise (model.py:1089-1110)
+    last = _assemble_state(eng, phys, Rum, Rvm, batched, filtered_prev=bool(semi_implicit or raw_filter))
     res: Dict[str, Any] = dict(static=static, t_seq=torch.arange(starttime_eff, tmax, dtype=torch.int32, device=dev),
                                last_state=last, starttime=starttime_eff)
     if return_history:
@@ -455,7 +462,7 @@ def run_model_scan(
     return res
 
 
-def _assemble_state(eng: Engine, phys: torch.Tensor, Rum, Rvm, batched: bool) -> State:
+def _assemble_state(eng: Engine, phys: torch.Tensor, Rum, Rvm, batched: bool, filtered_prev: bool = False) -> State:
     gd = eng.groups[0]
     four = gd["fourier"]
 
@@ -471,9 +478,13 @@ def _assemble_state(eng: Engine, phys: torch.Tensor, Rum, Rvm, batched: bool) ->
         return phys[k] if batched else phys[k, 0]
 
     dead = gd["member"][_lib.MS_DEAD] != 0
+    if filtered_prev:
+        pe, pd, pp = _lib.F_ETA_MID, _lib.F_DELTA_MID, _lib.F_PHI_MID
+    else:
+        pe, pd, pp = _lib.F_ETA_PREV, _lib.F_DELTA_PREV, _lib.F_PHI_PREV
     return State(
-        etam_prev=fo(_lib.F_ETA_PREV), etam_curr=fo(_lib.F_ETA), deltam_prev=fo(_lib.F_DELTA_PREV),
-        deltam_curr=fo(_lib.F_DELTA), Phim_prev=fo(_lib.F_PHI_PREV), Phim_curr=fo(_lib.F_PHI),
+        etam_prev=fo(pe), etam_curr=fo(_lib.F_ETA), deltam_prev=fo(pd),
+        deltam_curr=fo(_lib.F_DELTA), Phim_prev=fo(pp), Phim_curr=fo(_lib.F_PHI),
         eta_prev=ph(5), eta_curr=ph(0), delta_prev=ph(6), delta_curr=ph(1), Phi_prev=ph(7), Phi_curr=ph(2),
         U_curr=ph(3), V_curr=ph(4), Um_curr=fo(_lib.F_U), Vm_curr=fo(_lib.F_V), Am_curr=fo(_lib.F_A),
         Bm_curr=fo(_lib.F_B), Cm_curr=fo(_lib.F_C), Dm_curr=fo(_lib.F_D), Em_curr=fo(_lib.F_E),

@@ -65,6 +65,12 @@ class _NumpyBackend:
     def sqrt(self, x):
         return np.sqrt(x)
 
+    def exp(self, x):
+        return np.exp(x)
+
+    def clamp0(self, x):
+        return np.maximum(x, 0.0)
+
     def abs(self, x):
         return np.abs(x)
 
@@ -135,6 +141,12 @@ class _TorchBackend(_NumpyBackend):
 
     def sqrt(self, x):
         return self.t.sqrt(x) if isinstance(x, self.t.Tensor) else math.sqrt(x)
+
+    def exp(self, x):
+        return self.t.exp(x)
+
+    def clamp0(self, x):
+        return self.t.clamp_min(x, 0.0)
 
     def abs(self, x):
         return self.t.abs(x)
@@ -387,6 +399,21 @@ def sigma6Phi(xp, N, K6, a, dt):
     return 1 / (1 + 2 * dt * K6 * ncoeff)
 
 
+def sigma6_exponential(xp, N, K6, a, dt):
+    """Integrating-factor hyperdiffusion of eta, delta for the semi-implicit
+    scheme, clamped at zero below n = 1.  ``filters.py:154-185``."""
+    n = xp.asarray(np.arange(N + 1, dtype=np.float64))
+    ncoeff = ((n * n * n) / a**3) * (((n + 1) * (n + 1) * (n + 1)) / a**3)
+    return xp.exp(-(2 * dt * K6) * xp.clamp0(ncoeff - 8 / a**6))
+
+
+def sigma6Phi_exponential(xp, N, K6, a, dt):
+    """Same without the ``8/a^6`` offset.  ``filters.py:188-213``."""
+    n = xp.asarray(np.arange(N + 1, dtype=np.float64))
+    ncoeff = ((n * n * n) / a**3) * (((n + 1) * (n + 1) * (n + 1)) / a**3)
+    return xp.exp(-(2 * dt * K6) * ncoeff)
+
+
 def ABCDE(xp, U, V, eta, Phi, mus):
     """``initial_conditions.py:242-292``."""
     mu = np.asarray(mus)[:, None]
@@ -427,6 +454,8 @@ class Static:
     narray: Any
     sigma: Any
     sigmaPhi: Any
+    sigma_exp: Any
+    sigmaPhi_exp: Any
     Phieq: Any
 
 
@@ -459,6 +488,8 @@ def build_static(xp, *, M, dt, a, omega, g, Phibar, taurad, taudrag, DPhieq, K6,
     K6Phi_eff = K6 if K6Phi is None else K6Phi
     sig = sigma6(xp, N, K6, a, dt)
     sigP = sigma6Phi(xp, N, K6Phi_eff, a, dt)
+    sigX = sigma6_exponential(xp, N, K6, a, dt)          # model.py:517-518
+    sigPX = sigma6Phi_exponential(xp, N, K6Phi_eff, a, dt)
     if test is None:
         Phieq = Phieqfun(xp, Phibar, DPhieq, geo["lambdas"], mus)
     else:
@@ -468,7 +499,7 @@ def build_static(xp, *, M, dt, a, omega, g, Phibar, taurad, taudrag, DPhieq, K6,
         taudrag=taudrag, DPhieq=DPhieq, lambdas=geo["lambdas"], mus=mus, w=w, Pmn=Pmn, Hmn=Hmn,
         Pmnw=Pmnw, Hmnw=Hmnw, fmn=fmn, tstepcoeff=tstepcoeff, tstepcoeff2=tstepcoeff2,
         tstepcoeffmn=tstepcoeffmn, marray=marray, mJarray=mJarray, narray=narray, sigma=sig,
-        sigmaPhi=sigP, Phieq=Phieq,
+        sigmaPhi=sigP, sigma_exp=sigX, sigmaPhi_exp=sigPX, Phieq=Phieq,
     )
 
 
@@ -590,6 +621,66 @@ def explicit_eta(xp, s: Static, X, forcflag, diffflag):
     return out
 
 
+def _inv_taudrag(xp, taudrag):
+    """``1/taudrag`` with the ``taudrag == -1`` "no drag" sentinel mapped to 0
+    (``model.py:775-792``, ``semi_implicit_tdiff.py`` relax branch)."""
+    no_drag = _is_minus_one(taudrag)
+    if isinstance(no_drag, bool):
+        return 0.0 if no_drag else 1.0 / taudrag
+    return xp.where(no_drag, 0.0, 1.0 / xp.where(no_drag, 1.0, taudrag))
+
+
+def semi_implicit_step(xp, s: Static, X, forcflag, diffflag, relax, si_alpha, Rum_lag, Rvm_lag):
+    """Semi-implicit leapfrog: gravity waves (and, when ``relax``, Newtonian
+    relaxation and Rayleigh drag) weighted by ``si_alpha`` at the new level,
+    the rest explicit, then the exponential hyperdiffusion.  Returns the new
+    spectral (eta, delta, Phi).  ``semi_implicit_tdiff.py`` si_timestep
+    (dispatch ``time_stepping.py:387-488``, ``model.py:871-918``).
+
+    ``X["etam0"]`` etc. are the n-1 base: the Robert-Asselin-filtered Fourier
+    lineage (``model.py:1089-1106``)."""
+    two_dt = 2.0 * s.dt
+    if relax:
+        itd = _inv_taudrag(xp, s.taudrag)
+        itr = 1.0 / s.taurad
+        Fx, Gx = Rum_lag, Rvm_lag
+        PhiFx = X["PhiFm"] + X["Phim1"] * itr
+    else:
+        itd = itr = 0.0
+        Fx, Gx, PhiFx = X["Fm"], X["Gm"], X["PhiFm"]
+    Aeff = X["Am"] - Gx if forcflag else X["Am"]
+    Beff = X["Bm"] + Fx if forcflag else X["Bm"]
+    tc, mJ = s.tstepcoeff, s.mJarray
+    eta0 = fwd_leg_w(xp, X["etam0"], s.Pmnw)
+    del0 = fwd_leg_w(xp, X["deltam0"], s.Pmnw)
+    phi0 = fwd_leg_w(xp, X["Phim0"], s.Pmnw)
+    iA = fwd_leg_w(xp, tc * (1j) * mJ * Aeff, s.Pmnw)
+    iB = fwd_leg_w(xp, tc * (1j) * mJ * Beff, s.Pmnw)
+    iC = fwd_leg_w(xp, tc * (1j) * mJ * X["Cm"], s.Pmnw)
+    Emn = fwd_leg_w(xp, X["Em"], s.Pmnw)
+    hA = fwd_leg_w(xp, tc * Aeff, s.Hmnw)
+    hB = fwd_leg_w(xp, tc * Beff, s.Hmnw)
+    hD = fwd_leg_w(xp, tc * X["Dm"], s.Hmnw)
+    lam = s.narray / (s.a**2)  # -del^2 eigenvalue n(n+1)/a^2
+    xi = two_dt * si_alpha
+    ex = two_dt * (1.0 - si_alpha)
+    kd, kr = xi * itd, xi * itr
+    gd, gr = ex * itd, ex * itr
+    eta_s = eta0 - iA + hB - gd * (eta0 - s.fmn)
+    delta_s = del0 + iB + hA + two_dt * lam * Emn + ex * lam * phi0 - gd * del0
+    phi_s = phi0 - iC + hD - ex * s.Phibar * del0 - gr * phi0
+    if forcflag:
+        phi_s = phi_s + fwd_leg_w(xp, two_dt * PhiFx, s.Pmnw)
+    # the 2x2 (delta, Phi) system per degree, eliminated for delta
+    eta_n = (eta_s + kd * s.fmn) / (1.0 + kd)
+    bq, cq = xi * lam, xi * s.Phibar
+    delta_n = (delta_s + bq * phi_s / (1.0 + kr)) / ((1.0 + kd) + bq * cq / (1.0 + kr))
+    phi_n = (phi_s - cq * delta_n) / (1.0 + kr)
+    if diffflag:
+        eta_n, delta_n, phi_n = eta_n * s.sigma_exp, delta_n * s.sigma_exp, phi_n * s.sigmaPhi_exp
+    return eta_n, delta_n, phi_n
+
+
 # --------------------------------------------------------------------------
 # state
 # --------------------------------------------------------------------------
@@ -613,6 +704,10 @@ class Flags:
     diagnostics: bool = True
     alpha: Any = 0.01
     blowup_rms: float = 8000.0
+    semi_implicit: bool = False
+    raw_filter: bool = False
+    williams_alpha: Any = 0.53
+    si_alpha: Any = 0.5
 
 
 def forcing_phys(xp, s: Static, test, Phi, U, V):
@@ -684,10 +779,7 @@ def init_state(xp, s: Static, test, eta0, delta0, Phi0, U0, V0):
     PhiFm0, Fm0, Gm0 = (fwd_fft_trunc(xp, f, s.I, s.M) for f in (PhiF0, F0, G0))
     Am0, Bm0, Cm0, Dm0, Em0 = nonlinear_spectral(xp, s, eta0, Phi0, U0, V0)
     # _momentum_forcing_remainder (model.py:775-792)
-    if _is_minus_one(s.taudrag) is True:
-        inv_td = 0.0
-    else:
-        inv_td = 1.0 / s.taudrag
+    inv_td = _inv_taudrag(xp, s.taudrag)
     Rum0 = Fm0 + Um0 * inv_td
     Rvm0 = Gm0 + Vm0 * inv_td
     return dict(
@@ -713,9 +805,12 @@ def rms_winds(xp, s: Static, U, V):
 
 
 def step_once(xp, state, t, s: Static, flags: Flags, test, Uic, Vic):
-    """One step of the scan body.  ``model.py:795-1194`` (modEuler / explicit,
-    classic RA filter on the physical prev carry only, spectral prev carry =
-    unfiltered curr ``:1107-1110``)."""
+    """One step of the scan body.  ``model.py:795-1194``: modEuler, explicit or
+    semi-implicit tendency; classic RA filter on the physical prev carry, or
+    the RAW filter (``:1007-1087``) on both the physical and the Fourier
+    lineage.  The Fourier prev carry is the unfiltered curr (``:1107-1110``)
+    for classic RA without the semi-implicit scheme, the filtered Fourier
+    lineage otherwise (``:1089-1106``)."""
     X = dict(
         etam0=state["etam_prev"], etam1=state["etam_curr"], deltam0=state["deltam_prev"],
         deltam1=state["deltam_curr"], Phim0=state["Phim_prev"], Phim1=state["Phim_curr"],
@@ -731,7 +826,11 @@ def step_once(xp, state, t, s: Static, flags: Flags, test, Uic, Vic):
         rms = spin_min = 0.0
         dead_next = state["dead"]
 
-    if flags.expflag:
+    if flags.semi_implicit:
+        etamn, deltamn, Phimn = semi_implicit_step(
+            xp, s, X, flags.forcflag, flags.diffflag, bool(flags.forcflag) and test is None, flags.si_alpha,
+            state["Rum_lag"], state["Rvm_lag"])
+    elif flags.expflag:
         Phimn = explicit_phi(xp, s, X, flags.forcflag, flags.diffflag)
         deltamn = explicit_delta(xp, s, X, flags.forcflag, flags.diffflag)
         etamn = explicit_eta(xp, s, X, flags.forcflag, flags.diffflag)
@@ -752,24 +851,58 @@ def step_once(xp, state, t, s: Static, flags: Flags, test, Uic, Vic):
 
     do_ra = bool(flags.modalflag) and int(t) > 2
     al = flags.alpha
-    if do_ra:
-        eta_mid = state["eta_curr"] + al * (state["eta_prev"] - 2.0 * state["eta_curr"] + neweta)
-        delta_mid = state["delta_curr"] + al * (state["delta_prev"] - 2.0 * state["delta_curr"] + newdelta)
-        Phi_mid = state["Phi_curr"] + al * (state["Phi_prev"] - 2.0 * state["Phi_curr"] + newPhi)
-    else:
-        eta_mid, delta_mid, Phi_mid = state["eta_curr"], state["delta_curr"], state["Phi_curr"]
+    # filter weights: classic RA moves the mid level by al * d; RAW (Williams
+    # 2009) moves it by al * w * d and the new level by -al * (1 - w) * d
+    wa = flags.williams_alpha if flags.raw_filter else 1.0
+    lev = (("eta", neweta, "etam", newetam), ("delta", newdelta, "deltam", newdeltam),
+           ("Phi", newPhi, "Phim", newPhim))
+    mids, news, mmids, mnews = [], [], [], []
+    for name, nw, mname, mnw in lev:
+        prev, curr = state[name + "_prev"], state[name + "_curr"]
+        mprev, mcurr = state[mname + "_prev"], state[mname + "_curr"]
+        if do_ra:
+            d = prev - 2.0 * curr + nw
+            dm = mprev - 2.0 * mcurr + mnw
+            if flags.raw_filter:
+                mids.append(curr + al * wa * d)
+                news.append(nw - al * (1.0 - wa) * d)
+                mmids.append(mcurr + al * wa * dm)
+                mnews.append(mnw - al * (1.0 - wa) * dm)
+            else:
+                mids.append(curr + al * d)
+                news.append(nw)
+                mmids.append(mcurr + al * dm)
+                mnews.append(mnw)
+        else:
+            mids.append(curr)
+            news.append(nw)
+            mmids.append(mcurr)
+            mnews.append(mnw)
+    eta_mid, delta_mid, Phi_mid = mids
+    neweta, newdelta, newPhi = news
+    newetam, newdeltam, newPhim = mnews
+    if flags.semi_implicit or flags.raw_filter:
+        etam_mid, deltam_mid, Phim_mid = mmids
+    else:  # unfiltered Fourier prev carry of the classic path
+        etam_mid, deltam_mid, Phim_mid = state["etam_curr"], state["deltam_curr"], state["Phim_curr"]
 
     PhiF2, F2, G2 = forcing_phys(xp, s, test, newPhi, newU, newV)
     PhiFm2, Fm2, Gm2 = (fwd_fft_trunc(xp, f, s.I, s.M) for f in (PhiF2, F2, G2))
     Am2, Bm2, Cm2, Dm2, Em2 = nonlinear_spectral(xp, s, neweta, newPhi, newU, newV)
+    if flags.semi_implicit:  # lagged momentum-forcing remainder (model.py:1135-1143)
+        itd = _inv_taudrag(xp, s.taudrag)
+        Rum_n = state["Fm_curr"] + state["Um_curr"] * itd
+        Rvm_n = state["Gm_curr"] + state["Vm_curr"] * itd
+    else:
+        Rum_n, Rvm_n = state["Rum_lag"], state["Rvm_lag"]
 
     new = dict(
-        etam_prev=state["etam_curr"], etam_curr=newetam, deltam_prev=state["deltam_curr"],
-        deltam_curr=newdeltam, Phim_prev=state["Phim_curr"], Phim_curr=newPhim,
+        etam_prev=etam_mid, etam_curr=newetam, deltam_prev=deltam_mid,
+        deltam_curr=newdeltam, Phim_prev=Phim_mid, Phim_curr=newPhim,
         eta_prev=eta_mid, eta_curr=neweta, delta_prev=delta_mid, delta_curr=newdelta,
         Phi_prev=Phi_mid, Phi_curr=newPhi, U_curr=newU, V_curr=newV, Um_curr=newUm, Vm_curr=newVm,
         Am_curr=Am2, Bm_curr=Bm2, Cm_curr=Cm2, Dm_curr=Dm2, Em_curr=Em2, PhiFm_curr=PhiFm2,
-        Fm_curr=Fm2, Gm_curr=Gm2, Rum_lag=state["Rum_lag"], Rvm_lag=state["Rvm_lag"], dead=dead_next,
+        Fm_curr=Fm2, Gm_curr=Gm2, Rum_lag=Rum_n, Rvm_lag=Rvm_n, dead=dead_next,
     )
     out = dict(
         eta=neweta, delta=newdelta, Phi=newPhi, U=newU, V=newV, rms=rms, spin_min=spin_min,
@@ -797,7 +930,8 @@ def run_model_scan(xp=NUMPY, *, M, dt, tmax, Phibar, omega, a, test=None, g=9.8,
                    modalflag=True, alpha=0.01, expflag=False, K6=1.24e33, K6Phi=None,
                    starttime=None, eta0_init=None, delta0_init=None, Phi0_init=None,
                    U0_init=None, V0_init=None, diagnostics=True, return_history=True,
-                   record=None) -> Dict[str, Any]:
+                   record=None, semi_implicit=False, si_alpha=0.5, raw_filter=False,
+                   williams_alpha=0.53) -> Dict[str, Any]:
     """Driver.  ``model.py:1345-1765`` (validation, IC selection, ``t_seq = arange(starttime, tmax)``).
 
     ``record`` optionally lists history fields to keep (default: all five
@@ -807,13 +941,18 @@ def run_model_scan(xp=NUMPY, *, M, dt, tmax, Phibar, omega, a, test=None, g=9.8,
         raise ValueError("tmax must be >= 2 (SWAMPE uses a 2-level initialization).")
     if isinstance(dt, (int, float)) and float(dt) <= 0.0:
         raise ValueError("dt must be positive.")
+    if semi_implicit and expflag:  # model.py:1531-1537
+        raise ValueError("semi_implicit=True is incompatible with expflag=True (pick one scheme).")
+    if raw_filter and expflag:
+        raise ValueError("raw_filter=True is incompatible with expflag=True.")
     s = build_static(xp, M=M, dt=dt, a=a, omega=omega, g=g, Phibar=Phibar, taurad=taurad,
                      taudrag=taudrag, DPhieq=DPhieq, K6=K6, K6Phi=K6Phi, test=test)
     st0 = 2 if starttime is None else int(starttime)
     if st0 > tmax:
         raise ValueError(f"starttime={st0} must be <= tmax={tmax}.")
     flags = Flags(forcflag=forcflag, diffflag=diffflag, expflag=expflag, modalflag=modalflag,
-                  diagnostics=diagnostics, alpha=alpha)
+                  diagnostics=diagnostics, alpha=alpha, semi_implicit=bool(semi_implicit),
+                  raw_filter=bool(raw_filter), williams_alpha=williams_alpha, si_alpha=si_alpha)
     if eta0_init is not None or delta0_init is not None or Phi0_init is not None:
         if eta0_init is None or delta0_init is None or Phi0_init is None:
             raise ValueError("If providing explicit ICs, eta0_init, delta0_init, and Phi0_init must all be provided.")

@@ -4,6 +4,7 @@ product path without CUDA, continuation helpers and the per-member parameter
 rules.  All checks run before any device work."""
 import numpy as np
 import pytest
+import torch
 
 from my_swampe_gb300 import continuation
 from my_swampe_gb300.model import run_model_scan, run_model_scan_final
@@ -68,13 +69,19 @@ def test_contTime_non_numeric():
         run_model_scan(**BASE, tmax=4, contflag=True, contTime="ten")
 
 
-def test_semi_implicit_with_expflag_and_unimplemented_schemes():
+def test_semi_implicit_and_raw_reject_expflag():
+    # test_semi_implicit.py::test_semi_implicit_rejects_explicit_scheme,
+    # test_raw_filter.py::test_raw_filter_rejects_explicit_scheme
     with pytest.raises(ValueError, match="semi_implicit"):
         run_model_scan(**BASE, tmax=4, semi_implicit=True, expflag=True)
     with pytest.raises(ValueError, match="raw_filter"):
         run_model_scan(**BASE, tmax=4, raw_filter=True, expflag=True)
-    with pytest.raises(NotImplementedError):
-        run_model_scan(**BASE, tmax=4, semi_implicit=True)
+
+
+@pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU failure")
+def test_semi_implicit_has_no_cpu_fallback():
+    with pytest.raises(RuntimeError, match="CUDA"):
+        run_model_scan(**BASE, tmax=4, semi_implicit=True, raw_filter=True)
 
 
 def test_final_rejects_return_history():
