@@ -78,6 +78,13 @@ typedef struct {
   double* grad;       /* double[4][B]: d/d(taurad, taudrag, DPhieq, Phibar), accumulated */
 } swp_group_adjoint;
 
+/* Tangent-linear (forward-mode) buffers of one group. */
+typedef struct {
+  void* fourier;          /* complex[SWP_NFOURIER][M+1][B][J]: tangent of the Fourier state */
+  void* resid;            /* real[5][B][J][I]: tangent of the initial-condition residual     */
+  const double* dparams;  /* double[4][B]: tangents of taurad, taudrag, DPhieq, Phibar       */
+} swp_group_tangent;
+
 /* Flags of model.py RunFlags (model.py:156-226) plus the test selector. */
 typedef struct {
   int scheme;       /* 0 = modified Euler (default), 1 = explicit (expflag),
@@ -258,6 +265,24 @@ int swp_plan_set_tile(swp_plan* plan, int g, int mt);
  * zero: each call overwrites the part it reads. */
 int swp_adjoint_step_noalloc(swp_plan* plan, const swp_group_state* st_in, const swp_group_state* st_out,
                              const swp_group_adjoint* adj, const swp_flags* flags, int t, void* stream);
+
+/* Forward-mode derivative (tangent-linear model) of the run: the directional
+ * derivative of the state along tangents of the physical ICs and of taurad,
+ * taudrag, DPhieq, Phibar -- what jax.jvp / jax.jacfwd through run_model_scan
+ * give the reference (autodiff_utils.py:27-89 fwd_grad; the retrieval's
+ * forward-mode gradients).  Modified Euler, classic filter, diagnostics off,
+ * test 0 or 2.
+ *   swp_tangent_init: after swp_init_state on the same ICs, the tangent state
+ *     from dphys_ic[g] = real[5][B][J][I] (tangents of eta, delta, Phi, U, V).
+ *   swp_tangent_forward: advances the primal state st and its tangent together
+ *     by nsteps steps from t0 (replaces swp_forward for that window).
+ *   swp_tangent_output: tangents of the physical fields of swp_output_physical. */
+int swp_tangent_init(swp_plan* plan, const swp_group_state* st, const swp_group_tangent* tan,
+                     void* const* phys_ic, void* const* dphys_ic, const swp_flags* flags, void* stream);
+int swp_tangent_forward(swp_plan* plan, const swp_group_state* st, const swp_group_tangent* tan,
+                        const swp_flags* flags, int t0, int nsteps, void* stream);
+int swp_tangent_output(swp_plan* plan, const swp_group_state* st, const swp_group_tangent* tan,
+                       void* const* dphys_out, const swp_flags* flags, void* stream);
 
 #ifdef __cplusplus
 }

@@ -56,6 +56,14 @@ class GroupAdjoint(ctypes.Structure):
     ]
 
 
+class GroupTangent(ctypes.Structure):
+    _fields_ = [
+        ("fourier", ctypes.c_void_p),
+        ("resid", ctypes.c_void_p),
+        ("dparams", ctypes.c_void_p),
+    ]
+
+
 class Flags(ctypes.Structure):
     _fields_ = [
         ("scheme", ctypes.c_int),
@@ -77,6 +85,7 @@ EXPORTS = (
     "swp_adjoint_window", "swp_time_kernels", "swp_forward_checkpointed", "swp_adjoint_step_noalloc",
     "swp_tc_selftest", "swp_device_status", "swp_plan_uses_tensor_cores", "swp_forward_stored",
     "swp_adjoint_stored", "swp_plan_autotune", "swp_plan_tiles", "swp_plan_set_tile",
+    "swp_tangent_init", "swp_tangent_forward", "swp_tangent_output",
 )
 
 _lib = None
@@ -98,6 +107,7 @@ def load(path: os.PathLike | str | None = None) -> ctypes.CDLL:
     gsp = ctypes.POINTER(GroupState)
     gap = ctypes.POINTER(GroupAdjoint)
     fp = ctypes.POINTER(Flags)
+    gtp = ctypes.POINTER(GroupTangent)
     vpp = ctypes.POINTER(ctypes.c_void_p)
     sig = {
         "swp_plan_create": (i, [i, ip, ip, i, ctypes.POINTER(vp)]),
@@ -125,6 +135,9 @@ def load(path: os.PathLike | str | None = None) -> ctypes.CDLL:
         "swp_plan_autotune": (i, [vp, gsp, gap, fp, i, ip, vp]),
         "swp_plan_tiles": (i, [vp, i, ip, ip]),
         "swp_plan_set_tile": (i, [vp, i, i]),
+        "swp_tangent_init": (i, [vp, gsp, gtp, vpp, vpp, fp, vp]),
+        "swp_tangent_forward": (i, [vp, gsp, gtp, fp, i, i, vp]),
+        "swp_tangent_output": (i, [vp, gsp, gtp, vpp, fp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -13,6 +13,11 @@ member in FP64 on the device.
 This replaces reverse-mode ``jax.grad`` through ``run_model_scan_final``
 (reference ``unit_tests/test_autodiff.py:49-129``; ``model.py:1330-1334``
 per-step remat) with O(nsteps / ckpt_every) stored states.
+
+Forward mode (``torch.autograd.forward_ad`` dual tensors through
+:func:`integrate`, or :func:`my_swampe_gb300.autodiff_utils.fwd_grad`) runs
+the hand-written tangent-linear model alongside a primal re-run: what
+``jax.jvp`` / ``jax.jacfwd`` give the reference.
 """
 from __future__ import annotations
 
@@ -97,6 +102,22 @@ class Integration:
         out = eng.output_physical(self.flags)
         return [o[:5] for o in out]
 
+    # ------------------------------------------------------- forward mode
+    def run_tangent(self, ics: Sequence[torch.Tensor], dics: Sequence[torch.Tensor],
+                    dpar: Sequence[torch.Tensor]) -> List[torch.Tensor]:
+        """Primal run from ``ics`` with its tangent-linear model along ``dics``
+        (5, B, J, I) and ``dpar`` (4, B): d(taurad, taudrag, DPhieq, Phibar).
+        Returns per group the tangent of the final physical curr fields."""
+        eng = self.eng
+        xs = [x.to(device=eng.device, dtype=eng.rdtype).contiguous() for x in ics]
+        eng.init_state(xs, self.flags)
+        tfour, tresid, _ = eng.new_tangent_buffers()
+        dp = [d.to(device=eng.device, dtype=torch.float64).contiguous() for d in dpar]
+        eng.tangent_init(self.flags, xs, dics, tfour, tresid, dp)
+        eng.tangent_forward(self.flags, self.t0, self.nsteps, tfour, tresid, dp)
+        out = eng.tangent_output(self.flags, tfour, tresid, dp)
+        return [o[:5] for o in out]
+
     # ------------------------------------------------------------ backward
     def run_backward(self, dphys: Sequence[torch.Tensor]):
         eng = self.eng
@@ -131,6 +152,26 @@ class _IntegrateFn(torch.autograd.Function):
         outs = integ.run_forward(ics)
         ctx.integ = integ
         ctx.in_dtypes = [x.dtype for x in flat]
+        ctx.save_for_forward(*flat)
+        return tuple(o.to(flat[4].dtype) for o in outs)
+
+    @staticmethod
+    def jvp(ctx, _integ_t, *flat_t):
+        """Forward mode: the tangent-linear model along the input tangents."""
+        integ = ctx.integ
+        eng = integ.eng
+        flat = ctx.saved_tensors
+        ics, dics, dpar = [], [], []
+        for g, gd in enumerate(eng.groups):
+            tr, td, dp, pb, ic = flat[5 * g: 5 * g + 5]
+            eng.set_params(g, taurad=tr.detach(), taudrag=td.detach(), DPhieq=dp.detach(), Phibar=pb.detach())
+            ics.append(ic.detach())
+            t = flat_t[5 * g: 5 * g + 5]
+            dics.append(t[4] if t[4] is not None else torch.zeros_like(ic))
+            rows = [(x if x is not None else torch.zeros(gd["B"], device=eng.device)).to(eng.device, torch.float64)
+                    for x in t[:4]]
+            dpar.append(torch.stack([r.expand(gd["B"]) for r in rows]))  # taurad, taudrag, DPhieq, Phibar
+        outs = integ.run_tangent(ics, dics, dpar)
         return tuple(o.to(flat[4].dtype) for o in outs)
 
     @staticmethod

@@ -26,7 +26,7 @@ struct swp_plan {
   int M[MAXG] = {}, B[MAXG] = {}, MT[MAXG] = {}, JB[MAXG] = {};
   size_t spec_smem = 0;
   size_t spec_adj_smem = 0;
-  size_t grid_smem[8] = {};
+  size_t grid_smem[NGRIDMODE] = {};
   // tensor-core Legendre kernel of the FP32 step (every group at M = 42)
   bool use_tc = false;
   float* tcbasis[MAXG] = {};
@@ -307,6 +307,110 @@ int forward_impl(swp_plan* p, const swp_group_state* st, const swp_flags* f, int
   return run_graph(p, key, [&](cudaStream_t cs) {
     return forward_steps<T>(p, st, f, t0, nsteps, row0, write_prev_last, nullptr, cs);
   }, s);
+}
+
+// ------------------------------------------------------------ tangent-linear
+// The tangent state uses the primal's parameters, coefficient tables and
+// residual weights (the filter recursion does not depend on the state); only
+// its Fourier carries and residuals are its own.
+static void tangent_states(const swp_plan* p, const swp_group_state* st, const swp_group_tangent* tan,
+                           swp_group_state* tst) {
+  for (int g = 0; g < p->ng; ++g) {
+    tst[g] = st[g];
+    tst[g].fourier = tan[g].fourier;
+    tst[g].resid = tan[g].resid;
+    tst[g].diag = nullptr;
+    tst[g].hist = nullptr;
+  }
+}
+
+template <typename T>
+int tangent_init_impl(swp_plan* p, const swp_group_state* st, const swp_group_tangent* tan, void* const* phys,
+                      void* const* dphys, const swp_flags* f, cudaStream_t s) {
+  swp_group_state tst[MAXG];
+  tangent_states(p, st, tan, tst);
+  size_t es = sizeof(typename cplx<T>::type);
+  for (int g = 0; g < p->ng; ++g) {
+    size_t bytes = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
+    int rc = cuda_check(p, cudaMemsetAsync(tan[g].fourier, 0, bytes, s), "tangent state clear");
+    if (rc) return rc;
+  }
+  int nbg = 0;
+  GridLaunch<T> LG = make_grid<T>(p, tst, nbg);
+  LG.mode = GM_TL_INIT;
+  LG.cfg = make_cfg(f);
+  LG.cfg.diagnostics = 0;
+  for (int g = 0; g < p->ng; ++g) {
+    LG.grp[g].phys_in = (const T*)dphys[g];
+    LG.grp[g].phys_p = (const T*)phys[g];
+    LG.grp[g].dpar = tan[g].dparams;
+  }
+  return cuda_check(p, launch_grid<T>(LG, nbg, p->grid_smem[GM_TL_INIT], s), "tangent init launch");
+}
+
+// One window of primal + tangent steps.  Per step: the tangent Legendre step
+// (it reads the primal state before the step), the primal Legendre step, the
+// primal grid step, then the tangent grid step (linearised about the new
+// primal level).
+template <typename T>
+int tangent_steps(swp_plan* p, const swp_group_state* st, const swp_group_tangent* tan, const swp_flags* f, int t0,
+                  int nsteps, cudaStream_t s) {
+  swp_group_state tst[MAXG];
+  tangent_states(p, st, tan, tst);
+  int nbs = 0, nbg = 0;
+  SpecLaunch<T> LS = make_spec<T>(p, st, nbs);
+  SpecLaunch<T> LT = make_spec<T>(p, tst, nbs);
+  GridLaunch<T> LG = make_grid<T>(p, st, nbg);
+  GridLaunch<T> LGT = make_grid<T>(p, tst, nbg);
+  LS.mode = 0;
+  LT.mode = 3;
+  LG.mode = GM_STEP;
+  LGT.mode = GM_TL_STEP;
+  for (int g = 0; g < p->ng; ++g) {
+    LT.grp[g].four_p = (const typename cplx<T>::type*)st[g].fourier;
+    LT.grp[g].dpar = tan[g].dparams;
+    LGT.grp[g].primal = (const typename cplx<T>::type*)st[g].fourier;
+    LGT.grp[g].dpar = tan[g].dparams;
+    LG.grp[g].hist = nullptr;
+  }
+  StepCfg cfg = make_cfg(f);
+  cfg.diagnostics = 0;
+  if (nsteps > 0) {
+    int rc = update_coefs<T>(p, st, s);
+    if (rc) return rc;
+  }
+  for (int k = 0; k < nsteps; ++k) {
+    int t = t0 + k;
+    cfg.step = k;
+    cfg.ra_mode = (f->modalflag && t > 2) ? 2 : 1;
+    cfg.write_prev = k == nsteps - 1;
+    cfg.incremental = step_incremental(p, f, t) ? 1 : 0;
+    LS.cfg = LT.cfg = LG.cfg = LGT.cfg = cfg;
+    cudaError_t e = launch_spec<T>(LT, nbs, p->spec_smem, s);
+    if (e != cudaSuccess) return cuda_check(p, e, "tangent spectral kernel launch");
+    e = launch_step_spec<T>(p, LS, nbs, s);
+    if (e != cudaSuccess) return cuda_check(p, e, "spectral kernel launch");
+    e = launch_grid<T>(LG, nbg, p->grid_smem[GM_STEP], s);
+    if (e != cudaSuccess) return cuda_check(p, e, "grid kernel launch");
+    e = launch_grid<T>(LGT, nbg, p->grid_smem[GM_TL_STEP], s);
+    if (e != cudaSuccess) return cuda_check(p, e, "tangent grid kernel launch");
+  }
+  return SWP_OK;
+}
+
+template <typename T>
+int tangent_forward_impl(swp_plan* p, const swp_group_state* st, const swp_group_tangent* tan, const swp_flags* f,
+                         int t0, int nsteps, cudaStream_t s) {
+  if (nsteps < 4) return tangent_steps<T>(p, st, tan, f, t0, nsteps, s);
+  std::vector<uint64_t> key = {3, (uint64_t)t0, (uint64_t)nsteps};
+  key_flags(key, f);
+  key_state(key, p, st);
+  for (int g = 0; g < p->ng; ++g) {
+    key.push_back((uint64_t)tan[g].fourier);
+    key.push_back((uint64_t)tan[g].resid);
+    key.push_back((uint64_t)tan[g].dparams);
+  }
+  return run_graph(p, key, [&](cudaStream_t cs) { return tangent_steps<T>(p, st, tan, f, t0, nsteps, cs); }, s);
 }
 
 template <typename T>
@@ -765,7 +869,7 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
     p->spec_smem = std::max(p->spec_smem, ss);
     size_t sa = f64 ? spec_adj_smem_bytes<double>(M[g], J, p->MT[g]) : spec_adj_smem_bytes<float>(M[g], J, p->MT[g]);
     p->spec_adj_smem = std::max(p->spec_adj_smem, sa);
-    for (int mode = 0; mode < 8; ++mode) {
+    for (int mode = 0; mode < NGRIDMODE; ++mode) {
       const int jbm = grid_rows_per_cta(M[g], f64, mode);
       size_t gs = f64 ? grid_smem_bytes<double>(M[g], J, I, jbm, mode) : grid_smem_bytes<float>(M[g], J, I, jbm, mode);
       p->grid_smem[mode] = std::max(p->grid_smem[mode], gs);
@@ -873,16 +977,17 @@ int swp_diagnose_winds(swp_plan* p, const swp_group_state* st, void* const* ed, 
 }
 
 // Scheme switches every stepping entry checks (model.py:1531-1537).  The
-// adjoint covers the modified-Euler scheme with the classic filter.
+// adjoint and the tangent cover the modified-Euler scheme with the classic filter.
 static int check_scheme(swp_plan* p, const swp_flags* f, bool adjoint) {
   if (f->scheme < 0 || f->scheme > 2) return fail(p, SWP_ERR_ARG, "scheme must be 0, 1 or 2");
   if (f->test < 0 || f->test > 2) return fail(p, SWP_ERR_ARG, "test must be 0 (None), 1 or 2");
   if (f->raw_filter && f->scheme == 1)
     return fail(p, SWP_ERR_ARG, "raw_filter is incompatible with the explicit scheme");
   if (adjoint && f->scheme != 0)
-    return fail(p, SWP_ERR_UNSUPPORTED, "adjoint is implemented for the modified-Euler scheme");
+    return fail(p, SWP_ERR_UNSUPPORTED, "derivatives (adjoint, tangent) are implemented for the modified-Euler scheme");
   if (adjoint && f->raw_filter)
-    return fail(p, SWP_ERR_UNSUPPORTED, "adjoint is implemented for the classic Robert-Asselin filter");
+    return fail(p, SWP_ERR_UNSUPPORTED,
+                "derivatives (adjoint, tangent) are implemented for the classic Robert-Asselin filter");
   return SWP_OK;
 }
 
@@ -898,6 +1003,45 @@ int swp_forward(swp_plan* p, const swp_group_state* st, const swp_flags* f, int 
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? forward_impl<double>(p, st, f, t0, nsteps, row0, write_prev_last, s)
                                   : forward_impl<float>(p, st, f, t0, nsteps, row0, write_prev_last, s);
+}
+
+static int check_tangent(swp_plan* p, const swp_group_state* st, const swp_group_tangent* tan, const swp_flags* f) {
+  if (!p || !st || !tan || !f) return fail(p, SWP_ERR_ARG, "null argument");
+  if (int rc = check_scheme(p, f, true)) return rc;
+  if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "tangent of test=1 (fixed winds) is not implemented");
+  if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "tangent runs with diagnostics off (no blow-up gate)");
+  for (int g = 0; g < p->ng; ++g)
+    if (!tan[g].fourier || !tan[g].resid || !tan[g].dparams || !st[g].fourier || !st[g].params || !st[g].member)
+      return fail(p, SWP_ERR_ARG, "missing tangent buffer");
+  return SWP_OK;
+}
+
+int swp_tangent_init(swp_plan* p, const swp_group_state* st, const swp_group_tangent* tan, void* const* phys,
+                     void* const* dphys, const swp_flags* f, void* stream) {
+  if (int rc = check_tangent(p, st, tan, f)) return rc;
+  if (!phys || !dphys) return fail(p, SWP_ERR_ARG, "null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWP_FP64 ? tangent_init_impl<double>(p, st, tan, phys, dphys, f, s)
+                                  : tangent_init_impl<float>(p, st, tan, phys, dphys, f, s);
+}
+
+int swp_tangent_forward(swp_plan* p, const swp_group_state* st, const swp_group_tangent* tan, const swp_flags* f,
+                        int t0, int nsteps, void* stream) {
+  if (int rc = check_tangent(p, st, tan, f)) return rc;
+  if (nsteps < 0) return fail(p, SWP_ERR_ARG, "nsteps must be >= 0");
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWP_FP64 ? tangent_forward_impl<double>(p, st, tan, f, t0, nsteps, s)
+                                  : tangent_forward_impl<float>(p, st, tan, f, t0, nsteps, s);
+}
+
+int swp_tangent_output(swp_plan* p, const swp_group_state* st, const swp_group_tangent* tan, void* const* out,
+                       const swp_flags* f, void* stream) {
+  if (int rc = check_tangent(p, st, tan, f)) return rc;
+  if (!out) return fail(p, SWP_ERR_ARG, "null argument");
+  swp_group_state tst[MAXG];
+  tangent_states(p, st, tan, tst);
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWP_FP64 ? output_impl<double>(p, tst, out, f, s) : output_impl<float>(p, tst, out, f, s);
 }
 
 int swp_output_physical(swp_plan* p, const swp_group_state* st, void* const* out, const swp_flags* f, void* stream) {

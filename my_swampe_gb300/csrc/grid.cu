@@ -174,6 +174,50 @@ struct PhysicsAdj {
   }
 };
 
+// Tangent of Physics::eval (forward mode): x = (eta, Phi, U, V) with tangent
+// dx, parameter tangents dp = d(taurad, taudrag, DPhieq, Phibar).  Same
+// branch conventions as the adjoint: the clamp passes no tangent where Q < 0,
+// Phieq's Phibar cancels in Q, taudrag = -1 has no drag term.
+template <typename T>
+struct PhysicsTL {
+  T Pb, itr, itd, DPe;
+  bool nodrag, forced;
+  __device__ __forceinline__ void eval(T eta, T Phi, T U, T V, T deta, T dPhi, T dU, T dV, T ihalf, T day_s,
+                                       const T* dp, T* out) const {
+    out[0] = dU * eta + U * deta;
+    out[1] = dV * eta + V * deta;
+    out[2] = dU * Phi + U * dPhi;
+    out[3] = dV * Phi + V * dPhi;
+    out[4] = (T)2 * (U * dU + V * dV) * ihalf;
+    if (forced) {
+      T Phieq = Pb + DPe * day_s;
+      T Q = itr * (Phieq - (Phi + Pb));
+      // dQ = -itr dPhi - Q itr dtaurad + itr day_s dDPhieq
+      T dQ = itr * (day_s * dp[G_DPHIEQ] - dPhi) - Q * itr * dp[G_TAURAD];
+      bool pos = !(Q < (T)0);
+      T Qc = pos ? Q : (T)0, dQc = pos ? dQ : (T)0;
+      T pt = Phi + Pb;
+      T pts = fabs(pt) > (T)0 ? pt : tiny_val<T>();
+      const T ipts = recip_pts(pts);
+      T r = div_pts(Qc, ipts, pts);
+      T dr = div_pts(dQc - r * (dPhi + dp[G_PHIBAR]), ipts, pts);
+      T dRu = -(dU * r + U * dr), dRv = -(dV * r + V * dr);
+      out[5] = dQ;
+      if (nodrag) {
+        out[6] = dRu;
+        out[7] = dRv;
+      } else {
+        // d(U / taudrag) = dU itd - U itd^2 dtaudrag
+        const T ditd = itd * itd * dp[G_TAUDRAG];
+        out[6] = dRu - dU * itd + U * ditd;
+        out[7] = dRv - dV * itd + V * ditd;
+      }
+    } else {
+      out[5] = out[6] = out[7] = (T)0;
+    }
+  }
+};
+
 // Per-CTA context shared by the mode bodies.  The grid sizes are compile-time
 // (one instantiation per truncation), so every index division in the hot
 // loops is by a constant.
@@ -338,7 +382,10 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
   // threads of every CTA would load GB300's small FP64 pipe
   __shared__ T s_par[7];     // Phibar, 1/taurad, 1/taudrag, DPhieq, w_curr, w_mid, w_winds
   __shared__ int s_flag[2];  // no drag (taudrag == -1), member blown up
+  __shared__ T s_dpar[NGRAD];  // tangent-linear modes: d(taurad, taudrag, DPhieq, Phibar)
   if (threadIdx.x == 0) {
+    if (MODE == GM_TL_STEP || MODE == GM_TL_INIT)
+      for (int q = 0; q < NGRAD; ++q) s_dpar[q] = (T)G.dpar[q * B + b];
     const double Pb = G.par[P_PHIBAR * B + b], tr = G.par[P_TAURAD * B + b];
     const double td = G.par[P_TAUDRAG * B + b], DPe = G.par[P_DPHIEQ * B + b];
     const double wc = G.member ? G.member[MS_WCURR * B + b] : 0.0;
@@ -516,6 +563,51 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     return;
   }
 
+  if (MODE == GM_TL_STEP) {
+    // ------------------------------------------------ tangent of GM_STEP
+    // The new level is band-limited (no initial-condition residual): the primal
+    // eta, Phi, U, V (G.primal) and their tangents (G.four) go to the grid, the
+    // linearised nonlinear terms and forcing come back as tangent Fourier terms.
+    __syncthreads();
+    const int pf[4] = {F_ETA, F_PHI, F_U, F_V};
+    const T2* src[8];
+#pragma unroll
+    for (int f = 0; f < 8; ++f) src[f] = (f < 4 ? G.primal : G.four) + pf[f & 3] * FS;
+    stage_rows<T>(c, src, 8, bufB);
+    __syncthreads();
+    T2* zin = c2r_transform<T>(c, bufB, 8, bufA);
+    T2* zout = (zin == bufA) ? bufB : bufA;
+    PhysicsTL<T> pt;
+    pt.Pb = ph.Pb; pt.itr = ph.itr; pt.itd = ph.itd; pt.DPe = ph.DPe; pt.nodrag = ph.nodrag; pt.forced = ph.forced;
+    const int nout = ph.forced ? 8 : 5;
+    for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
+      int n = t % L, r = t / L, j = j0 + r;
+      T ihalf = g.ihalf[j];
+      T s = g.coslat[j];
+      T v[8][2];
+#pragma unroll
+      for (int f = 0; f < 8; ++f) {
+        T2 z = zin[((size_t)f * JB + r) * LS + n];
+        v[f][0] = z.x; v[f][1] = z.y;
+      }
+      T outs[2][8];
+#pragma unroll
+      for (int e = 0; e < 2; ++e)
+        pt.eval(v[0][e], v[1][e], v[2][e], v[3][e], v[4][e], v[5][e], v[6][e], v[7][e], ihalf,
+                c.sday[2 * n + e] * s, s_dpar, outs[e]);
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < nout) zout[((size_t)q * JB + r) * LS + n] = mk<T2>(outs[0][q], outs[1][q]);
+    }
+    __syncthreads();
+    T2* res = cfft_batch_c<-1, L>(zout, zin, nout * JB, c.twL);
+    T2* dst[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) dst[q] = G.four + (F_A + q) * FS;
+    write_r2c<T>(c, res, nout, dst, invI, invI);
+    return;
+  }
+
   if (MODE == GM_FWD2) {
     // ------------------------------------------------ physical eta, delta -> Fourier
     __syncthreads();
@@ -531,8 +623,11 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     return;
   }
 
-  if (MODE == GM_INIT) {
+  if (MODE == GM_INIT || MODE == GM_TL_INIT) {
     // ------------------------------------------------ physical ICs -> state
+    // (GM_TL_INIT: the tangent ICs -> tangent state; the Fourier carries and
+    // residuals are linear in the ICs, the nonlinear terms are linearised
+    // about the primal ICs in phys_p)
     // round 1: eta, delta, Phi, U, V -> Fourier curr (+prev, RA carry) and residuals
     __syncthreads();
     const int nf = 5;
@@ -583,6 +678,15 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       for (int e = 0; e < 2; ++e) {
         T eta = G.phys_in[0 * PS + po + e], Phi = G.phys_in[2 * PS + po + e];
         T U = G.phys_in[3 * PS + po + e], V = G.phys_in[4 * PS + po + e];
+        if (MODE == GM_TL_INIT) {
+          PhysicsTL<T> pt;
+          pt.Pb = ph.Pb; pt.itr = ph.itr; pt.itd = ph.itd; pt.DPe = ph.DPe; pt.nodrag = ph.nodrag;
+          pt.forced = ph.forced;
+          const T* xp = G.phys_p;
+          pt.eval(xp[0 * PS + po + e], xp[2 * PS + po + e], xp[3 * PS + po + e], xp[4 * PS + po + e], eta, Phi,
+                  U, V, ihalf, c.sday[2 * n + e] * s, s_dpar, outs[e]);
+          continue;
+        }
         ph.eval(eta, Phi, U, V, ihalf, c.sday[2 * n + e] * s, outs[e]);
         if (cfg.diagnostics) {
           double Ud = U, Vd = V;
@@ -801,6 +905,8 @@ void grid_set_attributes() {
   set_attr_one<double, GM_ADJ_INIT>(); set_attr_one<float, GM_ADJ_INIT>();
   set_attr_one<double, GM_ADJ_OUTPUT>(); set_attr_one<float, GM_ADJ_OUTPUT>();
   set_attr_one<double, GM_FWD2>(); set_attr_one<float, GM_FWD2>();
+  set_attr_one<double, GM_TL_STEP>(); set_attr_one<float, GM_TL_STEP>();
+  set_attr_one<double, GM_TL_INIT>(); set_attr_one<float, GM_TL_INIT>();
 }
 
 template <typename T>
@@ -826,6 +932,8 @@ cudaError_t launch_grid(const GridLaunch<T>& L0, int nblocks0, size_t smem, cuda
     case GM_ADJ_INIT: k_grid<T, GM_ADJ_INIT><<<nblocks, 256, smem, s>>>(L); break;
     case GM_ADJ_OUTPUT: k_grid<T, GM_ADJ_OUTPUT><<<nblocks, 256, smem, s>>>(L); break;
     case GM_FWD2: k_grid<T, GM_FWD2><<<nblocks, 256, smem, s>>>(L); break;
+    case GM_TL_STEP: k_grid<T, GM_TL_STEP><<<nblocks, 256, smem, s>>>(L); break;
+    case GM_TL_INIT: k_grid<T, GM_TL_INIT><<<nblocks, 256, smem, s>>>(L); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

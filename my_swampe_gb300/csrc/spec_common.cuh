@@ -192,6 +192,36 @@ __device__ __forceinline__ void step_combos_ld(const SpecGroup<T>& G, const Step
   }
 }
 
+// Tangent-linear step (modified Euler): the combined inputs are linear in the
+// state with Phibar in their coefficients (modEuler_tdiff.py:95-103, 185-193),
+// so their tangent is step_combos on the tangent state plus dPhibar times the
+// Phibar-derivative of those coefficients on the primal state `Fp` before the
+// step: Phi takes -dt delta - (tstep/8) i m Beff, -(tstep/8) Aeff on H and
+// -(E tstep2/4 + Phi / a^2) / 2 with n(n+1); delta takes -delta / a^2 with n(n+1).
+template <typename T>
+__device__ __forceinline__ void tangent_phibar_terms(const SpecGroup<T>& G, const StepCfg& cfg, int m, int b, int j,
+                                                     size_t FS, T dPb, typename cplx<T>::type* c) {
+  typedef typename cplx<T>::type T2;
+  constexpr int NSPX = SlotCount<T>::NP;
+  const T2* Fp = G.four_p;
+  const size_t o = ((size_t)m * G.B + b) * G.g.J + j;
+  const T* mc = G.mco;
+  const int B = G.B;
+  const T xm = (T)m;
+  const T t1 = G.jco[(size_t)b * G.g.J + j] * (T)0.25;
+  const T2 del = Fp[F_DELTA * FS + o], phi = Fp[F_PHI * FS + o], E = Fp[F_E * FS + o];
+  T2 A = Fp[F_A * FS + o], Bm = Fp[F_B * FS + o];
+  if (cfg.forcflag) {
+    A = csub(A, Fp[F_G * FS + o]);
+    Bm = cadd(Bm, Fp[F_F * FS + o]);
+  }
+  const T ia2 = mc[MC_IA2 * B + b], half = (T)0.5 * dPb;
+  c[SP_PHI1] = csub(c[SP_PHI1], cadd(cscale(del, mc[MC_DT * B + b] * dPb), cscale(imul(xm, Bm), half * t1)));
+  c[NSPX + SH_PHI1] = csub(c[NSPX + SH_PHI1], cscale(A, half * t1));
+  c[SP_PHI2] = csub(c[SP_PHI2], cscale(cadd(cscale(E, mc[MC_T2 * B + b]), cscale(phi, ia2)), half));
+  c[SP_D2] = csub(c[SP_D2], cscale(del, dPb * ia2));
+}
+
 // step_combos_ld on the state in global memory
 template <typename T>
 __device__ __forceinline__ void step_combos(const SpecGroup<T>& G, const StepCfg& cfg, int mode, bool incr, int m,

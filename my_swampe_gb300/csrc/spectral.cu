@@ -72,10 +72,11 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
   T* sigPm1 = sigm1 + MT * cntmax;
   T* tcmn = sigPm1 + MT * cntmax;
   int* sdead = (int*)(((uintptr_t)(tcmn + MT * cntmax) + 15) & ~(uintptr_t)15);  // [MT]
-  const bool incr = SlotCount<T>::INCR && cfg.incremental && mode == 0 && cfg.scheme == 0;
+  const bool step_mode = mode == 0 || mode == 3;  // 3: tangent-linear step on the tangent state
+  const bool incr = SlotCount<T>::INCR && cfg.incremental && step_mode && cfg.scheme == 0;
 
   // ---- phase 0: per-member spectral coefficients and the blow-up gate
-  load_spec_coefs<T>(G, cfg.diffflag && mode == 0, m, b0, mt, MT, cnt, cntmax, sig, sigP, sigm1, sigPm1, tcmn,
+  load_spec_coefs<T>(G, cfg.diffflag && step_mode, m, b0, mt, MT, cnt, cntmax, sig, sigP, sigm1, sigPm1, tcmn,
                      cfg.scheme == 2);
   if (threadIdx.x < MT) {
     int bt = threadIdx.x, dead = 0;
@@ -102,7 +103,8 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
       for (int side = 0; side < 2; ++side) {
         int j = side ? (J - 1 - jp) : jp;
         T2 c[NSLOT];
-        step_combos<T>(G, cfg, mode, incr, m, b, j, FS, c);
+        step_combos<T>(G, cfg, mode == 3 ? 0 : mode, incr, m, b, j, FS, c);
+        if (mode == 3) tangent_phibar_terms<T>(G, cfg, m, b, j, FS, (T)G.dpar[G_PHIBAR * G.B + b], c);
         if (side == 0) {
 #pragma unroll
           for (int q = 0; q < NSLOT; ++q) { xs[q] = c[q]; xa[q] = c[q]; }
@@ -177,7 +179,8 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
         }
       }
       const int bt = r >> 1, comp = r & 1;
-      const T om = bt < mt ? G.mco[MC_OM * G.B + b0 + bt] : (T)0;
+      // planetary vorticity f_{0,1}: a constant of the wind inversion, absent from its tangent
+      const T om = (bt < mt && mode != 3) ? G.mco[MC_OM * G.B + b0 + bt] : (T)0;
       // semi-implicit solve constants (semi_implicit_tdiff.py): implicit share
       // xi, implicit drag / relaxation kd, kr, explicit drag gd, Phibar, 1/a^2
       T si_xi = (T)0, si_kd = (T)0, si_kr = (T)0, si_gd = (T)0, si_pb = (T)0, si_ia2 = (T)0;

@@ -127,6 +127,8 @@ struct SpecGroup {
   typename cplx<T>::type* lam;          // adjoint Fourier fields (adjoint launches)
   const typename cplx<T>::type* lamY;   // adjoint of the K1 outputs (adjoint launches)
   double* grad;                         // [NGRAD][B] (adjoint launches)
+  const typename cplx<T>::type* four_p; // tangent-linear launches: primal state before the step
+  const double* dpar;                   // tangent-linear launches: [NGRAD][B] parameter tangents
   const T* nco;                         // coefficient tables of the call (CoefTables)
   const T* jco;
   const T* mco;
@@ -138,7 +140,7 @@ struct SpecLaunch {
   int ng;
   int prefix[MAXG + 1];
   StepCfg cfg;
-  int mode;                             // 0 = step, 2 = diagnose winds
+  int mode;                             // 0 = step, 2 = diagnose winds, 3 = tangent-linear step
 };
 
 // ------------------------------------------------------------------- grid ---
@@ -159,6 +161,9 @@ struct GridGroup {
   typename cplx<T>::type* lamy;         // adjoint of the K1 outputs [5][M+1][B][J]
   const typename cplx<T>::type* primal; // primal Fourier fields after the step
   double* grad;                         // [NGRAD][B]
+  // tangent-linear
+  const T* phys_p;                      // primal physical ICs (tangent init)
+  const double* dpar;                   // [NGRAD][B] parameter tangents
 };
 
 template <typename T>
@@ -178,7 +183,10 @@ enum GridMode {
   GM_ADJ_STEP = 4,   // adjoint of GM_STEP
   GM_ADJ_INIT = 5,   // adjoint of GM_INIT (gradient w.r.t. physical ICs)
   GM_ADJ_OUTPUT = 6, // adjoint of the physical curr fields of GM_OUTPUT
-  GM_FWD2 = 7        // physical eta, delta -> truncated Fourier (diagnosed winds)
+  GM_FWD2 = 7,       // physical eta, delta -> truncated Fourier (diagnosed winds)
+  GM_TL_STEP = 8,    // tangent of GM_STEP (linearised nonlinear terms and forcing)
+  GM_TL_INIT = 9,    // tangent of GM_INIT
+  NGRIDMODE = 10
 };
 
 template <typename T> size_t spec_smem_bytes(int M, int J, int MT);

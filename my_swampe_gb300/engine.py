@@ -325,6 +325,47 @@ class Engine:
                                                 self._adjs(lam, lamy, grad), ctypes.byref(flags.c()), int(t0),
                                                 int(nsteps), self.stream), "adjoint_window")
 
+    # ----------------------------------------------------------- tangent-linear
+    def new_tangent_buffers(self):
+        """Per group: tangent Fourier state, tangent IC residual, (4, B) parameter tangents
+        (d taurad, d taudrag, d DPhieq, d Phibar)."""
+        four = [torch.zeros_like(gd["fourier"]) for gd in self.groups]
+        resid = [torch.zeros_like(gd["resid"]) for gd in self.groups]
+        dpar = [torch.zeros((_lib.NGRAD, gd["B"]), dtype=torch.float64, device=self.device) for gd in self.groups]
+        return four, resid, dpar
+
+    def _tans(self, tfour, tresid, dpar) -> ctypes.Array:
+        arr = (_lib.GroupTangent * len(self.groups))()
+        for g in range(len(self.groups)):
+            arr[g].fourier = tfour[g].data_ptr()
+            arr[g].resid = tresid[g].data_ptr()
+            arr[g].dparams = dpar[g].data_ptr()
+        return arr
+
+    def tangent_init(self, flags: RunFlagsC, ics, dics, tfour, tresid, dpar) -> None:
+        """Tangent state from tangents dics[g] (5, B, J, I) of the physical ICs ics[g]
+        (after init_state on the same ICs)."""
+        xs = [x.to(device=self.device, dtype=self.rdtype).contiguous() for x in ics]
+        ds = [x.to(device=self.device, dtype=self.rdtype).contiguous() for x in dics]
+        self._check(self.lib.swp_tangent_init(self._plan, self._states(), self._tans(tfour, tresid, dpar),
+                                              _lib.ptr_array([x.data_ptr() for x in xs]),
+                                              _lib.ptr_array([x.data_ptr() for x in ds]), ctypes.byref(flags.c()),
+                                              self.stream), "tangent_init")
+
+    def tangent_forward(self, flags: RunFlagsC, t0: int, nsteps: int, tfour, tresid, dpar) -> None:
+        """Advance the primal state and its tangent together by nsteps steps."""
+        self._check(self.lib.swp_tangent_forward(self._plan, self._states(), self._tans(tfour, tresid, dpar),
+                                                 ctypes.byref(flags.c()), int(t0), int(nsteps), self.stream),
+                    "tangent_forward")
+
+    def tangent_output(self, flags: RunFlagsC, tfour, tresid, dpar) -> List[torch.Tensor]:
+        """Tangents of the physical fields of output_physical: (8, B, J, I) per group."""
+        outs = [torch.empty((8, gd["B"], gd["J"], gd["I"]), dtype=self.rdtype, device=self.device) for gd in self.groups]
+        self._check(self.lib.swp_tangent_output(self._plan, self._states(), self._tans(tfour, tresid, dpar),
+                                                _lib.ptr_array([o.data_ptr() for o in outs]), ctypes.byref(flags.c()),
+                                                self.stream), "tangent_output")
+        return outs
+
     def time_kernels(self, flags: RunFlagsC, nrep: int = 20, adjoint: bool = True, fourier=None):
         """Average ms per launch (CUDA events, library stream) of the spectral, grid,
         grid-adjoint and spectral-adjoint kernels on a scratch copy of the state."""

@@ -1,0 +1,148 @@
+"""The tangent-linear (forward-mode) model on the GPU, the counterpart of
+jax.jvp / jax.jacfwd through run_model_scan (autodiff_utils.py:27-89 fwd_grad):
+against central differences of the FP64 forward, against the hand-written
+adjoint by the dot-product identity <w, J v> = <J^T w, v>, and fwd_grad
+against the reverse-mode gradient."""
+import numpy as np
+import pytest
+import torch
+import torch.autograd.forward_ad as fwAD
+
+pytestmark = pytest.mark.gpu
+
+NSTEPS = 12
+
+
+def _setup(prec="fp64", B=2, test=None, seed=5):
+    from my_swampe_gb300 import workloads
+    from my_swampe_gb300.engine import Engine, RunFlagsC
+
+    eng = Engine([(42, B)], prec)
+    wl = workloads.forced_ensemble(eng, dt=600.0, Phibar=3.0e5, seed=seed)
+    flags = RunFlagsC(test=test, diagnostics=False, t_start=2)
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    ics = wl["ics"]
+    # a smooth direction: the ICs' own structure with random member weights, plus
+    # a smooth Phi pattern
+    w = torch.rand((5, B, 1, 1), generator=g, dtype=torch.float64).to(eng.device) - 0.5
+    dics = (ics * w).contiguous()
+    dics[2] += 1e-2 * wl["ics"][2].flip(-1)
+    p = wl["params"]
+    dpar = torch.stack([0.1 * p["taurad"], 0.1 * p["taudrag"], 0.1 * p["DPhieq"],
+                        torch.full((B,), 0.05 * 3.0e5, dtype=torch.float64, device=eng.device)])
+    dpar = dpar * (torch.rand((4, B), generator=g, dtype=torch.float64).to(eng.device) - 0.5)
+    return eng, flags, wl, ics, dics, dpar
+
+
+def _forward(eng, flags, wl, ics, params_shift=None, h=0.0):
+    from my_swampe_gb300 import workloads
+
+    p = dict(wl["params"])
+    if params_shift is not None:
+        for k, name in enumerate(("taurad", "taudrag", "DPhieq")):
+            p[name] = p[name] + h * params_shift[k]
+        p["Phibar"] = p["Phibar"] + h * params_shift[3]
+    workloads.apply_params(eng, 0, p)
+    eng.init_state([ics.to(eng.rdtype)], flags)
+    eng.forward(flags, t0=2, nsteps=NSTEPS)
+    return eng.output_physical(flags)[0][:5].double()
+
+
+def _tangent(eng, flags, wl, ics, dics, dpar):
+    from my_swampe_gb300 import workloads
+
+    workloads.apply_params(eng, 0, wl["params"])
+    eng.init_state([ics.to(eng.rdtype)], flags)
+    tf, tr, _ = eng.new_tangent_buffers()
+    eng.tangent_init(flags, [ics], [dics], tf, tr, [dpar])
+    eng.tangent_forward(flags, 2, NSTEPS, tf, tr, [dpar])
+    return eng.tangent_output(flags, tf, tr, [dpar])[0][:5].double()
+
+
+@pytest.mark.parametrize("test", [None, 2])
+def test_tangent_matches_central_differences(cuda, test):
+    eng, flags, wl, ics, dics, dpar = _setup(test=test)
+    tl = _tangent(eng, flags, wl, ics, dics, dpar)
+    h = 1e-6
+    fp = _forward(eng, flags, wl, ics + h * dics, dpar, h)
+    fm = _forward(eng, flags, wl, ics - h * dics, dpar, -h)
+    fd = (fp - fm) / (2 * h)
+    for k, name in enumerate(("eta", "delta", "Phi", "U", "V")):
+        rel = float(torch.linalg.norm(tl[k] - fd[k]) / torch.linalg.norm(fd[k]))
+        assert rel < 2e-6, (name, rel)
+
+
+def test_tangent_adjoint_dot_product(cuda):
+    """<w, J v> from the tangent model equals <J^T w, v> from the adjoint (FP64)."""
+    from my_swampe_gb300 import adjoint
+
+    eng, flags, wl, ics, dics, dpar = _setup()
+    p = wl["params"]
+    names = ("taurad", "taudrag", "DPhieq", "Phibar")
+    base = {k: (p[k] if torch.is_tensor(p[k]) else torch.full((2,), float(p[k]), dtype=torch.float64,
+                                                               device=eng.device)) for k in names}
+    from my_swampe_gb300 import workloads
+
+    workloads.apply_params(eng, 0, p)
+    wgt = torch.randn((5, 2, 64, 128), dtype=torch.float64, device=eng.device)
+    # reverse: J^T w
+    xs = {k: base[k].clone().requires_grad_(True) for k in names}
+    x0 = ics.clone().requires_grad_(True)
+    out = adjoint.integrate(eng, flags, t0=2, nsteps=NSTEPS, params=[xs], ics=[x0], store="all")[0]
+    grads = torch.autograd.grad((wgt * out).sum(), [x0] + [xs[k] for k in names])
+    lhs = float((grads[0] * dics).sum()) + sum(float((grads[1 + k] * dpar[k]).sum()) for k in range(4))
+    # forward: J v
+    with fwAD.dual_level():
+        dual_p = {k: fwAD.make_dual(base[k], dpar[i].contiguous()) for i, k in enumerate(names)}
+        dual_x = fwAD.make_dual(ics, dics)
+        out2 = adjoint.integrate(eng, flags, t0=2, nsteps=NSTEPS, params=[dual_p], ics=[dual_x], store="all")[0]
+        jv = fwAD.unpack_dual(out2).tangent
+    rhs = float((wgt * jv).sum())
+    assert abs(lhs - rhs) <= 1e-10 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+def test_fwd_grad_matches_reverse_mode(cuda):
+    """autodiff_utils.fwd_grad (forward mode, one tangent run per parameter)
+    against torch.autograd.grad through the adjoint, for a shared parameter vector."""
+    from my_swampe_gb300 import adjoint, workloads
+    from my_swampe_gb300.autodiff_utils import fwd_grad
+
+    eng, flags, wl, ics, _, _ = _setup()
+    workloads.apply_params(eng, 0, wl["params"])
+    target = _forward(eng, flags, wl, ics)[2] * 1.01
+    integ = adjoint.Integration(eng, flags, 2, NSTEPS, store="all")
+
+    def loss_fn(theta):
+        params = dict(taurad=theta[0] * torch.ones(2, dtype=torch.float64, device=eng.device),
+                      taudrag=theta[1] * torch.ones(2, dtype=torch.float64, device=eng.device),
+                      DPhieq=theta[2] * torch.ones(2, dtype=torch.float64, device=eng.device),
+                      Phibar=theta[3] * torch.ones(2, dtype=torch.float64, device=eng.device))
+        out = adjoint.integrate(eng, flags, 2, NSTEPS, [params], [ics], integration=integ)[0]
+        return ((out[2] - target) ** 2).mean()
+
+    theta = torch.tensor([36000.0, 21600.0, 1.0e6, 3.0e5], dtype=torch.float64, device=eng.device)
+    g_fwd = fwd_grad(loss_fn, theta)
+    th = theta.clone().requires_grad_(True)
+    g_rev = torch.autograd.grad(loss_fn(th), th)[0]
+    rel = (g_fwd - g_rev).abs() / g_rev.abs()
+    assert bool(torch.all(rel < 1e-8)), (g_fwd, g_rev)
+
+
+def test_fast_tangent_close_to_fp64(cuda):
+    """FP32 tangent model (incremental steps) against the FP64 one."""
+    t64 = _tangent(*_setup("fp64"))
+    eng, flags, wl, ics, dics, dpar = _setup("fast")
+    t32 = _tangent(eng, flags, wl, ics, dics, dpar)
+    for k, name in enumerate(("eta", "delta", "Phi")):
+        rel = float(torch.linalg.norm(t32[k] - t64[k]) / torch.linalg.norm(t64[k]))
+        assert rel < 1e-4, (name, rel)
+
+
+def test_tangent_refuses_unsupported(cuda):
+    from my_swampe_gb300.engine import RunFlagsC
+
+    eng, flags, wl, ics, dics, dpar = _setup()
+    tf, tr, _ = eng.new_tangent_buffers()
+    for bad in (RunFlagsC(scheme=2), RunFlagsC(raw_filter=True), RunFlagsC(test=1), RunFlagsC(diagnostics=True)):
+        with pytest.raises(RuntimeError):
+            eng.tangent_forward(bad, 2, 2, tf, tr, [dpar])

@@ -134,3 +134,28 @@ def test_continuation_pickles_round_trip(tmp_path):
     for a, b in zip(fields, back):
         np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(continuation.read_pickle("spinup-winds", custompath=str(tmp_path)), spin)
+
+
+def test_fwd_grad_argument_rules():
+    """autodiff_utils.py:27-89: theta must be 1-D, empty theta gives an empty
+    gradient, a non-positive chunk is refused (before any evaluation)."""
+    from my_swampe_gb300.autodiff_utils import fwd_grad
+
+    def never(theta):
+        raise AssertionError("loss evaluated")
+
+    with pytest.raises(ValueError, match="1-D"):
+        fwd_grad(never, torch.zeros((2, 2)))
+    assert fwd_grad(never, torch.zeros(0)).shape == (0,)
+    with pytest.raises(ValueError, match="chunk"):
+        fwd_grad(never, torch.zeros(3), chunk=0)
+
+
+def test_fwd_grad_on_a_cpu_function():
+    """The helper itself is plain forward-mode AD: check it on a closed form."""
+    from my_swampe_gb300.autodiff_utils import fwd_grad
+
+    theta = torch.tensor([0.3, -1.2, 2.0], dtype=torch.float64)
+    g = fwd_grad(lambda t: (t[0] * t[1]) ** 2 + torch.sin(t[2]), theta, chunk=2)
+    want = torch.tensor([2 * theta[0] * theta[1] ** 2, 2 * theta[1] * theta[0] ** 2, torch.cos(theta[2])])
+    assert torch.allclose(g, want, rtol=1e-14, atol=0)
