@@ -202,7 +202,8 @@ class Engine:
         gd = self.groups[g]
         for name, v in kw.items():
             row = PARAM_NAMES.index(name)
-            t = torch.as_tensor(v, dtype=torch.float64, device=self.device)
+            # values only: a parameter's gradient or tangent flows through adjoint.integrate
+            t = torch.as_tensor(v, dtype=torch.float64, device=self.device).detach()
             gd["params"][row].copy_(t.expand(gd["B"]) if t.dim() == 0 else t.reshape(gd["B"]))
 
     # ------------------------------------------------------------------ state

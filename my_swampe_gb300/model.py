@@ -20,6 +20,7 @@ from typing import Any, Dict, NamedTuple, Optional
 
 import numpy as np
 import torch
+import torch.autograd.forward_ad as fwAD
 
 from . import _lib, continuation
 from .engine import Engine, RunFlagsC
@@ -297,6 +298,21 @@ def _prepare_ic(x, J, I, B, batched, name, dev):
     raise ValueError(f"{name} must have shape {(J, I)}, got {tuple(t.shape)}.")
 
 
+def _tracked(x) -> bool:
+    """True for a tensor that carries a reverse-mode graph or a forward-mode tangent."""
+    if not torch.is_tensor(x):
+        return False
+    if x.requires_grad and torch.is_grad_enabled():
+        return True
+    return fwAD.unpack_dual(x).tangent is not None
+
+
+def _per_member(x, B: int, dev) -> torch.Tensor:
+    t = x if torch.is_tensor(x) else torch.as_tensor(x, dtype=torch.float64)
+    t = t.to(device=dev, dtype=torch.float64)
+    return t.expand(B) if t.dim() == 0 else t.reshape(B)
+
+
 def run_model_scan(
     *, M: int, dt, tmax: int, Phibar, omega, a, test: Optional[int] = None, g=9.8, forcflag: bool = True,
     taurad=86400.0, taudrag=86400.0, DPhieq=4 * (10**6), a1=0.05, diffflag: bool = True, modalflag: bool = True,
@@ -311,7 +327,11 @@ def run_model_scan(
     reference (``model.py:1345-1765``); ``remat_step``, ``jit_scan`` and
     ``donate_state`` are accepted for compatibility and have no effect (the
     scan body is always a compiled kernel pair and the state is updated in
-    place).  ``semi_implicit`` selects the semi-implicit leapfrog
+    place).  Tensors among taurad, taudrag, DPhieq, Phibar and the ``*_init``
+    fields that require grad (or carry forward-mode tangents) make the
+    ``last_state`` curr fields (eta, delta, Phi, U, V) differentiable through
+    the hand-written adjoint and tangent-linear kernels, the counterpart of
+    ``jax.grad`` / ``jax.jvp`` through the reference's scan.  ``semi_implicit`` selects the semi-implicit leapfrog
     (``semi_implicit_tdiff.py``) and ``raw_filter`` the Robert-Asselin-Williams
     filter (``model.py:1007-1087``); both run forward only (the hand-written
     adjoint covers the modified-Euler scheme with the classic filter).
@@ -380,6 +400,19 @@ def run_model_scan(
             if shp != (J, I) and not (batched and shp == (B, J, I)):
                 raise ValueError(f"{name} must have shape {(J, I)}, got {shp}.")
 
+    # differentiable inputs (the parameters the adjoint and the tangent model cover)
+    diff_inputs = (taurad, taudrag, DPhieq, Phibar, eta0_init, delta0_init, Phi0_init, U0_init, V0_init)
+    needs_grad = any(_tracked(x) for x in diff_inputs)
+    if any(_tracked(x) for x in (dt, a, omega, g, K6, K6Phi, alpha, si_alpha, williams_alpha)):
+        raise NotImplementedError("derivatives are implemented with respect to taurad, taudrag, DPhieq, Phibar "
+                                  "and the initial fields")
+    if needs_grad:
+        if semi_implicit or raw_filter or expflag or test == 1:
+            raise NotImplementedError("derivatives are implemented for the modified-Euler scheme with the classic "
+                                      "filter and test None or 2")
+        if U0_init is None and (_tracked(eta0_init) or _tracked(delta0_init)):
+            raise NotImplementedError("derivatives with respect to eta0_init / delta0_init need U0_init and V0_init")
+
     eng = Engine([(M, B)], precision, device)
     dev = eng.device
     K6Phi_eff = K6 if K6Phi is None else K6Phi
@@ -401,8 +434,14 @@ def run_model_scan(
     elif not contflag:
         if batched and not all(_is_python_scalar(v) for v in (a, omega, Phibar)):
             raise ValueError("analytic initial conditions need scalar a, omega and Phibar; pass *_init fields instead")
-        fields = _analytic_ic(M, float(a), float(omega), float(Phibar), test, float(a1), dev)
+        pb = float(Phibar.detach()) if torch.is_tensor(Phibar) else float(Phibar)
+        fields = _analytic_ic(M, float(a), float(omega), pb, test, float(a1), dev)
         eta0, delta0, Phi0, U0, V0 = (f.expand(B, J, I) for f in fields)
+        if _tracked(Phibar):
+            # the analytic Phi0 is linear in Phibar (initial_conditions.py:160-166):
+            # carry its derivative into the differentiable run
+            unit = _analytic_ic(M, float(a), float(omega), pb + 1.0, test, float(a1), dev)[2] - fields[2]
+            Phi0 = Phi0 + (Phibar - Phibar.detach()) * unit.expand(B, J, I)
     else:
         fields = []
         for name in ("eta", "delta", "Phi"):
@@ -424,14 +463,31 @@ def run_model_scan(
     gd = eng.groups[0]
     hist = [torch.empty((max(T, 0), 5, B, J, I), dtype=eng.rdtype, device=dev)] if return_history else None
     ics = torch.stack((eta0, delta0, Phi0, U0, V0), 0)
-    eng.init_state([ics], flags, diag=diag)
+    eng.init_state([ics.detach()], flags, diag=diag)
     four = gd["fourier"]
     # Rum_lag/Rvm_lag: pass-through carries of the semi-implicit scheme (model.py:734-739, 775-792)
     td = gd["params"][_lib.P_TAUDRAG]
     inv_td = torch.where(td == -1.0, torch.zeros_like(td), 1.0 / td).to(eng.rdtype)
     Rum = four[_lib.F_F] + four[_lib.F_U] * inv_td[None, :, None]
     Rvm = four[_lib.F_G] + four[_lib.F_V] * inv_td[None, :, None]
-    if T > 0:
+    dcurr = None
+    if needs_grad and T > 0:
+        # the differentiable final curr fields; with neither history nor
+        # diagnostics asked for, this run is the run (the engine holds its final state)
+        from . import adjoint
+
+        if return_history or diagnostics:
+            eng.forward(flags, t0=starttime_eff, nsteps=T, row0=0, diag=diag, hist=hist, write_prev_last=True)
+            saved = (four.clone(), gd["member"].clone())
+        dflags = RunFlagsC(scheme=0, forcflag=forcflag, diffflag=diffflag, modalflag=modalflag, test=test,
+                           diagnostics=False, t_start=starttime_eff)
+        dpar = dict(taurad=_per_member(taurad, B, dev), taudrag=_per_member(taudrag, B, dev),
+                    DPhieq=_per_member(DPhieq if test is None else 0.0, B, dev), Phibar=_per_member(Phibar, B, dev))
+        dcurr = adjoint.integrate(eng, dflags, starttime_eff, T, [dpar], [ics])[0]
+        if return_history or diagnostics:  # the gated run's state (dead flags included)
+            four.copy_(saved[0])
+            gd["member"].copy_(saved[1])
+    elif T > 0:
         eng.forward(flags, t0=starttime_eff, nsteps=T, row0=0, diag=diag, hist=hist, write_prev_last=True)
     phys = eng.output_physical(flags)[0]
     eng.check_device_status()
@@ -440,6 +496,10 @@ def run_model_scan(
     # the Fourier prev carry follows the filtered lineage with the semi-implicit
     # scheme or the RAW filter, the unfiltered curr otherwise (model.py:1089-1110)
     last = _assemble_state(eng, phys, Rum, Rvm, batched, filtered_prev=bool(semi_implicit or raw_filter))
+    if dcurr is not None:
+        pick = (lambda v: v) if batched else (lambda v: v[0])
+        last = last._replace(eta_curr=pick(dcurr[0]), delta_curr=pick(dcurr[1]), Phi_curr=pick(dcurr[2]),
+                             U_curr=pick(dcurr[3]), V_curr=pick(dcurr[4]))
     res: Dict[str, Any] = dict(static=static, t_seq=torch.arange(starttime_eff, tmax, dtype=torch.int32, device=dev),
                                last_state=last, starttime=starttime_eff)
     if return_history:

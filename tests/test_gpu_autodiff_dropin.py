@@ -1,0 +1,116 @@
+"""The reference's autodiff tests (unit_tests/test_autodiff.py) on the drop-in
+API: torch.autograd / forward-mode AD through run_model_scan_final itself,
+as jax.grad / jax.jvp go through the reference's."""
+import numpy as np
+import pytest
+import torch
+import torch.autograd.forward_ad as fwAD
+
+pytestmark = pytest.mark.gpu
+
+BASE = dict(M=42, dt=600.0, tmax=7, Phibar=3.0e5, omega=7.292e-5, a=6.37122e6, test=None, g=9.8, forcflag=True,
+            taurad=86400.0, taudrag=86400.0, DPhieq=4.0e6, diffflag=True, modalflag=True, alpha=0.01,
+            expflag=False, K6=1.24e33, diagnostics=False, jit_scan=True)
+
+
+def _loss(name, theta, **extra):
+    from my_swampe_gb300 import run_model_scan_final
+
+    kw = dict(BASE, **extra)
+    kw[name] = theta
+    Phi = run_model_scan_final(**kw)["last_state"].Phi_curr
+    return torch.mean(Phi * Phi)
+
+
+@pytest.mark.parametrize("name,value", [("DPhieq", 4.0e6), ("taurad", 86400.0), ("taudrag", 86400.0),
+                                        ("Phibar", 3.0e5)])
+def test_grad_returns_finite_for_each_scalar_parameter(cuda, name, value):
+    """test_autodiff.py:56-86 for the parameters the adjoint covers."""
+    th = torch.tensor(value, dtype=torch.float64, device="cuda", requires_grad=True)
+    g = torch.autograd.grad(_loss(name, th), th)[0]
+    assert g.shape == () and bool(torch.isfinite(g)) and float(g) != 0.0
+
+
+def test_other_parameters_refuse_gradients(cuda):
+    th = torch.tensor(1.24e33, dtype=torch.float64, device="cuda", requires_grad=True)
+    with pytest.raises(NotImplementedError):
+        _loss("K6", th)
+
+
+def test_jvp_returns_finite_for_DPhieq(cuda):
+    """test_autodiff.py:89-99"""
+    with fwAD.dual_level():
+        d = fwAD.make_dual(torch.tensor(4.0e6, dtype=torch.float64, device="cuda"),
+                           torch.tensor(1.0, dtype=torch.float64, device="cuda"))
+        out = fwAD.unpack_dual(_loss("DPhieq", d))
+    assert bool(torch.isfinite(out.primal)) and bool(torch.isfinite(out.tangent))
+    # forward mode equals reverse mode
+    th = torch.tensor(4.0e6, dtype=torch.float64, device="cuda", requires_grad=True)
+    g = torch.autograd.grad(_loss("DPhieq", th), th)[0]
+    assert abs(float(out.tangent) - float(g)) <= 1e-9 * abs(float(g))
+
+
+def test_grad_matches_finite_difference_for_DPhieq(cuda):
+    """test_autodiff.py:102-129: centred difference with eps = 1, rel < 1e-4."""
+    th = torch.tensor(4.0e6, dtype=torch.float64, device="cuda", requires_grad=True)
+    g_ad = float(torch.autograd.grad(_loss("DPhieq", th), th)[0])
+    with torch.no_grad():
+        fp = float(_loss("DPhieq", 4.0e6 + 1.0))
+        fm = float(_loss("DPhieq", 4.0e6 - 1.0))
+    g_fd = (fp - fm) / 2.0
+    assert g_ad != 0.0
+    assert abs(g_ad - g_fd) / max(abs(g_fd), 1e-30) < 1e-4
+
+
+def test_grad_wrt_initial_phi_field(cuda):
+    """test_autodiff.py:132-190: gradient with respect to a (J, I) initial Phi
+    (solid-body eta, zero delta and winds given explicitly)."""
+    from my_swampe_gb300 import run_model_scan_final
+    from oracle import swampe_oracle as o
+
+    mus = o.cached_geometry(42)["mus"]
+    eta0 = np.broadcast_to(2 * 7.292e-5 * mus[:, None], (64, 128)).copy()
+    z = np.zeros((64, 128))
+    phi = torch.zeros((64, 128), dtype=torch.float64, device="cuda", requires_grad=True)
+    sim = run_model_scan_final(M=42, dt=1200.0, tmax=5, Phibar=3.0e5, omega=7.292e-5, a=6.37122e6, test=None,
+                               eta0_init=eta0, delta0_init=z, Phi0_init=phi, U0_init=z, V0_init=z,
+                               diagnostics=False)
+    g = torch.autograd.grad(torch.mean(sim["last_state"].Phi_curr), phi)[0]
+    assert g.shape == (64, 128)
+    assert bool(torch.all(torch.isfinite(g))) and float(g.abs().max()) > 0.0
+
+
+def test_history_run_gradient_equals_final_run(cuda):
+    """With history and diagnostics on, the curr fields still carry the gradient,
+    and the history is the plain run's."""
+    from my_swampe_gb300 import run_model_scan
+
+    th = torch.tensor(4.0e6, dtype=torch.float64, device="cuda", requires_grad=True)
+    kw = dict(BASE)
+    kw.pop("diagnostics")
+    kw["DPhieq"] = th
+    res = run_model_scan(**kw, diagnostics=True)
+    Phi = res["last_state"].Phi_curr
+    g1 = torch.autograd.grad(torch.mean(Phi * Phi), th)[0]
+    th2 = torch.tensor(4.0e6, dtype=torch.float64, device="cuda", requires_grad=True)
+    g2 = torch.autograd.grad(_loss("DPhieq", th2), th2)[0]
+    assert abs(float(g1) - float(g2)) <= 1e-12 * abs(float(g2))
+    np.testing.assert_allclose(res["outs"]["Phi"][-1].detach().cpu().numpy(), Phi.detach().cpu().numpy(),
+                               rtol=0, atol=1e-9)
+
+
+def test_phibar_gradient_includes_the_analytic_initial_condition(cuda):
+    """test = 2 analytic ICs depend on Phibar: the gradient matches a centred difference."""
+    from my_swampe_gb300 import run_model_scan_final
+
+    kw = dict(M=42, dt=600.0, tmax=6, omega=7.2921159e-5, a=6.37122e6, test=2, forcflag=False)
+
+    def loss(pb):
+        Phi = run_model_scan_final(**kw, Phibar=pb)["last_state"].Phi_curr
+        return torch.mean(Phi * Phi)
+
+    th = torch.tensor(3.0e3, dtype=torch.float64, device="cuda", requires_grad=True)
+    g_ad = float(torch.autograd.grad(loss(th), th)[0])
+    with torch.no_grad():
+        g_fd = (float(loss(3.0e3 + 0.01)) - float(loss(3.0e3 - 0.01))) / 0.02
+    assert abs(g_ad - g_fd) <= 1e-6 * abs(g_fd), (g_ad, g_fd)
