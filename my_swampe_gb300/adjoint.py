@@ -29,6 +29,8 @@ from . import _lib
 from .engine import Engine, RunFlagsC
 
 GRAD_PARAMS = ("taurad", "taudrag", "DPhieq", "Phibar")
+PARAM_ROW = {"taurad": _lib.P_TAURAD, "taudrag": _lib.P_TAUDRAG, "DPhieq": _lib.P_DPHIEQ, "Phibar": _lib.P_PHIBAR,
+             "a": _lib.P_A, "dt": _lib.P_DT, "K6": _lib.P_K6, "K6Phi": _lib.P_K6PHI, "omega": _lib.P_OMEGA}
 
 
 class Integration:
@@ -106,7 +108,7 @@ class Integration:
     def run_tangent(self, ics: Sequence[torch.Tensor], dics: Sequence[torch.Tensor],
                     dpar: Sequence[torch.Tensor]) -> List[torch.Tensor]:
         """Primal run from ``ics`` with its tangent-linear model along ``dics``
-        (5, B, J, I) and ``dpar`` (4, B): d(taurad, taudrag, DPhieq, Phibar).
+        (5, B, J, I) and ``dpar`` (NTANGENT, B), rows in ``_lib.TANGENT_PARAMS``.
         Returns per group the tangent of the final physical curr fields."""
         eng = self.eng
         xs = [x.to(device=eng.device, dtype=eng.rdtype).contiguous() for x in ics]
@@ -138,22 +140,35 @@ class Integration:
         return dic, grad
 
 
+NP = _lib.NTANGENT        # differentiable per-member parameters (_lib.TANGENT_PARAMS)
+NF = NP + 1               # flat inputs per group: the parameters, then the initial fields
+
+
 class _IntegrateFn(torch.autograd.Function):
+    """flat = per group: the NP parameters of ``_lib.TANGENT_PARAMS`` as (B,)
+    tensors, then the initial fields (5, B, J, I).  Reverse mode: the adjoint
+    sweep gives the initial-field and taurad / taudrag / DPhieq / Phibar
+    gradients; a parameter that enters only the coefficient tables (a, dt,
+    K6, K6Phi, omega) gets its per-member gradient from one tangent-linear run
+    along it (members are independent, so one run serves all of them)."""
+
+    @staticmethod
+    def _set_params(eng, flat):
+        for g in range(len(eng.groups)):
+            vals = flat[NF * g: NF * g + NP]
+            eng.set_params(g, **{k: v.detach() for k, v in zip(_lib.TANGENT_PARAMS, vals)})
+
     @staticmethod
     def forward(ctx, integ: Integration, *flat):
-        # flat = per group: taurad, taudrag, DPhieq, Phibar (B,), ics (5, B, J, I)
         eng = integ.eng
-        ng = len(eng.groups)
-        ics = []
-        for g in range(ng):
-            tr, td, dp, pb, ic = flat[5 * g: 5 * g + 5]
-            eng.set_params(g, taurad=tr.detach(), taudrag=td.detach(), DPhieq=dp.detach(), Phibar=pb.detach())
-            ics.append(ic.detach())
+        _IntegrateFn._set_params(eng, flat)
+        ics = [flat[NF * g + NP].detach() for g in range(len(eng.groups))]
         outs = integ.run_forward(ics)
         ctx.integ = integ
         ctx.in_dtypes = [x.dtype for x in flat]
         ctx.save_for_forward(*flat)
-        return tuple(o.to(flat[4].dtype) for o in outs)
+        ctx.save_for_backward(*flat)
+        return tuple(o.to(flat[NP].dtype) for o in outs)
 
     @staticmethod
     def jvp(ctx, _integ_t, *flat_t):
@@ -161,32 +176,51 @@ class _IntegrateFn(torch.autograd.Function):
         integ = ctx.integ
         eng = integ.eng
         flat = ctx.saved_tensors
+        _IntegrateFn._set_params(eng, flat)
         ics, dics, dpar = [], [], []
         for g, gd in enumerate(eng.groups):
-            tr, td, dp, pb, ic = flat[5 * g: 5 * g + 5]
-            eng.set_params(g, taurad=tr.detach(), taudrag=td.detach(), DPhieq=dp.detach(), Phibar=pb.detach())
+            ic = flat[NF * g + NP]
             ics.append(ic.detach())
-            t = flat_t[5 * g: 5 * g + 5]
-            dics.append(t[4] if t[4] is not None else torch.zeros_like(ic))
+            t = flat_t[NF * g: NF * g + NF]
+            dics.append(t[NP] if t[NP] is not None else torch.zeros_like(ic))
             rows = [(x if x is not None else torch.zeros(gd["B"], device=eng.device)).to(eng.device, torch.float64)
-                    for x in t[:4]]
-            dpar.append(torch.stack([r.expand(gd["B"]) for r in rows]))  # taurad, taudrag, DPhieq, Phibar
+                    for x in t[:NP]]
+            dpar.append(torch.stack([r.expand(gd["B"]) for r in rows]))
         outs = integ.run_tangent(ics, dics, dpar)
-        return tuple(o.to(flat[4].dtype) for o in outs)
+        return tuple(o.to(flat[NP].dtype) for o in outs)
 
     @staticmethod
     def backward(ctx, *gouts):
         integ = ctx.integ
         eng = integ.eng
+        flat = ctx.saved_tensors
         dphys = [(g if g is not None else torch.zeros((5, gd["B"], gd["J"], gd["I"]), device=eng.device))
                  for g, gd in zip(gouts, eng.groups)]
         dic, grad = integ.run_backward(dphys)
-        res = [None]
+        res = [None] * (1 + NF * len(eng.groups))
         for g in range(len(eng.groups)):
+            o = 1 + NF * g
             gr = grad[g]
-            res += [gr[_lib.G_TAURAD].to(ctx.in_dtypes[5 * g]), gr[_lib.G_TAUDRAG].to(ctx.in_dtypes[5 * g + 1]),
-                    gr[_lib.G_DPHIEQ].to(ctx.in_dtypes[5 * g + 2]), gr[_lib.G_PHIBAR].to(ctx.in_dtypes[5 * g + 3]),
-                    dic[g].to(ctx.in_dtypes[5 * g + 4])]
+            for k, row in enumerate((_lib.G_TAURAD, _lib.G_TAUDRAG, _lib.G_DPHIEQ, _lib.G_PHIBAR)):
+                res[o + k] = gr[row].to(ctx.in_dtypes[NF * g + k])
+            res[o + NP] = dic[g].to(ctx.in_dtypes[NF * g + NP])
+        # coefficient-only parameters: one tangent run per parameter that needs a gradient
+        extra = [k for k in range(_lib.NGRAD, NP)
+                 if any(ctx.needs_input_grad[1 + NF * g + k] for g in range(len(eng.groups)))]
+        if extra:
+            _IntegrateFn._set_params(eng, flat)
+            ics = [flat[NF * g + NP].detach() for g in range(len(eng.groups))]
+            zeros = [torch.zeros_like(x) for x in ics]
+            for k in extra:
+                dpar = []
+                for gd in eng.groups:
+                    d = torch.zeros((NP, gd["B"]), dtype=torch.float64, device=eng.device)
+                    d[k] = 1.0
+                    dpar.append(d)
+                jk = integ.run_tangent(ics, zeros, dpar)
+                for g in range(len(eng.groups)):
+                    w = dphys[g].to(torch.float64)
+                    res[1 + NF * g + k] = (w * jk[g].to(torch.float64)).sum(dim=(0, 2, 3)).to(ctx.in_dtypes[NF * g + k])
         return tuple(res)
 
 
@@ -194,8 +228,9 @@ def integrate(engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, params: Se
               ckpt_every: int = 50, integration: Integration = None, store: str = "auto"):
     """Differentiable run of every group of ``engine``.
 
-    params[g]: dict with (B,) tensors 'taurad', 'taudrag', 'DPhieq', 'Phibar'
-    (the other per-member scalars are set beforehand with engine.set_params);
+    params[g]: dict with (B,) tensors (or scalars) 'taurad', 'taudrag', 'DPhieq',
+    'Phibar', and optionally 'a', 'dt', 'K6', 'K6Phi', 'omega' (absent ones keep
+    the values set with engine.set_params and get no gradient);
     ics[g]: (5, B, J, I) physical eta, delta, Phi, U, V.  Returns per group a
     (5, B, J, I) tensor of the final physical curr fields.  Passing the same
     ``integration`` object across calls reuses its checkpoint buffers and the
@@ -205,8 +240,13 @@ def integrate(engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, params: Se
     integ = integration if integration is not None else Integration(engine, flags, t0, nsteps, ckpt_every, store)
     flat = []
     for g, gd in enumerate(engine.groups):
-        for k in GRAD_PARAMS:
-            v = torch.as_tensor(params[g][k], device=engine.device, dtype=torch.float64)
+        for row, k in enumerate(_lib.TANGENT_PARAMS):
+            if k in params[g]:
+                v = torch.as_tensor(params[g][k], device=engine.device, dtype=torch.float64)
+            elif k in GRAD_PARAMS:
+                raise KeyError(f"params[{g}] needs {k!r}")
+            else:
+                v = gd["params"][PARAM_ROW[k]].clone()
             flat.append(v.expand(gd["B"]) if v.dim() == 0 else v)
         flat.append(ics[g])
     return list(_IntegrateFn.apply(integ, *flat))

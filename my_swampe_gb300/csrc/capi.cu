@@ -58,10 +58,10 @@ CoefTables<T> plan_coefs(const swp_plan* p, int g) {
 // Refresh the coefficient tables from the members' parameters: first launch of
 // every call that runs step kernels.
 template <typename T>
-int update_coefs(swp_plan* p, const swp_group_state* st, cudaStream_t s) {
+int update_coefs(swp_plan* p, const swp_group_state* st, cudaStream_t s, const swp_group_tangent* tan = nullptr) {
   for (int g = 0; g < p->ng; ++g) {
     cudaError_t e = launch_coefs<T>(st[g].params, p->geom[g].onemu2, p->M[g], p->B[g], p->geom[g].J,
-                                    plan_coefs<T>(p, g), s);
+                                    plan_coefs<T>(p, g), s, tan ? tan[g].dparams : nullptr);
     if (e != cudaSuccess) return cuda_check(p, e, "coefficient kernel launch");
   }
   return SWP_OK;
@@ -87,6 +87,7 @@ SpecLaunch<T> make_spec(const swp_plan* p, const swp_group_state* st, int& nbloc
     CoefTables<T> C = plan_coefs<T>(p, g);
     G.nco = C.nco;
     G.jco = C.jco;
+    G.djco = C.djco;
     G.mco = C.mco;
     L.prefix[g] = acc;
     acc += (p->M[g] + 1) * G.ntb;
@@ -375,8 +376,9 @@ int tangent_steps(swp_plan* p, const swp_group_state* st, const swp_group_tangen
   }
   StepCfg cfg = make_cfg(f);
   cfg.diagnostics = 0;
+  for (int g = 0; g < p->ng; ++g) cfg.tl_coef |= tan[g].coef_tangents != 0;
   if (nsteps > 0) {
-    int rc = update_coefs<T>(p, st, s);
+    int rc = update_coefs<T>(p, st, s, tan);
     if (rc) return rc;
   }
   for (int k = 0; k < nsteps; ++k) {
@@ -409,6 +411,7 @@ int tangent_forward_impl(swp_plan* p, const swp_group_state* st, const swp_group
     key.push_back((uint64_t)tan[g].fourier);
     key.push_back((uint64_t)tan[g].resid);
     key.push_back((uint64_t)tan[g].dparams);
+    key.push_back((uint64_t)(tan[g].coef_tangents != 0));
   }
   return run_graph(p, key, [&](cudaStream_t cs) { return tangent_steps<T>(p, st, tan, f, t0, nsteps, cs); }, s);
 }

@@ -10,6 +10,8 @@
 //   time_stepping.py:491-534   tstepcoeff, tstepcoeff2, tstepcoeffmn
 //   modEuler_tdiff.py:80-261, explicit_tdiff.py:62-226  scalar factors
 //   spectral_transform.py:577-594  a / (n(n+1)), omega / sqrt(0.375)
+// and, for a tangent-linear call, the derivatives of all of them along the
+// members' parameter tangents (a, dt, K6, K6Phi, omega, Phibar).
 #include <algorithm>
 #include "swp_internal.h"
 
@@ -17,7 +19,7 @@ namespace swp {
 
 template <typename T>
 __global__ void k_coefs(const double* __restrict__ par, const double* __restrict__ onemu2, int M, int B, int J,
-                        CoefTables<T> C) {
+                        CoefTables<T> C, const double* __restrict__ dpar) {
   const int cnt = M + 1;
   const int n_nco = B * cnt, n_jco = B * J;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_nco + n_jco + B; t += gridDim.x * blockDim.x) {
@@ -37,10 +39,27 @@ __global__ void k_coefs(const double* __restrict__ par, const double* __restrict
       C.nco[NC_TC * qs + o] = (T)((n == 0) ? 0.0 : a / ((double)n * (n + 1)));
       C.nco[NC_SIGX * qs + o] = (T)exp(-(2.0 * dt * K6) * fmax(ncoeff - 8.0 / a6, 0.0));
       C.nco[NC_SIGPX * qs + o] = (T)exp(-(2.0 * dt * K6P) * ncoeff);
+      // tangents: sigma = 1/(1+x) -> -sigma^2 dx, with x = 2 dt K6 r, r ~ a^-6
+      double dsig = 0.0, dsigp = 0.0, dtc = 0.0;
+      if (dpar) {
+        const double da = dpar[T_A * B + b], ddt = dpar[T_DT * B + b];
+        const double dK6 = dpar[T_K6 * B + b], dK6P = dpar[T_K6PHI * B + b];
+        const double r = ncoeff - 8.0 / a6, s1 = 1.0 / (1.0 + x), s2 = 1.0 / (1.0 + xp);
+        const double dx = 2.0 * ddt * K6 * r + 2.0 * dt * dK6 * r - 6.0 * (da / a) * x;
+        const double dxp = 2.0 * ddt * K6P * ncoeff + 2.0 * dt * dK6P * ncoeff - 6.0 * (da / a) * xp;
+        dsig = -s1 * s1 * dx;
+        dsigp = -s2 * s2 * dxp;
+        dtc = (n == 0) ? 0.0 : da / ((double)n * (n + 1));
+      }
+      C.nco[NC_DSIG * qs + o] = (T)dsig;
+      C.nco[NC_DSIGP * qs + o] = (T)dsigp;
+      C.nco[NC_DTC * qs + o] = (T)dtc;
     } else if (t < n_nco + n_jco) {
       const int u = t - n_nco, b = u / J, j = u % J;
       const double a = par[P_A * B + b], dt = par[P_DT * B + b];
-      C.jco[u] = (T)((2.0 * dt) / (a * onemu2[j]));
+      const double tsc = (2.0 * dt) / (a * onemu2[j]);
+      C.jco[u] = (T)tsc;
+      C.djco[u] = (T)(dpar ? (2.0 * dpar[T_DT * B + b]) / (a * onemu2[j]) - tsc * dpar[T_A * B + b] / a : 0.0);
     } else {
       const int b = t - n_nco - n_jco;
       const double a = par[P_A * B + b], dt = par[P_DT * B + b], Pb = par[P_PHIBAR * B + b];
@@ -66,21 +85,36 @@ __global__ void k_coefs(const double* __restrict__ par, const double* __restrict
       mc[MC_RAWM * B + b] = (T)(al * wa);
       mc[MC_RAWN * B + b] = (T)(al * (1.0 - wa));
       mc[MC_PB * B + b] = (T)Pb;
+      double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (dpar) {
+        const double da = dpar[T_A * B + b], ddt = dpar[T_DT * B + b], dPb = dpar[T_PHIBAR * B + b];
+        const double dom = dpar[T_OMEGA * B + b], a3 = a * a * a;
+        v[0] = (2.0 * ddt / (a * a) - 4.0 * dt * da / a3) / 4.0;  // (2 dt / a^2) / 4
+        v[1] = -2.0 * da / a3;                                    // 1 / a^2
+        v[2] = dPb * 0.5;                                          // Phibar / 2
+        v[3] = ddt * Pb + dt * dPb;                                // dt Phibar
+        v[4] = dPb / (a * a) - 2.0 * Pb * da / a3;                 // Phibar / a^2
+        v[5] = (ddt / 2.0) / (a * a) - dt * da / a3;               // (dt / 2) / a^2
+        v[6] = ddt;                                                // dt
+        v[7] = dom / sqrt(0.375);                                  // omega / sqrt(0.375)
+      }
+      const int dr[8] = {MC_DT2, MC_DIA2, MC_DHPB, MC_DDTPB, MC_DPBA2, MC_DPFD, MC_DDT, MC_DOM};
+      for (int q = 0; q < 8; ++q) mc[dr[q] * B + b] = (T)v[q];
     }
   }
 }
 
 template <typename T>
 cudaError_t launch_coefs(const double* par, const double* onemu2, int M, int B, int J, const CoefTables<T>& C,
-                         cudaStream_t s) {
+                         cudaStream_t s, const double* dpar) {
   const int total = B * (M + 1) + B * J + B;
   const int nb = std::min((total + 255) / 256, 1216);
-  k_coefs<T><<<nb, 256, 0, s>>>(par, onemu2, M, B, J, C);
+  k_coefs<T><<<nb, 256, 0, s>>>(par, onemu2, M, B, J, C, dpar);
   return cudaGetLastError();
 }
 template cudaError_t launch_coefs<double>(const double*, const double*, int, int, int, const CoefTables<double>&,
-                                          cudaStream_t);
+                                          cudaStream_t, const double*);
 template cudaError_t launch_coefs<float>(const double*, const double*, int, int, int, const CoefTables<float>&,
-                                         cudaStream_t);
+                                         cudaStream_t, const double*);
 
 }  // namespace swp

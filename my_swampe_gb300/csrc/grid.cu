@@ -237,6 +237,19 @@ struct GridCtx {
   T invI;
 };
 
+// Unforced runs (test 1, 2): the forcing terms PhiF, F, G are zero
+// (model.py:601-603).  Written explicitly for the CTA's rows, since an
+// out-of-place step or a caller's fresh buffer would leave them undefined.
+template <typename T, typename C>
+__device__ __forceinline__ void zero_forcing_rows(const C& c, typename cplx<T>::type* four) {
+  typedef typename cplx<T>::type T2;
+  constexpr int n1 = C::M + 1;
+  for (int t = threadIdx.x; t < 3 * n1 * C::JB; t += blockDim.x) {
+    const int r = t % C::JB, k = (t / C::JB) % n1, q = t / (C::JB * n1);
+    four[(F_PHIF + q) * c.FS + ((size_t)k * c.B + c.b) * C::J + c.j0 + r] = mk<T2>(0, 0);
+  }
+}
+
 // Stage the rows j0..j0+JB-1 of `nf` Fourier fields of member b into `stage`
 // ([f][r][m], m fastest; the global reads are JB-long contiguous runs).  The
 // field pointers go through a shared-memory table rather than a local array.
@@ -560,6 +573,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
 #pragma unroll
     for (int q = 0; q < 8; ++q) dst[q] = G.four + (F_A + q) * FS;
     write_r2c<T>(c, res, nout, dst, invI, invI);
+    if (!ph.forced) zero_forcing_rows<T>(c, G.four);
     return;
   }
 
@@ -715,6 +729,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
 #pragma unroll
     for (int q = 0; q < 8; ++q) dst[q] = G.four + (F_A + q) * FS;
     write_r2c<T>(c, res2, nout, dst, invI, invI);
+    if (!ph.forced) zero_forcing_rows<T>(c, G.four);
     return;
   }
 

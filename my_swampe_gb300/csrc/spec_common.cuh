@@ -193,14 +193,14 @@ __device__ __forceinline__ void step_combos_ld(const SpecGroup<T>& G, const Step
 }
 
 // Tangent-linear step (modified Euler): the combined inputs are linear in the
-// state with Phibar in their coefficients (modEuler_tdiff.py:95-103, 185-193),
-// so their tangent is step_combos on the tangent state plus dPhibar times the
-// Phibar-derivative of those coefficients on the primal state `Fp` before the
-// step: Phi takes -dt delta - (tstep/8) i m Beff, -(tstep/8) Aeff on H and
-// -(E tstep2/4 + Phi / a^2) / 2 with n(n+1); delta takes -delta / a^2 with n(n+1).
+// state, with coefficients that depend on the parameters (modEuler_tdiff.py:
+// 72-110, 162-201, 253-261): their tangent is step_combos on the tangent state
+// plus the tangents of the coefficients (the call's tables: tstepcoeff and the
+// scalar factors, along the members' tangents of a, dt and Phibar) times the
+// primal state before the step, `four_p`.
 template <typename T>
-__device__ __forceinline__ void tangent_phibar_terms(const SpecGroup<T>& G, const StepCfg& cfg, int m, int b, int j,
-                                                     size_t FS, T dPb, typename cplx<T>::type* c) {
+__device__ __forceinline__ void tangent_coef_terms(const SpecGroup<T>& G, const StepCfg& cfg, int m, int b, int j,
+                                                   size_t FS, typename cplx<T>::type* c) {
   typedef typename cplx<T>::type T2;
   constexpr int NSPX = SlotCount<T>::NP;
   const T2* Fp = G.four_p;
@@ -208,18 +208,36 @@ __device__ __forceinline__ void tangent_phibar_terms(const SpecGroup<T>& G, cons
   const T* mc = G.mco;
   const int B = G.B;
   const T xm = (T)m;
-  const T t1 = G.jco[(size_t)b * G.g.J + j] * (T)0.25;
+  const T tsc = G.jco[(size_t)b * G.g.J + j], dtsc = G.djco[(size_t)b * G.g.J + j];
+  const T t1 = tsc * (T)0.25, dt1 = dtsc * (T)0.25;
+  const T dte = cfg.forcflag ? dtsc : dtsc * (T)0.5;
+  const T t2 = mc[MC_T2 * B + b], ia2 = mc[MC_IA2 * B + b], hPb = mc[MC_HPB * B + b];
+  const T dt2 = mc[MC_DT2 * B + b], dia2 = mc[MC_DIA2 * B + b], dhPb = mc[MC_DHPB * B + b];
   const T2 del = Fp[F_DELTA * FS + o], phi = Fp[F_PHI * FS + o], E = Fp[F_E * FS + o];
-  T2 A = Fp[F_A * FS + o], Bm = Fp[F_B * FS + o];
-  if (cfg.forcflag) {
-    A = csub(A, Fp[F_G * FS + o]);
-    Bm = cadd(Bm, Fp[F_F * FS + o]);
-  }
-  const T ia2 = mc[MC_IA2 * B + b], half = (T)0.5 * dPb;
-  c[SP_PHI1] = csub(c[SP_PHI1], cadd(cscale(del, mc[MC_DT * B + b] * dPb), cscale(imul(xm, Bm), half * t1)));
-  c[NSPX + SH_PHI1] = csub(c[NSPX + SH_PHI1], cscale(A, half * t1));
-  c[SP_PHI2] = csub(c[SP_PHI2], cscale(cadd(cscale(E, mc[MC_T2 * B + b]), cscale(phi, ia2)), half));
-  c[SP_D2] = csub(c[SP_D2], cscale(del, dPb * ia2));
+  const T2 C = Fp[F_C * FS + o], D = Fp[F_D * FS + o];
+  const T2 A = Fp[F_A * FS + o], Bm = Fp[F_B * FS + o], Fm = Fp[F_F * FS + o], Gm = Fp[F_G * FS + o];
+  const T2 Bf = cadd(Bm, Fm), Af = csub(A, Gm);
+  const T2 Beff = cfg.forcflag ? Bf : Bm, Aeff = cfg.forcflag ? Af : A;
+  const T dht = dhPb * t1 + hPb * dt1;  // d(hPb t1)
+  // Phi
+  T2 p1 = cadd(cscale(imul(xm, C), dt1), cscale(del, mc[MC_DDTPB * B + b]));
+  p1 = cadd(p1, cscale(imul(xm, Beff), dht));
+  c[SP_PHI1] = csub(c[SP_PHI1], p1);
+  if (cfg.forcflag) c[SP_PHI1] = cadd(c[SP_PHI1], cscale(Fp[F_PHIF * FS + o], mc[MC_DDT * B + b]));
+  c[NSPX + SH_PHI1] = cadd(c[NSPX + SH_PHI1], csub(cscale(D, dt1), cscale(Aeff, dht)));
+  c[SP_PHI2] = csub(c[SP_PHI2], cadd(cscale(E, dt2 * hPb + t2 * dhPb), cscale(phi, dia2 * hPb + ia2 * dhPb)));
+  // delta
+  c[SP_D1] = cadd(c[SP_D1], cscale(imul(xm, Bf), dt1));
+  c[NSPX + SH_D1] = cadd(c[NSPX + SH_D1], cscale(Af, dt1));
+  const T q = (T)0.5 * (dt1 * ia2 + t1 * dia2);  // d(t1 ia2 / 2)
+  T2 d2 = cadd(cscale(cadd(phi, E), dt2), cscale(imul(xm, C), q));
+  d2 = csub(d2, cscale(del, mc[MC_DPBA2 * B + b]));
+  if (cfg.forcflag) d2 = cadd(d2, cscale(Fp[F_PHIF * FS + o], mc[MC_DPFD * B + b]));
+  c[SP_D2] = cadd(c[SP_D2], d2);
+  c[NSPX + SH_D2] = cadd(c[NSPX + SH_D2], cscale(D, q));
+  // eta
+  c[SP_E1] = csub(c[SP_E1], cscale(imul(xm, Aeff), dte));
+  c[NSPX + SH_E1] = cadd(c[NSPX + SH_E1], cscale(Beff, dte));
 }
 
 // step_combos_ld on the state in global memory

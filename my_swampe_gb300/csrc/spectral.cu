@@ -92,6 +92,14 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
     sdead[bt] = dead;
   }
 
+  // Tangent-linear step with coefficient tangents (a, dt, K6, K6Phi, omega): a
+  // first pass transforms the primal combined inputs of the pre-step state; the
+  // tangent's hyperdiffusion and wind-inversion terms multiply those spectra
+  // (kept per (n, member component) in Kin slots 0-2, which only their owner
+  // thread writes).
+  const bool tl_coef = mode == 3 && cfg.tl_coef;
+  for (int pass = tl_coef ? 0 : 1; pass < 2; ++pass) {
+  const bool prim = pass == 0;
   // ---- phase 1: combined, symmetrised inputs
   const T2* F = G.four;
   for (int t = threadIdx.x; t < MT * Jh; t += blockDim.x) {
@@ -103,8 +111,14 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
       for (int side = 0; side < 2; ++side) {
         int j = side ? (J - 1 - jp) : jp;
         T2 c[NSLOT];
-        step_combos<T>(G, cfg, mode == 3 ? 0 : mode, incr, m, b, j, FS, c);
-        if (mode == 3) tangent_phibar_terms<T>(G, cfg, m, b, j, FS, (T)G.dpar[G_PHIBAR * G.B + b], c);
+        if (prim) {
+          const T2* Fq = G.four_p;
+          const size_t o = ((size_t)m * G.B + b) * J + j;
+          step_combos_ld<T>(G, cfg, 0, incr, m, b, j, [&](int f) { return Fq[f * FS + o]; }, c);
+        } else {
+          step_combos<T>(G, cfg, mode == 3 ? 0 : mode, incr, m, b, j, FS, c);
+          if (mode == 3) tangent_coef_terms<T>(G, cfg, m, b, j, FS, c);
+        }
         if (side == 0) {
 #pragma unroll
           for (int q = 0; q < NSLOT; ++q) { xs[q] = c[q]; xa[q] = c[q]; }
@@ -179,8 +193,10 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
         }
       }
       const int bt = r >> 1, comp = r & 1;
-      // planetary vorticity f_{0,1}: a constant of the wind inversion, absent from its tangent
-      const T om = (bt < mt && mode != 3) ? G.mco[MC_OM * G.B + b0 + bt] : (T)0;
+      // planetary vorticity f_{0,1}: a constant of the wind inversion; its
+      // tangent is the omega tangent's
+      const T om = bt < mt ? G.mco[(mode == 3 ? MC_DOM : MC_OM) * G.B + b0 + bt] : (T)0;
+      const T om_p = (tl_coef && bt < mt) ? G.mco[MC_OM * G.B + b0 + bt] : (T)0;
       // semi-implicit solve constants (semi_implicit_tdiff.py): implicit share
       // xi, implicit drag / relaxation kd, kr, explicit drag gd, Phibar, 1/a^2
       T si_xi = (T)0, si_kd = (T)0, si_kr = (T)0, si_gd = (T)0, si_pb = (T)0, si_ia2 = (T)0;
@@ -204,8 +220,25 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
         int n = m + kk;
         T nn1 = (T)(n * (n + 1));
         T s = sig[bt * cntmax + kk], sp = sigP[bt * cntmax + kk], tc = tcmn[bt * cntmax + kk];
+        const int pc = par ? C0 + c : c;
+        if (prim) {
+          // primal pre-step spectra (incremental form: curr + tendency part)
+          T sphi = acc[SP_PHI1][k] + acc[NSPX + SH_PHI1][k] + nn1 * acc[SP_PHI2][k];
+          T sdel = acc[SP_D1][k] + acc[NSPX + SH_D1][k] + nn1 * (acc[SP_D2][k] + acc[NSPX + SH_D2][k]);
+          T seta = acc[SP_E1][k] + acc[NSPX + SH_E1][k];
+          if (incr) {
+            sphi += acc[NSPX > SP_IPHI ? SP_IPHI : 0][k];
+            sdel += acc[NSPX > SP_ID ? SP_ID : 0][k];
+            seta += acc[NSPX > SP_IE ? SP_IE : 0][k];
+          }
+          Kin[((size_t)0 * cntmax + pc) * R + r] = seta;
+          Kin[((size_t)1 * cntmax + pc) * R + r] = sdel;
+          Kin[((size_t)2 * cntmax + pc) * R + r] = sphi;
+          continue;
+        }
         T cphi, cdel, ceta;      // spectral eta, delta (full, for the winds)
         T kphi, kdel, keta;      // what the inverse transform turns into the new Fourier carries
+        T pce = (T)0, pcd = (T)0;  // primal spectral eta, delta after hyperdiffusion (tl_coef)
         if (mode == 2) {
           ceta = acc[SP_E1][k];
           cdel = acc[SP_D1][k];
@@ -251,13 +284,30 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
             ceta = s * seta;
             kphi = cphi; kdel = cdel; keta = ceta;
           }
+          if (tl_coef && bt < mt) {
+            // hyperdiffusion tangent: d(sigma) times the primal spectra
+            const size_t qs = (size_t)G.B * cntmax, qo = (size_t)(b0 + bt) * cntmax + n;
+            const T dsg = G.nco[NC_DSIG * qs + qo], dsp = G.nco[NC_DSIGP * qs + qo];
+            const T pe = Kin[((size_t)0 * cntmax + pc) * R + r], pd = Kin[((size_t)1 * cntmax + pc) * R + r];
+            const T pp = Kin[((size_t)2 * cntmax + pc) * R + r];
+            cphi += dsp * pp; cdel += dsg * pd; ceta += dsg * pe;
+            kphi += dsp * pp; kdel += dsg * pd; keta += dsg * pe;
+            pce = s * pe;
+            pcd = s * pd;
+          }
         }
         // wind inversion inputs (spectral_transform.py:577-594)
         T dp = (n == 0) ? (T)0 : cdel;
         T ep = (n == 0) ? (T)0 : ceta;
         if (m == 0 && n == 1 && comp == 0) ep -= om;
         T es = ep * tc, ds = dp * tc;
-        int pc = par ? C0 + c : c;
+        if (tl_coef && bt < mt) {  // tangent of a/(n(n+1)) times the primal (eta - f), delta
+          const T dtc = G.nco[(size_t)NC_DTC * G.B * cntmax + (size_t)(b0 + bt) * cntmax + n];
+          T epp = (n == 0) ? (T)0 : pce;
+          if (m == 0 && n == 1 && comp == 0) epp -= om_p;
+          es += epp * dtc;
+          ds += ((n == 0) ? (T)0 : pcd) * dtc;
+        }
         Kin[((size_t)0 * cntmax + pc) * R + r] = keta;
         Kin[((size_t)1 * cntmax + pc) * R + r] = kdel;
         Kin[((size_t)2 * cntmax + pc) * R + r] = kphi;
@@ -276,6 +326,7 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
     }
   }
   __syncthreads();
+  }  // pass
   // ---- phase 4: inverse basis block for m
   {
     const T* srcP = g.P_i + g.boff[m];

@@ -308,6 +308,7 @@ struct StepCfg {
   int raw;         // Robert-Asselin-Williams filter: the new level moves too
   int si_relax;    // semi-implicit: relaxation and drag implicit (forcflag, test None)
   int si_lag_init; // semi-implicit first step: lagged remainder from the current state
+  int tl_coef;     // tangent-linear step: differentiate the coefficient tables too
 };
 
 }  // namespace swp

@@ -20,6 +20,9 @@ enum MemberScalar { MS_WCURR = 0, MS_WMID, MS_DEAD, MS_UPDATED, NMEMBER };
 enum DiagIndex { D_RMS2 = 0, D_SPIN, D_PHIMIN, D_PHIMAX, D_DEAD, NDIAG };
 // Parameter gradients accumulated by the adjoint.
 enum GradIndex { G_TAURAD = 0, G_TAUDRAG, G_DPHIEQ, G_PHIBAR, NGRAD };
+// Parameter tangents of the tangent-linear model: the adjoint's four, then
+// those that enter only the coefficient tables.
+enum TangentIndex { T_TAURAD = 0, T_TAUDRAG, T_DPHIEQ, T_PHIBAR, T_A, T_DT, T_K6, T_K6PHI, T_OMEGA, NTANGENT };
 
 struct GroupGeom {
   int M = 0, J = 0, I = 0, L = 0;
@@ -75,7 +78,11 @@ constexpr int MAXG = 4;
 //                     (filters.py:154-213)
 //   jco[b][j]      tstepcoeff = 2 dt / (a (1 - mu_j^2)) (time_stepping.py:491-500)
 //   mco[q][b]      scalar factors of the tendencies (modEuler_tdiff.py, explicit_tdiff.py)
-enum NCoef { NC_SIG = 0, NC_SIGP, NC_SIGM1, NC_SIGPM1, NC_TC, NC_SIGX, NC_SIGPX, NNCO };
+enum NCoef {
+  NC_SIG = 0, NC_SIGP, NC_SIGM1, NC_SIGPM1, NC_TC, NC_SIGX, NC_SIGPX,
+  NC_DSIG, NC_DSIGP, NC_DTC,  // tangents of sigma, sigmaPhi, a/(n(n+1)) (tangent-linear launches)
+  NNCO
+};
 enum MCoef {
   MC_DT = 0,   // dt
   MC_T2,       // (2 dt / a^2) / 4
@@ -96,23 +103,30 @@ enum MCoef {
   MC_RAWM,     // alpha williams_alpha       (RAW: displacement of the mid level)
   MC_RAWN,     // alpha (1 - williams_alpha) (RAW: displacement of the new level)
   MC_PB,       // Phibar
+  // tangents of the step factors along the call's parameter tangents (tangent-linear launches)
+  MC_DT2, MC_DIA2, MC_DHPB, MC_DDTPB, MC_DPBA2, MC_DPFD, MC_DDT, MC_DOM,
   NMCO
 };
 template <typename T>
 struct CoefTables {
   T* nco = nullptr;   // [NNCO][B][M+1]
   T* jco = nullptr;   // [B][J]
+  T* djco = nullptr;  // [B][J] tangent of tstepcoeff
   T* mco = nullptr;   // [NMCO][B]
-  static size_t count(int M, int B, int J) { return (size_t)NNCO * B * (M + 1) + (size_t)B * J + (size_t)NMCO * B; }
+  static size_t count(int M, int B, int J) {
+    return (size_t)NNCO * B * (M + 1) + (size_t)2 * B * J + (size_t)NMCO * B;
+  }
   void carve(T* base, int M, int B, int J) {
     nco = base;
     jco = nco + (size_t)NNCO * B * (M + 1);
-    mco = jco + (size_t)B * J;
+    djco = jco + (size_t)B * J;
+    mco = djco + (size_t)B * J;
   }
 };
+// dpar: [NTANGENT][B] parameter tangents, or null (the tangent rows are then zero)
 template <typename T>
 cudaError_t launch_coefs(const double* par, const double* onemu2, int M, int B, int J, const CoefTables<T>& C,
-                         cudaStream_t s);
+                         cudaStream_t s, const double* dpar = nullptr);
 
 // --------------------------------------------------------------- spectral ---
 template <typename T>
@@ -131,6 +145,7 @@ struct SpecGroup {
   const double* dpar;                   // tangent-linear launches: [NGRAD][B] parameter tangents
   const T* nco;                         // coefficient tables of the call (CoefTables)
   const T* jco;
+  const T* djco;
   const T* mco;
 };
 

@@ -328,19 +328,23 @@ class Engine:
 
     # ----------------------------------------------------------- tangent-linear
     def new_tangent_buffers(self):
-        """Per group: tangent Fourier state, tangent IC residual, (4, B) parameter tangents
-        (d taurad, d taudrag, d DPhieq, d Phibar)."""
+        """Per group: tangent Fourier state, tangent IC residual, (NTANGENT, B) parameter
+        tangents in the order of ``_lib.TANGENT_PARAMS``."""
         four = [torch.zeros_like(gd["fourier"]) for gd in self.groups]
         resid = [torch.zeros_like(gd["resid"]) for gd in self.groups]
-        dpar = [torch.zeros((_lib.NGRAD, gd["B"]), dtype=torch.float64, device=self.device) for gd in self.groups]
+        dpar = [torch.zeros((_lib.NTANGENT, gd["B"]), dtype=torch.float64, device=self.device) for gd in self.groups]
         return four, resid, dpar
 
     def _tans(self, tfour, tresid, dpar) -> ctypes.Array:
         arr = (_lib.GroupTangent * len(self.groups))()
         for g in range(len(self.groups)):
+            if tuple(dpar[g].shape) != (_lib.NTANGENT, self.groups[g]["B"]) or dpar[g].dtype != torch.float64:
+                raise ValueError(f"parameter tangents must be float64 ({_lib.NTANGENT}, B)")
             arr[g].fourier = tfour[g].data_ptr()
             arr[g].resid = tresid[g].data_ptr()
             arr[g].dparams = dpar[g].data_ptr()
+            # rows a..omega enter only the coefficient tables: their pass runs when one is set
+            arr[g].coef_tangents = int(bool(torch.any(dpar[g][_lib.NGRAD:] != 0)))
         return arr
 
     def tangent_init(self, flags: RunFlagsC, ics, dics, tfour, tresid, dpar) -> None:

@@ -327,8 +327,9 @@ def run_model_scan(
     reference (``model.py:1345-1765``); ``remat_step``, ``jit_scan`` and
     ``donate_state`` are accepted for compatibility and have no effect (the
     scan body is always a compiled kernel pair and the state is updated in
-    place).  Tensors among taurad, taudrag, DPhieq, Phibar and the ``*_init``
-    fields that require grad (or carry forward-mode tangents) make the
+    place).  Tensors among taurad, taudrag, DPhieq, Phibar, a, dt, K6, K6Phi,
+    omega, alpha, g and the ``*_init`` fields that require grad (or carry
+    forward-mode tangents) make the
     ``last_state`` curr fields (eta, delta, Phi, U, V) differentiable through
     the hand-written adjoint and tangent-linear kernels, the counterpart of
     ``jax.grad`` / ``jax.jvp`` through the reference's scan.  ``semi_implicit`` selects the semi-implicit leapfrog
@@ -400,12 +401,17 @@ def run_model_scan(
             if shp != (J, I) and not (batched and shp == (B, J, I)):
                 raise ValueError(f"{name} must have shape {(J, I)}, got {shp}.")
 
-    # differentiable inputs (the parameters the adjoint and the tangent model cover)
-    diff_inputs = (taurad, taudrag, DPhieq, Phibar, eta0_init, delta0_init, Phi0_init, U0_init, V0_init)
+    # differentiable inputs: the per-member parameters the adjoint and the tangent
+    # model cover, the initial fields, and alpha and g, which the curr fields of
+    # the modified-Euler scheme do not depend on (their derivative is zero)
+    # K6Phi=None means K6Phi = K6 (model.py:512): then K6 drives both
+    coef_inputs = dict(a=a, dt=dt, K6=K6, K6Phi=K6 if K6Phi is None else K6Phi, omega=omega)
+    diff_inputs = (taurad, taudrag, DPhieq, Phibar, eta0_init, delta0_init, Phi0_init, U0_init, V0_init, alpha, g,
+                   *coef_inputs.values())
     needs_grad = any(_tracked(x) for x in diff_inputs)
-    if any(_tracked(x) for x in (dt, a, omega, g, K6, K6Phi, alpha, si_alpha, williams_alpha)):
-        raise NotImplementedError("derivatives are implemented with respect to taurad, taudrag, DPhieq, Phibar "
-                                  "and the initial fields")
+    if any(_tracked(x) for x in (si_alpha, williams_alpha)):
+        raise NotImplementedError("derivatives through the semi-implicit scheme and the RAW filter are not "
+                                  "implemented")
     if needs_grad:
         if semi_implicit or raw_filter or expflag or test == 1:
             raise NotImplementedError("derivatives are implemented for the modified-Euler scheme with the classic "
@@ -419,8 +425,9 @@ def run_model_scan(
     eng.set_params(0, dt=dt, a=a, omega=omega, Phibar=Phibar, taurad=taurad, taudrag=taudrag,
                    DPhieq=DPhieq if test is None else 0.0, K6=K6, K6Phi=K6Phi_eff, alpha=alpha,
                    si_alpha=si_alpha, williams_alpha=williams_alpha)
-    static = build_static(M=M, dt=dt, a=a, omega=omega, g=g, Phibar=Phibar, taurad=taurad, taudrag=taudrag,
-                          DPhieq=DPhieq, K6=K6, K6Phi=K6Phi, test=test, engine=eng)
+    nd = lambda x: x.detach() if torch.is_tensor(x) else x  # noqa: E731  (the Static record holds values)
+    static = build_static(M=M, dt=nd(dt), a=nd(a), omega=nd(omega), g=nd(g), Phibar=nd(Phibar), taurad=nd(taurad),
+                          taudrag=nd(taudrag), DPhieq=nd(DPhieq), K6=nd(K6), K6Phi=nd(K6Phi), test=test, engine=eng)
 
     if have_ic:
         eta0 = _prepare_ic(eta0_init, J, I, B, batched, "eta0_init", dev)
@@ -434,14 +441,25 @@ def run_model_scan(
     elif not contflag:
         if batched and not all(_is_python_scalar(v) for v in (a, omega, Phibar)):
             raise ValueError("analytic initial conditions need scalar a, omega and Phibar; pass *_init fields instead")
-        pb = float(Phibar.detach()) if torch.is_tensor(Phibar) else float(Phibar)
-        fields = _analytic_ic(M, float(a), float(omega), pb, test, float(a1), dev)
+        val = lambda x: float(x.detach()) if torch.is_tensor(x) else float(x)  # noqa: E731
+        av, omv, pb = val(a), val(omega), val(Phibar)
+        fields = _analytic_ic(M, av, omv, pb, test, float(a1), dev)
         eta0, delta0, Phi0, U0, V0 = (f.expand(B, J, I) for f in fields)
-        if _tracked(Phibar):
-            # the analytic Phi0 is linear in Phibar (initial_conditions.py:160-166):
-            # carry its derivative into the differentiable run
-            unit = _analytic_ic(M, float(a), float(omega), pb + 1.0, test, float(a1), dev)[2] - fields[2]
-            Phi0 = Phi0 + (Phibar - Phibar.detach()) * unit.expand(B, J, I)
+        # the analytic fields are polynomials of degree <= 2 in a, omega, Phibar
+        # (initial_conditions.py:18-47, 88-239), so a centred difference is their
+        # exact derivative: carry it into the differentiable run
+        for x, i in ((a, 0), (omega, 1), (Phibar, 2)):
+            if _tracked(x):
+                h = 1e-3 * abs((av, omv, pb)[i]) or 1e-3
+                arg = [av, omv, pb]
+                arg[i] += h
+                fp = _analytic_ic(M, *arg, test, float(a1), dev)
+                arg[i] -= 2 * h
+                fm = _analytic_ic(M, *arg, test, float(a1), dev)
+                d = [(u - v) / (2 * h) for u, v in zip(fp, fm)]
+                dx = x - x.detach()
+                eta0, delta0, Phi0, U0, V0 = (f + dx * dd.expand(B, J, I)
+                                              for f, dd in zip((eta0, delta0, Phi0, U0, V0), d))
     else:
         fields = []
         for name in ("eta", "delta", "Phi"):
@@ -483,7 +501,13 @@ def run_model_scan(
                            diagnostics=False, t_start=starttime_eff)
         dpar = dict(taurad=_per_member(taurad, B, dev), taudrag=_per_member(taudrag, B, dev),
                     DPhieq=_per_member(DPhieq if test is None else 0.0, B, dev), Phibar=_per_member(Phibar, B, dev))
+        for k, x in coef_inputs.items():
+            if _tracked(x):
+                dpar[k] = _per_member(x, B, dev)
         dcurr = adjoint.integrate(eng, dflags, starttime_eff, T, [dpar], [ics])[0]
+        for x in (alpha, g):  # zero derivative, but part of the graph
+            if _tracked(x):
+                dcurr = dcurr + 0.0 * x.to(dcurr.dtype).sum()
         if return_history or diagnostics:  # the gated run's state (dead flags included)
             four.copy_(saved[0])
             gd["member"].copy_(saved[1])

@@ -146,3 +146,38 @@ def test_stored_states_adjoint_matches_checkpointed(cuda, precision):
     np.testing.assert_array_equal(ic_a, ic_c)
     for k in g_a:
         assert abs(g_a[k] - g_c[k]) <= 1e-12 * max(abs(g_c[k]), 1e-300), (k, g_a[k], g_c[k])
+
+
+def test_unforced_out_of_place_steps_ignore_stale_memory(cuda):
+    """Unforced (test = 2) runs: the out-of-place steps of the stored-states form
+    and of the checkpointed form's window recompute write zero forcing terms
+    instead of leaving a slot's previous contents (the caching allocator hands
+    back dirty memory): both forms give the in-place forward and one gradient."""
+    import torch
+    from my_swampe_gb300 import adjoint, run_model_scan_final
+    from my_swampe_gb300.engine import Engine, RunFlagsC
+    from my_swampe_gb300.model import _analytic_ic
+
+    kw = dict(M=42, dt=600.0, omega=7.2921159e-5, a=6.37122e6, test=2, forcflag=False, Phibar=3.0e3)
+    ref = run_model_scan_final(**kw, tmax=8)["last_state"]
+    f = _analytic_ic(42, 6.37122e6, 7.2921159e-5, 3.0e3, 2, 0.05, torch.device("cuda"))
+    grads = {}
+    for store in ("all", "checkpoint"):
+        junk = torch.full((64 * 1024 * 1024,), 1e30, dtype=torch.float64, device="cuda")  # 512 MB of garbage
+        del junk
+        eng = Engine([(42, 1)], "fp64")
+        eng.set_params(0, dt=600.0, a=6.37122e6, omega=7.2921159e-5, K6=1.24e33, K6Phi=1.24e33, alpha=0.01)
+        ics = torch.stack(f, 0)[:, None].clone().requires_grad_(True)
+        params = dict(taurad=torch.full((1,), 86400.0, dtype=torch.float64, device="cuda"),
+                      taudrag=torch.full((1,), 86400.0, dtype=torch.float64, device="cuda"),
+                      DPhieq=torch.zeros(1, dtype=torch.float64, device="cuda"),
+                      Phibar=torch.full((1,), 3.0e3, dtype=torch.float64, device="cuda"))
+        out = adjoint.integrate(eng, RunFlagsC(test=2, forcflag=False), 2, 6, [params], [ics], ckpt_every=2,
+                                store=store)[0]
+        for k, name in enumerate(("eta_curr", "delta_curr", "Phi_curr", "U_curr", "V_curr")):
+            want = getattr(ref, name)
+            err = float((out[k, 0] - want).abs().max())
+            assert err <= 1e-9 * float(want.abs().max()) + 1e-300, (store, name, err)
+        grads[store] = torch.autograd.grad((out ** 2).sum(), ics)[0]
+    assert bool(torch.all(torch.isfinite(grads["all"])))
+    torch.testing.assert_close(grads["all"], grads["checkpoint"], rtol=1e-10, atol=1e-300)

@@ -23,18 +23,32 @@ def _loss(name, theta, **extra):
 
 
 @pytest.mark.parametrize("name,value", [("DPhieq", 4.0e6), ("taurad", 86400.0), ("taudrag", 86400.0),
-                                        ("Phibar", 3.0e5)])
+                                        ("K6", 1.24e33), ("Phibar", 3.0e5), ("omega", 7.292e-5),
+                                        ("a", 6.37122e6), ("dt", 600.0), ("alpha", 0.01)])
 def test_grad_returns_finite_for_each_scalar_parameter(cuda, name, value):
-    """test_autodiff.py:56-86 for the parameters the adjoint covers."""
+    """test_autodiff.py:56-86, every parameter the reference lists.  alpha only
+    filters the prev level, so the curr-field loss has a zero derivative."""
     th = torch.tensor(value, dtype=torch.float64, device="cuda", requires_grad=True)
     g = torch.autograd.grad(_loss(name, th), th)[0]
-    assert g.shape == () and bool(torch.isfinite(g)) and float(g) != 0.0
+    assert g.shape == () and bool(torch.isfinite(g))
+    assert (float(g) == 0.0) if name == "alpha" else (float(g) != 0.0)
 
 
-def test_other_parameters_refuse_gradients(cuda):
-    th = torch.tensor(1.24e33, dtype=torch.float64, device="cuda", requires_grad=True)
+@pytest.mark.parametrize("name,value,rel_h", [("K6", 1.24e33, 1e-2), ("omega", 7.292e-5, 1e-4),
+                                              ("a", 6.37122e6, 1e-5), ("dt", 600.0, 1e-5)])
+def test_coefficient_parameter_gradients_match_finite_differences(cuda, name, value, rel_h):
+    th = torch.tensor(value, dtype=torch.float64, device="cuda", requires_grad=True)
+    g_ad = float(torch.autograd.grad(_loss(name, th), th)[0])
+    h = rel_h * value
+    with torch.no_grad():
+        g_fd = (float(_loss(name, value + h)) - float(_loss(name, value - h))) / (2 * h)
+    assert abs(g_ad - g_fd) <= 1e-4 * abs(g_fd), (name, g_ad, g_fd)
+
+
+def test_opt_in_scheme_parameters_refuse_gradients(cuda):
+    th = torch.tensor(0.5, dtype=torch.float64, device="cuda", requires_grad=True)
     with pytest.raises(NotImplementedError):
-        _loss("K6", th)
+        _loss("si_alpha", th, semi_implicit=True)
 
 
 def test_jvp_returns_finite_for_DPhieq(cuda):

@@ -28,10 +28,19 @@ def _setup(prec="fp64", B=2, test=None, seed=5):
     dics = (ics * w).contiguous()
     dics[2] += 1e-2 * wl["ics"][2].flip(-1)
     p = wl["params"]
-    dpar = torch.stack([0.1 * p["taurad"], 0.1 * p["taudrag"], 0.1 * p["DPhieq"],
-                        torch.full((B,), 0.05 * 3.0e5, dtype=torch.float64, device=eng.device)])
-    dpar = dpar * (torch.rand((4, B), generator=g, dtype=torch.float64).to(eng.device) - 0.5)
+    dpar = torch.zeros((9, B), dtype=torch.float64, device=eng.device)
+    dpar[:4] = torch.stack([0.1 * p["taurad"], 0.1 * p["taudrag"], 0.1 * p["DPhieq"],
+                            torch.full((B,), 0.05 * 3.0e5, dtype=torch.float64, device=eng.device)])
+    dpar[:4] *= torch.rand((4, B), generator=g, dtype=torch.float64).to(eng.device) - 0.5
     return eng, flags, wl, ics, dics, dpar
+
+
+# the parameters that enter only the coefficient tables: tangent row, direction
+# scale, and the centred-difference step (their effect over 12 steps is small
+# next to the fields, so a step too small leaves the difference to round-off:
+# the error of these steps is <= 1e-6 except K6, K6Phi at <= 1e-6 .. 1e-5)
+COEF_PARAMS = (("a", 4, 1e-2, 1e-4), ("dt", 5, 1e-2, 1e-4), ("K6", 6, 1e-1, 1e-2), ("K6Phi", 7, 1e-1, 1e-2),
+               ("omega", 8, 1e-1, 1e-5))
 
 
 def _forward(eng, flags, wl, ics, params_shift=None, h=0.0):
@@ -39,9 +48,10 @@ def _forward(eng, flags, wl, ics, params_shift=None, h=0.0):
 
     p = dict(wl["params"])
     if params_shift is not None:
-        for k, name in enumerate(("taurad", "taudrag", "DPhieq")):
+        for k, name in enumerate(("taurad", "taudrag", "DPhieq", "Phibar", "a", "dt", "K6", "K6Phi", "omega")):
+            if name == "K6Phi" and "K6Phi" not in p:
+                p["K6Phi"] = p["K6"]
             p[name] = p[name] + h * params_shift[k]
-        p["Phibar"] = p["Phibar"] + h * params_shift[3]
     workloads.apply_params(eng, 0, p)
     eng.init_state([ics.to(eng.rdtype)], flags)
     eng.forward(flags, t0=2, nsteps=NSTEPS)
@@ -70,6 +80,54 @@ def test_tangent_matches_central_differences(cuda, test):
     for k, name in enumerate(("eta", "delta", "Phi", "U", "V")):
         rel = float(torch.linalg.norm(tl[k] - fd[k]) / torch.linalg.norm(fd[k]))
         assert rel < 2e-6, (name, rel)
+
+
+@pytest.mark.parametrize("name,row,scale,h", COEF_PARAMS)
+def test_coefficient_tangents_match_central_differences(cuda, name, row, scale, h):
+    """Tangents along a, dt, K6, K6Phi, omega (they enter the step only through
+    its coefficient tables) against central differences of the FP64 forward."""
+    eng, flags, wl, ics, _, _ = _setup()
+    p = wl["params"]
+    base = float(p.get(name, p["K6"]))
+    dpar = torch.zeros((9, 2), dtype=torch.float64, device=eng.device)
+    dpar[row] = torch.tensor([scale * base, -0.5 * scale * base], dtype=torch.float64)
+    zero = torch.zeros_like(ics)
+    tl = _tangent(eng, flags, wl, ics, zero, dpar)
+    fd = (_forward(eng, flags, wl, ics, dpar, h) - _forward(eng, flags, wl, ics, dpar, -h)) / (2 * h)
+    for k, fname in enumerate(("eta", "delta", "Phi", "U", "V")):
+        nrm = float(torch.linalg.norm(fd[k]))
+        rel = float(torch.linalg.norm(tl[k] - fd[k])) / max(nrm, 1e-300)
+        assert rel < 1e-5, (name, fname, rel, nrm)
+
+
+def test_coefficient_gradients_by_reverse_mode(cuda):
+    """Reverse-mode gradients with respect to a, dt, K6, K6Phi, omega through
+    integrate (one tangent run per parameter) against central differences."""
+    from my_swampe_gb300 import adjoint, workloads
+
+    eng, flags, wl, ics, _, _ = _setup()
+    workloads.apply_params(eng, 0, wl["params"])
+    p = wl["params"]
+    wgt = torch.randn((5, 2, 64, 128), dtype=torch.float64, device=eng.device)
+    vals = {k: torch.full((2,), float(p.get(k, p["K6"])), dtype=torch.float64, device=eng.device)
+            for k in ("a", "dt", "K6", "K6Phi", "omega")}
+    base = {k: (p[k] if torch.is_tensor(p[k]) else torch.full((2,), float(p[k]), dtype=torch.float64,
+                                                               device=eng.device))
+            for k in ("taurad", "taudrag", "DPhieq", "Phibar")}
+    xs = {k: v.clone().requires_grad_(True) for k, v in vals.items()}
+    out = adjoint.integrate(eng, flags, 2, NSTEPS, [dict(base, **xs)], [ics], store="all")[0]
+    grads = torch.autograd.grad((wgt * out).sum(), [xs[k] for k in vals])
+    rel_h = dict(a=1e-5, dt=1e-5, K6=1e-3, K6Phi=1e-3, omega=1e-5)
+    for (k, v), gk in zip(vals.items(), grads):
+        h = rel_h[k] * float(v[0])
+        with torch.no_grad():
+            lp = float((wgt * adjoint.integrate(eng, flags, 2, NSTEPS, [dict(base, **dict(vals, **{k: v + h}))],
+                                                [ics], store="all")[0]).sum())
+            lm = float((wgt * adjoint.integrate(eng, flags, 2, NSTEPS, [dict(base, **dict(vals, **{k: v - h}))],
+                                                [ics], store="all")[0]).sum())
+        fd = (lp - lm) / (2 * h)  # both members perturbed together: the sum of their gradients
+        # the tangent model itself is pinned above; this checks the reverse-mode plumbing
+        assert abs(float(gk.sum()) - fd) <= 1e-3 * abs(fd), (k, float(gk.sum()), fd)
 
 
 def test_tangent_adjoint_dot_product(cuda):
