@@ -9,6 +9,9 @@ gets its primal states as the library's Integration decides (--store auto):
 the FP32 run keeps all 1441 states (154 GB of HBM) and needs no
 recomputation; the FP64 run (twice the bytes) checkpoints every 50 steps and
 recomputes each window.  --store checkpoint forces the recomputing form.
+The ensemble runs as two groups of 128 members of one plan, each group's step
+chain on its own stream (--groups, swp_plan_set_concurrency): the groups'
+latency-bound kernels overlap; the results equal those of joint launches.
 
 value : fast path (FP32 state and pointwise math) on device-resident inputs,
         B * 1440 / seconds per step.  The plain FP64 GPU path is timed on the
@@ -113,45 +116,64 @@ def _flush_l2(buf):
     buf.add_(1.0)
 
 
-def _setup(precision, B, seed=1234, store="auto"):
-    import torch
+def _group_sizes(B, ngroups):
+    sizes = [B // ngroups] * ngroups
+    sizes[-1] += B - sum(sizes)
+    return sizes
+
+
+def _setup(precision, B, seed=1234, store="auto", ngroups=2):
+    """The B-member ensemble as `ngroups` groups of one plan, run concurrently
+    (one stream per group); member b keeps its seed (seed + b) whatever the split."""
     from my_swampe_gb300.engine import Engine, RunFlagsC
     from my_swampe_gb300.adjoint import Integration
     from my_swampe_gb300 import workloads
 
-    eng = Engine([(M_BENCH, B)], precision)
-    wl = workloads.forced_ensemble(eng, seed=seed)
-    workloads.apply_params(eng, 0, wl["params"])
+    sizes = _group_sizes(B, ngroups)
+    eng = Engine([(M_BENCH, b) for b in sizes], precision, concurrent=ngroups > 1)
+    wls, off = [], 0
+    for g, b in enumerate(sizes):
+        wl = workloads.forced_ensemble(eng, g=g, seed=seed + off)
+        workloads.apply_params(eng, g, wl["params"])
+        wls.append(wl)
+        off += b
     flags = RunFlagsC()
     integ = Integration(eng, flags, t0=2, nsteps=T_BENCH, ckpt_every=CKPT, store=store)
-    ics = wl["ics"].to(eng.rdtype)
-    return eng, wl, flags, integ, ics
+    ics = [wl["ics"].to(eng.rdtype) for wl in wls]
+    return eng, wls, flags, integ, ics
 
 
-def _target(eng, wl, flags, ics):
-    """Phi_target: a run at perturbed taurad (x1.1) and DPhieq (x0.9)."""
+def _target(eng, wls, flags, ics):
+    """Phi_target per group: a run at perturbed taurad (x1.1) and DPhieq (x0.9)."""
     from my_swampe_gb300 import workloads
 
-    p = dict(wl["params"])
-    p["taurad"] = p["taurad"] * 1.1
-    p["DPhieq"] = p["DPhieq"] * 0.9
-    workloads.apply_params(eng, 0, p)
-    eng.init_state([ics], flags)
+    for g, wl in enumerate(wls):
+        p = dict(wl["params"])
+        p["taurad"] = p["taurad"] * 1.1
+        p["DPhieq"] = p["DPhieq"] * 0.9
+        workloads.apply_params(eng, g, p)
+    eng.init_state(ics, flags)
     eng.forward(flags, t0=2, nsteps=T_BENCH)
-    tgt = eng.output_physical(flags)[0][2].clone()
-    workloads.apply_params(eng, 0, wl["params"])
+    tgt = [o[2].clone() for o in eng.output_physical(flags)]
+    for g, wl in enumerate(wls):
+        workloads.apply_params(eng, g, wl["params"])
     return tgt
 
 
-def _one_step(integ, ics, target):
-    """forward + adjoint of the loss mean((Phi_T - target)^2); device-resident."""
+def _one_step(integ, ics, targets):
+    """forward + adjoint of the loss mean over all members of (Phi_T - target)^2;
+    device-resident.  Returns per-group lists."""
     import torch
 
-    out = integ.run_forward([ics])[0]
-    d = torch.zeros_like(out)
-    d[2] = (2.0 / target.numel()) * (out[2] - target)
-    dic, grad = integ.run_backward([d])
-    return out, dic[0], grad[0]
+    outs = integ.run_forward(ics)
+    n = sum(t.numel() for t in targets)
+    ds = []
+    for out, tgt in zip(outs, targets):
+        d = torch.zeros_like(out)
+        d[2] = (2.0 / n) * (out[2] - tgt)
+        ds.append(d)
+    dic, grad = integ.run_backward(ds)
+    return outs, dic, grad
 
 
 def _time_steps(fn, steps, warmup, flush):
@@ -228,8 +250,9 @@ def run_ours(args):
     flush = lambda: _flush_l2(flush_buf)  # noqa: E731
 
     # ---------------- fast path (headline)
-    eng, wl, flags, integ, ics = _setup("fast", B, seed=1234 + 100000 * rank, store=args.store)
-    target = _target(eng, wl, flags, ics)
+    ng = args.groups
+    eng, wls, flags, integ, ics = _setup("fast", B, seed=1234 + 100000 * rank, store=args.store, ngroups=ng)
+    target = _target(eng, wls, flags, ics)
     state = {}
 
     def step_fast():
@@ -248,8 +271,8 @@ def run_ours(args):
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t_max = float(tt.item())
     value = world * B * T_BENCH / t_max
-    out_fast = state["out"].double()
-    grad_fast = state["grad"].clone()
+    out_fast = torch.cat([o.double() for o in state["out"]], dim=1)
+    grad_fast = torch.cat([g.clone() for g in state["grad"]], dim=1)
 
     # kernel roofline (CUDA events inside the library on the launching stream)
     kt = eng.time_kernels(flags, nrep=20, adjoint=True)
@@ -270,23 +293,29 @@ def run_ours(args):
     # ---------------- e2e through the public API with host buffers
     from my_swampe_gb300.adjoint import integrate, GRAD_PARAMS, Integration
 
-    host_ics = ics.detach().cpu().pin_memory()
-    host_par = {k: wl["params"][k].detach().cpu().pin_memory() for k in GRAD_PARAMS if k != "Phibar"}
-    host_par["Phibar"] = torch.full((B,), wl["params"]["Phibar"], dtype=torch.float64).pin_memory()
-    host_tgt = target.detach().cpu().pin_memory()
-    out_ic = torch.empty(host_ics.shape, dtype=host_ics.dtype).pin_memory()
-    out_par = torch.empty((4, B), dtype=torch.float64).pin_memory()
+    sizes = _group_sizes(B, ng)
+    host_ics = [x.detach().cpu().pin_memory() for x in ics]
+    host_par = []
+    for g, wl in enumerate(wls):
+        hp = {k: wl["params"][k].detach().cpu().pin_memory() for k in GRAD_PARAMS if k != "Phibar"}
+        hp["Phibar"] = torch.full((sizes[g],), wl["params"]["Phibar"], dtype=torch.float64).pin_memory()
+        host_par.append(hp)
+    host_tgt = [t.detach().cpu().pin_memory() for t in target]
+    out_ic = [torch.empty(x.shape, dtype=x.dtype).pin_memory() for x in host_ics]
+    out_par = [torch.empty((4, b), dtype=torch.float64).pin_memory() for b in sizes]
+    n_tgt = sum(t.numel() for t in host_tgt)
 
     def step_e2e():
-        d_ics = host_ics.to("cuda", non_blocking=True).requires_grad_(True)
-        d_par = {k: v.to("cuda", non_blocking=True).requires_grad_(True) for k, v in host_par.items()}
-        d_tgt = host_tgt.to("cuda", non_blocking=True)
-        out = integrate(eng, flags, 2, T_BENCH, [d_par], [d_ics], ckpt_every=CKPT, integration=integ)[0]
-        loss = torch.mean((out[2].double() - d_tgt.double()) ** 2)
+        d_ics = [x.to("cuda", non_blocking=True).requires_grad_(True) for x in host_ics]
+        d_par = [{k: v.to("cuda", non_blocking=True).requires_grad_(True) for k, v in hp.items()} for hp in host_par]
+        d_tgt = [t.to("cuda", non_blocking=True) for t in host_tgt]
+        outs = integrate(eng, flags, 2, T_BENCH, d_par, d_ics, ckpt_every=CKPT, integration=integ)
+        loss = sum(((o[2].double() - t.double()) ** 2).sum() for o, t in zip(outs, d_tgt)) / n_tgt
         loss.backward()
-        out_ic.copy_(d_ics.grad, non_blocking=True)
-        for k, name in enumerate(GRAD_PARAMS):
-            out_par[k].copy_(d_par[name].grad, non_blocking=True)
+        for g in range(ng):
+            out_ic[g].copy_(d_ics[g].grad, non_blocking=True)
+            for k, name in enumerate(GRAD_PARAMS):
+                out_par[g][k].copy_(d_par[g][name].grad, non_blocking=True)
 
     e2e_times = _time_steps(step_e2e, max(2, args.steps), 1, flush)
     e2e_t = float(np.mean(e2e_times))
@@ -294,9 +323,10 @@ def run_ours(args):
         tt = torch.tensor([e2e_t], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         e2e_t = float(tt.item())
-    h2d = host_ics.numel() * host_ics.element_size() + sum(v.numel() * 8 for v in host_par.values()) + \
-        host_tgt.numel() * host_tgt.element_size()
-    d2h = out_ic.numel() * out_ic.element_size() + out_par.numel() * 8
+    h2d = sum(x.numel() * x.element_size() for x in host_ics) + \
+        sum(v.numel() * 8 for hp in host_par for v in hp.values()) + \
+        sum(t.numel() * t.element_size() for t in host_tgt)
+    d2h = sum(x.numel() * x.element_size() for x in out_ic) + sum(x.numel() * 8 for x in out_par)
 
     store_fast = integ.store
     integ.release()
@@ -315,8 +345,9 @@ def run_ours(args):
     # ---------------- plain FP64 GPU path on the same workload
     fp64 = None
     if not args.skip_fp64:
-        eng64, wl64, flags64, integ64, ics64 = _setup("fp64", B, seed=1234 + 100000 * rank, store=args.store)
-        target64 = target.double()
+        eng64, wl64, flags64, integ64, ics64 = _setup("fp64", B, seed=1234 + 100000 * rank, store=args.store,
+                                                      ngroups=ng)
+        target64 = [t.double() for t in target]
         st64 = {}
 
         def step64():
@@ -324,14 +355,14 @@ def run_ours(args):
 
         t64 = _time_steps(step64, args.fp64_steps, 1, flush)
         v64 = B * T_BENCH / float(np.mean(t64))
-        o64 = st64["out"]
+        o64 = torch.cat(st64["out"], dim=1)
         err = {}
         for k, name in enumerate(("eta", "delta", "Phi")):
             ref = o64[k]
             dif = out_fast[k] - ref
             err[name] = {"rel_l2": float(torch.linalg.vector_norm(dif) / torch.linalg.vector_norm(ref)),
                          "max_abs": float(dif.abs().max()), "max_rel_to_fieldmax": float(dif.abs().max() / ref.abs().max())}
-        g64 = st64["grad"]
+        g64 = torch.cat(st64["grad"], dim=1)
         gerr = {name: float(torch.linalg.vector_norm(grad_fast[k] - g64[k]) / torch.linalg.vector_norm(g64[k]))
                 for k, name in enumerate(GRAD_PARAMS)}
         kt64 = eng64.time_kernels(flags64, nrep=5, adjoint=True)
@@ -354,11 +385,12 @@ def run_ours(args):
     # coefficient kernel + (grid adjoint, Legendre adjoint) per step backward;
     # checkpoints: a coefficient kernel per window both ways and, backward, the
     # 2 recompute kernels per step as well
+    # (with concurrent groups every per-step kernel runs once per group)
     if store_fast == "all":
-        launches = 4 + (1 + 2 * T_BENCH) + (1 + 2 * T_BENCH)
+        launches = 4 + ng * ((1 + 2 * T_BENCH) + (1 + 2 * T_BENCH))
     else:
         nwin = -(-T_BENCH // CKPT)
-        launches = 4 + (nwin + 2 * T_BENCH) + (nwin + 4 * T_BENCH)
+        launches = 4 + ng * ((nwin + 2 * T_BENCH) + (nwin + 4 * T_BENCH))
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(1e3 * t_max, 3), "higher_is_better": True, "scaling": "weak",
@@ -367,6 +399,8 @@ def run_ours(args):
         "config": {"workload": "forced ensemble fwd+adjoint, M=42 (64x128), B=256 members per GPU, 1440 steps, checkpoint every 50",
                    "members_per_gpu": B, "steps_per_member": T_BENCH, "ckpt_every": CKPT,
                    "adjoint_states": store_fast,
+                   "schedule": (f"{ng} groups of {'/'.join(str(b) for b in _group_sizes(B, ng))} members, "
+                                "one stream each (concurrent)") if ng > 1 else "all members in each launch",
                    "l2": "integration touches >= 9 GB (stored states or checkpoints + window slots) > L2 (126 MB); 512 MB L2 flush write between timed steps"},
         "e2e": {"value": round(world * B * T_BENCH / e2e_t, 1), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1e3 * e2e_t, 3)},
@@ -466,9 +500,9 @@ def run_profile(args):
     build()
     from my_swampe_gb300.adjoint import Integration
 
-    eng, wl, flags, _, ics = _setup(args.profile, args.B)
+    eng, wl, flags, _, ics = _setup(args.profile, args.B, ngroups=1)
     if args.profile_case == "steps":
-        eng.init_state([ics], flags)
+        eng.init_state(ics, flags)
         eng.forward(flags, t0=2, nsteps=3)
         four_in = [eng.groups[0]["fourier"].clone()]
         eng.forward(flags, t0=5, nsteps=1)
@@ -482,7 +516,7 @@ def run_profile(args):
         print(json.dumps({"profile": args.profile, "case": "steps", "B": args.B, "ok": True}))
         return
     integ = Integration(eng, flags, t0=2, nsteps=CKPT, ckpt_every=CKPT)
-    out = integ.run_forward([ics])[0]
+    out = integ.run_forward(ics)[0]
     d = torch.zeros_like(out)
     d[2] = out[2] / out[2].numel()
     integ.run_backward([d])
@@ -497,6 +531,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--B", type=int, default=B_BENCH)
+    ap.add_argument("--groups", type=int, default=2, choices=(1, 2, 3, 4),
+                    help="split the ensemble into this many concurrent groups (one stream each)")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")

@@ -288,6 +288,14 @@ int swp_tangent_forward(swp_plan* plan, const swp_group_state* st, const swp_gro
 int swp_tangent_output(swp_plan* plan, const swp_group_state* st, const swp_group_tangent* tan,
                        void* const* dphys_out, const swp_flags* flags, void* stream);
 
+/* Schedule of a plan with several groups: on = 1 runs each group's step chain
+ * on its own stream, forked from and joined to the caller's stream (parallel
+ * branches of the captured graphs), so that the latency-bound kernels of one
+ * group overlap those of another; 0 (default) launches all groups together.
+ * Splitting one ensemble into two groups of equal size and running them
+ * concurrently is the faster schedule on GB300.  Results do not depend on it. */
+int swp_plan_set_concurrency(swp_plan* plan, int on);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,7 +89,7 @@ EXPORTS = (
     "swp_adjoint_window", "swp_time_kernels", "swp_forward_checkpointed", "swp_adjoint_step_noalloc",
     "swp_tc_selftest", "swp_device_status", "swp_plan_uses_tensor_cores", "swp_forward_stored",
     "swp_adjoint_stored", "swp_plan_autotune", "swp_plan_tiles", "swp_plan_set_tile",
-    "swp_tangent_init", "swp_tangent_forward", "swp_tangent_output",
+    "swp_tangent_init", "swp_tangent_forward", "swp_tangent_output", "swp_plan_set_concurrency",
 )
 
 _lib = None
@@ -142,6 +142,7 @@ def load(path: os.PathLike | str | None = None) -> ctypes.CDLL:
         "swp_tangent_init": (i, [vp, gsp, gtp, vpp, vpp, fp, vp]),
         "swp_tangent_forward": (i, [vp, gsp, gtp, fp, i, i, vp]),
         "swp_tangent_output": (i, [vp, gsp, gtp, vpp, fp, vp]),
+        "swp_plan_set_concurrency": (i, [vp, i]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -33,6 +33,14 @@ struct swp_plan {
   float* tcbasis_adj[MAXG] = {};
   void* coefmem[MAXG] = {};              // per-call coefficient tables (CoefTables) of each group
   int* d_err = nullptr;                  // device error word set by bounded waits that ran out
+  // groups run concurrently: each group's step chain on its own stream (forked
+  // from and joined to the caller's), so that one group's latency-bound kernels
+  // overlap another's; gmask restricts launches to the groups of one chain
+  bool concurrent = false;
+  unsigned gmask = ~0u;
+  cudaStream_t side[MAXG] = {};
+  cudaEvent_t ev_fork = nullptr;
+  cudaEvent_t ev_join[MAXG] = {};
   std::string err;
 };
 
@@ -48,6 +56,40 @@ int cuda_check(swp_plan* p, cudaError_t e, const char* where) {
   return fail(p, SWP_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+// whether group g takes part in the launches being built (see swp_plan::gmask)
+inline bool active(const swp_plan* p, int g) { return (p->gmask >> g) & 1u; }
+
+// Run body(stream) once for all groups, or -- on a concurrent plan with more
+// than one group -- once per group on that group's stream, forked from `cs`
+// and joined back into it (inside a graph capture the chains become parallel
+// branches of the graph).
+template <typename F>
+int per_group_streams(swp_plan* p, cudaStream_t cs, F body) {
+  if (!p->concurrent || p->ng < 2) return body(cs);
+  cudaError_t e = cudaSuccess;
+  if (!p->ev_fork) e = cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming);
+  for (int g = 0; g < p->ng && e == cudaSuccess; ++g) {
+    if (!p->side[g]) e = cudaStreamCreateWithFlags(&p->side[g], cudaStreamNonBlocking);
+    if (e == cudaSuccess && !p->ev_join[g]) e = cudaEventCreateWithFlags(&p->ev_join[g], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) return cuda_check(p, e, "concurrent group streams");
+  if (int rc = cuda_check(p, cudaEventRecord(p->ev_fork, cs), "fork")) return rc;
+  int rc = SWP_OK;
+  for (int g = 0; g < p->ng && rc == SWP_OK; ++g) {
+    rc = cuda_check(p, cudaStreamWaitEvent(p->side[g], p->ev_fork, 0), "fork wait");
+    if (rc) break;
+    p->gmask = 1u << g;
+    rc = body(p->side[g]);
+    p->gmask = ~0u;
+    if (rc) break;
+    rc = cuda_check(p, cudaEventRecord(p->ev_join[g], p->side[g]), "join");
+    if (rc) break;
+    rc = cuda_check(p, cudaStreamWaitEvent(cs, p->ev_join[g], 0), "join wait");
+  }
+  p->gmask = ~0u;
+  return rc;
+}
+
 template <typename T>
 CoefTables<T> plan_coefs(const swp_plan* p, int g) {
   CoefTables<T> C;
@@ -60,6 +102,7 @@ CoefTables<T> plan_coefs(const swp_plan* p, int g) {
 template <typename T>
 int update_coefs(swp_plan* p, const swp_group_state* st, cudaStream_t s, const swp_group_tangent* tan = nullptr) {
   for (int g = 0; g < p->ng; ++g) {
+    if (!active(p, g)) continue;
     cudaError_t e = launch_coefs<T>(st[g].params, p->geom[g].onemu2, p->M[g], p->B[g], p->geom[g].J,
                                     plan_coefs<T>(p, g), s, tan ? tan[g].dparams : nullptr);
     if (e != cudaSuccess) return cuda_check(p, e, "coefficient kernel launch");
@@ -76,7 +119,7 @@ SpecLaunch<T> make_spec(const swp_plan* p, const swp_group_state* st, int& nbloc
   for (int g = 0; g < p->ng; ++g) {
     SpecGroup<T>& G = L.grp[g];
     G.g = p->geom[g].view<T>();
-    G.B = p->B[g];
+    G.B = active(p, g) ? p->B[g] : 0;  // an inactive group gets no CTAs
     G.MT = p->MT[g];
     G.ntb = (G.B + G.MT - 1) / G.MT;
     G.four = (typename cplx<T>::type*)st[g].fourier;
@@ -106,7 +149,7 @@ GridLaunch<T> make_grid(const swp_plan* p, const swp_group_state* st, int& nbloc
   for (int g = 0; g < p->ng; ++g) {
     GridGroup<T>& G = L.grp[g];
     G.g = p->geom[g].view<T>();
-    G.B = p->B[g];
+    G.B = active(p, g) ? p->B[g] : 0;  // an inactive group gets no CTAs
     G.JB = p->JB[g];
     G.njb = p->geom[g].J / G.JB;
     G.four = (typename cplx<T>::type*)st[g].fourier;
@@ -158,7 +201,7 @@ cudaError_t launch_step_spec(const swp_plan* p, const SpecLaunch<T>& LS, int nbs
       memset(&tb, 0, sizeof(tb));
       for (int g = 0; g < p->ng; ++g) {
         LT.grp[g].MT = mt;
-        LT.grp[g].ntb = (p->B[g] + mt - 1) / mt;
+        LT.grp[g].ntb = (LT.grp[g].B + mt - 1) / mt;
         LT.prefix[g] = acc;
         acc += (p->M[g] + 1) * LT.grp[g].ntb;
         tb.p[g] = p->tcbasis[g];
@@ -183,7 +226,7 @@ cudaError_t launch_step_spec_adj(const swp_plan* p, const SpecLaunch<T>& LS, int
       memset(&tb, 0, sizeof(tb));
       for (int g = 0; g < p->ng; ++g) {
         LT.grp[g].MT = mt;
-        LT.grp[g].ntb = (p->B[g] + mt - 1) / mt;
+        LT.grp[g].ntb = (LT.grp[g].B + mt - 1) / mt;
         LT.prefix[g] = acc;
         acc += (p->M[g] + 1) * LT.grp[g].ntb;
         tb.p[g] = p->tcbasis_adj[g];
@@ -243,7 +286,8 @@ int forward_steps(swp_plan* p, const swp_group_state* st, const swp_flags* f, in
 // Run `body(stream)` through a cached CUDA graph keyed by `key` (captured on the
 // plan's private stream, launched on the caller's stream).
 template <typename F>
-int run_graph(swp_plan* p, const std::vector<uint64_t>& key, F body, cudaStream_t s) {
+int run_graph(swp_plan* p, const std::vector<uint64_t>& key, F body0, cudaStream_t s) {
+  auto body = [&](cudaStream_t cs) { return per_group_streams(p, cs, body0); };
   if (!p->graphs_enabled) return body(s);
   GraphEntry* hit = nullptr;
   for (auto& ge : p->graphs)
@@ -648,6 +692,7 @@ int forward_ckpt_impl(swp_plan* p, const swp_group_state* st, const swp_flags* f
     int nwin = (nsteps + K - 1) / K;
     for (int w = 0; w < nwin; ++w) {
       for (int g = 0; g < p->ng; ++g) {
+        if (!active(p, g)) continue;
         size_t bytes = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
         int rc = cuda_check(p, cudaMemcpyAsync((char*)ckpt[g] + (size_t)w * bytes, st[g].fourier, bytes,
                                                cudaMemcpyDeviceToDevice, cs), "checkpoint copy");
@@ -676,6 +721,7 @@ int forward_stored_impl(swp_plan* p, const swp_group_state* st, const swp_flags*
   auto body = [&](cudaStream_t cs) -> int {
     for (int g = 0; g < p->ng; ++g) {
       size_t bytes = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
+      if (!active(p, g)) continue;
       int rc = cuda_check(p, cudaMemcpyAsync(states[g], st[g].fourier, bytes, cudaMemcpyDeviceToDevice, cs),
                           "stored forward: first state");
       if (rc) return rc;
@@ -684,6 +730,7 @@ int forward_stored_impl(swp_plan* p, const swp_group_state* st, const swp_flags*
     if (rc) return rc;
     for (int g = 0; g < p->ng; ++g) {
       size_t bytes = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
+      if (!active(p, g)) continue;
       rc = cuda_check(p, cudaMemcpyAsync(st[g].fourier, (const char*)states[g] + (size_t)nsteps * bytes, bytes,
                                          cudaMemcpyDeviceToDevice, cs), "stored forward: last state");
       if (rc) return rc;
@@ -910,6 +957,11 @@ int swp_plan_destroy(swp_plan* p) {
     if (ge.exec) cudaGraphExecDestroy(ge.exec);
   p->graphs.clear();
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  for (int g = 0; g < MAXG; ++g) {
+    if (p->side[g]) cudaStreamDestroy(p->side[g]);
+    if (p->ev_join[g]) cudaEventDestroy(p->ev_join[g]);
+  }
   for (int g = 0; g < p->ng; ++g) {
     if (p->geom[g].mem) cudaFree(p->geom[g].mem);
     if (p->tcbasis[g]) cudaFree(p->tcbasis[g]);
@@ -1187,6 +1239,13 @@ int swp_plan_set_tile(swp_plan* p, int g, int mt) {
   p->MT[g] = mt;
   refresh_spec_smem(p);
   clear_graphs(p);
+  return SWP_OK;
+}
+
+int swp_plan_set_concurrency(swp_plan* p, int on) {
+  if (!p) return fail(p, SWP_ERR_ARG, "null plan");
+  if (p->concurrent != (on != 0)) clear_graphs(p);  // graphs are captured per schedule
+  p->concurrent = on != 0;
   return SWP_OK;
 }
 

@@ -68,7 +68,7 @@ class Engine:
     """One plan + device state for a list of ``(M, B)`` groups."""
 
     def __init__(self, groups: Sequence[Tuple[int, int]], precision: str = "fp64", device=None,
-                 autotune: bool = False):
+                 autotune: bool = False, concurrent: bool = False):
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, got {precision!r}")
         for M, _ in groups:
@@ -111,6 +111,12 @@ class Engine:
         self._geo_cache: Dict[int, Dict[str, torch.Tensor]] = {}
         if autotune:
             self.autotune()
+        if concurrent:
+            self.set_concurrency(True)
+
+    def set_concurrency(self, on: bool) -> None:
+        """Run each group's step chain on its own stream (see swp_plan_set_concurrency)."""
+        self._check(self.lib.swp_plan_set_concurrency(self._plan, int(bool(on))), "set_concurrency")
 
     # ------------------------------------------------------------------ utils
     def __del__(self):
