@@ -34,7 +34,7 @@ MS_WCURR, MS_WMID, MS_DEAD, MS_UPDATED = range(4)
 D_RMS2, D_SPIN, D_PHIMIN, D_PHIMAX, D_DEAD = range(5)
 G_TAURAD, G_TAUDRAG, G_DPHIEQ, G_PHIBAR = range(4)
 # parameter tangents of the tangent-linear model (swampe_gb300.h SWP_NTANGENT)
-TANGENT_PARAMS = ("taurad", "taudrag", "DPhieq", "Phibar", "a", "dt", "K6", "K6Phi", "omega")
+TANGENT_PARAMS = ("taurad", "taudrag", "DPhieq", "Phibar", "a", "dt", "K6", "K6Phi", "omega", "si_alpha")
 NTANGENT = len(TANGENT_PARAMS)
 
 ERRORS = {1: "bad argument", 2: "CUDA error", 3: "numerical failure", 4: "bad state", 5: "unsupported"}

@@ -30,7 +30,8 @@ from .engine import Engine, RunFlagsC
 
 GRAD_PARAMS = ("taurad", "taudrag", "DPhieq", "Phibar")
 PARAM_ROW = {"taurad": _lib.P_TAURAD, "taudrag": _lib.P_TAUDRAG, "DPhieq": _lib.P_DPHIEQ, "Phibar": _lib.P_PHIBAR,
-             "a": _lib.P_A, "dt": _lib.P_DT, "K6": _lib.P_K6, "K6Phi": _lib.P_K6PHI, "omega": _lib.P_OMEGA}
+             "a": _lib.P_A, "dt": _lib.P_DT, "K6": _lib.P_K6, "K6Phi": _lib.P_K6PHI, "omega": _lib.P_OMEGA,
+             "si_alpha": _lib.P_SIALPHA}
 
 
 class Integration:
@@ -52,17 +53,20 @@ class Integration:
 
     def __init__(self, engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, ckpt_every: int = 50,
                  store: str = "auto", mem_fraction: float = 0.8):
-        if flags.scheme != 0:
-            raise NotImplementedError("the adjoint is implemented for the modified-Euler scheme")
+        if flags.scheme not in (0, 2):
+            raise NotImplementedError("derivatives are implemented for the modified-Euler and semi-implicit schemes")
         if flags.raw_filter:
-            raise NotImplementedError("the adjoint is implemented for the classic Robert-Asselin filter")
+            raise NotImplementedError("derivatives are implemented for the classic Robert-Asselin filter")
+        # the semi-implicit scheme has the tangent model but no adjoint: its
+        # gradients are per-parameter tangent runs (scalar parameters only)
+        self.tangent_only = flags.scheme == 2
         if flags.test == 1:
             raise NotImplementedError("the adjoint of test=1 (fixed winds) is not implemented")
         if nsteps < 1:
             raise ValueError("nsteps must be >= 1 for a differentiable run")
         self.eng = engine
-        self.flags = RunFlagsC(scheme=0, forcflag=flags.forcflag, diffflag=flags.diffflag, modalflag=flags.modalflag,
-                               test=flags.test, diagnostics=False, t_start=int(t0))
+        self.flags = RunFlagsC(scheme=flags.scheme, forcflag=flags.forcflag, diffflag=flags.diffflag,
+                               modalflag=flags.modalflag, test=flags.test, diagnostics=False, t_start=int(t0))
         self.t0 = int(t0)
         self.nsteps = int(nsteps)
         self.K = max(1, min(int(ckpt_every), self.nsteps))
@@ -71,9 +75,12 @@ class Integration:
         self.ics: List[torch.Tensor] = []
         self._slots = None
         self._states = None
+        self.ic_derivs = [{} for _ in engine.groups]
         if store not in ("auto", "all", "checkpoint"):
             raise ValueError(f"store must be 'auto', 'all' or 'checkpoint', got {store!r}")
-        if store == "auto":
+        if self.tangent_only:
+            store = "checkpoint"  # nothing is kept: the backward runs tangent runs from the initial fields
+        elif store == "auto":
             need = (self.nsteps + 1) * engine.state_bytes()
             free, _ = torch.cuda.mem_get_info(engine.device)
             store = "all" if need <= mem_fraction * free else "checkpoint"
@@ -90,6 +97,9 @@ class Integration:
         eng = self.eng
         self.ics = [x.to(device=eng.device, dtype=eng.rdtype).contiguous() for x in ics]
         eng.init_state(self.ics, self.flags)
+        if self.tangent_only:
+            eng.forward(self.flags, self.t0, self.nsteps)
+            return [o[:5] for o in eng.output_physical(self.flags)]
         if self.store == "all":
             if self._states is None:
                 self._states = [torch.empty((self.nsteps + 1,) + tuple(gd["fourier"].shape), dtype=eng.cdtype,
@@ -122,6 +132,9 @@ class Integration:
 
     # ------------------------------------------------------------ backward
     def run_backward(self, dphys: Sequence[torch.Tensor]):
+        if self.tangent_only:
+            raise NotImplementedError("the semi-implicit scheme has no adjoint (its parameter gradients are "
+                                      "tangent runs)")
         eng = self.eng
         lam, lamy, grad = eng.new_adjoint_buffers()
         eng.adjoint_seed(dphys, lam)
@@ -182,10 +195,15 @@ class _IntegrateFn(torch.autograd.Function):
             ic = flat[NF * g + NP]
             ics.append(ic.detach())
             t = flat_t[NF * g: NF * g + NF]
-            dics.append(t[NP] if t[NP] is not None else torch.zeros_like(ic))
             rows = [(x if x is not None else torch.zeros(gd["B"], device=eng.device)).to(eng.device, torch.float64)
                     for x in t[:NP]]
-            dpar.append(torch.stack([r.expand(gd["B"]) for r in rows]))
+            rows = [r.expand(gd["B"]) for r in rows]
+            dic = t[NP] if t[NP] is not None else torch.zeros_like(ic)
+            for k, name in enumerate(_lib.TANGENT_PARAMS):
+                if name in integ.ic_derivs[g]:
+                    dic = dic + rows[k][None, :, None, None].to(dic.dtype) * integ.ic_derivs[g][name].to(dic.dtype)
+            dics.append(dic)
+            dpar.append(torch.stack(rows))
         outs = integ.run_tangent(ics, dics, dpar)
         return tuple(o.to(flat[NP].dtype) for o in outs)
 
@@ -196,28 +214,37 @@ class _IntegrateFn(torch.autograd.Function):
         flat = ctx.saved_tensors
         dphys = [(g if g is not None else torch.zeros((5, gd["B"], gd["J"], gd["I"]), device=eng.device))
                  for g, gd in zip(gouts, eng.groups)]
-        dic, grad = integ.run_backward(dphys)
         res = [None] * (1 + NF * len(eng.groups))
-        for g in range(len(eng.groups)):
-            o = 1 + NF * g
-            gr = grad[g]
-            for k, row in enumerate((_lib.G_TAURAD, _lib.G_TAUDRAG, _lib.G_DPHIEQ, _lib.G_PHIBAR)):
-                res[o + k] = gr[row].to(ctx.in_dtypes[NF * g + k])
-            res[o + NP] = dic[g].to(ctx.in_dtypes[NF * g + NP])
-        # coefficient-only parameters: one tangent run per parameter that needs a gradient
-        extra = [k for k in range(_lib.NGRAD, NP)
+        first_extra = _lib.NGRAD
+        if integ.tangent_only:
+            if any(ctx.needs_input_grad[1 + NF * g + NP] for g in range(len(eng.groups))):
+                raise NotImplementedError("gradients with respect to the initial fields need the adjoint, which the "
+                                          "semi-implicit scheme does not have")
+            first_extra = 0
+        else:
+            dic, grad = integ.run_backward(dphys)
+            for g in range(len(eng.groups)):
+                o = 1 + NF * g
+                gr = grad[g]
+                for k, row in enumerate((_lib.G_TAURAD, _lib.G_TAUDRAG, _lib.G_DPHIEQ, _lib.G_PHIBAR)):
+                    res[o + k] = gr[row].to(ctx.in_dtypes[NF * g + k])
+                res[o + NP] = dic[g].to(ctx.in_dtypes[NF * g + NP])
+        # parameters without an adjoint term: one tangent run per parameter that needs a gradient
+        extra = [k for k in range(first_extra, NP)
                  if any(ctx.needs_input_grad[1 + NF * g + k] for g in range(len(eng.groups)))]
         if extra:
             _IntegrateFn._set_params(eng, flat)
             ics = [flat[NF * g + NP].detach() for g in range(len(eng.groups))]
-            zeros = [torch.zeros_like(x) for x in ics]
             for k in extra:
                 dpar = []
                 for gd in eng.groups:
                     d = torch.zeros((NP, gd["B"]), dtype=torch.float64, device=eng.device)
                     d[k] = 1.0
                     dpar.append(d)
-                jk = integ.run_tangent(ics, zeros, dpar)
+                name = _lib.TANGENT_PARAMS[k]
+                dics = [integ.ic_derivs[g][name].to(x.dtype) if name in integ.ic_derivs[g] else torch.zeros_like(x)
+                        for g, x in enumerate(ics)]
+                jk = integ.run_tangent(ics, dics, dpar)
                 for g in range(len(eng.groups)):
                     w = dphys[g].to(torch.float64)
                     res[1 + NF * g + k] = (w * jk[g].to(torch.float64)).sum(dim=(0, 2, 3)).to(ctx.in_dtypes[NF * g + k])
@@ -225,7 +252,7 @@ class _IntegrateFn(torch.autograd.Function):
 
 
 def integrate(engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, params: Sequence[dict], ics: Sequence[torch.Tensor],
-              ckpt_every: int = 50, integration: Integration = None, store: str = "auto"):
+              ckpt_every: int = 50, integration: Integration = None, store: str = "auto", ic_derivs=None):
     """Differentiable run of every group of ``engine``.
 
     params[g]: dict with (B,) tensors (or scalars) 'taurad', 'taudrag', 'DPhieq',
@@ -235,9 +262,13 @@ def integrate(engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, params: Se
     (5, B, J, I) tensor of the final physical curr fields.  Passing the same
     ``integration`` object across calls reuses its checkpoint buffers and the
     library's captured CUDA graphs.  ``store`` selects how the adjoint gets
-    its primal states (see :class:`Integration`).
+    its primal states (see :class:`Integration`).  ``ic_derivs[g]`` optionally
+    maps a parameter name to d(ics[g]) / d(parameter) (5, B, J, I): initial
+    fields that depend on a parameter outside the autograd graph (the
+    semi-implicit scheme's tangent runs take them as initial-field tangents).
     """
     integ = integration if integration is not None else Integration(engine, flags, t0, nsteps, ckpt_every, store)
+    integ.ic_derivs = ic_derivs if ic_derivs is not None else [{} for _ in engine.groups]
     flat = []
     for g, gd in enumerate(engine.groups):
         for row, k in enumerate(_lib.TANGENT_PARAMS):

@@ -51,9 +51,22 @@ __global__ void k_coefs(const double* __restrict__ par, const double* __restrict
         dsigp = -s2 * s2 * dxp;
         dtc = (n == 0) ? 0.0 : da / ((double)n * (n + 1));
       }
+      // exponential sigmas: exp(-2 dt K6 max(r, 0)), exp(-2 dt K6Phi ncoeff)
+      double dsigx = 0.0, dsigpx = 0.0;
+      if (dpar) {
+        const double da = dpar[T_A * B + b], ddt = dpar[T_DT * B + b];
+        const double dK6 = dpar[T_K6 * B + b], dK6P = dpar[T_K6PHI * B + b];
+        const double r = fmax(ncoeff - 8.0 / a6, 0.0);
+        const double dr = r > 0.0 ? -6.0 * (da / a) * r : 0.0, dnc = -6.0 * (da / a) * ncoeff;
+        dsigx = -exp(-(2.0 * dt * K6) * r) * (2.0 * ddt * K6 * r + 2.0 * dt * dK6 * r + 2.0 * dt * K6 * dr);
+        dsigpx = -exp(-(2.0 * dt * K6P) * ncoeff) * (2.0 * ddt * K6P * ncoeff + 2.0 * dt * dK6P * ncoeff +
+                                                     2.0 * dt * K6P * dnc);
+      }
       C.nco[NC_DSIG * qs + o] = (T)dsig;
       C.nco[NC_DSIGP * qs + o] = (T)dsigp;
       C.nco[NC_DTC * qs + o] = (T)dtc;
+      C.nco[NC_DSIGX * qs + o] = (T)dsigx;
+      C.nco[NC_DSIGPX * qs + o] = (T)dsigpx;
     } else if (t < n_nco + n_jco) {
       const int u = t - n_nco, b = u / J, j = u % J;
       const double a = par[P_A * B + b], dt = par[P_DT * B + b];
@@ -100,6 +113,20 @@ __global__ void k_coefs(const double* __restrict__ par, const double* __restrict
       }
       const int dr[8] = {MC_DT2, MC_DIA2, MC_DHPB, MC_DDTPB, MC_DPBA2, MC_DPFD, MC_DDT, MC_DOM};
       for (int q = 0; q < 8; ++q) mc[dr[q] * B + b] = (T)v[q];
+      // semi-implicit: xi = 2 dt sa, ex = 2 dt (1 - sa), 1/taudrag (0 for -1), 1/taurad
+      double w[4] = {0, 0, 0, 0};
+      if (dpar) {
+        const double ddt = dpar[T_DT * B + b], dsa = dpar[T_SIALPHA * B + b];
+        const double itd = td == -1.0 ? 0.0 : 1.0 / td, itr = 1.0 / par[P_TAURAD * B + b];
+        w[0] = 2.0 * ddt * sa + 2.0 * dt * dsa;
+        w[1] = 2.0 * ddt * (1.0 - sa) - 2.0 * dt * dsa;
+        w[2] = -itd * itd * dpar[T_TAUDRAG * B + b];
+        w[3] = -itr * itr * dpar[T_TAURAD * B + b];
+      }
+      mc[MC_DSIXI * B + b] = (T)w[0];
+      mc[MC_DSIEX * B + b] = (T)w[1];
+      mc[MC_DSIITD * B + b] = (T)w[2];
+      mc[MC_DSIITR * B + b] = (T)w[3];
     }
   }
 }

@@ -199,8 +199,16 @@ __device__ __forceinline__ void step_combos_ld(const SpecGroup<T>& G, const Step
 // scalar factors, along the members' tangents of a, dt and Phibar) times the
 // primal state before the step, `four_p`.
 template <typename T>
+__device__ __forceinline__ void tangent_coef_terms_si(const SpecGroup<T>& G, const StepCfg& cfg, int m, int b, int j,
+                                                      size_t FS, typename cplx<T>::type* c);
+
+template <typename T>
 __device__ __forceinline__ void tangent_coef_terms(const SpecGroup<T>& G, const StepCfg& cfg, int m, int b, int j,
                                                    size_t FS, typename cplx<T>::type* c) {
+  if (cfg.scheme == 2) {
+    tangent_coef_terms_si<T>(G, cfg, m, b, j, FS, c);
+    return;
+  }
   typedef typename cplx<T>::type T2;
   constexpr int NSPX = SlotCount<T>::NP;
   const T2* Fp = G.four_p;
@@ -238,6 +246,74 @@ __device__ __forceinline__ void tangent_coef_terms(const SpecGroup<T>& G, const 
   // eta
   c[SP_E1] = csub(c[SP_E1], cscale(imul(xm, Aeff), dte));
   c[NSPX + SH_E1] = cadd(c[NSPX + SH_E1], cscale(Beff, dte));
+}
+
+// The semi-implicit scheme's coefficient tangents (step_combos_ld scheme 2):
+// the shares 1 - gd, 1 - gr (gd = ex / taudrag, gr = ex / taurad under
+// relaxation), tstepcoeff, ex Phibar, 2 dt, 1/a^2, the relaxation part of the
+// Phi forcing and, on the first step, the drag part of the lagged remainder.
+template <typename T>
+__device__ __forceinline__ void tangent_coef_terms_si(const SpecGroup<T>& G, const StepCfg& cfg, int m, int b, int j,
+                                                      size_t FS, typename cplx<T>::type* c) {
+  typedef typename cplx<T>::type T2;
+  constexpr int NSPX = SlotCount<T>::NP;
+  const T2* Fp = G.four_p;
+  const size_t o = ((size_t)m * G.B + b) * G.g.J + j;
+  const T* mc = G.mco;
+  const int B = G.B;
+  const T xm = (T)m;
+  const T tsc = G.jco[(size_t)b * G.g.J + j], dtsc = G.djco[(size_t)b * G.g.J + j];
+  const T ex = mc[MC_SIEX * B + b], dex = mc[MC_DSIEX * B + b];
+  const T itd = cfg.si_relax ? mc[MC_SIITD * B + b] : (T)0, ditd = cfg.si_relax ? mc[MC_DSIITD * B + b] : (T)0;
+  const T itr = cfg.si_relax ? mc[MC_SIITR * B + b] : (T)0, ditr = cfg.si_relax ? mc[MC_DSIITR * B + b] : (T)0;
+  const T dgd = dex * itd + ex * ditd, dgr = dex * itr + ex * ditr;
+  const T pb = mc[MC_PB * B + b], dpb = (T)2 * mc[MC_DHPB * B + b];
+  const T tdt = mc[MC_2DT * B + b], dtdt = (T)2 * mc[MC_DDT * B + b];
+  const T ia2 = mc[MC_IA2 * B + b], dia2 = mc[MC_DIA2 * B + b];
+  const T2 eta0 = Fp[F_ETA_MID * FS + o], del0 = Fp[F_DELTA_MID * FS + o], phi0 = Fp[F_PHI_MID * FS + o];
+  const T2 A = Fp[F_A * FS + o], Bm = Fp[F_B * FS + o], C = Fp[F_C * FS + o], D = Fp[F_D * FS + o];
+  const T2 E = Fp[F_E * FS + o];
+  T2 Aeff = A, Beff = Bm, PFx = mk<T2>(0, 0), dPFx = mk<T2>(0, 0);
+  T2 dAc = mk<T2>(0, 0), dBc = mk<T2>(0, 0);  // coefficient tangents of Aeff, Beff (first step)
+  if (cfg.forcflag) {
+    T2 Fx, Gx;
+    if (cfg.si_relax) {
+      const T itd_all = mc[MC_SIITD * B + b], ditd_all = mc[MC_DSIITD * B + b];
+      if (cfg.si_lag_init) {
+        const T2 U = Fp[F_U * FS + o], V = Fp[F_V * FS + o];
+        Fx = cadd(Fp[F_F * FS + o], cscale(U, itd_all));
+        Gx = cadd(Fp[F_G * FS + o], cscale(V, itd_all));
+        dBc = cscale(U, ditd_all);
+        dAc = cscale(V, -ditd_all);
+      } else {
+        Fx = Fp[F_RU_LAG * FS + o];
+        Gx = Fp[F_RV_LAG * FS + o];
+      }
+      const T2 phi1 = Fp[F_PHI * FS + o];
+      PFx = cadd(Fp[F_PHIF * FS + o], cscale(phi1, itr));
+      dPFx = cscale(phi1, ditr);
+    } else {
+      Fx = Fp[F_F * FS + o];
+      Gx = Fp[F_G * FS + o];
+      PFx = Fp[F_PHIF * FS + o];
+    }
+    Aeff = csub(A, Gx);
+    Beff = cadd(Bm, Fx);
+  }
+  // eta: (1 - gd) eta0 - tsc i m Aeff ; H: tsc Beff
+  c[SP_E1] = csub(c[SP_E1], cadd(cscale(eta0, dgd), cadd(cscale(imul(xm, Aeff), dtsc), cscale(imul(xm, dAc), tsc))));
+  c[NSPX + SH_E1] = cadd(c[NSPX + SH_E1], cadd(cscale(Beff, dtsc), cscale(dBc, tsc)));
+  // delta: (1 - gd) delta0 + tsc i m Beff ; H: tsc Aeff ; n(n+1): (2 dt E + ex Phi0) / a^2
+  c[SP_D1] = cadd(c[SP_D1], csub(cadd(cscale(imul(xm, Beff), dtsc), cscale(imul(xm, dBc), tsc)), cscale(del0, dgd)));
+  c[NSPX + SH_D1] = cadd(c[NSPX + SH_D1], cadd(cscale(Aeff, dtsc), cscale(dAc, tsc)));
+  const T2 d2a = cadd(cscale(E, dtdt), cscale(phi0, dex)), d2b = cadd(cscale(E, tdt), cscale(phi0, ex));
+  c[SP_D2] = cadd(c[SP_D2], cadd(cscale(d2a, ia2), cscale(d2b, dia2)));
+  // Phi: (1 - gr) Phi0 - tsc i m C - ex Phibar delta0 + 2 dt PhiFx ; H: tsc D
+  T2 p1 = cadd(cscale(phi0, dgr), cscale(imul(xm, C), dtsc));
+  p1 = cadd(p1, cscale(del0, dex * pb + ex * dpb));
+  c[SP_PHI1] = csub(c[SP_PHI1], p1);
+  if (cfg.forcflag) c[SP_PHI1] = cadd(c[SP_PHI1], cadd(cscale(PFx, dtdt), cscale(dPFx, tdt)));
+  c[NSPX + SH_PHI1] = cadd(c[NSPX + SH_PHI1], cscale(D, dtsc));
 }
 
 // step_combos_ld on the state in global memory
@@ -320,9 +396,16 @@ __device__ __forceinline__ void store_step_point(const SpecGroup<T>& G, const St
 template <typename T>
 __device__ __forceinline__ void write_step_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
                                                  size_t o, int b, const typename cplx<T>::type* nw_in, bool uv,
-                                                 typename cplx<T>::type u, typename cplx<T>::type v) {
+                                                 typename cplx<T>::type u, typename cplx<T>::type v,
+                                                 bool tangent = false) {
   typename cplx<T>::type old[3], mid[3], lag[2];
   load_step_point<T>(G, cfg, incr, FS, o, old, mid, lag, b);
+  if (tangent && cfg.scheme == 2) {
+    // tangent of Fm + Um / taudrag: the primal winds times d(1/taudrag)
+    const typename scalar_of<typename cplx<T>::type>::type ditd = G.mco[MC_DSIITD * G.B + b];
+    lag[0] = cadd(lag[0], cscale(G.four_p[F_U * FS + o], ditd));
+    lag[1] = cadd(lag[1], cscale(G.four_p[F_V * FS + o], ditd));
+  }
   const T al = G.mco[(cfg.raw ? MC_RAWM : MC_ALPHA) * G.B + b];
   const T an = cfg.raw ? G.mco[MC_RAWN * G.B + b] : (T)0;
   store_step_point<T>(G, cfg, incr, FS, o, al, an, nw_in, uv, u, v, old, mid, lag);

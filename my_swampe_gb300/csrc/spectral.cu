@@ -200,17 +200,31 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
       // semi-implicit solve constants (semi_implicit_tdiff.py): implicit share
       // xi, implicit drag / relaxation kd, kr, explicit drag gd, Phibar, 1/a^2
       T si_xi = (T)0, si_kd = (T)0, si_kr = (T)0, si_gd = (T)0, si_pb = (T)0, si_ia2 = (T)0;
-      if (mode == 0 && cfg.scheme == 2 && bt < mt) {
+      // and, for the tangent step, their tangents
+      T si_dxi = (T)0, si_dkd = (T)0, si_dkr = (T)0, si_dgd = (T)0, si_dpb = (T)0, si_dia2 = (T)0;
+      if ((mode == 0 || mode == 3) && cfg.scheme == 2 && bt < mt) {
         const T* mc = G.mco;
         const int b = b0 + bt, B = G.B;
         si_xi = mc[MC_SIXI * B + b];
-        if (cfg.si_relax) {
-          si_kd = si_xi * mc[MC_SIITD * B + b];
-          si_kr = si_xi * mc[MC_SIITR * B + b];
-          si_gd = mc[MC_SIEX * B + b] * mc[MC_SIITD * B + b];
-        }
         si_pb = mc[MC_PB * B + b];
         si_ia2 = mc[MC_IA2 * B + b];
+        if (mode == 3) {
+          si_dxi = mc[MC_DSIXI * B + b];
+          si_dpb = (T)2 * mc[MC_DHPB * B + b];
+          si_dia2 = mc[MC_DIA2 * B + b];
+        }
+        if (cfg.si_relax) {
+          const T itd = mc[MC_SIITD * B + b], itr = mc[MC_SIITR * B + b], ex = mc[MC_SIEX * B + b];
+          si_kd = si_xi * itd;
+          si_kr = si_xi * itr;
+          si_gd = ex * itd;
+          if (mode == 3) {
+            const T ditd = mc[MC_DSIITD * B + b], ditr = mc[MC_DSIITR * B + b], dex = mc[MC_DSIEX * B + b];
+            si_dkd = si_dxi * itd + si_xi * ditd;
+            si_dkr = si_dxi * itr + si_xi * ditr;
+            si_dgd = dex * itd + ex * ditd;
+          }
+        }
       }
 #pragma unroll
       for (int k = 0; k < FWD_TC; ++k) {
@@ -244,6 +258,42 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
           cdel = acc[SP_D1][k];
           cphi = (T)0;
           kphi = cphi; kdel = cdel; keta = ceta;
+        } else if (cfg.scheme == 2 && mode == 3) {
+          // tangent of the implicit solve below: the tangent spectra through the
+          // primal solve, plus the solve's and the exponential sigmas' parameter
+          // tangents applied to the primal spectra (pass 0)
+          T seta = acc[SP_E1][k] + acc[NSPX + SH_E1][k];
+          T sdel = acc[SP_D1][k] + acc[NSPX + SH_D1][k] + nn1 * acc[SP_D2][k];
+          T sphi = acc[SP_PHI1][k] + acc[NSPX + SH_PHI1][k];
+          T Se = Kin[((size_t)0 * cntmax + pc) * R + r], Sd = Kin[((size_t)1 * cntmax + pc) * R + r];
+          T Sp = Kin[((size_t)2 * cntmax + pc) * R + r];
+          if (m == 0 && n == 1 && comp == 0) {
+            Se += (si_gd + si_kd) * om_p;
+            seta += (si_dgd + si_dkd) * om_p + (si_gd + si_kd) * om;  // om: tangent of f here
+          }
+          const T bq = si_xi * (nn1 * si_ia2), cq = si_xi * si_pb;
+          const T ikr = (T)1 / ((T)1 + si_kr), ikd = (T)1 / ((T)1 + si_kd);
+          const T Dn = ((T)1 + si_kd) + bq * cq * ikr;
+          const T dnew = (Sd + bq * Sp * ikr) / Dn, pnew = (Sp - cq * dnew) * ikr, enew = Se * ikd;
+          const T dbq = nn1 * (si_dxi * si_ia2 + si_xi * si_dia2), dcq = si_dxi * si_pb + si_xi * si_dpb;
+          const T dikr = -ikr * ikr * si_dkr;
+          const T denew = (seta - enew * si_dkd) * ikd;
+          const T dnum = sdel + dbq * Sp * ikr + bq * sphi * ikr + bq * Sp * dikr;
+          const T dD = si_dkd + dbq * cq * ikr + bq * dcq * ikr + bq * cq * dikr;
+          const T ddnew = (dnum - dnew * dD) / Dn;
+          const T dpnew = (sphi - dcq * dnew - cq * ddnew) * ikr + (Sp - cq * dnew) * dikr;
+          T dsg = (T)0, dsp = (T)0;
+          if (cfg.diffflag && bt < mt) {
+            const size_t qs = (size_t)G.B * cntmax, qo = (size_t)(b0 + bt) * cntmax + n;
+            dsg = G.nco[NC_DSIGX * qs + qo];
+            dsp = G.nco[NC_DSIGPX * qs + qo];
+          }
+          cphi = sp * dpnew + dsp * pnew;
+          cdel = s * ddnew + dsg * dnew;
+          ceta = s * denew + dsg * enew;
+          kphi = cphi; kdel = cdel; keta = ceta;
+          pce = s * enew;
+          pcd = s * dnew;
         } else if (cfg.scheme == 2) {
           // eta* , delta*, Phi* -> the implicit (delta, Phi) pair per degree,
           // eliminated for delta; then the exponential hyperdiffusion
@@ -416,7 +466,7 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
       continue;
     }
     const T2 nw[3] = {get(0), get(1), get(2)};
-    write_step_point<T>(G, cfg, incr, FS, o, b, nw, do_uv != 0, get(3), get(4));
+    write_step_point<T>(G, cfg, incr, FS, o, b, nw, do_uv != 0, get(3), get(4), mode == 3);
   }
   // residual weights of the initial condition in the physical curr / prev fields
   if (mode == 0 && m == 0 && threadIdx.x < mt && !sdead[threadIdx.x]) {

@@ -22,7 +22,9 @@ enum DiagIndex { D_RMS2 = 0, D_SPIN, D_PHIMIN, D_PHIMAX, D_DEAD, NDIAG };
 enum GradIndex { G_TAURAD = 0, G_TAUDRAG, G_DPHIEQ, G_PHIBAR, NGRAD };
 // Parameter tangents of the tangent-linear model: the adjoint's four, then
 // those that enter only the coefficient tables.
-enum TangentIndex { T_TAURAD = 0, T_TAUDRAG, T_DPHIEQ, T_PHIBAR, T_A, T_DT, T_K6, T_K6PHI, T_OMEGA, NTANGENT };
+enum TangentIndex {
+  T_TAURAD = 0, T_TAUDRAG, T_DPHIEQ, T_PHIBAR, T_A, T_DT, T_K6, T_K6PHI, T_OMEGA, T_SIALPHA, NTANGENT
+};
 
 struct GroupGeom {
   int M = 0, J = 0, I = 0, L = 0;
@@ -81,6 +83,7 @@ constexpr int MAXG = 4;
 enum NCoef {
   NC_SIG = 0, NC_SIGP, NC_SIGM1, NC_SIGPM1, NC_TC, NC_SIGX, NC_SIGPX,
   NC_DSIG, NC_DSIGP, NC_DTC,  // tangents of sigma, sigmaPhi, a/(n(n+1)) (tangent-linear launches)
+  NC_DSIGX, NC_DSIGPX,        // tangents of the exponential sigmas
   NNCO
 };
 enum MCoef {
@@ -105,6 +108,7 @@ enum MCoef {
   MC_PB,       // Phibar
   // tangents of the step factors along the call's parameter tangents (tangent-linear launches)
   MC_DT2, MC_DIA2, MC_DHPB, MC_DDTPB, MC_DPBA2, MC_DPFD, MC_DDT, MC_DOM,
+  MC_DSIXI, MC_DSIEX, MC_DSIITD, MC_DSIITR,  // of the semi-implicit shares and rates
   NMCO
 };
 template <typename T>

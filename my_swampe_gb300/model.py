@@ -377,6 +377,7 @@ def run_model_scan(
         raise ValueError(f"starttime={starttime_eff} must be <= tmax={tmax}.")
 
     have_ic = (eta0_init is not None) or (delta0_init is not None) or (Phi0_init is not None)
+    ic_derivs: Dict[str, torch.Tensor] = {}  # d(analytic initial fields) / d(parameter), semi-implicit runs
     if have_ic and (eta0_init is None or delta0_init is None or Phi0_init is None):
         raise ValueError("If providing explicit ICs, eta0_init, delta0_init, and Phi0_init must all be provided.")
     if have_ic and ((U0_init is None) != (V0_init is None)):
@@ -405,19 +406,22 @@ def run_model_scan(
     # model cover, the initial fields, and alpha and g, which the curr fields of
     # the modified-Euler scheme do not depend on (their derivative is zero)
     # K6Phi=None means K6Phi = K6 (model.py:512): then K6 drives both
-    coef_inputs = dict(a=a, dt=dt, K6=K6, K6Phi=K6 if K6Phi is None else K6Phi, omega=omega)
-    diff_inputs = (taurad, taudrag, DPhieq, Phibar, eta0_init, delta0_init, Phi0_init, U0_init, V0_init, alpha, g,
-                   *coef_inputs.values())
+    coef_inputs = dict(a=a, dt=dt, K6=K6, K6Phi=K6 if K6Phi is None else K6Phi, omega=omega, si_alpha=si_alpha)
+    ic_inputs = (eta0_init, delta0_init, Phi0_init, U0_init, V0_init)
+    diff_inputs = (taurad, taudrag, DPhieq, Phibar, *ic_inputs, alpha, g, *coef_inputs.values())
     needs_grad = any(_tracked(x) for x in diff_inputs)
-    if any(_tracked(x) for x in (si_alpha, williams_alpha)):
-        raise NotImplementedError("derivatives through the semi-implicit scheme and the RAW filter are not "
-                                  "implemented")
+    if _tracked(williams_alpha):
+        raise NotImplementedError("derivatives through the RAW filter are not implemented")
     if needs_grad:
-        if semi_implicit or raw_filter or expflag or test == 1:
-            raise NotImplementedError("derivatives are implemented for the modified-Euler scheme with the classic "
-                                      "filter and test None or 2")
+        if raw_filter or expflag or test == 1:
+            raise NotImplementedError("derivatives are implemented for the modified-Euler and semi-implicit "
+                                      "schemes with the classic filter and test None or 2")
         if U0_init is None and (_tracked(eta0_init) or _tracked(delta0_init)):
             raise NotImplementedError("derivatives with respect to eta0_init / delta0_init need U0_init and V0_init")
+        if semi_implicit and any(_tracked(x) for x in ic_inputs) and torch.is_grad_enabled():
+            if any(torch.is_tensor(x) and x.requires_grad for x in ic_inputs):
+                raise NotImplementedError("reverse-mode gradients with respect to the initial fields need the "
+                                          "adjoint, which the semi-implicit scheme does not have (forward mode works)")
 
     eng = Engine([(M, B)], precision, device)
     dev = eng.device
@@ -448,7 +452,9 @@ def run_model_scan(
         # the analytic fields are polynomials of degree <= 2 in a, omega, Phibar
         # (initial_conditions.py:18-47, 88-239), so a centred difference is their
         # exact derivative: carry it into the differentiable run
-        for x, i in ((a, 0), (omega, 1), (Phibar, 2)):
+        # (the semi-implicit scheme, which differentiates by tangent runs, takes
+        # them as initial-field tangents of the parameter directions instead)
+        for x, i, name in ((a, 0, "a"), (omega, 1, "omega"), (Phibar, 2, "Phibar")):
             if _tracked(x):
                 h = 1e-3 * abs((av, omv, pb)[i]) or 1e-3
                 arg = [av, omv, pb]
@@ -457,6 +463,9 @@ def run_model_scan(
                 arg[i] -= 2 * h
                 fm = _analytic_ic(M, *arg, test, float(a1), dev)
                 d = [(u - v) / (2 * h) for u, v in zip(fp, fm)]
+                if semi_implicit:
+                    ic_derivs[name] = torch.stack([dd.expand(B, J, I) for dd in d], 0)
+                    continue
                 dx = x - x.detach()
                 eta0, delta0, Phi0, U0, V0 = (f + dx * dd.expand(B, J, I)
                                               for f, dd in zip((eta0, delta0, Phi0, U0, V0), d))
@@ -497,14 +506,14 @@ def run_model_scan(
         if return_history or diagnostics:
             eng.forward(flags, t0=starttime_eff, nsteps=T, row0=0, diag=diag, hist=hist, write_prev_last=True)
             saved = (four.clone(), gd["member"].clone())
-        dflags = RunFlagsC(scheme=0, forcflag=forcflag, diffflag=diffflag, modalflag=modalflag, test=test,
-                           diagnostics=False, t_start=starttime_eff)
+        dflags = RunFlagsC(scheme=2 if semi_implicit else 0, forcflag=forcflag, diffflag=diffflag,
+                           modalflag=modalflag, test=test, diagnostics=False, t_start=starttime_eff)
         dpar = dict(taurad=_per_member(taurad, B, dev), taudrag=_per_member(taudrag, B, dev),
                     DPhieq=_per_member(DPhieq if test is None else 0.0, B, dev), Phibar=_per_member(Phibar, B, dev))
         for k, x in coef_inputs.items():
             if _tracked(x):
                 dpar[k] = _per_member(x, B, dev)
-        dcurr = adjoint.integrate(eng, dflags, starttime_eff, T, [dpar], [ics])[0]
+        dcurr = adjoint.integrate(eng, dflags, starttime_eff, T, [dpar], [ics], ic_derivs=[ic_derivs])[0]
         for x in (alpha, g):  # zero derivative, but part of the graph
             if _tracked(x):
                 dcurr = dcurr + 0.0 * x.to(dcurr.dtype).sum()

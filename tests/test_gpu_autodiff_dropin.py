@@ -45,10 +45,10 @@ def test_coefficient_parameter_gradients_match_finite_differences(cuda, name, va
     assert abs(g_ad - g_fd) <= 1e-4 * abs(g_fd), (name, g_ad, g_fd)
 
 
-def test_opt_in_scheme_parameters_refuse_gradients(cuda):
-    th = torch.tensor(0.5, dtype=torch.float64, device="cuda", requires_grad=True)
+def test_raw_filter_parameters_refuse_gradients(cuda):
+    th = torch.tensor(0.53, dtype=torch.float64, device="cuda", requires_grad=True)
     with pytest.raises(NotImplementedError):
-        _loss("si_alpha", th, semi_implicit=True)
+        _loss("williams_alpha", th, raw_filter=True)
 
 
 def test_jvp_returns_finite_for_DPhieq(cuda):
@@ -128,3 +128,80 @@ def test_phibar_gradient_includes_the_analytic_initial_condition(cuda):
     with torch.no_grad():
         g_fd = (float(loss(3.0e3 + 0.01)) - float(loss(3.0e3 - 0.01))) / 0.02
     assert abs(g_ad - g_fd) <= 1e-6 * abs(g_fd), (g_ad, g_fd)
+
+
+SYNTH = dict(M=42, Phibar=3.0e5, omega=3.2e-5, a=8.2e7, taudrag=21600.0, DPhieq=1.0e6, test=None, dt=600.0, tmax=40)
+
+
+def _si_loss(**kw):
+    from my_swampe_gb300 import run_model_scan_final
+
+    args = dict(SYNTH, taurad=36000.0, si_alpha=0.5)
+    args.update(kw)
+    Phi = run_model_scan_final(**args, semi_implicit=True, diagnostics=False)["last_state"].Phi_curr
+    return torch.mean(Phi ** 2)
+
+
+def test_semi_implicit_grad_wrt_taurad_finite_nonzero(cuda):
+    """test_semi_implicit.py:121-132 (through tangent runs: the scheme has no adjoint),
+    with a centred-difference check."""
+    th = torch.tensor(36000.0, dtype=torch.float64, device="cuda", requires_grad=True)
+    g = float(torch.autograd.grad(_si_loss(taurad=th), th)[0])
+    assert np.isfinite(g) and g != 0.0
+    with torch.no_grad():
+        fd = (float(_si_loss(taurad=36000.0 * (1 + 1e-5))) - float(_si_loss(taurad=36000.0 * (1 - 1e-5)))) / (
+            2 * 36000.0 * 1e-5)
+    assert abs(g - fd) <= 1e-4 * abs(fd), (g, fd)
+
+
+def test_semi_implicit_grad_wrt_si_alpha_finite(cuda):
+    """test_semi_implicit.py:135-149, with a centred-difference check."""
+    th = torch.tensor(0.5, dtype=torch.float64, device="cuda", requires_grad=True)
+    g = float(torch.autograd.grad(_si_loss(si_alpha=th), th)[0])
+    assert np.isfinite(g)
+    with torch.no_grad():
+        fd = (float(_si_loss(si_alpha=0.5 + 1e-5)) - float(_si_loss(si_alpha=0.5 - 1e-5))) / 2e-5
+    assert abs(g - fd) <= 1e-4 * abs(fd), (g, fd)
+
+
+def test_semi_implicit_forward_mode_equals_reverse(cuda):
+    with fwAD.dual_level():
+        d = fwAD.make_dual(torch.tensor(3.0e5, dtype=torch.float64, device="cuda"),
+                           torch.tensor(1.0, dtype=torch.float64, device="cuda"))
+        t = float(fwAD.unpack_dual(_si_loss(Phibar=d)).tangent)
+    th = torch.tensor(3.0e5, dtype=torch.float64, device="cuda", requires_grad=True)
+    g = float(torch.autograd.grad(_si_loss(Phibar=th), th)[0])
+    assert abs(t - g) <= 1e-9 * abs(g), (t, g)
+
+
+def test_semi_implicit_initial_field_gradient_refused(cuda):
+    from my_swampe_gb300 import run_model_scan_final
+
+    z = np.zeros((64, 128))
+    phi = torch.zeros((64, 128), dtype=torch.float64, device="cuda", requires_grad=True)
+    with pytest.raises(NotImplementedError):
+        run_model_scan_final(**SYNTH, semi_implicit=True, eta0_init=z, delta0_init=z, Phi0_init=phi, U0_init=z,
+                             V0_init=z)
+
+
+def test_semi_implicit_phibar_gradient_with_analytic_test2_initial_condition(cuda):
+    """The analytic test-2 fields depend on Phibar; the semi-implicit scheme's
+    tangent runs carry that dependence as an initial-field tangent."""
+    from my_swampe_gb300 import run_model_scan_final
+
+    kw = dict(M=42, dt=600.0, tmax=6, omega=7.2921159e-5, a=6.37122e6, test=2, forcflag=False, semi_implicit=True)
+
+    def loss(pb):
+        Phi = run_model_scan_final(**kw, Phibar=pb)["last_state"].Phi_curr
+        return torch.mean(Phi * Phi)
+
+    th = torch.tensor(3.0e3, dtype=torch.float64, device="cuda", requires_grad=True)
+    g_ad = float(torch.autograd.grad(loss(th), th)[0])
+    with fwAD.dual_level():
+        d = fwAD.make_dual(torch.tensor(3.0e3, dtype=torch.float64, device="cuda"),
+                           torch.tensor(1.0, dtype=torch.float64, device="cuda"))
+        g_fw = float(fwAD.unpack_dual(loss(d)).tangent)
+    with torch.no_grad():
+        g_fd = (float(loss(3.0e3 + 0.01)) - float(loss(3.0e3 - 0.01))) / 0.02
+    assert abs(g_ad - g_fd) <= 1e-6 * abs(g_fd), (g_ad, g_fd)
+    assert abs(g_fw - g_ad) <= 1e-9 * abs(g_ad), (g_fw, g_ad)

@@ -140,16 +140,20 @@ def test_semi_implicit_ensemble_of_alphas(cuda):
 
 
 def test_adjoint_rejects_opt_in_schemes(cuda):
-    """Forward only: the Python layer and the C ABI both refuse the adjoint of
-    the semi-implicit scheme and of the RAW filter."""
+    """The Python layer and the C ABI refuse the adjoint of the semi-implicit
+    scheme and of the RAW filter (the semi-implicit scheme differentiates by
+    tangent runs)."""
     import torch
     from my_swampe_gb300 import adjoint
     from my_swampe_gb300.engine import Engine, RunFlagsC
 
     eng = Engine([(42, 2)], "fp64")
-    for flags in (RunFlagsC(scheme=2), RunFlagsC(raw_filter=True)):
-        with pytest.raises(NotImplementedError):
-            adjoint.Integration(eng, flags, t0=2, nsteps=4, ckpt_every=2, store="checkpoint")
+    with pytest.raises(NotImplementedError):
+        adjoint.Integration(eng, RunFlagsC(raw_filter=True), t0=2, nsteps=4, ckpt_every=2, store="checkpoint")
+    # the semi-implicit scheme: tangent runs only, no adjoint sweep
+    integ = adjoint.Integration(eng, RunFlagsC(scheme=2), t0=2, nsteps=4, ckpt_every=2, store="checkpoint")
+    with pytest.raises(NotImplementedError):
+        integ.run_backward([torch.zeros((5, 2, 64, 128), dtype=torch.float64, device=eng.device)])
     lam, lamy, grad = eng.new_adjoint_buffers()
     gd = eng.groups[0]
     slots = [torch.empty((3,) + tuple(gd["fourier"].shape), dtype=eng.cdtype, device=eng.device)]

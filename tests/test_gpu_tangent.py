@@ -28,7 +28,7 @@ def _setup(prec="fp64", B=2, test=None, seed=5):
     dics = (ics * w).contiguous()
     dics[2] += 1e-2 * wl["ics"][2].flip(-1)
     p = wl["params"]
-    dpar = torch.zeros((9, B), dtype=torch.float64, device=eng.device)
+    dpar = torch.zeros((10, B), dtype=torch.float64, device=eng.device)
     dpar[:4] = torch.stack([0.1 * p["taurad"], 0.1 * p["taudrag"], 0.1 * p["DPhieq"],
                             torch.full((B,), 0.05 * 3.0e5, dtype=torch.float64, device=eng.device)])
     dpar[:4] *= torch.rand((4, B), generator=g, dtype=torch.float64).to(eng.device) - 0.5
@@ -48,9 +48,11 @@ def _forward(eng, flags, wl, ics, params_shift=None, h=0.0):
 
     p = dict(wl["params"])
     if params_shift is not None:
-        for k, name in enumerate(("taurad", "taudrag", "DPhieq", "Phibar", "a", "dt", "K6", "K6Phi", "omega")):
-            if name == "K6Phi" and "K6Phi" not in p:
-                p["K6Phi"] = p["K6"]
+        names = ("taurad", "taudrag", "DPhieq", "Phibar", "a", "dt", "K6", "K6Phi", "omega", "si_alpha")
+        for k in range(params_shift.shape[0]):
+            name = names[k]
+            if name == "si_alpha" and name not in p:
+                p[name] = 0.5
             p[name] = p[name] + h * params_shift[k]
     workloads.apply_params(eng, 0, p)
     eng.init_state([ics.to(eng.rdtype)], flags)
@@ -89,7 +91,7 @@ def test_coefficient_tangents_match_central_differences(cuda, name, row, scale, 
     eng, flags, wl, ics, _, _ = _setup()
     p = wl["params"]
     base = float(p.get(name, p["K6"]))
-    dpar = torch.zeros((9, 2), dtype=torch.float64, device=eng.device)
+    dpar = torch.zeros((10, 2), dtype=torch.float64, device=eng.device)
     dpar[row] = torch.tensor([scale * base, -0.5 * scale * base], dtype=torch.float64)
     zero = torch.zeros_like(ics)
     tl = _tangent(eng, flags, wl, ics, zero, dpar)
@@ -201,6 +203,49 @@ def test_tangent_refuses_unsupported(cuda):
 
     eng, flags, wl, ics, dics, dpar = _setup()
     tf, tr, _ = eng.new_tangent_buffers()
-    for bad in (RunFlagsC(scheme=2), RunFlagsC(raw_filter=True), RunFlagsC(test=1), RunFlagsC(diagnostics=True)):
+    for bad in (RunFlagsC(scheme=1), RunFlagsC(raw_filter=True), RunFlagsC(test=1), RunFlagsC(diagnostics=True)):
         with pytest.raises(RuntimeError):
             eng.tangent_forward(bad, 2, 2, tf, tr, [dpar])
+
+
+SI_PARAMS = (("taurad", 0, 1e-1, 1e-4), ("taudrag", 1, 1e-1, 1e-4), ("DPhieq", 2, 1e-1, 1e-4),
+             ("Phibar", 3, 1e-2, 1e-2), ("a", 4, 1e-2, 1e-4), ("dt", 5, 1e-2, 1e-4), ("K6", 6, 1e-1, 1e-2),
+             ("K6Phi", 7, 1e-1, 1e-2), ("omega", 8, 1e-1, 1e-5), ("si_alpha", 9, 1e-1, 1e-4))
+
+
+def _si_setup(precision="fp64"):
+    from my_swampe_gb300.engine import RunFlagsC
+
+    eng, _, wl, ics, dics, _ = _setup(precision)
+    eng.set_params(0, si_alpha=0.6)
+    wl["params"]["si_alpha"] = 0.6
+    return eng, RunFlagsC(scheme=2, diagnostics=False, t_start=2), wl, ics, dics
+
+
+@pytest.mark.parametrize("name,row,scale,h", SI_PARAMS)
+def test_semi_implicit_parameter_tangents_match_central_differences(cuda, name, row, scale, h):
+    """Tangent of the semi-implicit step (the implicit solve, its coefficients
+    and the lagged remainder) along each parameter, against central differences."""
+    eng, flags, wl, ics, _ = _si_setup()
+    p = wl["params"]
+    base = p[name] if torch.is_tensor(p.get(name)) else torch.full((2,), float(p[name]), dtype=torch.float64,
+                                                                       device=eng.device)
+    dpar = torch.zeros((10, 2), dtype=torch.float64, device=eng.device)
+    dpar[row] = scale * base * torch.tensor([1.0, -0.5], dtype=torch.float64, device=eng.device)
+    tl = _tangent(eng, flags, wl, ics, torch.zeros_like(ics), dpar)
+    fd = (_forward(eng, flags, wl, ics, dpar, h) - _forward(eng, flags, wl, ics, dpar, -h)) / (2 * h)
+    for k, fname in enumerate(("eta", "delta", "Phi", "U", "V")):
+        nrm = float(torch.linalg.norm(fd[k]))
+        rel = float(torch.linalg.norm(tl[k] - fd[k])) / max(nrm, 1e-300)
+        assert rel < 1e-5, (name, fname, rel, nrm)
+
+
+def test_semi_implicit_initial_field_tangent(cuda):
+    eng, flags, wl, ics, dics = _si_setup()
+    dpar = torch.zeros((10, 2), dtype=torch.float64, device=eng.device)
+    tl = _tangent(eng, flags, wl, ics, dics, dpar)
+    h = 1e-6
+    fd = (_forward(eng, flags, wl, ics + h * dics) - _forward(eng, flags, wl, ics - h * dics)) / (2 * h)
+    for k, fname in enumerate(("eta", "delta", "Phi", "U", "V")):
+        rel = float(torch.linalg.norm(tl[k] - fd[k]) / torch.linalg.norm(fd[k]))
+        assert rel < 2e-6, (fname, rel)
