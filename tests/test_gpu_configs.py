@@ -1,8 +1,8 @@
-"""The benchmark configurations as GPU tests (reduced lengths where the CPU
-oracle is the checker):
-  config 1  steady zonal geostrophic flow (test=2 regime, explicit ICs)
-  config 4  M=63 gradients of mean((Phi_T - Phi_target)^2) vs central FD
-  config 5  mixed truncations (M=42, 63, 106) in one launch == separate launches
+"""The benchmark workloads as GPU tests (reduced lengths where the CPU oracle
+is the checker):
+  steady zonal geostrophic flow, M=42, one member (test=2 regime, explicit ICs)
+  M=63 ensemble of 32: gradients of mean((Phi_T - Phi_target)^2) vs central FD
+  mixed truncations (M=42, 63, 106) in one launch == separate launches
 """
 import math
 
@@ -25,7 +25,7 @@ def _steady_ics(M, a=6.37122e6, Omega=7.292e-5):
     return dict(eta0_init=eta0, delta0_init=z, Phi0_init=Phi0, U0_init=U0, V0_init=z), dict(a=a, omega=Omega)
 
 
-def test_config1_steady_zonal_flow_and_blowup_gate(cuda):
+def test_steady_zonal_flow_and_blowup_gate(cuda):
     """Williamson test-2 balanced zonal flow (a = 6.37122e6, u0 = 2 pi a / 12 d,
     dt = 600 s, no diffusion).  The reference scheme does not hold this steady
     state: its modified-Euler coefficients (modEuler_tdiff.py:72-74) make it
@@ -51,7 +51,7 @@ def test_config1_steady_zonal_flow_and_blowup_gate(cuda):
     assert bool(g["last_state"].dead)
 
 
-def test_config5_mixed_truncations_in_one_launch(cuda):
+def test_mixed_truncations_in_one_launch(cuda):
     """Groups at M=42, 63, 106 stepped by one engine (grouped launches) give the
     same states as three single-group engines."""
     import torch
@@ -80,7 +80,7 @@ def test_config5_mixed_truncations_in_one_launch(cuda):
         assert diff == 0.0 or diff <= 1e-12 * out.abs().max().item(), (M, diff)
 
 
-def test_config4_M63_gradients_vs_central_fd(cuda):
+def test_M63_ensemble_gradients_vs_central_fd(cuda):
     """M=63 (96 x 192), B=2 forced, 60 steps, checkpoints every 25: gradients of
     mean((Phi_T - Phi_target)^2) w.r.t. taurad, DPhieq vs central FD (h = 1e-4
     relative; FD noise at 1e-6 relative is above the 1e-5 check here)."""
