@@ -249,3 +249,41 @@ def test_semi_implicit_initial_field_tangent(cuda):
     for k, fname in enumerate(("eta", "delta", "Phi", "U", "V")):
         rel = float(torch.linalg.norm(tl[k] - fd[k]) / torch.linalg.norm(fd[k]))
         assert rel < 2e-6, (fname, rel)
+
+
+@pytest.mark.parametrize("M,scheme", [(63, 0), (106, 0), (63, 2)])
+def test_tangent_other_truncations(cuda, M, scheme):
+    """Tangent along an initial-field direction plus Phibar and a (one
+    combined direction) at M = 63 and 106, against central differences."""
+    from my_swampe_gb300 import workloads
+    from my_swampe_gb300.engine import Engine, RunFlagsC
+
+    eng = Engine([(M, 2)], "fp64")
+    wl = workloads.forced_ensemble(eng, dt=300.0, Phibar=3.0e5, seed=9)
+    flags = RunFlagsC(scheme=scheme, diagnostics=False, t_start=2)
+    ics = wl["ics"]
+    dics = (ics * 0.01).contiguous()
+    dpar = torch.zeros((10, 2), dtype=torch.float64, device=eng.device)
+    dpar[3] = 3.0e3
+    dpar[4] = 8.2e5
+
+    def fwd(sh):
+        p = dict(wl["params"])
+        p["Phibar"] = p["Phibar"] + sh * dpar[3]
+        p["a"] = p["a"] + sh * dpar[4]
+        workloads.apply_params(eng, 0, p)
+        eng.init_state([ics + sh * dics], flags)
+        eng.forward(flags, t0=2, nsteps=6)
+        return eng.output_physical(flags)[0][:5].double()
+
+    workloads.apply_params(eng, 0, wl["params"])
+    eng.init_state([ics], flags)
+    tf, tr, _ = eng.new_tangent_buffers()
+    eng.tangent_init(flags, [ics], [dics], tf, tr, [dpar])
+    eng.tangent_forward(flags, 2, 6, tf, tr, [dpar])
+    tl = eng.tangent_output(flags, tf, tr, [dpar])[0][:5].double()
+    h = 1e-3
+    fd = (fwd(h) - fwd(-h)) / (2 * h)
+    for k, fname in enumerate(("eta", "delta", "Phi", "U", "V")):
+        rel = float(torch.linalg.norm(tl[k] - fd[k]) / torch.linalg.norm(fd[k]))
+        assert rel < 1e-5, (M, scheme, fname, rel)
