@@ -432,7 +432,7 @@ int tangent_steps(swp_plan* p, const swp_group_state* st, const swp_group_tangen
     cfg.step = k;
     cfg.ra_mode = (f->modalflag && t > 2) ? 2 : 1;
     // as forward_steps: the semi-implicit scheme keeps its lagged remainders in the prev slots
-    cfg.write_prev = f->scheme != 2 && k == nsteps - 1;
+    cfg.write_prev = f->scheme != 2 && (f->scheme == 1 || k == nsteps - 1);
     cfg.si_lag_init = f->scheme == 2 && t == f->t_start;
     cfg.incremental = step_incremental(p, f, t) ? 1 : 0;
     LS.cfg = LT.cfg = LG.cfg = LGT.cfg = cfg;
@@ -1067,8 +1067,6 @@ int swp_forward(swp_plan* p, const swp_group_state* st, const swp_flags* f, int 
 static int check_tangent(swp_plan* p, const swp_group_state* st, const swp_group_tangent* tan, const swp_flags* f) {
   if (!p || !st || !tan || !f) return fail(p, SWP_ERR_ARG, "null argument");
   if (int rc = check_scheme(p, f, false)) return rc;
-  if (f->scheme == 1)
-    return fail(p, SWP_ERR_UNSUPPORTED, "the tangent is implemented for the modified-Euler and semi-implicit schemes");
   if (f->raw_filter)
     return fail(p, SWP_ERR_UNSUPPORTED, "the tangent is implemented for the classic Robert-Asselin filter");
   if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "tangent of test=1 (fixed winds) is not implemented");

@@ -127,6 +127,7 @@ __global__ void k_coefs(const double* __restrict__ par, const double* __restrict
       mc[MC_DSIEX * B + b] = (T)w[1];
       mc[MC_DSIITD * B + b] = (T)w[2];
       mc[MC_DSIITR * B + b] = (T)w[3];
+      mc[MC_DITD * B + b] = (T)(dpar ? -dpar[T_TAUDRAG * B + b] / (td * td) : 0.0);
     }
   }
 }

@@ -201,12 +201,19 @@ __device__ __forceinline__ void step_combos_ld(const SpecGroup<T>& G, const Step
 template <typename T>
 __device__ __forceinline__ void tangent_coef_terms_si(const SpecGroup<T>& G, const StepCfg& cfg, int m, int b, int j,
                                                       size_t FS, typename cplx<T>::type* c);
+template <typename T>
+__device__ __forceinline__ void tangent_coef_terms_ex(const SpecGroup<T>& G, const StepCfg& cfg, int m, int b, int j,
+                                                      size_t FS, typename cplx<T>::type* c);
 
 template <typename T>
 __device__ __forceinline__ void tangent_coef_terms(const SpecGroup<T>& G, const StepCfg& cfg, int m, int b, int j,
                                                    size_t FS, typename cplx<T>::type* c) {
   if (cfg.scheme == 2) {
     tangent_coef_terms_si<T>(G, cfg, m, b, j, FS, c);
+    return;
+  }
+  if (cfg.scheme == 1) {
+    tangent_coef_terms_ex<T>(G, cfg, m, b, j, FS, c);
     return;
   }
   typedef typename cplx<T>::type T2;
@@ -314,6 +321,44 @@ __device__ __forceinline__ void tangent_coef_terms_si(const SpecGroup<T>& G, con
   c[SP_PHI1] = csub(c[SP_PHI1], p1);
   if (cfg.forcflag) c[SP_PHI1] = cadd(c[SP_PHI1], cadd(cscale(PFx, dtdt), cscale(dPFx, tdt)));
   c[NSPX + SH_PHI1] = cadd(c[NSPX + SH_PHI1], cscale(D, dtsc));
+}
+
+// The explicit scheme's coefficient tangents (step_combos_ld scheme 1):
+// tstepcoeff, 2 dt Phibar, 2 dt and 1 / taudrag (explicit_tdiff.py:62-78,
+// 134-155, 207-226) on the primal state before the step.
+template <typename T>
+__device__ __forceinline__ void tangent_coef_terms_ex(const SpecGroup<T>& G, const StepCfg& cfg, int m, int b, int j,
+                                                      size_t FS, typename cplx<T>::type* c) {
+  typedef typename cplx<T>::type T2;
+  constexpr int NSPX = SlotCount<T>::NP;
+  const T2* Fp = G.four_p;
+  const size_t o = ((size_t)m * G.B + b) * G.g.J + j;
+  const T* mc = G.mco;
+  const int B = G.B;
+  const T xm = (T)m;
+  const T t = G.jco[(size_t)b * G.g.J + j], dtc = G.djco[(size_t)b * G.g.J + j];
+  const T itd = mc[MC_ITD * B + b], ditd = mc[MC_DITD * B + b];
+  const T dt2 = (T)2 * mc[MC_DDT * B + b];                                  // d(2 dt)
+  const T d2dtpb = (T)2 * mc[MC_DDTPB * B + b];                             // d(2 dt Phibar)
+  const T2 del1 = Fp[F_DELTA * FS + o];
+  const T2 A = Fp[F_A * FS + o], Bm = Fp[F_B * FS + o], C = Fp[F_C * FS + o], D = Fp[F_D * FS + o];
+  // Phi: phi0 - t i m C - 2 dt Phibar delta1 + 2 dt PhiF ; H: t D
+  c[SP_PHI1] = csub(c[SP_PHI1], cadd(cscale(imul(xm, C), dtc), cscale(del1, d2dtpb)));
+  if (cfg.forcflag) c[SP_PHI1] = cadd(c[SP_PHI1], cscale(Fp[F_PHIF * FS + o], dt2));
+  c[NSPX + SH_PHI1] = cadd(c[NSPX + SH_PHI1], cscale(D, dtc));
+  // eta: eta0 - t i m A ; H: t B (plus the forced drag and forcing terms)
+  c[SP_E1] = csub(c[SP_E1], cscale(imul(xm, A), dtc));
+  c[NSPX + SH_E1] = cadd(c[NSPX + SH_E1], cscale(Bm, dtc));
+  if (cfg.forcflag) {
+    const T2 U = Fp[F_U * FS + o], V = Fp[F_V * FS + o], Fm = Fp[F_F * FS + o], Gm = Fp[F_G * FS + o];
+    const T dti = dtc * itd + t * ditd;  // d(t / taudrag)
+    // delta: - t/td i m U + t i m F ; H: t/td V - t G
+    c[SP_D1] = cadd(c[SP_D1], csub(cscale(imul(xm, Fm), dtc), cscale(imul(xm, U), dti)));
+    c[NSPX + SH_D1] = cadd(c[NSPX + SH_D1], csub(cscale(V, dti), cscale(Gm, dtc)));
+    // eta: - t/td i m V + t i m G ; H: t/td U + t F
+    c[SP_E1] = cadd(c[SP_E1], csub(cscale(imul(xm, Gm), dtc), cscale(imul(xm, V), dti)));
+    c[NSPX + SH_E1] = cadd(c[NSPX + SH_E1], cadd(cscale(U, dti), cscale(Fm, dtc)));
+  }
 }
 
 // step_combos_ld on the state in global memory

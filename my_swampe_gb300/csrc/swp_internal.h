@@ -109,6 +109,7 @@ enum MCoef {
   // tangents of the step factors along the call's parameter tangents (tangent-linear launches)
   MC_DT2, MC_DIA2, MC_DHPB, MC_DDTPB, MC_DPBA2, MC_DPFD, MC_DDT, MC_DOM,
   MC_DSIXI, MC_DSIEX, MC_DSIITD, MC_DSIITR,  // of the semi-implicit shares and rates
+  MC_DITD,     // of 1 / taudrag (explicit scheme; no sentinel)
   NMCO
 };
 template <typename T>

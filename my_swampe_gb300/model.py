@@ -412,16 +412,15 @@ def run_model_scan(
     needs_grad = any(_tracked(x) for x in diff_inputs)
     if _tracked(williams_alpha):
         raise NotImplementedError("derivatives through the RAW filter are not implemented")
+    tangent_only = bool(semi_implicit or expflag)  # schemes differentiated by tangent runs (no adjoint)
     if needs_grad:
-        if raw_filter or expflag or test == 1:
-            raise NotImplementedError("derivatives are implemented for the modified-Euler and semi-implicit "
-                                      "schemes with the classic filter and test None or 2")
+        if raw_filter or test == 1:
+            raise NotImplementedError("derivatives are implemented with the classic filter and test None or 2")
         if U0_init is None and (_tracked(eta0_init) or _tracked(delta0_init)):
             raise NotImplementedError("derivatives with respect to eta0_init / delta0_init need U0_init and V0_init")
-        if semi_implicit and any(_tracked(x) for x in ic_inputs) and torch.is_grad_enabled():
-            if any(torch.is_tensor(x) and x.requires_grad for x in ic_inputs):
-                raise NotImplementedError("reverse-mode gradients with respect to the initial fields need the "
-                                          "adjoint, which the semi-implicit scheme does not have (forward mode works)")
+        if tangent_only and torch.is_grad_enabled() and any(torch.is_tensor(x) and x.requires_grad for x in ic_inputs):
+            raise NotImplementedError("reverse-mode gradients with respect to the initial fields need the adjoint, "
+                                      "which the explicit and semi-implicit schemes do not have (forward mode works)")
 
     eng = Engine([(M, B)], precision, device)
     dev = eng.device
@@ -452,8 +451,8 @@ def run_model_scan(
         # the analytic fields are polynomials of degree <= 2 in a, omega, Phibar
         # (initial_conditions.py:18-47, 88-239), so a centred difference is their
         # exact derivative: carry it into the differentiable run
-        # (the semi-implicit scheme, which differentiates by tangent runs, takes
-        # them as initial-field tangents of the parameter directions instead)
+        # (the explicit and semi-implicit schemes, which differentiate by tangent
+        # runs, take them as initial-field tangents of the parameter directions)
         for x, i, name in ((a, 0, "a"), (omega, 1, "omega"), (Phibar, 2, "Phibar")):
             if _tracked(x):
                 h = 1e-3 * abs((av, omv, pb)[i]) or 1e-3
@@ -463,7 +462,7 @@ def run_model_scan(
                 arg[i] -= 2 * h
                 fm = _analytic_ic(M, *arg, test, float(a1), dev)
                 d = [(u - v) / (2 * h) for u, v in zip(fp, fm)]
-                if semi_implicit:
+                if semi_implicit or expflag:
                     ic_derivs[name] = torch.stack([dd.expand(B, J, I) for dd in d], 0)
                     continue
                 dx = x - x.detach()
@@ -506,7 +505,7 @@ def run_model_scan(
         if return_history or diagnostics:
             eng.forward(flags, t0=starttime_eff, nsteps=T, row0=0, diag=diag, hist=hist, write_prev_last=True)
             saved = (four.clone(), gd["member"].clone())
-        dflags = RunFlagsC(scheme=2 if semi_implicit else 0, forcflag=forcflag, diffflag=diffflag,
+        dflags = RunFlagsC(scheme=2 if semi_implicit else (1 if expflag else 0), forcflag=forcflag, diffflag=diffflag,
                            modalflag=modalflag, test=test, diagnostics=False, t_start=starttime_eff)
         dpar = dict(taurad=_per_member(taurad, B, dev), taudrag=_per_member(taudrag, B, dev),
                     DPhieq=_per_member(DPhieq if test is None else 0.0, B, dev), Phibar=_per_member(Phibar, B, dev))

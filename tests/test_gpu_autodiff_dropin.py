@@ -205,3 +205,15 @@ def test_semi_implicit_phibar_gradient_with_analytic_test2_initial_condition(cud
         g_fd = (float(loss(3.0e3 + 0.01)) - float(loss(3.0e3 - 0.01))) / 0.02
     assert abs(g_ad - g_fd) <= 1e-6 * abs(g_fd), (g_ad, g_fd)
     assert abs(g_fw - g_ad) <= 1e-9 * abs(g_ad), (g_fw, g_ad)
+
+
+def test_explicit_scheme_grad_matches_finite_differences(cuda):
+    """expflag=True: gradients through tangent runs (the explicit scheme has no adjoint)."""
+    def loss(d):
+        return _loss("DPhieq", d, expflag=True, dt=300.0)
+
+    th = torch.tensor(4.0e6, dtype=torch.float64, device="cuda", requires_grad=True)
+    g = float(torch.autograd.grad(loss(th), th)[0])
+    with torch.no_grad():
+        fd = (float(loss(4.0e6 + 1.0)) - float(loss(4.0e6 - 1.0))) / 2.0
+    assert g != 0.0 and abs(g - fd) <= 1e-4 * abs(fd), (g, fd)

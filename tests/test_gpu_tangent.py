@@ -203,7 +203,7 @@ def test_tangent_refuses_unsupported(cuda):
 
     eng, flags, wl, ics, dics, dpar = _setup()
     tf, tr, _ = eng.new_tangent_buffers()
-    for bad in (RunFlagsC(scheme=1), RunFlagsC(raw_filter=True), RunFlagsC(test=1), RunFlagsC(diagnostics=True)):
+    for bad in (RunFlagsC(raw_filter=True), RunFlagsC(test=1), RunFlagsC(diagnostics=True)):
         with pytest.raises(RuntimeError):
             eng.tangent_forward(bad, 2, 2, tf, tr, [dpar])
 
@@ -287,3 +287,26 @@ def test_tangent_other_truncations(cuda, M, scheme):
     for k, fname in enumerate(("eta", "delta", "Phi", "U", "V")):
         rel = float(torch.linalg.norm(tl[k] - fd[k]) / torch.linalg.norm(fd[k]))
         assert rel < 1e-5, (M, scheme, fname, rel)
+
+
+@pytest.mark.parametrize("name,row,scale,h", [("taurad", 0, 1e-1, 1e-4), ("taudrag", 1, 1e-1, 1e-4),
+                                              ("Phibar", 3, 1e-2, 1e-2), ("a", 4, 1e-2, 1e-4),
+                                              ("dt", 5, 1e-2, 1e-4), ("K6", 6, 1e-1, 1e-2)])
+def test_explicit_scheme_tangents_match_central_differences(cuda, name, row, scale, h):
+    """Tangent of the explicit leapfrog (expflag) along parameters, and along
+    an initial-field direction, against central differences."""
+    from my_swampe_gb300.engine import RunFlagsC
+
+    eng, _, wl, ics, dics, _ = _setup()
+    flags = RunFlagsC(scheme=1, diagnostics=False, t_start=2)
+    p = wl["params"]
+    base = p[name] if torch.is_tensor(p.get(name)) else torch.full((2,), float(p[name]), dtype=torch.float64,
+                                                                       device=eng.device)
+    dpar = torch.zeros((10, 2), dtype=torch.float64, device=eng.device)
+    dpar[row] = scale * base * torch.tensor([1.0, -0.5], dtype=torch.float64, device=eng.device)
+    tl = _tangent(eng, flags, wl, ics, 1e-3 * dics, dpar)
+    fd = (_forward(eng, flags, wl, ics + h * 1e-3 * dics, dpar, h) -
+          _forward(eng, flags, wl, ics - h * 1e-3 * dics, dpar, -h)) / (2 * h)
+    for k, fname in enumerate(("eta", "delta", "Phi", "U", "V")):
+        rel = float(torch.linalg.norm(tl[k] - fd[k]) / torch.linalg.norm(fd[k]))
+        assert rel < 1e-5, (name, fname, rel)
