@@ -3,7 +3,6 @@ jax.jvp / jax.jacfwd through run_model_scan (autodiff_utils.py:27-89 fwd_grad):
 against central differences of the FP64 forward, against the hand-written
 adjoint by the dot-product identity <w, J v> = <J^T w, v>, and fwd_grad
 against the reverse-mode gradient."""
-import numpy as np
 import pytest
 import torch
 import torch.autograd.forward_ad as fwAD
