@@ -461,7 +461,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     // (GM_TL_INIT: the tangent ICs -> tangent state; the Fourier carries and
     // residuals are linear in the ICs, the nonlinear terms are linearised
     // about the primal ICs in phys_p)
-    // round 1: eta, delta, Phi, U, V -> Fourier curr (+prev, RA carry) and residuals
+    // batch 1: eta, delta, Phi, U, V -> Fourier curr (+prev, RA carry) and residuals
     __syncthreads();
     const int nf = 5;
     for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
@@ -498,7 +498,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       G.resid[po + 1] = x[1] - z.y;
     }
     __syncthreads();
-    // round 2: nonlinear terms and forcing from the raw initial grids (model.py:723-732)
+    // batch 2: nonlinear terms and forcing from the raw initial grids (model.py:723-732)
     double lrms = 0.0, lspin = 1e300;
     const int nout = ph.forced ? 8 : 5;
     for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
