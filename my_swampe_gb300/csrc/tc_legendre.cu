@@ -48,7 +48,7 @@ constexpr int TC_RES = 8 * TC_CNT * 16;            // [g][n-m][member, re/im]
 constexpr int TC_OST = 2 * TC_J + 2;               // output staging row stride (floats)
 constexpr int TC_NOUT = 7;                         // eta, delta, Phi, Uprep, Vprep | U_H, V_H
 constexpr int TC_COEF = 5 * TC_MT * TC_CNT;
-constexpr int TC_TMEM_COLS = 256;                  // D1: 2 x 32, D2: 2 x 64
+constexpr int TC_TMEM_COLS = 256;                  // D1: 2 x (2 x 32), D2: 2 x 64 (D2 reuses D1's columns)
 static_assert(TC_RES0 + TC_RES <= TC_A, "D1 staging must fit in the A region");
 static_assert(TC_NOUT * TC_MT * TC_OST <= TC_A, "output staging must fit in the A region");
 // the MMA reads all 128 rows of the last A2 operand: they must stay in the A region
@@ -143,6 +143,24 @@ __device__ __forceinline__ void mma_3xtf32(uint32_t d_tmem, uint32_t aH, uint32_
     tc::mma_tf32(d_tmem, tc::make_desc(aL + off, 128, sbo), tc::make_desc(bH + off, 128, sbo), idesc, 1);
   }
 }
+// The same K-sweep in two MMAs per K-step.  The issue of an MMA, not its
+// arithmetic, is what the narrow (N = 32) GEMM1 waits on, so a_hi is applied
+// to b_hi and b_lo in one MMA of width 2n (the lo tile follows the hi tile in
+// shared memory: rows n..2n-1 of that operand), giving d[0, n) = a_hi b_hi and
+// d[n, 2n) = a_hi b_lo; a_lo b_hi then accumulates onto d[n, 2n).  The product
+// is d[0, n) + d[n, 2n).  idesc_2n / idesc_n describe the 128 x 2n / 128 x n MMAs.
+__device__ __forceinline__ void mma_3xtf32_2(uint32_t d_tmem, uint32_t aH, uint32_t aL, uint32_t bH, int n, int K,
+                                             uint32_t idesc_2n, uint32_t idesc_n) {
+  const uint32_t sbo = (uint32_t)(K / 4) * 128u;
+  for (int kk = 0; kk < K / 8; ++kk) {
+    const uint32_t off = (uint32_t)kk * 256u;
+    tc::mma_tf32(d_tmem, tc::make_desc(aH + off, 128, sbo), tc::make_desc(bH + off, 128, sbo), idesc_2n, kk > 0);
+    tc::mma_tf32(d_tmem + (uint32_t)n, tc::make_desc(aL + off, 128, sbo), tc::make_desc(bH + off, 128, sbo), idesc_n,
+                 1);
+  }
+}
+// the hi tile of a [hi, lo][N][K] operand pair is followed by its lo tile at (N / 8) stride offsets
+static_assert(TC_N1 * TC_K1 * 4 == (TC_N1 / 8) * (TC_K1 / 4) * 128, "B1 lo tile must follow its hi tile");
 }  // namespace
 
 __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ SpecLaunch<float> L,
@@ -288,7 +306,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       }
     }
   };
-  const uint32_t idesc1 = tc::idesc_tf32(TC_ROWS, TC_N1);
+  const uint32_t idesc1 = tc::idesc_tf32(TC_ROWS, TC_N1), idesc1w = tc::idesc_tf32(TC_ROWS, 2 * TC_N1);
   const uint32_t idesc2 = tc::idesc_tf32(TC_ROWS, TC_N2);
   const uint32_t aHs = tc::smem_u32(sA), aLs = aHs + (uint32_t)(TC_ROWS * TC_K1 * 4);
   const uint32_t bbase = tc::smem_u32(sB);
@@ -301,7 +319,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     __syncthreads();
     if (threadIdx.x == 0) {
       if (!tc::mbar_wait_bounded(&mbar[0], 0)) *sflag = 1;
-      if (!*sflag) mma_3xtf32(tbase, aHs, aLs, bbase, bbase + TC_N1 * TC_K1 * 4, TC_K1, idesc1);
+      if (!*sflag) mma_3xtf32_2(tbase, aHs, aLs, bbase, TC_N1, TC_K1, idesc1w, idesc1);
       tc::mma_commit(&mbar[1]);
       n_c1 = 1;
     }
@@ -316,7 +334,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     __syncthreads();
     if (threadIdx.x == 0) {
       const uint32_t b1 = bbase + 2u * TC_N1 * TC_K1 * 4u;
-      mma_3xtf32(tbase + TC_N1, aHs, aLs, b1, b1 + TC_N1 * TC_K1 * 4, TC_K1, idesc1);
+      mma_3xtf32_2(tbase + 2 * TC_N1, aHs, aLs, b1, TC_N1, TC_K1, idesc1w, idesc1);
       tc::mma_commit(&mbar[1]);
       n_c1 = 2;
     }
@@ -339,8 +357,11 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       const int Cp = par ? C1 : C0;
 #pragma unroll
       for (int c0 = 0; c0 < TC_N1; c0 += 16) {
-        float v[16];
-        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(par * TC_N1 + c0), v);
+        float v[16], v1[16];
+        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(2 * par * TC_N1 + c0), v);
+        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((2 * par + 1) * TC_N1 + c0), v1);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] += v1[i];
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           const int c = c0 + i;
@@ -651,7 +672,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
       }
     }
   };
-  const uint32_t idesc1 = tc::idesc_tf32(TC_ROWS, TC_N1);
+  const uint32_t idesc1 = tc::idesc_tf32(TC_ROWS, TC_N1), idesc1w = tc::idesc_tf32(TC_ROWS, 2 * TC_N1);
   const uint32_t idesc2 = tc::idesc_tf32(TC_ROWS, TC_N2);
   const uint32_t aHs = tc::smem_u32(sA), aLs = aHs + (uint32_t)(TC_ROWS * TC_K1 * 4);
   const uint32_t bbase = tc::smem_u32(sB);
@@ -664,7 +685,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
     __syncthreads();
     if (threadIdx.x == 0) {
       if (!tc::mbar_wait_bounded(&mbar[0], 0)) *sflag = 1;
-      if (!*sflag) mma_3xtf32(tbase, aHs, aLs, bbase, bbase + TC_N1 * TC_K1 * 4, TC_K1, idesc1);
+      if (!*sflag) mma_3xtf32_2(tbase, aHs, aLs, bbase, TC_N1, TC_K1, idesc1w, idesc1);
       tc::mma_commit(&mbar[1]);
       n_c1 = 1;
     }
@@ -679,7 +700,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
     __syncthreads();
     if (threadIdx.x == 0) {
       const uint32_t b1 = bbase + 2u * TC_N1 * TC_K1 * 4u;
-      mma_3xtf32(tbase + TC_N1, aHs, aLs, b1, b1 + TC_N1 * TC_K1 * 4, TC_K1, idesc1);
+      mma_3xtf32_2(tbase + 2 * TC_N1, aHs, aLs, b1, TC_N1, TC_K1, idesc1w, idesc1);
       tc::mma_commit(&mbar[1]);
       n_c1 = 2;
     }
@@ -701,8 +722,11 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
       const int Cp = par ? C1 : C0;
 #pragma unroll
       for (int c0 = 0; c0 < TC_N1; c0 += 16) {
-        float v[16];
-        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(par * TC_N1 + c0), v);
+        float v[16], v1[16];
+        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(2 * par * TC_N1 + c0), v);
+        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((2 * par + 1) * TC_N1 + c0), v1);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] += v1[i];
         if (gq < 7) {
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
