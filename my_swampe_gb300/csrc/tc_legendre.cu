@@ -256,6 +256,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   const int bt = (warp >> 2) * 4 + (lane >> 3);
   T2 xs[NSLOT], xa[NSLOT];
   T2 pold[2][3], pmid[2][3];  // write-out carries, loaded ahead of GEMM2
+  T wal[2], wan[2];           // the write-out's filter weights, loaded with them
   // one thread waits on each mbarrier and the block barrier releases the rest:
   // 256 spinning threads would take issue slots from the co-resident CTA
   bool ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[3], 0) : true;
@@ -443,7 +444,11 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
       const int t = threadIdx.x + u * 256, bti = t / J, j = t % J;
-      if (bti < mt) load_step_point<T>(G, cfg, incr, FS, ((size_t)m * G.B + b0 + bti) * J + j, pold[u], pmid[u]);
+      if (bti < mt) {
+        load_step_point<T>(G, cfg, incr, FS, ((size_t)m * G.B + b0 + bti) * J + j, pold[u], pmid[u]);
+        wal[u] = G.mco[(cfg.raw ? MC_RAWM : MC_ALPHA) * G.B + b0 + bti];
+        wan[u] = cfg.raw ? G.mco[MC_RAWN * G.B + b0 + bti] : (T)0;
+      }
     }
     if (threadIdx.x == 0) {
       if (!tc::mbar_wait_bounded(&mbar[0], 1)) *sflag = 1;
@@ -502,9 +507,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       const size_t o = ((size_t)m * G.B + b) * J + j;
       auto get = [&](int f) { return *(const float2*)&Out[(size_t)(f * TC_MT + bti) * TC_OST + 2 * j]; };
       const T2 nw[3] = {get(0), get(1), get(2)};
-      const T al = G.mco[(cfg.raw ? MC_RAWM : MC_ALPHA) * G.B + b];
-      const T an = cfg.raw ? G.mco[MC_RAWN * G.B + b] : (T)0;
-      store_step_point<T>(G, cfg, incr, FS, o, al, an, nw, cfg.test != 1, cadd(get(3), get(5)),
+      store_step_point<T>(G, cfg, incr, FS, o, wal[u], wan[u], nw, cfg.test != 1, cadd(get(3), get(5)),
                           cadd(get(4), get(6)), pold[u], pmid[u]);
     }
     if (m == 0 && threadIdx.x < mt && !sdead[threadIdx.x]) {
