@@ -115,6 +115,39 @@ __device__ __forceinline__ void stage_rows(const C& c, const typename cplx<T>::t
   }
 }
 
+// The adjoint step's batch 1 staged as stage_rows would: lambda of the first
+// nz nonlinear terms (F_A, F_B, ...) scaled 1/I at m = 0 and 1/(2I) above it,
+// then the primal eta, Phi, U, V unscaled.  The rows are copied raw with
+// cp.async, so that the copies can be issued at the start of the CTA and their
+// latency covers its set-up; adj_stage_finish completes them and applies the
+// scales.  Each thread scales exactly the elements it copied (same index loop),
+// so it needs only its own copies complete; a block barrier must follow.
+template <typename T, typename C>
+__device__ __forceinline__ void adj_stage_issue(const C& c, const GridGroup<T>& G, int nz, int nb1,
+                                                typename cplx<T>::type* stage) {
+  typedef typename cplx<T>::type T2;
+  constexpr int n1 = C::M + 1;
+  const int total = nb1 * n1 * C::JB;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int r = t % C::JB, k = (t / C::JB) % n1, f = t / (C::JB * n1);
+    const int q = f - nz;
+    const T2* p = f < nz ? G.lam + (size_t)(F_A + f) * c.FS
+                         : G.primal + (size_t)(q == 0 ? F_ETA : q == 1 ? F_PHI : q == 2 ? F_U : F_V) * c.FS;
+    cp_async<(int)sizeof(T2)>(stage + (f * C::JB + r) * n1 + k, p + ((size_t)k * c.B + c.b) * C::J + c.j0 + r);
+  }
+}
+template <typename T, typename C>
+__device__ __forceinline__ void adj_stage_finish(const C& c, int nz, typename cplx<T>::type* stage) {
+  typedef typename cplx<T>::type T2;
+  constexpr int n1 = C::M + 1;
+  cp_async_wait_all();
+  for (int t = threadIdx.x; t < nz * n1 * C::JB; t += blockDim.x) {
+    const int r = t % C::JB, k = (t / C::JB) % n1, f = t / (C::JB * n1);
+    T2& v = stage[(f * C::JB + r) * n1 + k];
+    v = cscale(v, k == 0 ? c.invI : c.invI * (T)0.5);
+  }
+}
+
 // C2R of the `nf` x JB staged rows (layout of stage_rows, scales already
 // applied): the half-length spectrum Z (c2r_pre) is formed inside the first,
 // twiddle-free radix-8 pass, which writes `other`; the remaining passes run in
@@ -202,6 +235,12 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
   c.twI = stw + L;
   c.sred = (double*)(((uintptr_t)(stw + 2 * L + 1) + 15) & ~(uintptr_t)15);
   c.invI = (T)1 / (T)I;
+  // adjoint step: batch 1's rows (the lambda of nz nonlinear terms with F, G
+  // taken from B, A inside a forced sweep, then 4 primal fields) are copied
+  // before the set-up below, which their latency then covers
+  const bool adj_tied = MODE == GM_ADJ_STEP && cfg.test == 0 && cfg.lam_fg_tied != 0;
+  const int adj_nz = adj_tied ? 6 : (cfg.test == 0 ? 8 : 5);
+  if (MODE == GM_ADJ_STEP) adj_stage_issue<T>(c, G, adj_nz, adj_nz + 4, c.bufB);
   for (int i = threadIdx.x; i < I; i += blockDim.x) c.sday[i] = G.g.dayc[i];
   for (int i = threadIdx.x; i < 2 * L + 1; i += blockDim.x) stw[i] = i < L ? G.g.twL[i] : G.g.twI[i - L];
   if (threadIdx.x == 0) { c.sred[0] = 0.0; c.sred[1] = 1e300; c.sred[2] = 1e300; c.sred[3] = -1e300; }
@@ -576,8 +615,12 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       else if (f < nb1) { src[f] = G.primal + pf[f - nz] * FS; s0[f] = (T)1; s1[f] = (T)1; }
       else { src[f] = nullptr; s0[f] = s1[f] = (T)0; }
     }
-    __syncthreads();
-    stage_rows<T>(c, src, nb1, bufB, s0, s1);
+    if (MODE == GM_ADJ_STEP) {
+      adj_stage_finish<T>(c, nz, bufB);  // the copies issued at the start of the CTA
+    } else {
+      __syncthreads();
+      stage_rows<T>(c, src, nb1, bufB, s0, s1);
+    }
     __syncthreads();
     T2* zin = c2r_transform<T>(c, bufB, nb1, bufA);
     T2* zout = (zin == bufA) ? bufB : bufA;

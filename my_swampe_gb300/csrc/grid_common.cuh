@@ -54,6 +54,19 @@ __device__ __forceinline__ T2 r2c_post(const T2* Z, int L, int k, const T2* twI,
   return cscale(cadd(e, cmul(o, twI[k])), scale);
 }
 
+// Asynchronous global -> shared copy of one element (8 or 16 bytes, aligned to
+// its size); the issuing thread completes its copies with cp_async_wait_all.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  static_assert(BYTES == 8 || BYTES == 16, "cp.async copies 8 or 16 bytes here");
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  if (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 __device__ __forceinline__ void atomic_min_d(double* addr, double v) {
   unsigned long long* a = (unsigned long long*)addr;
   unsigned long long old = *a, assumed;
