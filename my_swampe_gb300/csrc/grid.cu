@@ -148,6 +148,25 @@ __device__ __forceinline__ void adj_stage_finish(const C& c, int nz, typename cp
   }
 }
 
+// cp.async form of stage_rows without scales for the step's fields at staged
+// positions f0 .. f0+nf-1 of `four`, where position f holds field step_field(f):
+// eta, Phi, U, V, then delta (history runs).  Completed by cp_async_wait_all
+// and a block barrier.
+__host__ __device__ constexpr int step_field(int f) {
+  return f == 0 ? F_ETA : f == 1 ? F_PHI : f == 2 ? F_U : f == 3 ? F_V : F_DELTA;
+}
+template <typename T, typename C>
+__device__ __forceinline__ void step_stage_issue(const C& c, const typename cplx<T>::type* four, int f0, int nf,
+                                                 int fixed_field, typename cplx<T>::type* stage) {
+  constexpr int n1 = C::M + 1;
+  for (int t = threadIdx.x; t < nf * n1 * C::JB; t += blockDim.x) {
+    const int r = t % C::JB, k = (t / C::JB) % n1, f = f0 + t / (C::JB * n1);
+    const int fld = fixed_field >= 0 ? fixed_field : step_field(f);
+    cp_async<(int)sizeof(typename cplx<T>::type)>(stage + (f * C::JB + r) * n1 + k,
+                                                  four + (size_t)fld * c.FS + ((size_t)k * c.B + c.b) * C::J + c.j0 + r);
+  }
+}
+
 // C2R of the `nf` x JB staged rows (layout of stage_rows, scales already
 // applied): the half-length spectrum Z (c2r_pre) is formed inside the first,
 // twiddle-free radix-8 pass, which writes `other`; the remaining passes run in
@@ -241,6 +260,10 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
   const bool adj_tied = MODE == GM_ADJ_STEP && cfg.test == 0 && cfg.lam_fg_tied != 0;
   const int adj_nz = adj_tied ? 6 : (cfg.test == 0 ? 8 : 5);
   if (MODE == GM_ADJ_STEP) adj_stage_issue<T>(c, G, adj_nz, adj_nz + 4, c.bufB);
+  // step: likewise eta, Phi, U, V (and delta for the history); the diagnostic
+  // Phi row, which depends on the member's blow-up flag, follows the set-up
+  const int step_nfix = G.hist ? 5 : 4;
+  if (MODE == GM_STEP) step_stage_issue<T>(c, G.four, 0, step_nfix, -1, c.bufB);
   for (int i = threadIdx.x; i < I; i += blockDim.x) c.sday[i] = G.g.dayc[i];
   for (int i = threadIdx.x; i < 2 * L + 1; i += blockDim.x) stw[i] = i < L ? G.g.twL[i] : G.g.twI[i - L];
   if (threadIdx.x == 0) { c.sred[0] = 0.0; c.sred[1] = 1e300; c.sred[2] = 1e300; c.sred[3] = -1e300; }
@@ -315,8 +338,14 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
         if (rf >= 0 && G.resid && w != (T)0) { wv[f] = w; rfv[f] = rf; }
       }
     }
-    __syncthreads();
-    stage_rows<T>(c, src, nf, bufB);
+    if (MODE == GM_STEP) {
+      // the copies issued at the start of the CTA, plus the diagnostic row
+      if (cfg.diagnostics) step_stage_issue<T>(c, G.four, step_nfix, 1, dead ? F_PHI : F_PHI_MID, bufB);
+      cp_async_wait_all();
+    } else {
+      __syncthreads();
+      stage_rows<T>(c, src, nf, bufB);
+    }
     __syncthreads();
     T2* zin = c2r_transform<T>(c, bufB, nf, bufA);
     T2* zout = (zin == bufA) ? bufB : bufA;
