@@ -115,10 +115,11 @@ __device__ __forceinline__ void stage_rows(const C& c, const typename cplx<T>::t
   }
 }
 
-// The adjoint step's batch 1 staged as stage_rows would: lambda of the first
-// nz nonlinear terms (F_A, F_B, ...) scaled 1/I at m = 0 and 1/(2I) above it,
-// then the primal eta, Phi, U, V unscaled.  The rows are copied raw with
-// cp.async, so that the copies can be issued at the start of the CTA and their
+// The adjoint step's batch 1: lambda of the first nz nonlinear terms (F_A,
+// F_B, ...) scaled 1/I at m = 0 and 1/(2I) above it, then the primal eta, Phi,
+// U, V unscaled, staged as [f][m][r] (rows fastest, so that one 16-byte
+// cp.async moves Rows16 adjacent rows; c2r_transform<..., true> reads this
+// layout).  The copies are issued at the start of the CTA, so that their
 // latency covers its set-up; adj_stage_finish completes them and applies the
 // scales.  Each thread scales exactly the elements it copied (same index loop),
 // so it needs only its own copies complete; a block barrier must follow.
@@ -127,52 +128,62 @@ __device__ __forceinline__ void adj_stage_issue(const C& c, const GridGroup<T>& 
                                                 typename cplx<T>::type* stage) {
   typedef typename cplx<T>::type T2;
   constexpr int n1 = C::M + 1;
-  const int total = nb1 * n1 * C::JB;
+  constexpr int EPC = Rows16<T2>::N, RP = C::JB / EPC;
+  const int total = nb1 * n1 * RP;
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
-    const int r = t % C::JB, k = (t / C::JB) % n1, f = t / (C::JB * n1);
+    const int rp = t % RP, k = (t / RP) % n1, f = t / (RP * n1);
     const int q = f - nz;
     const T2* p = f < nz ? G.lam + (size_t)(F_A + f) * c.FS
                          : G.primal + (size_t)(q == 0 ? F_ETA : q == 1 ? F_PHI : q == 2 ? F_U : F_V) * c.FS;
-    cp_async<(int)sizeof(T2)>(stage + (f * C::JB + r) * n1 + k, p + ((size_t)k * c.B + c.b) * C::J + c.j0 + r);
+    cp_async<16>(stage + (f * n1 + k) * C::JB + rp * EPC, p + ((size_t)k * c.B + c.b) * C::J + c.j0 + rp * EPC);
   }
 }
 template <typename T, typename C>
 __device__ __forceinline__ void adj_stage_finish(const C& c, int nz, typename cplx<T>::type* stage) {
   typedef typename cplx<T>::type T2;
   constexpr int n1 = C::M + 1;
+  constexpr int EPC = Rows16<T2>::N, RP = C::JB / EPC;
   cp_async_wait_all();
-  for (int t = threadIdx.x; t < nz * n1 * C::JB; t += blockDim.x) {
-    const int r = t % C::JB, k = (t / C::JB) % n1, f = t / (C::JB * n1);
-    T2& v = stage[(f * C::JB + r) * n1 + k];
-    v = cscale(v, k == 0 ? c.invI : c.invI * (T)0.5);
+  for (int t = threadIdx.x; t < nz * n1 * RP; t += blockDim.x) {
+    const int rp = t % RP, k = (t / RP) % n1, f = t / (RP * n1);
+    const T sc = k == 0 ? c.invI : c.invI * (T)0.5;
+#pragma unroll
+    for (int e = 0; e < EPC; ++e) {
+      T2& v = stage[(f * n1 + k) * C::JB + rp * EPC + e];
+      v = cscale(v, sc);
+    }
   }
 }
 
-// cp.async form of stage_rows without scales for the step's fields at staged
-// positions f0 .. f0+nf-1 of `four`, where position f holds field step_field(f):
-// eta, Phi, U, V, then delta (history runs).  Completed by cp_async_wait_all
-// and a block barrier.
+// The step's fields at staged positions f0 .. f0+nf-1 of `four` (position f
+// holds step_field(f): eta, Phi, U, V, then delta for history runs, unless
+// fixed_field >= 0 names the field), unscaled, in the [f][m][r] layout of
+// adj_stage_issue, by 16-byte cp.async.  Completed by cp_async_wait_all and a
+// block barrier.
 __host__ __device__ constexpr int step_field(int f) {
   return f == 0 ? F_ETA : f == 1 ? F_PHI : f == 2 ? F_U : f == 3 ? F_V : F_DELTA;
 }
 template <typename T, typename C>
 __device__ __forceinline__ void step_stage_issue(const C& c, const typename cplx<T>::type* four, int f0, int nf,
                                                  int fixed_field, typename cplx<T>::type* stage) {
+  typedef typename cplx<T>::type T2;
   constexpr int n1 = C::M + 1;
-  for (int t = threadIdx.x; t < nf * n1 * C::JB; t += blockDim.x) {
-    const int r = t % C::JB, k = (t / C::JB) % n1, f = f0 + t / (C::JB * n1);
+  constexpr int EPC = Rows16<T2>::N, RP = C::JB / EPC;
+  for (int t = threadIdx.x; t < nf * n1 * RP; t += blockDim.x) {
+    const int rp = t % RP, k = (t / RP) % n1, f = f0 + t / (RP * n1);
     const int fld = fixed_field >= 0 ? fixed_field : step_field(f);
-    cp_async<(int)sizeof(typename cplx<T>::type)>(stage + (f * C::JB + r) * n1 + k,
-                                                  four + (size_t)fld * c.FS + ((size_t)k * c.B + c.b) * C::J + c.j0 + r);
+    cp_async<16>(stage + (f * n1 + k) * C::JB + rp * EPC,
+                 four + (size_t)fld * c.FS + ((size_t)k * c.B + c.b) * C::J + c.j0 + rp * EPC);
   }
 }
 
-// C2R of the `nf` x JB staged rows (layout of stage_rows, scales already
+// C2R of the `nf` x JB staged rows (layout of stage_rows, [f][r][m], or with
+// FMR the [f][m][r] layout of the cp.async staging; scales already
 // applied): the half-length spectrum Z (c2r_pre) is formed inside the first,
 // twiddle-free radix-8 pass, which writes `other`; the remaining passes run in
 // place of the staged rows.  Returns the buffer holding x_{2n} + i x_{2n+1}
 // ([t][n], stride LS).
-template <typename T, typename C>
+template <typename T, typename C, bool FMR = false>
 __device__ __forceinline__ typename cplx<T>::type* c2r_transform(const C& c, typename cplx<T>::type* stage, int nf,
                                                                   typename cplx<T>::type* other) {
   typedef typename cplx<T>::type T2;
@@ -181,10 +192,10 @@ __device__ __forceinline__ typename cplx<T>::type* c2r_transform(const C& c, typ
   const FastDiv divt(ntr);
   for (int task = threadIdx.x; task < ntr * PER; task += blockDim.x) {
     const int j = divt(task), t = task - j * ntr;
-    const T2* y = stage + (size_t)t * n1;
+    const T2* y = FMR ? stage + (size_t)(t / C::JB) * n1 * C::JB + t % C::JB : stage + (size_t)t * n1;
     T2 v[8];
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = c2r_pre<T2, T>(y, 1, C::M, L, j + r * PER, c.twI, (T)1, (T)1);
+    for (int r = 0; r < 8; ++r) v[r] = c2r_pre<T2, T>(y, FMR ? C::JB : 1, C::M, L, j + r * PER, c.twI, (T)1, (T)1);
     dftR<8, +1>(v);
     T2* dst = other + (size_t)t * LS + j * 8;
 #pragma unroll
@@ -204,12 +215,16 @@ __device__ __forceinline__ void write_r2c(const C& c, const typename cplx<T>::ty
   if (threadIdx.x < 16) s_dst[threadIdx.x] = (int)threadIdx.x < nf ? dst[threadIdx.x] : nullptr;
   __syncthreads();
   constexpr int n1 = C::M + 1;
+  constexpr int EPC = Rows16<T2>::N, RP = C::JB / EPC;  // rows per 16-byte store, stores per (field, m)
   // unrolled so that several independent bins are in flight per thread
 #pragma unroll 4
-  for (int t = threadIdx.x; t < nf * n1 * C::JB; t += blockDim.x) {
-    const int r = t % C::JB, k = (t / C::JB) % n1, q = t / (C::JB * n1);
-    const T2 v = r2c_post<T2, T>(res + ((size_t)q * C::JB + r) * C::LS, C::L, k, c.twI, k == 0 ? s0 : s);
-    s_dst[q][((size_t)k * c.B + c.b) * C::J + c.j0 + r] = v;
+  for (int t = threadIdx.x; t < nf * n1 * RP; t += blockDim.x) {
+    const int rp = t % RP, k = (t / RP) % n1, q = t / (RP * n1);
+    T2 v[EPC];
+#pragma unroll
+    for (int e = 0; e < EPC; ++e)
+      v[e] = r2c_post<T2, T>(res + ((size_t)q * C::JB + rp * EPC + e) * C::LS, C::L, k, c.twI, k == 0 ? s0 : s);
+    st_rows16(s_dst[q] + ((size_t)k * c.B + c.b) * C::J + c.j0 + rp * EPC, v);
   }
 }
 
@@ -347,7 +362,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       stage_rows<T>(c, src, nf, bufB);
     }
     __syncthreads();
-    T2* zin = c2r_transform<T>(c, bufB, nf, bufA);
+    T2* zin = MODE == GM_STEP ? c2r_transform<T, Ctx, true>(c, bufB, nf, bufA) : c2r_transform<T>(c, bufB, nf, bufA);
     T2* zout = (zin == bufA) ? bufB : bufA;
     // initial-condition residual (non-zero only before a member's first step and
     // for the fixed test-1 winds): added in shared memory, off the hot loop
@@ -651,7 +666,7 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       stage_rows<T>(c, src, nb1, bufB, s0, s1);
     }
     __syncthreads();
-    T2* zin = c2r_transform<T>(c, bufB, nb1, bufA);
+    T2* zin = MODE == GM_ADJ_STEP ? c2r_transform<T, Ctx, true>(c, bufB, nb1, bufA) : c2r_transform<T>(c, bufB, nb1, bufA);
     T2* zout = (zin == bufA) ? bufB : bufA;
     T gacc[NGRAD] = {(T)0, (T)0, (T)0, (T)0};
     for (int t = threadIdx.x; t < JB * L; t += blockDim.x) {
@@ -698,19 +713,21 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     if (MODE == GM_ADJ_STEP) {
       // adjoint of x = Re(Y_0) + 2 Re sum_{m>=1} Y_m e^{i theta}:  lambda Y_m = c_m sum_i lambda x_i e^{-i theta}
       const int n1 = M + 1;
-      const int yf[5] = {F_ETA, F_DELTA, F_PHI, F_U, F_V};
-      const int rmap[5] = {0, -1, 1, 2, 3};
-      constexpr int NY = 5 * (M + 1) * JB;
+      // lambda_y field q: eta, delta, Phi, U, V; of them, all but delta (q = 1)
+      // add the R2C of transform q - (q > 1) of this batch
+      constexpr int EPC = Rows16<T2>::N, RP = JB / EPC;
+      constexpr int NY = 5 * (M + 1) * RP;
       constexpr int NU = (NY + 255) / 256;
-      // a thread's lambda loads are issued before the transforms, so that
-      // their latency overlaps them, and before its first store
-      T2 lv[NU];
+      // a thread's lambda loads (16 bytes: EPC adjacent rows) are issued before
+      // the transforms, so that their latency overlaps them, and before its first store
+      T2 lv[NU][EPC];
 #pragma unroll
       for (int u = 0; u < NU; ++u) {
         const int t = threadIdx.x + u * 256;
         if (t < NY) {
-          const int r = t % JB, k = (t / JB) % n1, q = t / (JB * n1);
-          lv[u] = G.lam[yf[q] * FS + ((size_t)k * B + b) * J + j0 + r];
+          const int rp = t % RP, k = (t / RP) % n1, q = t / (RP * n1);
+          const int fy = q == 0 ? F_ETA : q == 1 ? F_DELTA : q == 2 ? F_PHI : q == 3 ? F_U : F_V;
+          ld_rows16(G.lam + (size_t)fy * FS + ((size_t)k * B + b) * J + j0 + rp * EPC, lv[u]);
         }
       }
       T2* res = cfft_batch_c<-1, L>(zout, zin, 4 * JB, c.twL);
@@ -718,11 +735,15 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       for (int u = 0; u < NU; ++u) {
         const int t = threadIdx.x + u * 256;
         if (t < NY) {
-          const int r = t % JB, k = (t / JB) % n1, q = t / (JB * n1);
-          const size_t o = ((size_t)k * B + b) * J + j0 + r;
-          T2 v = lv[u];
-          if (rmap[q] >= 0) v = cadd(v, r2c_post<T2, T>(res + ((size_t)rmap[q] * JB + r) * LS, L, k, c.twI, k == 0 ? (T)1 : (T)2));
-          G.lamy[(size_t)q * FS + o] = v;
+          const int rp = t % RP, k = (t / RP) % n1, q = t / (RP * n1);
+          if (q != 1) {
+            const int tq = q == 0 ? 0 : q - 1;
+#pragma unroll
+            for (int e = 0; e < EPC; ++e)
+              lv[u][e] = cadd(lv[u][e], r2c_post<T2, T>(res + ((size_t)tq * JB + rp * EPC + e) * LS, L, k, c.twI,
+                                                          k == 0 ? (T)1 : (T)2));
+          }
+          st_rows16(G.lamy + (size_t)q * FS + ((size_t)k * B + b) * J + j0 + rp * EPC, lv[u]);
         }
       }
       return;
