@@ -67,23 +67,6 @@ __device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// 16-byte global accesses of consecutive latitude rows: two complex values in
-// FP32, one in FP64 (Fourier fields keep the latitude fastest, so rows r, r+1
-// of one (m, member) are adjacent; the pointer is 16-byte aligned).  The grid
-// kernels are bound by the number of memory instructions in flight per SM
-// rather than by bytes, so each access moves 16 bytes.
-template <typename T2> struct Rows16 { static constexpr int N = 16 / (int)sizeof(T2); };
-__device__ __forceinline__ void ld_rows16(const float2* p, float2 (&v)[2]) {
-  const float4 w = *(const float4*)p;
-  v[0] = make_float2(w.x, w.y);
-  v[1] = make_float2(w.z, w.w);
-}
-__device__ __forceinline__ void ld_rows16(const double2* p, double2 (&v)[1]) { v[0] = *p; }
-__device__ __forceinline__ void st_rows16(float2* p, const float2 (&v)[2]) {
-  *(float4*)p = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
-}
-__device__ __forceinline__ void st_rows16(double2* p, const double2 (&v)[1]) { *p = v[0]; }
-
 __device__ __forceinline__ void atomic_min_d(double* addr, double v) {
   unsigned long long* a = (unsigned long long*)addr;
   unsigned long long old = *a, assumed;

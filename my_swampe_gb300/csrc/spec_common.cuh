@@ -438,6 +438,67 @@ __device__ __forceinline__ void store_step_point(const SpecGroup<T>& G, const St
   }
 }
 
+// load_step_point / store_step_point of the modified-Euler step for the
+// R = Rows16 adjacent latitudes j, j+1, ... at offset o of one (m, member),
+// with 16-byte accesses (no lagged remainders: scheme 0).  The arithmetic per
+// point is that of the single-point forms.
+template <typename T, int R = Rows16<typename cplx<T>::type>::N>
+__device__ __forceinline__ void load_step_rows(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
+                                               size_t o, typename cplx<T>::type (&old)[3][R],
+                                               typename cplx<T>::type (&mid)[3][R]) {
+  typedef typename cplx<T>::type T2;
+  const T2* Fi = G.four;
+  const bool need_old = incr || cfg.write_prev || cfg.ra_mode;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const int cf = q == 0 ? F_ETA : q == 1 ? F_DELTA : F_PHI;
+    const int rf = q == 0 ? F_ETA_MID : q == 1 ? F_DELTA_MID : F_PHI_MID;
+    if (need_old) ld_rows16(Fi + cf * FS + o, old[q]);
+    else
+#pragma unroll
+      for (int e = 0; e < R; ++e) old[q][e] = mk<T2>(0, 0);
+    if (cfg.ra_mode == 2) ld_rows16(Fi + rf * FS + o, mid[q]);
+    else
+#pragma unroll
+      for (int e = 0; e < R; ++e) mid[q][e] = mk<T2>(0, 0);
+  }
+}
+template <typename T, int R = Rows16<typename cplx<T>::type>::N>
+__device__ __forceinline__ void store_step_rows(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
+                                                size_t o, T al, T an, const typename cplx<T>::type (&nw_in)[3][R],
+                                                bool uv, const typename cplx<T>::type (&u)[R],
+                                                const typename cplx<T>::type (&v)[R],
+                                                const typename cplx<T>::type (&old)[3][R],
+                                                const typename cplx<T>::type (&mid)[3][R]) {
+  typedef typename cplx<T>::type T2;
+  T2* Fo = G.four_out;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const int cf = q == 0 ? F_ETA : q == 1 ? F_DELTA : F_PHI;
+    const int pf = q == 0 ? F_ETA_PREV : q == 1 ? F_DELTA_PREV : F_PHI_PREV;
+    const int rf = q == 0 ? F_ETA_MID : q == 1 ? F_DELTA_MID : F_PHI_MID;
+    T2 nw[R], rm[R];
+#pragma unroll
+    for (int e = 0; e < R; ++e) nw[e] = incr ? cadd(old[q][e], nw_in[q][e]) : nw_in[q][e];
+    if (cfg.write_prev) st_rows16(Fo + pf * FS + o, old[q]);
+    if (cfg.ra_mode == 1) st_rows16(Fo + rf * FS + o, old[q]);
+    else if (cfg.ra_mode == 2) {
+#pragma unroll
+      for (int e = 0; e < R; ++e) {
+        const T2 d = cadd(csub(mid[q][e], cscale(old[q][e], (T)2)), nw[e]);
+        rm[e] = cadd(old[q][e], cscale(d, al));
+        if (cfg.raw) nw[e] = csub(nw[e], cscale(d, an));
+      }
+      st_rows16(Fo + rf * FS + o, rm);
+    }
+    st_rows16(Fo + cf * FS + o, nw);
+  }
+  if (uv) {
+    st_rows16(Fo + F_U * FS + o, u);
+    st_rows16(Fo + F_V * FS + o, v);
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ void write_step_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
                                                  size_t o, int b, const typename cplx<T>::type* nw_in, bool uv,
@@ -504,11 +565,21 @@ __device__ __forceinline__ void adj_load_point(const SpecGroup<T>& G, bool incr,
 // step_combos, modified Euler): from the adjoints of the combined inputs
 // ld(q) -- slot order PhiP1, PhiP2, dP1, dP2, eP1, [identity Phi, delta, eta
 // when NK = 8], then the H slots PhiH1, dH1, dH2, eH1 -- to the adjoints of the
-// 19 state fields, written to G.lam.  Returns this point's term of dL/dPhibar
-// (modEuler_tdiff.py:80-103, 185-193).
+// state fields: lv = eta, delta, Phi, A, B, C, D, E, PhiF, F, G (adj_field
+// order; the other 8 of the 19 fields get zero).  Returns this point's term of
+// dL/dPhibar (modEuler_tdiff.py:80-103, 185-193).
+__host__ __device__ constexpr int adj_field(int q) {
+  return q == 0 ? F_ETA : q == 1 ? F_DELTA : q == 2 ? F_PHI : q == 3 ? F_A : q == 4 ? F_B : q == 5 ? F_C
+       : q == 6 ? F_D : q == 7 ? F_E : q == 8 ? F_PHIF : q == 9 ? F_F : F_G;
+}
+__host__ __device__ constexpr int adj_zero_field(int q) {  // the 8 fields whose adjoint the step zeroes
+  return q == 0 ? F_U : q == 1 ? F_V : q == 2 ? F_ETA_PREV : q == 3 ? F_DELTA_PREV : q == 4 ? F_PHI_PREV
+       : q == 5 ? F_ETA_MID : q == 6 ? F_DELTA_MID : F_PHI_MID;
+}
 template <typename T, int NK, typename LD>
-__device__ __forceinline__ T adj_store_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
-                                             size_t o, int m, int b, int j, LD ld, const AdjPointIn<T>& in) {
+__device__ __forceinline__ T adj_point_values(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, int m, int b,
+                                              int j, LD ld, const AdjPointIn<T>& in,
+                                              typename cplx<T>::type (&lv)[11]) {
   typedef typename cplx<T>::type T2;
   T2 lPhiP1 = ld(0), lPhiP2 = ld(1), ldP1 = ld(2), ldP2 = ld(3), leP1 = ld(4);
   T2 lPhiH1 = ld(NK), ldH1 = ld(NK + 1), ldH2 = ld(NK + 2), leH1 = ld(NK + 3);
@@ -546,14 +617,8 @@ __device__ __forceinline__ T adj_store_point(const SpecGroup<T>& G, const StepCf
   T2 lA = cadd(lAeff, lAf), lB = cadd(lBeff, lBf);
   T2 lF = cadd(cscale(lBeff, forc), lBf);
   T2 lG = csub(mk<T2>(0, 0), cadd(cscale(lAeff, forc), lAf));
-  const T2 z = mk<T2>(0, 0);
-  T2* LAM = G.lam;
-  LAM[F_ETA * FS + o] = leta; LAM[F_DELTA * FS + o] = ldel; LAM[F_PHI * FS + o] = lphi;
-  LAM[F_A * FS + o] = lA; LAM[F_B * FS + o] = lB; LAM[F_C * FS + o] = lC; LAM[F_D * FS + o] = lD;
-  LAM[F_E * FS + o] = lE; LAM[F_PHIF * FS + o] = lPF; LAM[F_F * FS + o] = lF; LAM[F_G * FS + o] = lG;
-  LAM[F_U * FS + o] = z; LAM[F_V * FS + o] = z;
-  LAM[F_ETA_PREV * FS + o] = z; LAM[F_DELTA_PREV * FS + o] = z; LAM[F_PHI_PREV * FS + o] = z;
-  LAM[F_ETA_MID * FS + o] = z; LAM[F_DELTA_MID * FS + o] = z; LAM[F_PHI_MID * FS + o] = z;
+  lv[0] = leta; lv[1] = ldel; lv[2] = lphi; lv[3] = lA; lv[4] = lB; lv[5] = lC; lv[6] = lD;
+  lv[7] = lE; lv[8] = lPF; lv[9] = lF; lv[10] = lG;
   if (!G.grad) return (T)0;
   // d(combined inputs)/dPhibar
   const T2 del = in.px[0], phi = in.px[1], E = in.px[2], A = in.px[3], Bm = in.px[4], Fm = in.px[5], Gm = in.px[6];
@@ -564,6 +629,79 @@ __device__ __forceinline__ T adj_store_point(const SpecGroup<T>& G, const StepCf
   T2 dd2 = cscale(del, -ia2);
   return lPhiP1.x * dP1.x + lPhiP1.y * dP1.y + lPhiH1.x * dH1.x + lPhiH1.y * dH1.y + lPhiP2.x * dP2.x +
          lPhiP2.y * dP2.y + ldP2.x * dd2.x + ldP2.y * dd2.y;
+}
+
+// adj_point_values written to G.lam at offset o of one point.
+template <typename T, int NK, typename LD>
+__device__ __forceinline__ T adj_store_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
+                                             size_t o, int m, int b, int j, LD ld, const AdjPointIn<T>& in) {
+  typedef typename cplx<T>::type T2;
+  T2 lv[11];
+  const T gp = adj_point_values<T, NK>(G, cfg, incr, m, b, j, ld, in, lv);
+#pragma unroll
+  for (int q = 0; q < 11; ++q) G.lam[adj_field(q) * FS + o] = lv[q];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) G.lam[adj_zero_field(q) * FS + o] = mk<T2>(0, 0);
+  return gp;
+}
+
+// adj_load_point / adj_store_point for the R = Rows16 adjacent latitudes
+// j0, j0+1, ... at offset o of one (m, member), with 16-byte accesses.
+// ld(q, e) is slot q at latitude j0 + e.  Returns the sum of the points'
+// dL/dPhibar terms (latitude j0 first).
+template <typename T, int R = Rows16<typename cplx<T>::type>::N>
+struct AdjRowsIn {
+  typename cplx<T>::type ly[3][R];
+  typename cplx<T>::type px[7][R];
+};
+template <typename T, int R = Rows16<typename cplx<T>::type>::N>
+__device__ __forceinline__ void adj_load_rows(const SpecGroup<T>& G, bool incr, size_t FS, size_t o,
+                                              AdjRowsIn<T, R>& in) {
+  typedef typename cplx<T>::type T2;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    if (incr) ld_rows16(G.lamY + q * FS + o, in.ly[q]);
+    else
+#pragma unroll
+      for (int e = 0; e < R; ++e) in.ly[q][e] = mk<T2>(0, 0);
+  }
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    const int pf = q == 0 ? F_DELTA : q == 1 ? F_PHI : q == 2 ? F_E : q == 3 ? F_A : q == 4 ? F_B : q == 5 ? F_F : F_G;
+    if (G.grad) ld_rows16(G.four + pf * FS + o, in.px[q]);
+    else
+#pragma unroll
+      for (int e = 0; e < R; ++e) in.px[q][e] = mk<T2>(0, 0);
+  }
+}
+template <typename T, int NK, typename LD, int R = Rows16<typename cplx<T>::type>::N>
+__device__ __forceinline__ T adj_store_rows(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
+                                            size_t o, int m, int b, int j0, LD ld, const AdjRowsIn<T, R>& in) {
+  typedef typename cplx<T>::type T2;
+  T2 lv[R][11];
+  T gp = (T)0;
+#pragma unroll
+  for (int e = 0; e < R; ++e) {
+    AdjPointIn<T> pin;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) pin.ly[q] = in.ly[q][e];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) pin.px[q] = in.px[q][e];
+    gp += adj_point_values<T, NK>(G, cfg, incr, m, b, j0 + e, [&](int q) { return ld(q, e); }, pin, lv[e]);
+  }
+#pragma unroll
+  for (int q = 0; q < 11; ++q) {
+    T2 w[R];
+#pragma unroll
+    for (int e = 0; e < R; ++e) w[e] = lv[e][q];
+    st_rows16(G.lam + adj_field(q) * FS + o, w);
+  }
+  T2 zz[R];
+#pragma unroll
+  for (int e = 0; e < R; ++e) zz[e] = mk<T2>(0, 0);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) st_rows16(G.lam + adj_zero_field(q) * FS + o, zz);
+  return gp;
 }
 
 }  // namespace swp

@@ -57,6 +57,23 @@ template <typename T2> __device__ __forceinline__ T2 cmulc(T2 a, T2 b) {
   T2 z; z.x = a.x * b.x + a.y * b.y; z.y = a.y * b.x - a.x * b.y; return z;
 }
 template <typename T2> __device__ __forceinline__ T2 cconj(T2 a) { a.y = -a.y; return a; }
+
+// 16-byte global accesses of consecutive latitude rows: two complex values in
+// FP32, one in FP64 (Fourier fields keep the latitude fastest, so rows j, j+1
+// of one (m, member) are adjacent; the pointer is 16-byte aligned).  The
+// kernels are bound by the number of memory instructions in flight per SM
+// rather than by bytes, so each access moves 16 bytes.
+template <typename T2> struct Rows16 { static constexpr int N = 16 / (int)sizeof(T2); };
+__device__ __forceinline__ void ld_rows16(const float2* p, float2 (&v)[2]) {
+  const float4 w = *(const float4*)p;
+  v[0] = make_float2(w.x, w.y);
+  v[1] = make_float2(w.z, w.w);
+}
+__device__ __forceinline__ void ld_rows16(const double2* p, double2 (&v)[1]) { v[0] = *p; }
+__device__ __forceinline__ void st_rows16(float2* p, const float2 (&v)[2]) {
+  *(float4*)p = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+}
+__device__ __forceinline__ void st_rows16(double2* p, const double2 (&v)[1]) { *p = v[0]; }
 template <typename T2> __device__ __forceinline__ T2 cscale(T2 a, typename scalar_of<T2>::type s) {
   a.x *= s; a.y *= s; return a;
 }

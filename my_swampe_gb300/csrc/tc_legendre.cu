@@ -255,8 +255,11 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   const int jp = (warp & 3) * 8 + (lane & 7);
   const int bt = (warp >> 2) * 4 + (lane >> 3);
   T2 xs[NSLOT], xa[NSLOT];
-  T2 pold[2][3], pmid[2][3];  // write-out carries, loaded ahead of GEMM2
-  T wal[2], wan[2];           // the write-out's filter weights, loaded with them
+  // write-out: thread -> member wbt, latitudes wj, wj + 1 (16-byte accesses)
+  static_assert(TC_MT * TC_J == 2 * 256, "one latitude pair per thread");
+  const int wbt = threadIdx.x / (TC_J / 2), wj = 2 * (threadIdx.x % (TC_J / 2));
+  T2 pold[3][2], pmid[3][2];  // its carries, loaded ahead of GEMM2
+  T wal = (T)0, wan = (T)0;   // its filter weights, loaded with them
   // one thread waits on each mbarrier and the block barrier releases the rest:
   // 256 spinning threads would take issue slots from the co-resident CTA
   bool ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[3], 0) : true;
@@ -437,18 +440,12 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     __syncthreads();
     tc::fence_after_sync();
     // ---- phase 5: GEMM2, both parities (rows 112..127 read the staging area and are ignored)
-    // Each thread first issues the global loads of its write-out points (the
-    // two (member, j) points t and t + 256 of phase 7), so that their latency
-    // overlaps the GEMM.
-    static_assert(TC_MT * TC_J == 2 * 256, "two write-out points per thread");
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int t = threadIdx.x + u * 256, bti = t / J, j = t % J;
-      if (bti < mt) {
-        load_step_point<T>(G, cfg, incr, FS, ((size_t)m * G.B + b0 + bti) * J + j, pold[u], pmid[u]);
-        wal[u] = G.mco[(cfg.raw ? MC_RAWM : MC_ALPHA) * G.B + b0 + bti];
-        wan[u] = cfg.raw ? G.mco[MC_RAWN * G.B + b0 + bti] : (T)0;
-      }
+    // Each thread first issues the global loads of its write-out pair, so that
+    // their latency overlaps the GEMM.
+    if (wbt < mt) {
+      load_step_rows<T>(G, cfg, incr, FS, ((size_t)m * G.B + b0 + wbt) * J + wj, pold, pmid);
+      wal = G.mco[(cfg.raw ? MC_RAWM : MC_ALPHA) * G.B + b0 + wbt];
+      wan = cfg.raw ? G.mco[MC_RAWN * G.B + b0 + wbt] : (T)0;
     }
     if (threadIdx.x == 0) {
       if (!tc::mbar_wait_bounded(&mbar[0], 1)) *sflag = 1;
@@ -499,16 +496,19 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     tc::fence_before_sync();
     __syncthreads();
     // ---- phase 7: write-out and carries (coalesced along j), as in k_spectral
+    if (wbt < mt && !sdead[wbt]) {
+      const size_t o = ((size_t)m * G.B + b0 + wbt) * J + wj;
+      auto get = [&](int f, int e) { return *(const float2*)&Out[(size_t)(f * TC_MT + wbt) * TC_OST + 2 * (wj + e)]; };
+      T2 nw[3][2], uu[2], vv[2];
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int t = threadIdx.x + u * 256, bti = t / J, j = t % J;
-      if (bti >= mt || sdead[bti]) continue;
-      const int b = b0 + bti;
-      const size_t o = ((size_t)m * G.B + b) * J + j;
-      auto get = [&](int f) { return *(const float2*)&Out[(size_t)(f * TC_MT + bti) * TC_OST + 2 * j]; };
-      const T2 nw[3] = {get(0), get(1), get(2)};
-      store_step_point<T>(G, cfg, incr, FS, o, wal[u], wan[u], nw, cfg.test != 1, cadd(get(3), get(5)),
-                          cadd(get(4), get(6)), pold[u], pmid[u]);
+      for (int e = 0; e < 2; ++e) {
+        nw[0][e] = get(0, e);
+        nw[1][e] = get(1, e);
+        nw[2][e] = get(2, e);
+        uu[e] = cadd(get(3, e), get(5, e));
+        vv[e] = cadd(get(4, e), get(6, e));
+      }
+      store_step_rows<T>(G, cfg, incr, FS, o, wal, wan, nw, cfg.test != 1, uu, vv, pold, pmid);
     }
     if (m == 0 && threadIdx.x < mt && !sdead[threadIdx.x]) {
       const int b = b0 + threadIdx.x;
@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
 //     row = slot q (8: PhiP1, PhiP2, dP1, dP2, eP1, identity Phi, delta, eta)
 //     x member x re/im = 128 rows, col = [Pw at j' | Hw at j']; the Hw columns
 //     of slots 0, 2, 3, 4 are the H slots PhiH1, dH1, dH2, eH1
-//   write-out: adj_store_point (transposed combination) + Phibar gradient.
+//   write-out: adj_store_rows (transposed combination) + Phibar gradient.
 // ===========================================================================
 namespace {
 constexpr int TCA_NIN = 5;                          // staged lambda of eta, delta, Phi, U, V
@@ -637,7 +637,10 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
   const int jp = (warp & 3) * 8 + (lane & 7);
   const int bt = (warp >> 2) * 4 + (lane >> 3);
   T2 ys[TCA_NIN], ya[TCA_NIN];
-  AdjPointIn<T> pin[2];  // write-out inputs, loaded ahead of GEMM2'
+  // write-out: warp -> member, lane -> latitudes 2 lane, 2 lane + 1 (16-byte accesses)
+  static_assert(TC_MT * TC_J == 2 * 256 && TC_J == 64, "one latitude pair per thread, a member per warp");
+  const int wbt = warp, wj = 2 * lane;
+  AdjRowsIn<T> pin;  // its inputs, loaded ahead of GEMM2'
   bool ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[3], 0) : true;
   ok = __syncthreads_and(ok);
   if (ok) {
@@ -786,12 +789,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
     __syncthreads();
     tc::fence_after_sync();
     // ---- phase 5: GEMM2', both parities; write-out inputs loaded meanwhile
-    static_assert(TC_MT * TC_J == 2 * 256, "two write-out points per thread");
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int t = threadIdx.x + u * 256, bti = t / J, j = t % J;
-      if (bti < mt) adj_load_point<T>(G, incr, FS, ((size_t)m * G.B + b0 + bti) * J + j, pin[u]);
-    }
+    if (wbt < mt) adj_load_rows<T>(G, incr, FS, ((size_t)m * G.B + b0 + wbt) * J + wj, pin);
     if (threadIdx.x == 0) {
       if (!tc::mbar_wait_bounded(&mbar[0], 1)) *sflag = 1;
       if (!*sflag) {
@@ -841,18 +839,15 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
     tc::fence_before_sync();
     __syncthreads();
     // ---- phase 7: transposed combination -> lambda of the state fields; Phibar gradient
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int t = threadIdx.x + u * 256, bti = t / J, j = t % J;
-      if (bti >= mt) continue;  // uniform over a warp: a warp covers 32 latitudes of one member
-      const int b = b0 + bti;
-      const size_t o = ((size_t)m * G.B + b) * J + j;
-      auto ld = [&](int q) { return *(const float2*)&Out[(size_t)(q * TC_MT + bti) * TC_OST + 2 * j]; };
-      T gp = adj_store_point<T, NKADJ>(G, cfg, incr, FS, o, m, b, j, ld, pin[u]);
+    if (wbt < mt) {  // uniform over a warp
+      const int b = b0 + wbt;
+      const size_t o = ((size_t)m * G.B + b) * J + wj;
+      auto ld = [&](int q, int e) { return *(const float2*)&Out[(size_t)(q * TC_MT + wbt) * TC_OST + 2 * (wj + e)]; };
+      T gp = adj_store_rows<T, NKADJ>(G, cfg, incr, FS, o, m, b, wj, ld, pin);
       if (G.grad) {
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) gp += __shfl_xor_sync(0xffffffffu, gp, off);
-        if (lane == 0) sgrad[bti * 2 + j / 32] = (double)gp;
+        if (lane == 0) { sgrad[wbt * 2] = (double)gp; sgrad[wbt * 2 + 1] = 0.0; }
       }
     }
     __syncthreads();
