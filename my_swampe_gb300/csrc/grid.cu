@@ -156,22 +156,22 @@ __device__ __forceinline__ void adj_stage_finish(const C& c, int nz, typename cp
 }
 
 // The step's fields at staged positions f0 .. f0+nf-1 of `four` (position f
-// holds step_field(f): eta, Phi, U, V, then delta for history runs, unless
-// fixed_field >= 0 names the field), unscaled, in the [f][m][r] layout of
-// adj_stage_issue, by 16-byte cp.async.  Completed by cp_async_wait_all and a
-// block barrier.
+// holds step_field(f - fofs): eta, Phi, U, V, then delta for history runs,
+// unless fixed_field >= 0 names the field), unscaled, in the [f][m][r] layout
+// of adj_stage_issue, by 16-byte cp.async.  Completed by cp_async_wait_all and
+// a block barrier.
 __host__ __device__ constexpr int step_field(int f) {
   return f == 0 ? F_ETA : f == 1 ? F_PHI : f == 2 ? F_U : f == 3 ? F_V : F_DELTA;
 }
 template <typename T, typename C>
 __device__ __forceinline__ void step_stage_issue(const C& c, const typename cplx<T>::type* four, int f0, int nf,
-                                                 int fixed_field, typename cplx<T>::type* stage) {
+                                                 int fixed_field, typename cplx<T>::type* stage, int fofs = 0) {
   typedef typename cplx<T>::type T2;
   constexpr int n1 = C::M + 1;
   constexpr int EPC = Rows16<T2>::N, RP = C::JB / EPC;
   for (int t = threadIdx.x; t < nf * n1 * RP; t += blockDim.x) {
     const int rp = t % RP, k = (t / RP) % n1, f = f0 + t / (RP * n1);
-    const int fld = fixed_field >= 0 ? fixed_field : step_field(f);
+    const int fld = fixed_field >= 0 ? fixed_field : step_field(f - fofs);
     cp_async<16>(stage + (f * n1 + k) * C::JB + rp * EPC,
                  four + (size_t)fld * c.FS + ((size_t)k * c.B + c.b) * C::J + c.j0 + rp * EPC);
   }
@@ -279,6 +279,11 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
   // Phi row, which depends on the member's blow-up flag, follows the set-up
   const int step_nfix = G.hist ? 5 : 4;
   if (MODE == GM_STEP) step_stage_issue<T>(c, G.four, 0, step_nfix, -1, c.bufB);
+  // tangent step: the primal eta, Phi, U, V, then their tangents
+  if (MODE == GM_TL_STEP) {
+    step_stage_issue<T>(c, G.primal, 0, 4, -1, c.bufB);
+    step_stage_issue<T>(c, G.four, 4, 4, -1, c.bufB, 4);
+  }
   for (int i = threadIdx.x; i < I; i += blockDim.x) c.sday[i] = G.g.dayc[i];
   for (int i = threadIdx.x; i < 2 * L + 1; i += blockDim.x) stw[i] = i < L ? G.g.twL[i] : G.g.twI[i - L];
   if (threadIdx.x == 0) { c.sred[0] = 0.0; c.sred[1] = 1e300; c.sred[2] = 1e300; c.sred[3] = -1e300; }
@@ -484,14 +489,9 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     // The new level is band-limited (no initial-condition residual): the primal
     // eta, Phi, U, V (G.primal) and their tangents (G.four) go to the grid, the
     // linearised nonlinear terms and forcing come back as tangent Fourier terms.
+    cp_async_wait_all();  // the copies issued at the start of the CTA
     __syncthreads();
-    const int pf[4] = {F_ETA, F_PHI, F_U, F_V};
-    const T2* src[8];
-#pragma unroll
-    for (int f = 0; f < 8; ++f) src[f] = (f < 4 ? G.primal : G.four) + pf[f & 3] * FS;
-    stage_rows<T>(c, src, 8, bufB);
-    __syncthreads();
-    T2* zin = c2r_transform<T>(c, bufB, 8, bufA);
+    T2* zin = c2r_transform<T, Ctx, true>(c, bufB, 8, bufA);
     T2* zout = (zin == bufA) ? bufB : bufA;
     PhysicsTL<T> pt;
     pt.Pb = ph.Pb; pt.itr = ph.itr; pt.itd = ph.itd; pt.DPe = ph.DPe; pt.nodrag = ph.nodrag; pt.forced = ph.forced;
