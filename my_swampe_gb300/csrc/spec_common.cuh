@@ -55,6 +55,30 @@ __device__ __forceinline__ void load_spec_coefs(const SpecGroup<T>& G, bool diff
   }
 }
 
+// The per-point step factors of the modified-Euler combination: tstepcoeff at
+// (member, latitude) and the member's 2dt/a^2/4, 1/a^2, Phibar/2, dt Phibar,
+// Phibar/a^2, dt/(2a^2) and dt.  The tensor-core step loads them while its
+// input copies are in flight; the other callers read them in place.
+template <typename T>
+struct StepCoefs {
+  T tsc, t2, ia2, hpb, dtpb, pba2, pfd, dt;
+};
+template <typename T>
+__device__ __forceinline__ StepCoefs<T> load_step_coefs(const SpecGroup<T>& G, int b, int j) {
+  const T* mc = G.mco;
+  const int B = G.B;
+  StepCoefs<T> k;
+  k.tsc = G.jco[(size_t)b * G.g.J + j];
+  k.t2 = mc[MC_T2 * B + b];
+  k.ia2 = mc[MC_IA2 * B + b];
+  k.hpb = mc[MC_HPB * B + b];
+  k.dtpb = mc[MC_DTPB * B + b];
+  k.pba2 = mc[MC_PBA2 * B + b];
+  k.pfd = mc[MC_PFD * B + b];
+  k.dt = mc[MC_DT * B + b];
+  return k;
+}
+
 // The combined inputs of the forward contraction at (m, member b, latitude j):
 // every reference tendency term that is a Legendre transform of a pointwise
 // product of Fourier inputs (modEuler_tdiff.py:72-110, 162-201, 253-261;
@@ -62,9 +86,11 @@ __device__ __forceinline__ void load_spec_coefs(const SpecGroup<T>& G, bool diff
 // and by the output factor (1 or n(n+1)) they are applied with.  mode 2 is the
 // plain transform of eta, delta used to diagnose winds (model.py:644-666).
 // `ld(f)` returns Fourier field f at the point (from global memory or a staged copy).
+// `kc`, if given, holds the point's step factors (modified Euler), loaded ahead.
 template <typename T, typename LD>
 __device__ __forceinline__ void step_combos_ld(const SpecGroup<T>& G, const StepCfg& cfg, int mode, bool incr, int m,
-                                               int b, int j, LD ld, typename cplx<T>::type* c) {
+                                               int b, int j, LD ld, typename cplx<T>::type* c,
+                                               const StepCoefs<T>* kc = nullptr) {
   typedef typename cplx<T>::type T2;
   constexpr int NSPX = SlotCount<T>::NP;
   constexpr int NSLOT = NSPX + NSH;
@@ -72,7 +98,7 @@ __device__ __forceinline__ void step_combos_ld(const SpecGroup<T>& G, const Step
   const T* mc = G.mco;
   const int B = G.B;
   const T xm = (T)m;
-  const T tsc = G.jco[(size_t)b * g.J + j];           // tstepcoeff
+  const T tsc = kc ? kc->tsc : G.jco[(size_t)b * g.J + j];  // tstepcoeff
   T2 z = mk<T2>(0, 0);
 #pragma unroll
   for (int q = 0; q < NSLOT; ++q) c[q] = z;
@@ -83,16 +109,17 @@ __device__ __forceinline__ void step_combos_ld(const SpecGroup<T>& G, const Step
     T2 eta = ld(F_ETA), del = ld(F_DELTA), phi = ld(F_PHI);
     T2 A = ld(F_A), Bm = ld(F_B), C = ld(F_C), D = ld(F_D);
     T2 E = ld(F_E), PF = ld(F_PHIF), Fm = ld(F_F), Gm = ld(F_G);
-    T t1 = tsc * (T)0.25, t2 = mc[MC_T2 * B + b];
-    T ia2 = mc[MC_IA2 * B + b];
-    T hPb = mc[MC_HPB * B + b];
+    const StepCoefs<T> k = kc ? *kc : load_step_coefs<T>(G, b, j);
+    T t1 = tsc * (T)0.25, t2 = k.t2;
+    T ia2 = k.ia2;
+    T hPb = k.hpb;
     T2 Bf = cadd(Bm, Fm), Af = csub(A, Gm);
     T2 Beff = cfg.forcflag ? Bf : Bm, Aeff = cfg.forcflag ? Af : A;
     // Phi (modEuler_tdiff.py:80-110); incremental form: curr goes to its own slot
     T2 p1 = incr ? cscale(imul(xm, C), -t1) : csub(phi, cscale(imul(xm, C), t1));
-    p1 = csub(p1, cscale(del, mc[MC_DTPB * B + b]));
+    p1 = csub(p1, cscale(del, k.dtpb));
     p1 = csub(p1, cscale(imul(xm, Beff), hPb * t1));
-    if (cfg.forcflag) p1 = cadd(p1, cscale(PF, mc[MC_DT * B + b]));
+    if (cfg.forcflag) p1 = cadd(p1, cscale(PF, k.dt));
     c[SP_PHI1] = p1;
     c[NSPX + SH_PHI1] = csub(cscale(D, t1), cscale(Aeff, hPb * t1));
     c[SP_PHI2] = cscale(cadd(cscale(E, t2), cscale(phi, ia2)), -hPb);
@@ -101,8 +128,8 @@ __device__ __forceinline__ void step_combos_ld(const SpecGroup<T>& G, const Step
     c[NSPX + SH_D1] = cscale(Af, t1);
     T2 d2 = cadd(cscale(phi, t2), cscale(E, t2));
     d2 = cadd(d2, cscale(imul(xm, C), t1 * (T)0.5 * ia2));
-    d2 = csub(d2, cscale(del, mc[MC_PBA2 * B + b]));
-    if (cfg.forcflag) d2 = cadd(d2, cscale(PF, mc[MC_PFD * B + b]));
+    d2 = csub(d2, cscale(del, k.pba2));
+    if (cfg.forcflag) d2 = cadd(d2, cscale(PF, k.pfd));
     c[SP_D2] = d2;
     c[NSPX + SH_D2] = cscale(D, t1 * (T)0.5 * ia2);
     // eta (modEuler_tdiff.py:253-261)

@@ -255,6 +255,14 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   const int jp = (warp & 3) * 8 + (lane & 7);
   const int bt = (warp >> 2) * 4 + (lane >> 3);
   T2 xs[NSLOT], xa[NSLOT];
+  // the combination's step factors at (member, j') and its mirror latitude,
+  // loaded while the input copies are in flight
+  StepCoefs<T> kc0{}, kc1{};
+  if (bt < mt) {
+    kc0 = load_step_coefs<T>(G, b0 + bt, jp);
+    kc1 = kc0;
+    kc1.tsc = G.jco[(size_t)(b0 + bt) * J + (J - 1 - jp)];
+  }
   // write-out: thread -> member wbt, latitudes wj, wj + 1 (16-byte accesses)
   static_assert(TC_MT * TC_J == 2 * 256, "one latitude pair per thread");
   const int wbt = threadIdx.x / (TC_J / 2), wj = 2 * (threadIdx.x % (TC_J / 2));
@@ -273,7 +281,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
         const int j = side ? (J - 1 - jp) : jp;
         T2 c[NSLOT];
         step_combos_ld<T>(G, cfg, 0, incr, m, b, j,
-                          [&](int f) { return stg[(stage_slot(f) * TC_MT + bt) * J + j]; }, c);
+                          [&](int f) { return stg[(stage_slot(f) * TC_MT + bt) * J + j]; }, c, side ? &kc1 : &kc0);
         if (side == 0) {
 #pragma unroll
           for (int q = 0; q < NSLOT; ++q) { xs[q] = c[q]; xa[q] = c[q]; }
