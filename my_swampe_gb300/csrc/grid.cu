@@ -12,8 +12,11 @@
 //     spectral_transform.py:309-328) with a half-length complex FFT.
 // Mixed-radix Stockham passes (radix 8/4/3/5) run in shared memory on
 // transforms padded to L+1 entries (bank-conflict-free across a warp).
-// Fourier rows are staged through shared memory with the latitude index
-// fastest, so every global access is a contiguous JB-element run.
+// Fourier rows are staged through shared memory.  The Fourier fields keep the
+// latitude index fastest, so a CTA's rows of one (field, m) are a contiguous
+// JB-element run.  The step, adjoint-step and tangent-step modes copy them
+// with 16-byte cp.async issued at the start of the CTA; the kernels are bound
+// by memory instructions in flight per SM rather than by bytes.
 // The kernel is specialised per mode at compile time.
 #include "grid_common.cuh"
 
