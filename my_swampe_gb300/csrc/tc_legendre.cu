@@ -503,7 +503,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     }
     tc::fence_before_sync();
     __syncthreads();
-    // ---- phase 7: write-out and carries (coalesced along j), as in k_spectral
+    // ---- phase 7: write-out and carries, by latitude pairs (16-byte accesses, coalesced along j)
     if (wbt < mt && !sdead[wbt]) {
       const size_t o = ((size_t)m * G.B + b0 + wbt) * J + wj;
       auto get = [&](int f, int e) { return *(const float2*)&Out[(size_t)(f * TC_MT + wbt) * TC_OST + 2 * (wj + e)]; };
