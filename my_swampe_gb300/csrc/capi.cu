@@ -863,8 +863,25 @@ int autotune_impl(swp_plan* p, const swp_group_state* st, const swp_group_adjoin
 
 namespace swp {
 // Entry points for other translation units (static_scratch.cu).
+// The kernels move Fourier rows with 16-byte accesses (two latitudes in FP32,
+// one in FP64), so every complex buffer must start on a 16-byte boundary, as
+// cudaMalloc and torch allocations do.  A misaligned buffer is refused here
+// rather than faulting on the device.
+static bool misaligned(const void* q) { return q && ((uintptr_t)q & 15u) != 0; }
+static int check_align(swp_plan* p, const swp_group_state* st, const swp_group_adjoint* adj = nullptr,
+                       void* const* arrays = nullptr, const swp_group_tangent* tan = nullptr) {
+  for (int g = 0; g < p->ng; ++g) {
+    if ((st && misaligned(st[g].fourier)) || (adj && (misaligned(adj[g].lam) || misaligned(adj[g].lam_y))) ||
+        (arrays && misaligned(arrays[g])) || (tan && misaligned(tan[g].fourier)))
+      return fail(p, SWP_ERR_ARG, "complex (Fourier) buffers must be 16-byte aligned");
+  }
+  return SWP_OK;
+}
+
 int adjoint_step_dispatch(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
                           const swp_group_adjoint* adj, const swp_flags* f, int t, cudaStream_t s) {
+  if (int rc = check_align(p, st_in, adj)) return rc;
+  if (int rc = check_align(p, st_out)) return rc;
   return p->precision == SWP_FP64 ? adjoint_step_impl<double>(p, st_in, st_out, adj, f, t, s)
                                   : adjoint_step_impl<float>(p, st_in, st_out, adj, f, t, s);
 }
@@ -1025,12 +1042,14 @@ int swp_init_state(swp_plan* p, const swp_group_state* st, void* const* phys_ic,
   if (f->diagnostics)
     for (int g = 0; g < p->ng; ++g)
       if (!st[g].diag) return fail(p, SWP_ERR_ARG, "diagnostics requested without a diag buffer");
+  if (int rc = check_align(p, st)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? init_impl<double>(p, st, phys_ic, f, s) : init_impl<float>(p, st, phys_ic, f, s);
 }
 
 int swp_diagnose_winds(swp_plan* p, const swp_group_state* st, void* const* ed, void* const* uv, void* stream) {
   if (!p || !st || !ed || !uv) return fail(p, SWP_ERR_ARG, "null argument");
+  if (int rc = check_align(p, st)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? winds_impl<double>(p, st, ed, uv, s) : winds_impl<float>(p, st, ed, uv, s);
 }
@@ -1059,6 +1078,7 @@ int swp_forward(swp_plan* p, const swp_group_state* st, const swp_flags* f, int 
     if (!st[g].fourier || !st[g].params || !st[g].member) return fail(p, SWP_ERR_ARG, "missing state buffer");
     if (f->diagnostics && !st[g].diag) return fail(p, SWP_ERR_ARG, "diagnostics requested without a diag buffer");
   }
+  if (int rc = check_align(p, st)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? forward_impl<double>(p, st, f, t0, nsteps, row0, write_prev_last, s)
                                   : forward_impl<float>(p, st, f, t0, nsteps, row0, write_prev_last, s);
@@ -1074,7 +1094,7 @@ static int check_tangent(swp_plan* p, const swp_group_state* st, const swp_group
   for (int g = 0; g < p->ng; ++g)
     if (!tan[g].fourier || !tan[g].resid || !tan[g].dparams || !st[g].fourier || !st[g].params || !st[g].member)
       return fail(p, SWP_ERR_ARG, "missing tangent buffer");
-  return SWP_OK;
+  return check_align(p, st, nullptr, nullptr, tan);
 }
 
 int swp_tangent_init(swp_plan* p, const swp_group_state* st, const swp_group_tangent* tan, void* const* phys,
@@ -1107,6 +1127,7 @@ int swp_tangent_output(swp_plan* p, const swp_group_state* st, const swp_group_t
 
 int swp_output_physical(swp_plan* p, const swp_group_state* st, void* const* out, const swp_flags* f, void* stream) {
   if (!p || !st || !out || !f) return fail(p, SWP_ERR_ARG, "null argument");
+  if (int rc = check_align(p, st)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? output_impl<double>(p, st, out, f, s) : output_impl<float>(p, st, out, f, s);
 }
@@ -1133,6 +1154,8 @@ int swp_adjoint_step(swp_plan* p, const swp_group_state* st_in, const swp_group_
   if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint runs with diagnostics off (no blow-up gate)");
   for (int g = 0; g < p->ng; ++g)
     if (!adj[g].lam || !adj[g].lam_y || !st_in[g].fourier || !st_out[g].fourier) return fail(p, SWP_ERR_ARG, "missing adjoint buffer");
+  if (int rc = check_align(p, st_in, adj)) return rc;
+  if (int rc = check_align(p, st_out)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? adjoint_step_impl<double>(p, st_in, st_out, adj, f, t, s)
                                   : adjoint_step_impl<float>(p, st_in, st_out, adj, f, t, s);
@@ -1140,6 +1163,7 @@ int swp_adjoint_step(swp_plan* p, const swp_group_state* st_in, const swp_group_
 
 int swp_adjoint_seed(swp_plan* p, const swp_group_state* st, const swp_group_adjoint* adj, void* const* dphys, void* stream) {
   if (!p || !st || !adj || !dphys) return fail(p, SWP_ERR_ARG, "null argument");
+  if (int rc = check_align(p, st, adj)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? adjoint_seed_impl<double>(p, st, adj, dphys, s)
                                   : adjoint_seed_impl<float>(p, st, adj, dphys, s);
@@ -1149,6 +1173,7 @@ int swp_adjoint_init(swp_plan* p, const swp_group_state* st, const swp_group_adj
                      void* const* dic, const swp_flags* f, void* stream) {
   if (!p || !st || !adj || !phys_ic || !dic || !f) return fail(p, SWP_ERR_ARG, "null argument");
   if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint of test=1 (fixed winds) is not implemented");
+  if (int rc = check_align(p, st, adj)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? adjoint_init_impl<double>(p, st, adj, phys_ic, dic, f, s)
                                   : adjoint_init_impl<float>(p, st, adj, phys_ic, dic, f, s);
@@ -1163,6 +1188,7 @@ int swp_adjoint_window(swp_plan* p, const swp_group_state* st, void* const* slot
   if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint runs with diagnostics off (no blow-up gate)");
   for (int g = 0; g < p->ng; ++g)
     if (!slots[g] || !adj[g].lam || !adj[g].lam_y || !st[g].fourier) return fail(p, SWP_ERR_ARG, "missing buffer");
+  if (int rc = check_align(p, st, adj, slots)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? adjoint_window_impl<double>(p, st, slots, adj, f, t0, nsteps, s)
                                   : adjoint_window_impl<float>(p, st, slots, adj, f, t0, nsteps, s);
@@ -1171,6 +1197,7 @@ int swp_adjoint_window(swp_plan* p, const swp_group_state* st, void* const* slot
 int swp_time_kernels(swp_plan* p, const swp_group_state* st, const swp_group_adjoint* adj, const swp_flags* f,
                      int nrep, float* ms_out, void* stream) {
   if (!p || !st || !f || !ms_out || nrep < 1) return fail(p, SWP_ERR_ARG, "bad argument");
+  if (int rc = check_align(p, st, adj)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? time_kernels_impl<double>(p, st, adj, f, nrep, ms_out, s)
                                   : time_kernels_impl<float>(p, st, adj, f, nrep, ms_out, s);
@@ -1184,6 +1211,7 @@ int swp_forward_checkpointed(swp_plan* p, const swp_group_state* st, const swp_f
   if (int rc = check_scheme(p, f, false)) return rc;
   for (int g = 0; g < p->ng; ++g)
     if (!ckpt[g] || !st[g].fourier || !st[g].params || !st[g].member) return fail(p, SWP_ERR_ARG, "missing buffer");
+  if (int rc = check_align(p, st)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? forward_ckpt_impl<double>(p, st, f, t0, nsteps, ckpt_every, ckpt, s)
                                   : forward_ckpt_impl<float>(p, st, f, t0, nsteps, ckpt_every, ckpt, s);
@@ -1197,6 +1225,7 @@ int swp_forward_stored(swp_plan* p, const swp_group_state* st, const swp_flags* 
   if (int rc = check_scheme(p, f, false)) return rc;
   for (int g = 0; g < p->ng; ++g)
     if (!states[g] || !st[g].fourier || !st[g].params || !st[g].member) return fail(p, SWP_ERR_ARG, "missing buffer");
+  if (int rc = check_align(p, st, nullptr, states)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? forward_stored_impl<double>(p, st, f, t0, nsteps, states, s)
                                   : forward_stored_impl<float>(p, st, f, t0, nsteps, states, s);
@@ -1211,6 +1240,7 @@ int swp_adjoint_stored(swp_plan* p, const swp_group_state* st, void* const* stat
   if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint runs with diagnostics off (no blow-up gate)");
   for (int g = 0; g < p->ng; ++g)
     if (!states[g] || !adj[g].lam || !adj[g].lam_y || !st[g].params) return fail(p, SWP_ERR_ARG, "missing buffer");
+  if (int rc = check_align(p, st, adj, states)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? adjoint_stored_impl<double>(p, st, states, adj, f, t0, nsteps, s)
                                   : adjoint_stored_impl<float>(p, st, states, adj, f, t0, nsteps, s);
@@ -1222,6 +1252,7 @@ int swp_plan_autotune(swp_plan* p, const swp_group_state* st, const swp_group_ad
   for (int g = 0; g < p->ng; ++g)
     if (!st[g].fourier || !st[g].params || !st[g].member || !adj[g].lam || !adj[g].lam_y)
       return fail(p, SWP_ERR_ARG, "missing buffer");
+  if (int rc = check_align(p, st, adj)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? autotune_impl<double>(p, st, adj, f, nrep, chosen_mt, s)
                                   : autotune_impl<float>(p, st, adj, f, nrep, chosen_mt, s);
