@@ -15,6 +15,10 @@
  *     message of the last failure on that plan.
  *   - All arrays are device pointers owned by the caller; the plan owns only
  *     static geometry and scratch.  `stream` is a cudaStream_t (NULL = legacy).
+ *   - Complex (Fourier) arrays -- fourier, lam, lam_y, tangent fourier, stored
+ *     states, window slots -- must be 16-byte aligned (cudaMalloc and torch
+ *     allocations are): the kernels move them with 16-byte accesses.  An
+ *     entry point refuses a misaligned one with SWP_ERR_ARG.
  *   - A plan is not re-entrant: one host thread and one stream per plan.
  *   - Precision SWP_FP64: every array of "compute type" is double/double2.
  *     Precision SWP_FAST: compute type is float/float2 (FP32 state, FP32
