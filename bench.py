@@ -175,6 +175,30 @@ def _one_step(integ, ics, targets):
     return outs, dic, grad
 
 
+def shard_seed(rank: int, base: int = 1234) -> int:
+    """Seed of rank `rank`'s member shard: every rank integrates its own B
+    members (member b of rank r is drawn from shard_seed(r) + b)."""
+    return base + 100000 * int(rank)
+
+
+def reduce_max_time(t: float, world: int, device) -> float:
+    """The job's time: the maximum over ranks of the per-rank time (the only
+    collective of the N > 1 bench; the data path has none)."""
+    if world <= 1:
+        return float(t)
+    import torch
+    import torch.distributed as dist
+
+    tt = torch.tensor([float(t)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_throughput(world: int, B: int, steps: int, t_max: float) -> float:
+    """Whole-job member-steps/s: all ranks' members over the slowest rank's time."""
+    return world * B * steps / t_max
+
+
 def _time_steps(fn, steps, warmup, flush):
     import torch
 
@@ -256,7 +280,7 @@ def run_ours(args):
 
     # ---------------- fast path (headline)
     ng = args.groups
-    eng, wls, flags, integ, ics = _setup("fast", B, seed=1234 + 100000 * rank, store=args.store, ngroups=ng)
+    eng, wls, flags, integ, ics = _setup("fast", B, seed=shard_seed(rank), store=args.store, ngroups=ng)
     target = _target(eng, wls, flags, ics)
     state = {}
 
@@ -269,13 +293,8 @@ def run_ours(args):
     sampler.start()
     times = _time_steps(step_fast, args.steps, args.warmup, flush)
     clocks = sampler.stop()
-    t_mean = float(np.mean(times))
-    t_max = t_mean
-    if world > 1:
-        tt = torch.tensor([t_mean], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = world * B * T_BENCH / t_max
+    t_max = reduce_max_time(float(np.mean(times)), world, "cuda")
+    value = job_throughput(world, B, T_BENCH, t_max)
     out_fast = torch.cat([o.double() for o in state["out"]], dim=1)
     grad_fast = torch.cat([g.clone() for g in state["grad"]], dim=1)
 
@@ -323,11 +342,7 @@ def run_ours(args):
                 out_par[g][k].copy_(d_par[g][name].grad, non_blocking=True)
 
     e2e_times = _time_steps(step_e2e, max(2, args.steps), 1, flush)
-    e2e_t = float(np.mean(e2e_times))
-    if world > 1:
-        tt = torch.tensor([e2e_t], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(tt.item())
+    e2e_t = reduce_max_time(float(np.mean(e2e_times)), world, "cuda")
     h2d = sum(x.numel() * x.element_size() for x in host_ics) + \
         sum(v.numel() * 8 for hp in host_par for v in hp.values()) + \
         sum(t.numel() * t.element_size() for t in host_tgt)
@@ -350,7 +365,7 @@ def run_ours(args):
     # ---------------- plain FP64 GPU path on the same workload
     fp64 = None
     if not args.skip_fp64:
-        eng64, wl64, flags64, integ64, ics64 = _setup("fp64", B, seed=1234 + 100000 * rank, store=args.store,
+        eng64, wl64, flags64, integ64, ics64 = _setup("fp64", B, seed=shard_seed(rank), store=args.store,
                                                       ngroups=ng)
         target64 = [t.double() for t in target]
         st64 = {}
@@ -401,13 +416,16 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": round(1e3 * t_max, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 state/pointwise, f32 Legendre (fast path); f64 plain path",
         "data": "synthetic (seeded forced ensemble: taurad, taudrag log-uniform [1e4,1e6] s, DPhieq U[1e5,4e6], Phi noise 1e-3*Phibar at n<=10)",
-        "config": {"workload": "forced ensemble fwd+adjoint, M=42 (64x128), B=256 members per GPU, 1440 steps, checkpoint every 50",
-                   "members_per_gpu": B, "steps_per_member": T_BENCH, "ckpt_every": CKPT,
+        "config": {"workload": (f"forced ensemble fwd+adjoint, M=42 (64x128), B={B} members per GPU, {T_BENCH} steps, "
+                                + ("all states stored (no recomputation)" if store_fast == "all"
+                                   else f"checkpoint every {CKPT} (windows recomputed)")),
+                   "members_per_gpu": B, "steps_per_member": T_BENCH,
+                   "ckpt_every": CKPT if store_fast != "all" else None,
                    "adjoint_states": store_fast,
                    "schedule": (f"{ng} groups of {'/'.join(str(b) for b in _group_sizes(B, ng))} members, "
                                 "one stream each (concurrent)") if ng > 1 else "all members in each launch",
                    "l2": "integration touches >= 9 GB (stored states or checkpoints + window slots) > L2 (126 MB); 512 MB L2 flush write between timed steps"},
-        "e2e": {"value": round(world * B * T_BENCH / e2e_t, 1), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+        "e2e": {"value": round(job_throughput(world, B, T_BENCH, e2e_t), 1), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1e3 * e2e_t, 3)},
         "roofline": roofline,
         "fp64_plain_gpu": fp64,

@@ -268,10 +268,14 @@ int swp_plan_set_tile(swp_plan* plan, int g, int mt);
  * cudaMalloc/cudaFree.  The plan must need at most that much scratch
  * (5*(M+1)*B*J complex values per group, 256-byte aligned), else SWP_ERR_ARG.
  * The first call on a device resolves the array's device address
- * (cudaGetSymbolAddress) -- make that first call before any stream capture.
- * All calls share the array: calls that overlap on the GPU (other streams,
- * other plans, other threads) race on it.  Nothing in it needs to start at
- * zero: each call overwrites the part it reads. */
+ * (cudaGetSymbolAddress) and caches it for the process -- make that first
+ * call before any stream capture, and do not cudaDeviceReset that device
+ * afterwards (the cached address would be stale).  All calls share the array:
+ * calls that overlap on the GPU (other streams, other plans, other threads)
+ * race on it.  Nothing in it needs to start at zero: each call overwrites the
+ * part it reads.  The argument checks are those of swp_adjoint_step (lam_y
+ * aside): a missing lam or Fourier buffer is SWP_ERR_ARG, a RAW-filtered,
+ * non-modified-Euler, test 1 or diagnostics run SWP_ERR_UNSUPPORTED. */
 int swp_adjoint_step_noalloc(swp_plan* plan, const swp_group_state* st_in, const swp_group_state* st_out,
                              const swp_group_adjoint* adj, const swp_flags* flags, int t, void* stream);
 
@@ -301,6 +305,17 @@ int swp_tangent_output(swp_plan* plan, const swp_group_state* st, const swp_grou
  * Splitting one ensemble into two groups of equal size and running them
  * concurrently is the faster schedule on GB300.  Results do not depend on it. */
 int swp_plan_set_concurrency(swp_plan* plan, int on);
+
+/* Poll limit of the bounded mbarrier waits inside the tensor-core kernels
+ * (no reference counterpart; default SWP_WAIT_LIMIT_DEFAULT).  A test hook for
+ * the failure path: with max_polls = 0 every such wait gives up at once, and
+ * each CTA then sets the plan's device error word, waits (bounded, with the
+ * fixed drain limit) for the copies and MMAs it issued, frees its TMEM and
+ * returns without writing its outputs -- what swp_device_status then reports,
+ * reached without hanging or faulting the GPU.  Captured graphs are dropped
+ * when the limit changes. */
+#define SWP_WAIT_LIMIT_DEFAULT (1u << 22)
+int swp_plan_set_wait_limit(swp_plan* plan, unsigned int max_polls);
 
 #ifdef __cplusplus
 }

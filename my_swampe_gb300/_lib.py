@@ -37,6 +37,8 @@ G_TAURAD, G_TAUDRAG, G_DPHIEQ, G_PHIBAR = range(4)
 TANGENT_PARAMS = ("taurad", "taudrag", "DPhieq", "Phibar", "a", "dt", "K6", "K6Phi", "omega", "si_alpha")
 NTANGENT = len(TANGENT_PARAMS)
 
+WAIT_LIMIT_DEFAULT = 1 << 22  # swampe_gb300.h SWP_WAIT_LIMIT_DEFAULT
+
 ERRORS = {1: "bad argument", 2: "CUDA error", 3: "numerical failure", 4: "bad state", 5: "unsupported"}
 
 
@@ -90,6 +92,7 @@ EXPORTS = (
     "swp_tc_selftest", "swp_device_status", "swp_plan_uses_tensor_cores", "swp_forward_stored",
     "swp_adjoint_stored", "swp_plan_autotune", "swp_plan_tiles", "swp_plan_set_tile",
     "swp_tangent_init", "swp_tangent_forward", "swp_tangent_output", "swp_plan_set_concurrency",
+    "swp_plan_set_wait_limit",
 )
 
 _lib = None
@@ -143,6 +146,7 @@ def load(path: os.PathLike | str | None = None) -> ctypes.CDLL:
         "swp_tangent_forward": (i, [vp, gsp, gtp, fp, i, i, vp]),
         "swp_tangent_output": (i, [vp, gsp, gtp, vpp, fp, vp]),
         "swp_plan_set_concurrency": (i, [vp, i]),
+        "swp_plan_set_wait_limit": (i, [vp, ctypes.c_uint]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

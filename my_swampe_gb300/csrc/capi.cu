@@ -33,6 +33,7 @@ struct swp_plan {
   float* tcbasis_adj[MAXG] = {};
   void* coefmem[MAXG] = {};              // per-call coefficient tables (CoefTables) of each group
   int* d_err = nullptr;                  // device error word set by bounded waits that ran out
+  uint32_t tc_wait_limit = TC_WAIT_LIMIT_DEFAULT;  // mbarrier polls before a tensor-core wait gives up
   // groups run concurrently: each group's step chain on its own stream (forked
   // from and joined to the caller's), so that one group's latency-bound kernels
   // overlap another's; gmask restricts launches to the groups of one chain
@@ -199,6 +200,7 @@ cudaError_t launch_step_spec(const swp_plan* p, const SpecLaunch<T>& LS, int nbs
       int acc = 0;
       TcBasis tb;
       memset(&tb, 0, sizeof(tb));
+      tb.wait_limit = p->tc_wait_limit;
       for (int g = 0; g < p->ng; ++g) {
         LT.grp[g].MT = mt;
         LT.grp[g].ntb = (LT.grp[g].B + mt - 1) / mt;
@@ -224,6 +226,7 @@ cudaError_t launch_step_spec_adj(const swp_plan* p, const SpecLaunch<T>& LS, int
       int acc = 0;
       TcBasis tb;
       memset(&tb, 0, sizeof(tb));
+      tb.wait_limit = p->tc_wait_limit;
       for (int g = 0; g < p->ng; ++g) {
         LT.grp[g].MT = mt;
         LT.grp[g].ntb = (LT.grp[g].B + mt - 1) / mt;
@@ -878,10 +881,39 @@ static int check_align(swp_plan* p, const swp_group_state* st, const swp_group_a
   return SWP_OK;
 }
 
+// Scheme switches every stepping entry checks (model.py:1531-1537).  The
+// adjoint and the tangent cover the modified-Euler scheme with the classic filter.
+int check_scheme(swp_plan* p, const swp_flags* f, bool adjoint) {
+  if (f->scheme < 0 || f->scheme > 2) return fail(p, SWP_ERR_ARG, "scheme must be 0, 1 or 2");
+  if (f->test < 0 || f->test > 2) return fail(p, SWP_ERR_ARG, "test must be 0 (None), 1 or 2");
+  if (f->raw_filter && f->scheme == 1)
+    return fail(p, SWP_ERR_ARG, "raw_filter is incompatible with the explicit scheme");
+  if (adjoint && f->scheme != 0)
+    return fail(p, SWP_ERR_UNSUPPORTED, "derivatives (adjoint, tangent) are implemented for the modified-Euler scheme");
+  if (adjoint && f->raw_filter)
+    return fail(p, SWP_ERR_UNSUPPORTED,
+                "derivatives (adjoint, tangent) are implemented for the classic Robert-Asselin filter");
+  return SWP_OK;
+}
+
+// Argument checks of the adjoint step, shared by swp_adjoint_step and its
+// allocation-free variant (need_lamy = false: the variant supplies lam_y).
+int adjoint_step_checks(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
+                        const swp_group_adjoint* adj, const swp_flags* f, bool need_lamy) {
+  if (!p || !st_in || !st_out || !adj || !f) return fail(p, SWP_ERR_ARG, "null argument");
+  if (int rc = check_scheme(p, f, true)) return rc;
+  if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint of test=1 (fixed winds) is not implemented");
+  if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint runs with diagnostics off (no blow-up gate)");
+  for (int g = 0; g < p->ng; ++g)
+    if (!adj[g].lam || (need_lamy && !adj[g].lam_y) || !st_in[g].fourier || !st_out[g].fourier)
+      return fail(p, SWP_ERR_ARG, "missing adjoint buffer");
+  if (int rc = check_align(p, st_in, adj)) return rc;
+  return check_align(p, st_out);
+}
+
 int adjoint_step_dispatch(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
                           const swp_group_adjoint* adj, const swp_flags* f, int t, cudaStream_t s) {
-  if (int rc = check_align(p, st_in, adj)) return rc;
-  if (int rc = check_align(p, st_out)) return rc;
+  if (int rc = adjoint_step_checks(p, st_in, st_out, adj, f, true)) return rc;
   return p->precision == SWP_FP64 ? adjoint_step_impl<double>(p, st_in, st_out, adj, f, t, s)
                                   : adjoint_step_impl<float>(p, st_in, st_out, adj, f, t, s);
 }
@@ -1054,21 +1086,6 @@ int swp_diagnose_winds(swp_plan* p, const swp_group_state* st, void* const* ed, 
   return p->precision == SWP_FP64 ? winds_impl<double>(p, st, ed, uv, s) : winds_impl<float>(p, st, ed, uv, s);
 }
 
-// Scheme switches every stepping entry checks (model.py:1531-1537).  The
-// adjoint and the tangent cover the modified-Euler scheme with the classic filter.
-static int check_scheme(swp_plan* p, const swp_flags* f, bool adjoint) {
-  if (f->scheme < 0 || f->scheme > 2) return fail(p, SWP_ERR_ARG, "scheme must be 0, 1 or 2");
-  if (f->test < 0 || f->test > 2) return fail(p, SWP_ERR_ARG, "test must be 0 (None), 1 or 2");
-  if (f->raw_filter && f->scheme == 1)
-    return fail(p, SWP_ERR_ARG, "raw_filter is incompatible with the explicit scheme");
-  if (adjoint && f->scheme != 0)
-    return fail(p, SWP_ERR_UNSUPPORTED, "derivatives (adjoint, tangent) are implemented for the modified-Euler scheme");
-  if (adjoint && f->raw_filter)
-    return fail(p, SWP_ERR_UNSUPPORTED,
-                "derivatives (adjoint, tangent) are implemented for the classic Robert-Asselin filter");
-  return SWP_OK;
-}
-
 int swp_forward(swp_plan* p, const swp_group_state* st, const swp_flags* f, int t0, int nsteps, int row0,
                 int write_prev_last, void* stream) {
   if (!p || !st || !f) return fail(p, SWP_ERR_ARG, "null argument");
@@ -1148,14 +1165,7 @@ int swp_state_copy(swp_plan* p, const swp_group_state* st, void* const* ckpt, in
 
 int swp_adjoint_step(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
                      const swp_group_adjoint* adj, const swp_flags* f, int t, void* stream) {
-  if (!p || !st_in || !st_out || !adj || !f) return fail(p, SWP_ERR_ARG, "null argument");
-  if (int rc = check_scheme(p, f, true)) return rc;
-  if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint of test=1 (fixed winds) is not implemented");
-  if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "adjoint runs with diagnostics off (no blow-up gate)");
-  for (int g = 0; g < p->ng; ++g)
-    if (!adj[g].lam || !adj[g].lam_y || !st_in[g].fourier || !st_out[g].fourier) return fail(p, SWP_ERR_ARG, "missing adjoint buffer");
-  if (int rc = check_align(p, st_in, adj)) return rc;
-  if (int rc = check_align(p, st_out)) return rc;
+  if (int rc = adjoint_step_checks(p, st_in, st_out, adj, f, true)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWP_FP64 ? adjoint_step_impl<double>(p, st_in, st_out, adj, f, t, s)
                                   : adjoint_step_impl<float>(p, st_in, st_out, adj, f, t, s);
@@ -1276,6 +1286,13 @@ int swp_plan_set_tile(swp_plan* p, int g, int mt) {
   p->MT[g] = mt;
   refresh_spec_smem(p);
   clear_graphs(p);
+  return SWP_OK;
+}
+
+int swp_plan_set_wait_limit(swp_plan* p, unsigned int max_polls) {
+  if (!p) return SWP_ERR_ARG;
+  if (p->tc_wait_limit != max_polls) clear_graphs(p);  // the limit is a launch argument of the captured kernels
+  p->tc_wait_limit = max_polls;
   return SWP_OK;
 }
 

@@ -20,6 +20,8 @@ int adjoint_step_dispatch(swp_plan* p, const swp_group_state* st_in, const swp_g
 int plan_groups(const swp_plan* p);
 size_t plan_lamy_bytes(const swp_plan* p, int g);
 int plan_fail(swp_plan* p, int code, const char* msg);
+int adjoint_step_checks(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
+                        const swp_group_adjoint* adj, const swp_flags* f, bool need_lamy);
 }  // namespace swp
 
 // Every device that loads this library holds this array until the process exits.
@@ -32,6 +34,9 @@ std::mutex g_scratch_mu;
 
 // Device address of the scratch array on the current device, resolved once
 // per device (the name is only a host-side stand-in for the device symbol).
+// The cache is never invalidated: after cudaDeviceReset the library's module
+// is loaded anew and the cached address may be stale, so resetting a device
+// after the first call on it is not supported.
 int scratch_address(void** out, std::string& err) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -55,7 +60,8 @@ int scratch_address(void** out, std::string& err) {
 extern "C" int swp_adjoint_step_noalloc(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
                                         const swp_group_adjoint* adj, const swp_flags* f, int t, void* stream) {
   using namespace swp;
-  if (!p || !st_in || !st_out || !adj || !f) return plan_fail(p, SWP_ERR_ARG, "null argument");
+  // the same argument checks as swp_adjoint_step, except that lam_y is not the caller's
+  if (int rc = adjoint_step_checks(p, st_in, st_out, adj, f, false)) return rc;
   int ng = plan_groups(p);
   // lam_y of every group is carved out of the static array, 256-byte aligned
   size_t need = 0;
@@ -78,7 +84,5 @@ extern "C" int swp_adjoint_step_noalloc(swp_plan* p, const swp_group_state* st_i
     a[g] = adj[g];
     a[g].lam_y = (char*)base + off[g];
   }
-  if (f->scheme != 0 || f->test == 1 || f->diagnostics)
-    return plan_fail(p, SWP_ERR_UNSUPPORTED, "adjoint: modified Euler, test != 1, diagnostics off");
   return adjoint_step_dispatch(p, st_in, st_out, a, f, t, (cudaStream_t)stream);
 }

@@ -220,7 +220,12 @@ void grid_set_attributes();
 int grid_rows_per_cta(int M, bool fp64, int mode);  // JB the grid kernel is compiled for
 
 // tensor-core Legendre kernel of the FP32 modified-Euler step (tc_legendre.cu)
-struct TcBasis { const float* p[MAXG]; };  // packed basis of each group
+// packed basis of each group, and the poll limit of the kernels' mbarrier waits
+struct TcBasis {
+  const float* p[MAXG];
+  uint32_t wait_limit;
+};
+constexpr uint32_t TC_WAIT_LIMIT_DEFAULT = SWP_WAIT_LIMIT_DEFAULT;
 size_t spec_tc_smem_bytes();
 size_t spec_tc_basis_floats();
 int spec_tc_members_per_cta();

@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   T wal = (T)0, wan = (T)0;   // its filter weights, loaded with them
   // one thread waits on each mbarrier and the block barrier releases the rest:
   // 256 spinning threads would take issue slots from the co-resident CTA
-  bool ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[3], 0) : true;
+  bool ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[3], 0, basis.wait_limit) : true;
   ok = __syncthreads_and(ok);
   if (ok) {
     const T2* stg = (const T2*)sA;
@@ -330,12 +330,12 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     tc::fence_proxy_async();
     __syncthreads();
     if (threadIdx.x == 0) {
-      if (!tc::mbar_wait_bounded(&mbar[0], 0)) *sflag = 1;
+      if (!tc::mbar_wait_bounded(&mbar[0], 0, basis.wait_limit)) *sflag = 1;
       if (!*sflag) mma_3xtf32_2(tbase, aHs, aLs, bbase, TC_N1, TC_K1, idesc1w, idesc1);
       tc::mma_commit(&mbar[1]);
       n_c1 = 1;
     }
-    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 0) : true;
+    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 0, basis.wait_limit) : true;
     ok = __syncthreads_and(ok);
     tc::fence_after_sync();
     ok = ok && !*sflag;  // written by thread 0 before the barrier: the same value for every thread
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       tc::mma_commit(&mbar[1]);
       n_c1 = 2;
     }
-    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 1) : true;
+    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 1, basis.wait_limit) : true;
     ok = __syncthreads_and(ok);
     tc::fence_after_sync();
   }
@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       wan = cfg.raw ? G.mco[MC_RAWN * G.B + b0 + wbt] : (T)0;
     }
     if (threadIdx.x == 0) {
-      if (!tc::mbar_wait_bounded(&mbar[0], 1)) *sflag = 1;
+      if (!tc::mbar_wait_bounded(&mbar[0], 1, basis.wait_limit)) *sflag = 1;
       if (!*sflag) {
         for (int par = 0; par < 2; ++par) {
           const uint32_t a2 = aHs + (uint32_t)(2 * par * TC_A2) * 4u;
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       tc::mma_commit(&mbar[2]);
       n_c2 = 1;
     }
-    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[2], 0) : true;
+    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[2], 0, basis.wait_limit) : true;
     ok = __syncthreads_and(ok);
     tc::fence_after_sync();
     ok = ok && !*sflag;
@@ -649,7 +649,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
   static_assert(TC_MT * TC_J == 2 * 256 && TC_J == 64, "one latitude pair per thread, a member per warp");
   const int wbt = warp, wj = 2 * lane;
   AdjRowsIn<T> pin;  // its inputs, loaded ahead of GEMM2'
-  bool ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[3], 0) : true;
+  bool ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[3], 0, basis.wait_limit) : true;
   ok = __syncthreads_and(ok);
   if (ok) {
     const T2* stg = (const T2*)sA;
@@ -698,12 +698,12 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
     tc::fence_proxy_async();
     __syncthreads();
     if (threadIdx.x == 0) {
-      if (!tc::mbar_wait_bounded(&mbar[0], 0)) *sflag = 1;
+      if (!tc::mbar_wait_bounded(&mbar[0], 0, basis.wait_limit)) *sflag = 1;
       if (!*sflag) mma_3xtf32_2(tbase, aHs, aLs, bbase, TC_N1, TC_K1, idesc1w, idesc1);
       tc::mma_commit(&mbar[1]);
       n_c1 = 1;
     }
-    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 0) : true;
+    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 0, basis.wait_limit) : true;
     ok = __syncthreads_and(ok);
     tc::fence_after_sync();
     ok = ok && !*sflag;
@@ -718,7 +718,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
       tc::mma_commit(&mbar[1]);
       n_c1 = 2;
     }
-    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 1) : true;
+    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 1, basis.wait_limit) : true;
     ok = __syncthreads_and(ok);
     tc::fence_after_sync();
   }
@@ -799,7 +799,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
     // ---- phase 5: GEMM2', both parities; write-out inputs loaded meanwhile
     if (wbt < mt) adj_load_rows<T>(G, incr, FS, ((size_t)m * G.B + b0 + wbt) * J + wj, pin);
     if (threadIdx.x == 0) {
-      if (!tc::mbar_wait_bounded(&mbar[0], 1)) *sflag = 1;
+      if (!tc::mbar_wait_bounded(&mbar[0], 1, basis.wait_limit)) *sflag = 1;
       if (!*sflag) {
         for (int par = 0; par < 2; ++par) {
           const uint32_t a2 = aHs + (uint32_t)(2 * par * TCA_A2) * 4u;
@@ -811,7 +811,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
       tc::mma_commit(&mbar[2]);
       n_c2 = 1;
     }
-    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[2], 0) : true;
+    ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[2], 0, basis.wait_limit) : true;
     ok = __syncthreads_and(ok);
     tc::fence_after_sync();
     ok = ok && !*sflag;

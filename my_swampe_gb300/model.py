@@ -15,6 +15,7 @@ launch (leading member axis on every output).
 from __future__ import annotations
 
 import math
+import warnings
 from dataclasses import dataclass
 from typing import Any, Dict, NamedTuple, Optional
 
@@ -600,8 +601,9 @@ def run_model(M, dt, tmax, Phibar, omega, a, test=None, g=9.8, forcflag=True, ta
               *, K6Phi=None, semi_implicit=False, si_alpha=0.5, raw_filter=False, williams_alpha=0.53,
               jit_scan=True, as_numpy=True, precision="fp64", device=None) -> Dict[str, Any]:
     """SWAMPE-compatible wrapper (``model.py:1954-2219``): history on the host,
-    legacy ``(tmax, 2)`` spinup/geopot arrays, optional pickle saving and
-    matplotlib plots every savefreq/plotfreq steps."""
+    legacy ``(tmax, 2)`` spinup/geopot arrays (``:2106-2158``) and optional
+    pickle saving every savefreq steps.  ``plotflag`` only warns: host plotting
+    (``plotting.py``) is not part of this package."""
     result = run_model_scan(M=M, dt=dt, tmax=tmax, Phibar=Phibar, omega=omega, a=a, test=test, g=g,
                             forcflag=forcflag, taurad=taurad, taudrag=taudrag, DPhieq=DPhieq, a1=a1,
                             diffflag=diffflag, modalflag=modalflag, alpha=alpha, expflag=expflag, K6=K6,
@@ -644,7 +646,10 @@ def run_model(M, dt, tmax, Phibar, omega, a, test=None, g=9.8, forcflag=True, ta
                 continuation.save_data(ts, hist["eta"][k], hist["delta"][k], hist["Phi"][k], hist["U"][k],
                                        hist["V"][k], spin, geop, custompath=custompath)
     if plotflag:
-        _plot_history(hist, static, t_seq, dt, timeunits, plotfreq, Phibar, minlevel, maxlevel, spin)
+        # model.py:2180-2203 draws matplotlib figures on the host; plotting is not
+        # part of this package (the histories it would draw are returned)
+        warnings.warn("run_model(plotflag=True): plotting is not part of my_swampe_gb300; plot the returned "
+                      "fields with the reference's my_swampe.plotting", stacklevel=2)
     if verbose:
         print("GCM run completed!")
     T = hist["eta"].shape[0]
@@ -653,27 +658,6 @@ def run_model(M, dt, tmax, Phibar, omega, a, test=None, g=9.8, forcflag=True, ta
         U=hist["U"][-1] if T else None, V=hist["V"][-1] if T else None, spinup=spin, geopot=geop,
         lambdas=conv(static.lambdas), mus=conv(static.mus), t_seq=t_seq,
     )
-
-
-def _plot_history(hist, static, t_seq, dt, timeunits, plotfreq, Phibar, minlevel, maxlevel, spin):  # pragma: no cover
-    """Minimal host plotting hook: zonal-mean wind and geopotential maps with matplotlib if installed."""
-    try:
-        import matplotlib
-
-        matplotlib.use("Agg")
-        import matplotlib.pyplot as plt
-    except Exception:
-        return
-    mus = np.asarray(static.mus.detach().cpu())
-    for k, t in enumerate(t_seq):
-        if int(t) % int(plotfreq) != 0:
-            continue
-        fig, ax = plt.subplots(1, 2, figsize=(10, 4))
-        ax[0].plot(np.mean(hist["U"][k], axis=1), np.degrees(np.arcsin(mus)))
-        ax[0].set_xlabel("mean zonal wind (m/s)")
-        ax[1].imshow(hist["Phi"][k] + float(Phibar), origin="lower", aspect="auto", vmin=minlevel, vmax=maxlevel)
-        fig.suptitle(f"t = {continuation.compute_timestamp(timeunits, int(t), dt)} {timeunits}")
-        plt.close(fig)
 
 
 def run_model_gpu(*args, **kwargs) -> Dict[str, Any]:

@@ -203,10 +203,31 @@ def build_lambdas(I: int) -> np.ndarray:
     return np.linspace(-np.pi, np.pi, num=int(I), endpoint=False)
 
 
+# Quadrature override: J -> (mus, w).  Empty means SciPy's roots_legendre, as
+# the reference.  The GPU path builds its nodes and weights by Newton's method
+# to ~1e-15 (SciPy's weights err by up to ~3e-11 near the poles), so the
+# parity tests of the GPU path load the same exact values here: both sides
+# then see identical quadrature and differ only by FP64 round-off.
+_QUADRATURE: Dict[int, Any] = {}
+
+
+def set_quadrature(table=None) -> None:
+    """Use ``table[J] = (mus, w)`` as the Gauss-Legendre nodes and weights
+    (``None`` restores SciPy's ``roots_legendre``).  Clears the geometry cache."""
+    _QUADRATURE.clear()
+    if table:
+        for J, (mus, w) in table.items():
+            _QUADRATURE[int(J)] = (np.asarray(mus, np.float64).copy(), np.asarray(w, np.float64).copy())
+    cached_geometry.cache_clear()
+
+
 def gauss_legendre(J: int):
     """Gauss-Legendre nodes/weights.  ``spectral_transform.py:80-114``."""
     import scipy.special as sp
 
+    if int(J) in _QUADRATURE:
+        mus, w = _QUADRATURE[int(J)]
+        return mus.copy(), w.copy()
     mus, w = sp.roots_legendre(int(J))
     return np.asarray(mus, np.float64), np.asarray(w, np.float64)
 
@@ -991,3 +1012,24 @@ def run_model_scan_final(xp=NUMPY, **kw):
     """``model.py:1844-1951``: same as run_model_scan without history, diagnostics off."""
     kw.setdefault("diagnostics", False)
     return run_model_scan(xp, return_history=False, **kw)
+
+
+def legacy_diagnostics(xp, res, tmax: int, test, a1: float = 0.05, contflag: bool = False):
+    """``run_model``'s ``(tmax, 2)`` spinup / geopot arrays.  ``model.py:2106-2158``:
+    row t-1 of each step t in t_seq holds (min wind speed, RMS wind) and
+    (min Phi, max Phi); without continuation row 0 comes from the analytic
+    initial condition."""
+    spin = np.zeros((int(tmax), 2))
+    geop = np.zeros((int(tmax), 2))
+    outs = res["outs"]
+    for k, t in enumerate(res["t_seq"]):
+        i = int(t) - 1
+        if 0 <= i < tmax:
+            spin[i] = (outs["spin_min"][k], outs["rms"][k])
+            geop[i] = (outs["phi_min"][k], outs["phi_max"][k])
+    if not contflag:
+        s = res["static"]
+        _, _, Phi0, U0, V0 = (xp.to_numpy(f) for f in analytic_ic(xp, s, test, a1))
+        spin[0] = (np.min(np.sqrt(U0 * U0 + V0 * V0)), float(xp.to_numpy(rms_winds(xp, s, U0, V0))))
+        geop[0] = (np.min(Phi0), np.max(Phi0))
+    return spin, geop

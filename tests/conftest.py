@@ -1,6 +1,8 @@
+import contextlib
 import sys
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -42,3 +44,26 @@ FIXTURE_CASES = {
 }
 # reference tolerances (test_parity_reference_regression.py:58-64)
 ATOL = {"eta": 1.0e-10, "delta": 1.0e-10, "Phi": 5.0e-8, "U": 1.0e-9, "V": 1.0e-9}
+# Tolerances of the GPU FP64 path against the oracle on identical inputs
+# (same Gauss-Legendre quadrature): the reference's own for the physical fields
+# and their Fourier coefficients (a Fourier coefficient fft(x / I)[m] is bounded
+# by max |x|); products and forcing terms, for which the reference states none,
+# get 1e-11 of their maximum.
+STATE_ATOL = {"etam_curr": ATOL["eta"], "etam_prev": ATOL["eta"], "deltam_curr": ATOL["delta"],
+              "deltam_prev": ATOL["delta"], "Phim_curr": ATOL["Phi"], "Phim_prev": ATOL["Phi"],
+              "Um_curr": ATOL["U"], "Vm_curr": ATOL["V"]}
+PRODUCT_REL = 1e-11
+
+
+@contextlib.contextmanager
+def exact_quadrature():
+    """Run the oracle on the exact (mpmath) Gauss-Legendre nodes and weights that
+    the GPU path builds, instead of SciPy's roots_legendre."""
+    from oracle import swampe_oracle as o
+
+    exact = np.load(GOLDEN / "gauss_legendre.npz")
+    o.set_quadrature({J: (exact[f"mu{J}"], exact[f"w{J}"]) for J in (64, 96, 160)})
+    try:
+        yield
+    finally:
+        o.set_quadrature(None)

@@ -1,7 +1,7 @@
 """The opt-in schemes on the GPU: the semi-implicit leapfrog
 (semi_implicit_tdiff.py) and the Robert-Asselin-Williams filter
 (model.py:1007-1087), forward, against the FP64 oracle on identical inputs
-(2e-9 of each field's maximum, as the classic path) and against the
+(the reference's absolute tolerances, as the classic path) and against the
 properties the reference's tests assert (unit_tests/test_semi_implicit.py,
 unit_tests/test_raw_filter.py)."""
 import numpy as np

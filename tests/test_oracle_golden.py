@@ -33,6 +33,19 @@ def test_oracle_matches_reference_fixtures(case):
     np.testing.assert_allclose(got, ref["phase_curve"], rtol=0, atol=1e-10)
 
 
+@pytest.mark.parametrize("case", list(FIXTURE_CASES))
+def test_oracle_legacy_spinup_geopot_match_fixtures(case):
+    """run_model's (tmax, 2) spinup / geopot arrays (model.py:2106-2158) against
+    the arrays the reference fixtures carry: wind diagnostics at the U/V
+    tolerance, Phi extrema at the Phi tolerance."""
+    ref = np.load(GOLDEN / f"{case}.npz")
+    kw = FIXTURE_CASES[case]
+    r = o.run_model_scan(**kw)
+    spin, geop = o.legacy_diagnostics(o.NUMPY, r, kw["tmax"], kw["test"])
+    np.testing.assert_allclose(spin, ref["spinup"], rtol=0, atol=ATOL["U"])
+    np.testing.assert_allclose(geop, ref["geopot"], rtol=0, atol=ATOL["Phi"])
+
+
 def test_oracle_transform_kats():
     """unit_tests/test_transform_stack.py:37-97."""
     geo = o.cached_geometry(42)
