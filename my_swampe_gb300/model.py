@@ -16,7 +16,8 @@ from __future__ import annotations
 
 import math
 import warnings
-from dataclasses import dataclass
+from collections import OrderedDict
+from dataclasses import dataclass, replace as _dc_replace
 from typing import Any, Dict, NamedTuple, Optional
 
 import numpy as np
@@ -50,6 +51,32 @@ def _geometry_engine(M: int) -> Engine:
     if M not in _GEO_ENGINES:
         _GEO_ENGINES[M] = Engine([(M, 1)], "fp64")
     return _GEO_ENGINES[M]
+
+
+# Engines (plan, geometry, packed bases, device state, captured step graphs)
+# reused across calls, keyed on (M, B, precision, device): the counterpart of
+# the reference's lru_cache'd geometry and per-key compiled scans
+# (model.py:62-153).  A call never returns views of an engine's buffers.
+_ENGINE_CACHE: "OrderedDict[tuple, Engine]" = OrderedDict()
+_ENGINE_CACHE_SIZE = 8
+
+
+def _engine_for(M: int, B: int, precision: str, device=None) -> Engine:
+    dev = torch.device(device) if device is not None else (
+        torch.device("cuda", torch.cuda.current_device()) if torch.cuda.is_available() else torch.device("cuda"))
+    key = (int(M), int(B), precision, dev.type, dev.index)
+    eng = _ENGINE_CACHE.pop(key, None)
+    if eng is None:
+        eng = Engine([(int(M), int(B))], precision, device)
+    _ENGINE_CACHE[key] = eng
+    while len(_ENGINE_CACHE) > _ENGINE_CACHE_SIZE:
+        _ENGINE_CACHE.popitem(last=False)
+    return eng
+
+
+def clear_engine_cache() -> None:
+    """Release the cached engines (their plans and device buffers)."""
+    _ENGINE_CACHE.clear()
 
 
 @dataclass(frozen=True)
@@ -103,6 +130,13 @@ class Static:
     sigma_exp: torch.Tensor
     sigmaPhi_exp: torch.Tensor
     Phieq: torch.Tensor
+    # scalars the tables above were built from: the kernels rebuild their
+    # coefficient tables and Phieq from these (dataclasses.replace of taurad,
+    # taudrag, ... takes effect, as in the retrieval's fast path)
+    DPhieq: Any = None
+    K6: Any = None
+    K6Phi: Any = None
+    test: Optional[int] = None
 
 
 class State(NamedTuple):
@@ -204,7 +238,7 @@ def build_static(*, M, dt, a, omega, g, Phibar, taurad, taudrag, DPhieq, K6, K6P
         fmn=fmn, tstepcoeff=tsc, tstepcoeff2=tsc2, tstepcoeffmn=tcmn,
         marray=mm[:, None].expand(M + 1, N + 1), mJarray=mm[None, :].expand(J, M + 1), narray=nn1[None, :].expand(M + 1, N + 1),
         sigma=_sig(K6_, True, False), sigmaPhi=_sig(K6P, False, False), sigma_exp=_sig(K6_, True, True),
-        sigmaPhi_exp=_sig(K6P, False, True), Phieq=Phieq,
+        sigmaPhi_exp=_sig(K6P, False, True), Phieq=Phieq, DPhieq=DP, K6=K6_, K6Phi=K6P, test=test,
     )
 
 
@@ -423,7 +457,7 @@ def run_model_scan(
             raise NotImplementedError("reverse-mode gradients with respect to the initial fields need the adjoint, "
                                       "which the explicit and semi-implicit schemes do not have (forward mode works)")
 
-    eng = Engine([(M, B)], precision, device)
+    eng = _engine_for(M, B, precision, device)
     dev = eng.device
     K6Phi_eff = K6 if K6Phi is None else K6Phi
     eng.set_params(0, dt=dt, a=a, omega=omega, Phibar=Phibar, taurad=taurad, taudrag=taudrag,
@@ -559,12 +593,12 @@ def _assemble_state(eng: Engine, phys: torch.Tensor, Rum, Rvm, batched: bool, fi
     gd = eng.groups[0]
     four = gd["fourier"]
 
-    def fo(k):  # (M+1, B, J) -> (B, J, M+1)
-        v = four[k].permute(1, 2, 0)
+    def fo(k):  # (M+1, B, J) -> (B, J, M+1), a copy (the engine's buffers are reused)
+        v = four[k].permute(1, 2, 0).clone(memory_format=torch.contiguous_format)
         return v if batched else v[0]
 
     def fr(t):
-        v = t.permute(1, 2, 0)
+        v = t.permute(1, 2, 0).clone(memory_format=torch.contiguous_format)
         return v if batched else v[0]
 
     def ph(k):
@@ -586,12 +620,370 @@ def _assemble_state(eng: Engine, phys: torch.Tensor, Rum, Rvm, batched: bool, fi
     )
 
 
-def run_model_scan_final(**kw) -> Dict[str, Any]:
-    """``model.py:1844-1951``: terminal state only; diagnostics off by default."""
-    if "return_history" in kw:
-        raise TypeError("run_model_scan_final() got an unexpected keyword argument 'return_history'")
-    kw.setdefault("diagnostics", False)
-    return run_model_scan(return_history=False, **kw)
+# ---------------------------------------------------------------------------
+# The scan core's own entry points (model.py:694-772, 1197-1342), which the
+# retrieval calls directly (retrieval/scripts/pipeline.py:646-688, 870-927):
+# build_static + _init_state_from_fields once, then simulate_scan_last (or a
+# loop of _step_once_state_only) per parameter sample, with
+# dataclasses.replace(static, taurad=..., taudrag=...) and optional FP32 casts
+# of static and state (which select the fast precision here).
+# ---------------------------------------------------------------------------
+# State Fourier field -> Fourier slot of the engine
+_STATE_SLOTS = (("etam_curr", _lib.F_ETA), ("deltam_curr", _lib.F_DELTA), ("Phim_curr", _lib.F_PHI),
+                ("Um_curr", _lib.F_U), ("Vm_curr", _lib.F_V), ("Am_curr", _lib.F_A), ("Bm_curr", _lib.F_B),
+                ("Cm_curr", _lib.F_C), ("Dm_curr", _lib.F_D), ("Em_curr", _lib.F_E), ("PhiFm_curr", _lib.F_PHIF),
+                ("Fm_curr", _lib.F_F), ("Gm_curr", _lib.F_G))
+_PREV_NAMES = ("etam_prev", "deltam_prev", "Phim_prev")
+_PREV_SLOTS = (_lib.F_ETA_PREV, _lib.F_DELTA_PREV, _lib.F_PHI_PREV)
+_MID_SLOTS = (_lib.F_ETA_MID, _lib.F_DELTA_MID, _lib.F_PHI_MID)
+_STATIC_PARAMS = ("dt", "a", "omega", "Phibar", "taurad", "taudrag", "DPhieq", "K6", "K6Phi")
+
+
+def _state_precision(x) -> str:
+    dt = x.dtype if torch.is_tensor(x) else np.asarray(x).dtype
+    return "fast" if dt in (torch.float32, torch.complex64, np.float32, np.complex64) else "fp64"
+
+
+def _flags_c(flags: "RunFlags", test, t_start: int, diagnostics: Optional[bool] = None) -> RunFlagsC:
+    return RunFlagsC(scheme=2 if flags.semi_implicit else (1 if flags.expflag else 0), forcflag=flags.forcflag,
+                     diffflag=flags.diffflag, modalflag=flags.modalflag, test=test,
+                     diagnostics=flags.diagnostics if diagnostics is None else diagnostics,
+                     blowup_rms=float(flags.blowup_rms), t_start=int(t_start), raw_filter=bool(flags.raw_filter))
+
+
+def _static_values(static: Static, flags: "RunFlags", test) -> Dict[str, Any]:
+    """Per-member parameter values of a Static (tensors keep their autograd
+    graph and forward-mode tangents)."""
+    if static.K6 is None or static.DPhieq is None:
+        raise ValueError("this Static carries no K6 / DPhieq: build it with my_swampe_gb300.model.build_static")
+    vals = {k: getattr(static, k) for k in _STATIC_PARAMS}
+    if vals["K6Phi"] is None:
+        vals["K6Phi"] = vals["K6"]
+    if test is not None:
+        vals["DPhieq"] = 0.0
+    vals.update(alpha=flags.alpha, si_alpha=flags.si_alpha, williams_alpha=flags.williams_alpha)
+    return vals
+
+
+def _set_static_params(eng: Engine, vals: Dict[str, Any]) -> None:
+    nd = {k: (v.detach() if torch.is_tensor(v) else v) for k, v in vals.items()}
+    eng.set_params(0, **nd)
+
+
+def _init_state_from_fields(*, static: Static, flags: "RunFlags", test: Optional[int], eta0, delta0, Phi0, U0,
+                            V0) -> State:
+    """Two-level initial state, prev == curr == the given physical fields
+    (model.py:694-772): forcing at the initial step, truncated Fourier
+    coefficients of the eight fields, the nonlinear terms and the lagged
+    momentum-forcing remainder, computed by the library's INIT kernel.  The
+    fields are (J, I) or (B, J, I); float32 fields build the state in the
+    fast precision."""
+    prec = _state_precision(eta0)
+    dev = static.mus.device
+    rdt = torch.float64 if prec == "fp64" else torch.float32
+    f0 = [torch.as_tensor(x, device=dev).to(rdt) for x in (eta0, delta0, Phi0, U0, V0)]
+    batched = f0[0].dim() == 3
+    B = f0[0].shape[0] if batched else 1
+    eng = _engine_for(static.M, B, prec, dev)
+    J, I = eng.groups[0]["J"], eng.groups[0]["I"]
+    for name, x in zip(("eta0", "delta0", "Phi0", "U0", "V0"), f0):
+        if tuple(x.shape[-2:]) != (J, I) or (batched and x.shape != f0[0].shape):
+            raise ValueError(f"{name} must have shape {(J, I)} (or (B, J, I)), got {tuple(x.shape)}")
+    _set_static_params(eng, _static_values(static, flags, test))
+    ics = torch.stack([x if batched else x[None] for x in f0], 0)
+    eng.init_state([ics], _flags_c(flags, test, 2, diagnostics=False))
+    gd = eng.groups[0]
+    four = gd["fourier"]
+    td = gd["params"][_lib.P_TAUDRAG]
+    inv_td = torch.where(td == -1.0, torch.zeros_like(td), 1.0 / td).to(eng.rdtype)
+    Rum = four[_lib.F_F] + four[_lib.F_U] * inv_td[None, :, None]
+    Rvm = four[_lib.F_G] + four[_lib.F_V] * inv_td[None, :, None]
+    phys = torch.stack([ics[k] for k in (0, 1, 2, 3, 4, 0, 1, 2)], 0)
+    st = _assemble_state(eng, phys, Rum, Rvm, batched)
+    # physical members are the given fields themselves, as in the reference
+    return st._replace(eta_prev=f0[0], eta_curr=f0[0], delta_prev=f0[1], delta_curr=f0[1], Phi_prev=f0[2],
+                       Phi_curr=f0[2], U_curr=f0[3], V_curr=f0[4],
+                       dead=torch.zeros(st.dead.shape, dtype=torch.bool, device=dev))
+
+
+def _load_state(eng: Engine, flags: "RunFlags", state0: State, test, t0: int, diag=None) -> int:
+    """Put a reference-layout State into the engine; returns the t_start the
+    steps must use.
+
+    The Fourier carries are taken as given.  The physical fields enter as the
+    synthesis of their truncated Fourier coefficients plus their part beyond
+    the truncation, carried as the engine's residual with per-member weights:
+    a two-level state (prev == curr, e.g. from _init_state_from_fields) keeps
+    the residual on both levels; a stepped state (band-limited curr, e.g. a
+    previous run's last_state) keeps the prev level's.  A member whose prev and
+    curr levels both carry different content beyond the truncation is refused."""
+    gd = eng.groups[0]
+    four, resid, member = gd["fourier"], gd["resid"], gd["member"]
+    dev, rdt, cdt = eng.device, eng.rdtype, eng.cdtype
+    batched = torch.as_tensor(state0.eta_curr).dim() == 3
+
+    def ph(x):
+        t = torch.as_tensor(x, device=dev).detach().to(rdt)
+        return t if batched else t[None]
+
+    def fo(x):  # (B, J, M+1) -> (M+1, B, J)
+        t = torch.as_tensor(x, device=dev).detach().to(cdt)
+        return (t if batched else t[None]).permute(2, 0, 1)
+
+    pc = torch.stack([ph(getattr(state0, n)) for n in ("eta_curr", "delta_curr", "Phi_curr", "U_curr", "V_curr")])
+    pp = torch.stack([ph(getattr(state0, n)) for n in ("eta_prev", "delta_prev", "Phi_prev")])
+    fresh = (pp == pc[:3]).flatten(2).all(dim=2).all(dim=0)  # (B,): prev == curr
+    mid = r_p = None
+    if not bool(fresh.all()):
+        eng.init_state([torch.cat([pp, pc[3:]], 0)], _flags_c(flags, test, t0, diagnostics=False))
+        mid = four[[_lib.F_ETA, _lib.F_DELTA, _lib.F_PHI]].clone()
+        r_p = resid[:3].clone()
+    eng.init_state([pc], _flags_c(flags, test, t0), diag=diag)
+    for name, slot in _STATE_SLOTS:
+        four[slot].copy_(fo(getattr(state0, name)))
+    filtered = bool(flags.semi_implicit or flags.raw_filter)
+    for name, ps, ms in zip(_PREV_NAMES, _PREV_SLOTS, _MID_SLOTS):
+        v = fo(getattr(state0, name))
+        if filtered:
+            four[ms].copy_(v)   # the Fourier prev carry is the filtered lineage
+            four[ps].copy_(v)
+        else:
+            four[ps].copy_(v)
+            if mid is not None:
+                four[ms].copy_(mid[_MID_SLOTS.index(ms)])
+    if flags.semi_implicit:  # the lagged remainders live in the unfiltered prev slots
+        four[_lib.F_RU_LAG].copy_(fo(state0.Rum_lag))
+        four[_lib.F_RV_LAG].copy_(fo(state0.Rvm_lag))
+    stepped = torch.zeros_like(fresh)
+    if r_p is not None:
+        tol = 1e-9 if eng.precision == "fp64" else 1e-5
+        scale = pc.abs().flatten(2).amax(dim=2).clamp_min(1e-300)[..., None, None]  # (5, B, 1, 1)
+        r_c = resid.clone()
+        rc_small = ((r_c.abs() <= tol * scale).flatten(2).all(dim=2)).all(dim=0)
+        same = ((r_p - r_c[:3]).abs() <= tol * scale[:3]).flatten(2).all(dim=2).all(dim=0)
+        stepped = ~fresh & rc_small
+        bad = ~fresh & ~stepped & ~same
+        if bool(bad.any()):
+            raise NotImplementedError(
+                "state0 members " + str(torch.nonzero(bad).flatten().tolist()) + " carry different content beyond "
+                "the truncation on their prev and curr levels; only two-level states (prev == curr) and stepped "
+                "states (band-limited curr) are supported")
+        sel = stepped[None, :, None, None]
+        resid[:3].copy_(torch.where(sel, r_p, r_c[:3]))
+        w1 = torch.ones_like(member[_lib.MS_WCURR])
+        member[_lib.MS_WCURR].copy_(torch.where(stepped, torch.zeros_like(w1), w1))
+        member[_lib.MS_WMID].copy_(w1)
+        member[_lib.MS_UPDATED].copy_(stepped.to(member.dtype))
+    dead = torch.as_tensor(state0.dead, device=dev).reshape(-1).to(member.dtype)
+    member[_lib.MS_DEAD].copy_(dead.expand(member.shape[1]))
+    # stepped members advance by increments from the first step (fast precision);
+    # the semi-implicit scheme takes its lagged remainders from the state
+    return t0 - 1 if (flags.semi_implicit or bool(stepped.all())) else t0
+
+
+def _t_window(t_seq):
+    t = torch.as_tensor(t_seq).reshape(-1).to("cpu", torch.int64)
+    n = int(t.numel())
+    if n and not torch.equal(t, torch.arange(int(t[0]), int(t[0]) + n)):
+        raise ValueError("t_seq must be consecutive time indices (arange(t0, t0 + n))")
+    return (int(t[0]) if n else 2), n
+
+
+def _uv_matches_state(Uic, Vic, state0) -> bool:
+    return all(x is None or torch.equal(torch.as_tensor(x).to(torch.as_tensor(y).device, torch.as_tensor(y).dtype),
+                                        torch.as_tensor(y))
+               for x, y in ((Uic, state0.U_curr), (Vic, state0.V_curr)))
+
+
+def _scan_checks(static: Static, flags: "RunFlags", state0: State, test, Uic, Vic):
+    if test not in (None, 1, 2):
+        raise NotImplementedError(f"test={test} is not implemented (use None, 1 or 2)")
+    if flags.semi_implicit and flags.expflag:
+        raise ValueError("semi_implicit=True is incompatible with expflag=True (pick one scheme).")
+    if flags.raw_filter and flags.expflag:
+        raise ValueError("raw_filter=True is incompatible with expflag=True.")
+    if test == 1 and not _uv_matches_state(Uic, Vic, state0):
+        raise NotImplementedError("test=1 pins the winds to the state's own U_curr, V_curr: Uic, Vic must equal them")
+
+
+def _run_loaded(static: Static, flags: "RunFlags", state0: State, test, t0: int, n: int, hist: bool):
+    """Load state0, step n times from t0; returns (engine, physical outputs,
+    diagnostics rows or None, history or None, batched)."""
+    prec = _state_precision(state0.etam_curr)
+    batched = torch.as_tensor(state0.eta_curr).dim() == 3
+    B = torch.as_tensor(state0.eta_curr).shape[0] if batched else 1
+    dev = static.mus.device
+    eng = _engine_for(static.M, B, prec, dev)
+    _set_static_params(eng, _static_values(static, flags, test))
+    diag = eng.new_diag(n) if flags.diagnostics else None
+    t_start = _load_state(eng, flags, state0, test, t0, diag=diag)
+    fc = _flags_c(flags, test, t_start)
+    gd = eng.groups[0]
+    h = [torch.empty((n, 5, B, gd["J"], gd["I"]), dtype=eng.rdtype, device=eng.device)] if hist else None
+    if n > 0:
+        eng.forward(fc, t0=t0, nsteps=n, row0=0, diag=diag, hist=h, write_prev_last=True)
+    phys = eng.output_physical(fc)[0]
+    eng.check_device_status()
+    return eng, fc, phys, diag, h, batched
+
+
+def _state_after(eng: Engine, flags: "RunFlags", phys, batched: bool, state0: State) -> State:
+    four = eng.groups[0]["fourier"]
+    if flags.semi_implicit:
+        Rum, Rvm = four[_lib.F_RU_LAG], four[_lib.F_RV_LAG]
+        st = _assemble_state(eng, phys, Rum, Rvm, batched, filtered_prev=True)
+    else:  # pass-through carries (model.py:1144-1145)
+        st = _assemble_state(eng, phys, four[_lib.F_F], four[_lib.F_G], batched,
+                             filtered_prev=bool(flags.raw_filter))
+        st = st._replace(Rum_lag=state0.Rum_lag, Rvm_lag=state0.Rvm_lag)
+    return st
+
+
+class _ScanLastFn(torch.autograd.Function):
+    """Derivatives of simulate_scan_last's curr fields (eta, delta, Phi, U, V)
+    in the Static's scalar parameters, with state0 held fixed (as the
+    retrieval's fast path does: its state0 is built once from the base
+    parameters).  Forward mode: the tangent-linear model from a zero initial
+    tangent.  Reverse mode: one tangent run per parameter that needs a
+    gradient (members are independent: one run serves every member)."""
+
+    @staticmethod
+    def forward(ctx, ctl, *params):
+        ctx.ctl = ctl
+        ctx.save_for_forward(*params)
+        ctx.save_for_backward(*params)
+        return ctl["out"]
+
+    @staticmethod
+    def _tangent(ctx, dpar_rows):
+        ctl = ctx.ctl
+        eng, flags, state0, test, t0, n = ctl["eng"], ctl["flags"], ctl["state0"], ctl["test"], ctl["t0"], ctl["n"]
+        _set_static_params(eng, ctl["vals"])
+        t_start = _load_state(eng, flags, state0, test, t0)
+        fc = _flags_c(flags, test, t_start, diagnostics=False)
+        tfour, tresid, _ = eng.new_tangent_buffers()
+        eng.tangent_forward(fc, t0, n, tfour, tresid, [dpar_rows])
+        out = eng.tangent_output(fc, tfour, tresid, [dpar_rows])[0][:5]
+        eng.check_device_status()
+        return out
+
+    @staticmethod
+    def jvp(ctx, _ctl_t, *params_t):
+        B = ctx.ctl["B"]
+        dev = ctx.ctl["eng"].device
+        rows = torch.zeros((_lib.NTANGENT, B), dtype=torch.float64, device=dev)
+        for k, t in enumerate(params_t):
+            if t is not None:
+                rows[k] = torch.as_tensor(t, device=dev).to(torch.float64).expand(B)
+        out = _ScanLastFn._tangent(ctx, rows)
+        return out.to(ctx.ctl["out"].dtype)
+
+    @staticmethod
+    def backward(ctx, gout):
+        B = ctx.ctl["B"]
+        dev = ctx.ctl["eng"].device
+        params = ctx.saved_tensors
+        res = [None] * (1 + len(params))
+        w = gout.to(torch.float64)
+        for k in range(len(params)):
+            if not ctx.needs_input_grad[1 + k]:
+                continue
+            rows = torch.zeros((_lib.NTANGENT, B), dtype=torch.float64, device=dev)
+            rows[k] = 1.0
+            jk = _ScanLastFn._tangent(ctx, rows).to(torch.float64)
+            g = (w * jk).sum(dim=(0, 2, 3))
+            res[1 + k] = g.sum().reshape(params[k].shape).to(params[k].dtype) if params[k].dim() == 0 else \
+                g.reshape(params[k].shape).to(params[k].dtype)
+        return tuple(res)
+
+
+def simulate_scan_last(*, static: Static, flags: "RunFlags", state0: State, t_seq, test: Optional[int], Uic, Vic,
+                       remat_step: bool = False) -> State:
+    """Advance state0 along t_seq without a time history (model.py:1281-1342);
+    returns the final State.  ``remat_step`` is accepted for compatibility (the
+    kernels keep no per-step residuals).  float32 state fields select the fast
+    precision.  The scalar parameters of ``static`` (dt, a, omega, Phibar,
+    taurad, taudrag, DPhieq, K6, K6Phi) rebuild the coefficient tables, so a
+    ``dataclasses.replace(static, taurad=..., taudrag=...)`` takes effect; as
+    tensors that require grad or carry forward-mode tangents they make the
+    curr fields of the result differentiable, with state0 held fixed."""
+    _scan_checks(static, flags, state0, test, Uic, Vic)
+    t0, n = _t_window(t_seq)
+    vals = _static_values(static, flags, test)
+    eng, fc, phys, _, _, batched = _run_loaded(static, flags, state0, test, t0, n, hist=False)
+    st = _state_after(eng, flags, phys, batched, state0)
+    tracked = [k for k in _lib.TANGENT_PARAMS if k in vals and _tracked(vals[k])]
+    if tracked and n > 0:
+        if flags.raw_filter or test == 1:
+            raise NotImplementedError("derivatives are implemented with the classic filter and test None or 2")
+        B = eng.groups[0]["B"]
+        dev = eng.device
+        params = [torch.as_tensor(vals[k], dtype=torch.float64, device=dev) if k in vals else
+                  torch.zeros((), dtype=torch.float64, device=dev) for k in _lib.TANGENT_PARAMS]
+        out = torch.stack([phys[k] for k in range(5)], 0)
+        ctl = dict(eng=eng, flags=flags, state0=state0, test=test, t0=t0, n=n, B=B, vals=vals, out=out)
+        dcurr = _ScanLastFn.apply(ctl, *params)
+        pick = (lambda v: v) if batched else (lambda v: v[0])
+        st = st._replace(eta_curr=pick(dcurr[0]), delta_curr=pick(dcurr[1]), Phi_curr=pick(dcurr[2]),
+                         U_curr=pick(dcurr[3]), V_curr=pick(dcurr[4]))
+    return st
+
+
+def simulate_scan(*, static: Static, flags: "RunFlags", state0: State, t_seq, test: Optional[int], Uic, Vic):
+    """Advance state0 along t_seq keeping the per-step outputs
+    (model.py:1237-1278): returns (last_state, outs) with outs["eta" | "delta"
+    | "Phi" | "U" | "V"] of shape (T, J, I) (member axis first for ensembles)
+    and, with flags.diagnostics, "rms", "spin_min", "phi_min", "phi_max",
+    "dead" of shape (T,)."""
+    _scan_checks(static, flags, state0, test, Uic, Vic)
+    t0, n = _t_window(t_seq)
+    eng, fc, phys, diag, h, batched = _run_loaded(static, flags, state0, test, t0, n, hist=True)
+    st = _state_after(eng, flags, phys, batched, state0)
+    outs: Dict[str, Any] = {}
+    for k, name in enumerate(("eta", "delta", "Phi", "U", "V")):
+        v = h[0][:, k]
+        outs[name] = v.permute(1, 0, 2, 3) if batched else v[:, 0]
+    B = eng.groups[0]["B"]
+    if diag is not None:
+        d = diag[0][:n]
+        vals = dict(rms=torch.sqrt(d[:, _lib.D_RMS2]), spin_min=d[:, _lib.D_SPIN], phi_min=d[:, _lib.D_PHIMIN],
+                    phi_max=d[:, _lib.D_PHIMAX], dead=d[:, _lib.D_DEAD] != 0)
+    else:
+        z = torch.zeros((n, B), dtype=torch.float64, device=eng.device)
+        vals = dict(rms=z, spin_min=z, phi_min=z, phi_max=z, dead=torch.zeros((n, B), dtype=torch.bool,
+                                                                                device=eng.device))
+    for k, v in vals.items():
+        outs[k] = v.t() if batched else v[:, 0]
+    return st, outs
+
+
+def _step_once_state_only(state: State, t, static: Static, flags: "RunFlags", test: Optional[int], Uic, Vic) -> State:
+    """One step returning only the new State (model.py:1197-1235)."""
+    t = int(torch.as_tensor(t).reshape(()).item())
+    return simulate_scan_last(static=static, flags=flags, state0=state, t_seq=[t], test=test, Uic=Uic, Vic=Vic)
+
+
+def run_model_scan_final(
+    *, M: int, dt, tmax: int, Phibar, omega, a, test: Optional[int] = None, g=9.8, forcflag: bool = True,
+    taurad=86400.0, taudrag=86400.0, DPhieq=4 * (10**6), a1=0.05, diffflag: bool = True, modalflag: bool = True,
+    alpha=0.01, expflag: bool = False, K6=1.24 * (10**33), K6Phi=None, contflag: bool = False,
+    custompath: Optional[str] = None, contTime=None, timeunits: str = "hours", starttime: Optional[int] = None,
+    eta0_init=None, delta0_init=None, Phi0_init=None, U0_init=None, V0_init=None,
+    semi_implicit: bool = False, si_alpha=0.5, raw_filter: bool = False, williams_alpha=0.53,
+    diagnostics: bool = False, remat_step: bool = False, jit_scan: bool = True, donate_state: bool = False,
+    precision: str = "fp64", device=None,
+) -> Dict[str, Any]:
+    """``model.py:1844-1951``: terminal state only (``static``, ``t_seq``,
+    ``last_state``, ``starttime``); the same keywords as :func:`run_model_scan`
+    without ``return_history``, diagnostics off by default."""
+    return run_model_scan(
+        M=M, dt=dt, tmax=tmax, Phibar=Phibar, omega=omega, a=a, test=test, g=g, forcflag=forcflag, taurad=taurad,
+        taudrag=taudrag, DPhieq=DPhieq, a1=a1, diffflag=diffflag, modalflag=modalflag, alpha=alpha, expflag=expflag,
+        K6=K6, K6Phi=K6Phi, contflag=contflag, custompath=custompath, contTime=contTime, timeunits=timeunits,
+        starttime=starttime, eta0_init=eta0_init, delta0_init=delta0_init, Phi0_init=Phi0_init, U0_init=U0_init,
+        V0_init=V0_init, semi_implicit=semi_implicit, si_alpha=si_alpha, raw_filter=raw_filter,
+        williams_alpha=williams_alpha, diagnostics=diagnostics, return_history=False, remat_step=remat_step,
+        jit_scan=jit_scan, donate_state=donate_state, precision=precision, device=device)
 
 
 def run_model(M, dt, tmax, Phibar, omega, a, test=None, g=9.8, forcflag=True, taurad=86400, taudrag=86400,

@@ -4,8 +4,9 @@
    member of four gets a wind of 20 km/s in its host-prepared initial
    condition, so its RMS wind is above blowup_rms = 8000 m/s from the first
    step.  Only that member's dead flag trips (dead_first_idx 0, every history
-   row its frozen initial state); the other members are bit-identical to a run
-   of the clean ensemble.  Both precisions (the tensor-core Legendre kernel
+   row its frozen initial state); the other members' fields are bit-identical
+   to a run of the clean ensemble (their diagnostics, reduced with atomics,
+   equal to round-off).  Both precisions (the tensor-core Legendre kernel
    has its own gate).
 2. The bounded waits of the tensor-core kernels: with the plan's poll limit
    at 0 (swp_plan_set_wait_limit) every mbarrier wait gives up at once.  The
@@ -51,8 +52,12 @@ def test_blowup_gate_freezes_only_the_blown_member(cuda, precision):
     assert bad["last_state"].dead.tolist() == [False, False, True, False]
     assert bool(bad["outs"]["dead"][2].all()) and not bool(bad["outs"]["dead"][[0, 1, 3]].any())
     keep = [0, 1, 3]
-    for k in ("eta", "delta", "Phi", "U", "V", "rms", "spin_min", "phi_min", "phi_max"):
+    for k in ("eta", "delta", "Phi", "U", "V"):
         assert torch.equal(bad["outs"][k][keep], clean["outs"][k][keep]), k
+    # the diagnostics are sums over latitude blocks reduced with atomics, whose
+    # order varies from run to run: equal to round-off
+    for k in ("rms", "spin_min", "phi_min", "phi_max"):
+        torch.testing.assert_close(bad["outs"][k][keep], clean["outs"][k][keep], rtol=1e-12, atol=0, msg=k)
     for name in ("eta_curr", "delta_curr", "Phi_curr", "U_curr", "V_curr", "etam_curr", "Phim_curr", "Am_curr"):
         assert torch.equal(getattr(bad["last_state"], name)[keep], getattr(clean["last_state"], name)[keep]), name
     # the dead member keeps its initial state in every history row

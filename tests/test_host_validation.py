@@ -159,3 +159,47 @@ def test_fwd_grad_on_a_cpu_function():
     g = fwd_grad(lambda t: (t[0] * t[1]) ** 2 + torch.sin(t[2]), theta, chunk=2)
     want = torch.tensor([2 * theta[0] * theta[1] ** 2, 2 * theta[1] * theta[0] ** 2, torch.cos(theta[2])])
     assert torch.allclose(g, want, rtol=1e-14, atol=0)
+
+
+# run_model_scan_final's keywords and defaults (reference model.py:1844-1886)
+_FINAL_SIGNATURE = dict(
+    M=None, dt=None, tmax=None, Phibar=None, omega=None, a=None, test=None, g=9.8, forcflag=True, taurad=86400.0,
+    taudrag=86400.0, DPhieq=4 * (10**6), a1=0.05, diffflag=True, modalflag=True, alpha=0.01, expflag=False,
+    K6=1.24 * (10**33), K6Phi=None, contflag=False, custompath=None, contTime=None, timeunits="hours",
+    starttime=None, eta0_init=None, delta0_init=None, Phi0_init=None, U0_init=None, V0_init=None,
+    semi_implicit=False, si_alpha=0.5, raw_filter=False, williams_alpha=0.53, diagnostics=False,
+    remat_step=False, jit_scan=True, donate_state=False,
+)
+
+
+def test_run_model_scan_final_keeps_the_reference_signature():
+    import inspect
+
+    from my_swampe_gb300 import run_model_scan_final
+
+    params = inspect.signature(run_model_scan_final).parameters
+    for name, default in _FINAL_SIGNATURE.items():
+        assert name in params, name
+        p = params[name]
+        assert p.kind == inspect.Parameter.KEYWORD_ONLY, name
+        if default is None and name in ("M", "dt", "tmax", "Phibar", "omega", "a"):
+            assert p.default is inspect.Parameter.empty, name
+        else:
+            assert p.default == default, (name, p.default, default)
+    assert "return_history" not in params
+
+
+def test_scan_core_entry_points_exist():
+    import inspect
+
+    from my_swampe_gb300 import model
+
+    for fn, names in ((model._init_state_from_fields, ("static", "flags", "test", "eta0", "delta0", "Phi0", "U0", "V0")),
+                      (model.simulate_scan_last, ("static", "flags", "state0", "t_seq", "test", "Uic", "Vic",
+                                                  "remat_step")),
+                      (model.simulate_scan, ("static", "flags", "state0", "t_seq", "test", "Uic", "Vic")),
+                      (model._step_once_state_only, ("state", "t", "static", "flags", "test", "Uic", "Vic"))):
+        assert tuple(inspect.signature(fn).parameters)[: len(names)] == names, fn.__name__
+    import dataclasses
+
+    assert dataclasses.is_dataclass(model.Static) and model.RunFlags(alpha=0.02).alpha == 0.02
