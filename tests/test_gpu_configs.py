@@ -1,8 +1,16 @@
-"""The benchmark workloads as GPU tests (reduced lengths where the CPU oracle
-is the checker):
+"""The benchmark workloads as GPU tests:
   steady zonal geostrophic flow, M=42, one member (test=2 regime, explicit ICs)
-  M=63 ensemble of 32: gradients of mean((Phi_T - Phi_target)^2) vs central FD
-  mixed truncations (M=42, 63, 106) in one launch == separate launches
+  forced single member, M=42, FP64, 28,800 steps (10 days at dt = 30 s): the
+    oracle over a 100-step prefix at the reference's tolerances, then finite
+    and ungated to the end
+  forced ensemble, M=42, B=8, 1440 steps: the fast path's error against the
+    FP64 path (relative L2 of Phi <= 1e-5)
+  M=63 ensemble of 32, 2000 steps, checkpoints every 50: gradients of
+    mean((Phi_T - Phi_target)^2) in FP64 and in the fast precision against
+    central differences
+  mixed truncations (M=42, 63, 106) in one launch == separate launches, and the
+    64 / 32 / 8 member mixed ensemble over 1440 steps in the fast precision with
+    its error per group against FP64
 """
 import math
 
@@ -128,3 +136,164 @@ def test_M63_ensemble_gradients_vs_central_fd(cuda):
         fd = ((lp - lm) / (2 * h) / 2).cpu().numpy()
         ad = par[name].grad.cpu().numpy()
         np.testing.assert_allclose(ad, fd, rtol=1e-5, err_msg=name)
+
+
+def _forced_single_ics(seed=2024):
+    """Config 2's initial state: rest (eta = 2 Omega mu, delta = U = V = 0) with
+    Phi = seeded Gaussian noise of amplitude 1e-3 Phibar on the spectral
+    coefficients with n <= 10."""
+    geo = o.cached_geometry(42)
+    J, I = geo["J"], geo["I"]
+    mu = geo["mus"][:, None] * np.ones((1, I))
+    rng = np.random.default_rng(seed)
+    c = np.zeros((43, 43), complex)
+    for m in range(11):
+        for n in range(m, 11):
+            c[m, n] = 1e-3 * 4.0e6 * (rng.standard_normal() + (1j * rng.standard_normal() if m > 0 else 0.0))
+    Phi0 = np.real(o.invrs_fft(o.NUMPY, o.invrs_leg(o.NUMPY, c, I, 42, geo["Pmn"]), I))
+    z = np.zeros((J, I))
+    return dict(eta0_init=2 * 3.2e-5 * mu, delta0_init=z, Phi0_init=Phi0, U0_init=z, V0_init=z)
+
+
+def test_forced_single_member_ten_days(cuda):
+    """B=1, FP64, forced synchronously rotating regime (a = 8.2e7, Omega =
+    3.2e-5, Phibar = DPhieq = 4e6, taurad = taudrag = 1 day, dt = 30 s), 28,800
+    steps.  The first 100 steps against the oracle at the reference's
+    tolerances (same quadrature); the whole run finite, never gated, with Phi
+    within the forcing's range."""
+    import torch
+    from conftest import ATOL, exact_quadrature
+    from my_swampe_gb300 import run_model_scan, run_model_scan_final
+
+    kw = dict(M=42, dt=30.0, Phibar=4.0e6, omega=3.2e-5, a=8.2e7, test=None, taurad=86400.0, taudrag=86400.0,
+              DPhieq=4.0e6, **_forced_single_ics())
+    g = run_model_scan(tmax=2 + 100, **kw)
+    with exact_quadrature():
+        r = o.run_model_scan(tmax=2 + 100, record=("Phi",), **kw)
+    assert int(g["dead_first_idx"]) == -1 and r["dead_first_idx"] == -1
+    for f in ("eta", "delta", "Phi", "U", "V"):
+        np.testing.assert_allclose(getattr(g["last_state"], f + "_curr").cpu().numpy(),
+                                   np.asarray(r["last_state"][f + "_curr"]), rtol=0, atol=ATOL[f], err_msg=f)
+    np.testing.assert_allclose(g["outs"]["Phi"].cpu().numpy(), np.asarray(r["outs"]["Phi"]), rtol=0, atol=ATOL["Phi"])
+    full = run_model_scan(tmax=2 + 28800, return_history=False, diagnostics=True, **kw)
+    last = full["last_state"]
+    assert not bool(last.dead)
+    for f in ("eta_curr", "delta_curr", "Phi_curr", "U_curr", "V_curr"):
+        assert bool(torch.isfinite(getattr(last, f)).all()), f
+    # Phi + Phibar relaxes towards Phieq in [Phibar, Phibar + DPhieq]
+    phi = last.Phi_curr
+    assert float(phi.min()) > -4.0e6 and float(phi.max()) < 2 * 4.0e6
+    fin = run_model_scan_final(tmax=2 + 28800, **kw)["last_state"]
+    assert torch.equal(fin.Phi_curr, last.Phi_curr)
+
+
+def test_fast_path_error_after_1440_steps(cuda):
+    """Forced ensemble (B=8, the benchmark's regime and parameter sampling),
+    1440 steps: the fast path (FP32 state, tensor-core Legendre kernels)
+    against the FP64 path.  Relative L2 bounds: Phi 1e-5 (the benchmark spec's
+    target), eta 1e-5, delta 5e-5 (the smallest field)."""
+    import torch
+    from my_swampe_gb300 import workloads
+    from my_swampe_gb300.engine import Engine, RunFlagsC
+
+    outs = {}
+    for prec in ("fp64", "fast"):
+        eng = Engine([(42, 8)], prec)
+        if prec == "fast":
+            assert eng.uses_tensor_cores
+        wl = workloads.forced_ensemble(eng, seed=1234)
+        workloads.apply_params(eng, 0, wl["params"])
+        flags = RunFlagsC()
+        eng.init_state([wl["ics"]], flags)
+        eng.forward(flags, t0=2, nsteps=1440)
+        eng.check_device_status()
+        outs[prec] = eng.output_physical(flags)[0].double()
+    for k, name, tol in ((0, "eta", 1e-5), (1, "delta", 5e-5), (2, "Phi", 1e-5)):
+        ref = outs["fp64"][k]
+        rel = float(torch.linalg.vector_norm(outs["fast"][k] - ref) / torch.linalg.vector_norm(ref))
+        assert rel <= tol, (name, rel)
+
+
+def _m63_losses(eng, wl, p, target, nsteps):
+    from my_swampe_gb300 import workloads
+    from my_swampe_gb300.engine import RunFlagsC
+
+    flags = RunFlagsC()
+    workloads.apply_params(eng, 0, p)
+    eng.init_state([wl["ics"].to(eng.rdtype)], flags)
+    eng.forward(flags, t0=2, nsteps=nsteps)
+    res = eng.output_physical(flags)[0][2].double()
+    return ((res - target) ** 2).mean(dim=(1, 2))  # per member (members are independent)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fast"])
+def test_M63_ensemble_of_32_gradients_2000_steps(cuda, precision):
+    """M=63 (96 x 192), B=32 forced, dt = 20 s, 2000 steps, checkpoints every
+    50: gradients of mean((Phi_T - Phi_target)^2) (target: a run at taurad x1.1,
+    DPhieq x0.9) in taurad, taudrag, DPhieq, Phibar against central differences
+    of the FP64 forward (h = 1e-6 relative) on members 0, 7, 19, 31.  FP64:
+    relative 1e-5; fast precision (FP32 state, its own adjoint): 1e-3."""
+    import torch
+    from my_swampe_gb300 import workloads
+    from my_swampe_gb300.adjoint import integrate
+    from my_swampe_gb300.engine import Engine, RunFlagsC
+
+    B, nsteps = 32, 2000
+    e64 = Engine([(63, B)], "fp64")
+    wl = workloads.forced_ensemble(e64, seed=63, dt=20.0)
+    p = dict(wl["params"])
+    p["Phibar"] = torch.full((B,), float(p["Phibar"]), dtype=torch.float64, device=e64.device)
+    p_tgt = dict(p, taurad=p["taurad"] * 1.1, DPhieq=p["DPhieq"] * 0.9)
+    target = None
+    flags = RunFlagsC()
+    workloads.apply_params(e64, 0, p_tgt)
+    e64.init_state([wl["ics"]], flags)
+    e64.forward(flags, t0=2, nsteps=nsteps)
+    target = e64.output_physical(flags)[0][2].clone()
+    eng = e64 if precision == "fp64" else Engine([(63, B)], "fast")
+    workloads.apply_params(eng, 0, p)
+    par = {k: p[k].clone().requires_grad_(True) for k in ("taurad", "taudrag", "DPhieq", "Phibar")}
+    ic = wl["ics"].to(eng.rdtype).clone().requires_grad_(True)
+    out = integrate(eng, flags, 2, nsteps, [par], [ic], ckpt_every=50, store="checkpoint")[0]
+    loss = torch.mean((out[2].double() - target) ** 2)
+    loss.backward()
+    members = [0, 7, 19, 31]
+    tol = 1e-5 if precision == "fp64" else 1e-3
+    for name in ("taurad", "taudrag", "DPhieq", "Phibar"):
+        h = 1e-6 * p[name].abs()
+        lp = _m63_losses(e64, wl, dict(p, **{name: p[name] + h}), target, nsteps)
+        lm = _m63_losses(e64, wl, dict(p, **{name: p[name] - h}), target, nsteps)
+        fd = ((lp - lm) / (2 * h) / B).cpu().numpy()
+        ad = par[name].grad.cpu().numpy()
+        np.testing.assert_allclose(ad[members], fd[members], rtol=tol, err_msg=f"{precision} {name}")
+    assert np.isfinite(ic.grad.cpu().numpy()).all()
+
+
+def test_mixed_truncations_1440_steps_fast_vs_fp64(cuda):
+    """64 members at M=42 (dt 30 s), 32 at M=63 (dt 20 s) and 8 at M=106
+    (dt 12 s), forced, parameters sampled per member, 1440 steps in one plan
+    (one launch per step kernel for all groups): the fast path against the FP64
+    path, relative L2 per group (bounds: Phi, eta 1e-5; delta 5e-5)."""
+    import torch
+    from my_swampe_gb300 import workloads
+    from my_swampe_gb300.engine import Engine, RunFlagsC
+
+    spec = [(42, 64, 30.0), (63, 32, 20.0), (106, 8, 12.0)]
+    outs = {}
+    for prec in ("fp64", "fast"):
+        eng = Engine([(M, B) for M, B, _ in spec], prec)
+        ics = []
+        for g, (M, B, dt) in enumerate(spec):
+            wl = workloads.forced_ensemble(eng, g=g, seed=500 + 1000 * g, dt=dt)
+            workloads.apply_params(eng, g, wl["params"])
+            ics.append(wl["ics"])
+        flags = RunFlagsC()
+        eng.init_state(ics, flags)
+        eng.forward(flags, t0=2, nsteps=1440)
+        eng.check_device_status()
+        outs[prec] = [o_.double() for o_ in eng.output_physical(flags)]
+    for g, (M, B, _) in enumerate(spec):
+        for k, name, tol in ((0, "eta", 1e-5), (1, "delta", 5e-5), (2, "Phi", 1e-5)):
+            ref = outs["fp64"][g][k]
+            rel = float(torch.linalg.vector_norm(outs["fast"][g][k] - ref) / torch.linalg.vector_norm(ref))
+            assert rel <= tol, (M, name, rel)

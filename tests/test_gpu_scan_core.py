@@ -95,10 +95,15 @@ def test_retrieval_call_sequence_equals_run_model_scan_final(cuda, precision):
     st = state0
     for t in t_seq:
         st = _step_once_state_only(st, t, static, flags, None, ics[3], ics[4])
+    # the curr fields come from the Fourier carries, which are reloaded exactly;
+    # the physical prev level is reloaded through an FFT round trip (round-off)
+    rel = 1e-12 if precision == "fp64" else 1e-6
     for f in FIELDS:
         assert torch.equal(getattr(st, f + "_curr"), getattr(last, f + "_curr")), f
         if f in ("eta", "delta", "Phi"):
-            torch.testing.assert_close(getattr(st, f + "_prev"), getattr(last, f + "_prev"), rtol=1e-12, atol=0)
+            want_prev = getattr(last, f + "_prev")
+            torch.testing.assert_close(getattr(st, f + "_prev"), want_prev, rtol=0,
+                                       atol=rel * float(want_prev.abs().max()))
 
 
 def test_fast_path_with_replaced_parameters_matches_oracle(cuda):
@@ -145,9 +150,10 @@ def test_chained_runs_equal_one_run(cuda, precision):
                            Vic=ics[4])
     for f in FIELDS:
         assert torch.equal(getattr(b, f + "_curr"), getattr(one, f + "_curr")), f
-    rtol = 1e-12 if precision == "fp64" else 1e-5
+    rel = 1e-12 if precision == "fp64" else 1e-6
     for f in ("eta", "delta", "Phi"):
-        torch.testing.assert_close(getattr(b, f + "_prev"), getattr(one, f + "_prev"), rtol=rtol, atol=rtol)
+        want_prev = getattr(one, f + "_prev")
+        torch.testing.assert_close(getattr(b, f + "_prev"), want_prev, rtol=0, atol=rel * float(want_prev.abs().max()))
     # simulate_scan keeps the history: its last row is the final curr field
     st, outs = simulate_scan(static=static, flags=_flags(diagnostics=True), state0=a, t_seq=range(7, 14), test=None,
                              Uic=ics[3], Vic=ics[4])
