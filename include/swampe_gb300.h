@@ -234,19 +234,23 @@ int swp_tc_selftest(const float* A, const float* B, float* D, int N, int K, int 
  * and clears the word. */
 int swp_device_status(swp_plan* plan, int* status, void* stream);
 
-/* 1 if the plan's modified-Euler steps run the tcgen05 Legendre kernel (FP32
- * plans whose groups are all M = 42, unless SWP_NO_TC=1 was set when the plan
- * was created), else 0.  No reference counterpart. */
+/* Which groups' modified-Euler steps run the tcgen05 Legendre kernels: bit g
+ * set for group g (so 1 or 0 for a one-group plan).  FP32 plans use them for
+ * the groups at M = 42 or 63, unless SWP_NO_TC=1 was set when the plan was
+ * created or the autotuner chose the SIMT kernel for the group.  No reference
+ * counterpart. */
 int swp_plan_uses_tensor_cores(const swp_plan* plan);
 
-/* Autotuner of the plan's tile shapes (no reference counterpart): for every
- * group, each member tile MT in {1, 2, 4, 8} (<= B) of the SIMT Legendre
- * kernels that fits in shared memory is timed -- nrep launches of the step's
- * Legendre kernel and of its adjoint on the caller's buffers st / adj, which
- * it overwrites (pass scratch copies) -- and the fastest is kept for the
- * plan's later calls (captured graphs are dropped).  chosen_mt[g] (may be
- * NULL) receives the choice.  The tensor-core kernels (FP32, M = 42) keep
- * their fixed tile of 8 members and are not affected. */
+/* Autotuner of the plan's Legendre kernels and tile shapes (no reference
+ * counterpart): for every group, the candidates are the tensor-core kernels
+ * (FP32 plans, M = 42 or 63: a fixed tile of 8 members) and each member tile
+ * MT in {1, 2, 4, 8} (<= B) of the SIMT kernels that fits in shared memory.
+ * Each is timed -- nrep launches of the step's Legendre kernel and of its
+ * adjoint on the caller's buffers st / adj, which it overwrites (pass scratch
+ * copies) -- and the fastest is kept for the plan's later calls (captured
+ * graphs are dropped).  chosen_mt[g] (may be NULL) receives the choice: 0 for
+ * the tensor-core kernels, else the SIMT tile (which the steps without a
+ * tensor-core form keep using either way). */
 int swp_plan_autotune(swp_plan* plan, const swp_group_state* st, const swp_group_adjoint* adj,
                       const swp_flags* flags, int nrep, int* chosen_mt, void* stream);
 
@@ -254,8 +258,10 @@ int swp_plan_autotune(swp_plan* plan, const swp_group_state* st, const swp_group
  * latitude rows per CTA of the grid step kernel. */
 int swp_plan_tiles(const swp_plan* plan, int g, int* mt, int* jb);
 
-/* Set the member tile of group g (1, 2, 4 or 8) -- e.g. a previously tuned
- * value; SWP_ERR_ARG if it does not fit in shared memory. */
+/* Set the Legendre kernel of group g -- e.g. a previously tuned choice: mt = 1,
+ * 2, 4 or 8 runs its modified-Euler steps on the SIMT kernels with that member
+ * tile (SWP_ERR_ARG if it does not fit in shared memory), mt = 0 on the
+ * tensor-core kernels (SWP_ERR_ARG if the group cannot run them). */
 int swp_plan_set_tile(swp_plan* plan, int g, int mt);
 
 /* Allocation-free swp_adjoint_step (no counterpart in the reference, which has

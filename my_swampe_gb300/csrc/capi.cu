@@ -27,8 +27,10 @@ struct swp_plan {
   size_t spec_smem = 0;
   size_t spec_adj_smem = 0;
   size_t grid_smem[NGRIDMODE] = {};
-  // tensor-core Legendre kernel of the FP32 step (every group at M = 42)
+  // tensor-core Legendre kernels of the FP32 step: tc[g] for the groups that
+  // run them (M = 42 or 63), use_tc if any group does
   bool use_tc = false;
+  bool tc[MAXG] = {};
   float* tcbasis[MAXG] = {};
   float* tcbasis_adj[MAXG] = {};
   void* coefmem[MAXG] = {};              // per-call coefficient tables (CoefTables) of each group
@@ -189,27 +191,67 @@ bool step_incremental(const swp_plan* p, const swp_flags* f, int t) {
   return p->precision == SWP_FAST && f->scheme == 0 && !f->raw_filter && t > f->t_start;
 }
 
+// Tensor-core launches of one step: one launch per truncation present (42, 63),
+// each over the groups of that truncation (the others get no CTAs).
+template <typename Launch>
+cudaError_t launch_tc_per_truncation(const swp_plan* p, const SpecLaunch<float>& LS, float* const* bases,
+                                     Launch launch) {
+  const int mt = spec_tc_members_per_cta();
+  for (int Mt : {42, 63}) {
+    SpecLaunch<float> LT = LS;
+    int acc = 0;
+    TcBasis tb;
+    memset(&tb, 0, sizeof(tb));
+    tb.wait_limit = p->tc_wait_limit;
+    bool any = false;
+    for (int g = 0; g < p->ng; ++g) {
+      if (p->M[g] != Mt || !p->tc[g]) LT.grp[g].B = 0;
+      LT.grp[g].MT = mt;
+      LT.grp[g].ntb = (LT.grp[g].B + mt - 1) / mt;
+      LT.prefix[g] = acc;
+      acc += (p->M[g] + 1) * LT.grp[g].ntb;
+      tb.p[g] = bases[g];
+      any = any || (p->M[g] == Mt && LT.grp[g].B > 0);
+    }
+    LT.prefix[p->ng] = acc;
+    if (!any) continue;
+    cudaError_t e = launch(Mt, LT, acc, tb);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// The SIMT launch of the groups that do not run the tensor-core kernels (the
+// others get no CTAs); returns the block count through nb.
+template <typename T>
+SpecLaunch<T> simt_only(const swp_plan* p, const SpecLaunch<T>& LS, int& nb) {
+  SpecLaunch<T> L = LS;
+  int acc = 0;
+  for (int g = 0; g < p->ng; ++g) {
+    if (p->tc[g]) L.grp[g].B = 0;
+    L.grp[g].ntb = (L.grp[g].B + L.grp[g].MT - 1) / L.grp[g].MT;
+    L.prefix[g] = acc;
+    acc += (p->M[g] + 1) * L.grp[g].ntb;
+  }
+  L.prefix[p->ng] = acc;
+  nb = acc;
+  return L;
+}
+
 // The Legendre kernel of a modified-Euler step: tcgen05 (3xTF32) on the FP32
 // path when the plan packed the tensor-core basis, the SIMT kernel otherwise.
 template <typename T>
 cudaError_t launch_step_spec(const swp_plan* p, const SpecLaunch<T>& LS, int nbs, cudaStream_t s) {
   if constexpr (std::is_same<T, float>::value) {
     if (p->use_tc && LS.mode == 0 && LS.cfg.scheme == 0) {
-      SpecLaunch<float> LT = LS;
-      const int mt = spec_tc_members_per_cta();
-      int acc = 0;
-      TcBasis tb;
-      memset(&tb, 0, sizeof(tb));
-      tb.wait_limit = p->tc_wait_limit;
-      for (int g = 0; g < p->ng; ++g) {
-        LT.grp[g].MT = mt;
-        LT.grp[g].ntb = (LT.grp[g].B + mt - 1) / mt;
-        LT.prefix[g] = acc;
-        acc += (p->M[g] + 1) * LT.grp[g].ntb;
-        tb.p[g] = p->tcbasis[g];
-      }
-      LT.prefix[p->ng] = acc;
-      return launch_spec_tc(LT, acc, tb, p->d_err, s);
+      cudaError_t e = launch_tc_per_truncation(p, LS, p->tcbasis, [&](int Mt, const SpecLaunch<float>& LT, int n,
+                                                                      const TcBasis& tb) {
+        return launch_spec_tc(Mt, LT, n, tb, p->d_err, s);
+      });
+      int nb = 0;
+      SpecLaunch<float> LR = simt_only(p, LS, nb);
+      if (e == cudaSuccess && nb > 0) e = launch_spec<T>(LR, nb, p->spec_smem, s);
+      return e;
     }
   }
   return launch_spec<T>(LS, nbs, p->spec_smem, s);
@@ -221,21 +263,14 @@ template <typename T>
 cudaError_t launch_step_spec_adj(const swp_plan* p, const SpecLaunch<T>& LS, int nbs, cudaStream_t s) {
   if constexpr (std::is_same<T, float>::value) {
     if (p->use_tc && LS.cfg.scheme == 0) {
-      SpecLaunch<float> LT = LS;
-      const int mt = spec_tc_members_per_cta();
-      int acc = 0;
-      TcBasis tb;
-      memset(&tb, 0, sizeof(tb));
-      tb.wait_limit = p->tc_wait_limit;
-      for (int g = 0; g < p->ng; ++g) {
-        LT.grp[g].MT = mt;
-        LT.grp[g].ntb = (LT.grp[g].B + mt - 1) / mt;
-        LT.prefix[g] = acc;
-        acc += (p->M[g] + 1) * LT.grp[g].ntb;
-        tb.p[g] = p->tcbasis_adj[g];
-      }
-      LT.prefix[p->ng] = acc;
-      return launch_spec_adj_tc(LT, acc, tb, p->d_err, s);
+      cudaError_t e = launch_tc_per_truncation(p, LS, p->tcbasis_adj, [&](int Mt, const SpecLaunch<float>& LT,
+                                                                          int n, const TcBasis& tb) {
+        return launch_spec_adj_tc(Mt, LT, n, tb, p->d_err, s);
+      });
+      int nb = 0;
+      SpecLaunch<float> LR = simt_only(p, LS, nb);
+      if (e == cudaSuccess && nb > 0) e = launch_spec_adj<T>(LR, nb, p->spec_adj_smem, s);
+      return e;
     }
   }
   return launch_spec_adj<T>(LS, nbs, p->spec_adj_smem, s);
@@ -349,6 +384,38 @@ template <typename T>
 int forward_impl(swp_plan* p, const swp_group_state* st, const swp_flags* f, int t0, int nsteps,
                  int row0, int write_prev_last, cudaStream_t s) {
   if (nsteps < 4) return forward_steps<T>(p, st, f, t0, nsteps, row0, write_prev_last, nullptr, s);
+  bool plain = true;  // no per-step rows (diagnostics, history)
+  for (int g = 0; g < p->ng; ++g) plain = plain && !st[g].diag && !st[g].hist;
+  constexpr int WIN = 128;
+  if (plain && nsteps > 2 * WIN) {
+    // A long run is a few step windows, each a captured graph.  From t_steady on
+    // every step launches the same kernels with the same arguments (the step
+    // index only selects the projected first step, the filter's start at t = 3
+    // and the semi-implicit lag initialisation), so one window graph serves the
+    // whole run instead of a graph of every step.
+    const int t_steady = std::max(3, f->t_start + 1);
+    const int head = std::min(nsteps, std::max(0, t_steady - t0));
+    int done = 0;
+    if (head > 0) {
+      if (int rc = forward_impl<T>(p, st, f, t0, head, row0, write_prev_last && head == nsteps, s)) return rc;
+      done = head;
+    }
+    while (done < nsteps) {
+      const int n = std::min(WIN, nsteps - done);
+      const int wpl = (write_prev_last && done + n == nsteps) ? 1 : 0;
+      const int tw = t0 + done;
+      std::vector<uint64_t> key = {5, (uint64_t)n, (uint64_t)wpl};
+      key_flags(key, f);
+      key_state(key, p, st);
+      int rc = n < 4 ? forward_steps<T>(p, st, f, tw, n, row0, wpl, nullptr, s)
+                     : run_graph(p, key, [&](cudaStream_t cs) {
+                         return forward_steps<T>(p, st, f, tw, n, row0, wpl, nullptr, cs);
+                       }, s);
+      if (rc) return rc;
+      done += n;
+    }
+    return SWP_OK;
+  }
   std::vector<uint64_t> key = {1, (uint64_t)t0, (uint64_t)nsteps, (uint64_t)row0, (uint64_t)write_prev_last};
   key_flags(key, f);
   key_state(key, p, st);
@@ -818,13 +885,22 @@ int autotune_impl(swp_plan* p, const swp_group_state* st, const swp_group_adjoin
   for (int g = 0; g < p->ng && rc == SWP_OK; ++g) {
     const int J = p->geom[g].J;
     const int keep = p->MT[g];
-    int best = keep;
+    const bool keep_tc = p->tc[g];
+    // candidates: the tensor-core kernels (0, where the plan packed their basis)
+    // and the SIMT member tiles 1, 2, 4, 8
+    const bool tc_able = p->tcbasis[g] != nullptr;
+    int best = keep, best_mt = keep;
     float best_ms = 3.4e38f;
-    for (int mt = 1; mt <= 8 && mt <= std::max(1, p->B[g]); mt *= 2) {
-      size_t ss = f64 ? spec_smem_bytes<double>(p->M[g], J, mt) : spec_smem_bytes<float>(p->M[g], J, mt);
-      size_t sa = f64 ? spec_adj_smem_bytes<double>(p->M[g], J, mt) : spec_adj_smem_bytes<float>(p->M[g], J, mt);
-      if (ss > 227 * 1024 || sa > 227 * 1024) continue;
-      p->MT[g] = mt;
+    for (int mt = tc_able ? 0 : 1; mt <= 8 && mt <= std::max(1, p->B[g]); mt = mt ? 2 * mt : 1) {
+      if (mt > 0) {
+        size_t ss = f64 ? spec_smem_bytes<double>(p->M[g], J, mt) : spec_smem_bytes<float>(p->M[g], J, mt);
+        size_t sa = f64 ? spec_adj_smem_bytes<double>(p->M[g], J, mt) : spec_adj_smem_bytes<float>(p->M[g], J, mt);
+        if (ss > 227 * 1024 || sa > 227 * 1024) continue;
+        p->MT[g] = mt;
+      }
+      p->tc[g] = mt == 0;
+      p->use_tc = false;
+      for (int q = 0; q < p->ng; ++q) p->use_tc = p->use_tc || p->tc[q];
       refresh_spec_smem(p);
       int nbs = 0;
       SpecLaunch<T> LS = make_spec<T>(p, st, nbs);
@@ -842,19 +918,28 @@ int autotune_impl(swp_plan* p, const swp_group_state* st, const swp_group_adjoin
       cudaError_t e = cudaSuccess;
       for (int r = 0; r < nrep + 1 && e == cudaSuccess; ++r) {  // the first repetition warms up
         if (r == 1) cudaEventRecord(e0, s);
-        e = launch_spec<T>(LS, nbs, p->spec_smem, s);
-        if (e == cudaSuccess) e = launch_spec_adj<T>(LA, nbs, p->spec_adj_smem, s);
+        e = launch_step_spec<T>(p, LS, nbs, s);
+        if (e == cudaSuccess) e = launch_step_spec_adj<T>(p, LA, nbs, s);
       }
       cudaEventRecord(e1, s);
       if (e == cudaSuccess) e = cudaEventSynchronize(e1);
       float ms = 0.f;
       if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
       if (e != cudaSuccess) { rc = cuda_check(p, e, "autotune launch"); break; }
-      if (ms < best_ms) { best_ms = ms; best = mt; }
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = mt;
+        if (mt > 0) best_mt = mt;
+      }
     }
-    p->MT[g] = rc == SWP_OK ? best : keep;
-    if (chosen) chosen[g] = p->MT[g];
+    // the SIMT tile stays set for the kernels without a tensor-core form
+    // (tangent, explicit and semi-implicit steps)
+    p->tc[g] = rc == SWP_OK ? best == 0 : keep_tc;
+    p->MT[g] = rc == SWP_OK ? (best > 0 ? best : (best_mt > 0 ? best_mt : keep)) : keep;
+    if (chosen) chosen[g] = p->tc[g] ? 0 : p->MT[g];
   }
+  p->use_tc = false;
+  for (int q = 0; q < p->ng; ++q) p->use_tc = p->use_tc || p->tc[q];
   refresh_spec_smem(p);
   clear_graphs(p);  // captured graphs hold the old launch shapes
   cudaEventDestroy(e0);
@@ -978,15 +1063,20 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
       p->grid_smem[mode] = std::max(p->grid_smem[mode], gs);
     }
   }
-  // tensor-core step kernel: FP32 plans whose groups are all M = 42, unless SWP_NO_TC=1
+  // tensor-core step kernels: FP32 plans whose groups are all M = 42 or 63, unless SWP_NO_TC=1
   const char* tc_env = getenv("SWP_NO_TC");
-  bool tc = precision == SWP_FAST && !(tc_env && tc_env[0] == '1');
-  for (int g = 0; g < ngroups; ++g) tc = tc && spec_tc_supported(M[g]);
+  const bool tc_on = precision == SWP_FAST && !(tc_env && tc_env[0] == '1');
+  bool tc = false;
+  for (int g = 0; g < ngroups; ++g) {
+    p->tc[g] = tc_on && spec_tc_supported(M[g]);
+    tc = tc || p->tc[g];
+  }
   if (tc) {
     for (int g = 0; g < ngroups; ++g) {
-      if (cudaMalloc(&p->tcbasis[g], spec_tc_basis_floats() * sizeof(float)) != cudaSuccess ||
+      if (!p->tc[g]) continue;
+      if (cudaMalloc(&p->tcbasis[g], spec_tc_basis_floats(M[g]) * sizeof(float)) != cudaSuccess ||
           pack_tc_basis(p->geom[g], p->tcbasis[g], s) != SWP_OK ||
-          cudaMalloc(&p->tcbasis_adj[g], spec_tc_basis_floats() * sizeof(float)) != cudaSuccess ||
+          cudaMalloc(&p->tcbasis_adj[g], spec_tc_basis_floats(M[g]) * sizeof(float)) != cudaSuccess ||
           pack_tc_basis_adj(p->geom[g], p->tcbasis_adj[g], s) != SWP_OK) {
         p->err = "tensor-core basis packing failed";
         *out = p;
@@ -1038,7 +1128,12 @@ int swp_device_status(swp_plan* p, int* status, void* stream) {
   return SWP_OK;
 }
 
-int swp_plan_uses_tensor_cores(const swp_plan* p) { return p && p->use_tc ? 1 : 0; }
+int swp_plan_uses_tensor_cores(const swp_plan* p) {
+  int mask = 0;
+  if (p)
+    for (int g = 0; g < p->ng; ++g) mask |= p->tc[g] ? (1 << g) : 0;
+  return mask;
+}
 
 int swp_plan_dims(const swp_plan* p, int g, int* M, int* J, int* I, int* B) {
   if (!p || g < 0 || g >= p->ng) return SWP_ERR_ARG;
@@ -1279,11 +1374,21 @@ int swp_plan_set_tile(swp_plan* p, int g, int mt) {
   if (!p || g < 0 || g >= p->ng) return SWP_ERR_ARG;
   const bool f64 = p->precision == SWP_FP64;
   const int J = p->geom[g].J;
-  if (mt < 1 || mt > 8 || (mt & (mt - 1)) != 0) return fail(p, SWP_ERR_ARG, "member tile must be 1, 2, 4 or 8");
+  if (mt == 0) {  // the tensor-core kernels
+    if (!p->tcbasis[g]) return fail(p, SWP_ERR_ARG, "this group cannot run the tensor-core kernels");
+    if (!p->tc[g]) clear_graphs(p);
+    p->tc[g] = true;
+    p->use_tc = true;
+    return SWP_OK;
+  }
+  if (mt < 1 || mt > 8 || (mt & (mt - 1)) != 0) return fail(p, SWP_ERR_ARG, "member tile must be 0, 1, 2, 4 or 8");
   size_t ss = f64 ? spec_smem_bytes<double>(p->M[g], J, mt) : spec_smem_bytes<float>(p->M[g], J, mt);
   size_t sa = f64 ? spec_adj_smem_bytes<double>(p->M[g], J, mt) : spec_adj_smem_bytes<float>(p->M[g], J, mt);
   if (ss > 227 * 1024 || sa > 227 * 1024) return fail(p, SWP_ERR_ARG, "member tile does not fit in shared memory");
   p->MT[g] = mt;
+  p->tc[g] = false;
+  p->use_tc = false;
+  for (int q = 0; q < p->ng; ++q) p->use_tc = p->use_tc || p->tc[q];
   refresh_spec_smem(p);
   clear_graphs(p);
   return SWP_OK;

@@ -219,23 +219,24 @@ void spec_set_attributes();
 void grid_set_attributes();
 int grid_rows_per_cta(int M, bool fp64, int mode);  // JB the grid kernel is compiled for
 
-// tensor-core Legendre kernel of the FP32 modified-Euler step (tc_legendre.cu)
+// tensor-core Legendre kernels of the FP32 modified-Euler step (tc_legendre.cu), M = 42 and 63
 // packed basis of each group, and the poll limit of the kernels' mbarrier waits
 struct TcBasis {
   const float* p[MAXG];
   uint32_t wait_limit;
 };
 constexpr uint32_t TC_WAIT_LIMIT_DEFAULT = SWP_WAIT_LIMIT_DEFAULT;
-size_t spec_tc_smem_bytes();
-size_t spec_tc_basis_floats();
+size_t spec_tc_smem_bytes(int M);
+size_t spec_tc_basis_floats(int M);
 int spec_tc_members_per_cta();
 bool spec_tc_supported(int M);
 int pack_tc_basis(const GroupGeom& gg, float* out, cudaStream_t s);
 void spec_tc_set_attributes();
-cudaError_t launch_spec_tc(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err, cudaStream_t s);
+cudaError_t launch_spec_tc(int M, const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
+                           cudaStream_t s);
 int pack_tc_basis_adj(const GroupGeom& gg, float* out, cudaStream_t s);
-size_t spec_tc_adj_smem_bytes();
-cudaError_t launch_spec_adj_tc(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
+size_t spec_tc_adj_smem_bytes(int M);
+cudaError_t launch_spec_adj_tc(int M, const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
                                cudaStream_t s);
 
 }  // namespace swp

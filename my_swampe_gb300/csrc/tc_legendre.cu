@@ -1,5 +1,8 @@
 // Tensor-core (tcgen05) Legendre sandwich of one modified-Euler step, FP32
-// fast path, truncation M = 42 (64 x 128 Gauss grid).
+// fast path, compiled per truncation: M = 42 (64 x 128 Gauss grid, two CTAs
+// per SM) and M = 63 (96 x 192, one CTA per SM).  The shapes below are those
+// of M = 42; TcShape<M, J> gives them for any truncation whose operands fit in
+// shared memory.
 //
 // Same per-m decomposition and arithmetic as k_spectral (spectral.cu), with the
 // two contractions issued as kind::tf32 MMAs in 3xTF32 split precision
@@ -7,13 +10,13 @@
 //   GEMM1, forward Legendre, once per parity of n - m:
 //     D1[row, c] = sum_k A1[row, k] B1[c, k]
 //     row = group g (8) x member (8) x re/im (2) = 128,
-//     k = [Pw at j' (32) | Hw at j' (32)], c -> n = m + par + 2c (N = 32)
+//     k = [Pw at j' (J/2) | Hw at j' (J/2)], c -> n = m + par + 2c (N = 32)
 //   epilogue in shared memory: n(n+1), hyperdiffusion, the incremental form,
 //     wind-inversion inputs (spectral_transform.py:577-594, filters.py:95-151)
 //   GEMM2, inverse Legendre, once per parity:
 //     D2[row, col] = sum_c A2[row, c] B2[col, c]
 //     row = input q (7) x member (8) x re/im (2) = 112 (of the 128 MMA rows),
-//     col = [P at j' (32) | H at j' (32)]
+//     col = [P at j' (J/2) | H at j' (J/2)]
 // The forward groups are the combined inputs of step_combos paired as
 //   g0 (PhiP1 | PhiH1)  g1 (PhiP2 | 0)  g2 (dP1 | dH1)  g3 (dP2 | dH2)
 //   g4 (eP1 | eH1)      g5..g7 (curr Phi, delta, eta | 0)
@@ -29,34 +32,63 @@
 namespace swp {
 
 namespace {
-constexpr int TC_M = 42, TC_J = 64, TC_JH = 32;
-constexpr int TC_MT = 8;                           // members per CTA
-constexpr int TC_CNT = TC_M + 1;                   // n = m..M, at most 43
-constexpr int TC_ROWS = 128;                       // MMA M
-constexpr int TC_K1 = 2 * TC_JH;                   // 64
-constexpr int TC_N1 = 32;                          // >= ceil(43 / 2), multiple of 16
-constexpr int TC_R2 = 112;                         // used rows of GEMM2
-constexpr int TC_K2 = 24;                          // >= ceil(43 / 2), multiple of 8
-constexpr int TC_N2 = 2 * TC_JH;                   // 64
-constexpr int TC_B1 = 4 * TC_N1 * TC_K1;           // [par][hi, lo][N1][K1] = 8192 floats
-constexpr int TC_B2 = 4 * TC_N2 * TC_K2;           // [par][hi, lo][N2][K2] = 6144 floats
-constexpr int TC_BLOCK = TC_B1 + TC_B2;            // packed basis floats per m
-constexpr int TC_A = 2 * TC_ROWS * TC_K1;          // A region: 16384 floats (64 KB)
-constexpr int TC_A2 = TC_R2 * TC_K2;               // one A2 operand (2688 floats)
-constexpr int TC_RES0 = 4 * TC_A2;                 // D1 staging inside the A region
-constexpr int TC_RES = 8 * TC_CNT * 16;            // [g][n-m][member, re/im]
-constexpr int TC_OST = 2 * TC_J + 2;               // output staging row stride (floats)
-constexpr int TC_NOUT = 7;                         // eta, delta, Phi, Uprep, Vprep | U_H, V_H
-constexpr int TC_COEF = 5 * TC_MT * TC_CNT;
-constexpr int TC_TMEM_COLS = 256;                  // D1: 2 x (2 x 32), D2: 2 x 64 (D2 reuses D1's columns)
-static_assert(TC_RES0 + TC_RES <= TC_A, "D1 staging must fit in the A region");
-static_assert(TC_NOUT * TC_MT * TC_OST <= TC_A, "output staging must fit in the A region");
-// the MMA reads all 128 rows of the last A2 operand: they must stay in the A region
-static_assert(3 * TC_A2 + TC_ROWS * TC_K2 <= TC_A, "A2 over-read must stay in the A region");
-static_assert(TC_B2 <= TC_B1, "B2 reuses the B1 buffer");
-// inputs of a modified-Euler step, staged by bulk copies at the start of the A region
-constexpr int TC_NIN = 11;
-static_assert(TC_NIN * TC_MT * TC_J * 2 <= TC_A, "staged inputs must fit in the A region");
+// Operand shapes of truncation M on J Gauss latitudes.
+template <int M_, int J_>
+struct TcShape {
+  static constexpr int M = M_, J = J_, JH = J_ / 2;
+  static constexpr int MT = 8;                         // members per CTA
+  static constexpr int CNT = M + 1;                    // n = m..M
+  static constexpr int HALF = (CNT + 1) / 2;           // n of one parity, at most
+  static constexpr int ROWS = 128;                     // MMA M
+  static constexpr int K1 = 2 * JH;
+  static constexpr int N1 = (HALF + 15) / 16 * 16;     // multiple of 16
+  static constexpr int R2 = 112;                       // used rows of GEMM2
+  static constexpr int K2 = (HALF + 7) / 8 * 8;        // multiple of 8
+  static constexpr int N2 = 2 * JH;
+  static constexpr int B1 = 4 * N1 * K1;               // [par][hi, lo][N1][K1]
+  static constexpr int B2 = 4 * N2 * K2;               // [par][hi, lo][N2][K2]
+  static constexpr int BLOCK = B1 + B2;                // packed basis floats per m
+  static constexpr int A = 2 * ROWS * K1;              // A region
+  static constexpr int A2 = R2 * K2;                   // one A2 operand
+  static constexpr int RES0 = 4 * A2;                  // D1 staging inside the A region
+  static constexpr int RES = 8 * CNT * 16;             // [g][n-m][member, re/im]
+  static constexpr int OST = 2 * J + 2;                // output staging row stride (floats)
+  static constexpr int NOUT = 7;                       // eta, delta, Phi, Uprep, Vprep | U_H, V_H
+  static constexpr int COEF = 5 * MT * CNT;
+  static constexpr int TMEM_COLS = 256;                // D1: 2 x (2 x N1), D2: 2 x N2 (reusing D1's columns)
+  static constexpr int NIN = 11;                       // staged inputs of a modified-Euler step
+  // (member, j') pairs of the combination: warp tasks of 4 members x 8 j'
+  static constexpr int NTASK = (MT / 4) * (JH / 8);
+  static constexpr int NPAIR = (NTASK + 7) / 8;        // per thread
+  // write-out latitude pairs (16-byte accesses) per thread
+  static constexpr int NWPAIR = (MT * J / 2 + 255) / 256;
+  // adjoint
+  static constexpr int ANIN = 5;                       // staged lambda of eta, delta, Phi, U, V
+  static constexpr int AA2 = ROWS * K2;                // one A2' operand: 128 rows
+  static constexpr int ARES0 = 4 * AA2;
+  static constexpr int ARES = 7 * CNT * 16;
+  static constexpr int ANOUT = 12;                     // 8 P slots + 4 H slots
+  static constexpr int AA = ARES0 + ARES > A ? ARES0 + ARES : A;
+  static constexpr int MINB = 2 * (A + B1 + COEF) * 4 + 512 <= 227 * 1024 ? 2 : 1;  // CTAs per SM
+
+  static_assert(JH % 16 == 0 && MT % 4 == 0, "latitude blocks of 16, member blocks of 4");
+  static_assert(RES0 + RES <= A, "D1 staging must fit in the A region");
+  static_assert(NOUT * MT * OST <= A, "output staging must fit in the A region");
+  // the MMA reads all 128 rows of the last A2 operand: they must stay in the A region
+  static_assert(3 * A2 + ROWS * K2 <= A, "A2 over-read must stay in the A region");
+  static_assert(B2 <= B1, "B2 reuses the B1 buffer");
+  static_assert(NIN * MT * J * 2 <= A, "staged inputs must fit in the A region");
+  static_assert(4 * N1 <= TMEM_COLS && 2 * N1 + 2 * N2 <= TMEM_COLS, "TMEM columns");
+  static_assert(N1 <= 128 && N2 <= 256 && N2 % 16 == 0, "MMA N");
+  // the hi tile of a [hi, lo][N][K] operand pair is followed by its lo tile at (N / 8) stride offsets
+  static_assert(N1 * K1 * 4 == (N1 / 8) * (K1 / 4) * 128, "B1 lo tile must follow its hi tile");
+  static_assert(ANOUT * MT * OST <= AA, "adjoint output staging must fit in the A region");
+  static_assert(ANIN * MT * J * 2 <= AA, "staged lambda must fit in the A region");
+  static_assert(MT * J / 2 <= B1, "the adjoint's Phibar terms reuse the B buffer");
+};
+typedef TcShape<42, 64> Tc42;
+typedef TcShape<63, 96> Tc63;
+
 __host__ __device__ constexpr int stage_field(int q) {  // staged slot -> Fourier field
   return q == 0 ? F_ETA : q == 1 ? F_DELTA : q == 2 ? F_PHI : F_A + (q - 3);
 }
@@ -65,7 +97,7 @@ __host__ __device__ constexpr int stage_field(int q) {  // staged slot -> Fourie
 __host__ __device__ constexpr int stage_slot(int f) {
   return f == F_ETA ? 0 : f == F_DELTA ? 1 : f == F_PHI ? 2 : (f >= F_A && f <= F_G) ? f - F_A + 3 : 0;
 }
-static_assert(F_G - F_A + 4 == TC_NIN, "staged fields");
+static_assert(F_G - F_A + 4 == 11, "staged fields");
 
 // slots of forward group g (compile-time, so that the slot arrays stay in registers)
 __host__ __device__ constexpr int group_p(int g) {
@@ -75,60 +107,77 @@ __host__ __device__ constexpr int group_p(int g) {
 __host__ __device__ constexpr int group_h(int g) {
   return g == 0 ? SH_PHI1 : g == 2 ? SH_D1 : g == 3 ? SH_D2 : g == 4 ? SH_E1 : -1;
 }
+
+template <typename F>
+auto tc_dispatch(int M, F f) -> decltype(f(Tc42())) {
+  return M == 63 ? f(Tc63()) : f(Tc42());
+}
 }  // namespace
 
-size_t spec_tc_smem_bytes() { return (size_t)(TC_A + TC_B1 + TC_COEF) * sizeof(float) + 256; }
-size_t spec_tc_basis_floats() { return (size_t)TC_CNT * TC_BLOCK; }
-int spec_tc_members_per_cta() { return TC_MT; }
-bool spec_tc_supported(int M) { return M == TC_M; }
+size_t spec_tc_smem_bytes(int M) {
+  return tc_dispatch(M, [](auto S) { return (size_t)(S.A + S.B1 + S.COEF) * sizeof(float) + 256; });
+}
+size_t spec_tc_basis_floats(int M) { return tc_dispatch(M, [](auto S) { return (size_t)S.CNT * S.BLOCK; }); }
+int spec_tc_members_per_cta() { return 8; }
+bool spec_tc_supported(int M) { return M == 42 || M == 63; }
 
-// Pack the FP64 basis of M = 42 into the per-m GEMM operand blocks.
+// Pack the FP64 basis into the per-m GEMM operand blocks of shape S.
+template <class S>
 __global__ void k_pack_tc_basis(const double* __restrict__ Pw_f, const double* __restrict__ Hw_f,
                                 const double* __restrict__ P_i, const double* __restrict__ H_i,
                                 const int* __restrict__ boff, float* __restrict__ out) {
   const int m = blockIdx.x;
-  const int cnt = TC_CNT - m, C0 = (cnt + 1) / 2, C1 = cnt / 2;
-  float* blk = out + (size_t)m * TC_BLOCK;
-  for (int i = threadIdx.x; i < TC_BLOCK; i += blockDim.x) blk[i] = 0.f;
+  const int cnt = S::CNT - m, C0 = (cnt + 1) / 2, C1 = cnt / 2;
+  float* blk = out + (size_t)m * S::BLOCK;
+  for (int i = threadIdx.x; i < S::BLOCK; i += blockDim.x) blk[i] = 0.f;
   __syncthreads();
   const int base = boff[m];
   for (int par = 0; par < 2; ++par) {
     const int Cp = par ? C1 : C0;
-    const int poff = par ? TC_JH * C0 : 0;
-    float* b1h = blk + (size_t)(2 * par) * TC_N1 * TC_K1;
-    float* b1l = b1h + TC_N1 * TC_K1;
-    float* b2h = blk + TC_B1 + (size_t)(2 * par) * TC_N2 * TC_K2;
-    float* b2l = b2h + TC_N2 * TC_K2;
-    for (int i = threadIdx.x; i < Cp * TC_K1; i += blockDim.x) {
-      const int c = i / TC_K1, k = i % TC_K1, jp = k % TC_JH;
-      const double v = (k < TC_JH) ? Pw_f[base + poff + jp * Cp + c] : Hw_f[base + poff + jp * Cp + c];
+    const int poff = par ? S::JH * C0 : 0;
+    float* b1h = blk + (size_t)(2 * par) * S::N1 * S::K1;
+    float* b1l = b1h + S::N1 * S::K1;
+    float* b2h = blk + S::B1 + (size_t)(2 * par) * S::N2 * S::K2;
+    float* b2l = b2h + S::N2 * S::K2;
+    for (int i = threadIdx.x; i < Cp * S::K1; i += blockDim.x) {
+      const int c = i / S::K1, k = i % S::K1, jp = k % S::JH;
+      const double v = (k < S::JH) ? Pw_f[base + poff + jp * Cp + c] : Hw_f[base + poff + jp * Cp + c];
       const float hi = tc::to_tf32((float)v);
-      b1h[tc::cm_index(c, k, TC_K1)] = hi;
-      b1l[tc::cm_index(c, k, TC_K1)] = tc::to_tf32((float)(v - (double)hi));
+      b1h[tc::cm_index(c, k, S::K1)] = hi;
+      b1l[tc::cm_index(c, k, S::K1)] = tc::to_tf32((float)(v - (double)hi));
     }
-    for (int i = threadIdx.x; i < TC_N2 * Cp; i += blockDim.x) {
-      const int col = i / Cp, c = i % Cp, jp = col % TC_JH;
-      const double v = (col < TC_JH) ? P_i[base + poff + c * TC_JH + jp] : H_i[base + poff + c * TC_JH + jp];
+    for (int i = threadIdx.x; i < S::N2 * Cp; i += blockDim.x) {
+      const int col = i / Cp, c = i % Cp, jp = col % S::JH;
+      const double v = (col < S::JH) ? P_i[base + poff + c * S::JH + jp] : H_i[base + poff + c * S::JH + jp];
       const float hi = tc::to_tf32((float)v);
-      b2h[tc::cm_index(col, c, TC_K2)] = hi;
-      b2l[tc::cm_index(col, c, TC_K2)] = tc::to_tf32((float)(v - (double)hi));
+      b2h[tc::cm_index(col, c, S::K2)] = hi;
+      b2l[tc::cm_index(col, c, S::K2)] = tc::to_tf32((float)(v - (double)hi));
     }
   }
 }
 
+namespace {
+int pack_basis(const GroupGeom& gg, const double* f1, const double* f2, const double* i1, const double* i2,
+               float* out, cudaStream_t s) {
+  if (!spec_tc_supported(gg.M)) return SWP_ERR_ARG;
+  return tc_dispatch(gg.M, [&](auto S) {
+    typedef decltype(S) Sh;
+    if (gg.J != Sh::J) return SWP_ERR_ARG;
+    k_pack_tc_basis<Sh><<<Sh::CNT, 256, 0, s>>>(f1, f2, i1, i2, gg.boff, out);
+    return cudaGetLastError() == cudaSuccess ? SWP_OK : SWP_ERR_CUDA;
+  });
+}
+}  // namespace
+
 int pack_tc_basis(const GroupGeom& gg, float* out, cudaStream_t s) {
-  if (gg.M != TC_M || gg.J != TC_J) return SWP_ERR_ARG;
-  k_pack_tc_basis<<<TC_CNT, 256, 0, s>>>(gg.b64[B_PW_F], gg.b64[B_HW_F], gg.b64[B_P_I], gg.b64[B_H_I], gg.boff, out);
-  return cudaGetLastError() == cudaSuccess ? SWP_OK : SWP_ERR_CUDA;
+  return pack_basis(gg, gg.b64[B_PW_F], gg.b64[B_HW_F], gg.b64[B_P_I], gg.b64[B_H_I], out, s);
 }
 
 // The adjoint's operand blocks: GEMM1' contracts with the unweighted basis in
 // the forward layout (transposed inverse Legendre), GEMM2' with the weighted
 // basis in the inverse layout (transposed forward Legendre).
 int pack_tc_basis_adj(const GroupGeom& gg, float* out, cudaStream_t s) {
-  if (gg.M != TC_M || gg.J != TC_J) return SWP_ERR_ARG;
-  k_pack_tc_basis<<<TC_CNT, 256, 0, s>>>(gg.b64[B_P_F], gg.b64[B_H_F], gg.b64[B_PW_I], gg.b64[B_HW_I], gg.boff, out);
-  return cudaGetLastError() == cudaSuccess ? SWP_OK : SWP_ERR_CUDA;
+  return pack_basis(gg, gg.b64[B_P_F], gg.b64[B_H_F], gg.b64[B_PW_I], gg.b64[B_HW_I], out, s);
 }
 
 namespace {
@@ -159,16 +208,16 @@ __device__ __forceinline__ void mma_3xtf32_2(uint32_t d_tmem, uint32_t aH, uint3
                  1);
   }
 }
-// the hi tile of a [hi, lo][N][K] operand pair is followed by its lo tile at (N / 8) stride offsets
-static_assert(TC_N1 * TC_K1 * 4 == (TC_N1 / 8) * (TC_K1 / 4) * 128, "B1 lo tile must follow its hi tile");
 }  // namespace
 
-__global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ SpecLaunch<float> L,
-                                                        const __grid_constant__ TcBasis basis, int* err) {
+template <class S>
+__global__ void __launch_bounds__(256, S::MINB) k_spectral_tc(const __grid_constant__ SpecLaunch<float> L,
+                                                              const __grid_constant__ TcBasis basis, int* err) {
   typedef float T;
   typedef float2 T2;
   constexpr int NSPX = SlotCount<float>::NP;
   constexpr int NSLOT = NSPX + NSH;
+  constexpr int MT = S::MT, J = S::J, JH = S::JH, CNT = S::CNT;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   int idx;
   const SpecGroup<T>& G = pick_group(L, idx);
@@ -176,12 +225,11 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   while (gi + 1 < L.ng && (int)blockIdx.x >= L.prefix[gi + 1]) ++gi;
   const float* gbasis = basis.p[gi];
   const StepCfg& cfg = L.cfg;
-  const int J = TC_J;
   const int m = idx / G.ntb;
-  const int b0 = (idx % G.ntb) * TC_MT;
-  const int mt = min(TC_MT, G.B - b0);
-  const int cnt = TC_CNT - m, C0 = (cnt + 1) / 2, C1 = cnt / 2;
-  const size_t FS = (size_t)TC_CNT * G.B * J;
+  const int b0 = (idx % G.ntb) * MT;
+  const int mt = min(MT, G.B - b0);
+  const int cnt = CNT - m, C0 = (cnt + 1) / 2, C1 = cnt / 2;
+  const size_t FS = (size_t)CNT * G.B * J;
   const bool incr = cfg.incremental != 0;
   if (cfg.scheme != 0 || L.mode != 0) {  // the host launches this kernel for modified-Euler steps only
     if (threadIdx.x == 0) atomicExch(err, 2);
@@ -189,15 +237,15 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   }
 
   float* sA = (float*)smem_raw;            // staged inputs | A1 | A2 + D1 staging | output staging
-  float* sB = sA + TC_A;                   // B1, then B2
-  float* sRes = sA + TC_RES0;
-  float* sig = sB + TC_B1;                 // [MT][CNT] x 5
-  float* sigP = sig + TC_MT * TC_CNT;
-  float* sigm1 = sigP + TC_MT * TC_CNT;
-  float* sigPm1 = sigm1 + TC_MT * TC_CNT;
-  float* tcmn = sigPm1 + TC_MT * TC_CNT;
+  float* sB = sA + S::A;                   // B1, then B2
+  float* sRes = sA + S::RES0;
+  float* sig = sB + S::B1;                 // [MT][CNT] x 5
+  float* sigP = sig + MT * CNT;
+  float* sigm1 = sigP + MT * CNT;
+  float* sigPm1 = sigm1 + MT * CNT;
+  float* tcmn = sigPm1 + MT * CNT;
   // [4]: 0 basis copies, 1 GEMM1 commits, 2 GEMM2 commit, 3 input copies
-  uint64_t* mbar = (uint64_t*)(((uintptr_t)(tcmn + TC_MT * TC_CNT) + 15) & ~(uintptr_t)15);
+  uint64_t* mbar = (uint64_t*)(((uintptr_t)(tcmn + MT * CNT) + 15) & ~(uintptr_t)15);
   uint32_t* tslot = (uint32_t*)(mbar + 4);
   int* sflag = (int*)(tslot + 1);
   int* sdead = sflag + 1;                  // [MT]
@@ -214,24 +262,24 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     for (int q = 0; q < 4; ++q) tc::mbar_init(&mbar[q], 1);
     tc::fence_mbar_init();
     const uint32_t row_bytes = (uint32_t)(mt * J * sizeof(T2));
-    tc::mbar_expect_tx(&mbar[3], row_bytes * TC_NIN);
+    tc::mbar_expect_tx(&mbar[3], row_bytes * S::NIN);
 #pragma unroll
-    for (int q = 0; q < TC_NIN; ++q) {
+    for (int q = 0; q < S::NIN; ++q) {
       const int f = stage_field(q);
-      tc::bulk_g2s(sA + (size_t)q * TC_MT * J * 2, G.four + (size_t)f * FS + ((size_t)m * G.B + b0) * J, row_bytes,
+      tc::bulk_g2s(sA + (size_t)q * MT * J * 2, G.four + (size_t)f * FS + ((size_t)m * G.B + b0) * J, row_bytes,
                    &mbar[3]);
     }
     n_in = 1;
-    tc::mbar_expect_tx(&mbar[0], (uint32_t)(TC_B1 * sizeof(float)));
-    tc::bulk_g2s(sB, gbasis + (size_t)m * TC_BLOCK, (uint32_t)(TC_B1 * sizeof(float)), &mbar[0]);
+    tc::mbar_expect_tx(&mbar[0], (uint32_t)(S::B1 * sizeof(float)));
+    tc::bulk_g2s(sB, gbasis + (size_t)m * S::BLOCK, (uint32_t)(S::B1 * sizeof(float)), &mbar[0]);
     n_tma = 1;
   }
   if (warp == 0) {
-    tc::tmem_alloc(tslot, TC_TMEM_COLS);
+    tc::tmem_alloc(tslot, S::TMEM_COLS);
     tc::tmem_relinquish();
   }
-  load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, TC_MT, cnt, TC_CNT, sig, sigP, sigm1, sigPm1, tcmn);
-  if (threadIdx.x < TC_MT) {
+  load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, CNT, sig, sigP, sigm1, sigPm1, tcmn);
+  if (threadIdx.x < MT) {
     const int bt = threadIdx.x;
     int dead = 0;
     if (bt < mt && cfg.diagnostics) {
@@ -251,76 +299,103 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   const uint32_t tbase = *tslot;
 
   // ---- phase 1: combined, symmetrised inputs of (member, j') from the staged
-  // copy; a warp covers 4 members x 8 j'
-  const int jp = (warp & 3) * 8 + (lane & 7);
-  const int bt = (warp >> 2) * 4 + (lane >> 3);
-  T2 xs[NSLOT], xa[NSLOT];
+  // copy.  A warp task covers 4 members x 8 j'; thread k of a task takes member
+  // 4 mb + lane / 8 and latitude 8 jb + lane % 8.
+  int jp[S::NPAIR], bt[S::NPAIR];
+  bool has[S::NPAIR];
+#pragma unroll
+  for (int k = 0; k < S::NPAIR; ++k) {
+    const int task = warp + 8 * k;
+    has[k] = task < S::NTASK;
+    const int jb = has[k] ? task % (JH / 8) : 0, mb = has[k] ? task / (JH / 8) : 0;
+    jp[k] = jb * 8 + (lane & 7);
+    bt[k] = mb * 4 + (lane >> 3);
+  }
+  T2 xs[S::NPAIR][NSLOT], xa[S::NPAIR][NSLOT];
   // the combination's step factors at (member, j') and its mirror latitude,
   // loaded while the input copies are in flight
-  StepCoefs<T> kc0{}, kc1{};
-  if (bt < mt) {
-    kc0 = load_step_coefs<T>(G, b0 + bt, jp);
-    kc1 = kc0;
-    kc1.tsc = G.jco[(size_t)(b0 + bt) * J + (J - 1 - jp)];
+  StepCoefs<T> kc0[S::NPAIR], kc1[S::NPAIR];
+#pragma unroll
+  for (int k = 0; k < S::NPAIR; ++k) {
+    kc0[k] = StepCoefs<T>{};
+    kc1[k] = StepCoefs<T>{};
+    if (has[k] && bt[k] < mt) {
+      kc0[k] = load_step_coefs<T>(G, b0 + bt[k], jp[k]);
+      kc1[k] = kc0[k];
+      kc1[k].tsc = G.jco[(size_t)(b0 + bt[k]) * J + (J - 1 - jp[k])];
+    }
   }
   // write-out: thread -> member wbt, latitudes wj, wj + 1 (16-byte accesses)
-  static_assert(TC_MT * TC_J == 2 * 256, "one latitude pair per thread");
-  const int wbt = threadIdx.x / (TC_J / 2), wj = 2 * (threadIdx.x % (TC_J / 2));
-  T2 pold[3][2], pmid[3][2];  // its carries, loaded ahead of GEMM2
-  T wal = (T)0, wan = (T)0;   // its filter weights, loaded with them
+  int wbt[S::NWPAIR], wj[S::NWPAIR];
+#pragma unroll
+  for (int k = 0; k < S::NWPAIR; ++k) {
+    const int q = threadIdx.x + 256 * k;
+    wbt[k] = q < MT * J / 2 ? q / (J / 2) : MT;
+    wj[k] = 2 * (q % (J / 2));
+  }
+  T2 pold[S::NWPAIR][3][2], pmid[S::NWPAIR][3][2];  // its carries, loaded ahead of GEMM2
+  T wal[S::NWPAIR], wan[S::NWPAIR];                 // its filter weights, loaded with them
   // one thread waits on each mbarrier and the block barrier releases the rest:
   // 256 spinning threads would take issue slots from the co-resident CTA
   bool ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[3], 0, basis.wait_limit) : true;
   ok = __syncthreads_and(ok);
   if (ok) {
     const T2* stg = (const T2*)sA;
-    if (bt < mt) {
-      const int b = b0 + bt;
 #pragma unroll
-      for (int side = 0; side < 2; ++side) {
-        const int j = side ? (J - 1 - jp) : jp;
-        T2 c[NSLOT];
-        step_combos_ld<T>(G, cfg, 0, incr, m, b, j,
-                          [&](int f) { return stg[(stage_slot(f) * TC_MT + bt) * J + j]; }, c, side ? &kc1 : &kc0);
-        if (side == 0) {
+    for (int k = 0; k < S::NPAIR; ++k) {
+      if (has[k] && bt[k] < mt) {
+        const int b = b0 + bt[k];
 #pragma unroll
-          for (int q = 0; q < NSLOT; ++q) { xs[q] = c[q]; xa[q] = c[q]; }
-        } else {
+        for (int side = 0; side < 2; ++side) {
+          const int j = side ? (J - 1 - jp[k]) : jp[k];
+          T2 c[NSLOT];
+          step_combos_ld<T>(G, cfg, 0, incr, m, b, j,
+                            [&](int f) { return stg[(stage_slot(f) * MT + bt[k]) * J + j]; }, c,
+                            side ? &kc1[k] : &kc0[k]);
+          if (side == 0) {
 #pragma unroll
-          for (int q = 0; q < NSLOT; ++q) { xs[q] = cadd(xs[q], c[q]); xa[q] = csub(xa[q], c[q]); }
+            for (int q = 0; q < NSLOT; ++q) { xs[k][q] = c[q]; xa[k][q] = c[q]; }
+          } else {
+#pragma unroll
+            for (int q = 0; q < NSLOT; ++q) { xs[k][q] = cadd(xs[k][q], c[q]); xa[k][q] = csub(xa[k][q], c[q]); }
+          }
         }
-      }
-    } else {
+      } else {
 #pragma unroll
-      for (int q = 0; q < NSLOT; ++q) { xs[q] = mk<T2>(0, 0); xa[q] = xs[q]; }
+        for (int q = 0; q < NSLOT; ++q) { xs[k][q] = mk<T2>(0, 0); xa[k][q] = xs[k][q]; }
+      }
     }
   }
   // parity 0: P slots take the symmetric sum and H slots the antisymmetric one; parity 1 the reverse
   auto write_A1 = [&](int par) {
     float* aH = sA;
-    float* aL = sA + TC_ROWS * TC_K1;
+    float* aL = sA + S::ROWS * S::K1;
 #pragma unroll
-    for (int gq = 0; gq < 8; ++gq) {
-      const int sp = group_p(gq), sh = group_h(gq);
-      const T2 vp = par ? xa[sp] : xs[sp];
-      T2 vh = mk<T2>(0, 0);
-      if (sh >= 0) vh = par ? xs[NSPX + sh] : xa[NSPX + sh];
+    for (int k = 0; k < S::NPAIR; ++k) {
+      if (!has[k]) continue;
 #pragma unroll
-      for (int comp = 0; comp < 2; ++comp) {
-        const int row = gq * 16 + bt * 2 + comp;
-        float hi, lo;
-        tc::split_tf32(comp ? vp.y : vp.x, hi, lo);
-        aH[tc::cm_index(row, jp, TC_K1)] = hi;
-        aL[tc::cm_index(row, jp, TC_K1)] = lo;
-        tc::split_tf32(comp ? vh.y : vh.x, hi, lo);
-        aH[tc::cm_index(row, TC_JH + jp, TC_K1)] = hi;
-        aL[tc::cm_index(row, TC_JH + jp, TC_K1)] = lo;
+      for (int gq = 0; gq < 8; ++gq) {
+        const int sp = group_p(gq), sh = group_h(gq);
+        const T2 vp = par ? xa[k][sp] : xs[k][sp];
+        T2 vh = mk<T2>(0, 0);
+        if (sh >= 0) vh = par ? xs[k][NSPX + sh] : xa[k][NSPX + sh];
+#pragma unroll
+        for (int comp = 0; comp < 2; ++comp) {
+          const int row = gq * 16 + bt[k] * 2 + comp;
+          float hi, lo;
+          tc::split_tf32(comp ? vp.y : vp.x, hi, lo);
+          aH[tc::cm_index(row, jp[k], S::K1)] = hi;
+          aL[tc::cm_index(row, jp[k], S::K1)] = lo;
+          tc::split_tf32(comp ? vh.y : vh.x, hi, lo);
+          aH[tc::cm_index(row, JH + jp[k], S::K1)] = hi;
+          aL[tc::cm_index(row, JH + jp[k], S::K1)] = lo;
+        }
       }
     }
   };
-  const uint32_t idesc1 = tc::idesc_tf32(TC_ROWS, TC_N1), idesc1w = tc::idesc_tf32(TC_ROWS, 2 * TC_N1);
-  const uint32_t idesc2 = tc::idesc_tf32(TC_ROWS, TC_N2);
-  const uint32_t aHs = tc::smem_u32(sA), aLs = aHs + (uint32_t)(TC_ROWS * TC_K1 * 4);
+  const uint32_t idesc1 = tc::idesc_tf32(S::ROWS, S::N1), idesc1w = tc::idesc_tf32(S::ROWS, 2 * S::N1);
+  const uint32_t idesc2 = tc::idesc_tf32(S::ROWS, S::N2);
+  const uint32_t aHs = tc::smem_u32(sA), aLs = aHs + (uint32_t)(S::ROWS * S::K1 * 4);
   const uint32_t bbase = tc::smem_u32(sB);
 
   // ---- phase 2: GEMM1, parity 0 then parity 1 (the A buffer is refilled in between)
@@ -331,7 +406,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     __syncthreads();
     if (threadIdx.x == 0) {
       if (!tc::mbar_wait_bounded(&mbar[0], 0, basis.wait_limit)) *sflag = 1;
-      if (!*sflag) mma_3xtf32_2(tbase, aHs, aLs, bbase, TC_N1, TC_K1, idesc1w, idesc1);
+      if (!*sflag) mma_3xtf32_2(tbase, aHs, aLs, bbase, S::N1, S::K1, idesc1w, idesc1);
       tc::mma_commit(&mbar[1]);
       n_c1 = 1;
     }
@@ -345,8 +420,8 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     tc::fence_proxy_async();
     __syncthreads();
     if (threadIdx.x == 0) {
-      const uint32_t b1 = bbase + 2u * TC_N1 * TC_K1 * 4u;
-      mma_3xtf32_2(tbase + 2 * TC_N1, aHs, aLs, b1, TC_N1, TC_K1, idesc1w, idesc1);
+      const uint32_t b1 = bbase + 2u * S::N1 * S::K1 * 4u;
+      mma_3xtf32_2(tbase + 2 * S::N1, aHs, aLs, b1, S::N1, S::K1, idesc1w, idesc1);
       tc::mma_commit(&mbar[1]);
       n_c1 = 2;
     }
@@ -357,8 +432,8 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   if (ok) {
     // B1 is no longer read: fetch B2 into the same buffer, overlapped with the epilogue
     if (threadIdx.x == 0) {
-      tc::mbar_expect_tx(&mbar[0], (uint32_t)(TC_B2 * sizeof(float)));
-      tc::bulk_g2s(sB, gbasis + (size_t)m * TC_BLOCK + TC_B1, (uint32_t)(TC_B2 * sizeof(float)), &mbar[0]);
+      tc::mbar_expect_tx(&mbar[0], (uint32_t)(S::B2 * sizeof(float)));
+      tc::bulk_g2s(sB, gbasis + (size_t)m * S::BLOCK + S::B1, (uint32_t)(S::B2 * sizeof(float)), &mbar[0]);
       n_tma = 2;
     }
     // ---- phase 3: D1 -> staging sRes[g][n-m][member, re/im]; zero the A2 operands
@@ -368,41 +443,41 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       const int gq = row >> 4, btc = row & 15;
       const int Cp = par ? C1 : C0;
 #pragma unroll
-      for (int c0 = 0; c0 < TC_N1; c0 += 16) {
+      for (int c0 = 0; c0 < S::N1; c0 += 16) {
         float v[16], v1[16];
-        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(2 * par * TC_N1 + c0), v);
-        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((2 * par + 1) * TC_N1 + c0), v1);
+        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(2 * par * S::N1 + c0), v);
+        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((2 * par + 1) * S::N1 + c0), v1);
 #pragma unroll
         for (int i = 0; i < 16; ++i) v[i] += v1[i];
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           const int c = c0 + i;
-          if (c < Cp) sRes[(gq * TC_CNT + (par + 2 * c)) * 16 + btc] = v[i];
+          if (c < Cp) sRes[(gq * CNT + (par + 2 * c)) * 16 + btc] = v[i];
         }
       }
     }
-    for (int i = threadIdx.x; i < TC_RES0; i += blockDim.x) sA[i] = 0.f;
+    for (int i = threadIdx.x; i < S::RES0; i += blockDim.x) sA[i] = 0.f;
     tc::fence_before_sync();
     __syncthreads();
     // ---- phase 4: spectral epilogue -> A2 operands [par][hi, lo][112 rows][K2]
-    for (int t = threadIdx.x; t < TC_MT * cnt; t += blockDim.x) {
-      const int bti = t % TC_MT, kk = t / TC_MT, n = m + kk;
+    for (int t = threadIdx.x; t < MT * cnt; t += blockDim.x) {
+      const int bti = t % MT, kk = t / MT, n = m + kk;
       const int par = kk & 1, c = kk >> 1;
-      const T s = sig[bti * TC_CNT + kk], sp = sigP[bti * TC_CNT + kk], tcv = tcmn[bti * TC_CNT + kk];
-      const T sm1 = sigm1[bti * TC_CNT + kk], spm1 = sigPm1[bti * TC_CNT + kk];
+      const T s = sig[bti * CNT + kk], sp = sigP[bti * CNT + kk], tcv = tcmn[bti * CNT + kk];
+      const T sm1 = sigm1[bti * CNT + kk], spm1 = sigPm1[bti * CNT + kk];
       const T nn1 = (T)(n * (n + 1));
       const T om = bti < mt ? G.mco[MC_OM * G.B + b0 + bti] : (T)0;
       T kv[7][2];
 #pragma unroll
       for (int comp = 0; comp < 2; ++comp) {
-        auto S = [&](int gq) { return sRes[(gq * TC_CNT + kk) * 16 + bti * 2 + comp]; };
-        const T sphi = S(0) + nn1 * S(1);
-        const T sdel = S(2) + nn1 * S(3);
-        const T seta = S(4);
+        auto R = [&](int gq) { return sRes[(gq * CNT + kk) * 16 + bti * 2 + comp]; };
+        const T sphi = R(0) + nn1 * R(1);
+        const T sdel = R(2) + nn1 * R(3);
+        const T seta = R(4);
         T cdel, ceta, kphi, kdel, keta;
         if (incr) {
           // new = curr + Inv(dc), dc = (sigma - 1) Fwd(curr) + sigma * tendency
-          const T iphi = S(5), idel = S(6), ieta = S(7);
+          const T iphi = R(5), idel = R(6), ieta = R(7);
           cdel = s * (idel + sdel);
           ceta = s * (ieta + seta);
           kphi = spm1 * iphi + sp * sphi;
@@ -430,8 +505,8 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       kv[3][1] = xm * kv[6][0];
       kv[4][0] = xm * kv[5][1];
       kv[4][1] = -xm * kv[5][0];
-      float* aH = sA + (size_t)(2 * par) * TC_A2;
-      float* aL = aH + TC_A2;
+      float* aH = sA + (size_t)(2 * par) * S::A2;
+      float* aL = aH + S::A2;
 #pragma unroll
       for (int q = 0; q < 7; ++q)
 #pragma unroll
@@ -439,8 +514,8 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
           const int row = q * 16 + bti * 2 + comp;
           float hi, lo;
           tc::split_tf32(kv[q][comp], hi, lo);
-          aH[tc::cm_index(row, c, TC_K2)] = hi;
-          aL[tc::cm_index(row, c, TC_K2)] = lo;
+          aH[tc::cm_index(row, c, S::K2)] = hi;
+          aL[tc::cm_index(row, c, S::K2)] = lo;
         }
     }
     tc::fence_proxy_async();
@@ -448,20 +523,25 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     __syncthreads();
     tc::fence_after_sync();
     // ---- phase 5: GEMM2, both parities (rows 112..127 read the staging area and are ignored)
-    // Each thread first issues the global loads of its write-out pair, so that
+    // Each thread first issues the global loads of its write-out pairs, so that
     // their latency overlaps the GEMM.
-    if (wbt < mt) {
-      load_step_rows<T>(G, cfg, incr, FS, ((size_t)m * G.B + b0 + wbt) * J + wj, pold, pmid);
-      wal = G.mco[(cfg.raw ? MC_RAWM : MC_ALPHA) * G.B + b0 + wbt];
-      wan = cfg.raw ? G.mco[MC_RAWN * G.B + b0 + wbt] : (T)0;
+#pragma unroll
+    for (int k = 0; k < S::NWPAIR; ++k) {
+      wal[k] = (T)0;
+      wan[k] = (T)0;
+      if (wbt[k] < mt) {
+        load_step_rows<T>(G, cfg, incr, FS, ((size_t)m * G.B + b0 + wbt[k]) * J + wj[k], pold[k], pmid[k]);
+        wal[k] = G.mco[(cfg.raw ? MC_RAWM : MC_ALPHA) * G.B + b0 + wbt[k]];
+        wan[k] = cfg.raw ? G.mco[MC_RAWN * G.B + b0 + wbt[k]] : (T)0;
+      }
     }
     if (threadIdx.x == 0) {
       if (!tc::mbar_wait_bounded(&mbar[0], 1, basis.wait_limit)) *sflag = 1;
       if (!*sflag) {
         for (int par = 0; par < 2; ++par) {
-          const uint32_t a2 = aHs + (uint32_t)(2 * par * TC_A2) * 4u;
-          const uint32_t bp = bbase + (uint32_t)(2 * par * TC_N2 * TC_K2) * 4u;
-          mma_3xtf32(tbase + 2 * TC_N1 + par * TC_N2, a2, a2 + TC_A2 * 4, bp, bp + TC_N2 * TC_K2 * 4, TC_K2,
+          const uint32_t a2 = aHs + (uint32_t)(2 * par * S::A2) * 4u;
+          const uint32_t bp = bbase + (uint32_t)(2 * par * S::N2 * S::K2) * 4u;
+          mma_3xtf32(tbase + 2 * S::N1 + par * S::N2, a2, a2 + S::A2 * 4, bp, bp + S::N2 * S::K2 * 4, S::K2,
                      idesc2);
         }
       }
@@ -485,13 +565,13 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
       const bool active = hcols ? (q == 5 || q == 6) : (q <= 4);
       const uint32_t lanes = (uint32_t)(quarter * 32) << 16;
 #pragma unroll
-      for (int cc = 0; cc < 2; ++cc) {
-        const int col0 = half * TC_JH + cc * 16;
+      for (int cc = 0; cc < JH / 16; ++cc) {
+        const int col0 = half * JH + cc * 16;
         float E[16], O[16];
-        tc::tmem_ld16(tbase + lanes + (uint32_t)(2 * TC_N1 + col0), E);
-        tc::tmem_ld16(tbase + lanes + (uint32_t)(2 * TC_N1 + TC_N2 + col0), O);
+        tc::tmem_ld16(tbase + lanes + (uint32_t)(2 * S::N1 + col0), E);
+        tc::tmem_ld16(tbase + lanes + (uint32_t)(2 * S::N1 + S::N2 + col0), O);
         if (active) {
-          float* o = Out + (size_t)(q * TC_MT + bti) * TC_OST + comp;
+          float* o = Out + (size_t)(q * MT + bti) * S::OST + comp;
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             const int jj = cc * 16 + i;
@@ -504,19 +584,24 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
     tc::fence_before_sync();
     __syncthreads();
     // ---- phase 7: write-out and carries, by latitude pairs (16-byte accesses, coalesced along j)
-    if (wbt < mt && !sdead[wbt]) {
-      const size_t o = ((size_t)m * G.B + b0 + wbt) * J + wj;
-      auto get = [&](int f, int e) { return *(const float2*)&Out[(size_t)(f * TC_MT + wbt) * TC_OST + 2 * (wj + e)]; };
-      T2 nw[3][2], uu[2], vv[2];
 #pragma unroll
-      for (int e = 0; e < 2; ++e) {
-        nw[0][e] = get(0, e);
-        nw[1][e] = get(1, e);
-        nw[2][e] = get(2, e);
-        uu[e] = cadd(get(3, e), get(5, e));
-        vv[e] = cadd(get(4, e), get(6, e));
+    for (int k = 0; k < S::NWPAIR; ++k) {
+      if (wbt[k] < mt && !sdead[wbt[k]]) {
+        const size_t o = ((size_t)m * G.B + b0 + wbt[k]) * J + wj[k];
+        auto get = [&](int f, int e) {
+          return *(const float2*)&Out[(size_t)(f * MT + wbt[k]) * S::OST + 2 * (wj[k] + e)];
+        };
+        T2 nw[3][2], uu[2], vv[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          nw[0][e] = get(0, e);
+          nw[1][e] = get(1, e);
+          nw[2][e] = get(2, e);
+          uu[e] = cadd(get(3, e), get(5, e));
+          vv[e] = cadd(get(4, e), get(6, e));
+        }
+        store_step_rows<T>(G, cfg, incr, FS, o, wal[k], wan[k], nw, cfg.test != 1, uu, vv, pold[k], pmid[k]);
       }
-      store_step_rows<T>(G, cfg, incr, FS, o, wal, wan, nw, cfg.test != 1, uu, vv, pold, pmid);
     }
     if (m == 0 && threadIdx.x < mt && !sdead[threadIdx.x]) {
       const int b = b0 + threadIdx.x;
@@ -538,7 +623,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tbase, TC_TMEM_COLS);
+  if (warp == 0) tc::tmem_dealloc(tbase, S::TMEM_COLS);
 }
 
 
@@ -558,26 +643,22 @@ __global__ void __launch_bounds__(256, 2) k_spectral_tc(const __grid_constant__ 
 //   write-out: adj_store_rows (transposed combination) + Phibar gradient.
 // ===========================================================================
 namespace {
-constexpr int TCA_NIN = 5;                          // staged lambda of eta, delta, Phi, U, V
-constexpr int TCA_A2 = TC_ROWS * TC_K2;             // one A2' operand: 128 rows (3072 floats)
-constexpr int TCA_RES0 = 4 * TCA_A2;                // D1' staging after the A2' operands
-constexpr int TCA_RES = 7 * TC_CNT * 16;            // [q][n-m][member, re/im]
-constexpr int TCA_NOUT = 12;                        // 8 P slots + 4 H slots
-constexpr int TCA_A = TCA_RES0 + TCA_RES > TC_A ? TCA_RES0 + TCA_RES : TC_A;
-static_assert(TCA_NOUT * TC_MT * TC_OST <= TCA_A, "adjoint output staging must fit in the A region");
-static_assert(TCA_NIN * TC_MT * TC_J * 2 <= TCA_A, "staged lambda must fit in the A region");
 __host__ __device__ constexpr int adj_hslot(int q) {  // H result of GEMM2' row group q, or -1
   return q == 0 ? 0 : q == 2 ? 1 : q == 3 ? 2 : q == 4 ? 3 : -1;
 }
 }  // namespace
 
-size_t spec_tc_adj_smem_bytes() { return (size_t)(TCA_A + TC_B1 + TC_COEF) * sizeof(float) + 256; }
+size_t spec_tc_adj_smem_bytes(int M) {
+  return tc_dispatch(M, [](auto S) { return (size_t)(S.AA + S.B1 + S.COEF) * sizeof(float) + 256; });
+}
 
-__global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constant__ SpecLaunch<float> L,
-                                                            const __grid_constant__ TcBasis basis, int* err) {
+template <class S>
+__global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_constant__ SpecLaunch<float> L,
+                                                                  const __grid_constant__ TcBasis basis, int* err) {
   typedef float T;
   typedef float2 T2;
   constexpr int NKADJ = 8;
+  constexpr int MT = S::MT, J = S::J, JH = S::JH, CNT = S::CNT;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   int idx;
   const SpecGroup<T>& G = pick_group(L, idx);
@@ -585,12 +666,11 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
   while (gi + 1 < L.ng && (int)blockIdx.x >= L.prefix[gi + 1]) ++gi;
   const float* gbasis = basis.p[gi];
   const StepCfg& cfg = L.cfg;
-  const int J = TC_J;
   const int m = idx / G.ntb;
-  const int b0 = (idx % G.ntb) * TC_MT;
-  const int mt = min(TC_MT, G.B - b0);
-  const int cnt = TC_CNT - m, C0 = (cnt + 1) / 2, C1 = cnt / 2;
-  const size_t FS = (size_t)TC_CNT * G.B * J;
+  const int b0 = (idx % G.ntb) * MT;
+  const int mt = min(MT, G.B - b0);
+  const int cnt = CNT - m, C0 = (cnt + 1) / 2, C1 = cnt / 2;
+  const size_t FS = (size_t)CNT * G.B * J;
   const bool incr = cfg.incremental != 0;
   if (cfg.scheme != 0) {  // the host launches this kernel for modified-Euler steps only
     if (threadIdx.x == 0) atomicExch(err, 2);
@@ -598,17 +678,16 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
   }
 
   float* sA = (float*)smem_raw;            // staged lambda | A1' | A2' + D1' staging | output staging
-  float* sB = sA + TCA_A;                  // B1', then B2'
-  float* sRes = sA + TCA_RES0;
-  float* sig = sB + TC_B1;
-  float* sigP = sig + TC_MT * TC_CNT;
-  float* sigm1 = sigP + TC_MT * TC_CNT;
-  float* sigPm1 = sigm1 + TC_MT * TC_CNT;
-  float* tcmn = sigPm1 + TC_MT * TC_CNT;
-  uint64_t* mbar = (uint64_t*)(((uintptr_t)(tcmn + TC_MT * TC_CNT) + 15) & ~(uintptr_t)15);  // [4]
+  float* sB = sA + S::AA;                  // B1', then B2'; after GEMM2' the per-pair Phibar terms
+  float* sRes = sA + S::ARES0;
+  float* sig = sB + S::B1;
+  float* sigP = sig + MT * CNT;
+  float* sigm1 = sigP + MT * CNT;
+  float* sigPm1 = sigm1 + MT * CNT;
+  float* tcmn = sigPm1 + MT * CNT;
+  uint64_t* mbar = (uint64_t*)(((uintptr_t)(tcmn + MT * CNT) + 15) & ~(uintptr_t)15);  // [4]
   uint32_t* tslot = (uint32_t*)(mbar + 4);
   int* sflag = (int*)(tslot + 1);
-  double* sgrad = (double*)(((uintptr_t)(sflag + 1) + 15) & ~(uintptr_t)15);  // [MT][2]
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int n_tma = 0, n_in = 0, n_c1 = 0, n_c2 = 0;
@@ -620,75 +699,93 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
     for (int q = 0; q < 4; ++q) tc::mbar_init(&mbar[q], 1);
     tc::fence_mbar_init();
     const uint32_t row_bytes = (uint32_t)(mt * J * sizeof(T2));
-    tc::mbar_expect_tx(&mbar[3], row_bytes * TCA_NIN);
+    tc::mbar_expect_tx(&mbar[3], row_bytes * S::ANIN);
 #pragma unroll
-    for (int q = 0; q < TCA_NIN; ++q)
-      tc::bulk_g2s(sA + (size_t)q * TC_MT * J * 2, G.lamY + (size_t)q * FS + ((size_t)m * G.B + b0) * J, row_bytes,
+    for (int q = 0; q < S::ANIN; ++q)
+      tc::bulk_g2s(sA + (size_t)q * MT * J * 2, G.lamY + (size_t)q * FS + ((size_t)m * G.B + b0) * J, row_bytes,
                    &mbar[3]);
     n_in = 1;
-    tc::mbar_expect_tx(&mbar[0], (uint32_t)(TC_B1 * sizeof(float)));
-    tc::bulk_g2s(sB, gbasis + (size_t)m * TC_BLOCK, (uint32_t)(TC_B1 * sizeof(float)), &mbar[0]);
+    tc::mbar_expect_tx(&mbar[0], (uint32_t)(S::B1 * sizeof(float)));
+    tc::bulk_g2s(sB, gbasis + (size_t)m * S::BLOCK, (uint32_t)(S::B1 * sizeof(float)), &mbar[0]);
     n_tma = 1;
   }
   if (warp == 0) {
-    tc::tmem_alloc(tslot, TC_TMEM_COLS);
+    tc::tmem_alloc(tslot, S::TMEM_COLS);
     tc::tmem_relinquish();
   }
-  load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, TC_MT, cnt, TC_CNT, sig, sigP, sigm1, sigPm1, tcmn);
-  if (threadIdx.x < 2 * TC_MT) sgrad[threadIdx.x] = 0.0;
+  load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, CNT, sig, sigP, sigm1, sigPm1, tcmn);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
 
-  // ---- phase 1: symmetrised lambda_Y of (member, j')
-  const int jp = (warp & 3) * 8 + (lane & 7);
-  const int bt = (warp >> 2) * 4 + (lane >> 3);
-  T2 ys[TCA_NIN], ya[TCA_NIN];
-  // write-out: warp -> member, lane -> latitudes 2 lane, 2 lane + 1 (16-byte accesses)
-  static_assert(TC_MT * TC_J == 2 * 256 && TC_J == 64, "one latitude pair per thread, a member per warp");
-  const int wbt = warp, wj = 2 * lane;
-  AdjRowsIn<T> pin;  // its inputs, loaded ahead of GEMM2'
+  // ---- phase 1: symmetrised lambda_Y of (member, j'); warp tasks of 4 members x 8 j'
+  int jp[S::NPAIR], bt[S::NPAIR];
+  bool has[S::NPAIR];
+#pragma unroll
+  for (int k = 0; k < S::NPAIR; ++k) {
+    const int task = warp + 8 * k;
+    has[k] = task < S::NTASK;
+    const int jb = has[k] ? task % (JH / 8) : 0, mb = has[k] ? task / (JH / 8) : 0;
+    jp[k] = jb * 8 + (lane & 7);
+    bt[k] = mb * 4 + (lane >> 3);
+  }
+  T2 ys[S::NPAIR][S::ANIN], ya[S::NPAIR][S::ANIN];
+  // write-out: thread -> member wbt, latitudes wj, wj + 1 (16-byte accesses)
+  int wbt[S::NWPAIR], wj[S::NWPAIR];
+#pragma unroll
+  for (int k = 0; k < S::NWPAIR; ++k) {
+    const int q = threadIdx.x + 256 * k;
+    wbt[k] = q < MT * J / 2 ? q / (J / 2) : MT;
+    wj[k] = 2 * (q % (J / 2));
+  }
+  AdjRowsIn<T> pin[S::NWPAIR];  // its inputs, loaded ahead of GEMM2'
   bool ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[3], 0, basis.wait_limit) : true;
   ok = __syncthreads_and(ok);
   if (ok) {
     const T2* stg = (const T2*)sA;
 #pragma unroll
-    for (int f = 0; f < TCA_NIN; ++f) {
-      if (bt < mt) {
-        const T2 u = stg[(f * TC_MT + bt) * J + jp], v = stg[(f * TC_MT + bt) * J + (J - 1 - jp)];
-        ys[f] = cadd(u, v);
-        ya[f] = csub(u, v);
-      } else {
-        ys[f] = mk<T2>(0, 0);
-        ya[f] = ys[f];
+    for (int k = 0; k < S::NPAIR; ++k)
+#pragma unroll
+      for (int f = 0; f < S::ANIN; ++f) {
+        if (has[k] && bt[k] < mt) {
+          const T2 u = stg[(f * MT + bt[k]) * J + jp[k]], v = stg[(f * MT + bt[k]) * J + (J - 1 - jp[k])];
+          ys[k][f] = cadd(u, v);
+          ya[k][f] = csub(u, v);
+        } else {
+          ys[k][f] = mk<T2>(0, 0);
+          ya[k][f] = ys[k][f];
+        }
       }
-    }
   }
   // parity 0: the P groups take the symmetric sums, the H groups the antisymmetric ones
   auto write_A1 = [&](int par) {
     float* aH = sA;
-    float* aL = sA + TC_ROWS * TC_K1;
+    float* aL = sA + S::ROWS * S::K1;
 #pragma unroll
-    for (int gq = 0; gq < 7; ++gq) {
-      const bool hg = gq >= 5;
-      const int f = hg ? gq - 2 : gq;  // H groups carry lambda U, V
-      const T2 v = hg ? (par ? ys[f] : ya[f]) : (par ? ya[f] : ys[f]);
+    for (int k = 0; k < S::NPAIR; ++k) {
+      if (!has[k]) continue;
 #pragma unroll
-      for (int comp = 0; comp < 2; ++comp) {
-        const int row = gq * 16 + bt * 2 + comp;
-        float hi, lo;
-        tc::split_tf32(comp ? v.y : v.x, hi, lo);
-        aH[tc::cm_index(row, hg ? TC_JH + jp : jp, TC_K1)] = hi;
-        aL[tc::cm_index(row, hg ? TC_JH + jp : jp, TC_K1)] = lo;
-        aH[tc::cm_index(row, hg ? jp : TC_JH + jp, TC_K1)] = 0.f;
-        aL[tc::cm_index(row, hg ? jp : TC_JH + jp, TC_K1)] = 0.f;
+      for (int gq = 0; gq < 7; ++gq) {
+        const bool hg = gq >= 5;
+        const int f = hg ? gq - 2 : gq;  // H groups carry lambda U, V
+        const T2 v = hg ? (par ? ys[k][f] : ya[k][f]) : (par ? ya[k][f] : ys[k][f]);
+#pragma unroll
+        for (int comp = 0; comp < 2; ++comp) {
+          const int row = gq * 16 + bt[k] * 2 + comp;
+          float hi, lo;
+          tc::split_tf32(comp ? v.y : v.x, hi, lo);
+          aH[tc::cm_index(row, hg ? JH + jp[k] : jp[k], S::K1)] = hi;
+          aL[tc::cm_index(row, hg ? JH + jp[k] : jp[k], S::K1)] = lo;
+          aH[tc::cm_index(row, hg ? jp[k] : JH + jp[k], S::K1)] = 0.f;
+          aL[tc::cm_index(row, hg ? jp[k] : JH + jp[k], S::K1)] = 0.f;
+        }
       }
     }
   };
-  const uint32_t idesc1 = tc::idesc_tf32(TC_ROWS, TC_N1), idesc1w = tc::idesc_tf32(TC_ROWS, 2 * TC_N1);
-  const uint32_t idesc2 = tc::idesc_tf32(TC_ROWS, TC_N2);
-  const uint32_t aHs = tc::smem_u32(sA), aLs = aHs + (uint32_t)(TC_ROWS * TC_K1 * 4);
+  const uint32_t idesc1 = tc::idesc_tf32(S::ROWS, S::N1), idesc1w = tc::idesc_tf32(S::ROWS, 2 * S::N1);
+  const uint32_t idesc2 = tc::idesc_tf32(S::ROWS, S::N2);
+  const uint32_t aHs = tc::smem_u32(sA), aLs = aHs + (uint32_t)(S::ROWS * S::K1 * 4);
   const uint32_t bbase = tc::smem_u32(sB);
 
   // ---- phase 2: GEMM1', parity 0 then parity 1
@@ -699,7 +796,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
     __syncthreads();
     if (threadIdx.x == 0) {
       if (!tc::mbar_wait_bounded(&mbar[0], 0, basis.wait_limit)) *sflag = 1;
-      if (!*sflag) mma_3xtf32_2(tbase, aHs, aLs, bbase, TC_N1, TC_K1, idesc1w, idesc1);
+      if (!*sflag) mma_3xtf32_2(tbase, aHs, aLs, bbase, S::N1, S::K1, idesc1w, idesc1);
       tc::mma_commit(&mbar[1]);
       n_c1 = 1;
     }
@@ -713,8 +810,8 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
     tc::fence_proxy_async();
     __syncthreads();
     if (threadIdx.x == 0) {
-      const uint32_t b1 = bbase + 2u * TC_N1 * TC_K1 * 4u;
-      mma_3xtf32_2(tbase + 2 * TC_N1, aHs, aLs, b1, TC_N1, TC_K1, idesc1w, idesc1);
+      const uint32_t b1 = bbase + 2u * S::N1 * S::K1 * 4u;
+      mma_3xtf32_2(tbase + 2 * S::N1, aHs, aLs, b1, S::N1, S::K1, idesc1w, idesc1);
       tc::mma_commit(&mbar[1]);
       n_c1 = 2;
     }
@@ -724,8 +821,8 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
   }
   if (ok) {
     if (threadIdx.x == 0) {
-      tc::mbar_expect_tx(&mbar[0], (uint32_t)(TC_B2 * sizeof(float)));
-      tc::bulk_g2s(sB, gbasis + (size_t)m * TC_BLOCK + TC_B1, (uint32_t)(TC_B2 * sizeof(float)), &mbar[0]);
+      tc::mbar_expect_tx(&mbar[0], (uint32_t)(S::B2 * sizeof(float)));
+      tc::bulk_g2s(sB, gbasis + (size_t)m * S::BLOCK + S::B1, (uint32_t)(S::B2 * sizeof(float)), &mbar[0]);
       n_tma = 2;
     }
     // ---- phase 3: D1' -> sRes[q][n-m][member, re/im]; zero the A2' operands
@@ -735,52 +832,52 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
       const int gq = row >> 4, btc = row & 15;
       const int Cp = par ? C1 : C0;
 #pragma unroll
-      for (int c0 = 0; c0 < TC_N1; c0 += 16) {
+      for (int c0 = 0; c0 < S::N1; c0 += 16) {
         float v[16], v1[16];
-        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(2 * par * TC_N1 + c0), v);
-        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((2 * par + 1) * TC_N1 + c0), v1);
+        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(2 * par * S::N1 + c0), v);
+        tc::tmem_ld16(tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((2 * par + 1) * S::N1 + c0), v1);
 #pragma unroll
         for (int i = 0; i < 16; ++i) v[i] += v1[i];
         if (gq < 7) {
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             const int c = c0 + i;
-            if (c < Cp) sRes[(gq * TC_CNT + (par + 2 * c)) * 16 + btc] = v[i];
+            if (c < Cp) sRes[(gq * CNT + (par + 2 * c)) * 16 + btc] = v[i];
           }
         }
       }
     }
-    for (int i = threadIdx.x; i < TCA_RES0; i += blockDim.x) sA[i] = 0.f;
+    for (int i = threadIdx.x; i < S::ARES0; i += blockDim.x) sA[i] = 0.f;
     tc::fence_before_sync();
     __syncthreads();
     // ---- phase 4: transposed wind inversion, n(n+1), hyperdiffusion -> A2' [par][hi, lo][128][K2]
-    for (int t = threadIdx.x; t < TC_MT * cnt; t += blockDim.x) {
-      const int bti = t % TC_MT, kk = t / TC_MT, n = m + kk;
+    for (int t = threadIdx.x; t < MT * cnt; t += blockDim.x) {
+      const int bti = t % MT, kk = t / MT, n = m + kk;
       const int par = kk & 1, c = kk >> 1;
-      auto S = [&](int q, int comp) { return sRes[(q * TC_CNT + kk) * 16 + bti * 2 + comp]; };
+      auto R = [&](int q, int comp) { return sRes[(q * CNT + kk) * 16 + bti * 2 + comp]; };
       const T xm = (T)m;
-      const T tcv = tcmn[bti * TC_CNT + kk];
-      const T s = sig[bti * TC_CNT + kk], sp = sigP[bti * TC_CNT + kk];
-      const T sm1 = sigm1[bti * TC_CNT + kk], spm1 = sigPm1[bti * TC_CNT + kk];
+      const T tcv = tcmn[bti * CNT + kk];
+      const T s = sig[bti * CNT + kk], sp = sigP[bti * CNT + kk];
+      const T sm1 = sigm1[bti * CNT + kk], spm1 = sigPm1[bti * CNT + kk];
       const T nn1 = (T)(n * (n + 1));
       // lambda delta_s = (i m) lambda Uprep - lambda Hin_V ; lambda eta_s = (i m) lambda Vprep + lambda Hin_U
-      const T lds_r = -xm * S(3, 1) - S(6, 0), lds_i = xm * S(3, 0) - S(6, 1);
-      const T les_r = -xm * S(4, 1) + S(5, 0), les_i = xm * S(4, 0) + S(5, 1);
+      const T lds_r = -xm * R(3, 1) - R(6, 0), lds_i = xm * R(3, 0) - R(6, 1);
+      const T les_r = -xm * R(4, 1) + R(5, 0), les_i = xm * R(4, 0) + R(5, 1);
       const T w = (n == 0) ? (T)0 : tcv;
-      const T lce_r = S(0, 0) + w * les_r, lce_i = S(0, 1) + w * les_i;
-      const T lcd_r = S(1, 0) + w * lds_r, lcd_i = S(1, 1) + w * lds_i;
-      const T lcp_r = S(2, 0), lcp_i = S(2, 1);
+      const T lce_r = R(0, 0) + w * les_r, lce_i = R(0, 1) + w * les_i;
+      const T lcd_r = R(1, 0) + w * lds_r, lcd_i = R(1, 1) + w * lds_i;
+      const T lcp_r = R(2, 0), lcp_i = R(2, 1);
       T kv[NKADJ][2];
       kv[0][0] = sp * lcp_r; kv[0][1] = sp * lcp_i;
       kv[1][0] = nn1 * sp * lcp_r; kv[1][1] = nn1 * sp * lcp_i;
       kv[2][0] = s * lcd_r; kv[2][1] = s * lcd_i;
       kv[3][0] = nn1 * s * lcd_r; kv[3][1] = nn1 * s * lcd_i;
       kv[4][0] = s * lce_r; kv[4][1] = s * lce_i;
-      kv[5][0] = incr ? spm1 * S(2, 0) : (T)0; kv[5][1] = incr ? spm1 * S(2, 1) : (T)0;
-      kv[6][0] = incr ? (s * w * lds_r + sm1 * S(1, 0)) : (T)0; kv[6][1] = incr ? (s * w * lds_i + sm1 * S(1, 1)) : (T)0;
-      kv[7][0] = incr ? (s * w * les_r + sm1 * S(0, 0)) : (T)0; kv[7][1] = incr ? (s * w * les_i + sm1 * S(0, 1)) : (T)0;
-      float* aH = sA + (size_t)(2 * par) * TCA_A2;
-      float* aL = aH + TCA_A2;
+      kv[5][0] = incr ? spm1 * R(2, 0) : (T)0; kv[5][1] = incr ? spm1 * R(2, 1) : (T)0;
+      kv[6][0] = incr ? (s * w * lds_r + sm1 * R(1, 0)) : (T)0; kv[6][1] = incr ? (s * w * lds_i + sm1 * R(1, 1)) : (T)0;
+      kv[7][0] = incr ? (s * w * les_r + sm1 * R(0, 0)) : (T)0; kv[7][1] = incr ? (s * w * les_i + sm1 * R(0, 1)) : (T)0;
+      float* aH = sA + (size_t)(2 * par) * S::AA2;
+      float* aL = aH + S::AA2;
 #pragma unroll
       for (int q = 0; q < NKADJ; ++q)
 #pragma unroll
@@ -788,8 +885,8 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
           const int row = q * 16 + bti * 2 + comp;
           float hi, lo;
           tc::split_tf32(kv[q][comp], hi, lo);
-          aH[tc::cm_index(row, c, TC_K2)] = hi;
-          aL[tc::cm_index(row, c, TC_K2)] = lo;
+          aH[tc::cm_index(row, c, S::K2)] = hi;
+          aL[tc::cm_index(row, c, S::K2)] = lo;
         }
     }
     tc::fence_proxy_async();
@@ -797,14 +894,16 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
     __syncthreads();
     tc::fence_after_sync();
     // ---- phase 5: GEMM2', both parities; write-out inputs loaded meanwhile
-    if (wbt < mt) adj_load_rows<T>(G, incr, FS, ((size_t)m * G.B + b0 + wbt) * J + wj, pin);
+#pragma unroll
+    for (int k = 0; k < S::NWPAIR; ++k)
+      if (wbt[k] < mt) adj_load_rows<T>(G, incr, FS, ((size_t)m * G.B + b0 + wbt[k]) * J + wj[k], pin[k]);
     if (threadIdx.x == 0) {
       if (!tc::mbar_wait_bounded(&mbar[0], 1, basis.wait_limit)) *sflag = 1;
       if (!*sflag) {
         for (int par = 0; par < 2; ++par) {
-          const uint32_t a2 = aHs + (uint32_t)(2 * par * TCA_A2) * 4u;
-          const uint32_t bp = bbase + (uint32_t)(2 * par * TC_N2 * TC_K2) * 4u;
-          mma_3xtf32(tbase + 2 * TC_N1 + par * TC_N2, a2, a2 + TCA_A2 * 4, bp, bp + TC_N2 * TC_K2 * 4, TC_K2,
+          const uint32_t a2 = aHs + (uint32_t)(2 * par * S::AA2) * 4u;
+          const uint32_t bp = bbase + (uint32_t)(2 * par * S::N2 * S::K2) * 4u;
+          mma_3xtf32(tbase + 2 * S::N1 + par * S::N2, a2, a2 + S::AA2 * 4, bp, bp + S::N2 * S::K2 * 4, S::K2,
                      idesc2);
         }
       }
@@ -828,13 +927,13 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
       const int slot = hcols ? (adj_hslot(q) >= 0 ? NKADJ + adj_hslot(q) : -1) : q;
       const uint32_t lanes = (uint32_t)(quarter * 32) << 16;
 #pragma unroll
-      for (int cc = 0; cc < 2; ++cc) {
-        const int col0 = half * TC_JH + cc * 16;
+      for (int cc = 0; cc < JH / 16; ++cc) {
+        const int col0 = half * JH + cc * 16;
         float E[16], O[16];
-        tc::tmem_ld16(tbase + lanes + (uint32_t)(2 * TC_N1 + col0), E);
-        tc::tmem_ld16(tbase + lanes + (uint32_t)(2 * TC_N1 + TC_N2 + col0), O);
+        tc::tmem_ld16(tbase + lanes + (uint32_t)(2 * S::N1 + col0), E);
+        tc::tmem_ld16(tbase + lanes + (uint32_t)(2 * S::N1 + S::N2 + col0), O);
         if (slot >= 0) {
-          float* o = Out + (size_t)(slot * TC_MT + bti) * TC_OST + comp;
+          float* o = Out + (size_t)(slot * MT + bti) * S::OST + comp;
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             const int jj = cc * 16 + i;
@@ -846,21 +945,27 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
     }
     tc::fence_before_sync();
     __syncthreads();
-    // ---- phase 7: transposed combination -> lambda of the state fields; Phibar gradient
-    if (wbt < mt) {  // uniform over a warp
-      const int b = b0 + wbt;
-      const size_t o = ((size_t)m * G.B + b) * J + wj;
-      auto ld = [&](int q, int e) { return *(const float2*)&Out[(size_t)(q * TC_MT + wbt) * TC_OST + 2 * (wj + e)]; };
-      T gp = adj_store_rows<T, NKADJ>(G, cfg, incr, FS, o, m, b, wj, ld, pin);
-      if (G.grad) {
+    // ---- phase 7: transposed combination -> lambda of the state fields; the
+    // Phibar gradient terms of each latitude pair go to sgp (the B buffer is free)
+    float* sgp = sB;  // [MT][J / 2]
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) gp += __shfl_xor_sync(0xffffffffu, gp, off);
-        if (lane == 0) { sgrad[wbt * 2] = (double)gp; sgrad[wbt * 2 + 1] = 0.0; }
+    for (int k = 0; k < S::NWPAIR; ++k) {
+      if (wbt[k] < mt) {
+        const int b = b0 + wbt[k];
+        const size_t o = ((size_t)m * G.B + b) * J + wj[k];
+        auto ld = [&](int q, int e) {
+          return *(const float2*)&Out[(size_t)(q * MT + wbt[k]) * S::OST + 2 * (wj[k] + e)];
+        };
+        const T gp = adj_store_rows<T, NKADJ>(G, cfg, incr, FS, o, m, b, wj[k], ld, pin[k]);
+        sgp[wbt[k] * (J / 2) + wj[k] / 2] = gp;
       }
     }
     __syncthreads();
-    if (G.grad && threadIdx.x < mt)
-      atomicAdd(&G.grad[G_PHIBAR * G.B + b0 + threadIdx.x], sgrad[threadIdx.x * 2] + sgrad[threadIdx.x * 2 + 1]);
+    if (G.grad && threadIdx.x < mt) {  // per member, summed in a fixed order
+      double acc = 0.0;
+      for (int i = 0; i < J / 2; ++i) acc += (double)sgp[threadIdx.x * (J / 2) + i];
+      atomicAdd(&G.grad[G_PHIBAR * G.B + b0 + threadIdx.x], acc);
+    }
   } else {
     if (threadIdx.x == 0) {
       atomicExch(err, 1);
@@ -872,22 +977,33 @@ __global__ void __launch_bounds__(256, 2) k_spectral_adj_tc(const __grid_constan
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tbase, TC_TMEM_COLS);
+  if (warp == 0) tc::tmem_dealloc(tbase, S::TMEM_COLS);
 }
 
 void spec_tc_set_attributes() {
-  cudaFuncSetAttribute(k_spectral_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spec_tc_smem_bytes());
-  cudaFuncSetAttribute(k_spectral_adj_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spec_tc_adj_smem_bytes());
+  cudaFuncSetAttribute(k_spectral_tc<Tc42>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spec_tc_smem_bytes(42));
+  cudaFuncSetAttribute(k_spectral_adj_tc<Tc42>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)spec_tc_adj_smem_bytes(42));
+  cudaFuncSetAttribute(k_spectral_tc<Tc63>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spec_tc_smem_bytes(63));
+  cudaFuncSetAttribute(k_spectral_adj_tc<Tc63>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)spec_tc_adj_smem_bytes(63));
 }
 
-cudaError_t launch_spec_tc(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err, cudaStream_t s) {
-  k_spectral_tc<<<nblocks, 256, spec_tc_smem_bytes(), s>>>(L, basis, err);
+// One launch per truncation: L holds only the groups of truncation M (the
+// others have no members, so no CTAs).
+cudaError_t launch_spec_tc(int M, const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
+                           cudaStream_t s) {
+  if (nblocks <= 0) return cudaSuccess;
+  if (M == 63) k_spectral_tc<Tc63><<<nblocks, 256, spec_tc_smem_bytes(63), s>>>(L, basis, err);
+  else k_spectral_tc<Tc42><<<nblocks, 256, spec_tc_smem_bytes(42), s>>>(L, basis, err);
   return cudaGetLastError();
 }
 
-cudaError_t launch_spec_adj_tc(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
+cudaError_t launch_spec_adj_tc(int M, const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
                                cudaStream_t s) {
-  k_spectral_adj_tc<<<nblocks, 256, spec_tc_adj_smem_bytes(), s>>>(L, basis, err);
+  if (nblocks <= 0) return cudaSuccess;
+  if (M == 63) k_spectral_adj_tc<Tc63><<<nblocks, 256, spec_tc_adj_smem_bytes(63), s>>>(L, basis, err);
+  else k_spectral_adj_tc<Tc42><<<nblocks, 256, spec_tc_adj_smem_bytes(42), s>>>(L, basis, err);
   return cudaGetLastError();
 }
 

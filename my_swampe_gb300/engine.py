@@ -147,7 +147,9 @@ class Engine:
         _lib.check(rc, self._plan, what)
 
     def tiles(self) -> List[Tuple[int, int]]:
-        """(member tile of the SIMT Legendre kernels, latitude rows per grid CTA) per group."""
+        """(member tile of the SIMT Legendre kernels, latitude rows per grid CTA) per group
+        (groups on the tensor-core kernels keep a SIMT tile for the steps without a
+        tensor-core form)."""
         out = []
         for g in range(len(self.groups)):
             mt, jb = ctypes.c_int(), ctypes.c_int()
@@ -156,7 +158,8 @@ class Engine:
         return out
 
     def autotune(self, nrep: int = 5, use_cache: bool = True) -> List[int]:
-        """Pick the member tile of every group by timing (swp_plan_autotune) on
+        """Pick the Legendre kernel of every group -- the tensor-core kernels (0)
+        or a SIMT member tile (1, 2, 4, 8) -- by timing (swp_plan_autotune) on
         scratch copies of this engine's buffers.  Results are cached per
         (precision, groups) for the process."""
         key = (self.precision, tuple((gd["M"], gd["B"]) for gd in self.groups))
@@ -175,8 +178,14 @@ class Engine:
 
     @property
     def uses_tensor_cores(self) -> bool:
-        """True when the modified-Euler steps run the tcgen05 Legendre kernel."""
+        """True when the modified-Euler steps of some group run the tcgen05 Legendre kernels."""
         return bool(self.lib.swp_plan_uses_tensor_cores(self._plan))
+
+    @property
+    def tensor_core_groups(self) -> List[int]:
+        """The groups whose modified-Euler steps run the tcgen05 Legendre kernels."""
+        mask = int(self.lib.swp_plan_uses_tensor_cores(self._plan))
+        return [g for g in range(len(self.groups)) if (mask >> g) & 1]
 
     def check_device_status(self) -> None:
         """Synchronise and raise if a bounded device wait ran out since the last check."""

@@ -1,5 +1,6 @@
-"""The tcgen05 Legendre kernel of the FP32 modified-Euler step (M = 42) against
-the SIMT FP32 kernel and the FP64 path, through the C ABI.
+"""The tcgen05 Legendre kernels of the FP32 modified-Euler step (M = 42 and
+M = 63, one instantiation each) against the SIMT FP32 kernel and the FP64
+path, through the C ABI.
 
 Both FP32 kernels carry the same incremental step form.  The SIMT kernel
 contracts FP32 operands (24 significant bits); the tensor-core one contracts
@@ -39,8 +40,11 @@ def test_tensor_core_path_selection(cuda):
     assert _engine([(42, 4), (42, 9)], "fast").uses_tensor_cores
     assert not _engine([(42, 4)], "fast", tc=False).uses_tensor_cores
     assert not _engine([(42, 4)], "fp64").uses_tensor_cores
-    assert not _engine([(63, 4)], "fast").uses_tensor_cores
-    assert not _engine([(42, 4), (63, 4)], "fast").uses_tensor_cores
+    assert _engine([(63, 4)], "fast").uses_tensor_cores
+    assert _engine([(42, 4), (63, 4)], "fast").uses_tensor_cores
+    assert not _engine([(106, 4)], "fast").uses_tensor_cores
+    mixed = _engine([(42, 4), (106, 4), (63, 2)], "fast")
+    assert mixed.tensor_core_groups == [0, 2]
 
 
 def _run(eng, nsteps, seeds, modal=1):
@@ -67,15 +71,15 @@ def _rel(a, b):
     return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
 
 
-@pytest.mark.parametrize("B", [8, 13])
-def test_tc_step_matches_simt_and_fp64(cuda, B):
+@pytest.mark.parametrize("M,B", [(42, 8), (42, 13), (63, 8), (63, 13)])
+def test_tc_step_matches_simt_and_fp64(cuda, M, B):
     """B = 13 leaves a ragged member tile (5 of 8)."""
     nsteps = 200
-    tc = _engine([(42, B)], "fast")
+    tc = _engine([(M, B)], "fast")
     assert tc.uses_tensor_cores
     out_tc = _run(tc, nsteps, [21])
-    out_simt = _run(_engine([(42, B)], "fast", tc=False), nsteps, [21])
-    out_64 = _run(_engine([(42, B)], "fp64"), nsteps, [21])
+    out_simt = _run(_engine([(M, B)], "fast", tc=False), nsteps, [21])
+    out_64 = _run(_engine([(M, B)], "fp64"), nsteps, [21])
     bounds = dict(eta=(5e-6, 1.5e-5), delta=(5e-6, 1.5e-5), Phi=(5e-6, 1.5e-5), U=(1e-4, 5e-4), V=(1e-4, 5e-4))
     for k, name in enumerate(("eta", "delta", "Phi", "U", "V")):
         r_tc = _rel(out_tc[0][k], out_64[0][k])
@@ -86,14 +90,15 @@ def test_tc_step_matches_simt_and_fp64(cuda, B):
         assert _rel(out_tc[0][k], out_simt[0][k]) < b_tc, name
 
 
-def test_tc_step_two_groups_one_launch(cuda):
-    """Two M = 42 groups with different member counts in one launch match
-    each group run on its own."""
+@pytest.mark.parametrize("Ms", [(42, 42), (42, 63), (63, 42)])
+def test_tc_step_two_groups_one_launch(cuda, Ms):
+    """Two groups with different member counts (and truncations) in one plan
+    match each group run on its own."""
     import torch
 
-    both = _run(_engine([(42, 5), (42, 11)], "fast"), 40, [3, 4])
-    a = _run(_engine([(42, 5)], "fast"), 40, [3])
-    b = _run(_engine([(42, 11)], "fast"), 40, [4])
+    both = _run(_engine([(Ms[0], 5), (Ms[1], 11)], "fast"), 40, [3, 4])
+    a = _run(_engine([(Ms[0], 5)], "fast"), 40, [3])
+    b = _run(_engine([(Ms[1], 11)], "fast"), 40, [4])
     for k in range(5):
         assert torch.equal(both[0][k], a[0][k])
         assert torch.equal(both[1][k], b[0][k])
@@ -140,16 +145,16 @@ def _grads(eng, nsteps=40):
     return {k: v.grad.clone() for k, v in p.items()}, ics.grad.double().clone()
 
 
-@pytest.mark.parametrize("B", [8, 11])
-def test_tc_adjoint_matches_simt_adjoint(cuda, B):
+@pytest.mark.parametrize("M,B", [(42, 8), (42, 11), (63, 8), (63, 11)])
+def test_tc_adjoint_matches_simt_adjoint(cuda, M, B):
     """The tcgen05 Legendre adjoint (3xTF32) against the SIMT FP32 adjoint on the
     same forward (bounds: 3xTF32 operand rounding, as for the forward kernel)."""
     import torch
 
-    tc = _engine([(42, B)], "fast")
+    tc = _engine([(M, B)], "fast")
     assert tc.uses_tensor_cores
     g_tc, ic_tc = _grads(tc)
-    g_simt, ic_simt = _grads(_engine([(42, B)], "fast", tc=False))
+    g_simt, ic_simt = _grads(_engine([(M, B)], "fast", tc=False))
     for k in g_tc:
         rel = float(torch.linalg.vector_norm(g_tc[k] - g_simt[k]) / torch.linalg.vector_norm(g_simt[k]))
         assert rel < 2e-5, (k, rel)
@@ -158,10 +163,10 @@ def test_tc_adjoint_matches_simt_adjoint(cuda, B):
         assert rel < 2e-4, (f, rel)
 
 
-@pytest.mark.parametrize("precision,M", [("fp64", 42), ("fast", 63)])
+@pytest.mark.parametrize("precision,M", [("fp64", 42), ("fast", 106)])
 def test_autotuned_tiles_give_identical_steps(cuda, precision, M):
     """The autotuner picks a member tile among those that fit; a step's result
-    does not depend on the tile (each member's arithmetic is the same)."""
+    does not depend on the SIMT tile (each member's arithmetic is the same)."""
     import torch
     from my_swampe_gb300 import workloads
     from my_swampe_gb300.engine import Engine, RunFlagsC
@@ -182,3 +187,24 @@ def test_autotuned_tiles_give_identical_steps(cuda, precision, M):
         eng.forward(flags, t0=2, nsteps=6)
         outs.append(eng.output_physical(flags)[0])
     assert torch.equal(outs[0], outs[1])
+
+
+def test_autotuner_chooses_between_tensor_cores_and_simt(cuda):
+    """For groups that can run the tensor-core kernels the autotuner times them
+    against the SIMT tiles; the plan then runs what it reports (0 = tensor
+    cores), and the steps of each choice match the kernel run directly."""
+    import torch
+    from my_swampe_gb300.engine import Engine
+
+    eng = _engine([(42, 16), (63, 8), (106, 4)], "fast")
+    chosen = eng.autotune(nrep=2, use_cache=False)
+    assert chosen[2] in (1, 2, 4)
+    assert eng.tensor_core_groups == [g for g in range(3) if chosen[g] == 0]
+    got = _run(eng, 20, [31, 32, 33])
+    for g, (M, B) in enumerate([(42, 16), (63, 8), (106, 4)]):
+        single = _engine([(M, B)], "fast", tc=chosen[g] == 0)
+        if chosen[g] > 0:
+            single.lib.swp_plan_set_tile(single._plan, 0, chosen[g])
+        want = _run(single, 20, [31 + g])
+        for k in range(5):
+            assert torch.equal(got[g][k], want[0][k]), (M, k)
