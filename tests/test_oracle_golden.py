@@ -81,3 +81,22 @@ def test_oracle_torch_backend_matches_numpy():
     a = o.run_model_scan_final(**kw)["last_state"]["Phi_curr"]
     b = o.run_model_scan_final(o.torch_backend(), **kw)["last_state"]["Phi_curr"]
     np.testing.assert_allclose(np.asarray(a), b.detach().numpy(), rtol=0, atol=1e-9)
+
+
+def test_reference_M106_basis_round_trip_amplifies_modes():
+    """The reference's M=106 basis carries its scaling-table underflow
+    (spectral_transform.py:117-146): for m >~ 80 the weighted forward-inverse
+    Legendre round trip is no longer a projector.  Its largest eigenvalue is
+    1.33 (at m = 83), so a scheme that re-projects the full state every step
+    (the reference's FP64 steps) amplifies those modes; for m <= 79 it is the
+    identity to 1e-10."""
+    geo = o.cached_geometry(106)
+    P, w = geo["Pmn"], geo["w"]
+    worst = {}
+    for m in range(107):
+        Pm = P[:, m, m:]
+        ev = np.abs(np.linalg.eigvals((w[:, None] * Pm).T @ Pm))
+        worst[m] = (ev.max(), ev.min())
+    assert all(abs(worst[m][0] - 1) < 1e-10 and abs(worst[m][1] - 1) < 1e-10 for m in range(80))
+    top = max(range(107), key=lambda m: worst[m][0])
+    assert top == 83 and 1.3 < worst[83][0] < 1.35
