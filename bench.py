@@ -121,7 +121,7 @@ def _group_sizes(B, ngroups):
     return sizes
 
 
-def _setup(precision, B, seed=1234, store="auto", ngroups=2):
+def _setup(precision, B, seed=1234, store="auto", ngroups=2, M=M_BENCH):
     """The B-member ensemble as `ngroups` groups of one plan, run concurrently
     (one stream per group); member b keeps its seed (seed + b) whatever the split."""
     from my_swampe_gb300.engine import Engine, RunFlagsC
@@ -129,7 +129,7 @@ def _setup(precision, B, seed=1234, store="auto", ngroups=2):
     from my_swampe_gb300 import workloads
 
     sizes = _group_sizes(B, ngroups)
-    eng = Engine([(M_BENCH, b) for b in sizes], precision, concurrent=ngroups > 1)
+    eng = Engine([(M, b) for b in sizes], precision, concurrent=ngroups > 1)
     wls, off = [], 0
     for g, b in enumerate(sizes):
         wl = workloads.forced_ensemble(eng, g=g, seed=seed + off)
@@ -691,7 +691,7 @@ def run_profile(args):
     build()
     from my_swampe_gb300.adjoint import Integration
 
-    eng, wl, flags, _, ics = _setup(args.profile, args.B, ngroups=1)
+    eng, wl, flags, _, ics = _setup(args.profile, args.B, ngroups=1, M=args.profile_M)
     if args.profile_case == "steps":
         eng.init_state(ics, flags)
         eng.forward(flags, t0=2, nsteps=3)
@@ -704,7 +704,8 @@ def run_profile(args):
             eng.adjoint_step(flags, four_in, four_out, lam, lamy, grad, t=6)
         torch.cuda.synchronize()
         eng.check_device_status()
-        print(json.dumps({"profile": args.profile, "case": "steps", "B": args.B, "ok": True}))
+        print(json.dumps({"profile": args.profile, "case": "steps", "M": args.profile_M, "B": args.B,
+                          "tensor_core_groups": eng.tensor_core_groups, "ok": True}))
         return
     integ = Integration(eng, flags, t0=2, nsteps=CKPT, ckpt_every=CKPT)
     out = integ.run_forward(ics)[0]
@@ -735,6 +736,8 @@ def main():
     ap.add_argument("--profile", choices=("fast", "fp64"), default=None,
                     help="run a small case of the workload (for ncu) instead of timing")
     ap.add_argument("--profile-case", choices=("window", "steps"), default="window")
+    ap.add_argument("--profile-M", type=int, choices=(42, 63, 106), default=M_BENCH,
+                    help="truncation of the profiled case")
     ap.add_argument("--store", choices=("auto", "all", "checkpoint"), default="auto",
                     help="how the adjoint gets its primal states (Integration store policy)")
     args = ap.parse_args()
