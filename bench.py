@@ -581,9 +581,9 @@ def _mixed_leg(steps=2):
             store = integ.store
             integ.release()
         eng.init_state(ics, flags)
-        eng.forward(flags, t0=2, nsteps=100)
+        eng.forward(flags, t0=2, nsteps=50)
         early = [x.double() for x in eng.output_physical(flags)]
-        eng.forward(flags, t0=102, nsteps=T_BENCH - 100)
+        eng.forward(flags, t0=52, nsteps=T_BENCH - 50)
         eng.check_device_status()
         outs[prec] = (early, [x.double() for x in eng.output_physical(flags)])
         del eng
@@ -591,9 +591,9 @@ def _mixed_leg(steps=2):
     err = {}
     for g, (M, B, _) in enumerate(spec):
         # the reference's FP64 algorithm overflows at M=106 in this regime (its damaged
-        # basis amplifies modes m >= 80 on every full re-projection): compared after 100 steps
+        # basis amplifies modes m = 80..89 on every full re-projection): compared after 50 steps
         late_ok = bool(torch.isfinite(outs["fp64"][1][g]).all())
-        at, nst = (1, T_BENCH) if late_ok else (0, 100)
+        at, nst = (1, T_BENCH) if late_ok else (0, 50)
         e = {"after_steps": nst, "fast_finite_after_1440": bool(torch.isfinite(outs["fast"][1][g]).all())}
         for k, name in enumerate(("eta", "delta", "Phi")):
             ref = outs["fp64"][at][g][k]

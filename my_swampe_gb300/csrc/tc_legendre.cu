@@ -85,6 +85,7 @@ struct TcShape {
   static_assert(ANOUT * MT * OST <= AA, "adjoint output staging must fit in the A region");
   static_assert(ANIN * MT * J * 2 <= AA, "staged lambda must fit in the A region");
   static_assert(MT * J / 2 <= B1, "the adjoint's Phibar terms reuse the B buffer");
+  static_assert(MT <= 8, "one warp per member reduces the adjoint's Phibar terms");
 };
 typedef TcShape<42, 64> Tc42;
 typedef TcShape<63, 96> Tc63;
@@ -961,10 +962,12 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_c
       }
     }
     __syncthreads();
-    if (G.grad && threadIdx.x < mt) {  // per member, summed in a fixed order
-      double acc = 0.0;
-      for (int i = 0; i < J / 2; ++i) acc += (double)sgp[threadIdx.x * (J / 2) + i];
-      atomicAdd(&G.grad[G_PHIBAR * G.B + b0 + threadIdx.x], acc);
+    if (G.grad && warp < mt) {  // one warp per member, reduced in a fixed order
+      float acc = 0.f;
+      for (int i = lane; i < J / 2; i += 32) acc += sgp[warp * (J / 2) + i];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+      if (lane == 0) atomicAdd(&G.grad[G_PHIBAR * G.B + b0 + warp], (double)acc);
     }
   } else {
     if (threadIdx.x == 0) {
