@@ -134,7 +134,7 @@ class Integration:
             raise NotImplementedError("the explicit and semi-implicit schemes have no adjoint (their parameter "
                                       "gradients are tangent runs)")
         eng = self.eng
-        lam, lamy, grad = eng.new_adjoint_buffers()
+        lam, lamy, grad = eng.adjoint_buffers()
         eng.adjoint_seed(dphys, lam)
         if self.store == "all":
             eng.adjoint_stored(self.flags, self._states, lam, lamy, grad, t0=self.t0, nsteps=self.nsteps)
@@ -223,9 +223,9 @@ class _IntegrateFn(torch.autograd.Function):
             dic, grad = integ.run_backward(dphys)
             for g in range(len(eng.groups)):
                 o = 1 + NF * g
-                gr = grad[g]
+                gr = grad[g]  # the engine's buffer: copied out
                 for k, row in enumerate((_lib.G_TAURAD, _lib.G_TAUDRAG, _lib.G_DPHIEQ, _lib.G_PHIBAR)):
-                    res[o + k] = gr[row].to(ctx.in_dtypes[NF * g + k])
+                    res[o + k] = gr[row].to(ctx.in_dtypes[NF * g + k], copy=True)
                 res[o + NP] = dic[g].to(ctx.in_dtypes[NF * g + NP])
         # parameters without an adjoint term: one tangent run per parameter that needs a gradient
         extra = [k for k in range(first_extra, NP)

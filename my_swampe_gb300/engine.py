@@ -291,6 +291,17 @@ class Engine:
         grad = [torch.zeros((_lib.NGRAD, gd["B"]), dtype=torch.float64, device=self.device) for gd in self.groups]
         return lam, lamy, grad
 
+    def adjoint_buffers(self):
+        """This engine's own adjoint buffers (lam, lam_y, grad), kept across calls
+        so that the captured adjoint graphs, which hold their addresses, are
+        replayed rather than captured again; grad is zeroed.  Whatever is handed
+        to a caller from them must be copied first."""
+        if getattr(self, "_adj_bufs", None) is None:
+            self._adj_bufs = self.new_adjoint_buffers()
+        for gr in self._adj_bufs[2]:
+            gr.zero_()
+        return self._adj_bufs
+
     def adjoint_seed(self, dphys: Sequence[torch.Tensor], lam) -> None:
         """lam <- adjoint of the Fourier state from gradients of the physical curr fields (5, B, J, I)."""
         xs = [d.to(device=self.device, dtype=self.rdtype).contiguous() for d in dphys]
