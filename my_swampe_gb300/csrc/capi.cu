@@ -35,6 +35,7 @@ struct swp_plan {
   float* tcbasis_adj[MAXG] = {};
   void* coefmem[MAXG] = {};              // per-call coefficient tables (CoefTables) of each group
   int* d_err = nullptr;                  // device error word set by bounded waits that ran out
+  SchedCounter* d_sched = nullptr;       // persistent-launch counters: one per group chain, one for joint launches
   uint32_t tc_wait_limit = TC_WAIT_LIMIT_DEFAULT;  // mbarrier polls before a tensor-core wait gives up
   // groups run concurrently: each group's step chain on its own stream (forked
   // from and joined to the caller's), so that one group's latency-bound kernels
@@ -113,6 +114,27 @@ int update_coefs(swp_plan* p, const swp_group_state* st, cudaStream_t s, const s
   return SWP_OK;
 }
 
+// Persistent scheduling of a SIMT Legendre launch: the groups in order of
+// decreasing truncation (their units cost the most), and the counter of the
+// chain the launch belongs to (a group's own stream, or the joint launches).
+template <typename T>
+void set_schedule(const swp_plan* p, SpecLaunch<T>& L) {
+  int order[MAXG];
+  for (int g = 0; g < p->ng; ++g) order[g] = g;
+  std::stable_sort(order, order + p->ng, [&](int a, int b) { return p->M[a] > p->M[b]; });
+  int acc = 0;
+  for (int k = 0; k < p->ng; ++k) {
+    L.sorder[k] = order[k];
+    L.sprefix[k] = acc;
+    acc += (p->M[order[k]] + 1) * L.grp[order[k]].ntb;
+  }
+  L.sprefix[p->ng] = acc;
+  int chain = MAXG;
+  if (p->concurrent && p->ng > 1 && __builtin_popcount(p->gmask & ((1u << p->ng) - 1)) == 1)
+    chain = __builtin_ctz(p->gmask);
+  L.sched = p->d_sched ? p->d_sched + chain : nullptr;
+}
+
 template <typename T>
 SpecLaunch<T> make_spec(const swp_plan* p, const swp_group_state* st, int& nblocks) {
   SpecLaunch<T> L;
@@ -140,6 +162,7 @@ SpecLaunch<T> make_spec(const swp_plan* p, const swp_group_state* st, int& nbloc
   }
   L.prefix[p->ng] = acc;
   nblocks = acc;
+  set_schedule(p, L);
   return L;
 }
 
@@ -235,6 +258,7 @@ SpecLaunch<T> simt_only(const swp_plan* p, const SpecLaunch<T>& LS, int& nb) {
   }
   L.prefix[p->ng] = acc;
   nb = acc;
+  set_schedule(p, L);
   return L;
 }
 
@@ -895,7 +919,7 @@ int autotune_impl(swp_plan* p, const swp_group_state* st, const swp_group_adjoin
       if (mt > 0) {
         size_t ss = f64 ? spec_smem_bytes<double>(p->M[g], J, mt) : spec_smem_bytes<float>(p->M[g], J, mt);
         size_t sa = f64 ? spec_adj_smem_bytes<double>(p->M[g], J, mt) : spec_adj_smem_bytes<float>(p->M[g], J, mt);
-        if (ss > 227 * 1024 || sa > 227 * 1024) continue;
+        if (ss > (size_t)SPEC_DYN_SMEM_MAX || sa > (size_t)SPEC_DYN_SMEM_MAX) continue;
         p->MT[g] = mt;
       }
       p->tc[g] = mt == 0;
@@ -1027,6 +1051,12 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
   grid_set_attributes();
   spec_tc_set_attributes();
   cudaStream_t s = 0;
+  if (cudaMalloc(&p->d_sched, (MAXG + 1) * sizeof(SchedCounter)) != cudaSuccess ||
+      cudaMemset(p->d_sched, 0, (MAXG + 1) * sizeof(SchedCounter)) != cudaSuccess) {
+    p->err = "scheduler counter allocation failed";
+    *out = p;
+    return SWP_ERR_CUDA;
+  }
   if (cudaMalloc(&p->d_err, sizeof(int)) != cudaSuccess || cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess) {
     p->err = "device error word allocation failed";
     *out = p;
@@ -1112,6 +1142,7 @@ int swp_plan_destroy(swp_plan* p) {
     if (p->coefmem[g]) cudaFree(p->coefmem[g]);
   }
   if (p->d_err) cudaFree(p->d_err);
+  if (p->d_sched) cudaFree(p->d_sched);
   delete p;
   return SWP_OK;
 }
@@ -1384,7 +1415,8 @@ int swp_plan_set_tile(swp_plan* p, int g, int mt) {
   if (mt < 1 || mt > 8 || (mt & (mt - 1)) != 0) return fail(p, SWP_ERR_ARG, "member tile must be 0, 1, 2, 4 or 8");
   size_t ss = f64 ? spec_smem_bytes<double>(p->M[g], J, mt) : spec_smem_bytes<float>(p->M[g], J, mt);
   size_t sa = f64 ? spec_adj_smem_bytes<double>(p->M[g], J, mt) : spec_adj_smem_bytes<float>(p->M[g], J, mt);
-  if (ss > 227 * 1024 || sa > 227 * 1024) return fail(p, SWP_ERR_ARG, "member tile does not fit in shared memory");
+  if (ss > (size_t)SPEC_DYN_SMEM_MAX || sa > (size_t)SPEC_DYN_SMEM_MAX)
+    return fail(p, SWP_ERR_ARG, "member tile does not fit in shared memory");
   p->MT[g] = mt;
   p->tc[g] = false;
   p->use_tc = false;

@@ -19,6 +19,7 @@
 // into 9 combined inputs per member (5 on Pw, 4 on Hw), and both contractions
 // use the equatorial symmetry of the Gauss grid, Pbar(-mu) = (-1)^(n-m) Pbar(mu),
 // so each contraction runs over J/2 latitudes.
+#include <algorithm>
 #include "swp_internal.h"
 #include "spec_common.cuh"
 
@@ -42,14 +43,48 @@ size_t spec_smem_bytes(int M, int J, int MT) {
 template size_t spec_smem_bytes<double>(int, int, int);
 template size_t spec_smem_bytes<float>(int, int, int);
 
+// Run body(group, unit index) for every unit of the launch: one unit per CTA,
+// or -- persistent launches (L.sched set) -- units taken in turn from the
+// launch's counter by resident CTAs, largest truncation first (its units cost
+// the most), m ascending within a group.  No CTA waits on another: the last
+// CTA to finish resets the counter for the next launch on the stream.
+template <typename T, typename F>
+__device__ __forceinline__ void for_each_unit(const SpecLaunch<T>& L, F body) {
+  if (!L.sched) {
+    int idx;
+    const SpecGroup<T>& G = pick_group(L, idx);
+    body(G, idx);
+    return;
+  }
+  __shared__ int s_unit;
+  const int total = L.prefix[L.ng];
+  for (;;) {
+    if (threadIdx.x == 0) s_unit = atomicAdd(&L.sched->next, 1);
+    __syncthreads();
+    const int u = s_unit;
+    __syncthreads();
+    if (u >= total) break;
+    int k = 0;
+    while (k + 1 < L.ng && u >= L.sprefix[k + 1]) ++k;
+    body(L.grp[L.sorder[k]], u - L.sprefix[k]);
+    __syncthreads();  // the next unit reuses the shared memory
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&L.sched->done, 1) == (int)gridDim.x - 1) {
+      L.sched->next = 0;
+      L.sched->done = 0;
+      __threadfence();
+    }
+  }
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLaunch<T> L) {
+__device__ __forceinline__ void spectral_unit(const SpecLaunch<T>& L, const SpecGroup<T>& G, const int idx) {
   typedef typename cplx<T>::type T2;
   constexpr int NSPX = SlotCount<T>::NP;
   constexpr int NSLOT = NSPX + NSH;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  int idx;
-  const SpecGroup<T>& G = pick_group(L, idx);
   const StepCfg& cfg = L.cfg;
   const int mode = L.mode;
   const Geom<T>& g = G.g;
@@ -479,6 +514,11 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLa
   }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLaunch<T> L) {
+  for_each_unit(L, [&](const SpecGroup<T>& G, int idx) { spectral_unit<T>(L, G, idx); });
+}
+
 // ---------------------------------------------------------------------------
 // Adjoint of k_spectral (modified Euler, mode 0).  Same per-m decomposition:
 //   lambda of the Fourier outputs (eta, delta, Phi, U, V at column m)
@@ -512,13 +552,11 @@ template size_t spec_adj_smem_bytes<double>(int, int, int);
 template size_t spec_adj_smem_bytes<float>(int, int, int);
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ SpecLaunch<T> L) {
+__device__ __forceinline__ void spectral_adj_unit(const SpecLaunch<T>& L, const SpecGroup<T>& G, const int idx) {
   typedef typename cplx<T>::type T2;
   constexpr int NKADJ = AdjCount<T>::NK;
   constexpr int NCAD = NKADJ + 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  int idx;
-  const SpecGroup<T>& G = pick_group(L, idx);
   const StepCfg& cfg = L.cfg;
   const bool incr = SlotCount<T>::INCR && cfg.incremental;
   const Geom<T>& g = G.g;
@@ -766,23 +804,53 @@ __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ Sp
 }
 
 template <typename T>
+__global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ SpecLaunch<T> L) {
+  for_each_unit(L, [&](const SpecGroup<T>& G, int idx) { spectral_adj_unit<T>(L, G, idx); });
+}
+
+namespace {
+// CTAs of a persistent launch: every slot the kernel can keep resident, never
+// more than the launch has units.
+template <typename K>
+int persistent_blocks(K kernel, int nunits, size_t smem) {
+  static int nsm = 0;
+  if (nsm == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
+      nsm = 1;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, smem) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  return std::max(1, std::min(nunits, per_sm * nsm));
+}
+}  // namespace
+
+template <typename T>
 cudaError_t launch_spec_adj(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
-  k_spectral_adj<T><<<nblocks, 256, smem, s>>>(L);
+  if (nblocks <= 0) return cudaSuccess;
+  const int grid = L.sched ? persistent_blocks(k_spectral_adj<T>, nblocks, smem) : nblocks;
+  k_spectral_adj<T><<<grid, 256, smem, s>>>(L);
   return cudaGetLastError();
 }
 template cudaError_t launch_spec_adj<double>(const SpecLaunch<double>&, int, size_t, cudaStream_t);
 template cudaError_t launch_spec_adj<float>(const SpecLaunch<float>&, int, size_t, cudaStream_t);
 
+// Largest dynamic shared memory a SIMT kernel may request: 227 KB per block
+// minus its static shared memory (the persistent scheduler's unit slot).
 void spec_set_attributes() {
-  cudaFuncSetAttribute(k_spectral<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_spectral<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_spectral_adj<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_spectral_adj<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_spectral<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_DYN_SMEM_MAX);
+  cudaFuncSetAttribute(k_spectral<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_DYN_SMEM_MAX);
+  cudaFuncSetAttribute(k_spectral_adj<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_DYN_SMEM_MAX);
+  cudaFuncSetAttribute(k_spectral_adj<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_DYN_SMEM_MAX);
 }
 
 template <typename T>
 cudaError_t launch_spec(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
-  k_spectral<T><<<nblocks, 256, smem, s>>>(L);
+  if (nblocks <= 0) return cudaSuccess;
+  const int grid = L.sched ? persistent_blocks(k_spectral<T>, nblocks, smem) : nblocks;
+  k_spectral<T><<<grid, 256, smem, s>>>(L);
   return cudaGetLastError();
 }
 template cudaError_t launch_spec<double>(const SpecLaunch<double>&, int, size_t, cudaStream_t);

@@ -154,6 +154,14 @@ struct SpecGroup {
   const T* mco;
 };
 
+// Work counter of a persistent launch: units are taken in turn by CTAs that
+// stay resident; the last CTA out resets both words for the next launch on
+// the same stream.
+struct SchedCounter {
+  int next;
+  int done;
+};
+
 template <typename T>
 struct SpecLaunch {
   SpecGroup<T> grp[MAXG];
@@ -161,6 +169,12 @@ struct SpecLaunch {
   int prefix[MAXG + 1];
   StepCfg cfg;
   int mode;                             // 0 = step, 2 = diagnose winds, 3 = tangent-linear step
+  // persistent scheduling (SIMT kernels): when sched is set the launch has one
+  // CTA per resident slot, which take units in order of decreasing truncation
+  // (sorder: groups by decreasing M; sprefix: unit offsets in that order)
+  SchedCounter* sched;
+  int sorder[MAXG];
+  int sprefix[MAXG + 1];
 };
 
 // ------------------------------------------------------------------- grid ---
@@ -216,6 +230,9 @@ template <typename T> cudaError_t launch_spec(const SpecLaunch<T>& L, int nblock
 template <typename T> cudaError_t launch_spec_adj(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s);
 template <typename T> cudaError_t launch_grid(const GridLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s);
 void spec_set_attributes();
+// dynamic shared memory a SIMT Legendre kernel may use (the rest of the 227 KB
+// is kept for its static shared memory)
+constexpr int SPEC_DYN_SMEM_MAX = 227 * 1024 - 128;
 void grid_set_attributes();
 int grid_rows_per_cta(int M, bool fp64, int mode);  // JB the grid kernel is compiled for
 
