@@ -187,6 +187,41 @@ def test_fwd_grad_matches_reverse_mode(cuda):
     assert bool(torch.all(rel < 1e-8)), (g_fwd, g_rev)
 
 
+@pytest.mark.parametrize("chunk", [None, 3])
+def test_batched_fwd_grad_equals_sequential(cuda, chunk):
+    """fwd_grad(batched=True): the p directions as p members of one run, each
+    with its own tangent (chunk=3: two runs of 3 and 1 members), against the
+    sequential form on the drop-in API."""
+    from my_swampe_gb300 import run_model_scan_final, workloads
+    from my_swampe_gb300.autodiff_utils import fwd_grad
+    from my_swampe_gb300.engine import Engine
+
+    eng = Engine([(42, 1)], "fp64")
+    wl = workloads.forced_ensemble(eng, dt=600.0, Phibar=3.0e5, seed=7)
+    ics = [wl["ics"][k, 0] for k in range(5)]  # (J, I) each
+    target = 1.01 * ics[2]
+    kw = dict(M=42, dt=600.0, tmax=2 + NSTEPS, omega=3.2e-5, a=8.2e7, K6=1.24e33)
+
+    def run(th):  # th: (k, 4) rows -> (k, J, I) terminal Phi of k members
+        k = th.shape[0]
+        f = [x.expand(k, *x.shape) for x in ics]
+        return run_model_scan_final(**kw, taurad=th[:, 0], taudrag=th[:, 1], DPhieq=th[:, 2], Phibar=th[:, 3],
+                                    eta0_init=f[0], delta0_init=f[1], Phi0_init=f[2], U0_init=f[3],
+                                    V0_init=f[4])["last_state"].Phi_curr
+
+    def loss_batched(th):
+        return ((run(th) - target) ** 2).mean(dim=(1, 2))
+
+    def loss_one(th):
+        return loss_batched(th[None])[0]
+
+    theta = torch.tensor([36000.0, 21600.0, 1.0e6, 3.0e5], dtype=torch.float64, device=eng.device)
+    g_seq = fwd_grad(loss_one, theta)
+    g_bat = fwd_grad(loss_batched, theta, chunk=chunk, batched=True)
+    rel = (g_bat - g_seq).abs() / g_seq.abs()
+    assert bool(torch.all(rel < 1e-12)), (g_bat, g_seq)
+
+
 def test_fast_tangent_close_to_fp64(cuda):
     """FP32 tangent model (incremental steps) against the FP64 one."""
     t64 = _tangent(*_setup("fp64"))
