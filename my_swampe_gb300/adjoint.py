@@ -81,6 +81,9 @@ class Integration:
         elif store == "auto":
             need = (self.nsteps + 1) * engine.state_bytes()
             free, _ = torch.cuda.mem_get_info(engine.device)
+            # memory torch's caching allocator holds but no tensor uses (e.g. the
+            # stored states of a previous run) is available too
+            free += torch.cuda.memory_reserved(engine.device) - torch.cuda.memory_allocated(engine.device)
             store = "all" if need <= mem_fraction * free else "checkpoint"
         self.store = store
 
