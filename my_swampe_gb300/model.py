@@ -67,7 +67,10 @@ def _engine_for(M: int, B: int, precision: str, device=None) -> Engine:
     key = (int(M), int(B), precision, dev.type, dev.index)
     eng = _ENGINE_CACHE.pop(key, None)
     if eng is None:
-        eng = Engine([(int(M), int(B))], precision, device)
+        # ensembles of 32 members or more: the autotuner picks the Legendre kernel
+        # (tensor cores or a SIMT member tile) once per (M, B, precision) in the
+        # process; smaller ones keep the default (tensor cores where available)
+        eng = Engine([(int(M), int(B))], precision, device, autotune=int(B) >= 32)
     _ENGINE_CACHE[key] = eng
     while len(_ENGINE_CACHE) > _ENGINE_CACHE_SIZE:
         _ENGINE_CACHE.popitem(last=False)
