@@ -236,14 +236,14 @@ int swp_device_status(swp_plan* plan, int* status, void* stream);
 
 /* Which groups' modified-Euler steps run the tcgen05 Legendre kernels: bit g
  * set for group g (so 1 or 0 for a one-group plan).  FP32 plans use them for
- * the groups at M = 42 or 63, unless SWP_NO_TC=1 was set when the plan was
+ * every group (M = 42, 63, 106), unless SWP_NO_TC=1 was set when the plan was
  * created or the autotuner chose the SIMT kernel for the group.  No reference
  * counterpart. */
 int swp_plan_uses_tensor_cores(const swp_plan* plan);
 
 /* Autotuner of the plan's Legendre kernels and tile shapes (no reference
  * counterpart): for every group, the candidates are the tensor-core kernels
- * (FP32 plans, M = 42 or 63: a fixed tile of 8 members) and each member tile
+ * (FP32 plans: a fixed tile of 8 members) and each member tile
  * MT in {1, 2, 4, 8} (<= B) of the SIMT kernels that fits in shared memory.
  * Each is timed -- nrep launches of the step's Legendre kernel and of its
  * adjoint on the caller's buffers st / adj, which it overwrites (pass scratch

@@ -28,7 +28,7 @@ struct swp_plan {
   size_t spec_adj_smem = 0;
   size_t grid_smem[NGRIDMODE] = {};
   // tensor-core Legendre kernels of the FP32 step: tc[g] for the groups that
-  // run them (M = 42 or 63), use_tc if any group does
+  // run them (M = 42, 63 or 106), use_tc if any group does
   bool use_tc = false;
   bool tc[MAXG] = {};
   float* tcbasis[MAXG] = {};
@@ -214,13 +214,19 @@ bool step_incremental(const swp_plan* p, const swp_flags* f, int t) {
   return p->precision == SWP_FAST && f->scheme == 0 && !f->raw_filter && t > f->t_start;
 }
 
-// Tensor-core launches of one step: one launch per truncation present (42, 63),
-// each over the groups of that truncation (the others get no CTAs).
+// Whether group g runs the tensor-core form of the forward (adjoint = false) or
+// adjoint Legendre kernel.
+bool tc_group(const swp_plan* p, int g, bool adjoint) {
+  return p->tc[g] && (!adjoint || spec_tc_adj_supported(p->M[g]));
+}
+
+// Tensor-core launches of one step: one launch per truncation present (42, 63,
+// 106), each over the groups of that truncation (the others get no CTAs).
 template <typename Launch>
 cudaError_t launch_tc_per_truncation(const swp_plan* p, const SpecLaunch<float>& LS, float* const* bases,
-                                     Launch launch) {
+                                     bool adjoint, Launch launch) {
   const int mt = spec_tc_members_per_cta();
-  for (int Mt : {42, 63}) {
+  for (int Mt : {42, 63, 106}) {
     SpecLaunch<float> LT = LS;
     int acc = 0;
     TcBasis tb;
@@ -228,7 +234,7 @@ cudaError_t launch_tc_per_truncation(const swp_plan* p, const SpecLaunch<float>&
     tb.wait_limit = p->tc_wait_limit;
     bool any = false;
     for (int g = 0; g < p->ng; ++g) {
-      if (p->M[g] != Mt || !p->tc[g]) LT.grp[g].B = 0;
+      if (p->M[g] != Mt || !tc_group(p, g, adjoint)) LT.grp[g].B = 0;
       LT.grp[g].MT = mt;
       LT.grp[g].ntb = (LT.grp[g].B + mt - 1) / mt;
       LT.prefix[g] = acc;
@@ -247,11 +253,11 @@ cudaError_t launch_tc_per_truncation(const swp_plan* p, const SpecLaunch<float>&
 // The SIMT launch of the groups that do not run the tensor-core kernels (the
 // others get no CTAs); returns the block count through nb.
 template <typename T>
-SpecLaunch<T> simt_only(const swp_plan* p, const SpecLaunch<T>& LS, int& nb) {
+SpecLaunch<T> simt_only(const swp_plan* p, const SpecLaunch<T>& LS, bool adjoint, int& nb) {
   SpecLaunch<T> L = LS;
   int acc = 0;
   for (int g = 0; g < p->ng; ++g) {
-    if (p->tc[g]) L.grp[g].B = 0;
+    if (tc_group(p, g, adjoint)) L.grp[g].B = 0;
     L.grp[g].ntb = (L.grp[g].B + L.grp[g].MT - 1) / L.grp[g].MT;
     L.prefix[g] = acc;
     acc += (p->M[g] + 1) * L.grp[g].ntb;
@@ -268,12 +274,12 @@ template <typename T>
 cudaError_t launch_step_spec(const swp_plan* p, const SpecLaunch<T>& LS, int nbs, cudaStream_t s) {
   if constexpr (std::is_same<T, float>::value) {
     if (p->use_tc && LS.mode == 0 && LS.cfg.scheme == 0) {
-      cudaError_t e = launch_tc_per_truncation(p, LS, p->tcbasis, [&](int Mt, const SpecLaunch<float>& LT, int n,
-                                                                      const TcBasis& tb) {
-        return launch_spec_tc(Mt, LT, n, tb, p->d_err, s);
-      });
+      cudaError_t e = launch_tc_per_truncation(p, LS, p->tcbasis, false,
+                                               [&](int Mt, const SpecLaunch<float>& LT, int n, const TcBasis& tb) {
+                                                 return launch_spec_tc(Mt, LT, n, tb, p->d_err, s);
+                                               });
       int nb = 0;
-      SpecLaunch<float> LR = simt_only(p, LS, nb);
+      SpecLaunch<float> LR = simt_only(p, LS, false, nb);
       if (e == cudaSuccess && nb > 0) e = launch_spec<T>(LR, nb, p->spec_smem, s);
       return e;
     }
@@ -287,12 +293,12 @@ template <typename T>
 cudaError_t launch_step_spec_adj(const swp_plan* p, const SpecLaunch<T>& LS, int nbs, cudaStream_t s) {
   if constexpr (std::is_same<T, float>::value) {
     if (p->use_tc && LS.cfg.scheme == 0) {
-      cudaError_t e = launch_tc_per_truncation(p, LS, p->tcbasis_adj, [&](int Mt, const SpecLaunch<float>& LT,
-                                                                          int n, const TcBasis& tb) {
-        return launch_spec_adj_tc(Mt, LT, n, tb, p->d_err, s);
-      });
+      cudaError_t e = launch_tc_per_truncation(p, LS, p->tcbasis_adj, true,
+                                               [&](int Mt, const SpecLaunch<float>& LT, int n, const TcBasis& tb) {
+                                                 return launch_spec_adj_tc(Mt, LT, n, tb, p->d_err, s);
+                                               });
       int nb = 0;
-      SpecLaunch<float> LR = simt_only(p, LS, nb);
+      SpecLaunch<float> LR = simt_only(p, LS, true, nb);
       if (e == cudaSuccess && nb > 0) e = launch_spec_adj<T>(LR, nb, p->spec_adj_smem, s);
       return e;
     }
@@ -1093,7 +1099,7 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
       p->grid_smem[mode] = std::max(p->grid_smem[mode], gs);
     }
   }
-  // tensor-core step kernels: FP32 plans whose groups are all M = 42 or 63, unless SWP_NO_TC=1
+  // tensor-core step kernels: every group of an FP32 plan, unless SWP_NO_TC=1
   const char* tc_env = getenv("SWP_NO_TC");
   const bool tc_on = precision == SWP_FAST && !(tc_env && tc_env[0] == '1');
   bool tc = false;
@@ -1104,10 +1110,11 @@ int swp_plan_create(int ngroups, const int* M, const int* B, int precision, swp_
   if (tc) {
     for (int g = 0; g < ngroups; ++g) {
       if (!p->tc[g]) continue;
+      const bool adj = spec_tc_adj_supported(M[g]);
       if (cudaMalloc(&p->tcbasis[g], spec_tc_basis_floats(M[g]) * sizeof(float)) != cudaSuccess ||
           pack_tc_basis(p->geom[g], p->tcbasis[g], s) != SWP_OK ||
-          cudaMalloc(&p->tcbasis_adj[g], spec_tc_basis_floats(M[g]) * sizeof(float)) != cudaSuccess ||
-          pack_tc_basis_adj(p->geom[g], p->tcbasis_adj[g], s) != SWP_OK) {
+          (adj && cudaMalloc(&p->tcbasis_adj[g], spec_tc_adj_basis_floats(M[g]) * sizeof(float)) != cudaSuccess) ||
+          (adj && pack_tc_basis_adj(p->geom[g], p->tcbasis_adj[g], s) != SWP_OK)) {
         p->err = "tensor-core basis packing failed";
         *out = p;
         return SWP_ERR_CUDA;

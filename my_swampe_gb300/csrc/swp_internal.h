@@ -236,7 +236,8 @@ constexpr int SPEC_DYN_SMEM_MAX = 227 * 1024 - 128;
 void grid_set_attributes();
 int grid_rows_per_cta(int M, bool fp64, int mode);  // JB the grid kernel is compiled for
 
-// tensor-core Legendre kernels of the FP32 modified-Euler step (tc_legendre.cu), M = 42 and 63
+// tensor-core Legendre kernels of the FP32 modified-Euler step and its adjoint
+// (tc_legendre.cu: M = 42 and 63; tc_legendre106.cu: M = 106)
 // packed basis of each group, and the poll limit of the kernels' mbarrier waits
 struct TcBasis {
   const float* p[MAXG];
@@ -246,7 +247,9 @@ constexpr uint32_t TC_WAIT_LIMIT_DEFAULT = SWP_WAIT_LIMIT_DEFAULT;
 size_t spec_tc_smem_bytes(int M);
 size_t spec_tc_basis_floats(int M);
 int spec_tc_members_per_cta();
-bool spec_tc_supported(int M);
+bool spec_tc_supported(int M);      // forward kernel
+bool spec_tc_adj_supported(int M);  // adjoint kernel
+size_t spec_tc_adj_basis_floats(int M);
 int pack_tc_basis(const GroupGeom& gg, float* out, cudaStream_t s);
 void spec_tc_set_attributes();
 cudaError_t launch_spec_tc(int M, const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
@@ -255,5 +258,14 @@ int pack_tc_basis_adj(const GroupGeom& gg, float* out, cudaStream_t s);
 size_t spec_tc_adj_smem_bytes(int M);
 cudaError_t launch_spec_adj_tc(int M, const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
                                cudaStream_t s);
+size_t spec_tc106_smem_bytes();
+size_t spec_tc106_adj_smem_bytes();
+size_t spec_tc106_basis_floats();
+int pack_tc106_basis(const GroupGeom& gg, float* out, bool adjoint, cudaStream_t s);
+void spec_tc106_set_attributes();
+cudaError_t launch_spec_tc106(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
+                              cudaStream_t s);
+cudaError_t launch_spec_adj_tc106(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
+                                  cudaStream_t s);
 
 }  // namespace swp

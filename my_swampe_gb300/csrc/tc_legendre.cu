@@ -1,6 +1,7 @@
 // Tensor-core (tcgen05) Legendre sandwich of one modified-Euler step, FP32
 // fast path, compiled per truncation: M = 42 (64 x 128 Gauss grid, two CTAs
-// per SM) and M = 63 (96 x 192, one CTA per SM).  The shapes below are those
+// per SM) and M = 63 (96 x 192, one CTA per SM); M = 106, whose operands do not
+// fit in one CTA's shared memory, has its own chunked kernel (tc_legendre106.cu).  The shapes below are those
 // of M = 42; TcShape<M, J> gives them for any truncation whose operands fit in
 // shared memory.
 //
@@ -116,11 +117,17 @@ auto tc_dispatch(int M, F f) -> decltype(f(Tc42())) {
 }  // namespace
 
 size_t spec_tc_smem_bytes(int M) {
+  if (M == 106) return spec_tc106_smem_bytes();
   return tc_dispatch(M, [](auto S) { return (size_t)(S.A + S.B1 + S.COEF) * sizeof(float) + 256; });
 }
-size_t spec_tc_basis_floats(int M) { return tc_dispatch(M, [](auto S) { return (size_t)S.CNT * S.BLOCK; }); }
+size_t spec_tc_basis_floats(int M) {
+  if (M == 106) return spec_tc106_basis_floats();
+  return tc_dispatch(M, [](auto S) { return (size_t)S.CNT * S.BLOCK; });
+}
+size_t spec_tc_adj_basis_floats(int M) { return spec_tc_basis_floats(M); }
 int spec_tc_members_per_cta() { return 8; }
-bool spec_tc_supported(int M) { return M == 42 || M == 63; }
+bool spec_tc_supported(int M) { return M == 42 || M == 63 || M == 106; }
+bool spec_tc_adj_supported(int M) { return spec_tc_supported(M); }
 
 // Pack the FP64 basis into the per-m GEMM operand blocks of shape S.
 template <class S>
@@ -171,6 +178,7 @@ int pack_basis(const GroupGeom& gg, const double* f1, const double* f2, const do
 }  // namespace
 
 int pack_tc_basis(const GroupGeom& gg, float* out, cudaStream_t s) {
+  if (gg.M == 106) return pack_tc106_basis(gg, out, false, s);
   return pack_basis(gg, gg.b64[B_PW_F], gg.b64[B_HW_F], gg.b64[B_P_I], gg.b64[B_H_I], out, s);
 }
 
@@ -178,6 +186,7 @@ int pack_tc_basis(const GroupGeom& gg, float* out, cudaStream_t s) {
 // the forward layout (transposed inverse Legendre), GEMM2' with the weighted
 // basis in the inverse layout (transposed forward Legendre).
 int pack_tc_basis_adj(const GroupGeom& gg, float* out, cudaStream_t s) {
+  if (gg.M == 106) return pack_tc106_basis(gg, out, true, s);
   return pack_basis(gg, gg.b64[B_P_F], gg.b64[B_H_F], gg.b64[B_PW_I], gg.b64[B_HW_I], out, s);
 }
 
@@ -650,6 +659,7 @@ __host__ __device__ constexpr int adj_hslot(int q) {  // H result of GEMM2' row 
 }  // namespace
 
 size_t spec_tc_adj_smem_bytes(int M) {
+  if (M == 106) return spec_tc106_adj_smem_bytes();
   return tc_dispatch(M, [](auto S) { return (size_t)(S.AA + S.B1 + S.COEF) * sizeof(float) + 256; });
 }
 
@@ -990,6 +1000,7 @@ void spec_tc_set_attributes() {
   cudaFuncSetAttribute(k_spectral_tc<Tc63>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spec_tc_smem_bytes(63));
   cudaFuncSetAttribute(k_spectral_adj_tc<Tc63>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)spec_tc_adj_smem_bytes(63));
+  spec_tc106_set_attributes();
 }
 
 // One launch per truncation: L holds only the groups of truncation M (the
@@ -997,6 +1008,7 @@ void spec_tc_set_attributes() {
 cudaError_t launch_spec_tc(int M, const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
                            cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
+  if (M == 106) return launch_spec_tc106(L, nblocks, basis, err, s);
   if (M == 63) k_spectral_tc<Tc63><<<nblocks, 256, spec_tc_smem_bytes(63), s>>>(L, basis, err);
   else k_spectral_tc<Tc42><<<nblocks, 256, spec_tc_smem_bytes(42), s>>>(L, basis, err);
   return cudaGetLastError();
@@ -1005,6 +1017,7 @@ cudaError_t launch_spec_tc(int M, const SpecLaunch<float>& L, int nblocks, const
 cudaError_t launch_spec_adj_tc(int M, const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
                                cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
+  if (M == 106) return launch_spec_adj_tc106(L, nblocks, basis, err, s);
   if (M == 63) k_spectral_adj_tc<Tc63><<<nblocks, 256, spec_tc_adj_smem_bytes(63), s>>>(L, basis, err);
   else k_spectral_adj_tc<Tc42><<<nblocks, 256, spec_tc_adj_smem_bytes(42), s>>>(L, basis, err);
   return cudaGetLastError();

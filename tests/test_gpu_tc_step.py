@@ -1,6 +1,6 @@
 """The tcgen05 Legendre kernels of the FP32 modified-Euler step (M = 42 and
-M = 63, one instantiation each) against the SIMT FP32 kernel and the FP64
-path, through the C ABI.
+M = 63, one instantiation each; M = 106, a chunked kernel of its own) against
+the SIMT FP32 kernel and the FP64 path, through the C ABI.
 
 Both FP32 kernels carry the same incremental step form.  The SIMT kernel
 contracts FP32 operands (24 significant bits); the tensor-core one contracts
@@ -42,18 +42,19 @@ def test_tensor_core_path_selection(cuda):
     assert not _engine([(42, 4)], "fp64").uses_tensor_cores
     assert _engine([(63, 4)], "fast").uses_tensor_cores
     assert _engine([(42, 4), (63, 4)], "fast").uses_tensor_cores
-    assert not _engine([(106, 4)], "fast").uses_tensor_cores
+    assert _engine([(106, 4)], "fast").uses_tensor_cores
     mixed = _engine([(42, 4), (106, 4), (63, 2)], "fast")
-    assert mixed.tensor_core_groups == [0, 2]
+    assert mixed.tensor_core_groups == [0, 1, 2]
+    assert _engine([(42, 4), (106, 4)], "fp64").tensor_core_groups == []
 
 
-def _run(eng, nsteps, seeds, modal=1):
+def _run(eng, nsteps, seeds, modal=1, dt=30.0):
     from my_swampe_gb300 import workloads
     from my_swampe_gb300.engine import RunFlagsC
 
     ics = []
     for g, seed in enumerate(seeds):
-        wl = workloads.forced_ensemble(eng, g=g, seed=seed)
+        wl = workloads.forced_ensemble(eng, g=g, seed=seed, dt=dt)
         workloads.apply_params(eng, g, wl["params"])
         ics.append(wl["ics"])
     flags = RunFlagsC()
@@ -71,26 +72,44 @@ def _rel(a, b):
     return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
 
 
-@pytest.mark.parametrize("M,B", [(42, 8), (42, 13), (63, 8), (63, 13)])
+# (SIMT vs FP64, tensor cores vs FP64, tensor cores vs SIMT) relative L2 bounds
+_STEP_BOUNDS = {
+    # 200 steps of 30 s
+    42: dict(eta=(5e-6, 1.5e-5, 1.5e-5), delta=(5e-6, 1.5e-5, 1.5e-5), Phi=(5e-6, 1.5e-5, 1.5e-5),
+             U=(1e-4, 5e-4, 5e-4), V=(1e-4, 5e-4, 5e-4)),
+    # 50 steps of 12 s.  The FP32 steps leave FP64 in delta by 2.1e-4 on either
+    # kernel: the reference's M = 106 basis amplifies some of its modes, which
+    # the incremental FP32 form and the FP64 projection form treat differently.
+    # After 600 s of spin-up the winds are tiny next to the planetary vorticity
+    # they are inverted from: U on the tensor-core path observed 2.5e-3 (SIMT
+    # 4.4e-4), the 3xTF32 rounding of that cancellation.
+    106: dict(eta=(5e-6, 1.5e-5, 1.5e-5), delta=(1e-3, 1e-3, 5e-5), Phi=(1e-5, 1.5e-5, 1.5e-5),
+              U=(2e-3, 1e-2, 1e-2), V=(5e-5, 2e-4, 2e-4)),
+}
+_STEP_BOUNDS[63] = _STEP_BOUNDS[42]
+
+
+@pytest.mark.parametrize("M,B", [(42, 8), (42, 13), (63, 8), (63, 13), (106, 8), (106, 13)])
 def test_tc_step_matches_simt_and_fp64(cuda, M, B):
-    """B = 13 leaves a ragged member tile (5 of 8)."""
-    nsteps = 200
+    """B = 13 leaves a ragged member tile (5 of 8).  M = 106 runs the chunked
+    kernel (GEMM1 over 5 latitude chunks, GEMM2 over two column halves)."""
+    nsteps, dt = (50, 12.0) if M == 106 else (200, 30.0)
     tc = _engine([(M, B)], "fast")
     assert tc.uses_tensor_cores
-    out_tc = _run(tc, nsteps, [21])
-    out_simt = _run(_engine([(M, B)], "fast", tc=False), nsteps, [21])
-    out_64 = _run(_engine([(M, B)], "fp64"), nsteps, [21])
-    bounds = dict(eta=(5e-6, 1.5e-5), delta=(5e-6, 1.5e-5), Phi=(5e-6, 1.5e-5), U=(1e-4, 5e-4), V=(1e-4, 5e-4))
+    out_tc = _run(tc, nsteps, [21], dt=dt)
+    out_simt = _run(_engine([(M, B)], "fast", tc=False), nsteps, [21], dt=dt)
+    out_64 = _run(_engine([(M, B)], "fp64"), nsteps, [21], dt=dt)
     for k, name in enumerate(("eta", "delta", "Phi", "U", "V")):
         r_tc = _rel(out_tc[0][k], out_64[0][k])
         r_simt = _rel(out_simt[0][k], out_64[0][k])
-        b_simt, b_tc = bounds[name]
+        r_ts = _rel(out_tc[0][k], out_simt[0][k])
+        b_simt, b_tc, b_ts = _STEP_BOUNDS[M][name]
         assert r_simt < b_simt, (name, r_tc, r_simt)
         assert r_tc < b_tc, (name, r_tc, r_simt)
-        assert _rel(out_tc[0][k], out_simt[0][k]) < b_tc, name
+        assert r_ts < b_ts, (name, r_ts)
 
 
-@pytest.mark.parametrize("Ms", [(42, 42), (42, 63), (63, 42)])
+@pytest.mark.parametrize("Ms", [(42, 42), (42, 63), (63, 42), (106, 42), (63, 106)])
 def test_tc_step_two_groups_one_launch(cuda, Ms):
     """Two groups with different member counts (and truncations) in one plan
     match each group run on its own."""
@@ -125,13 +144,13 @@ def test_tc_step_with_diagnostics_matches_fp64(cuda):
     np.testing.assert_array_equal(f32["outs"]["dead"].cpu().numpy(), f64["outs"]["dead"].cpu().numpy())
 
 
-def _grads(eng, nsteps=40):
+def _grads(eng, nsteps=40, dt=30.0):
     import torch
     from my_swampe_gb300 import workloads
     from my_swampe_gb300.adjoint import GRAD_PARAMS, integrate
     from my_swampe_gb300.engine import RunFlagsC
 
-    wl = workloads.forced_ensemble(eng, seed=9)
+    wl = workloads.forced_ensemble(eng, seed=9, dt=dt)
     workloads.apply_params(eng, 0, wl["params"])
     B = eng.groups[0]["B"]
     p = {k: torch.as_tensor(wl["params"][k], dtype=torch.float64, device=eng.device).expand(B).clone().requires_grad_(True)
@@ -145,19 +164,26 @@ def _grads(eng, nsteps=40):
     return {k: v.grad.clone() for k, v in p.items()}, ics.grad.double().clone()
 
 
-@pytest.mark.parametrize("M,B", [(42, 8), (42, 11), (63, 8), (63, 11)])
+@pytest.mark.parametrize("M,B", [(42, 8), (42, 11), (63, 8), (63, 11), (106, 8), (106, 11)])
 def test_tc_adjoint_matches_simt_adjoint(cuda, M, B):
     """The tcgen05 Legendre adjoint (3xTF32) against the SIMT FP32 adjoint on the
-    same forward (bounds: 3xTF32 operand rounding, as for the forward kernel)."""
+    same forward (bounds: 3xTF32 operand rounding, as for the forward kernel).
+    Each run takes the forward of its own plan (tensor cores or SIMT); M = 106
+    runs the chunked kernels, at dt = 12 s.  There the drag gradient, a
+    contraction with the winds, carries the tensor-core forward's larger wind
+    error of the spin-up (U 2.5e-3 after 50 steps): observed 7.6e-5 against the
+    SIMT run and 7.4e-5 against FP64 (SIMT: 4.2e-6), bound 2e-4; every other
+    gradient stays within 2.6e-6 of FP64."""
     import torch
 
+    dt = 12.0 if M == 106 else 30.0
     tc = _engine([(M, B)], "fast")
     assert tc.uses_tensor_cores
-    g_tc, ic_tc = _grads(tc)
-    g_simt, ic_simt = _grads(_engine([(M, B)], "fast", tc=False))
+    g_tc, ic_tc = _grads(tc, dt=dt)
+    g_simt, ic_simt = _grads(_engine([(M, B)], "fast", tc=False), dt=dt)
     for k in g_tc:
         rel = float(torch.linalg.vector_norm(g_tc[k] - g_simt[k]) / torch.linalg.vector_norm(g_simt[k]))
-        assert rel < 2e-5, (k, rel)
+        assert rel < (2e-4 if (M, k) == (106, "taudrag") else 2e-5), (k, rel)
     for f in range(5):
         rel = float(torch.linalg.vector_norm(ic_tc[f] - ic_simt[f]) / torch.linalg.vector_norm(ic_simt[f]))
         assert rel < 2e-4, (f, rel)
@@ -173,7 +199,7 @@ def test_autotuned_tiles_give_identical_steps(cuda, precision, M):
 
     outs = []
     for tile in (None, 1):
-        eng = Engine([(M, 6)], precision)
+        eng = _engine([(M, 6)], precision, tc=False)
         if tile is None:
             chosen = eng.autotune(nrep=2, use_cache=False)
             assert chosen[0] in (1, 2, 4) and eng.tiles()[0][0] == chosen[0]
@@ -198,7 +224,7 @@ def test_autotuner_chooses_between_tensor_cores_and_simt(cuda):
 
     eng = _engine([(42, 16), (63, 8), (106, 4)], "fast")
     chosen = eng.autotune(nrep=2, use_cache=False)
-    assert chosen[2] in (1, 2, 4)
+    assert chosen[2] in (0, 1, 2, 4)
     assert eng.tensor_core_groups == [g for g in range(3) if chosen[g] == 0]
     got = _run(eng, 20, [31, 32, 33])
     for g, (M, B) in enumerate([(42, 16), (63, 8), (106, 4)]):
