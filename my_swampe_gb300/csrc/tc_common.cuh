@@ -106,6 +106,47 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                : "memory");
 }
 
+// Warp-collective forms: every lane of one warp executes them, in warp-uniform
+// control flow and with the same arguments, and the lane that elect.sync picks
+// (the same one each time with all 32 lanes active) issues.  An MMA issued
+// from such a warp keeps its descriptors in uniform registers; issued from one
+// thread of divergent code it costs more cycles per instruction.
+__device__ __forceinline__ void mma_tf32_warp(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                              uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p, e;\n\tsetp.ne.b32 p, %4, 0;\n\telect.sync _|e, 0xffffffff;\n\t"
+      "@e tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+      : "memory");
+}
+// commit of the MMAs the elected lane issued (the same lane as mma_tf32_warp's)
+__device__ __forceinline__ void mma_commit_warp(uint64_t* mbar) {
+  asm volatile(
+      "{\n\t.reg .pred e;\n\telect.sync _|e, 0xffffffff;\n\t"
+      "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}" ::"r"(smem_u32(mbar))
+      : "memory");
+}
+// expect_tx and the bulk copy it covers, issued by the elected lane
+__device__ __forceinline__ void bulk_g2s_warp(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+  asm volatile(
+      "{\n\t.reg .pred e;\n\telect.sync _|e, 0xffffffff;\n\t"
+      "@e mbarrier.arrive.expect_tx.shared::cta.b64 _, [%3], %2;\n\t"
+      "@e cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n\t}" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+      : "memory");
+}
+// bounded wait by the whole warp; the result is the same in every lane
+__device__ __forceinline__ bool mbar_wait_bounded_warp(uint64_t* mbar, uint32_t parity, uint32_t max_iter) {
+  for (uint32_t it = 0; it < max_iter; ++it)
+    if (__any_sync(0xffffffffu, mbar_try_wait(mbar, parity))) return true;
+  return false;
+}
+// descriptor of the operand that starts `bytes` (a multiple of 16) further on:
+// the start address is the low 14-bit field, in 16-byte units (shared-memory
+// addresses stay below 2^18, so the field does not overflow)
+__device__ __forceinline__ uint64_t desc_advance(uint64_t desc, uint32_t bytes) { return desc + (bytes >> 4); }
+
 // TMEM -> registers: this warp's 32 lanes, 16 consecutive 32-bit columns.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   uint32_t r[16];

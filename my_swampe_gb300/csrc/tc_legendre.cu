@@ -191,15 +191,20 @@ int pack_tc_basis_adj(const GroupGeom& gg, float* out, cudaStream_t s) {
 }
 
 namespace {
+// The MMAs are issued by warp 0 as a whole (warp-collective forms, one elected
+// lane issues), with the descriptors of a K-sweep built once and advanced by
+// 256 bytes (8 TF32 columns of the core-matrix layout) per K-step.
 // the three products of one 3xTF32 K-sweep into d_tmem (K a multiple of 8)
 __device__ __forceinline__ void mma_3xtf32(uint32_t d_tmem, uint32_t aH, uint32_t aL, uint32_t bH, uint32_t bL, int K,
                                            uint32_t idesc) {
   const uint32_t sbo = (uint32_t)(K / 4) * 128u;
+  const uint64_t dAH = tc::make_desc(aH, 128, sbo), dAL = tc::make_desc(aL, 128, sbo);
+  const uint64_t dBH = tc::make_desc(bH, 128, sbo), dBL = tc::make_desc(bL, 128, sbo);
   for (int kk = 0; kk < K / 8; ++kk) {
     const uint32_t off = (uint32_t)kk * 256u;
-    tc::mma_tf32(d_tmem, tc::make_desc(aH + off, 128, sbo), tc::make_desc(bH + off, 128, sbo), idesc, kk > 0);
-    tc::mma_tf32(d_tmem, tc::make_desc(aH + off, 128, sbo), tc::make_desc(bL + off, 128, sbo), idesc, 1);
-    tc::mma_tf32(d_tmem, tc::make_desc(aL + off, 128, sbo), tc::make_desc(bH + off, 128, sbo), idesc, 1);
+    tc::mma_tf32_warp(d_tmem, tc::desc_advance(dAH, off), tc::desc_advance(dBH, off), idesc, kk > 0);
+    tc::mma_tf32_warp(d_tmem, tc::desc_advance(dAH, off), tc::desc_advance(dBL, off), idesc, 1);
+    tc::mma_tf32_warp(d_tmem, tc::desc_advance(dAL, off), tc::desc_advance(dBH, off), idesc, 1);
   }
 }
 // The same K-sweep in two MMAs per K-step.  The issue of an MMA, not its
@@ -211,11 +216,12 @@ __device__ __forceinline__ void mma_3xtf32(uint32_t d_tmem, uint32_t aH, uint32_
 __device__ __forceinline__ void mma_3xtf32_2(uint32_t d_tmem, uint32_t aH, uint32_t aL, uint32_t bH, int n, int K,
                                              uint32_t idesc_2n, uint32_t idesc_n) {
   const uint32_t sbo = (uint32_t)(K / 4) * 128u;
+  const uint64_t dAH = tc::make_desc(aH, 128, sbo), dAL = tc::make_desc(aL, 128, sbo);
+  const uint64_t dBH = tc::make_desc(bH, 128, sbo);
   for (int kk = 0; kk < K / 8; ++kk) {
     const uint32_t off = (uint32_t)kk * 256u;
-    tc::mma_tf32(d_tmem, tc::make_desc(aH + off, 128, sbo), tc::make_desc(bH + off, 128, sbo), idesc_2n, kk > 0);
-    tc::mma_tf32(d_tmem + (uint32_t)n, tc::make_desc(aL + off, 128, sbo), tc::make_desc(bH + off, 128, sbo), idesc_n,
-                 1);
+    tc::mma_tf32_warp(d_tmem, tc::desc_advance(dAH, off), tc::desc_advance(dBH, off), idesc_2n, kk > 0);
+    tc::mma_tf32_warp(d_tmem + (uint32_t)n, tc::desc_advance(dAL, off), tc::desc_advance(dBH, off), idesc_n, 1);
   }
 }
 }  // namespace
@@ -414,10 +420,11 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_tc(const __grid_const
     write_A1(0);
     tc::fence_proxy_async();
     __syncthreads();
-    if (threadIdx.x == 0) {
-      if (!tc::mbar_wait_bounded(&mbar[0], 0, basis.wait_limit)) *sflag = 1;
-      if (!*sflag) mma_3xtf32_2(tbase, aHs, aLs, bbase, S::N1, S::K1, idesc1w, idesc1);
-      tc::mma_commit(&mbar[1]);
+    if (warp == 0) {  // warp-collective MMA issue
+      const bool good = tc::mbar_wait_bounded_warp(&mbar[0], 0, basis.wait_limit);
+      if (!good) *sflag = 1;
+      if (good) mma_3xtf32_2(tbase, aHs, aLs, bbase, S::N1, S::K1, idesc1w, idesc1);
+      tc::mma_commit_warp(&mbar[1]);
       n_c1 = 1;
     }
     ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 0, basis.wait_limit) : true;
@@ -429,10 +436,10 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_tc(const __grid_const
     write_A1(1);
     tc::fence_proxy_async();
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (warp == 0) {
       const uint32_t b1 = bbase + 2u * S::N1 * S::K1 * 4u;
       mma_3xtf32_2(tbase + 2 * S::N1, aHs, aLs, b1, S::N1, S::K1, idesc1w, idesc1);
-      tc::mma_commit(&mbar[1]);
+      tc::mma_commit_warp(&mbar[1]);
       n_c1 = 2;
     }
     ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 1, basis.wait_limit) : true;
@@ -545,9 +552,10 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_tc(const __grid_const
         wan[k] = cfg.raw ? G.mco[MC_RAWN * G.B + b0 + wbt[k]] : (T)0;
       }
     }
-    if (threadIdx.x == 0) {
-      if (!tc::mbar_wait_bounded(&mbar[0], 1, basis.wait_limit)) *sflag = 1;
-      if (!*sflag) {
+    if (warp == 0) {
+      const bool good = tc::mbar_wait_bounded_warp(&mbar[0], 1, basis.wait_limit);
+      if (!good) *sflag = 1;
+      if (good) {
         for (int par = 0; par < 2; ++par) {
           const uint32_t a2 = aHs + (uint32_t)(2 * par * S::A2) * 4u;
           const uint32_t bp = bbase + (uint32_t)(2 * par * S::N2 * S::K2) * 4u;
@@ -555,7 +563,7 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_tc(const __grid_const
                      idesc2);
         }
       }
-      tc::mma_commit(&mbar[2]);
+      tc::mma_commit_warp(&mbar[2]);
       n_c2 = 1;
     }
     ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[2], 0, basis.wait_limit) : true;
@@ -805,10 +813,11 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_c
     write_A1(0);
     tc::fence_proxy_async();
     __syncthreads();
-    if (threadIdx.x == 0) {
-      if (!tc::mbar_wait_bounded(&mbar[0], 0, basis.wait_limit)) *sflag = 1;
-      if (!*sflag) mma_3xtf32_2(tbase, aHs, aLs, bbase, S::N1, S::K1, idesc1w, idesc1);
-      tc::mma_commit(&mbar[1]);
+    if (warp == 0) {  // warp-collective MMA issue
+      const bool good = tc::mbar_wait_bounded_warp(&mbar[0], 0, basis.wait_limit);
+      if (!good) *sflag = 1;
+      if (good) mma_3xtf32_2(tbase, aHs, aLs, bbase, S::N1, S::K1, idesc1w, idesc1);
+      tc::mma_commit_warp(&mbar[1]);
       n_c1 = 1;
     }
     ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 0, basis.wait_limit) : true;
@@ -820,10 +829,10 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_c
     write_A1(1);
     tc::fence_proxy_async();
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (warp == 0) {
       const uint32_t b1 = bbase + 2u * S::N1 * S::K1 * 4u;
       mma_3xtf32_2(tbase + 2 * S::N1, aHs, aLs, b1, S::N1, S::K1, idesc1w, idesc1);
-      tc::mma_commit(&mbar[1]);
+      tc::mma_commit_warp(&mbar[1]);
       n_c1 = 2;
     }
     ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 1, basis.wait_limit) : true;
@@ -908,9 +917,10 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_c
 #pragma unroll
     for (int k = 0; k < S::NWPAIR; ++k)
       if (wbt[k] < mt) adj_load_rows<T>(G, incr, FS, ((size_t)m * G.B + b0 + wbt[k]) * J + wj[k], pin[k]);
-    if (threadIdx.x == 0) {
-      if (!tc::mbar_wait_bounded(&mbar[0], 1, basis.wait_limit)) *sflag = 1;
-      if (!*sflag) {
+    if (warp == 0) {
+      const bool good = tc::mbar_wait_bounded_warp(&mbar[0], 1, basis.wait_limit);
+      if (!good) *sflag = 1;
+      if (good) {
         for (int par = 0; par < 2; ++par) {
           const uint32_t a2 = aHs + (uint32_t)(2 * par * S::AA2) * 4u;
           const uint32_t bp = bbase + (uint32_t)(2 * par * S::N2 * S::K2) * 4u;
@@ -918,7 +928,7 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_c
                      idesc2);
         }
       }
-      tc::mma_commit(&mbar[2]);
+      tc::mma_commit_warp(&mbar[2]);
       n_c2 = 1;
     }
     ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[2], 0, basis.wait_limit) : true;

@@ -78,40 +78,60 @@ __host__ __device__ constexpr int group_p106(int g) {
 __host__ __device__ constexpr int group_h106(int g) {
   return g == 0 ? SH_PHI1 : g == 2 ? SH_D1 : g == 3 ? SH_D2 : g == 4 ? SH_E1 : -1;
 }
+// the Fourier fields the modified-Euler combination reads (eta, delta, Phi,
+// A..G) <-> register slots of the prefetched chunk inputs
+__host__ __device__ constexpr int field106(int q) {
+  return q == 0 ? F_ETA : q == 1 ? F_DELTA : q == 2 ? F_PHI : F_A + (q - 3);
+}
+__host__ __device__ constexpr int slot106(int f) {
+  return f == F_ETA ? 0 : f == F_DELTA ? 1 : f == F_PHI ? 2 : (f >= F_A && f <= F_G) ? f - F_A + 3 : 0;
+}
+static_assert(F_G - F_A + 4 == 11, "prefetched fields");
 __host__ __device__ constexpr int adj_hslot106(int q) {  // H result of GEMM2' row group q, or -1
   return q == 0 ? 0 : q == 2 ? 1 : q == 3 ? 2 : q == 4 ? 3 : -1;
 }
 
+// The MMAs are issued by warp 0 as a whole (warp-collective forms, one elected
+// lane issues), with the descriptors of a K-sweep built once and advanced by
+// 256 bytes (8 TF32 columns of the core-matrix layout) per K-step.
 // the three products of one 3xTF32 K-sweep into d_tmem (operands of K columns)
-__device__ __forceinline__ void mma3(uint32_t d_tmem, uint32_t aH, uint32_t aL, uint32_t bH, uint32_t bL, int K,
+template <int K>
+__device__ __forceinline__ void mma3(uint32_t d_tmem, uint32_t aH, uint32_t aL, uint32_t bH, uint32_t bL,
                                      uint32_t idesc) {
-  const uint32_t sbo = (uint32_t)(K / 4) * 128u;
+  constexpr uint32_t sbo = (uint32_t)(K / 4) * 128u;
+  const uint64_t dAH = tc::make_desc(aH, 128, sbo), dAL = tc::make_desc(aL, 128, sbo);
+  const uint64_t dBH = tc::make_desc(bH, 128, sbo), dBL = tc::make_desc(bL, 128, sbo);
+#pragma unroll
   for (int kk = 0; kk < K / 8; ++kk) {
     const uint32_t off = (uint32_t)kk * 256u;
-    tc::mma_tf32(d_tmem, tc::make_desc(aH + off, 128, sbo), tc::make_desc(bH + off, 128, sbo), idesc, kk > 0);
-    tc::mma_tf32(d_tmem, tc::make_desc(aH + off, 128, sbo), tc::make_desc(bL + off, 128, sbo), idesc, 1);
-    tc::mma_tf32(d_tmem, tc::make_desc(aL + off, 128, sbo), tc::make_desc(bH + off, 128, sbo), idesc, 1);
+    tc::mma_tf32_warp(d_tmem, tc::desc_advance(dAH, off), tc::desc_advance(dBH, off), idesc, kk > 0);
+    tc::mma_tf32_warp(d_tmem, tc::desc_advance(dAH, off), tc::desc_advance(dBL, off), idesc, 1);
+    tc::mma_tf32_warp(d_tmem, tc::desc_advance(dAL, off), tc::desc_advance(dBH, off), idesc, 1);
   }
 }
 // one chunk of the GEMM1 sweep in two MMAs per K-step (a_hi [b_hi; b_lo], then
 // a_lo b_hi onto the second half); the first MMA of the first chunk overwrites
 __device__ __forceinline__ void mma2_chunk(uint32_t d_tmem, uint32_t aH, uint32_t aL, uint32_t bH, bool first,
                                            uint32_t idesc_2n, uint32_t idesc_n) {
-  const uint32_t sbo = (uint32_t)(S::KC / 4) * 128u;
+  constexpr uint32_t sbo = (uint32_t)(S::KC / 4) * 128u;
+  const uint64_t dAH = tc::make_desc(aH, 128, sbo), dAL = tc::make_desc(aL, 128, sbo);
+  const uint64_t dBH = tc::make_desc(bH, 128, sbo);
+#pragma unroll
   for (int kk = 0; kk < S::KC / 8; ++kk) {
     const uint32_t off = (uint32_t)kk * 256u;
-    tc::mma_tf32(d_tmem, tc::make_desc(aH + off, 128, sbo), tc::make_desc(bH + off, 128, sbo), idesc_2n,
-                 (first && kk == 0) ? 0u : 1u);
-    tc::mma_tf32(d_tmem + (uint32_t)S::N1, tc::make_desc(aL + off, 128, sbo), tc::make_desc(bH + off, 128, sbo),
-                 idesc_n, 1);
+    tc::mma_tf32_warp(d_tmem, tc::desc_advance(dAH, off), tc::desc_advance(dBH, off), idesc_2n,
+                      (first && kk == 0) ? 0u : 1u);
+    tc::mma_tf32_warp(d_tmem + (uint32_t)S::N1, tc::desc_advance(dAL, off), tc::desc_advance(dBH, off), idesc_n, 1);
   }
 }
 
-// Thread 0's record of the CTA's mbarriers: the phases it armed on each (a bulk
+// Warp 0's record of the CTA's mbarriers: the phases it armed on each (a bulk
 // copy or an MMA commit) and how many of them it has waited for, so that every
 // wait names the next phase and the drain after a timeout waits for exactly the
-// phases still open.  Barriers: 0, 1 B1 chunk copies per stage; 2, 3 GEMM1
-// commits per stage; 4, 5 B2 half copies per buffer; 6, 7 GEMM2 commits per buffer.
+// phases still open.  Every lane of warp 0 keeps the same record; the copies
+// and commits are issued by one elected lane.  Barriers: 0, 1 B1 chunk copies
+// per stage; 2, 3 GEMM1 commits per stage; 4, 5 B2 half copies per buffer;
+// 6, 7 GEMM2 commits per buffer.
 struct BarLog {
   static constexpr int NB = 8;
   uint64_t* bar;
@@ -121,16 +141,15 @@ struct BarLog {
     for (int q = 0; q < NB; ++q) iss[q] = wtd[q] = 0;
   }
   __device__ void copy(int q, void* dst, const void* src, uint32_t bytes) {
-    tc::mbar_expect_tx(&bar[q], bytes);
-    tc::bulk_g2s(dst, src, bytes, &bar[q]);
+    tc::bulk_g2s_warp(dst, src, bytes, &bar[q]);
     ++iss[q];
   }
   __device__ void commit(int q) {
-    tc::mma_commit(&bar[q]);
+    tc::mma_commit_warp(&bar[q]);
     ++iss[q];
   }
   __device__ bool wait(int q, uint32_t limit) {
-    if (!tc::mbar_wait_bounded(&bar[q], (uint32_t)(wtd[q] & 1), limit)) return false;
+    if (!tc::mbar_wait_bounded_warp(&bar[q], (uint32_t)(wtd[q] & 1), limit)) return false;
     ++wtd[q];
     return true;
   }
@@ -143,22 +162,22 @@ struct BarLog {
 
 constexpr uint32_t B1_BYTES = 2 * S::BCH * sizeof(float), B2_BYTES = S::B2H * sizeof(float);
 
-// CTA set-up shared by both kernels: the mbarriers and the first two B1 chunk
-// copies (thread 0), TMEM (warp 0).
+// CTA set-up shared by both kernels, by warp 0: the mbarriers, the first two
+// B1 chunk copies, TMEM.
 __device__ __forceinline__ void setup_chunks(BarLog& bl, float* sR, const float* mblock, uint32_t* tslot,
                                              int* sflag) {
+  if ((threadIdx.x >> 5) != 0) return;
   if (threadIdx.x == 0) {
     *sflag = 0;
 #pragma unroll
     for (int q = 0; q < BarLog::NB; ++q) tc::mbar_init(&bl.bar[q], 1);
     tc::fence_mbar_init();
-    for (int s = 0; s < 2; ++s)
-      bl.copy(s, sR + (size_t)s * S::STAGE + 2 * S::ACH, mblock + (size_t)s * 2 * S::BCH, B1_BYTES);
   }
-  if ((threadIdx.x >> 5) == 0) {
-    tc::tmem_alloc(tslot, S::TMEM_COLS);
-    tc::tmem_relinquish();
-  }
+  __syncwarp();
+  for (int s = 0; s < 2; ++s)
+    bl.copy(s, sR + (size_t)s * S::STAGE + 2 * S::ACH, mblock + (size_t)s * 2 * S::BCH, B1_BYTES);
+  tc::tmem_alloc(tslot, S::TMEM_COLS);
+  tc::tmem_relinquish();
 }
 
 // The thread's place in a chunk: member bt, latitude pair jl of the chunk, side
@@ -178,25 +197,30 @@ struct ChunkLane {
 };
 
 // GEMM1 over the latitude chunks into D1 (TMEM columns [128 par, 128 par + 128)).
-// inputs(ch, vp, vh) gives, for the thread's (member, j' = 16 ch + jl), the
-// values of the 8 row groups on the P and the H columns, already summed with the
-// mirror latitude: symmetric on side 0, antisymmetric on side 1.  Parity 0 takes
-// the symmetric P sums and the antisymmetric H sums, parity 1 the reverse, so the
-// side 0 thread writes parity 0's P columns and parity 1's H columns, the side 1
-// thread the other two.  Returns false (the same value in every thread) when a
-// wait ran out.
-template <class Inputs>
+// fetch(ch, raw) issues the global loads of the thread's inputs at (member,
+// j' = 16 ch + jl) into registers -- one chunk ahead, so that their latency
+// overlaps the stores and barriers of the current chunk; the caller has fetched
+// chunk 0.  form(ch, raw, vp, vh) gives the values of the 8 row groups on the P and
+// the H columns, already summed with the mirror latitude: symmetric on side 0,
+// antisymmetric on side 1.  Parity 0 takes the symmetric P sums and the
+// antisymmetric H sums, parity 1 the reverse, so the side 0 thread writes parity
+// 0's P columns and parity 1's H columns, the side 1 thread the other two.
+// Returns false (the same value in every thread) when a wait ran out.
+template <class Raw, class Fetch, class Form>
 __device__ __forceinline__ bool gemm1_chunks(BarLog& bl, float* sR, const float* mblock, uint32_t tbase,
-                                             int* sflag, uint32_t lim, const ChunkLane& cl, Inputs inputs) {
+                                             int* sflag, uint32_t lim, const ChunkLane& cl, Raw& raw, Fetch fetch,
+                                             Form form) {
   const uint32_t rbase = tc::smem_u32(sR);
   const uint32_t idesc1 = tc::idesc_tf32(S::ROWS, S::N1), idesc1w = tc::idesc_tf32(S::ROWS, 2 * S::N1);
+  const bool warp0 = (threadIdx.x >> 5) == 0;
   bool ok = true;
   for (int ch = 0; ch < S::NCH; ++ch) {
     const int st = ch & 1;
     float2 vp[8], vh[8];
-    inputs(ch, vp, vh);
+    form(ch, raw, vp, vh);
+    if (ch + 1 < S::NCH) fetch(ch + 1, raw);
     // the stage is free once the MMAs of chunk ch - 2 are done; its next B1 chunk is then fetched
-    if (threadIdx.x == 0 && ch >= 2) {
+    if (warp0 && ch >= 2) {
       if (!bl.wait(2 + st, lim))
         *sflag = 1;
       else
@@ -226,9 +250,10 @@ __device__ __forceinline__ bool gemm1_chunks(BarLog& bl, float* sR, const float*
     }
     tc::fence_proxy_async();
     __syncthreads();
-    if (threadIdx.x == 0) {
-      if (!bl.wait(st, lim)) *sflag = 1;
-      if (!*sflag) {
+    if (warp0) {
+      const bool good = bl.wait(st, lim);  // the same in every lane of warp 0
+      if (!good) *sflag = 1;
+      if (good) {
         const uint32_t sa = rbase + (uint32_t)(st * S::STAGE) * 4u;
         for (int par = 0; par < 2; ++par) {
           const uint32_t a_hi = sa + (uint32_t)(par * S::ACH) * 4u;
@@ -242,7 +267,7 @@ __device__ __forceinline__ bool gemm1_chunks(BarLog& bl, float* sR, const float*
   }
   // the last chunk's commit covers every GEMM1 MMA
   if (ok) {
-    bool w = threadIdx.x == 0 ? bl.wait(2 + ((S::NCH - 1) & 1), lim) : true;
+    bool w = warp0 ? bl.wait(2 + ((S::NCH - 1) & 1), lim) : true;
     ok = __syncthreads_and(w);
     tc::fence_after_sync();
     ok = ok && !*sflag;
@@ -284,15 +309,15 @@ __device__ __forceinline__ void read_d1(uint32_t tbase, float* res, int ngroups,
 // GEMM2 over the four units u = 2 par + half (128 x 80 x K2 each) into D2
 // (TMEM columns [160 par, 160 par + 160)), B2 halves double-buffered (buffer
 // u % 2).  Unit 0's copy into buffer 0 was issued before the epilogue; buffer 1
-// (the D1 staging) is filled here.  Thread 0 only; false when a wait ran out.
+// (the D1 staging) is filled here.  Warp 0 only; false when a wait ran out.
 __device__ __forceinline__ bool gemm2_halves(BarLog& bl, float* const* buf, const float* mblock, uint32_t a2base,
                                              int a2_floats, uint32_t tbase, uint32_t lim) {
   const uint32_t idesc2 = tc::idesc_tf32(S::ROWS, S::N2H);
   auto unit_mma = [&](int u) {
     const uint32_t a2 = a2base + (uint32_t)(2 * (u >> 1) * a2_floats) * 4u;
     const uint32_t bh = tc::smem_u32(buf[u & 1]);
-    mma3(tbase + (uint32_t)((u >> 1) * S::N2 + (u & 1) * S::N2H), a2, a2 + (uint32_t)a2_floats * 4u, bh,
-         bh + S::N2H * S::K2 * 4u, S::K2, idesc2);
+    mma3<S::K2>(tbase + (uint32_t)((u >> 1) * S::N2 + (u & 1) * S::N2H), a2, a2 + (uint32_t)a2_floats * 4u, bh,
+                bh + S::N2H * S::K2 * 4u, idesc2);
     bl.commit(6 + (u & 1));
   };
   // issue u0, u1; refill each buffer with the same half of parity 1 once its MMAs are done; issue u2, u3
@@ -434,10 +459,49 @@ __global__ void __launch_bounds__(256, 1) k_spectral_tc106(const __grid_constant
   uint32_t* tslot = (uint32_t*)(mbar + BarLog::NB);
   int* sflag = (int*)(tslot + 1);
   int* sdead = sflag + 1;                  // [MT]
-  BarLog bl(mbar);                         // used by thread 0
+  BarLog bl(mbar);                         // used by warp 0
 
-  // ---- phase 0: barriers, the first two B1 chunks, TMEM; coefficients; blow-up gate
+  // chunk inputs of the thread: the 11 Fourier fields step_combos_ld reads
+  // (eta, delta, Phi, A..G) and the step factors at (member, j)
+  const ChunkLane cl;
+  struct Raw {
+    T2 v[11];
+    StepCoefs<T> kc;
+  } raw;
+  auto fetch = [&](int ch, Raw& r) {
+    const int jp = ch * S::CJ + cl.jl;
+    const int j = cl.side ? (J - 1 - jp) : jp;
+    if (cl.bt < mt) {
+      const int b = b0 + cl.bt;
+      const size_t o = ((size_t)m * G.B + b) * J + j;
+#pragma unroll
+      for (int q = 0; q < 11; ++q) r.v[q] = G.four[(size_t)field106(q) * FS + o];
+      r.kc = load_step_coefs<T>(G, b, j);
+    }
+  };
+  auto form = [&](int ch, const Raw& r, T2* vp, T2* vh) {
+    T2 c[NSLOT];
+    if (cl.bt < mt) {
+      const int jp = ch * S::CJ + cl.jl;
+      const int j = cl.side ? (J - 1 - jp) : jp;
+      step_combos_ld<T>(G, cfg, 0, incr, m, b0 + cl.bt, j, [&](int f) { return r.v[slot106(f)]; }, c, &r.kc);
+    } else {
+#pragma unroll
+      for (int q = 0; q < NSLOT; ++q) c[q] = mk<T2>(0, 0);
+    }
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) c[q] = mirror_sum(c[q], cl.side);
+#pragma unroll
+    for (int gq = 0; gq < 8; ++gq) {
+      vp[gq] = c[group_p106(gq)];
+      vh[gq] = group_h106(gq) >= 0 ? c[NSPX + group_h106(gq)] : mk<T2>(0, 0);
+    }
+  };
+
+  // ---- phase 0: barriers, the first two B1 chunks, TMEM; chunk 0's inputs;
+  // coefficients; blow-up gate
   setup_chunks(bl, sR, mblock, tslot, sflag);
+  fetch(0, raw);
   load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, CNT, sig, sigP, sigm1, sigPm1, tcmn);
   if (threadIdx.x < MT) {
     const int bt = threadIdx.x;
@@ -458,30 +522,8 @@ __global__ void __launch_bounds__(256, 1) k_spectral_tc106(const __grid_constant
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
 
-  // ---- phase 1: GEMM1 over the latitude chunks; the combined inputs of
-  // step_combos_ld at (member, j), read from the state in global memory
-  const ChunkLane cl;
-  bool ok = gemm1_chunks(bl, sR, mblock, tbase, sflag, basis.wait_limit, cl, [&](int ch, T2* vp, T2* vh) {
-    const int jp = ch * S::CJ + cl.jl;
-    const int j = cl.side ? (J - 1 - jp) : jp;
-    T2 c[NSLOT];
-    if (cl.bt < mt) {
-      const int b = b0 + cl.bt;
-      const size_t o = ((size_t)m * G.B + b) * J + j;
-      StepCoefs<T> kc = load_step_coefs<T>(G, b, j);
-      step_combos_ld<T>(G, cfg, 0, incr, m, b, j, [&](int f) { return G.four[(size_t)f * FS + o]; }, c, &kc);
-    } else {
-#pragma unroll
-      for (int q = 0; q < NSLOT; ++q) c[q] = mk<T2>(0, 0);
-    }
-#pragma unroll
-    for (int q = 0; q < NSLOT; ++q) c[q] = mirror_sum(c[q], cl.side);
-#pragma unroll
-    for (int gq = 0; gq < 8; ++gq) {
-      vp[gq] = c[group_p106(gq)];
-      vh[gq] = group_h106(gq) >= 0 ? c[NSPX + group_h106(gq)] : mk<T2>(0, 0);
-    }
-  });
+  // ---- phase 1: GEMM1 over the latitude chunks
+  bool ok = gemm1_chunks(bl, sR, mblock, tbase, sflag, basis.wait_limit, cl, raw, fetch, form);
 
   // post-GEMM1 layout
   float* sA2 = sR;
@@ -499,7 +541,7 @@ __global__ void __launch_bounds__(256, 1) k_spectral_tc106(const __grid_constant
   T wal[S::NWPAIR], wan[S::NWPAIR];
   if (ok) {
     // B2 (parity 0, column half 0) into buffer 0, overlapped with the epilogue
-    if (threadIdx.x == 0) bl.copy(4, buf[0], mblock + S::B1, B2_BYTES);
+    if (threadIdx.x < 32) bl.copy(4, buf[0], mblock + S::B1, B2_BYTES);
     // ---- phase 2: D1 -> staging sRes[g][n-m][member, re/im]; zero the A2 operands
     read_d1(tbase, sRes, 8, C0, C1);
     for (int i = threadIdx.x; i < 4 * S::A2; i += blockDim.x) sA2[i] = 0.f;
@@ -580,7 +622,7 @@ __global__ void __launch_bounds__(256, 1) k_spectral_tc106(const __grid_constant
         wan[k] = cfg.raw ? G.mco[MC_RAWN * G.B + b0 + wbt[k]] : (T)0;
       }
     }
-    if (threadIdx.x == 0 && !gemm2_halves(bl, buf, mblock, tc::smem_u32(sA2), S::A2, tbase, basis.wait_limit))
+    if (threadIdx.x < 32 && !gemm2_halves(bl, buf, mblock, tc::smem_u32(sA2), S::A2, tbase, basis.wait_limit))
       *sflag = 1;
     ok = __syncthreads_and(!*sflag);
     tc::fence_after_sync();
@@ -620,9 +662,9 @@ __global__ void __launch_bounds__(256, 1) k_spectral_tc106(const __grid_constant
       G.member[MS_WCURR * G.B + b] = wc;
       G.member[MS_UPDATED * G.B + b] = 1.0;
     }
-  } else if (threadIdx.x == 0) {
+  } else if (threadIdx.x < 32) {
     // a wait ran out: report, then drain (bounded) what this CTA issued before freeing TMEM
-    atomicExch(err, 1);
+    if (threadIdx.x == 0) atomicExch(err, 1);
     bl.drain();
   }
   tc::fence_before_sync();
@@ -676,31 +718,41 @@ __global__ void __launch_bounds__(256, 1) k_spectral_adj_tc106(const __grid_cons
   int* sflag = (int*)(tslot + 1);
   BarLog bl(mbar);
 
-  // ---- phase 0: barriers, the first two B1' chunks, TMEM; coefficients
+  // chunk inputs of the thread: lambda_Y of eta, delta, Phi, Uprep, Vprep at (member, j)
+  const ChunkLane cl;
+  struct Raw {
+    T2 y[5];
+  } raw;
+  auto fetch = [&](int ch, Raw& r) {
+    const int jp = ch * S::CJ + cl.jl;
+    const int j = cl.side ? (J - 1 - jp) : jp;
+    const size_t o = ((size_t)m * G.B + b0 + cl.bt) * J + j;
+#pragma unroll
+    for (int f = 0; f < 5; ++f) r.y[f] = cl.bt < mt ? G.lamY[(size_t)f * FS + o] : mk<T2>(0, 0);
+  };
+  // lambda_Y of eta, delta, Phi, Uprep, Vprep on the P columns, of U, V on the H columns
+  auto form = [&](int, const Raw& r, T2* vp, T2* vh) {
+    T2 y[5];
+#pragma unroll
+    for (int f = 0; f < 5; ++f) y[f] = mirror_sum(r.y[f], cl.side);
+#pragma unroll
+    for (int gq = 0; gq < 8; ++gq) {
+      vp[gq] = gq < 5 ? y[gq] : mk<T2>(0, 0);
+      vh[gq] = (gq == 5 || gq == 6) ? y[gq - 2] : mk<T2>(0, 0);
+    }
+  };
+
+  // ---- phase 0: barriers, the first two B1' chunks, TMEM; chunk 0's inputs; coefficients
   setup_chunks(bl, sR, mblock, tslot, sflag);
+  fetch(0, raw);
   load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, CNT, sig, sigP, sigm1, sigPm1, tcmn);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
 
-  // ---- phase 1: GEMM1' over the latitude chunks; lambda_Y of eta, delta, Phi,
-  // Uprep, Vprep on the P columns, of U, V on the H columns
-  const ChunkLane cl;
-  bool ok = gemm1_chunks(bl, sR, mblock, tbase, sflag, basis.wait_limit, cl, [&](int ch, T2* vp, T2* vh) {
-    const int jp = ch * S::CJ + cl.jl;
-    const int j = cl.side ? (J - 1 - jp) : jp;
-    const bool live = cl.bt < mt;
-    const size_t o = ((size_t)m * G.B + b0 + (live ? cl.bt : 0)) * J + j;
-    T2 y[5];
-#pragma unroll
-    for (int f = 0; f < 5; ++f) y[f] = mirror_sum(live ? G.lamY[(size_t)f * FS + o] : mk<T2>(0, 0), cl.side);
-#pragma unroll
-    for (int gq = 0; gq < 8; ++gq) {
-      vp[gq] = gq < 5 ? y[gq] : mk<T2>(0, 0);
-      vh[gq] = (gq == 5 || gq == 6) ? y[gq - 2] : mk<T2>(0, 0);
-    }
-  });
+  // ---- phase 1: GEMM1' over the latitude chunks
+  bool ok = gemm1_chunks(bl, sR, mblock, tbase, sflag, basis.wait_limit, cl, raw, fetch, form);
 
   float* sA2 = sR;
   float* sRes = sR + S::AOFF_RES;
@@ -714,7 +766,7 @@ __global__ void __launch_bounds__(256, 1) k_spectral_adj_tc106(const __grid_cons
   }
   AdjRowsIn<T> pin[S::NWPAIR];  // write-out inputs, loaded ahead of GEMM2'
   if (ok) {
-    if (threadIdx.x == 0) bl.copy(4, buf[0], mblock + S::B1, B2_BYTES);
+    if (threadIdx.x < 32) bl.copy(4, buf[0], mblock + S::B1, B2_BYTES);
     // ---- phase 2: D1' -> sRes[q][n-m][member, re/im] (7 groups); zero the A2' operands
     read_d1(tbase, sRes, 7, C0, C1);
     for (int i = threadIdx.x; i < 4 * S::AA2; i += blockDim.x) sA2[i] = 0.f;
@@ -767,7 +819,7 @@ __global__ void __launch_bounds__(256, 1) k_spectral_adj_tc106(const __grid_cons
 #pragma unroll
     for (int k = 0; k < S::NWPAIR; ++k)
       if (wbt[k] < mt) adj_load_rows<T>(G, incr, FS, ((size_t)m * G.B + b0 + wbt[k]) * J + wj[k], pin[k]);
-    if (threadIdx.x == 0 && !gemm2_halves(bl, buf, mblock, tc::smem_u32(sA2), S::AA2, tbase, basis.wait_limit))
+    if (threadIdx.x < 32 && !gemm2_halves(bl, buf, mblock, tc::smem_u32(sA2), S::AA2, tbase, basis.wait_limit))
       *sflag = 1;
     ok = __syncthreads_and(!*sflag);
     tc::fence_after_sync();
@@ -804,8 +856,8 @@ __global__ void __launch_bounds__(256, 1) k_spectral_adj_tc106(const __grid_cons
       for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
       if (lane == 0) atomicAdd(&G.grad[G_PHIBAR * G.B + b0 + warp], (double)acc);
     }
-  } else if (threadIdx.x == 0) {
-    atomicExch(err, 1);
+  } else if (threadIdx.x < 32) {
+    if (threadIdx.x == 0) atomicExch(err, 1);
     bl.drain();
   }
   tc::fence_before_sync();
