@@ -55,9 +55,9 @@ class Integration:
                  store: str = "auto", mem_fraction: float = 0.8):
         if flags.raw_filter:
             raise NotImplementedError("derivatives are implemented for the classic Robert-Asselin filter")
-        # the explicit and semi-implicit schemes have the tangent model but no
-        # adjoint: their gradients are per-parameter tangent runs (scalar parameters only)
-        self.tangent_only = flags.scheme in (1, 2)
+        # the semi-implicit scheme has the tangent model but no adjoint: its
+        # gradients are per-parameter tangent runs (scalar parameters only)
+        self.tangent_only = flags.scheme == 2
         if flags.test == 1:
             raise NotImplementedError("the adjoint of test=1 (fixed winds) is not implemented")
         if nsteps < 1:
@@ -134,8 +134,8 @@ class Integration:
     # ------------------------------------------------------------ backward
     def run_backward(self, dphys: Sequence[torch.Tensor]):
         if self.tangent_only:
-            raise NotImplementedError("the explicit and semi-implicit schemes have no adjoint (their parameter "
-                                      "gradients are tangent runs)")
+            raise NotImplementedError("the semi-implicit scheme has no adjoint (its parameter gradients are "
+                                      "tangent runs)")
         eng = self.eng
         lam, lamy, grad = eng.adjoint_buffers()
         eng.adjoint_seed(dphys, lam)
@@ -220,7 +220,7 @@ class _IntegrateFn(torch.autograd.Function):
         if integ.tangent_only:
             if any(ctx.needs_input_grad[1 + NF * g + NP] for g in range(len(eng.groups))):
                 raise NotImplementedError("gradients with respect to the initial fields need the adjoint, which the "
-                                          "explicit and semi-implicit schemes do not have")
+                                          "semi-implicit scheme does not have")
             first_extra = 0
         else:
             dic, grad = integ.run_backward(dphys)

@@ -608,7 +608,7 @@ int winds_impl(swp_plan* p, const swp_group_state* st, void* const* ed, void* co
 
 // `sweep`: the step is one of an adjoint sweep, whose lambda always comes from
 // the Legendre adjoint (or the seed), so the grid adjoint may use its tied
-// F / G components.
+// F / G components (modified Euler; the explicit scheme's are not tied).
 template <typename T>
 int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
                       const swp_group_adjoint* adj, const swp_flags* f, int t, cudaStream_t s,
@@ -621,7 +621,7 @@ int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group
   GridLaunch<T> LG = make_grid<T>(p, st_out, nbg);
   LG.mode = GM_ADJ_STEP;
   LG.cfg = make_cfg(f);
-  LG.cfg.lam_fg_tied = (sweep && f->forcflag && f->test == 0) ? 1 : 0;
+  LG.cfg.lam_fg_tied = (sweep && f->forcflag && f->test == 0 && f->scheme == 0) ? 1 : 0;
   for (int g = 0; g < p->ng; ++g) {
     LG.grp[g].primal = (const typename cplx<T>::type*)st_out[g].fourier;
     LG.grp[g].lam = (typename cplx<T>::type*)adj[g].lam;
@@ -737,7 +737,7 @@ int time_kernels_impl(swp_plan* p, const swp_group_state* st, const swp_group_ad
   GridLaunch<T> LGa = LG;
   SpecLaunch<T> LSa = LS;
   LGa.mode = GM_ADJ_STEP;
-  LGa.cfg.lam_fg_tied = (f->forcflag && f->test == 0) ? 1 : 0;  // as inside an adjoint sweep
+  LGa.cfg.lam_fg_tied = (f->forcflag && f->test == 0 && f->scheme == 0) ? 1 : 0;  // as inside an adjoint sweep
   if (adj) {
     for (int g = 0; g < p->ng; ++g) {
       LGa.grp[g].primal = LG.grp[g].four;
@@ -997,14 +997,16 @@ static int check_align(swp_plan* p, const swp_group_state* st, const swp_group_a
 }
 
 // Scheme switches every stepping entry checks (model.py:1531-1537).  The
-// adjoint and the tangent cover the modified-Euler scheme with the classic filter.
+// adjoint covers the modified-Euler and explicit schemes with the classic filter.
 int check_scheme(swp_plan* p, const swp_flags* f, bool adjoint) {
   if (f->scheme < 0 || f->scheme > 2) return fail(p, SWP_ERR_ARG, "scheme must be 0, 1 or 2");
   if (f->test < 0 || f->test > 2) return fail(p, SWP_ERR_ARG, "test must be 0 (None), 1 or 2");
   if (f->raw_filter && f->scheme == 1)
     return fail(p, SWP_ERR_ARG, "raw_filter is incompatible with the explicit scheme");
-  if (adjoint && f->scheme != 0)
-    return fail(p, SWP_ERR_UNSUPPORTED, "derivatives (adjoint, tangent) are implemented for the modified-Euler scheme");
+  if (adjoint && f->scheme == 2)
+    return fail(p, SWP_ERR_UNSUPPORTED,
+                "the adjoint is implemented for the modified-Euler and explicit schemes (the semi-implicit scheme "
+                "differentiates by tangent runs)");
   if (adjoint && f->raw_filter)
     return fail(p, SWP_ERR_UNSUPPORTED,
                 "derivatives (adjoint, tangent) are implemented for the classic Robert-Asselin filter");

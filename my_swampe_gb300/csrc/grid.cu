@@ -760,6 +760,22 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     for (int f = 0; f < 5; ++f) { src2[f] = G.lam + cf[f] * FS; s20[f] = invI; s21[f] = invI * (T)0.5; }
     stage_rows<T>(c, src2, 5, bufB, s20, s21);
     __syncthreads();
+    // the initial state also sets the Fourier prev and mid carries of eta,
+    // delta, Phi to curr (GM_INIT): their adjoints add to curr's (nonzero for
+    // the explicit scheme, whose steps read the prev level)
+    {
+      constexpr int n1 = M + 1;
+      for (int t = threadIdx.x; t < 3 * n1 * JB; t += blockDim.x) {
+        const int r = t % JB, k = (t / JB) % n1, f = t / (JB * n1);
+        const size_t o = ((size_t)k * B + b) * J + j0 + r;
+        const int pf = f == 0 ? F_ETA_PREV : f == 1 ? F_DELTA_PREV : F_PHI_PREV;
+        const int mf = f == 0 ? F_ETA_MID : f == 1 ? F_DELTA_MID : F_PHI_MID;
+        const T2 add = cadd(G.lam[pf * FS + o], G.lam[mf * FS + o]);
+        T2& dst = bufB[(f * JB + r) * n1 + k];
+        dst = cadd(dst, cscale(add, k == 0 ? s20[f] : s21[f]));
+      }
+    }
+    __syncthreads();
     T2* z2 = c2r_transform<T>(c, bufB, 5, bufA);
     for (int t = threadIdx.x; t < 5 * JB * L; t += blockDim.x) {
       int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;

@@ -568,19 +568,34 @@ __device__ __forceinline__ void step_residual_weights(const StepCfg& cfg, double
 
 // ----------------------------------------------------------------- adjoint
 // Global values the adjoint write-out of one (m, member, latitude) point
-// reads: the adjoint of the step's curr outputs (incremental form) and the
-// primal inputs of the Phibar gradient.  Loaded ahead of the stores.
+// reads, loaded ahead of the stores:
+//   modified Euler: the adjoint of the step's curr outputs (incremental form)
+//   and the primal delta, Phi, E, A, B, F, G (Phibar gradient);
+//   explicit leapfrog: the adjoint of the Fourier prev level after the step
+//   (the step moves curr there), and the primal curr delta, U, V (Phibar and
+//   taudrag gradients).
 template <typename T>
 struct AdjPointIn {
-  typename cplx<T>::type ly[3];  // lamY eta, delta, Phi
-  typename cplx<T>::type px[7];  // primal delta, Phi, E, A, B, F, G
+  typename cplx<T>::type ly[3];  // lamY eta, delta, Phi | lambda eta, delta, Phi prev (explicit)
+  typename cplx<T>::type px[7];  // primal delta, Phi, E, A, B, F, G | delta, U, V (explicit)
 };
 
 template <typename T>
-__device__ __forceinline__ void adj_load_point(const SpecGroup<T>& G, bool incr, size_t FS, size_t o,
-                                               AdjPointIn<T>& in) {
+__device__ __forceinline__ void adj_load_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
+                                               size_t o, AdjPointIn<T>& in) {
   typedef typename cplx<T>::type T2;
   const T2 z = mk<T2>(0, 0);
+  if (cfg.scheme == 1) {
+    const int lf[3] = {F_ETA_PREV, F_DELTA_PREV, F_PHI_PREV};
+    const int pf[3] = {F_DELTA, F_U, F_V};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) in.ly[q] = G.lam[lf[q] * FS + o];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) in.px[q] = G.grad ? G.four[pf[q] * FS + o] : z;
+#pragma unroll
+    for (int q = 3; q < 7; ++q) in.px[q] = z;
+    return;
+  }
 #pragma unroll
   for (int q = 0; q < 3; ++q) in.ly[q] = incr ? G.lamY[q * FS + o] : z;
   const int pf[7] = {F_DELTA, F_PHI, F_E, F_A, F_B, F_F, F_G};
@@ -658,11 +673,84 @@ __device__ __forceinline__ T adj_point_values(const SpecGroup<T>& G, const StepC
          lPhiP2.y * dP2.y + ldP2.x * dd2.x + ldP2.y * dd2.y;
 }
 
-// adj_point_values written to G.lam at offset o of one point.
+// Transposed combination of the explicit leapfrog (adjoint of step_combos
+// scheme 1; explicit_tdiff.py:62-78, 134-155, 207-226) at one point.  The step
+// reads the Fourier prev level (eta0, delta0, Phi0), curr delta, A..D, PhiF,
+// F, G, U, V, and moves curr into prev (the unfiltered Fourier carry,
+// model.py:1107-1110); so the adjoint of the state before the step is
+//   prev: from the P slots directly;  curr: the adjoint of prev after the step
+//   (in.ly), plus -2 dt Phibar lambda_PhiP1 on delta;  U, V, A..D, PhiF, F, G:
+//   from the slots;  E and the mid carries: zero.
+// lv takes the 16 written fields in adj_field_ex order.  Returns this point's
+// dL/dPhibar term and adds its dL/dtaudrag term to gtd.
+__host__ __device__ constexpr int adj_field_ex(int q) {
+  return q == 0 ? F_ETA_PREV : q == 1 ? F_DELTA_PREV : q == 2 ? F_PHI_PREV : q == 3 ? F_ETA : q == 4 ? F_DELTA
+       : q == 5 ? F_PHI : q == 6 ? F_U : q == 7 ? F_V : q == 8 ? F_A : q == 9 ? F_B : q == 10 ? F_C
+       : q == 11 ? F_D : q == 12 ? F_E : q == 13 ? F_PHIF : q == 14 ? F_F : F_G;
+}
+template <typename T, int NK, typename LD>
+__device__ __forceinline__ T adj_point_values_ex(const SpecGroup<T>& G, const StepCfg& cfg, int m, int b, int j,
+                                                 LD ld, const AdjPointIn<T>& in, typename cplx<T>::type (&lv)[16],
+                                                 T& gtd) {
+  typedef typename cplx<T>::type T2;
+  const T2 lP1 = ld(0), ldP1 = ld(2), leP1 = ld(4);
+  const T2 lPH1 = ld(NK), ldH1 = ld(NK + 1), leH1 = ld(NK + 3);
+  const T* mc = G.mco;
+  const int B = G.B;
+  const T t = G.jco[(size_t)b * G.g.J + j];
+  const T itd = mc[MC_ITD * B + b];
+  const T xm = (T)m;
+  const T forc = cfg.forcflag ? (T)1 : (T)0;
+  const T2 z = mk<T2>(0, 0);
+  // conj(i alpha m) z = -i alpha m z
+  auto mimul = [&](T alpha, T2 v) { return imul(-alpha * xm, v); };
+  const T2 ldel1 = cscale(lP1, -mc[MC_2DTPB * B + b]);
+  lv[0] = leP1;                                    // eta0 (prev)
+  lv[1] = ldP1;                                    // delta0
+  lv[2] = lP1;                                     // Phi0
+  lv[3] = in.ly[0];                                // curr eta -> prev after the step
+  lv[4] = cadd(in.ly[1], ldel1);                   // curr delta: carry and -2 dt Phibar delta1
+  lv[5] = in.ly[2];                                // curr Phi
+  lv[6] = cscale(cadd(mimul(-t * itd, ldP1), cscale(leH1, t * itd)), forc);  // U
+  lv[7] = cscale(cadd(cscale(ldH1, t * itd), mimul(-t * itd, leP1)), forc);  // V
+  lv[8] = mimul(-t, leP1);                         // A
+  lv[9] = cscale(leH1, t);                         // B
+  lv[10] = mimul(-t, lP1);                         // C
+  lv[11] = cscale(lPH1, t);                        // D
+  lv[12] = z;                                      // E
+  lv[13] = cscale(lP1, forc * mc[MC_2DT * B + b]); // PhiF
+  lv[14] = cscale(cadd(mimul(t, ldP1), cscale(leH1, t)), forc);    // F
+  lv[15] = cscale(cadd(cscale(ldH1, -t), mimul(t, leP1)), forc);   // G
+  if (!G.grad) return (T)0;
+  const T2 del1 = in.px[0], U = in.px[1], V = in.px[2];
+  // d(slots)/d(1/taudrag): dP1 -t (i m U), dH1 t V, eP1 -t (i m V), eH1 t U; d(1/taudrag)/dtaudrag = -itd^2
+  const T2 dP1 = cscale(imul(xm, U), -t), dH1 = cscale(V, t), eP1 = cscale(imul(xm, V), -t), eH1 = cscale(U, t);
+  const T s_itd = ldP1.x * dP1.x + ldP1.y * dP1.y + ldH1.x * dH1.x + ldH1.y * dH1.y + leP1.x * eP1.x +
+                  leP1.y * eP1.y + leH1.x * eH1.x + leH1.y * eH1.y;
+  gtd += -forc * itd * itd * s_itd;
+  // d(PhiP1)/dPhibar = -2 dt delta1
+  const T tdt = mc[MC_2DT * B + b];
+  return -tdt * (lP1.x * del1.x + lP1.y * del1.y);
+}
+
+// adj_point_values (modified Euler) or adj_point_values_ex (explicit) written
+// to G.lam at offset o of one point.  Returns the point's dL/dPhibar term and
+// adds its dL/dtaudrag term (explicit scheme) to gtd.
 template <typename T, int NK, typename LD>
 __device__ __forceinline__ T adj_store_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
-                                             size_t o, int m, int b, int j, LD ld, const AdjPointIn<T>& in) {
+                                             size_t o, int m, int b, int j, LD ld, const AdjPointIn<T>& in,
+                                             T& gtd) {
   typedef typename cplx<T>::type T2;
+  if (cfg.scheme == 1) {
+    T2 lv[16];
+    const T gp = adj_point_values_ex<T, NK>(G, cfg, m, b, j, ld, in, lv, gtd);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) G.lam[adj_field_ex(q) * FS + o] = lv[q];
+    G.lam[F_ETA_MID * FS + o] = mk<T2>(0, 0);
+    G.lam[F_DELTA_MID * FS + o] = mk<T2>(0, 0);
+    G.lam[F_PHI_MID * FS + o] = mk<T2>(0, 0);
+    return gp;
+  }
   T2 lv[11];
   const T gp = adj_point_values<T, NK>(G, cfg, incr, m, b, j, ld, in, lv);
 #pragma unroll

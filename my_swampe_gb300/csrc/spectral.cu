@@ -546,7 +546,7 @@ size_t spec_adj_smem_bytes(int M, int J, int MT) {
   size_t sres = (size_t)NYS * cnt * R;
   size_t kad = (size_t)NK * cnt * R;
   size_t coef = (size_t)5 * MT * cnt;
-  return (x + bf + sres + kad + coef) * sizeof(T) + 16 + (size_t)MT * (J / 32) * sizeof(double);
+  return (x + bf + sres + kad + coef) * sizeof(T) + 16 + (size_t)2 * MT * (J / 32) * sizeof(double);
 }
 template size_t spec_adj_smem_bytes<double>(int, int, int);
 template size_t spec_adj_smem_bytes<float>(int, int, int);
@@ -581,13 +581,13 @@ __device__ __forceinline__ void spectral_adj_unit(const SpecLaunch<T>& L, const 
   T* sigm1 = sigP + MT * cntmax;
   T* sigPm1 = sigm1 + MT * cntmax;
   T* tcmn = sigPm1 + MT * cntmax;
-  // [MT][J/32] Phibar gradient partials of each warp-sized run of latitudes
-  // (doubles: round the address up to 16 bytes)
+  // [2][MT][J/32] Phibar and taudrag gradient partials of each warp-sized run
+  // of latitudes (doubles: round the address up to 16 bytes)
   double* sgrad = (double*)(((uintptr_t)(tcmn + MT * cntmax) + 15) & ~(uintptr_t)15);
   const int nws = J / 32;
 
   load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, cntmax, sig, sigP, sigm1, sigPm1, tcmn);
-  for (int t = threadIdx.x; t < MT * nws; t += blockDim.x) sgrad[t] = 0.0;
+  for (int t = threadIdx.x; t < 2 * MT * nws; t += blockDim.x) sgrad[t] = 0.0;
 
   // ---- phase 1: symmetrised adjoints of the step outputs at column m
   const T2* LY = G.lamY;  // [5][M+1][B][J]
@@ -785,21 +785,33 @@ __device__ __forceinline__ void spectral_adj_unit(const SpecLaunch<T>& L, const 
     size_t o = ((size_t)m * G.B + b) * J + j;
     auto ld = [&](int q) { return mk<T2>(Cad[(((size_t)q * MT + bt) * J + j) * 2], Cad[(((size_t)q * MT + bt) * J + j) * 2 + 1]); };
     AdjPointIn<T> in;
-    adj_load_point<T>(G, incr, FS, o, in);
-    T gp = adj_store_point<T, NKADJ>(G, cfg, incr, FS, o, m, b, j, ld, in);
+    adj_load_point<T>(G, cfg, incr, FS, o, in);
+    T gtd = (T)0;
+    T gp = adj_store_point<T, NKADJ>(G, cfg, incr, FS, o, m, b, j, ld, in, gtd);
     if (G.grad) {
       // J is a multiple of 32, so a warp holds one member: reduce over the warp
       // in the compute type, accumulate the warp sums in FP64
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) gp += __shfl_xor_sync(0xffffffffu, gp, off);
-      if ((threadIdx.x & 31) == 0) sgrad[bt * nws + j / 32] = (double)gp;
+      for (int off = 16; off > 0; off >>= 1) {
+        gp += __shfl_xor_sync(0xffffffffu, gp, off);
+        gtd += __shfl_xor_sync(0xffffffffu, gtd, off);
+      }
+      if ((threadIdx.x & 31) == 0) {
+        sgrad[bt * nws + j / 32] = (double)gp;
+        sgrad[(MT + bt) * nws + j / 32] = (double)gtd;
+      }
     }
   }
   __syncthreads();
   if (G.grad && threadIdx.x < mt) {
-    double acc = 0.0;
-    for (int w = 0; w < nws; ++w) acc += sgrad[threadIdx.x * nws + w];
+    double acc = 0.0, acd = 0.0;
+    for (int w = 0; w < nws; ++w) {
+      acc += sgrad[threadIdx.x * nws + w];
+      acd += sgrad[(MT + threadIdx.x) * nws + w];
+    }
     atomicAdd(&G.grad[G_PHIBAR * G.B + b0 + threadIdx.x], acc);
+    // the explicit scheme's own drag terms (modified Euler: its drag is the grid physics')
+    if (cfg.scheme == 1) atomicAdd(&G.grad[G_TAUDRAG * G.B + b0 + threadIdx.x], acd);
   }
 }
 

@@ -450,7 +450,7 @@ def run_model_scan(
     needs_grad = any(_tracked(x) for x in diff_inputs)
     if _tracked(williams_alpha):
         raise NotImplementedError("derivatives through the RAW filter are not implemented")
-    tangent_only = bool(semi_implicit or expflag)  # schemes differentiated by tangent runs (no adjoint)
+    tangent_only = bool(semi_implicit)  # the scheme differentiated by tangent runs (no adjoint)
     if needs_grad:
         if raw_filter or test == 1:
             raise NotImplementedError("derivatives are implemented with the classic filter and test None or 2")
@@ -458,7 +458,7 @@ def run_model_scan(
             raise NotImplementedError("derivatives with respect to eta0_init / delta0_init need U0_init and V0_init")
         if tangent_only and torch.is_grad_enabled() and any(torch.is_tensor(x) and x.requires_grad for x in ic_inputs):
             raise NotImplementedError("reverse-mode gradients with respect to the initial fields need the adjoint, "
-                                      "which the explicit and semi-implicit schemes do not have (forward mode works)")
+                                      "which the semi-implicit scheme does not have (forward mode works)")
 
     eng = _engine_for(M, B, precision, device)
     dev = eng.device
@@ -489,8 +489,8 @@ def run_model_scan(
         # the analytic fields are polynomials of degree <= 2 in a, omega, Phibar
         # (initial_conditions.py:18-47, 88-239), so a centred difference is their
         # exact derivative: carry it into the differentiable run
-        # (the explicit and semi-implicit schemes, which differentiate by tangent
-        # runs, take them as initial-field tangents of the parameter directions)
+        # (the semi-implicit scheme, which differentiates by tangent runs, takes
+        # them as initial-field tangents of the parameter directions)
         for x, i, name in ((a, 0, "a"), (omega, 1, "omega"), (Phibar, 2, "Phibar")):
             if _tracked(x):
                 h = 1e-3 * abs((av, omv, pb)[i]) or 1e-3
@@ -500,7 +500,7 @@ def run_model_scan(
                 arg[i] -= 2 * h
                 fm = _analytic_ic(M, *arg, test, float(a1), dev)
                 d = [(u - v) / (2 * h) for u, v in zip(fp, fm)]
-                if semi_implicit or expflag:
+                if semi_implicit:
                     ic_derivs[name] = torch.stack([dd.expand(B, J, I) for dd in d], 0)
                     continue
                 dx = x - x.detach()

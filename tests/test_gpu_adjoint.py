@@ -28,7 +28,7 @@ def _case(M=42, seed=0):
     return params, (eta0, delta0, Phi0, U0, V0), W
 
 
-def _gpu_grads(params, ics, W, nsteps, ckpt_every, M=42, precision="fp64", store="checkpoint"):
+def _gpu_grads(params, ics, W, nsteps, ckpt_every, M=42, precision="fp64", store="checkpoint", scheme=0):
     import torch
     from my_swampe_gb300.engine import Engine, RunFlagsC
     from my_swampe_gb300.adjoint import integrate
@@ -40,7 +40,7 @@ def _gpu_grads(params, ics, W, nsteps, ckpt_every, M=42, precision="fp64", store
     p = {k: torch.tensor([params[k]], dtype=torch.float64, device=dev, requires_grad=True)
          for k in ("taurad", "taudrag", "DPhieq", "Phibar")}
     ic = torch.tensor(np.stack(ics)[:, None], dtype=torch.float64, device=dev, requires_grad=True)
-    out = integrate(eng, RunFlagsC(), t0=2, nsteps=nsteps, params=[p], ics=[ic], ckpt_every=ckpt_every,
+    out = integrate(eng, RunFlagsC(scheme=scheme), t0=2, nsteps=nsteps, params=[p], ics=[ic], ckpt_every=ckpt_every,
                     store=store)[0]
     Wt = torch.tensor(W[:, None], dtype=torch.float64, device=dev)
     loss = (out.double() * Wt).sum()
@@ -48,7 +48,7 @@ def _gpu_grads(params, ics, W, nsteps, ckpt_every, M=42, precision="fp64", store
     return float(loss.detach()), {k: float(v.grad[0]) for k, v in p.items()}, ic.grad[:, 0].cpu().numpy()
 
 
-def _oracle_grads(params, ics, W, nsteps, M=42):
+def _oracle_grads(params, ics, W, nsteps, M=42, expflag=False):
     import torch
 
     xp = o.torch_backend()
@@ -57,7 +57,7 @@ def _oracle_grads(params, ics, W, nsteps, M=42):
     r = o.run_model_scan_final(xp, M=M, dt=params["dt"], tmax=2 + nsteps, Phibar=p["Phibar"], omega=params["omega"],
                                a=params["a"], test=None, taurad=p["taurad"], taudrag=p["taudrag"], DPhieq=p["DPhieq"],
                                K6=params["K6"], eta0_init=ic[0], delta0_init=ic[1], Phi0_init=ic[2], U0_init=ic[3],
-                               V0_init=ic[4])["last_state"]
+                               V0_init=ic[4], expflag=expflag)["last_state"]
     outs = [r[f + "_curr"] for f in ("eta", "delta", "Phi", "U", "V")]
     loss = sum((x * torch.tensor(W[k])).sum() for k, x in enumerate(outs))
     loss.backward()
@@ -78,6 +78,26 @@ def test_adjoint_matches_torch_autograd_through_oracle(cuda):
         assert err <= 1e-8 * scale, (f, err, scale)
 
 
+@pytest.mark.parametrize("store", ["checkpoint", "all"])
+def test_explicit_adjoint_matches_torch_autograd_through_oracle(cuda, store):
+    """The explicit leapfrog's hand-written adjoint (transposed combination of
+    explicit_tdiff.py, the Fourier prev carry, its own drag terms in the taudrag
+    gradient) against torch autograd through the oracle's expflag path: the
+    loss, the four parameter gradients and the initial-field gradients."""
+    params, ics, W = _case(seed=5)
+    params = dict(params, dt=300.0)
+    nsteps = 5
+    lg, pg, icg = _gpu_grads(params, ics, W, nsteps, ckpt_every=3, store=store, scheme=1)
+    lo, po, ico = _oracle_grads(params, ics, W, nsteps, expflag=True)
+    assert abs(lg - lo) <= 1e-9 * abs(lo)
+    for k in po:
+        assert abs(pg[k] - po[k]) <= 1e-7 * max(abs(po[k]), 1e-300), (k, pg[k], po[k])
+    for f in range(5):
+        scale = np.max(np.abs(ico[f]))
+        err = np.max(np.abs(icg[f] - ico[f]))
+        assert err <= 1e-8 * scale, (f, err, scale)
+
+
 def test_adjoint_checkpoint_window_invariance(cuda):
     params, ics, W = _case(seed=1)
     ref = _gpu_grads(params, ics, W, 7, ckpt_every=7)
@@ -88,23 +108,26 @@ def test_adjoint_checkpoint_window_invariance(cuda):
         np.testing.assert_allclose(got[2], ref[2], rtol=0, atol=1e-12 * np.max(np.abs(ref[2])))
 
 
-def test_param_gradients_match_central_fd(cuda):
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_param_gradients_match_central_fd(cuda, scheme):
     """unit_tests/test_autodiff.py:102-129 style central differences of the GPU
     forward.  With h = 1e-6 relative the difference quotient is limited by the
     forward's own round-off (~1e-10 per grid value, summed over 40k values),
     so it is checked to 5e-3; with h = 1e-4 relative (truncation error ~h^2)
-    it is checked to 2e-5."""
+    it is checked to 2e-5.  Scheme 1 is the explicit leapfrog (dt = 300 s)."""
     import torch
     from my_swampe_gb300.engine import Engine, RunFlagsC
 
     params, ics, W = _case(seed=2)
+    if scheme == 1:
+        params = dict(params, dt=300.0)
     nsteps = 6
-    _, pg, _ = _gpu_grads(params, ics, W, nsteps, ckpt_every=4)
+    _, pg, _ = _gpu_grads(params, ics, W, nsteps, ckpt_every=4, scheme=scheme)
     eng = Engine([(42, 2)], "fp64")
     eng.set_params(0, dt=params["dt"], a=params["a"], omega=params["omega"], K6=params["K6"], K6Phi=params["K6"], alpha=0.01)
     Wt = torch.tensor(W, device=eng.device)
     ic = torch.tensor(np.stack(ics)[:, None], dtype=torch.float64, device=eng.device).expand(5, 2, *W.shape[1:]).contiguous()
-    flags = RunFlagsC()
+    flags = RunFlagsC(scheme=scheme)
     for k in ("taurad", "taudrag", "DPhieq", "Phibar"):
         assert pg[k] != 0.0
         for rel_h, tol in ((1e-6, 5e-3), (1e-4, 2e-5)):

@@ -208,7 +208,7 @@ def test_semi_implicit_phibar_gradient_with_analytic_test2_initial_condition(cud
 
 
 def test_explicit_scheme_grad_matches_finite_differences(cuda):
-    """expflag=True: gradients through tangent runs (the explicit scheme has no adjoint)."""
+    """expflag=True: reverse mode through the explicit scheme's adjoint."""
     def loss(d):
         return _loss("DPhieq", d, expflag=True, dt=300.0)
 
@@ -217,3 +217,33 @@ def test_explicit_scheme_grad_matches_finite_differences(cuda):
     with torch.no_grad():
         fd = (float(loss(4.0e6 + 1.0)) - float(loss(4.0e6 - 1.0))) / 2.0
     assert g != 0.0 and abs(g - fd) <= 1e-4 * abs(fd), (g, fd)
+
+
+def test_explicit_scheme_initial_field_gradient_matches_finite_differences(cuda):
+    """expflag=True: the gradient in Phi0_init (explicit ICs with winds) from the
+    adjoint, along a random direction, against a central difference."""
+    from my_swampe_gb300 import run_model_scan_final
+    from oracle import swampe_oracle as o
+
+    geo = o.cached_geometry(42)
+    J, I = geo["J"], geo["I"]
+    mu = torch.tensor(geo["mus"], dtype=torch.float64, device="cuda")[:, None]
+    rng = np.random.default_rng(11)
+    eta0 = (2 * 7.292e-5 * mu).expand(J, I).contiguous()
+    Phi0 = torch.tensor(3e3 * rng.standard_normal((J, I)), dtype=torch.float64, device="cuda")
+    U0 = (10.0 * torch.sqrt(1 - mu**2)).expand(J, I).contiguous()
+    z = torch.zeros((J, I), dtype=torch.float64, device="cuda")
+    kw = dict(BASE, expflag=True, dt=300.0, eta0_init=eta0, delta0_init=z, U0_init=U0, V0_init=z)
+
+    def loss(p):
+        Phi = run_model_scan_final(**kw, Phi0_init=p)["last_state"].Phi_curr
+        return torch.mean(Phi * Phi)
+
+    th = Phi0.clone().requires_grad_(True)
+    g = torch.autograd.grad(loss(th), th)[0]
+    v = torch.tensor(rng.standard_normal((J, I)), dtype=torch.float64, device="cuda")
+    h = 1e-2
+    with torch.no_grad():
+        fd = (float(loss(Phi0 + h * v)) - float(loss(Phi0 - h * v))) / (2 * h)
+    ad = float((g * v).sum())
+    assert abs(ad - fd) <= 1e-6 * abs(fd), (ad, fd)

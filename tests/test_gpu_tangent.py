@@ -131,11 +131,15 @@ def test_coefficient_gradients_by_reverse_mode(cuda):
         assert abs(float(gk.sum()) - fd) <= 1e-3 * abs(fd), (k, float(gk.sum()), fd)
 
 
-def test_tangent_adjoint_dot_product(cuda):
-    """<w, J v> from the tangent model equals <J^T w, v> from the adjoint (FP64)."""
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_tangent_adjoint_dot_product(cuda, scheme):
+    """<w, J v> from the tangent model equals <J^T w, v> from the adjoint (FP64),
+    for the modified-Euler and the explicit scheme."""
     from my_swampe_gb300 import adjoint
+    from my_swampe_gb300.engine import RunFlagsC
 
     eng, flags, wl, ics, dics, dpar = _setup()
+    flags = RunFlagsC(scheme=scheme, diagnostics=False, t_start=2)
     p = wl["params"]
     names = ("taurad", "taudrag", "DPhieq", "Phibar")
     base = {k: (p[k] if torch.is_tensor(p[k]) else torch.full((2,), float(p[k]), dtype=torch.float64,
