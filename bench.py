@@ -393,7 +393,7 @@ def run_ours(args):
                       "h2d_bytes_per_step": int(di_h2d), "d2h_bytes_per_step": int(di_d2h),
                       "ms_per_step": round(1e3 * di_t, 3),
                       "api": "my_swampe_gb300.run_model_scan_final (differentiable) + torch.autograd backward, "
-                             "one group of B members"}
+                             "B members (run as two concurrent halves)"}
         del step_dropin
         torch.cuda.empty_cache()
     # ---------------- fast path with the FP64 run's state policy (checkpoints + recompute),
