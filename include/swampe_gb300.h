@@ -166,9 +166,10 @@ int swp_output_physical(swp_plan* plan, const swp_group_state* st, void* const* 
  * (same layout as st[g].fourier).  dir = 0: state -> ckpt, 1: ckpt -> state. */
 int swp_state_copy(swp_plan* plan, const swp_group_state* st, void* const* ckpt, int dir, void* stream);
 
-/* Adjoint of one step t (modified Euler or explicit leapfrog, forced or
- * unforced, diagnostics off; the semi-implicit scheme and the RAW filter are
- * SWP_ERR_UNSUPPORTED).
+/* Adjoint of one step t (modified Euler, explicit or semi-implicit leapfrog,
+ * forced or unforced, diagnostics off; the RAW filter is SWP_ERR_UNSUPPORTED).
+ * The semi-implicit step propagates the state's adjoint only: its parameter
+ * gradients are not accumulated (take them from tangent runs).
  * On entry adj[g].lam holds the adjoint of the state after the step; primal
  * st_in[g] is the state before the step and st_out[g] the state after it.
  * On exit adj[g].lam holds the adjoint of the state before the step and
@@ -283,7 +284,7 @@ int swp_plan_set_tile(swp_plan* plan, int g, int mt);
  * race on it.  Nothing in it needs to start at zero: each call overwrites the
  * part it reads.  The argument checks are those of swp_adjoint_step (lam_y
  * aside): a missing lam or Fourier buffer is SWP_ERR_ARG, a RAW-filtered,
- * semi-implicit, test 1 or diagnostics run SWP_ERR_UNSUPPORTED. */
+ * test 1 or diagnostics run SWP_ERR_UNSUPPORTED. */
 int swp_adjoint_step_noalloc(swp_plan* plan, const swp_group_state* st_in, const swp_group_state* st_out,
                              const swp_group_adjoint* adj, const swp_flags* flags, int t, void* stream);
 

@@ -55,9 +55,9 @@ class Integration:
                  store: str = "auto", mem_fraction: float = 0.8):
         if flags.raw_filter:
             raise NotImplementedError("derivatives are implemented for the classic Robert-Asselin filter")
-        # the semi-implicit scheme has the tangent model but no adjoint: its
-        # gradients are per-parameter tangent runs (scalar parameters only)
-        self.tangent_only = flags.scheme == 2
+        # the semi-implicit scheme's adjoint propagates the state (initial-field
+        # gradients); its parameter gradients are per-parameter tangent runs
+        self.param_tangents = flags.scheme == 2
         if flags.test == 1:
             raise NotImplementedError("the adjoint of test=1 (fixed winds) is not implemented")
         if nsteps < 1:
@@ -76,9 +76,7 @@ class Integration:
         self.ic_derivs = [{} for _ in engine.groups]
         if store not in ("auto", "all", "checkpoint"):
             raise ValueError(f"store must be 'auto', 'all' or 'checkpoint', got {store!r}")
-        if self.tangent_only:
-            store = "checkpoint"  # nothing is kept: the backward runs tangent runs from the initial fields
-        elif store == "auto":
+        if store == "auto":
             need = (self.nsteps + 1) * engine.state_bytes()
             free, _ = torch.cuda.mem_get_info(engine.device)
             # memory torch's caching allocator holds but no tensor uses (e.g. the
@@ -98,9 +96,6 @@ class Integration:
         eng = self.eng
         self.ics = [x.to(device=eng.device, dtype=eng.rdtype).contiguous() for x in ics]
         eng.init_state(self.ics, self.flags)
-        if self.tangent_only:
-            eng.forward(self.flags, self.t0, self.nsteps)
-            return [o[:5] for o in eng.output_physical(self.flags)]
         if self.store == "all":
             if self._states is None:
                 self._states = [torch.empty((self.nsteps + 1,) + tuple(gd["fourier"].shape), dtype=eng.cdtype,
@@ -133,9 +128,8 @@ class Integration:
 
     # ------------------------------------------------------------ backward
     def run_backward(self, dphys: Sequence[torch.Tensor]):
-        if self.tangent_only:
-            raise NotImplementedError("the semi-implicit scheme has no adjoint (its parameter gradients are "
-                                      "tangent runs)")
+        """The adjoint sweep: initial-field gradients and (modified Euler,
+        explicit) the gradients in taurad, taudrag, DPhieq, Phibar."""
         eng = self.eng
         lam, lamy, grad = eng.adjoint_buffers()
         eng.adjoint_seed(dphys, lam)
@@ -217,11 +211,14 @@ class _IntegrateFn(torch.autograd.Function):
                  for g, gd in zip(gouts, eng.groups)]
         res = [None] * (1 + NF * len(eng.groups))
         first_extra = _lib.NGRAD
-        if integ.tangent_only:
-            if any(ctx.needs_input_grad[1 + NF * g + NP] for g in range(len(eng.groups))):
-                raise NotImplementedError("gradients with respect to the initial fields need the adjoint, which the "
-                                          "semi-implicit scheme does not have")
+        if integ.param_tangents:
+            # semi-implicit: the adjoint for the initial fields (when asked for),
+            # tangent runs for every parameter
             first_extra = 0
+            if any(ctx.needs_input_grad[1 + NF * g + NP] for g in range(len(eng.groups))):
+                dic, _ = integ.run_backward(dphys)
+                for g in range(len(eng.groups)):
+                    res[1 + NF * g + NP] = dic[g].to(ctx.in_dtypes[NF * g + NP])
         else:
             dic, grad = integ.run_backward(dphys)
             for g in range(len(eng.groups)):

@@ -635,6 +635,9 @@ int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group
   LS.mode = 0;
   LS.cfg = make_cfg(f);
   LS.cfg.incremental = step_incremental(p, f, t) ? 1 : 0;
+  // the carries of step t, as forward_steps sets them (read by the semi-implicit adjoint)
+  LS.cfg.ra_mode = (f->modalflag && t > 2) ? 2 : 1;
+  LS.cfg.si_lag_init = f->scheme == 2 && t == f->t_start;
   for (int g = 0; g < p->ng; ++g) {
     LS.grp[g].lam = (typename cplx<T>::type*)adj[g].lam;
     LS.grp[g].lamY = (const typename cplx<T>::type*)adj[g].lam_y;
@@ -997,16 +1000,14 @@ static int check_align(swp_plan* p, const swp_group_state* st, const swp_group_a
 }
 
 // Scheme switches every stepping entry checks (model.py:1531-1537).  The
-// adjoint covers the modified-Euler and explicit schemes with the classic filter.
+// adjoint covers the three schemes with the classic filter (the semi-implicit
+// scheme's adjoint propagates the state only: its parameter gradients are
+// tangent runs).
 int check_scheme(swp_plan* p, const swp_flags* f, bool adjoint) {
   if (f->scheme < 0 || f->scheme > 2) return fail(p, SWP_ERR_ARG, "scheme must be 0, 1 or 2");
   if (f->test < 0 || f->test > 2) return fail(p, SWP_ERR_ARG, "test must be 0 (None), 1 or 2");
   if (f->raw_filter && f->scheme == 1)
     return fail(p, SWP_ERR_ARG, "raw_filter is incompatible with the explicit scheme");
-  if (adjoint && f->scheme == 2)
-    return fail(p, SWP_ERR_UNSUPPORTED,
-                "the adjoint is implemented for the modified-Euler and explicit schemes (the semi-implicit scheme "
-                "differentiates by tangent runs)");
   if (adjoint && f->raw_filter)
     return fail(p, SWP_ERR_UNSUPPORTED,
                 "derivatives (adjoint, tangent) are implemented for the classic Robert-Asselin filter");

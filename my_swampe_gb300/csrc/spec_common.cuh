@@ -573,11 +573,15 @@ __device__ __forceinline__ void step_residual_weights(const StepCfg& cfg, double
 //   and the primal delta, Phi, E, A, B, F, G (Phibar gradient);
 //   explicit leapfrog: the adjoint of the Fourier prev level after the step
 //   (the step moves curr there), and the primal curr delta, U, V (Phibar and
-//   taudrag gradients).
+//   taudrag gradients);
+//   semi-implicit leapfrog: the adjoint of the filtered mid carry and of the
+//   lagged remainders after the step (its parameter gradients are tangent runs).
 template <typename T>
 struct AdjPointIn {
-  typename cplx<T>::type ly[3];  // lamY eta, delta, Phi | lambda eta, delta, Phi prev (explicit)
-  typename cplx<T>::type px[7];  // primal delta, Phi, E, A, B, F, G | delta, U, V (explicit)
+  // lamY eta, delta, Phi | lambda eta, delta, Phi prev (explicit) | lambda eta, delta, Phi mid (semi-implicit)
+  typename cplx<T>::type ly[3];
+  // primal delta, Phi, E, A, B, F, G | delta, U, V (explicit) | lambda of the lagged remainders (semi-implicit)
+  typename cplx<T>::type px[7];
 };
 
 template <typename T>
@@ -585,6 +589,16 @@ __device__ __forceinline__ void adj_load_point(const SpecGroup<T>& G, const Step
                                                size_t o, AdjPointIn<T>& in) {
   typedef typename cplx<T>::type T2;
   const T2 z = mk<T2>(0, 0);
+  if (cfg.scheme == 2) {
+    const int lf[3] = {F_ETA_MID, F_DELTA_MID, F_PHI_MID};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) in.ly[q] = G.lam[lf[q] * FS + o];
+    in.px[0] = G.lam[F_RU_LAG * FS + o];
+    in.px[1] = G.lam[F_RV_LAG * FS + o];
+#pragma unroll
+    for (int q = 2; q < 7; ++q) in.px[q] = z;
+    return;
+  }
   if (cfg.scheme == 1) {
     const int lf[3] = {F_ETA_PREV, F_DELTA_PREV, F_PHI_PREV};
     const int pf[3] = {F_DELTA, F_U, F_V};
@@ -733,14 +747,90 @@ __device__ __forceinline__ T adj_point_values_ex(const SpecGroup<T>& G, const St
   return -tdt * (lP1.x * del1.x + lP1.y * del1.y);
 }
 
-// adj_point_values (modified Euler) or adj_point_values_ex (explicit) written
-// to G.lam at offset o of one point.  Returns the point's dL/dPhibar term and
-// adds its dL/dtaudrag term (explicit scheme) to gtd.
+// Transposed combination of the semi-implicit leapfrog (adjoint of
+// step_combos_ld scheme 2, semi_implicit_tdiff.py si_timestep) at one point,
+// with the step's carries: the Robert-Asselin update of the filtered mid level
+// (mid' = curr + al (mid - 2 curr + new), or curr on the first steps; its new
+// level's share enters through lamY) and the lagged remainders (lag' = F + U /
+// taudrag of the incoming state).  The step reads the mid level (the n-1 base),
+// A..E, PhiF, F, G or the lagged remainders, Phi (relaxation) and, on the first
+// step, U, V.  lv takes all 19 fields in field order; the parameter gradients
+// of this scheme are tangent runs, so there is no gradient term.
+template <typename T, int NK, typename LD>
+__device__ __forceinline__ void adj_point_values_si(const SpecGroup<T>& G, const StepCfg& cfg, int m, int b, int j,
+                                                    LD ld, const AdjPointIn<T>& in,
+                                                    typename cplx<T>::type (&lv)[NFOURIER]) {
+  typedef typename cplx<T>::type T2;
+  const T2 lP1 = ld(0), lD1 = ld(2), lD2 = ld(3), lE1 = ld(4);
+  const T2 lPH1 = ld(NK), lDH1 = ld(NK + 1), lEH1 = ld(NK + 3);
+  const T* mc = G.mco;
+  const int B = G.B;
+  const T tsc = G.jco[(size_t)b * G.g.J + j];
+  const T xm = (T)m;
+  const bool relax = cfg.si_relax != 0;
+  const T forc = cfg.forcflag ? (T)1 : (T)0;
+  const T ex = mc[MC_SIEX * B + b];
+  const T itd = relax ? mc[MC_SIITD * B + b] : (T)0, itr = relax ? mc[MC_SIITR * B + b] : (T)0;
+  const T gd = ex * itd, gr = ex * itr, tdt = mc[MC_2DT * B + b];
+  const T ia2 = mc[MC_IA2 * B + b], pb = mc[MC_PB * B + b];
+  const T2 z = mk<T2>(0, 0);
+  auto mimul = [&](T alpha, T2 v) { return imul(-alpha * xm, v); };  // conj(i alpha m) v
+  const T2 lAeff = cadd(mimul(-tsc, lE1), cscale(lDH1, tsc));
+  const T2 lBeff = cadd(mimul(tsc, lD1), cscale(lEH1, tsc));
+  const T2 lFx = cscale(lBeff, forc), lGx = cscale(lAeff, -forc), lPFx = cscale(lP1, forc * tdt);
+  // the Robert-Asselin carry: old curr -> mid' with weight 1 - 2 al (or 1), mid -> mid' with al
+  const bool ra2 = cfg.ra_mode == 2;
+  const T al = ra2 ? mc[MC_ALPHA * B + b] : (T)0;
+  const T c_old = ra2 ? (T)1 - (T)2 * al : (T)1;
+  // the lagged remainders after the step, F + U / taudrag of the incoming state (always written)
+  const T itd_lag = mc[MC_SIITD * B + b];
+  const T2 lRu = in.px[0], lRv = in.px[1];
+  const bool from_state = !relax || cfg.si_lag_init;  // Fx, Gx are F, G (+ U, V / taudrag on the first step)
+#pragma unroll
+  for (int q = 0; q < NFOURIER; ++q) lv[q] = z;
+  lv[F_ETA] = cscale(in.ly[0], c_old);
+  lv[F_DELTA] = cscale(in.ly[1], c_old);
+  lv[F_PHI] = cadd(cscale(in.ly[2], c_old), cscale(lPFx, itr));
+  lv[F_U] = cscale(lRu, itd_lag);
+  lv[F_V] = cscale(lRv, itd_lag);
+  if (relax && cfg.si_lag_init) {
+    lv[F_U] = cadd(lv[F_U], cscale(lFx, itd));
+    lv[F_V] = cadd(lv[F_V], cscale(lGx, itd));
+  }
+  lv[F_A] = lAeff;
+  lv[F_B] = lBeff;
+  lv[F_C] = mimul(-tsc, lP1);
+  lv[F_D] = cscale(lPH1, tsc);
+  lv[F_E] = cscale(lD2, ia2 * tdt);
+  lv[F_PHIF] = lPFx;
+  lv[F_F] = from_state ? cadd(lRu, lFx) : lRu;
+  lv[F_G] = from_state ? cadd(lRv, lGx) : lRv;
+  lv[F_ETA_MID] = cadd(cscale(lE1, (T)1 - gd), cscale(in.ly[0], al));
+  lv[F_DELTA_MID] = cadd(csub(cscale(lD1, (T)1 - gd), cscale(lP1, ex * pb)), cscale(in.ly[1], al));
+  lv[F_PHI_MID] = cadd(cadd(cscale(lP1, (T)1 - gr), cscale(lD2, ia2 * ex)), cscale(in.ly[2], al));
+  // the lagged remainders before the step are read from the carry after the first step
+  lv[F_RU_LAG] = from_state ? z : lFx;
+  lv[F_RV_LAG] = from_state ? z : lGx;
+}
+
+// adj_point_values (modified Euler), adj_point_values_ex (explicit) or
+// adj_point_values_si (semi-implicit) written to G.lam at offset o of one
+// point.  Returns the point's dL/dPhibar term and adds its dL/dtaudrag term
+// (explicit scheme) to gtd.
 template <typename T, int NK, typename LD>
 __device__ __forceinline__ T adj_store_point(const SpecGroup<T>& G, const StepCfg& cfg, bool incr, size_t FS,
                                              size_t o, int m, int b, int j, LD ld, const AdjPointIn<T>& in,
                                              T& gtd) {
   typedef typename cplx<T>::type T2;
+  if (cfg.scheme == 2) {
+    T2 lv[NFOURIER];
+    adj_point_values_si<T, NK>(G, cfg, m, b, j, ld, in, lv);
+    // F_PHI_PREV is neither read nor written by the semi-implicit step: its adjoint passes through
+#pragma unroll
+    for (int q = 0; q < NFOURIER; ++q)
+      if (q != F_PHI_PREV) G.lam[q * FS + o] = lv[q];
+    return (T)0;
+  }
   if (cfg.scheme == 1) {
     T2 lv[16];
     const T gp = adj_point_values_ex<T, NK>(G, cfg, m, b, j, ld, in, lv, gtd);

@@ -586,20 +586,30 @@ __device__ __forceinline__ void spectral_adj_unit(const SpecLaunch<T>& L, const 
   double* sgrad = (double*)(((uintptr_t)(tcmn + MT * cntmax) + 15) & ~(uintptr_t)15);
   const int nws = J / 32;
 
-  load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, cntmax, sig, sigP, sigm1, sigPm1, tcmn);
+  load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, cntmax, sig, sigP, sigm1, sigPm1, tcmn,
+                     cfg.scheme == 2);
   for (int t = threadIdx.x; t < 2 * MT * nws; t += blockDim.x) sgrad[t] = 0.0;
 
-  // ---- phase 1: symmetrised adjoints of the step outputs at column m
+  // ---- phase 1: symmetrised adjoints of the step outputs at column m.  The
+  // semi-implicit step's new level also enters its filtered mid carry with
+  // weight al (Robert-Asselin update), whose adjoint adds here.
   const T2* LY = G.lamY;  // [5][M+1][B][J]
+  const bool si_ra = cfg.scheme == 2 && cfg.ra_mode == 2;
   for (int t = threadIdx.x; t < MT * Jh; t += blockDim.x) {
     int bt = t / Jh, jp = t % Jh;
     T2 ys[5], ya[5];
     if (bt < mt) {
       int b = b0 + bt;
       size_t on = ((size_t)m * G.B + b) * J + jp, os = ((size_t)m * G.B + b) * J + (J - 1 - jp);
+      const T al = si_ra ? G.mco[MC_ALPHA * G.B + b] : (T)0;
 #pragma unroll
       for (int f = 0; f < 5; ++f) {
         T2 u = LY[f * FS + on], v = LY[f * FS + os];
+        if (si_ra && f < 3) {
+          const int mf = f == 0 ? F_ETA_MID : f == 1 ? F_DELTA_MID : F_PHI_MID;
+          u = cadd(u, cscale(G.lam[mf * FS + on], al));
+          v = cadd(v, cscale(G.lam[mf * FS + os], al));
+        }
         ys[f] = cadd(u, v);
         ya[f] = csub(u, v);
       }
@@ -696,11 +706,40 @@ __device__ __forceinline__ void spectral_adj_unit(const SpecLaunch<T>& L, const 
     T lcd_r = S(1, 0) + w * lds_r, lcd_i = S(1, 1) + w * lds_i;
     T lcp_r = S(2, 0), lcp_i = S(2, 1);
     auto K = [&](int q, int comp, T v) { Kad[((size_t)q * cntmax + pc) * R + 2 * bt + comp] = v; };
-    K(0, 0, sp * lcp_r); K(0, 1, sp * lcp_i);
-    K(1, 0, nn1 * sp * lcp_r); K(1, 1, nn1 * sp * lcp_i);
-    K(2, 0, s * lcd_r); K(2, 1, s * lcd_i);
-    K(3, 0, nn1 * s * lcd_r); K(3, 1, nn1 * s * lcd_i);
-    K(4, 0, s * lce_r); K(4, 1, s * lce_i);
+    if (cfg.scheme == 2) {
+      // transpose of the semi-implicit solve per degree (spectral_unit):
+      //   dnew = (sdel + bq ikr sphi) / Dn,  pnew = (sphi - cq dnew) ikr,  enew = seta ikd,
+      // then the exponential sigmas; slot map as below with PhiP2 unused
+      T xi = (T)0, kd = (T)0, kr = (T)0, pbv = (T)0, ia2 = (T)0;
+      if (bt < mt) {
+        const T* mc = G.mco;
+        const int b = b0 + bt, B = G.B;
+        xi = mc[MC_SIXI * B + b];
+        pbv = mc[MC_PB * B + b];
+        ia2 = mc[MC_IA2 * B + b];
+        if (cfg.si_relax) {
+          kd = xi * mc[MC_SIITD * B + b];
+          kr = xi * mc[MC_SIITR * B + b];
+        }
+      }
+      const T bq = xi * (nn1 * ia2), cq = xi * pbv;
+      const T ikr = (T)1 / ((T)1 + kr), ikd = (T)1 / ((T)1 + kd);
+      const T Dn = ((T)1 + kd) + bq * cq * ikr;
+      const T lpn_r = sp * lcp_r, lpn_i = sp * lcp_i;
+      const T ldn_r = s * lcd_r - cq * ikr * lpn_r, ldn_i = s * lcd_i - cq * ikr * lpn_i;
+      const T lsd_r = ldn_r / Dn, lsd_i = ldn_i / Dn;
+      K(0, 0, ikr * lpn_r + bq * ikr * lsd_r); K(0, 1, ikr * lpn_i + bq * ikr * lsd_i);
+      K(1, 0, (T)0); K(1, 1, (T)0);
+      K(2, 0, lsd_r); K(2, 1, lsd_i);
+      K(3, 0, nn1 * lsd_r); K(3, 1, nn1 * lsd_i);
+      K(4, 0, ikd * s * lce_r); K(4, 1, ikd * s * lce_i);
+    } else {
+      K(0, 0, sp * lcp_r); K(0, 1, sp * lcp_i);
+      K(1, 0, nn1 * sp * lcp_r); K(1, 1, nn1 * sp * lcp_i);
+      K(2, 0, s * lcd_r); K(2, 1, s * lcd_i);
+      K(3, 0, nn1 * s * lcd_r); K(3, 1, nn1 * s * lcd_i);
+      K(4, 0, s * lce_r); K(4, 1, s * lce_i);
+    }
     if (NKADJ > 5) {
       // identity slots of the incremental form: d/d Fwd(curr) of
       //   dc_f = (sigma_f - 1) Fwd(curr_f) + ...  and of the full c_eta, c_delta used for the winds

@@ -442,7 +442,6 @@ def run_model_scan(
         raise ValueError(f"starttime={starttime_eff} must be <= tmax={tmax}.")
 
     have_ic = (eta0_init is not None) or (delta0_init is not None) or (Phi0_init is not None)
-    ic_derivs: Dict[str, torch.Tensor] = {}  # d(analytic initial fields) / d(parameter), semi-implicit runs
     if have_ic and (eta0_init is None or delta0_init is None or Phi0_init is None):
         raise ValueError("If providing explicit ICs, eta0_init, delta0_init, and Phi0_init must all be provided.")
     if have_ic and ((U0_init is None) != (V0_init is None)):
@@ -477,15 +476,11 @@ def run_model_scan(
     needs_grad = any(_tracked(x) for x in diff_inputs)
     if _tracked(williams_alpha):
         raise NotImplementedError("derivatives through the RAW filter are not implemented")
-    tangent_only = bool(semi_implicit)  # the scheme differentiated by tangent runs (no adjoint)
     if needs_grad:
         if raw_filter or test == 1:
             raise NotImplementedError("derivatives are implemented with the classic filter and test None or 2")
         if U0_init is None and (_tracked(eta0_init) or _tracked(delta0_init)):
             raise NotImplementedError("derivatives with respect to eta0_init / delta0_init need U0_init and V0_init")
-        if tangent_only and torch.is_grad_enabled() and any(torch.is_tensor(x) and x.requires_grad for x in ic_inputs):
-            raise NotImplementedError("reverse-mode gradients with respect to the initial fields need the adjoint, "
-                                      "which the semi-implicit scheme does not have (forward mode works)")
 
     split = (batched and B >= _SPLIT_MIN_B and tmax > starttime_eff and test != 1
              and not (return_history or diagnostics or semi_implicit or raw_filter))
@@ -518,8 +513,6 @@ def run_model_scan(
         # the analytic fields are polynomials of degree <= 2 in a, omega, Phibar
         # (initial_conditions.py:18-47, 88-239), so a centred difference is their
         # exact derivative: carry it into the differentiable run
-        # (the semi-implicit scheme, which differentiates by tangent runs, takes
-        # them as initial-field tangents of the parameter directions)
         for x, i, name in ((a, 0, "a"), (omega, 1, "omega"), (Phibar, 2, "Phibar")):
             if _tracked(x):
                 h = 1e-3 * abs((av, omv, pb)[i]) or 1e-3
@@ -529,9 +522,6 @@ def run_model_scan(
                 arg[i] -= 2 * h
                 fm = _analytic_ic(M, *arg, test, float(a1), dev)
                 d = [(u - v) / (2 * h) for u, v in zip(fp, fm)]
-                if semi_implicit:
-                    ic_derivs[name] = torch.stack([dd.expand(B, J, I) for dd in d], 0)
-                    continue
                 dx = x - x.detach()
                 eta0, delta0, Phi0, U0, V0 = (f + dx * dd.expand(B, J, I)
                                               for f, dd in zip((eta0, delta0, Phi0, U0, V0), d))
@@ -587,7 +577,7 @@ def run_model_scan(
         for k, x in coef_inputs.items():
             if _tracked(x):
                 dpar[k] = _per_member(x, B, dev)
-        dcurr = adjoint.integrate(eng, dflags, starttime_eff, T, [dpar], [ics], ic_derivs=[ic_derivs])[0]
+        dcurr = adjoint.integrate(eng, dflags, starttime_eff, T, [dpar], [ics])[0]
         for x in (alpha, g):  # zero derivative, but part of the graph
             if _tracked(x):
                 dcurr = dcurr + 0.0 * x.to(dcurr.dtype).sum()
@@ -672,8 +662,7 @@ def _run_split(M, B, precision, device, flags: RunFlagsC, t0: int, T: int, ics: 
         for k, x in coef_inputs.items():
             if _tracked(x):
                 dpar[k] = _per_member(x, B, dev)
-        outs = adjoint.integrate(eng, dflags, t0, T, [{k: v[sl] for k, v in dpar.items()} for sl in sls], ics_g,
-                                 ic_derivs=[{}, {}])
+        outs = adjoint.integrate(eng, dflags, t0, T, [{k: v[sl] for k, v in dpar.items()} for sl in sls], ics_g)
         dcurr = torch.cat(outs, dim=1)
         for x in zero_deriv:  # zero derivative, but part of the graph
             if _tracked(x):

@@ -174,19 +174,41 @@ def test_semi_implicit_forward_mode_equals_reverse(cuda):
     assert abs(t - g) <= 1e-9 * abs(g), (t, g)
 
 
-def test_semi_implicit_initial_field_gradient_refused(cuda):
+def test_semi_implicit_initial_field_gradient_matches_finite_differences(cuda):
+    """The semi-implicit scheme's adjoint (initial fields; its parameter
+    gradients are tangent runs): the gradient in Phi0_init along a random
+    direction against a central difference, forced, 20 steps."""
     from my_swampe_gb300 import run_model_scan_final
+    from oracle import swampe_oracle as o
 
-    z = np.zeros((64, 128))
-    phi = torch.zeros((64, 128), dtype=torch.float64, device="cuda", requires_grad=True)
-    with pytest.raises(NotImplementedError):
-        run_model_scan_final(**SYNTH, semi_implicit=True, eta0_init=z, delta0_init=z, Phi0_init=phi, U0_init=z,
-                             V0_init=z)
+    geo = o.cached_geometry(42)
+    J, I = geo["J"], geo["I"]
+    mu = torch.tensor(geo["mus"], dtype=torch.float64, device="cuda")[:, None]
+    rng = np.random.default_rng(12)
+    eta0 = (2 * 3.2e-5 * mu).expand(J, I).contiguous()
+    Phi0 = torch.tensor(3e3 * rng.standard_normal((J, I)), dtype=torch.float64, device="cuda")
+    U0 = (10.0 * torch.sqrt(1 - mu**2)).expand(J, I).contiguous()
+    z = torch.zeros((J, I), dtype=torch.float64, device="cuda")
+    kw = dict(SYNTH, tmax=22, semi_implicit=True, eta0_init=eta0, delta0_init=z, U0_init=U0, V0_init=z)
+
+    def loss(p):
+        Phi = run_model_scan_final(**kw, Phi0_init=p)["last_state"].Phi_curr
+        return torch.mean(Phi * Phi)
+
+    th = Phi0.clone().requires_grad_(True)
+    g = torch.autograd.grad(loss(th), th)[0]
+    v = torch.tensor(rng.standard_normal((J, I)), dtype=torch.float64, device="cuda")
+    h = 1e-2
+    with torch.no_grad():
+        fd = (float(loss(Phi0 + h * v)) - float(loss(Phi0 - h * v))) / (2 * h)
+    ad = float((g * v).sum())
+    assert abs(ad - fd) <= 1e-6 * abs(fd), (ad, fd)
 
 
 def test_semi_implicit_phibar_gradient_with_analytic_test2_initial_condition(cuda):
-    """The analytic test-2 fields depend on Phibar; the semi-implicit scheme's
-    tangent runs carry that dependence as an initial-field tangent."""
+    """The analytic test-2 fields depend on Phibar: that dependence reaches the
+    gradient through the initial fields (the semi-implicit adjoint), the
+    dynamics' through a tangent run."""
     from my_swampe_gb300 import run_model_scan_final
 
     kw = dict(M=42, dt=600.0, tmax=6, omega=7.2921159e-5, a=6.37122e6, test=2, forcflag=False, semi_implicit=True)

@@ -139,10 +139,8 @@ def test_semi_implicit_ensemble_of_alphas(cuda):
         np.testing.assert_allclose(ens[i], direct, rtol=0, atol=1e-10)
 
 
-def test_adjoint_rejects_opt_in_schemes(cuda):
-    """The Python layer and the C ABI refuse the adjoint of the semi-implicit
-    scheme and of the RAW filter (the semi-implicit scheme differentiates by
-    tangent runs)."""
+def test_adjoint_rejects_raw_filter(cuda):
+    """The Python layer and the C ABI refuse the adjoint of the RAW filter."""
     import torch
     from my_swampe_gb300 import adjoint
     from my_swampe_gb300.engine import Engine, RunFlagsC
@@ -150,16 +148,11 @@ def test_adjoint_rejects_opt_in_schemes(cuda):
     eng = Engine([(42, 2)], "fp64")
     with pytest.raises(NotImplementedError):
         adjoint.Integration(eng, RunFlagsC(raw_filter=True), t0=2, nsteps=4, ckpt_every=2, store="checkpoint")
-    # the semi-implicit scheme: tangent runs only, no adjoint sweep
-    integ = adjoint.Integration(eng, RunFlagsC(scheme=2), t0=2, nsteps=4, ckpt_every=2, store="checkpoint")
-    with pytest.raises(NotImplementedError):
-        integ.run_backward([torch.zeros((5, 2, 64, 128), dtype=torch.float64, device=eng.device)])
     lam, lamy, grad = eng.new_adjoint_buffers()
     gd = eng.groups[0]
     slots = [torch.empty((3,) + tuple(gd["fourier"].shape), dtype=eng.cdtype, device=eng.device)]
-    for flags in (RunFlagsC(scheme=2), RunFlagsC(raw_filter=True)):
-        with pytest.raises(RuntimeError, match="modified-Euler|classic"):
-            eng.adjoint_window(flags, [gd["fourier"]], slots, lam, lamy, grad, t0=2, nsteps=2)
+    with pytest.raises(RuntimeError, match="classic"):
+        eng.adjoint_window(RunFlagsC(raw_filter=True), [gd["fourier"]], slots, lam, lamy, grad, t0=2, nsteps=2)
 
 
 def test_raw_filter_fast_precision_is_close(cuda):

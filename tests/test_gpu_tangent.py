@@ -131,10 +131,12 @@ def test_coefficient_gradients_by_reverse_mode(cuda):
         assert abs(float(gk.sum()) - fd) <= 1e-3 * abs(fd), (k, float(gk.sum()), fd)
 
 
-@pytest.mark.parametrize("scheme", [0, 1])
+@pytest.mark.parametrize("scheme", [0, 1, 2])
 def test_tangent_adjoint_dot_product(cuda, scheme):
     """<w, J v> from the tangent model equals <J^T w, v> from the adjoint (FP64),
-    for the modified-Euler and the explicit scheme."""
+    for the modified-Euler, explicit and semi-implicit schemes (the last one's
+    reverse-mode parameter terms are tangent runs, its initial-field terms the
+    adjoint)."""
     from my_swampe_gb300 import adjoint
     from my_swampe_gb300.engine import RunFlagsC
 
