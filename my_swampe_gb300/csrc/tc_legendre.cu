@@ -294,7 +294,6 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_tc(const __grid_const
     tc::tmem_alloc(tslot, S::TMEM_COLS);
     tc::tmem_relinquish();
   }
-  load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, CNT, sig, sigP, sigm1, sigPm1, tcmn);
   if (threadIdx.x < MT) {
     const int bt = threadIdx.x;
     int dead = 0;
@@ -427,6 +426,8 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_tc(const __grid_const
       tc::mma_commit_warp(&mbar[1]);
       n_c1 = 1;
     }
+    // the epilogue's per-(member, n) coefficients, gathered while the MMAs run
+    load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, CNT, sig, sigP, sigm1, sigPm1, tcmn);
     ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 0, basis.wait_limit) : true;
     ok = __syncthreads_and(ok);
     tc::fence_after_sync();
@@ -540,18 +541,8 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_tc(const __grid_const
     __syncthreads();
     tc::fence_after_sync();
     // ---- phase 5: GEMM2, both parities (rows 112..127 read the staging area and are ignored)
-    // Each thread first issues the global loads of its write-out pairs, so that
-    // their latency overlaps the GEMM.
-#pragma unroll
-    for (int k = 0; k < S::NWPAIR; ++k) {
-      wal[k] = (T)0;
-      wan[k] = (T)0;
-      if (wbt[k] < mt) {
-        load_step_rows<T>(G, cfg, incr, FS, ((size_t)m * G.B + b0 + wbt[k]) * J + wj[k], pold[k], pmid[k]);
-        wal[k] = G.mco[(cfg.raw ? MC_RAWM : MC_ALPHA) * G.B + b0 + wbt[k]];
-        wan[k] = cfg.raw ? G.mco[MC_RAWN * G.B + b0 + wbt[k]] : (T)0;
-      }
-    }
+    // Warp 0 issues the MMAs first; then every thread issues the global loads
+    // of its write-out pairs, whose latency overlaps the GEMM.
     if (warp == 0) {
       const bool good = tc::mbar_wait_bounded_warp(&mbar[0], 1, basis.wait_limit);
       if (!good) *sflag = 1;
@@ -565,6 +556,16 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_tc(const __grid_const
       }
       tc::mma_commit_warp(&mbar[2]);
       n_c2 = 1;
+    }
+#pragma unroll
+    for (int k = 0; k < S::NWPAIR; ++k) {
+      wal[k] = (T)0;
+      wan[k] = (T)0;
+      if (wbt[k] < mt) {
+        load_step_rows<T>(G, cfg, incr, FS, ((size_t)m * G.B + b0 + wbt[k]) * J + wj[k], pold[k], pmid[k]);
+        wal[k] = G.mco[(cfg.raw ? MC_RAWM : MC_ALPHA) * G.B + b0 + wbt[k]];
+        wan[k] = cfg.raw ? G.mco[MC_RAWN * G.B + b0 + wbt[k]] : (T)0;
+      }
     }
     ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[2], 0, basis.wait_limit) : true;
     ok = __syncthreads_and(ok);
@@ -732,7 +733,6 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_c
     tc::tmem_alloc(tslot, S::TMEM_COLS);
     tc::tmem_relinquish();
   }
-  load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, CNT, sig, sigP, sigm1, sigPm1, tcmn);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -820,6 +820,8 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_c
       tc::mma_commit_warp(&mbar[1]);
       n_c1 = 1;
     }
+    // the epilogue's per-(member, n) coefficients, gathered while the MMAs run
+    load_spec_coefs<T>(G, cfg.diffflag != 0, m, b0, mt, MT, cnt, CNT, sig, sigP, sigm1, sigPm1, tcmn);
     ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[1], 0, basis.wait_limit) : true;
     ok = __syncthreads_and(ok);
     tc::fence_after_sync();
@@ -913,10 +915,7 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_c
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    // ---- phase 5: GEMM2', both parities; write-out inputs loaded meanwhile
-#pragma unroll
-    for (int k = 0; k < S::NWPAIR; ++k)
-      if (wbt[k] < mt) adj_load_rows<T>(G, incr, FS, ((size_t)m * G.B + b0 + wbt[k]) * J + wj[k], pin[k]);
+    // ---- phase 5: GEMM2', both parities; write-out inputs loaded meanwhile (after the MMA issue)
     if (warp == 0) {
       const bool good = tc::mbar_wait_bounded_warp(&mbar[0], 1, basis.wait_limit);
       if (!good) *sflag = 1;
@@ -931,6 +930,9 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_c
       tc::mma_commit_warp(&mbar[2]);
       n_c2 = 1;
     }
+#pragma unroll
+    for (int k = 0; k < S::NWPAIR; ++k)
+      if (wbt[k] < mt) adj_load_rows<T>(G, incr, FS, ((size_t)m * G.B + b0 + wbt[k]) * J + wj[k], pin[k]);
     ok = threadIdx.x == 0 ? tc::mbar_wait_bounded(&mbar[2], 0, basis.wait_limit) : true;
     ok = __syncthreads_and(ok);
     tc::fence_after_sync();
