@@ -60,6 +60,23 @@ def _peaks():
     return 6800.0, "fallback"
 
 
+def _tensor_peak():
+    """Dense bf16 TFLOP/s (burst), measured or the fallback."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["bf16_tflops"]), "measured"
+        except Exception:
+            pass
+    return 1900.0, "fallback"
+
+
+# Algorithmic Legendre FLOPs of one member-step at M=42 (forward; the adjoint
+# transposes the same transforms): 18 distinct complex transforms (11 forward,
+# 7 inverse), each 4 J sum_m (M + 1 - m) = 4 * 64 * 946 real flops.
+LEGENDRE_FLOP_M42 = 18 * 4 * 64 * 946
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -314,6 +331,22 @@ def run_ours(args):
                 "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": _ncu_traffic(dom),
                 "ms_per_launch": {k: round(v, 5) for k, v in per_step.items()},
                 "algorithmic_bytes_per_launch": alg}
+    # every kernel against HBM; the Legendre kernels also in algorithmic TFLOP/s
+    # against the dense bf16 peak (their 3xTF32 MMAs issue about 2.5x these flops)
+    tpeak, tpeak_kind = _tensor_peak()
+    per_kernel = {}
+    for k, ms in per_step.items():
+        ab = _algorithmic_bytes(k, B, elem=8)
+        gbs = ab / (ms * 1e-3) / 1e9
+        e = {"ms": round(ms, 5), "algorithmic_bytes": ab, "gbs": round(gbs, 1), "frac_hbm": round(gbs / peak, 4)}
+        if k in ("spectral", "spectral_adj"):
+            fl = LEGENDRE_FLOP_M42 * B
+            tf = fl / (ms * 1e-3) / 1e12
+            e.update(algorithmic_flop=fl, tflops=round(tf, 2), frac_tensor_bf16=round(tf / tpeak, 5))
+        per_kernel[k] = e
+    roofline["per_kernel"] = per_kernel
+    roofline["tensor_peak_tflops"] = tpeak
+    roofline["tensor_peak_kind"] = tpeak_kind
 
     # ---------------- e2e through the public API with host buffers
     from my_swampe_gb300.adjoint import integrate, GRAD_PARAMS, Integration
