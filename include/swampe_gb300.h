@@ -83,15 +83,21 @@ typedef struct {
 } swp_group_adjoint;
 
 /* Tangent-linear (forward-mode) buffers of one group. */
-#define SWP_NTANGENT 10
+#define SWP_NTANGENT 12
 typedef struct {
   void* fourier;          /* complex[SWP_NFOURIER][M+1][B][J]: tangent of the Fourier state */
   void* resid;            /* real[5][B][J][I]: tangent of the initial-condition residual     */
   const double* dparams;  /* double[SWP_NTANGENT][B]: tangents of taurad, taudrag, DPhieq,
-                             Phibar, a, dt, K6, K6Phi, omega, si_alpha                      */
-  int coef_tangents;      /* nonzero when rows a..si_alpha may be nonzero: the step then also
-                             differentiates its coefficient tables (one more Legendre pass;
-                             always taken by the semi-implicit scheme)                      */
+                             Phibar, a, dt, K6, K6Phi, omega, si_alpha, alpha (the
+                             Robert-Asselin coefficient), williams_alpha (RAW filter)      */
+  int coef_tangents;      /* nonzero when rows a..williams_alpha may be nonzero: the step
+                             then also differentiates its coefficient tables (one more
+                             Legendre pass; always taken by the semi-implicit scheme) and
+                             its filter weights (the primal Legendre step then runs on the
+                             SIMT kernel and adds the weights' tangents times its
+                             displacement to the tangent carries)                         */
+  double* dweights;       /* double[2][B]: tangents of the residual weights w_curr, w_mid
+                             (member[0..1] of the state), kept by the library             */
 } swp_group_tangent;
 
 /* Flags of model.py RunFlags (model.py:156-226) plus the test selector. */
@@ -293,8 +299,8 @@ int swp_adjoint_step_noalloc(swp_plan* plan, const swp_group_state* st_in, const
  * taudrag, DPhieq, Phibar -- what jax.jvp / jax.jacfwd through run_model_scan
  * give the reference (autodiff_utils.py:27-89 fwd_grad; the retrieval's
  * forward-mode gradients), along the ICs and the per-member parameters of
- * dparams.  Modified Euler or semi-implicit scheme, classic filter, diagnostics
- * off, test 0 or 2.
+ * dparams.  Modified Euler, explicit or semi-implicit scheme, classic or RAW
+ * filter, diagnostics off, test 0 or 2.
  *   swp_tangent_init: after swp_init_state on the same ICs, the tangent state
  *     from dphys_ic[g] = real[5][B][J][I] (tangents of eta, delta, Phi, U, V).
  *   swp_tangent_forward: advances the primal state st and its tangent together

@@ -34,7 +34,8 @@ MS_WCURR, MS_WMID, MS_DEAD, MS_UPDATED = range(4)
 D_RMS2, D_SPIN, D_PHIMIN, D_PHIMAX, D_DEAD = range(5)
 G_TAURAD, G_TAUDRAG, G_DPHIEQ, G_PHIBAR = range(4)
 # parameter tangents of the tangent-linear model (swampe_gb300.h SWP_NTANGENT)
-TANGENT_PARAMS = ("taurad", "taudrag", "DPhieq", "Phibar", "a", "dt", "K6", "K6Phi", "omega", "si_alpha")
+TANGENT_PARAMS = ("taurad", "taudrag", "DPhieq", "Phibar", "a", "dt", "K6", "K6Phi", "omega", "si_alpha", "alpha",
+                  "williams_alpha")
 NTANGENT = len(TANGENT_PARAMS)
 
 WAIT_LIMIT_DEFAULT = 1 << 22  # swampe_gb300.h SWP_WAIT_LIMIT_DEFAULT
@@ -67,6 +68,7 @@ class GroupTangent(ctypes.Structure):
         ("resid", ctypes.c_void_p),
         ("dparams", ctypes.c_void_p),
         ("coef_tangents", ctypes.c_int),
+        ("dweights", ctypes.c_void_p),
     ]
 
 

@@ -31,7 +31,7 @@ from .engine import Engine, RunFlagsC
 GRAD_PARAMS = ("taurad", "taudrag", "DPhieq", "Phibar")
 PARAM_ROW = {"taurad": _lib.P_TAURAD, "taudrag": _lib.P_TAUDRAG, "DPhieq": _lib.P_DPHIEQ, "Phibar": _lib.P_PHIBAR,
              "a": _lib.P_A, "dt": _lib.P_DT, "K6": _lib.P_K6, "K6Phi": _lib.P_K6PHI, "omega": _lib.P_OMEGA,
-             "si_alpha": _lib.P_SIALPHA}
+             "si_alpha": _lib.P_SIALPHA, "alpha": _lib.P_ALPHA, "williams_alpha": _lib.P_WALPHA}
 
 
 class Integration:
@@ -53,18 +53,20 @@ class Integration:
 
     def __init__(self, engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, ckpt_every: int = 50,
                  store: str = "auto", mem_fraction: float = 0.8):
-        if flags.raw_filter:
-            raise NotImplementedError("derivatives are implemented for the classic Robert-Asselin filter")
         # the semi-implicit scheme's adjoint propagates the state (initial-field
-        # gradients); its parameter gradients are per-parameter tangent runs
-        self.param_tangents = flags.scheme == 2
+        # gradients); its parameter gradients are per-parameter tangent runs.  The
+        # RAW filter has no adjoint: its parameter gradients are tangent runs too,
+        # and it has no reverse-mode initial-field gradients
+        self.param_tangents = flags.scheme == 2 or bool(flags.raw_filter)
+        self.raw_filter = bool(flags.raw_filter)
         if flags.test == 1:
             raise NotImplementedError("the adjoint of test=1 (fixed winds) is not implemented")
         if nsteps < 1:
             raise ValueError("nsteps must be >= 1 for a differentiable run")
         self.eng = engine
         self.flags = RunFlagsC(scheme=flags.scheme, forcflag=flags.forcflag, diffflag=flags.diffflag,
-                               modalflag=flags.modalflag, test=flags.test, diagnostics=False, t_start=int(t0))
+                               modalflag=flags.modalflag, test=flags.test, diagnostics=False, t_start=int(t0),
+                               raw_filter=bool(flags.raw_filter))
         self.t0 = int(t0)
         self.nsteps = int(nsteps)
         self.K = max(1, min(int(ckpt_every), self.nsteps))
@@ -96,6 +98,9 @@ class Integration:
         eng = self.eng
         self.ics = [x.to(device=eng.device, dtype=eng.rdtype).contiguous() for x in ics]
         eng.init_state(self.ics, self.flags)
+        if self.raw_filter:  # no adjoint sweep follows: nothing to keep
+            eng.forward(self.flags, t0=self.t0, nsteps=self.nsteps)
+            return [o[:5] for o in eng.output_physical(self.flags)]
         if self.store == "all":
             if self._states is None:
                 self._states = [torch.empty((self.nsteps + 1,) + tuple(gd["fourier"].shape), dtype=eng.cdtype,
@@ -156,9 +161,11 @@ class _IntegrateFn(torch.autograd.Function):
     """flat = per group: the NP parameters of ``_lib.TANGENT_PARAMS`` as (B,)
     tensors, then the initial fields (5, B, J, I).  Reverse mode: the adjoint
     sweep gives the initial-field and taurad / taudrag / DPhieq / Phibar
-    gradients; a parameter that enters only the coefficient tables (a, dt,
-    K6, K6Phi, omega) gets its per-member gradient from one tangent-linear run
-    along it (members are independent, so one run serves all of them)."""
+    gradients; a parameter that enters only the coefficient tables or the
+    filter weights (a, dt, K6, K6Phi, omega, si_alpha, alpha, williams_alpha)
+    gets its per-member gradient from one tangent-linear run along it (members
+    are independent, so one run serves all of them).  With the semi-implicit
+    scheme or the RAW filter every parameter gradient is such a run."""
 
     @staticmethod
     def _set_params(eng, flat):
@@ -216,6 +223,9 @@ class _IntegrateFn(torch.autograd.Function):
             # tangent runs for every parameter
             first_extra = 0
             if any(ctx.needs_input_grad[1 + NF * g + NP] for g in range(len(eng.groups))):
+                if integ.raw_filter:
+                    raise NotImplementedError("reverse-mode initial-field gradients through the RAW filter are not "
+                                              "implemented (forward mode and parameter gradients are)")
                 dic, _ = integ.run_backward(dphys)
                 for g in range(len(eng.groups)):
                     res[1 + NF * g + NP] = dic[g].to(ctx.in_dtypes[NF * g + NP])
@@ -254,8 +264,9 @@ def integrate(engine: Engine, flags: RunFlagsC, t0: int, nsteps: int, params: Se
     """Differentiable run of every group of ``engine``.
 
     params[g]: dict with (B,) tensors (or scalars) 'taurad', 'taudrag', 'DPhieq',
-    'Phibar', and optionally 'a', 'dt', 'K6', 'K6Phi', 'omega' (absent ones keep
-    the values set with engine.set_params and get no gradient);
+    'Phibar', and optionally 'a', 'dt', 'K6', 'K6Phi', 'omega', 'si_alpha',
+    'alpha', 'williams_alpha' (absent ones keep the values set with
+    engine.set_params and get no gradient);
     ics[g]: (5, B, J, I) physical eta, delta, Phi, U, V.  Returns per group a
     (5, B, J, I) tensor of the final physical curr fields.  Passing the same
     ``integration`` object across calls reuses its checkpoint buffers and the

@@ -273,7 +273,7 @@ SpecLaunch<T> simt_only(const swp_plan* p, const SpecLaunch<T>& LS, bool adjoint
 template <typename T>
 cudaError_t launch_step_spec(const swp_plan* p, const SpecLaunch<T>& LS, int nbs, cudaStream_t s) {
   if constexpr (std::is_same<T, float>::value) {
-    if (p->use_tc && LS.mode == 0 && LS.cfg.scheme == 0) {
+    if (p->use_tc && LS.mode == 0 && LS.cfg.scheme == 0 && !LS.cfg.tl_filter) {
       cudaError_t e = launch_tc_per_truncation(p, LS, p->tcbasis, false,
                                                [&](int Mt, const SpecLaunch<float>& LT, int n, const TcBasis& tb) {
                                                  return launch_spec_tc(Mt, LT, n, tb, p->d_err, s);
@@ -479,6 +479,10 @@ int tangent_init_impl(swp_plan* p, const swp_group_state* st, const swp_group_ta
     size_t bytes = (size_t)SWP_NFOURIER * (p->M[g] + 1) * p->B[g] * p->geom[g].J * es;
     int rc = cuda_check(p, cudaMemsetAsync(tan[g].fourier, 0, bytes, s), "tangent state clear");
     if (rc) return rc;
+    // the initial residual weights are constants
+    rc = cuda_check(p, cudaMemsetAsync(tan[g].dweights, 0, 2 * sizeof(double) * p->B[g], s),
+                    "tangent weights clear");
+    if (rc) return rc;
   }
   int nbg = 0;
   GridLaunch<T> LG = make_grid<T>(p, tst, nbg);
@@ -496,7 +500,11 @@ int tangent_init_impl(swp_plan* p, const swp_group_state* st, const swp_group_ta
 // One window of primal + tangent steps.  Per step: the tangent Legendre step
 // (it reads the primal state before the step), the primal Legendre step, the
 // primal grid step, then the tangent grid step (linearised about the new
-// primal level).
+// primal level).  Along tangents of the filter weights (alpha, williams_alpha)
+// the filtered levels also move by the weights' tangents times the primal
+// displacement mid - 2 curr + new, which exists only inside the primal step:
+// that step (then on the SIMT kernel) adds those terms to the tangent carries
+// and advances the tangents of the residual weights.
 template <typename T>
 int tangent_steps(swp_plan* p, const swp_group_state* st, const swp_group_tangent* tan, const swp_flags* f, int t0,
                   int nsteps, cudaStream_t s) {
@@ -514,8 +522,13 @@ int tangent_steps(swp_plan* p, const swp_group_state* st, const swp_group_tangen
   for (int g = 0; g < p->ng; ++g) {
     LT.grp[g].four_p = (const typename cplx<T>::type*)st[g].fourier;
     LT.grp[g].dpar = tan[g].dparams;
+    LS.grp[g].four_t = (typename cplx<T>::type*)tan[g].fourier;
+    LS.grp[g].dpar = tan[g].dparams;
+    LS.grp[g].dw = tan[g].dweights;
     LGT.grp[g].primal = (const typename cplx<T>::type*)st[g].fourier;
     LGT.grp[g].dpar = tan[g].dparams;
+    LGT.grp[g].resid_p = (const T*)st[g].resid;
+    LGT.grp[g].dw = tan[g].dweights;
     LG.grp[g].hist = nullptr;
   }
   StepCfg cfg = make_cfg(f);
@@ -536,6 +549,7 @@ int tangent_steps(swp_plan* p, const swp_group_state* st, const swp_group_tangen
     cfg.si_lag_init = f->scheme == 2 && t == f->t_start;
     cfg.incremental = step_incremental(p, f, t) ? 1 : 0;
     LS.cfg = LT.cfg = LG.cfg = LGT.cfg = cfg;
+    LS.cfg.tl_filter = cfg.tl_coef && cfg.ra_mode == 2;
     cudaError_t e = launch_spec<T>(LT, nbs, p->spec_smem, s);
     if (e != cudaSuccess) return cuda_check(p, e, "tangent spectral kernel launch");
     e = launch_step_spec<T>(p, LS, nbs, s);
@@ -559,6 +573,7 @@ int tangent_forward_impl(swp_plan* p, const swp_group_state* st, const swp_group
     key.push_back((uint64_t)tan[g].fourier);
     key.push_back((uint64_t)tan[g].resid);
     key.push_back((uint64_t)tan[g].dparams);
+    key.push_back((uint64_t)tan[g].dweights);
     key.push_back((uint64_t)(tan[g].coef_tangents != 0));
   }
   return run_graph(p, key, [&](cudaStream_t cs) { return tangent_steps<T>(p, st, tan, f, t0, nsteps, cs); }, s);
@@ -575,13 +590,21 @@ int init_impl(swp_plan* p, const swp_group_state* st, void* const* phys, const s
 }
 
 template <typename T>
-int output_impl(swp_plan* p, const swp_group_state* st, void* const* out, const swp_flags* f, cudaStream_t s) {
+int output_impl(swp_plan* p, const swp_group_state* st, void* const* out, const swp_flags* f, cudaStream_t s,
+                const swp_group_state* primal = nullptr, const swp_group_tangent* tan = nullptr) {
   int nbg = 0;
   GridLaunch<T> LG = make_grid<T>(p, st, nbg);
   LG.mode = GM_OUTPUT;
   LG.cfg = make_cfg(f);
   LG.cfg.diagnostics = 0;
-  for (int g = 0; g < p->ng; ++g) LG.grp[g].phys_out = (T*)out[g];
+  for (int g = 0; g < p->ng; ++g) {
+    LG.grp[g].phys_out = (T*)out[g];
+    // tangent output: the residual weights' tangents times the primal residual
+    if (primal && tan) {
+      LG.grp[g].resid_p = (const T*)primal[g].resid;
+      LG.grp[g].dw = tan[g].dweights;
+    }
+  }
   return cuda_check(p, launch_grid<T>(LG, nbg, p->grid_smem[GM_OUTPUT], s), "output kernel launch");
 }
 
@@ -1010,7 +1033,8 @@ int check_scheme(swp_plan* p, const swp_flags* f, bool adjoint) {
     return fail(p, SWP_ERR_ARG, "raw_filter is incompatible with the explicit scheme");
   if (adjoint && f->raw_filter)
     return fail(p, SWP_ERR_UNSUPPORTED,
-                "derivatives (adjoint, tangent) are implemented for the classic Robert-Asselin filter");
+                "the adjoint is implemented for the classic Robert-Asselin filter (RAW-filtered runs "
+                "have tangents only)");
   return SWP_OK;
 }
 
@@ -1240,12 +1264,11 @@ int swp_forward(swp_plan* p, const swp_group_state* st, const swp_flags* f, int 
 static int check_tangent(swp_plan* p, const swp_group_state* st, const swp_group_tangent* tan, const swp_flags* f) {
   if (!p || !st || !tan || !f) return fail(p, SWP_ERR_ARG, "null argument");
   if (int rc = check_scheme(p, f, false)) return rc;
-  if (f->raw_filter)
-    return fail(p, SWP_ERR_UNSUPPORTED, "the tangent is implemented for the classic Robert-Asselin filter");
   if (f->test == 1) return fail(p, SWP_ERR_UNSUPPORTED, "tangent of test=1 (fixed winds) is not implemented");
   if (f->diagnostics) return fail(p, SWP_ERR_UNSUPPORTED, "tangent runs with diagnostics off (no blow-up gate)");
   for (int g = 0; g < p->ng; ++g)
-    if (!tan[g].fourier || !tan[g].resid || !tan[g].dparams || !st[g].fourier || !st[g].params || !st[g].member)
+    if (!tan[g].fourier || !tan[g].resid || !tan[g].dparams || !tan[g].dweights || !st[g].fourier ||
+        !st[g].params || !st[g].member)
       return fail(p, SWP_ERR_ARG, "missing tangent buffer");
   return check_align(p, st, nullptr, nullptr, tan);
 }
@@ -1275,7 +1298,8 @@ int swp_tangent_output(swp_plan* p, const swp_group_state* st, const swp_group_t
   swp_group_state tst[MAXG];
   tangent_states(p, st, tan, tst);
   cudaStream_t s = (cudaStream_t)stream;
-  return p->precision == SWP_FP64 ? output_impl<double>(p, tst, out, f, s) : output_impl<float>(p, tst, out, f, s);
+  return p->precision == SWP_FP64 ? output_impl<double>(p, tst, out, f, s, st, tan)
+                                  : output_impl<float>(p, tst, out, f, s, st, tan);
 }
 
 int swp_output_physical(swp_plan* p, const swp_group_state* st, void* const* out, const swp_flags* f, void* stream) {

@@ -128,6 +128,11 @@ __global__ void k_coefs(const double* __restrict__ par, const double* __restrict
       mc[MC_DSIITD * B + b] = (T)w[2];
       mc[MC_DSIITR * B + b] = (T)w[3];
       mc[MC_DITD * B + b] = (T)(dpar ? -dpar[T_TAUDRAG * B + b] / (td * td) : 0.0);
+      // the filter weights: alpha (classic), alpha wa and alpha (1 - wa) (RAW)
+      const double dal = dpar ? dpar[T_ALPHA * B + b] : 0.0, dwa = dpar ? dpar[T_WALPHA * B + b] : 0.0;
+      mc[MC_DALPHA * B + b] = (T)dal;
+      mc[MC_DRAWM * B + b] = (T)(dal * wa + al * dwa);
+      mc[MC_DRAWN * B + b] = (T)(dal * (1.0 - wa) - al * dwa);
     }
   }
 }

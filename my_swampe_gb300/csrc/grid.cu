@@ -300,9 +300,12 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
   __shared__ T s_par[7];     // Phibar, 1/taurad, 1/taudrag, DPhieq, w_curr, w_mid, w_winds
   __shared__ int s_flag[2];  // no drag (taudrag == -1), member blown up
   __shared__ T s_dpar[NGRAD];  // tangent-linear modes: d(taurad, taudrag, DPhieq, Phibar)
+  __shared__ T s_dw[2];        // tangent step and output: tangents of w_curr, w_mid
   if (threadIdx.x == 0) {
     if (MODE == GM_TL_STEP || MODE == GM_TL_INIT)
       for (int q = 0; q < NGRAD; ++q) s_dpar[q] = (T)G.dpar[q * B + b];
+    s_dw[0] = G.dw ? (T)G.dw[b] : (T)0;
+    s_dw[1] = G.dw ? (T)G.dw[B + b] : (T)0;
     const double Pb = G.par[P_PHIBAR * B + b], tr = G.par[P_TAURAD * B + b];
     const double td = G.par[P_TAUDRAG * B + b], DPe = G.par[P_DPHIEQ * B + b];
     const double wc = G.member ? G.member[MS_WCURR * B + b] : 0.0;
@@ -340,11 +343,12 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
       fl[nf++] = F_U; fl[nf++] = F_V;
     }
     const T2* src[8];
-    T wv[8];
+    T wv[8], dwv[8];
     int rfv[8];
 #pragma unroll
     for (int f = 0; f < 8; ++f) {
       wv[f] = (T)0;
+      dwv[f] = (T)0;
       rfv[f] = 0;
       src[f] = nullptr;
       if (f < nf) {
@@ -356,9 +360,13 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
         else if (fld == F_PHI || fld == F_PHI_MID) rf = R_PHI;
         else if (fld == F_U) rf = R_U;
         else if (fld == F_V) rf = R_V;
-        T w = (fld == F_ETA_MID || fld == F_DELTA_MID || fld == F_PHI_MID) ? wmid : wcur;
+        const bool is_mid = fld == F_ETA_MID || fld == F_DELTA_MID || fld == F_PHI_MID;
+        T w = is_mid ? wmid : wcur;
+        // tangent output: the weights' own tangents times the primal residual
+        // (zero for the winds, whose weight is zero once a member has stepped)
+        T dwt = (G.resid_p && rf >= 0 && rf <= R_PHI) ? s_dw[is_mid ? 1 : 0] : (T)0;
         if (fld == F_U || fld == F_V) w = cfg.test == 1 ? (T)1 : wuv;  // test 1: fixed initial winds (model.py:979-983)
-        if (rf >= 0 && G.resid && w != (T)0) { wv[f] = w; rfv[f] = rf; }
+        if (rf >= 0 && G.resid && (w != (T)0 || dwt != (T)0)) { wv[f] = w; dwv[f] = dwt; rfv[f] = rf; }
       }
     }
     if (MODE == GM_STEP) {
@@ -376,20 +384,25 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     // for the fixed test-1 winds): added in shared memory, off the hot loop
     bool need_resid = false;
 #pragma unroll
-    for (int f = 0; f < 8; ++f) need_resid |= (wv[f] != (T)0);
+    for (int f = 0; f < 8; ++f) need_resid |= (wv[f] != (T)0 || dwv[f] != (T)0);
     if (need_resid) {
       for (int t = threadIdx.x; t < nf * JB * L; t += blockDim.x) {
         int n = t % L, fr = t / L, r = fr % JB, f = fr / JB;
-        T w = (T)0;
+        T w = (T)0, dwt = (T)0;
         int rf = 0;
 #pragma unroll
         for (int q = 0; q < 8; ++q)
-          if (q == f) { w = wv[q]; rf = rfv[q]; }
-        if (w != (T)0) {
-          const T* rs = G.resid + rf * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
+          if (q == f) { w = wv[q]; dwt = dwv[q]; rf = rfv[q]; }
+        if (w != (T)0 || dwt != (T)0) {
+          const size_t ro = rf * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
+          const T* rs = G.resid + ro;
           T2 z = zin[(size_t)fr * LS + n];
           z.x += w * rs[0];
           z.y += w * rs[1];
+          if (dwt != (T)0) {
+            z.x += dwt * G.resid_p[ro];
+            z.y += dwt * G.resid_p[ro + 1];
+          }
           zin[(size_t)fr * LS + n] = z;
         }
       }
@@ -496,6 +509,30 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
     __syncthreads();
     T2* zin = c2r_transform<T, Ctx, true>(c, bufB, 8, bufA);
     T2* zout = (zin == bufA) ? bufB : bufA;
+    // The RAW filter leaves the initial-condition residual in the curr eta and
+    // Phi with weight w_curr (the primal step adds it too); its tangent is
+    // w_curr times the tangent residual plus the weight's tangent times the
+    // primal residual.  The winds of a stepped member carry none.
+    {
+      const T wc = s_par[4], dwc = s_dw[0];
+      if ((wc != (T)0 || dwc != (T)0) && G.resid_p && G.resid) {
+        for (int t = threadIdx.x; t < 2 * JB * L; t += blockDim.x) {
+          int n = t % L, fr = t / L, r = fr % JB, q = fr / JB;  // q 0: eta, 1: Phi
+          const size_t ro = (q == 0 ? R_ETA : R_PHI) * PS + ((size_t)b * J + j0 + r) * I + 2 * n;
+          const T* rp = G.resid_p + ro;
+          const T* rt = G.resid + ro;
+          T2 zp = zin[((size_t)q * JB + r) * LS + n];
+          T2 zt = zin[((size_t)(4 + q) * JB + r) * LS + n];
+          zp.x += wc * rp[0];
+          zp.y += wc * rp[1];
+          zt.x += wc * rt[0] + dwc * rp[0];
+          zt.y += wc * rt[1] + dwc * rp[1];
+          zin[((size_t)q * JB + r) * LS + n] = zp;
+          zin[((size_t)(4 + q) * JB + r) * LS + n] = zt;
+        }
+        __syncthreads();
+      }
+    }
     PhysicsTL<T> pt;
     pt.Pb = ph.Pb; pt.itr = ph.itr; pt.itd = ph.itd; pt.DPe = ph.DPe; pt.nodrag = ph.nodrag; pt.forced = ph.forced;
     const int nout = ph.forced ? 8 : 5;

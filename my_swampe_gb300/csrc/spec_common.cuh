@@ -436,7 +436,8 @@ __device__ __forceinline__ void store_step_point(const SpecGroup<T>& G, const St
                                                  typename cplx<T>::type u, typename cplx<T>::type v,
                                                  const typename cplx<T>::type* old,
                                                  const typename cplx<T>::type* mid,
-                                                 const typename cplx<T>::type* lag = nullptr) {
+                                                 const typename cplx<T>::type* lag = nullptr, T dal = (T)0,
+                                                 T dan = (T)0) {
   typedef typename cplx<T>::type T2;
   T2* Fo = G.four_out;
   const int cf[3] = {F_ETA, F_DELTA, F_PHI};
@@ -452,6 +453,13 @@ __device__ __forceinline__ void store_step_point(const SpecGroup<T>& G, const St
       const T2 d = cadd(csub(mid[q], cscale(old[q], (T)2)), nw);
       Fo[rf[q] * FS + o] = cadd(old[q], cscale(d, al));
       if (cfg.raw) nw = csub(nw, cscale(d, an));
+      if (cfg.tl_filter) {
+        // primal step of a tangent run: the filter weights' tangents times this
+        // displacement (the tangent step, launched before, wrote the rest)
+        T2* Ft = G.four_t;
+        Ft[rf[q] * FS + o] = cadd(Ft[rf[q] * FS + o], cscale(d, dal));
+        if (cfg.raw) Ft[cf[q] * FS + o] = csub(Ft[cf[q] * FS + o], cscale(d, dan));
+      }
     }
     Fo[cf[q] * FS + o] = nw;
   }
@@ -541,12 +549,40 @@ __device__ __forceinline__ void write_step_point(const SpecGroup<T>& G, const St
   }
   const T al = G.mco[(cfg.raw ? MC_RAWM : MC_ALPHA) * G.B + b];
   const T an = cfg.raw ? G.mco[MC_RAWN * G.B + b] : (T)0;
-  store_step_point<T>(G, cfg, incr, FS, o, al, an, nw_in, uv, u, v, old, mid, lag);
+  T dal = (T)0, dan = (T)0;
+  if (cfg.tl_filter) {
+    dal = G.mco[(cfg.raw ? MC_DRAWM : MC_DALPHA) * G.B + b];
+    dan = cfg.raw ? G.mco[MC_DRAWN * G.B + b] : (T)0;
+  }
+  store_step_point<T>(G, cfg, incr, FS, o, al, an, nw_in, uv, u, v, old, mid, lag, dal, dan);
 }
 
 // Residual weights of the initial condition in the physical curr / mid fields
 // after a step (the new level is band-limited): classic RA mid = curr + al d,
-// RAW also moves the new level by -an d (model.py:988-1087).
+// RAW also moves the new level by -an d (model.py:988-1087).  With dwc, dwm
+// (tangent runs with filter-weight tangents) their tangents along dal (alpha)
+// and dwa (williams_alpha) go along, from the same weights before the step.
+__device__ __forceinline__ void step_residual_weights_tl(const StepCfg& cfg, double al, double wa, double dal,
+                                                         double dwa, double wc, double wm, double& dwc,
+                                                         double& dwm) {
+  if (cfg.ra_mode == 1) {
+    dwm = dwc;
+    dwc = 0.0;
+  } else if (cfg.ra_mode == 2) {
+    const double dw = wm - 2.0 * wc, ddw = dwm - 2.0 * dwc;
+    if (cfg.raw) {
+      const double m = al * wa, n = al * (1.0 - wa);
+      const double dm = dal * wa + al * dwa, dn = dal * (1.0 - wa) - al * dwa;
+      dwm = dwc + dm * dw + m * ddw;
+      dwc = -(dn * dw + n * ddw);
+    } else {
+      dwm = dwc + dal * dw + al * ddw;
+      dwc = 0.0;
+    }
+  } else {
+    dwc = 0.0;
+  }
+}
 __device__ __forceinline__ void step_residual_weights(const StepCfg& cfg, double al, double wa, double& wc,
                                                       double& wm) {
   if (cfg.ra_mode == 1) {

@@ -507,6 +507,13 @@ __device__ __forceinline__ void spectral_unit(const SpecLaunch<T>& L, const Spec
   if (mode == 0 && m == 0 && threadIdx.x < mt && !sdead[threadIdx.x]) {
     int b = b0 + threadIdx.x;
     double wc = G.member[MS_WCURR * G.B + b], wm = G.member[MS_WMID * G.B + b];
+    if (cfg.tl_filter) {
+      double dwc = G.dw[b], dwm = G.dw[G.B + b];
+      step_residual_weights_tl(cfg, G.par[P_ALPHA * G.B + b], G.par[P_WALPHA * G.B + b],
+                               G.dpar[T_ALPHA * G.B + b], G.dpar[T_WALPHA * G.B + b], wc, wm, dwc, dwm);
+      G.dw[b] = dwc;
+      G.dw[G.B + b] = dwm;
+    }
     step_residual_weights(cfg, G.par[P_ALPHA * G.B + b], G.par[P_WALPHA * G.B + b], wc, wm);
     G.member[MS_WMID * G.B + b] = wm;
     G.member[MS_WCURR * G.B + b] = wc;

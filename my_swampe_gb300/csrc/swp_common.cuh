@@ -326,6 +326,8 @@ struct StepCfg {
   int si_relax;    // semi-implicit: relaxation and drag implicit (forcflag, test None)
   int si_lag_init; // semi-implicit first step: lagged remainder from the current state
   int tl_coef;     // tangent-linear step: differentiate the coefficient tables too
+  int tl_filter;   // primal step of a tangent run: add the filter weights' tangents times the
+                   // displacement to the tangent carries (SpecGroup four_t, dw)
 };
 
 }  // namespace swp

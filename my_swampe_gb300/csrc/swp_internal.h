@@ -23,8 +23,10 @@ enum GradIndex { G_TAURAD = 0, G_TAUDRAG, G_DPHIEQ, G_PHIBAR, NGRAD };
 // Parameter tangents of the tangent-linear model: the adjoint's four, then
 // those that enter only the coefficient tables.
 enum TangentIndex {
-  T_TAURAD = 0, T_TAUDRAG, T_DPHIEQ, T_PHIBAR, T_A, T_DT, T_K6, T_K6PHI, T_OMEGA, T_SIALPHA, NTANGENT
+  T_TAURAD = 0, T_TAUDRAG, T_DPHIEQ, T_PHIBAR, T_A, T_DT, T_K6, T_K6PHI, T_OMEGA, T_SIALPHA, T_ALPHA, T_WALPHA,
+  NTANGENT
 };
+static_assert(NTANGENT == SWP_NTANGENT, "tangent rows of the C ABI");
 
 struct GroupGeom {
   int M = 0, J = 0, I = 0, L = 0;
@@ -110,6 +112,7 @@ enum MCoef {
   MC_DT2, MC_DIA2, MC_DHPB, MC_DDTPB, MC_DPBA2, MC_DPFD, MC_DDT, MC_DOM,
   MC_DSIXI, MC_DSIEX, MC_DSIITD, MC_DSIITR,  // of the semi-implicit shares and rates
   MC_DITD,     // of 1 / taudrag (explicit scheme; no sentinel)
+  MC_DALPHA, MC_DRAWM, MC_DRAWN,  // of alpha, alpha williams_alpha, alpha (1 - williams_alpha)
   NMCO
 };
 template <typename T>
@@ -147,7 +150,11 @@ struct SpecGroup {
   const typename cplx<T>::type* lamY;   // adjoint of the K1 outputs (adjoint launches)
   double* grad;                         // [NGRAD][B] (adjoint launches)
   const typename cplx<T>::type* four_p; // tangent-linear launches: primal state before the step
-  const double* dpar;                   // tangent-linear launches: [NGRAD][B] parameter tangents
+  const double* dpar;                   // tangent-linear launches: [NTANGENT][B] parameter tangents
+  // primal step of a tangent run with filter-weight tangents (cfg.tl_filter):
+  // the tangent Fourier state and the tangents of the residual weights [2][B]
+  typename cplx<T>::type* four_t;
+  double* dw;
   const T* nco;                         // coefficient tables of the call (CoefTables)
   const T* jco;
   const T* djco;
@@ -197,7 +204,9 @@ struct GridGroup {
   double* grad;                         // [NGRAD][B]
   // tangent-linear
   const T* phys_p;                      // primal physical ICs (tangent init)
-  const double* dpar;                   // [NGRAD][B] parameter tangents
+  const double* dpar;                   // [NTANGENT][B] parameter tangents
+  const T* resid_p;                     // primal IC residual (tangent step and output)
+  const double* dw;                     // tangents of the residual weights [2][B] (tangent step and output)
 };
 
 template <typename T>

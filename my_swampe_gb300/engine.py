@@ -107,6 +107,8 @@ class Engine:
             gd["params"][_lib.P_SIALPHA] = 0.5   # RunFlags defaults (model.py:186-187)
             gd["params"][_lib.P_WALPHA] = 0.53
             gd["member"] = torch.zeros((_lib.NMEMBER, gd["B"]), dtype=torch.float64, device=dev)
+            # tangents of the residual weights (member rows w_curr, w_mid) of a tangent run
+            gd["dweights"] = torch.zeros((2, gd["B"]), dtype=torch.float64, device=dev)
             self.groups.append(gd)
         self._geo_cache: Dict[int, Dict[str, torch.Tensor]] = {}
         if autotune:
@@ -358,6 +360,8 @@ class Engine:
         tangents in the order of ``_lib.TANGENT_PARAMS``."""
         four = [torch.zeros_like(gd["fourier"]) for gd in self.groups]
         resid = [torch.zeros_like(gd["resid"]) for gd in self.groups]
+        for gd in self.groups:  # a fresh tangent: the residual weights' tangents start at zero
+            gd["dweights"].zero_()
         dpar = [torch.zeros((_lib.NTANGENT, gd["B"]), dtype=torch.float64, device=self.device) for gd in self.groups]
         return four, resid, dpar
 
@@ -369,8 +373,10 @@ class Engine:
             arr[g].fourier = tfour[g].data_ptr()
             arr[g].resid = tresid[g].data_ptr()
             arr[g].dparams = dpar[g].data_ptr()
-            # rows a..omega enter only the coefficient tables: their pass runs when one is set
+            # rows a..williams_alpha enter only the coefficient tables and the filter
+            # weights: their pass runs when one is set
             arr[g].coef_tangents = int(bool(torch.any(dpar[g][_lib.NGRAD:] != 0)))
+            arr[g].dweights = self.groups[g]["dweights"].data_ptr()
         return arr
 
     def tangent_init(self, flags: RunFlagsC, ics, dics, tfour, tresid, dpar) -> None:

@@ -393,14 +393,16 @@ def run_model_scan(
     ``donate_state`` are accepted for compatibility and have no effect (the
     scan body is always a compiled kernel pair and the state is updated in
     place).  Tensors among taurad, taudrag, DPhieq, Phibar, a, dt, K6, K6Phi,
-    omega, alpha, g and the ``*_init`` fields that require grad (or carry
+    omega, si_alpha, alpha, williams_alpha, g and the ``*_init`` fields that require grad (or carry
     forward-mode tangents) make the
     ``last_state`` curr fields (eta, delta, Phi, U, V) differentiable through
     the hand-written adjoint and tangent-linear kernels, the counterpart of
     ``jax.grad`` / ``jax.jvp`` through the reference's scan.  ``semi_implicit`` selects the semi-implicit leapfrog
     (``semi_implicit_tdiff.py``) and ``raw_filter`` the Robert-Asselin-Williams
-    filter (``model.py:1007-1087``); both run forward only (the hand-written
-    adjoint covers the modified-Euler scheme with the classic filter).
+    filter (``model.py:1007-1087``).  Their parameter gradients (si_alpha,
+    alpha and williams_alpha among them) are tangent-linear runs; the
+    semi-implicit scheme's initial-field gradients come from its adjoint, and
+    the RAW filter has forward-mode initial-field derivatives only.
     """
     if tmax < 2:
         raise ValueError("tmax must be >= 2 (SWAMPE uses a 2-level initialization).")
@@ -467,20 +469,32 @@ def run_model_scan(
                 raise ValueError(f"{name} must have shape {(J, I)}, got {shp}.")
 
     # differentiable inputs: the per-member parameters the adjoint and the tangent
-    # model cover, the initial fields, and alpha and g, which the curr fields of
-    # the modified-Euler scheme do not depend on (their derivative is zero)
+    # model cover, the initial fields, and g.  alpha moves the curr fields only
+    # where the filtered level feeds the trajectory (the semi-implicit scheme's
+    # n-1 base, the RAW filter's new level), williams_alpha only with the RAW
+    # filter; elsewhere their derivative (and that of g) is zero.
     # K6Phi=None means K6Phi = K6 (model.py:512): then K6 drives both
     coef_inputs = dict(a=a, dt=dt, K6=K6, K6Phi=K6 if K6Phi is None else K6Phi, omega=omega, si_alpha=si_alpha)
+    zero_deriv = [g]
+    if semi_implicit or raw_filter:
+        coef_inputs["alpha"] = alpha
+    else:
+        zero_deriv.append(alpha)
+    if raw_filter:
+        coef_inputs["williams_alpha"] = williams_alpha
+    else:
+        zero_deriv.append(williams_alpha)
     ic_inputs = (eta0_init, delta0_init, Phi0_init, U0_init, V0_init)
-    diff_inputs = (taurad, taudrag, DPhieq, Phibar, *ic_inputs, alpha, g, *coef_inputs.values())
+    diff_inputs = (taurad, taudrag, DPhieq, Phibar, *ic_inputs, *zero_deriv, *coef_inputs.values())
     needs_grad = any(_tracked(x) for x in diff_inputs)
-    if _tracked(williams_alpha):
-        raise NotImplementedError("derivatives through the RAW filter are not implemented")
     if needs_grad:
-        if raw_filter or test == 1:
-            raise NotImplementedError("derivatives are implemented with the classic filter and test None or 2")
+        if test == 1:
+            raise NotImplementedError("derivatives are implemented for test None or 2")
         if U0_init is None and (_tracked(eta0_init) or _tracked(delta0_init)):
             raise NotImplementedError("derivatives with respect to eta0_init / delta0_init need U0_init and V0_init")
+        if raw_filter and any(torch.is_tensor(x) and x.requires_grad for x in ic_inputs):
+            raise NotImplementedError("reverse-mode initial-field gradients through the RAW filter are not "
+                                      "implemented (forward mode and parameter gradients are)")
 
     split = (batched and B >= _SPLIT_MIN_B and tmax > starttime_eff and test != 1
              and not (return_history or diagnostics or semi_implicit or raw_filter))
@@ -494,6 +508,7 @@ def run_model_scan(
     static = build_static(M=M, dt=nd(dt), a=nd(a), omega=nd(omega), g=nd(g), Phibar=nd(Phibar), taurad=nd(taurad),
                           taudrag=nd(taudrag), DPhieq=nd(DPhieq), K6=nd(K6), K6Phi=nd(K6Phi), test=test, engine=eng)
 
+    ic_derivs: Dict[str, torch.Tensor] = {}  # d(initial fields) / d(parameter), outside the autograd graph
     if have_ic:
         eta0 = _prepare_ic(eta0_init, J, I, B, batched, "eta0_init", dev)
         delta0 = _prepare_ic(delta0_init, J, I, B, batched, "delta0_init", dev)
@@ -512,7 +527,9 @@ def run_model_scan(
         eta0, delta0, Phi0, U0, V0 = (f.expand(B, J, I) for f in fields)
         # the analytic fields are polynomials of degree <= 2 in a, omega, Phibar
         # (initial_conditions.py:18-47, 88-239), so a centred difference is their
-        # exact derivative: carry it into the differentiable run
+        # exact derivative: carry it into the differentiable run (with the RAW
+        # filter, which has no adjoint, as initial-field tangents of the
+        # parameter's tangent runs)
         for x, i, name in ((a, 0, "a"), (omega, 1, "omega"), (Phibar, 2, "Phibar")):
             if _tracked(x):
                 h = 1e-3 * abs((av, omv, pb)[i]) or 1e-3
@@ -522,6 +539,9 @@ def run_model_scan(
                 arg[i] -= 2 * h
                 fm = _analytic_ic(M, *arg, test, float(a1), dev)
                 d = [(u - v) / (2 * h) for u, v in zip(fp, fm)]
+                if raw_filter:
+                    ic_derivs[name] = torch.stack([dd.expand(B, J, I) for dd in d], 0)
+                    continue
                 dx = x - x.detach()
                 eta0, delta0, Phi0, U0, V0 = (f + dx * dd.expand(B, J, I)
                                               for f, dd in zip((eta0, delta0, Phi0, U0, V0), d))
@@ -547,7 +567,7 @@ def run_model_scan(
             M, B, precision, device, flags, starttime_eff, T, ics=torch.stack((eta0, delta0, Phi0, U0, V0), 0),
             pvals=dict(dt=dt, a=a, omega=omega, Phibar=Phibar, taurad=taurad, taudrag=taudrag,
                        DPhieq=DPhieq if test is None else 0.0, K6=K6, K6Phi=K6Phi_eff, alpha=alpha),
-            needs_grad=needs_grad, coef_inputs=coef_inputs, zero_deriv=(alpha, g), batched=batched)
+            needs_grad=needs_grad, coef_inputs=coef_inputs, zero_deriv=tuple(zero_deriv), batched=batched)
         return dict(static=static, t_seq=torch.arange(starttime_eff, tmax, dtype=torch.int32, device=dev),
                     last_state=last, starttime=starttime_eff)
     diag = eng.new_diag(T) if diagnostics else None
@@ -571,14 +591,15 @@ def run_model_scan(
             eng.forward(flags, t0=starttime_eff, nsteps=T, row0=0, diag=diag, hist=hist, write_prev_last=True)
             saved = (four.clone(), gd["member"].clone())
         dflags = RunFlagsC(scheme=2 if semi_implicit else (1 if expflag else 0), forcflag=forcflag, diffflag=diffflag,
-                           modalflag=modalflag, test=test, diagnostics=False, t_start=starttime_eff)
+                           modalflag=modalflag, test=test, diagnostics=False, t_start=starttime_eff,
+                           raw_filter=bool(raw_filter))
         dpar = dict(taurad=_per_member(taurad, B, dev), taudrag=_per_member(taudrag, B, dev),
                     DPhieq=_per_member(DPhieq if test is None else 0.0, B, dev), Phibar=_per_member(Phibar, B, dev))
         for k, x in coef_inputs.items():
             if _tracked(x):
                 dpar[k] = _per_member(x, B, dev)
-        dcurr = adjoint.integrate(eng, dflags, starttime_eff, T, [dpar], [ics])[0]
-        for x in (alpha, g):  # zero derivative, but part of the graph
+        dcurr = adjoint.integrate(eng, dflags, starttime_eff, T, [dpar], [ics], ic_derivs=[ic_derivs])[0]
+        for x in zero_deriv:  # zero derivative, but part of the graph
             if _tracked(x):
                 dcurr = dcurr + 0.0 * x.to(dcurr.dtype).sum()
         if return_history or diagnostics:  # the gated run's state (dead flags included)
@@ -1004,8 +1025,8 @@ def simulate_scan_last(*, static: Static, flags: "RunFlags", state0: State, t_se
     st = _state_after(eng, flags, phys, batched, state0)
     tracked = [k for k in _lib.TANGENT_PARAMS if k in vals and _tracked(vals[k])]
     if tracked and n > 0:
-        if flags.raw_filter or test == 1:
-            raise NotImplementedError("derivatives are implemented with the classic filter and test None or 2")
+        if test == 1:
+            raise NotImplementedError("derivatives are implemented for test None or 2")
         B = eng.groups[0]["B"]
         dev = eng.device
         params = [torch.as_tensor(vals[k], dtype=torch.float64, device=dev) if k in vals else

@@ -45,12 +45,6 @@ def test_coefficient_parameter_gradients_match_finite_differences(cuda, name, va
     assert abs(g_ad - g_fd) <= 1e-4 * abs(g_fd), (name, g_ad, g_fd)
 
 
-def test_raw_filter_parameters_refuse_gradients(cuda):
-    th = torch.tensor(0.53, dtype=torch.float64, device="cuda", requires_grad=True)
-    with pytest.raises(NotImplementedError):
-        _loss("williams_alpha", th, raw_filter=True)
-
-
 def test_jvp_returns_finite_for_DPhieq(cuda):
     """test_autodiff.py:89-99"""
     with fwAD.dual_level():

@@ -7,6 +7,8 @@ import pytest
 import torch
 import torch.autograd.forward_ad as fwAD
 
+from my_swampe_gb300._lib import NTANGENT as NTAN
+
 pytestmark = pytest.mark.gpu
 
 NSTEPS = 12
@@ -27,7 +29,7 @@ def _setup(prec="fp64", B=2, test=None, seed=5):
     dics = (ics * w).contiguous()
     dics[2] += 1e-2 * wl["ics"][2].flip(-1)
     p = wl["params"]
-    dpar = torch.zeros((10, B), dtype=torch.float64, device=eng.device)
+    dpar = torch.zeros((NTAN, B), dtype=torch.float64, device=eng.device)
     dpar[:4] = torch.stack([0.1 * p["taurad"], 0.1 * p["taudrag"], 0.1 * p["DPhieq"],
                             torch.full((B,), 0.05 * 3.0e5, dtype=torch.float64, device=eng.device)])
     dpar[:4] *= torch.rand((4, B), generator=g, dtype=torch.float64).to(eng.device) - 0.5
@@ -47,11 +49,13 @@ def _forward(eng, flags, wl, ics, params_shift=None, h=0.0):
 
     p = dict(wl["params"])
     if params_shift is not None:
-        names = ("taurad", "taudrag", "DPhieq", "Phibar", "a", "dt", "K6", "K6Phi", "omega", "si_alpha")
+        names = ("taurad", "taudrag", "DPhieq", "Phibar", "a", "dt", "K6", "K6Phi", "omega", "si_alpha", "alpha",
+                 "williams_alpha")
+        defaults = dict(si_alpha=0.5, alpha=0.01, williams_alpha=0.53)
         for k in range(params_shift.shape[0]):
             name = names[k]
-            if name == "si_alpha" and name not in p:
-                p[name] = 0.5
+            if name not in p:
+                p[name] = defaults[name]
             p[name] = p[name] + h * params_shift[k]
     workloads.apply_params(eng, 0, p)
     eng.init_state([ics.to(eng.rdtype)], flags)
@@ -90,7 +94,7 @@ def test_coefficient_tangents_match_central_differences(cuda, name, row, scale, 
     eng, flags, wl, ics, _, _ = _setup()
     p = wl["params"]
     base = float(p.get(name, p["K6"]))
-    dpar = torch.zeros((10, 2), dtype=torch.float64, device=eng.device)
+    dpar = torch.zeros((NTAN, 2), dtype=torch.float64, device=eng.device)
     dpar[row] = torch.tensor([scale * base, -0.5 * scale * base], dtype=torch.float64)
     zero = torch.zeros_like(ics)
     tl = _tangent(eng, flags, wl, ics, zero, dpar)
@@ -243,7 +247,7 @@ def test_tangent_refuses_unsupported(cuda):
 
     eng, flags, wl, ics, dics, dpar = _setup()
     tf, tr, _ = eng.new_tangent_buffers()
-    for bad in (RunFlagsC(raw_filter=True), RunFlagsC(test=1), RunFlagsC(diagnostics=True)):
+    for bad in (RunFlagsC(test=1), RunFlagsC(diagnostics=True)):
         with pytest.raises(RuntimeError):
             eng.tangent_forward(bad, 2, 2, tf, tr, [dpar])
 
@@ -270,7 +274,7 @@ def test_semi_implicit_parameter_tangents_match_central_differences(cuda, name, 
     p = wl["params"]
     base = p[name] if torch.is_tensor(p.get(name)) else torch.full((2,), float(p[name]), dtype=torch.float64,
                                                                        device=eng.device)
-    dpar = torch.zeros((10, 2), dtype=torch.float64, device=eng.device)
+    dpar = torch.zeros((NTAN, 2), dtype=torch.float64, device=eng.device)
     dpar[row] = scale * base * torch.tensor([1.0, -0.5], dtype=torch.float64, device=eng.device)
     tl = _tangent(eng, flags, wl, ics, torch.zeros_like(ics), dpar)
     fd = (_forward(eng, flags, wl, ics, dpar, h) - _forward(eng, flags, wl, ics, dpar, -h)) / (2 * h)
@@ -282,7 +286,7 @@ def test_semi_implicit_parameter_tangents_match_central_differences(cuda, name, 
 
 def test_semi_implicit_initial_field_tangent(cuda):
     eng, flags, wl, ics, dics = _si_setup()
-    dpar = torch.zeros((10, 2), dtype=torch.float64, device=eng.device)
+    dpar = torch.zeros((NTAN, 2), dtype=torch.float64, device=eng.device)
     tl = _tangent(eng, flags, wl, ics, dics, dpar)
     h = 1e-6
     fd = (_forward(eng, flags, wl, ics + h * dics) - _forward(eng, flags, wl, ics - h * dics)) / (2 * h)
@@ -303,7 +307,7 @@ def test_tangent_other_truncations(cuda, M, scheme):
     flags = RunFlagsC(scheme=scheme, diagnostics=False, t_start=2)
     ics = wl["ics"]
     dics = (ics * 0.01).contiguous()
-    dpar = torch.zeros((10, 2), dtype=torch.float64, device=eng.device)
+    dpar = torch.zeros((NTAN, 2), dtype=torch.float64, device=eng.device)
     dpar[3] = 3.0e3
     dpar[4] = 8.2e5
 
@@ -342,7 +346,7 @@ def test_explicit_scheme_tangents_match_central_differences(cuda, name, row, sca
     p = wl["params"]
     base = p[name] if torch.is_tensor(p.get(name)) else torch.full((2,), float(p[name]), dtype=torch.float64,
                                                                        device=eng.device)
-    dpar = torch.zeros((10, 2), dtype=torch.float64, device=eng.device)
+    dpar = torch.zeros((NTAN, 2), dtype=torch.float64, device=eng.device)
     dpar[row] = scale * base * torch.tensor([1.0, -0.5], dtype=torch.float64, device=eng.device)
     tl = _tangent(eng, flags, wl, ics, 1e-3 * dics, dpar)
     fd = (_forward(eng, flags, wl, ics + h * 1e-3 * dics, dpar, h) -
