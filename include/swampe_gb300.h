@@ -332,6 +332,56 @@ int swp_plan_set_concurrency(swp_plan* plan, int on);
 #define SWP_WAIT_LIMIT_DEFAULT (1u << 22)
 int swp_plan_set_wait_limit(swp_plan* plan, unsigned int max_polls);
 
+/* ---------------------------------------------------------------- emission
+ * The retrieval's emission stage on ensembles of terminal Phi fields
+ * (retrieval/scripts/pipeline.py:690-1000), FP64 like the reference's.  These
+ * entries take no plan: every array is a device pointer, fields are
+ * real[B][J][I] (latitude-major pixels, the model's grid), and a status of
+ * SWP_ERR_ARG means a null pointer, a size below 1 or a bad configuration.
+ * Non-finite inputs give all-NaN outputs per member, as the reference's guards. */
+#define SWP_EMISSION_MAX_BANDS 8
+typedef struct {
+  int temp_mode;          /* 0 "geopotential": T = (Phibar + Phi) / R_d;
+                             1 "linear": T = T_ref + Phi / phi_to_T_scale; then max(T, Tmin)
+                             (pipeline.py:696-714 phi_to_temperature)                       */
+  double R_d, T_ref, phi_to_T_scale, Tmin;
+  int model;              /* 0 "bolometric": T^4; 1 "planck": sum_k w_k / (expm1(x_k) + 1e-30),
+                             x_k = h c / (lambda_k kB T) clipped to [0, x_clip]
+                             (pipeline.py:716-754 temperature_to_intensity)                 */
+  int nbands;             /* planck: wavelengths used, 1..SWP_EMISSION_MAX_BANDS            */
+  double wavelengths[SWP_EMISSION_MAX_BANDS];   /* m                                        */
+  double band_weights[SWP_EMISSION_MAX_BANDS];  /* summing to 1 (one band: weight 1)        */
+  double x_clip;
+} swp_emission_cfg;
+
+/* One pass of the emission maps per member.  input selects what `in` holds
+ * (0 Phi, 1 T, 2 intensity) and stage what `out` receives (0 T, 1 intensity,
+ * 2 the weighted relative intensity sqrt(w_j) I / I_mean that the projector
+ * multiplies, I_mean the w-weighted mean over the finite pixels); input <= stage.
+ * Phibar: double[B] (geopotential mode); w_lat: double[J] Gauss weights
+ * (stage 2); ok: int[B] or NULL, set at stage 2 to whether the map passed the
+ * guards of intensity_map_to_y_dense (pipeline.py:821-837). */
+int swp_emission_map(const double* in, const double* Phibar, int B, int J, int I, const double* w_lat,
+                     const swp_emission_cfg* cfg, int input, int stage, double* out, int* ok, void* stream);
+/* y[b] = projector . rhs[b], divided by its first coefficient, all NaN unless
+ * ok[b], y0 and every coefficient pass the guards (pipeline.py:838-846
+ * intensity_map_to_y_dense).  projector: double[ncoef][npix], the weighted
+ * ridge least-squares inverse of the Ylm design matrix (pipeline.py:808-819). */
+int swp_emission_project(const double* rhs, const int* ok, int B, int npix, const double* projector, int ncoef,
+                         double* y, void* stream);
+/* The planet's light curve, linear in its map: lc[b][t] = amplitude[b]
+ * sum_c design[t][c] y[b][c] (pipeline.py:983-994, amplitude = planet_fpfs;
+ * design = the light-curve model's flux for unit coefficient vectors;
+ * amplitude NULL = 1). */
+int swp_phase_curve_linear(const double* y, const double* design, const double* amplitude, int B, int ncoef,
+                           int ntimes, double* lc, void* stream);
+/* The simplified phase-curve projection of the reference's parity test
+ * (unit_tests/test_parity_reference_regression.py:67-82): flux[b][k] = sum over
+ * pixels of Phi max(cos(lambda_i - phase_k), 0) sqrt(1 - mu_j^2), lambda_i =
+ * -pi + 2 pi i / I, divided by mean_k |flux| when positive.  mus: double[J]. */
+int swp_phase_curve_simple(const double* phi, int B, int J, int I, const double* mus, const double* phases,
+                           int nphase, double* flux, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

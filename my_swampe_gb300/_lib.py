@@ -86,6 +86,24 @@ class Flags(ctypes.Structure):
     ]
 
 
+EMISSION_MAX_BANDS = 8  # swampe_gb300.h SWP_EMISSION_MAX_BANDS
+
+
+class EmissionCfg(ctypes.Structure):
+    _fields_ = [
+        ("temp_mode", ctypes.c_int),
+        ("R_d", ctypes.c_double),
+        ("T_ref", ctypes.c_double),
+        ("phi_to_T_scale", ctypes.c_double),
+        ("Tmin", ctypes.c_double),
+        ("model", ctypes.c_int),
+        ("nbands", ctypes.c_int),
+        ("wavelengths", ctypes.c_double * EMISSION_MAX_BANDS),
+        ("band_weights", ctypes.c_double * EMISSION_MAX_BANDS),
+        ("x_clip", ctypes.c_double),
+    ]
+
+
 EXPORTS = (
     "swp_plan_create", "swp_plan_destroy", "swp_plan_dims", "swp_last_error", "swp_geometry",
     "swp_init_state", "swp_diagnose_winds", "swp_forward", "swp_output_physical",
@@ -94,7 +112,8 @@ EXPORTS = (
     "swp_tc_selftest", "swp_device_status", "swp_plan_uses_tensor_cores", "swp_forward_stored",
     "swp_adjoint_stored", "swp_plan_autotune", "swp_plan_tiles", "swp_plan_set_tile",
     "swp_tangent_init", "swp_tangent_forward", "swp_tangent_output", "swp_plan_set_concurrency",
-    "swp_plan_set_wait_limit",
+    "swp_plan_set_wait_limit", "swp_emission_map", "swp_emission_project", "swp_phase_curve_linear",
+    "swp_phase_curve_simple",
 )
 
 _lib = None
@@ -149,6 +168,10 @@ def load(path: os.PathLike | str | None = None) -> ctypes.CDLL:
         "swp_tangent_output": (i, [vp, gsp, gtp, vpp, fp, vp]),
         "swp_plan_set_concurrency": (i, [vp, i]),
         "swp_plan_set_wait_limit": (i, [vp, ctypes.c_uint]),
+        "swp_emission_map": (i, [vp, vp, i, i, i, vp, ctypes.POINTER(EmissionCfg), i, i, vp, vp, vp]),
+        "swp_emission_project": (i, [vp, vp, i, i, vp, i, vp, vp]),
+        "swp_phase_curve_linear": (i, [vp, vp, vp, i, i, i, vp, vp]),
+        "swp_phase_curve_simple": (i, [vp, i, i, i, vp, vp, i, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
