@@ -475,6 +475,7 @@ def run_ours(args):
     # ---------------- other workloads: the drop-in API's forward rate, the mixed-truncation ensemble
     dropin = None if args.skip_dropin else _dropin_leg()
     mixed = None if args.skip_mixed else _mixed_leg()
+    emission = None if args.skip_emission else _emission_leg()
 
     # ---------------- CPU baseline (oracle restatement, torch autograd, host cores)
     cpu = None
@@ -517,6 +518,7 @@ def run_ours(args):
         "fp64_plain_gpu": fp64,
         "dropin_forward": dropin,
         "mixed_truncations": mixed,
+        "emission_stage": emission,
         "cpu_baseline": cpu,
         "gpu_launches": launches * args.steps,
         "clocks": clocks,
@@ -639,6 +641,46 @@ def _mixed_leg(steps=2):
                         "one plan (groups concurrent)",
             "member_steps_per_s": round(rate, 1), "adjoint_states": store, "tensor_core_groups": tc_groups,
             "error_fast_vs_fp64": err}
+
+
+def _emission_leg(B=256, ydeg=10, ntimes=200, reps=20):
+    """The retrieval's emission stage on B terminal Phi fields (M = 42 grid):
+    Phi -> T -> intensity -> ydeg-10 Ylm coefficients -> phase curve, FP64.
+    The projector and the light-curve design matrix are seeded random
+    matrices of the right shapes (the kernels' cost does not depend on their
+    values)."""
+    import numpy as np
+    import torch
+
+    from my_swampe_gb300 import emission as em
+
+    J, I = 64, 128
+    dev = torch.device("cuda")
+    gen = torch.Generator(device=dev).manual_seed(42)
+    ncoef = (ydeg + 1) ** 2
+    lat = torch.linspace(-1.5, 1.5, J, dtype=torch.float64, device=dev)[:, None]
+    lon = torch.linspace(-np.pi, np.pi, I + 1, dtype=torch.float64, device=dev)[None, :I]
+    phi = (4e4 * torch.cos(lon) * torch.cos(lat))[None] * (1 + torch.rand((B, 1, 1), generator=gen, device=dev,
+                                                                          dtype=torch.float64))
+    P = torch.randn((ncoef, J * I), generator=gen, device=dev, dtype=torch.float64) / (J * I)
+    A = torch.randn((ntimes, ncoef), generator=gen, device=dev, dtype=torch.float64)
+    w = torch.cos(lat[:, 0]) * (np.pi / J)
+    amp = torch.full((B,), 1500e-6, dtype=torch.float64, device=dev)
+    cfg = em.EmissionConfig()
+
+    def call():
+        y = em.emission_coefficients(phi, 4e5, P, w, cfg)
+        return em.phase_curve(y, A, amp)
+
+    lc = call()
+    assert bool(torch.isfinite(lc).all())
+    times = _time_steps(call, reps, 3, lambda: None)
+    t = float(np.median(times))
+    alg = (B * J * I + ncoef * J * I) * 8  # each Phi field and the projector read once
+    return {"workload": f"B={B} terminal Phi fields (M=42 grid) -> T -> T^4 -> ydeg={ydeg} coefficients "
+                        f"({ncoef}) -> phase curve at {ntimes} times, FP64",
+            "ms_per_call": round(1e3 * t, 4), "members_per_s": round(B / t, 1),
+            "algorithmic_gbs": round(alg / t / 1e9, 1), "launches_per_call": 4}
 
 
 def _cpu_baseline(members, nsteps):
@@ -765,6 +807,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-dropin", action="store_true", help="skip the drop-in API forward leg")
     ap.add_argument("--skip-mixed", action="store_true", help="skip the mixed-truncation leg")
+    ap.add_argument("--skip-emission", action="store_true", help="skip the emission-stage leg")
     ap.add_argument("--cpu-members", type=int, default=1)
     ap.add_argument("--cpu-nsteps", type=int, default=40)
     ap.add_argument("--ref-nsteps", type=int, default=20)

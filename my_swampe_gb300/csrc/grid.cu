@@ -859,6 +859,7 @@ __host__ __device__ constexpr int grid_jb(int M, int mode) {
 template <typename T, int MODE>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (MODE == GM_ADJ_STEP ? 4 : 3) : 2)
     k_grid(const __grid_constant__ GridLaunch<T> Lc) {
+  pdl_enter();
   int idx;
   const GridGroup<T>& G = pick_ggroup(Lc, idx);
   switch (G.g.M) {  // groups of different truncations share one launch
@@ -906,20 +907,21 @@ cudaError_t launch_grid(const GridLaunch<T>& L0, int nblocks0, size_t smem, cuda
     nblocks += G.B * G.njb;
   }
   L.prefix[L.ng] = nblocks;
+  cudaError_t e = cudaSuccess;
   switch (L.mode) {
-    case GM_STEP: k_grid<T, GM_STEP><<<nblocks, 256, smem, s>>>(L); break;
-    case GM_INIT: k_grid<T, GM_INIT><<<nblocks, 256, smem, s>>>(L); break;
-    case GM_OUTPUT: k_grid<T, GM_OUTPUT><<<nblocks, 256, smem, s>>>(L); break;
-    case GM_WINDS: k_grid<T, GM_WINDS><<<nblocks, 256, smem, s>>>(L); break;
-    case GM_ADJ_STEP: k_grid<T, GM_ADJ_STEP><<<nblocks, 256, smem, s>>>(L); break;
-    case GM_ADJ_INIT: k_grid<T, GM_ADJ_INIT><<<nblocks, 256, smem, s>>>(L); break;
-    case GM_ADJ_OUTPUT: k_grid<T, GM_ADJ_OUTPUT><<<nblocks, 256, smem, s>>>(L); break;
-    case GM_FWD2: k_grid<T, GM_FWD2><<<nblocks, 256, smem, s>>>(L); break;
-    case GM_TL_STEP: k_grid<T, GM_TL_STEP><<<nblocks, 256, smem, s>>>(L); break;
-    case GM_TL_INIT: k_grid<T, GM_TL_INIT><<<nblocks, 256, smem, s>>>(L); break;
+    case GM_STEP: e = launch_pdl(k_grid<T, GM_STEP>, nblocks, 256, smem, s, L); break;
+    case GM_INIT: e = launch_pdl(k_grid<T, GM_INIT>, nblocks, 256, smem, s, L); break;
+    case GM_OUTPUT: e = launch_pdl(k_grid<T, GM_OUTPUT>, nblocks, 256, smem, s, L); break;
+    case GM_WINDS: e = launch_pdl(k_grid<T, GM_WINDS>, nblocks, 256, smem, s, L); break;
+    case GM_ADJ_STEP: e = launch_pdl(k_grid<T, GM_ADJ_STEP>, nblocks, 256, smem, s, L); break;
+    case GM_ADJ_INIT: e = launch_pdl(k_grid<T, GM_ADJ_INIT>, nblocks, 256, smem, s, L); break;
+    case GM_ADJ_OUTPUT: e = launch_pdl(k_grid<T, GM_ADJ_OUTPUT>, nblocks, 256, smem, s, L); break;
+    case GM_FWD2: e = launch_pdl(k_grid<T, GM_FWD2>, nblocks, 256, smem, s, L); break;
+    case GM_TL_STEP: e = launch_pdl(k_grid<T, GM_TL_STEP>, nblocks, 256, smem, s, L); break;
+    case GM_TL_INIT: e = launch_pdl(k_grid<T, GM_TL_INIT>, nblocks, 256, smem, s, L); break;
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 template cudaError_t launch_grid<double>(const GridLaunch<double>&, int, size_t, cudaStream_t);
 template cudaError_t launch_grid<float>(const GridLaunch<float>&, int, size_t, cudaStream_t);

@@ -523,6 +523,7 @@ __device__ __forceinline__ void spectral_unit(const SpecLaunch<T>& L, const Spec
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ SpecLaunch<T> L) {
+  pdl_enter();
   for_each_unit(L, [&](const SpecGroup<T>& G, int idx) { spectral_unit<T>(L, G, idx); });
 }
 
@@ -863,6 +864,7 @@ __device__ __forceinline__ void spectral_adj_unit(const SpecLaunch<T>& L, const 
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_spectral_adj(const __grid_constant__ SpecLaunch<T> L) {
+  pdl_enter();
   for_each_unit(L, [&](const SpecGroup<T>& G, int idx) { spectral_adj_unit<T>(L, G, idx); });
 }
 
@@ -889,14 +891,22 @@ template <typename T>
 cudaError_t launch_spec_adj(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
   const int grid = L.sched ? persistent_blocks(k_spectral_adj<T>, nblocks, smem) : nblocks;
-  k_spectral_adj<T><<<grid, 256, smem, s>>>(L);
-  return cudaGetLastError();
+  cudaError_t e = launch_pdl(k_spectral_adj<T>, grid, 256, smem, s, L);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 template cudaError_t launch_spec_adj<double>(const SpecLaunch<double>&, int, size_t, cudaStream_t);
 template cudaError_t launch_spec_adj<float>(const SpecLaunch<float>&, int, size_t, cudaStream_t);
 
 // Largest dynamic shared memory a SIMT kernel may request: 227 KB per block
 // minus its static shared memory (the persistent scheduler's unit slot).
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("SWP_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 void spec_set_attributes() {
   cudaFuncSetAttribute(k_spectral<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_DYN_SMEM_MAX);
   cudaFuncSetAttribute(k_spectral<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_DYN_SMEM_MAX);
@@ -908,8 +918,8 @@ template <typename T>
 cudaError_t launch_spec(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
   const int grid = L.sched ? persistent_blocks(k_spectral<T>, nblocks, smem) : nblocks;
-  k_spectral<T><<<grid, 256, smem, s>>>(L);
-  return cudaGetLastError();
+  cudaError_t e = launch_pdl(k_spectral<T>, grid, 256, smem, s, L);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 template cudaError_t launch_spec<double>(const SpecLaunch<double>&, int, size_t, cudaStream_t);
 template cudaError_t launch_spec<float>(const SpecLaunch<float>&, int, size_t, cudaStream_t);

@@ -330,4 +330,18 @@ struct StepCfg {
                    // displacement to the tangent carries (SpecGroup four_t, dw)
 };
 
+// Programmatic dependent launch.  The step kernels are launched with the
+// programmatic-serialization attribute (launch_pdl), so that a kernel's CTAs
+// can be scheduled while its predecessor in the stream drains its last wave.
+// Every such kernel lets its own dependent launch at once and then waits, before
+// its first access to global memory that another kernel writes, until the
+// predecessor has completed and its writes are visible.  Launched without the
+// attribute, both instructions return at once.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_enter() {
+  pdl_trigger();
+  pdl_wait();
+}
+
 }  // namespace swp

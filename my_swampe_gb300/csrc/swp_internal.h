@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <string>
+#include <utility>
 #include <vector>
 #include "swp_common.cuh"
 #include "../../include/swampe_gb300.h"
@@ -231,6 +232,25 @@ enum GridMode {
   GM_TL_INIT = 9,    // tangent of GM_INIT
   NGRIDMODE = 10
 };
+
+// Launch of a step kernel with programmatic stream serialization (see
+// pdl_enter): on unless the environment sets SWP_PDL=0.
+bool pdl_enabled();
+template <typename... Params, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(Params...), int nblocks, int threads, size_t smem, cudaStream_t s,
+                       Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)nblocks);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 template <typename T> size_t spec_smem_bytes(int M, int J, int MT);
 template <typename T> size_t spec_adj_smem_bytes(int M, int J, int MT);

@@ -235,6 +235,7 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_tc(const __grid_const
   constexpr int NSLOT = NSPX + NSH;
   constexpr int MT = S::MT, J = S::J, JH = S::JH, CNT = S::CNT;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
+  pdl_trigger();
   int idx;
   const SpecGroup<T>& G = pick_group(L, idx);
   int gi = 0;
@@ -270,13 +271,25 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_tc(const __grid_const
   // what thread 0 has issued, for the bounded drain on failure
   int n_tma = 0, n_in = 0, n_c1 = 0, n_c2 = 0;
 
-  // ---- phase 0: barriers; bulk copies of the tile's inputs (one contiguous block
-  // of mt x J values per field) and of the forward basis; TMEM; coefficients; blow-up gate
+  // ---- phase 0: barriers; bulk copies of the forward basis and of the tile's
+  // inputs (one contiguous block of mt x J values per field); TMEM;
+  // coefficients; blow-up gate.  The basis and TMEM do not depend on the
+  // previous kernel in the stream: they come before the wait for it.
   if (threadIdx.x == 0) {
     *sflag = 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) tc::mbar_init(&mbar[q], 1);
     tc::fence_mbar_init();
+    tc::mbar_expect_tx(&mbar[0], (uint32_t)(S::B1 * sizeof(float)));
+    tc::bulk_g2s(sB, gbasis + (size_t)m * S::BLOCK, (uint32_t)(S::B1 * sizeof(float)), &mbar[0]);
+    n_tma = 1;
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, S::TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  pdl_wait();
+  if (threadIdx.x == 0) {
     const uint32_t row_bytes = (uint32_t)(mt * J * sizeof(T2));
     tc::mbar_expect_tx(&mbar[3], row_bytes * S::NIN);
 #pragma unroll
@@ -286,13 +299,6 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_tc(const __grid_const
                    &mbar[3]);
     }
     n_in = 1;
-    tc::mbar_expect_tx(&mbar[0], (uint32_t)(S::B1 * sizeof(float)));
-    tc::bulk_g2s(sB, gbasis + (size_t)m * S::BLOCK, (uint32_t)(S::B1 * sizeof(float)), &mbar[0]);
-    n_tma = 1;
-  }
-  if (warp == 0) {
-    tc::tmem_alloc(tslot, S::TMEM_COLS);
-    tc::tmem_relinquish();
   }
   if (threadIdx.x < MT) {
     const int bt = threadIdx.x;
@@ -680,6 +686,7 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_c
   constexpr int NKADJ = 8;
   constexpr int MT = S::MT, J = S::J, JH = S::JH, CNT = S::CNT;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
+  pdl_trigger();
   int idx;
   const SpecGroup<T>& G = pick_group(L, idx);
   int gi = 0;
@@ -712,19 +719,13 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_c
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int n_tma = 0, n_in = 0, n_c1 = 0, n_c2 = 0;
 
-  // ---- phase 0: barriers; bulk copies of lambda_Y (5 fields) and of B1'; TMEM; coefficients
+  // ---- phase 0: barriers; bulk copies of B1' and (after the wait for the
+  // previous kernel in the stream) of lambda_Y (5 fields); TMEM; coefficients
   if (threadIdx.x == 0) {
     *sflag = 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) tc::mbar_init(&mbar[q], 1);
     tc::fence_mbar_init();
-    const uint32_t row_bytes = (uint32_t)(mt * J * sizeof(T2));
-    tc::mbar_expect_tx(&mbar[3], row_bytes * S::ANIN);
-#pragma unroll
-    for (int q = 0; q < S::ANIN; ++q)
-      tc::bulk_g2s(sA + (size_t)q * MT * J * 2, G.lamY + (size_t)q * FS + ((size_t)m * G.B + b0) * J, row_bytes,
-                   &mbar[3]);
-    n_in = 1;
     tc::mbar_expect_tx(&mbar[0], (uint32_t)(S::B1 * sizeof(float)));
     tc::bulk_g2s(sB, gbasis + (size_t)m * S::BLOCK, (uint32_t)(S::B1 * sizeof(float)), &mbar[0]);
     n_tma = 1;
@@ -732,6 +733,16 @@ __global__ void __launch_bounds__(256, S::MINB) k_spectral_adj_tc(const __grid_c
   if (warp == 0) {
     tc::tmem_alloc(tslot, S::TMEM_COLS);
     tc::tmem_relinquish();
+  }
+  pdl_wait();
+  if (threadIdx.x == 0) {
+    const uint32_t row_bytes = (uint32_t)(mt * J * sizeof(T2));
+    tc::mbar_expect_tx(&mbar[3], row_bytes * S::ANIN);
+#pragma unroll
+    for (int q = 0; q < S::ANIN; ++q)
+      tc::bulk_g2s(sA + (size_t)q * MT * J * 2, G.lamY + (size_t)q * FS + ((size_t)m * G.B + b0) * J, row_bytes,
+                   &mbar[3]);
+    n_in = 1;
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -1021,18 +1032,19 @@ cudaError_t launch_spec_tc(int M, const SpecLaunch<float>& L, int nblocks, const
                            cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
   if (M == 106) return launch_spec_tc106(L, nblocks, basis, err, s);
-  if (M == 63) k_spectral_tc<Tc63><<<nblocks, 256, spec_tc_smem_bytes(63), s>>>(L, basis, err);
-  else k_spectral_tc<Tc42><<<nblocks, 256, spec_tc_smem_bytes(42), s>>>(L, basis, err);
-  return cudaGetLastError();
+  cudaError_t e = M == 63 ? launch_pdl(k_spectral_tc<Tc63>, nblocks, 256, spec_tc_smem_bytes(63), s, L, basis, err)
+                          : launch_pdl(k_spectral_tc<Tc42>, nblocks, 256, spec_tc_smem_bytes(42), s, L, basis, err);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_spec_adj_tc(int M, const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
                                cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
   if (M == 106) return launch_spec_adj_tc106(L, nblocks, basis, err, s);
-  if (M == 63) k_spectral_adj_tc<Tc63><<<nblocks, 256, spec_tc_adj_smem_bytes(63), s>>>(L, basis, err);
-  else k_spectral_adj_tc<Tc42><<<nblocks, 256, spec_tc_adj_smem_bytes(42), s>>>(L, basis, err);
-  return cudaGetLastError();
+  cudaError_t e =
+      M == 63 ? launch_pdl(k_spectral_adj_tc<Tc63>, nblocks, 256, spec_tc_adj_smem_bytes(63), s, L, basis, err)
+              : launch_pdl(k_spectral_adj_tc<Tc42>, nblocks, 256, spec_tc_adj_smem_bytes(42), s, L, basis, err);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 }  // namespace swp

@@ -432,6 +432,7 @@ __global__ void __launch_bounds__(256, 1) k_spectral_tc106(const __grid_constant
   constexpr int NSLOT = NSPX + NSH;
   constexpr int MT = S::MT, J = S::J, CNT = S::CNT;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
+  pdl_enter();
   int idx;
   const SpecGroup<T>& G = pick_group(L, idx);
   int gi = 0;
@@ -690,6 +691,7 @@ __global__ void __launch_bounds__(256, 1) k_spectral_adj_tc106(const __grid_cons
   constexpr int NKADJ = 8;
   constexpr int MT = S::MT, J = S::J, JH = S::JH, CNT = S::CNT;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
+  pdl_enter();
   int idx;
   const SpecGroup<T>& G = pick_group(L, idx);
   int gi = 0;
@@ -874,15 +876,15 @@ void spec_tc106_set_attributes() {
 cudaError_t launch_spec_tc106(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
                               cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
-  k_spectral_tc106<<<nblocks, 256, spec_tc106_smem_bytes(), s>>>(L, basis, err);
-  return cudaGetLastError();
+  cudaError_t e = launch_pdl(k_spectral_tc106, nblocks, 256, spec_tc106_smem_bytes(), s, L, basis, err);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_spec_adj_tc106(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
                                   cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
-  k_spectral_adj_tc106<<<nblocks, 256, spec_tc106_adj_smem_bytes(), s>>>(L, basis, err);
-  return cudaGetLastError();
+  cudaError_t e = launch_pdl(k_spectral_adj_tc106, nblocks, 256, spec_tc106_adj_smem_bytes(), s, L, basis, err);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 }  // namespace swp
