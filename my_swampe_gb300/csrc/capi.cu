@@ -632,10 +632,13 @@ int winds_impl(swp_plan* p, const swp_group_state* st, void* const* ed, void* co
 // `sweep`: the step is one of an adjoint sweep, whose lambda always comes from
 // the Legendre adjoint (or the seed), so the grid adjoint may use its tied
 // F / G components (modified Euler; the explicit scheme's are not tied).
+// `zeroed`: an earlier step of the same sweep has zeroed the adjoint of U, V
+// and of the prev / mid carries (modified Euler: no step input reads them).
 template <typename T>
 int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group_state* st_out,
                       const swp_group_adjoint* adj, const swp_flags* f, int t, cudaStream_t s,
-                      bool refresh_coefs = true, bool sweep = false) {
+                      bool refresh_coefs = true, bool sweep = false, bool zeroed = false) {
+  zeroed = zeroed && sweep && f->scheme == 0;
   int nbg = 0, nbs = 0;
   if (refresh_coefs) {
     int rc = update_coefs<T>(p, st_in, s);
@@ -645,6 +648,7 @@ int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group
   LG.mode = GM_ADJ_STEP;
   LG.cfg = make_cfg(f);
   LG.cfg.lam_fg_tied = (sweep && f->forcflag && f->test == 0 && f->scheme == 0) ? 1 : 0;
+  LG.cfg.adj_zeroed = zeroed ? 1 : 0;
   for (int g = 0; g < p->ng; ++g) {
     LG.grp[g].primal = (const typename cplx<T>::type*)st_out[g].fourier;
     LG.grp[g].lam = (typename cplx<T>::type*)adj[g].lam;
@@ -661,6 +665,7 @@ int adjoint_step_impl(swp_plan* p, const swp_group_state* st_in, const swp_group
   // the carries of step t, as forward_steps sets them (read by the semi-implicit adjoint)
   LS.cfg.ra_mode = (f->modalflag && t > 2) ? 2 : 1;
   LS.cfg.si_lag_init = f->scheme == 2 && t == f->t_start;
+  LS.cfg.adj_zeroed = zeroed ? 1 : 0;
   for (int g = 0; g < p->ng; ++g) {
     LS.grp[g].lam = (typename cplx<T>::type*)adj[g].lam;
     LS.grp[g].lamY = (const typename cplx<T>::type*)adj[g].lam_y;
@@ -728,7 +733,7 @@ int adjoint_window_impl(swp_plan* p, const swp_group_state* st, void* const* slo
         a[g].fourier = (char*)slots[g] + (size_t)k * ss;
         b[g].fourier = (char*)slots[g] + (size_t)(k + 1) * ss;
       }
-      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, t0 + k, cs, false, true);
+      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, t0 + k, cs, false, true, k != nsteps - 1);
       if (rc) return rc;
     }
     return SWP_OK;
@@ -891,7 +896,7 @@ int adjoint_stored_impl(swp_plan* p, const swp_group_state* st, void* const* sta
         a[g].fourier = (char*)states[g] + (size_t)k * ss;
         b[g].fourier = (char*)states[g] + (size_t)(k + 1) * ss;
       }
-      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, t0 + k, cs, false, true);
+      rc = adjoint_step_impl<T>(p, a.data(), b.data(), adj, f, t0 + k, cs, false, true, k != nsteps - 1);
       if (rc) return rc;
     }
     return SWP_OK;

@@ -767,7 +767,12 @@ __device__ __forceinline__ void grid_body(const GridLaunch<T>& Lc, const GridGro
         if (t < NY) {
           const int rp = t % RP, k = (t / RP) % n1, q = t / (RP * n1);
           const int fy = q == 0 ? F_ETA : q == 1 ? F_DELTA : q == 2 ? F_PHI : q == 3 ? F_U : F_V;
-          ld_rows16(G.lam + (size_t)fy * FS + ((size_t)k * B + b) * J + j0 + rp * EPC, lv[u]);
+          if (q >= 3 && cfg.adj_zeroed) {  // lambda of U, V: zero after the sweep's first step
+#pragma unroll
+            for (int e = 0; e < EPC; ++e) lv[u][e] = mk<T2>(0, 0);
+          } else {
+            ld_rows16(G.lam + (size_t)fy * FS + ((size_t)k * B + b) * J + j0 + rp * EPC, lv[u]);
+          }
         }
       }
       T2* res = cfft_batch_c<-1, L>(zout, zin, 4 * JB, c.twL);

@@ -881,8 +881,9 @@ __device__ __forceinline__ T adj_store_point(const SpecGroup<T>& G, const StepCf
   const T gp = adj_point_values<T, NK>(G, cfg, incr, m, b, j, ld, in, lv);
 #pragma unroll
   for (int q = 0; q < 11; ++q) G.lam[adj_field(q) * FS + o] = lv[q];
+  if (!cfg.adj_zeroed)
 #pragma unroll
-  for (int q = 0; q < 8; ++q) G.lam[adj_zero_field(q) * FS + o] = mk<T2>(0, 0);
+    for (int q = 0; q < 8; ++q) G.lam[adj_zero_field(q) * FS + o] = mk<T2>(0, 0);
   return gp;
 }
 
@@ -937,11 +938,13 @@ __device__ __forceinline__ T adj_store_rows(const SpecGroup<T>& G, const StepCfg
     for (int e = 0; e < R; ++e) w[e] = lv[e][q];
     st_rows16(G.lam + adj_field(q) * FS + o, w);
   }
-  T2 zz[R];
+  if (!cfg.adj_zeroed) {
+    T2 zz[R];
 #pragma unroll
-  for (int e = 0; e < R; ++e) zz[e] = mk<T2>(0, 0);
+    for (int e = 0; e < R; ++e) zz[e] = mk<T2>(0, 0);
 #pragma unroll
-  for (int q = 0; q < 8; ++q) st_rows16(G.lam + adj_zero_field(q) * FS + o, zz);
+    for (int q = 0; q < 8; ++q) st_rows16(G.lam + adj_zero_field(q) * FS + o, zz);
+  }
   return gp;
 }
 

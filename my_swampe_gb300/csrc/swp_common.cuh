@@ -328,6 +328,9 @@ struct StepCfg {
   int tl_coef;     // tangent-linear step: differentiate the coefficient tables too
   int tl_filter;   // primal step of a tangent run: add the filter weights' tangents times the
                    // displacement to the tangent carries (SpecGroup four_t, dw)
+  int adj_zeroed;  // modified-Euler adjoint sweep after its first step: the adjoint of U, V and
+                   // of the prev / mid carries is already zero (an earlier step of the sweep
+                   // wrote it), so the step neither reads nor rewrites it
 };
 
 // Programmatic dependent launch.  The step kernels are launched with the
