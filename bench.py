@@ -242,9 +242,11 @@ def _algorithmic_bytes(kernel, B, J=64, M=42, elem=8):
     per member) each kernel must read and write.
       spectral : reads 11 step inputs + 3 RA-filtered carries, writes 3 curr + U, V + 3 carries
       grid     : reads eta, Phi, U, V; writes A..E, PhiF, F, G
-      grid_adj : reads 4 primal + 8 lambda(A..G) + 5 lambda(outputs); writes 5
-      spectral_adj : reads 5 lambda(outputs) + 7 primal inputs; writes 19 lambda fields"""
-    cols = {"spectral": 22, "grid": 12, "grid_adj": 22, "spectral_adj": 31}[kernel]
+      grid_adj : reads 4 primal + 6 lambda(A..E, PhiF; those of F, G equal B, -A) + 3 lambda(eta,
+                 delta, Phi outputs; those of U, V are zero inside a sweep); writes 5
+      spectral_adj : reads 5 lambda(outputs) + 7 primal inputs; writes 11 lambda fields (the
+                 other 8 stay zero inside a sweep)"""
+    cols = {"spectral": 22, "grid": 12, "grid_adj": 18, "spectral_adj": 23}[kernel]
     return cols * J * (M + 1) * elem * B
 
 
@@ -758,13 +760,18 @@ def run_profile(args):
     --profile-case steps: init, 4 forward steps, 3 adjoint steps, each launched
         on its own (no graphs): a handful of launches of every step kernel, for
         full captures (launch order: grid INIT, then per forward step Legendre +
-        grid STEP, then per adjoint step grid ADJ_STEP + Legendre adjoint)."""
+        grid STEP, then per adjoint step grid ADJ_STEP + Legendre adjoint).
+    --profile-case emission: the emission-stage leg once (B members, FP64)."""
     import torch
 
     torch.cuda.set_device(0)
     from __graft_entry__ import build
 
     build()
+    if args.profile_case == "emission":
+        r = _emission_leg(B=args.B, reps=1)
+        print(json.dumps({"profile": "emission", "B": args.B, "ok": True, "ms_per_call": r["ms_per_call"]}))
+        return
     from my_swampe_gb300.adjoint import Integration
 
     # no autotuning here: its timing launches would come before the profiled ones
@@ -813,7 +820,7 @@ def main():
     ap.add_argument("--ref-nsteps", type=int, default=20)
     ap.add_argument("--profile", choices=("fast", "fp64"), default=None,
                     help="run a small case of the workload (for ncu) instead of timing")
-    ap.add_argument("--profile-case", choices=("window", "steps"), default="window")
+    ap.add_argument("--profile-case", choices=("window", "steps", "emission"), default="window")
     ap.add_argument("--profile-M", type=int, choices=(42, 63, 106), default=M_BENCH,
                     help="truncation of the profiled case")
     ap.add_argument("--store", choices=("auto", "all", "checkpoint"), default="auto",

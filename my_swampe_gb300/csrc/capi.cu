@@ -769,6 +769,8 @@ int time_kernels_impl(swp_plan* p, const swp_group_state* st, const swp_group_ad
   SpecLaunch<T> LSa = LS;
   LGa.mode = GM_ADJ_STEP;
   LGa.cfg.lam_fg_tied = (f->forcflag && f->test == 0 && f->scheme == 0) ? 1 : 0;  // as inside an adjoint sweep
+  // the steady state of a modified-Euler sweep: lambda of U, V, prev, mid already zero
+  LGa.cfg.adj_zeroed = LSa.cfg.adj_zeroed = f->scheme == 0 ? 1 : 0;
   if (adj) {
     for (int g = 0; g < p->ng; ++g) {
       LGa.grp[g].primal = LG.grp[g].four;
