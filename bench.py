@@ -761,6 +761,9 @@ def run_profile(args):
         on its own (no graphs): a handful of launches of every step kernel, for
         full captures (launch order: grid INIT, then per forward step Legendre +
         grid STEP, then per adjoint step grid ADJ_STEP + Legendre adjoint).
+    --profile-case sweep: init, 4 forward steps with every state kept, then the
+        adjoint sweep over them (its steps after the first skip the zero
+        columns, as inside the bench's sweeps).
     --profile-case emission: the emission-stage leg once (B members, FP64)."""
     import torch
 
@@ -776,6 +779,19 @@ def run_profile(args):
 
     # no autotuning here: its timing launches would come before the profiled ones
     eng, wl, flags, _, ics = _setup(args.profile, args.B, ngroups=1, M=args.profile_M, autotune=False)
+    if args.profile_case == "sweep":
+        eng.init_state(ics, flags)
+        gd = eng.groups[0]
+        states = [torch.empty((5,) + tuple(gd["fourier"].shape), dtype=eng.cdtype, device=eng.device)]
+        eng.forward_stored(flags, t0=2, nsteps=4, states=states)
+        lam, lamy, grad = eng.new_adjoint_buffers()
+        lam[0].copy_(torch.randn_like(lam[0]))
+        eng.adjoint_stored(flags, states, lam, lamy, grad, t0=2, nsteps=4)
+        torch.cuda.synchronize()
+        eng.check_device_status()
+        print(json.dumps({"profile": args.profile, "case": "sweep", "M": args.profile_M, "B": args.B,
+                          "tensor_core_groups": eng.tensor_core_groups, "ok": True}))
+        return
     if args.profile_case == "steps":
         eng.init_state(ics, flags)
         eng.forward(flags, t0=2, nsteps=3)
@@ -820,7 +836,7 @@ def main():
     ap.add_argument("--ref-nsteps", type=int, default=20)
     ap.add_argument("--profile", choices=("fast", "fp64"), default=None,
                     help="run a small case of the workload (for ncu) instead of timing")
-    ap.add_argument("--profile-case", choices=("window", "steps", "emission"), default="window")
+    ap.add_argument("--profile-case", choices=("window", "steps", "sweep", "emission"), default="window")
     ap.add_argument("--profile-M", type=int, choices=(42, 63, 106), default=M_BENCH,
                     help="truncation of the profiled case")
     ap.add_argument("--store", choices=("auto", "all", "checkpoint"), default="auto",
