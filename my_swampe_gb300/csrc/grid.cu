@@ -913,17 +913,18 @@ cudaError_t launch_grid(const GridLaunch<T>& L0, int nblocks0, size_t smem, cuda
   }
   L.prefix[L.ng] = nblocks;
   cudaError_t e = cudaSuccess;
+  constexpr bool f32 = std::is_same<T, float>::value;
   switch (L.mode) {
-    case GM_STEP: e = launch_pdl(k_grid<T, GM_STEP>, nblocks, 256, smem, s, L); break;
-    case GM_INIT: e = launch_pdl(k_grid<T, GM_INIT>, nblocks, 256, smem, s, L); break;
-    case GM_OUTPUT: e = launch_pdl(k_grid<T, GM_OUTPUT>, nblocks, 256, smem, s, L); break;
-    case GM_WINDS: e = launch_pdl(k_grid<T, GM_WINDS>, nblocks, 256, smem, s, L); break;
-    case GM_ADJ_STEP: e = launch_pdl(k_grid<T, GM_ADJ_STEP>, nblocks, 256, smem, s, L); break;
-    case GM_ADJ_INIT: e = launch_pdl(k_grid<T, GM_ADJ_INIT>, nblocks, 256, smem, s, L); break;
-    case GM_ADJ_OUTPUT: e = launch_pdl(k_grid<T, GM_ADJ_OUTPUT>, nblocks, 256, smem, s, L); break;
-    case GM_FWD2: e = launch_pdl(k_grid<T, GM_FWD2>, nblocks, 256, smem, s, L); break;
-    case GM_TL_STEP: e = launch_pdl(k_grid<T, GM_TL_STEP>, nblocks, 256, smem, s, L); break;
-    case GM_TL_INIT: e = launch_pdl(k_grid<T, GM_TL_INIT>, nblocks, 256, smem, s, L); break;
+    case GM_STEP: e = launch_pdl(k_grid<T, GM_STEP>, nblocks, 256, smem, s, f32, L); break;
+    case GM_INIT: e = launch_pdl(k_grid<T, GM_INIT>, nblocks, 256, smem, s, f32, L); break;
+    case GM_OUTPUT: e = launch_pdl(k_grid<T, GM_OUTPUT>, nblocks, 256, smem, s, f32, L); break;
+    case GM_WINDS: e = launch_pdl(k_grid<T, GM_WINDS>, nblocks, 256, smem, s, f32, L); break;
+    case GM_ADJ_STEP: e = launch_pdl(k_grid<T, GM_ADJ_STEP>, nblocks, 256, smem, s, f32, L); break;
+    case GM_ADJ_INIT: e = launch_pdl(k_grid<T, GM_ADJ_INIT>, nblocks, 256, smem, s, f32, L); break;
+    case GM_ADJ_OUTPUT: e = launch_pdl(k_grid<T, GM_ADJ_OUTPUT>, nblocks, 256, smem, s, f32, L); break;
+    case GM_FWD2: e = launch_pdl(k_grid<T, GM_FWD2>, nblocks, 256, smem, s, f32, L); break;
+    case GM_TL_STEP: e = launch_pdl(k_grid<T, GM_TL_STEP>, nblocks, 256, smem, s, f32, L); break;
+    case GM_TL_INIT: e = launch_pdl(k_grid<T, GM_TL_INIT>, nblocks, 256, smem, s, f32, L); break;
     default: return cudaErrorInvalidValue;
   }
   return e != cudaSuccess ? e : cudaGetLastError();

@@ -891,7 +891,7 @@ template <typename T>
 cudaError_t launch_spec_adj(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
   const int grid = L.sched ? persistent_blocks(k_spectral_adj<T>, nblocks, smem) : nblocks;
-  cudaError_t e = launch_pdl(k_spectral_adj<T>, grid, 256, smem, s, L);
+  cudaError_t e = launch_pdl(k_spectral_adj<T>, grid, 256, smem, s, std::is_same<T, float>::value, L);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 template cudaError_t launch_spec_adj<double>(const SpecLaunch<double>&, int, size_t, cudaStream_t);
@@ -918,7 +918,7 @@ template <typename T>
 cudaError_t launch_spec(const SpecLaunch<T>& L, int nblocks, size_t smem, cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
   const int grid = L.sched ? persistent_blocks(k_spectral<T>, nblocks, smem) : nblocks;
-  cudaError_t e = launch_pdl(k_spectral<T>, grid, 256, smem, s, L);
+  cudaError_t e = launch_pdl(k_spectral<T>, grid, 256, smem, s, std::is_same<T, float>::value, L);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 template cudaError_t launch_spec<double>(const SpecLaunch<double>&, int, size_t, cudaStream_t);

@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 #include "swp_common.cuh"
@@ -234,11 +235,13 @@ enum GridMode {
 };
 
 // Launch of a step kernel with programmatic stream serialization (see
-// pdl_enter): on unless the environment sets SWP_PDL=0.
+// pdl_enter): on for the FP32 kernels unless the environment sets SWP_PDL=0.
+// The FP64 kernels launch plainly: measured, the attribute cost the
+// single-member FP64 drop-in run 15% and gained nothing at 64 members.
 bool pdl_enabled();
 template <typename... Params, typename... Args>
 cudaError_t launch_pdl(void (*kernel)(Params...), int nblocks, int threads, size_t smem, cudaStream_t s,
-                       Args&&... args) {
+                       bool fp32, Args&&... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)nblocks);
   cfg.blockDim = dim3((unsigned)threads);
@@ -248,7 +251,7 @@ cudaError_t launch_pdl(void (*kernel)(Params...), int nblocks, int threads, size
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
-  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  cfg.numAttrs = (fp32 && pdl_enabled()) ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 

@@ -1032,8 +1032,8 @@ cudaError_t launch_spec_tc(int M, const SpecLaunch<float>& L, int nblocks, const
                            cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
   if (M == 106) return launch_spec_tc106(L, nblocks, basis, err, s);
-  cudaError_t e = M == 63 ? launch_pdl(k_spectral_tc<Tc63>, nblocks, 256, spec_tc_smem_bytes(63), s, L, basis, err)
-                          : launch_pdl(k_spectral_tc<Tc42>, nblocks, 256, spec_tc_smem_bytes(42), s, L, basis, err);
+  cudaError_t e = M == 63 ? launch_pdl(k_spectral_tc<Tc63>, nblocks, 256, spec_tc_smem_bytes(63), s, true, L, basis, err)
+                          : launch_pdl(k_spectral_tc<Tc42>, nblocks, 256, spec_tc_smem_bytes(42), s, true, L, basis, err);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 
@@ -1042,8 +1042,8 @@ cudaError_t launch_spec_adj_tc(int M, const SpecLaunch<float>& L, int nblocks, c
   if (nblocks <= 0) return cudaSuccess;
   if (M == 106) return launch_spec_adj_tc106(L, nblocks, basis, err, s);
   cudaError_t e =
-      M == 63 ? launch_pdl(k_spectral_adj_tc<Tc63>, nblocks, 256, spec_tc_adj_smem_bytes(63), s, L, basis, err)
-              : launch_pdl(k_spectral_adj_tc<Tc42>, nblocks, 256, spec_tc_adj_smem_bytes(42), s, L, basis, err);
+      M == 63 ? launch_pdl(k_spectral_adj_tc<Tc63>, nblocks, 256, spec_tc_adj_smem_bytes(63), s, true, L, basis, err)
+              : launch_pdl(k_spectral_adj_tc<Tc42>, nblocks, 256, spec_tc_adj_smem_bytes(42), s, true, L, basis, err);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 

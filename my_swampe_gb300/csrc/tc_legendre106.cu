@@ -876,14 +876,14 @@ void spec_tc106_set_attributes() {
 cudaError_t launch_spec_tc106(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
                               cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
-  cudaError_t e = launch_pdl(k_spectral_tc106, nblocks, 256, spec_tc106_smem_bytes(), s, L, basis, err);
+  cudaError_t e = launch_pdl(k_spectral_tc106, nblocks, 256, spec_tc106_smem_bytes(), s, true, L, basis, err);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_spec_adj_tc106(const SpecLaunch<float>& L, int nblocks, const TcBasis& basis, int* err,
                                   cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
-  cudaError_t e = launch_pdl(k_spectral_adj_tc106, nblocks, 256, spec_tc106_adj_smem_bytes(), s, L, basis, err);
+  cudaError_t e = launch_pdl(k_spectral_adj_tc106, nblocks, 256, spec_tc106_adj_smem_bytes(), s, true, L, basis, err);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 
