@@ -99,6 +99,19 @@ def test_semi_implicit_alpha_gradient_matches_torch_autograd_through_oracle(cuda
         assert abs(pg[k] - po[k]) <= 1e-7 * abs(po[k]), (k, pg[k], po[k])
 
 
+def test_raw_with_semi_implicit_parameter_gradients_match_oracle(cuda):
+    """The RAW filter on the semi-implicit scheme's filtered lineage (its n-1
+    base): all six parameter gradients against torch autograd through the oracle."""
+    params, ics, W = _case(seed=25)
+    params = dict(params, dt=600.0)
+    lg, pg = _gpu(params, ics, W, 5, scheme=2, raw=True)
+    lo, po = _oracle(params, ics, W, 5, semi_implicit=True, raw=True)
+    assert abs(lg - lo) <= 1e-9 * abs(lo)
+    for k in PARAMS:
+        assert po[k] != 0.0, k
+        assert abs(pg[k] - po[k]) <= 1e-7 * abs(po[k]), (k, pg[k], po[k])
+
+
 def test_classic_filter_alpha_does_not_move_the_curr_fields(cuda):
     """Modified Euler with the classic filter never reads the filtered level:
     the alpha and williams_alpha derivatives of the curr fields are zero."""
