@@ -125,6 +125,32 @@ def test_emission_coefficients_match_oracle(cuda, model):
         assert _rel(yi, want) <= 1e-12
 
 
+@pytest.mark.parametrize("JI", [(96, 192), (160, 320)])
+def test_emission_coefficients_on_the_larger_grids(cuda, JI):
+    """M = 63 and M = 106 grids, linear temperature mode, band-averaged Planck
+    intensity, ydeg = 6 (49 coefficients)."""
+    from my_swampe_gb300.emission import EmissionConfig, emission_coefficients
+
+    Jg, Ig = JI
+    mu, w = np.polynomial.legendre.leggauss(Jg)
+    lat = np.repeat(np.arcsin(mu), Ig)
+    lon = np.tile(np.linspace(-np.pi, np.pi, Ig, endpoint=False), Jg)
+    P = eo.build_projector(eo.real_ylm_design(6, lat, lon), w)
+    rng = np.random.default_rng(Jg)
+    lam = np.linspace(-np.pi, np.pi, Ig, endpoint=False)[None, :]
+    phi = np.stack([3e4 * k * np.cos(lam) * np.sqrt(1 - mu[:, None] ** 2) + 1e3 * rng.standard_normal((Jg, Ig))
+                    for k in (1, 2, 3)])
+    kw = dict(emission_temp_mode="linear", emission_model="planck", planck_band_wavelengths_m=[3.6e-6, 4.5e-6],
+              planck_band_weights=[1.0, 1.0])
+    y = emission_coefficients(torch.tensor(phi, device="cuda"), 0.0, torch.tensor(P, device="cuda"),
+                              torch.tensor(w, device="cuda"), EmissionConfig(**kw)).cpu().numpy()
+    for b in range(3):
+        T = eo.phi_to_temperature(phi[b], 0.0, temp_mode="linear")
+        Imap = eo.temperature_to_intensity(T, emission_model="planck", planck_band_wavelengths_m=[3.6e-6, 4.5e-6],
+                                           planck_band_weights=[1.0, 1.0])
+        assert _rel(y[b], eo.intensity_map_to_y_dense(Imap, P, w)) <= 1e-12, b
+
+
 def test_non_finite_member_gives_nan_and_leaves_the_others(cuda):
     from my_swampe_gb300.emission import emission_coefficients, intensity_map_to_y_dense
 
