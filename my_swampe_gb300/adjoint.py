@@ -207,6 +207,7 @@ class _IntegrateFn(torch.autograd.Function):
             dics.append(dic)
             dpar.append(torch.stack(rows))
         outs = integ.run_tangent(ics, dics, dpar)
+        eng.check_device_status()
         return tuple(o.to(flat[NP].dtype) for o in outs)
 
     @staticmethod
@@ -256,6 +257,9 @@ class _IntegrateFn(torch.autograd.Function):
                 for g in range(len(eng.groups)):
                     w = dphys[g].to(torch.float64)
                     res[1 + NF * g + k] = (w * jk[g].to(torch.float64)).sum(dim=(0, 2, 3)).to(ctx.in_dtypes[NF * g + k])
+        # a bounded wait of a tensor-core kernel (recomputed forward, adjoint,
+        # tangent runs) that ran out makes these gradients invalid: raise
+        eng.check_device_status()
         return tuple(res)
 
 

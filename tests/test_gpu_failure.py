@@ -113,3 +113,35 @@ def test_tensor_core_wait_limit_reports_and_recovers(cuda):
     ref_eng.forward(flags, t0=2, nsteps=3)
     want = ref_eng.output_physical(flags)[0]
     assert torch.equal(got, want)
+
+
+def test_differentiable_run_reports_a_timeout_at_backward(cuda):
+    """A tensor-core wait that runs out inside a differentiable run (forward or
+    adjoint sweep) surfaces as an error of the backward pass, which checks the
+    device status before it returns gradients."""
+    from my_swampe_gb300 import _lib, workloads
+    from my_swampe_gb300.adjoint import integrate
+    from my_swampe_gb300.engine import Engine, RunFlagsC
+
+    eng = Engine([(42, 8)], "fast")
+    wl = workloads.forced_ensemble(eng, seed=3, Phibar=3.0e5, dt=600.0)
+    workloads.apply_params(eng, 0, wl["params"])
+    assert eng.uses_tensor_cores
+    lib = _lib.load()
+    p = {k: torch.as_tensor(wl["params"][k], dtype=torch.float64, device=eng.device).expand(8).clone()
+         .requires_grad_(True) for k in ("taurad", "taudrag", "DPhieq")}
+    p["Phibar"] = torch.full((8,), float(wl["params"]["Phibar"]), dtype=torch.float64, device=eng.device)
+
+    def run():
+        out = integrate(eng, RunFlagsC(), t0=2, nsteps=4, params=[p], ics=[wl["ics"]], store="all")[0]
+        (out[2].double() ** 2).mean().backward()
+
+    run()  # clean
+    assert lib.swp_plan_set_wait_limit(eng._plan, 0) == 0
+    try:
+        with pytest.raises(RuntimeError, match="timed out"):
+            run()
+    finally:
+        assert lib.swp_plan_set_wait_limit(eng._plan, _lib.WAIT_LIMIT_DEFAULT) == 0
+    eng.check_device_status()  # cleared by the failed check
+    run()
