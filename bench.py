@@ -472,7 +472,11 @@ def run_ours(args):
                 "speedup_at_equal_state_policy": round((fast_ckpt if fast_ckpt else value) / (world * v64), 2),
                 "error_fast_vs_fp64_after_1440": err,
                 "grad_rel_l2_fast_vs_fp64": gerr,
-                "ms_per_launch": {k: round(v, 5) for k, v in kt64.items()}}
+                "ms_per_launch": {k: round(v, 5) for k, v in kt64.items()},
+                # the FP64 Legendre kernel against the chip's FP64 (non-tensor) rate:
+                # SMs x 2 DFMA x 2 FLOP x the SM clock under load
+                "legendre_fp64_tflops": round(LEGENDRE_FLOP_M42 * B / (kt64["spectral"] * 1e-3) / 1e12, 3),
+                "fp64_peak_tflops_nominal": round(_fp64_peak_tflops(clocks), 3)}
 
     # ---------------- other workloads: the drop-in API's forward rate, the mixed-truncation ensemble
     dropin = None if args.skip_dropin else _dropin_leg()
@@ -643,6 +647,15 @@ def _mixed_leg(steps=2):
                         "one plan (groups concurrent)",
             "member_steps_per_s": round(rate, 1), "adjoint_states": store, "tensor_core_groups": tc_groups,
             "error_fast_vs_fp64": err}
+
+
+def _fp64_peak_tflops(clocks):
+    """GB300's FP64 (non-tensor) rate: 2 DFMA per cycle per SM at the sampled SM clock."""
+    import torch
+
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    return nsm * 2 * 2 * mhz * 1e6 / 1e12
 
 
 def _emission_leg(B=256, ydeg=10, ntimes=200, reps=20):
