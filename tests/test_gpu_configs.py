@@ -192,7 +192,8 @@ def test_fast_path_error_after_1440_steps(cuda):
     """Forced ensemble (B=8, the benchmark's regime and parameter sampling),
     1440 steps: the fast path (FP32 state, tensor-core Legendre kernels)
     against the FP64 path.  Relative L2 bounds: Phi 1e-5 (the benchmark spec's
-    target), eta 1e-5, delta 5e-5 (the smallest field)."""
+    target), eta 1e-5, delta 5e-5 (the smallest field); the same for the
+    Robert-Asselin filtered (prev) fields."""
     import torch
     from my_swampe_gb300 import workloads
     from my_swampe_gb300.engine import Engine, RunFlagsC
@@ -209,7 +210,8 @@ def test_fast_path_error_after_1440_steps(cuda):
         eng.forward(flags, t0=2, nsteps=1440)
         eng.check_device_status()
         outs[prec] = eng.output_physical(flags)[0].double()
-    for k, name, tol in ((0, "eta", 1e-5), (1, "delta", 5e-5), (2, "Phi", 1e-5)):
+    for k, name, tol in ((0, "eta", 1e-5), (1, "delta", 5e-5), (2, "Phi", 1e-5), (5, "eta_prev", 1e-5),
+                         (6, "delta_prev", 5e-5), (7, "Phi_prev", 1e-5)):
         ref = outs["fp64"][k]
         rel = float(torch.linalg.vector_norm(outs["fast"][k] - ref) / torch.linalg.vector_norm(ref))
         assert rel <= tol, (name, rel)
