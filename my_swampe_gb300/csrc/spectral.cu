@@ -897,8 +897,7 @@ cudaError_t launch_spec_adj(const SpecLaunch<T>& L, int nblocks, size_t smem, cu
 template cudaError_t launch_spec_adj<double>(const SpecLaunch<double>&, int, size_t, cudaStream_t);
 template cudaError_t launch_spec_adj<float>(const SpecLaunch<float>&, int, size_t, cudaStream_t);
 
-// Largest dynamic shared memory a SIMT kernel may request: 227 KB per block
-// minus its static shared memory (the persistent scheduler's unit slot).
+// Programmatic dependent launch of the FP32 step kernels, unless SWP_PDL=0.
 bool pdl_enabled() {
   static const bool on = [] {
     const char* e = getenv("SWP_PDL");
