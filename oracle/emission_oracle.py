@@ -1,6 +1,6 @@
 """CPU FP64 oracle for the emission stage of the retrieval.
 
-TEST INFRASTRUCTURE ONLY.  This module is a checker: it may be imported by
+TEST INFRASTRUCTURE ONLY.  This module is an oracle: it may be imported by
 ``tests/`` and by ``__graft_entry__.smoke()``.  The GPU product path
 (``my_swampe_gb300.emission``) never imports it.
 

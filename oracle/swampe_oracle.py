@@ -1,6 +1,6 @@
 """CPU FP64 oracle for the SWAMPE-JAX time-stepping core.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker: it may be imported by
+TEST INFRASTRUCTURE ONLY.  This module is the oracle: it may be imported by
 ``tests/``, by ``__graft_entry__.smoke()`` and by the CPU-baseline leg of
 ``bench.py``.  The GPU product path never imports it.
 

@@ -191,8 +191,8 @@ def test_forced_single_member_ten_days(cuda):
 def test_fast_path_error_after_1440_steps(cuda):
     """Forced ensemble (B=8, the benchmark's regime and parameter sampling),
     1440 steps: the fast path (FP32 state, tensor-core Legendre kernels)
-    against the FP64 path.  Relative L2 bounds: Phi 1e-5 (the benchmark spec's
-    target), eta 1e-5, delta 5e-5 (the smallest field); the same for the
+    against the FP64 path.  Relative L2 bounds: Phi 1e-5 (the split-precision
+    path's accuracy target), eta 1e-5, delta 5e-5 (the smallest field); the same for the
     Robert-Asselin filtered (prev) fields."""
     import torch
     from my_swampe_gb300 import workloads
